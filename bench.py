@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark of the fused extended-likelihood FdF on one GB300.
+
+Workload (the production shape): the COMPASS 88-wave 3pi wave set -- 7
+negative + 80 positive reflectivity waves + flat wave, rank 2 (341
+parameters) -- over 1,000,000 synthetic data events stored as complex64
+structure-of-arrays (696 MB, larger than the 129 MB L2, so no flush is needed
+between steps), normalisation/acceptance integrals from 5,000,000 synthetic MC
+events built on the GPU.  A step is one FdF (value + full gradient) at a new
+parameter point.
+
+  value     FdF evaluations per second with parameters and results resident in
+            HBM (device-resident entry point, CUDA events on the launch stream)
+  e2e       the same through the C ABI with host buffers (pwa_likelihood_fdf):
+            every step copies the parameters host->device and the value and
+            gradient device->host
+  roofline  the fused event kernel: algorithmic bytes (N x W x 8) over its own
+            CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline  the FP64 oracle (restatement of pwaLikelihood::FdF with the
+            reference's compensated sums) on this machine's host cores
+
+`--impl reference` times the reference's CPU FdF (the oracle restatement; the
+reference itself cannot be built here) on all host threads instead.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_NEG, N_POS, RANK = 7, 80, 2
+METRIC = "FdF evals/s at 88 waves x 1M events"
+UNIT = "FdF/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-data", type=int, default=1_000_000)
+    ap.add_argument("--n-mc", type=int, default=5_000_000)
+    ap.add_argument("--reduction", default="fp64", choices=["fp64", "kahan_fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "fdf_main_compass88.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the GPU runs the workload."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.remove(self.path)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_likelihood(names, refl, data_c64, mc_c64, accepted, rank):
+    """FP64 oracle (the CPU restatement of the reference) on the given amplitudes."""
+    from oracle.oracle import OracleIntegral, OracleLikelihood
+    mc = mc_c64.astype(np.complex128)
+    norm, acc = OracleIntegral(), OracleIntegral()
+    assert norm.integrate(names, mc) and acc.integrate(names, mc, in_bin=accepted)
+    L = OracleLikelihood()
+    assert L.init(names, refl, None, rank, 0.0)
+    assert L.addNormIntegral(norm) and L.addAccIntegral(acc)
+    for k, n in enumerate(names):
+        assert L.addAmplitude(n, data_c64[k].astype(np.complex128))
+    assert L.finishInit()
+    return L
+
+
+def time_oracle(L, par, threads, min_seconds, max_reps):
+    """Median seconds of one oracle FdF."""
+    ts = []
+    t_start = time.perf_counter()
+    while len(ts) < max_reps and (len(ts) < 1 or time.perf_counter() - t_start < min_seconds):
+        t0 = time.perf_counter()
+        L.FdF(par, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts), len(ts)
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU FdF (oracle restatement) on all host threads."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from rootpwa_gb300 import synth
+    names, refl = synth.wave_names(N_NEG, N_POS)
+    rng = np.random.Generator(np.random.PCG64(1))
+    model = synth.AmplitudeModel(len(names), 8, rng)
+    par = rng.standard_normal(synth.n_pars(N_NEG, N_POS, RANK))
+    threads = cpu_threads()
+    # size the per-step event sample so that warm-up + steps take about two minutes
+    calib = model.draw(rng, 20_000)
+    mc = model.draw(rng, 20_000)
+    acc = rng.random(20_000) < 0.6
+    Lc = oracle_likelihood(names, refl, calib, mc, acc, RANK)
+    t_cal, _ = time_oracle(Lc, par, threads, 0.5, 5)
+    per_event = t_cal / 20_000
+    budget = 120.0
+    n_sample = int(budget / max(1, args.steps + args.warmup) / per_event)
+    n_sample = max(20_000, min(args.n_data, n_sample))
+    data = model.draw(rng, n_sample)
+    L = oracle_likelihood(names, refl, data, mc, acc, RANK)
+    for _ in range(args.warmup):
+        L.FdF(par, threads=threads)
+    ts = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        L.FdF(par * (1.0 + 1e-3 * (k % 7)), threads=threads)
+        ts.append(time.perf_counter() - t0)
+    t_step = sum(ts) / len(ts)
+    value = 1.0 / (t_step * args.n_data / n_sample)
+    sample = ("FP64 oracle FdF (restatement of pwaLikelihood::FdF, compensated sums) over %d of the %d events "
+              "per step on %d host threads, scaled to %d events" % (n_sample, args.n_data, threads, args.n_data))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3 * args.n_data / n_sample,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "compass88: 7-/80+ waves + flat, rank 2, %d events" % args.n_data,
+                       "waves": 88, "rank": RANK, "events": args.n_data, "parameters": len(par)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import rootpwa_gb300 as R
+    from rootpwa_gb300 import synth
+    from rootpwa_gb300 import _native as N
+
+    names, refl = synth.wave_names(N_NEG, N_POS)
+    W = len(names)
+    rng = np.random.Generator(np.random.PCG64(1))
+    model = synth.AmplitudeModel(W, 8, rng)
+    P = synth.n_pars(N_NEG, N_POS, RANK)
+    par0 = rng.standard_normal(P)
+
+    # ---- set-up (not timed): amplitudes on the device, integrals on the GPU ----
+    data = synth.draw_device(model, args.n_data, seed=11 + rank)
+    mc = synth.draw_device(model, args.n_mc, seed=1011 + rank)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2011 + rank)
+    accepted = (torch.rand(args.n_mc, generator=g, device="cuda") < 0.6).to(torch.uint8).cpu().numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    norm = R.ampIntegralMatrix()
+    norm.integrate(names, mc, precision="fp32")
+    integral_s = time.perf_counter() - t0
+    acc = R.ampIntegralMatrix()
+    acc.integrate(names, mc, inBin=accepted, precision="fp32")
+    del mc
+    torch.cuda.empty_cache()
+    L = R.pwaLikelihood()
+    L.init(names, refl, None, RANK, 0.0)
+    L.addNormIntegral(norm)
+    L.addAccIntegral(acc)
+    for k, n in enumerate(names):
+        L.addAmplitude(n, data[k])
+    L.finishInit()
+    L.setReduction(args.reduction)
+    stream = torch.cuda.Stream()
+    L.setStream(stream.cuda_stream)
+
+    # distinct parameter points, resident in HBM
+    n_pts = 64
+    pts = np.stack([par0 * (1.0 + 0.01 * k) for k in range(n_pts)])
+    d_par = torch.from_numpy(pts).cuda()
+    d_out = torch.zeros((n_pts, P + 2), dtype=torch.float64, device="cuda")
+    par_ptr = [d_par[k].data_ptr() for k in range(n_pts)]
+    out_ptr = [d_out[k].data_ptr() for k in range(n_pts)]
+    lib = N.lib()
+    h = L._h
+    fdf_dev = lib.pwa_likelihood_fdf_device
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    def step(i):
+        st = fdf_dev(h, C.c_void_p(par_ptr[i % n_pts]), C.c_void_p(out_ptr[i % n_pts]), 1, sptr)
+        if st:
+            N.check(st)
+
+    for i in range(max(3, args.warmup)):
+        step(i)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    # keep the GPU busy for about a second before the timed region so that
+    # the clock samples describe the sustained state of this workload
+    t_pre = time.perf_counter()
+    i = 0
+    while time.perf_counter() - t_pre < 1.0:
+        step(i)
+        i += 1
+        if i % 200 == 0:
+            stream.synchronize()
+    stream.synchronize()
+    L.setTiming(True)
+    launches0 = lib.pwa_kernel_launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    launches = lib.pwa_kernel_launch_count() - launches0
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    main_ms, fin_ms, n_timed = L.kernelTimes()
+    L.setTiming(False)
+    out = d_out.cpu().numpy()
+    assert np.all(out[:, P + 1] == 0.0), "device error flag set"
+    assert np.all(np.isfinite(out[:, :P + 1]))
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+
+    # cross-check the device-resident result against the host entry point
+    f_host, g_host = L.FdF(pts[0])
+    f_dev = out[0, 0]
+    assert abs(f_dev - f_host) <= 1e-12 * abs(f_host), (f_dev, f_host)
+
+    # ---- e2e: the C-ABI call with host buffers ----
+    n_e2e = args.e2e_steps or min(args.steps, 2000)
+    host_pts = [np.ascontiguousarray(p) for p in pts]
+    fbuf = C.c_double()
+    gbuf = np.zeros(P)
+    gptr = gbuf.ctypes.data_as(C.POINTER(C.c_double))
+    pptrs = [p.ctypes.data_as(C.POINTER(C.c_double)) for p in host_pts]
+    fdf_host = lib.pwa_likelihood_fdf
+    for i in range(3):
+        N.check(fdf_host(h, pptrs[i % n_pts], C.byref(fbuf), gptr))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for i in range(n_e2e):
+        st = fdf_host(h, pptrs[i % n_pts], C.byref(fbuf), gptr)
+        if st:
+            N.check(st)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n_e2e / e2e_s
+
+    # ---- roofline of the fused event kernel ----
+    alg_bytes = args.n_data * W * 8
+    avg_main_s = main_ms / max(1, n_timed) / 1e3
+    achieved = alg_bytes / avg_main_s / 1e9
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "kernel": "fdfMainKernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": profile_traffic(),
+                "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": avg_main_s * 1e6,
+                "finalize_avg_us": fin_ms / max(1, n_timed) * 1e3, "frac_of_8TBs_spec": achieved / 8000.0}
+
+    # ---- CPU baseline: the FP64 oracle on this machine's host cores ----
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n_cpu = args.n_data
+        host = data[:, :n_cpu].cpu().numpy()
+        rng2 = np.random.Generator(np.random.PCG64(5))
+        mc_s = model.draw(rng2, 20_000)
+        acc_s = rng2.random(20_000) < 0.6
+        Lo = oracle_likelihood(names, refl, host, mc_s, acc_s, RANK)
+        del host
+        threads = cpu_threads()
+        t_all, reps_all = time_oracle(Lo, pts[0], threads, 8.0, 10)
+        t_one, reps_one = time_oracle(Lo, pts[0], 1, 0.0, 1)
+        cpu = {"value": 1.0 / t_all, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": ("FP64 oracle FdF over all %d events (%d reps, median) on %d host threads; "
+                          "single-thread (the reference is single-threaded): %.4f FdF/s" %
+                          (n_cpu, reps_all, threads, 1.0 / t_one)),
+               "single_thread_value": 1.0 / t_one}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 (complex64 store, FP64 cross-tile reductions)",
+                "data": "synthetic",
+                "config": {"workload": "compass88: 7-/80+ waves + flat, rank 2, %d events per GPU" % args.n_data,
+                           "waves": 88, "rank": RANK, "events": args.n_data, "parameters": P,
+                           "mc_events": args.n_mc, "reduction": args.reduction,
+                           "l2": "inputs (%.0f MB) larger than L2 (129 MB); no flush" % (alg_bytes / 1e6),
+                           "entry": "pwa_likelihood_fdf_device (parameters and results in HBM)"},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": P * 8,
+                        "d2h_bytes_per_step": (P + 2) * 8, "entry": "pwa_likelihood_fdf (host buffers)"},
+                "gpu_launches": int(launches), "launches_per_step": launches / args.steps,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "extra": {"integral_norm_fp32_s": integral_s, "mc_events": args.n_mc}}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

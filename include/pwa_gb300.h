@@ -1,0 +1,237 @@
+/*
+ * pwa_gb300.h -- C ABI of the GB300-native extended-likelihood engine.
+ *
+ * The engine replaces the hot path of ROOTPWA's
+ *   rpwa::pwaLikelihood<std::complex<double>>   (partialWaveFit/pwaLikelihood.h:66-320)
+ *   rpwa::ampIntegralMatrix                      (decayAmplitude/ampIntegralMatrix.h:67-173)
+ * with hand-written sm_103a CUDA kernels.  Every entry point mirrors one
+ * reference method (cited beside it) with the same argument meaning, the same
+ * call order and the same semantics; ROOT/Boost types are replaced by plain
+ * pointers and sizes.
+ *
+ * Conventions
+ *   - Every function returns an int status (PWA_SUCCESS == 0).  The reference
+ *     reports setup failures as `false` + printErr and evaluation before
+ *     finishInit() as a bare `throw;` (pwaLikelihood.cc:177-180); here both are
+ *     status codes, and pwa_last_error() returns the message of the calling
+ *     thread's last failure.
+ *   - Sizes are 64-bit where they count events.
+ *   - Complex numbers are interleaved (re, im) pairs: complex128 = 2 doubles,
+ *     complex64 = 2 floats.
+ *   - Parameter arrays follow the reference's function-parameter layout
+ *     (pwaLikelihood.cc:1487-1556): for rank r, reflectivity (negative first),
+ *     wave w in wave-list order: w < r absent, w == r one real parameter,
+ *     w > r (Re, Im); the flat wave's real amplitude is the last parameter.
+ *   - A handle may be used by one host thread at a time (the reference's
+ *     evaluation methods write mutable caches and are not thread-safe either,
+ *     pwaLikelihood.h:311-319).  Different handles are independent.
+ */
+#ifndef PWA_GB300_H
+#define PWA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PWA_GB300_ABI_VERSION 1
+
+typedef struct pwa_likelihood pwa_likelihood;
+typedef struct pwa_integral   pwa_integral;
+
+enum pwa_status {
+	PWA_SUCCESS                = 0,
+	PWA_ERROR_INVALID_ARGUMENT = 1,  /* null pointer, size mismatch, unknown wave */
+	PWA_ERROR_INVALID_STATE    = 2,  /* call out of the reference's setup order */
+	PWA_ERROR_CUDA             = 3,  /* a CUDA runtime call failed */
+	PWA_ERROR_OUT_OF_MEMORY    = 4,
+	PWA_ERROR_DEVICE_TIMEOUT   = 5,  /* a bounded device-side wait expired */
+	PWA_ERROR_IO               = 6,  /* file could not be read or written */
+	PWA_ERROR_UNSUPPORTED      = 7,  /* shape outside the compiled kernel variants */
+	PWA_ERROR_NUMERICAL        = 8   /* e.g. singular Hessian in CovarianceMatrix */
+};
+
+/* pwaLikelihood::priorEnum (pwaLikelihood.h:108-111) */
+enum pwa_prior { PWA_PRIOR_FLAT = 0, PWA_PRIOR_HALF_CAUCHY = 1 };
+
+/* element type and residence of amplitude arrays handed to the engine */
+enum pwa_amp_type { PWA_COMPLEX64 = 0, PWA_COMPLEX128 = 1 };
+enum pwa_memory   { PWA_MEMORY_HOST = 0, PWA_MEMORY_DEVICE = 1 };
+
+/* cross-event reduction of the FdF kernel: FP32 per 128-event tile, then
+ * FP64 (default) or compensated FP32 across tiles; FP64 across blocks always. */
+enum pwa_reduction { PWA_REDUCE_FP64 = 0, PWA_REDUCE_KAHAN_FP32 = 1 };
+
+/* arithmetic of the integral-matrix Gram kernel */
+enum pwa_precision {
+	PWA_PRECISION_FP64      = 0,  /* FP64 SIMT products and sums (slow on GB300; the accuracy reference) */
+	PWA_PRECISION_FP32      = 1,  /* FP32 SIMT FMA, FP64 across chunks */
+	PWA_PRECISION_TF32      = 2,  /* tcgen05 kind::tf32, FP32 accumulate in TMEM, FP64 across CTAs */
+	PWA_PRECISION_TF32X3    = 3,  /* tcgen05 tf32 split hi+lo (3 products), FP32 accumulate, FP64 across CTAs */
+	PWA_PRECISION_BF16X3    = 4   /* tcgen05 kind::f16 bf16 split hi+lo (3 products), FP32 accumulate */
+};
+
+/* function-call statistics, pwaLikelihood::functionCallEnum (pwaLikelihood.h:89-96) */
+enum pwa_call { PWA_CALL_FDF = 0, PWA_CALL_GRADIENT = 1, PWA_CALL_DOEVAL = 2, PWA_CALL_DODERIVATIVE = 3,
+                PWA_CALL_HESSIAN = 4 };
+
+/* ------------------------------------------------------------------------ */
+/* library                                                                   */
+/* ------------------------------------------------------------------------ */
+int         pwa_abi_version(void);
+const char* pwa_last_error(void);
+/* number of CUDA kernels this library launched since load (all handles) */
+uint64_t    pwa_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* ampIntegralMatrix                                                          */
+/* ------------------------------------------------------------------------ */
+/* ampIntegralMatrix() (ampIntegralMatrix.cc:66-79) */
+int pwa_integral_create(pwa_integral** out);
+int pwa_integral_destroy(pwa_integral* I);
+/* operator= (ampIntegralMatrix.cc:107-123) */
+int pwa_integral_copy(pwa_integral* dst, const pwa_integral* src);
+/* setWaveNames (ampIntegralMatrix.cc:255-277) */
+int pwa_integral_set_wave_names(pwa_integral* I, uint32_t nWaves, const char* const* waveNames);
+/*
+ * integrate (ampIntegralMatrix.cc:300-489), on the GPU.
+ * amps: [wave][event][subAmp] complex, host or device memory.  The reference
+ * reads one ROOT tree per wave; here the waves are the rows of one array.
+ * weights: optional importance-sampling weights w in the order the reference
+ * reads its weight file: one per event that passes the bin selection, each
+ * event entering with 1/w and the matrix renormalised by the mean of 1/w
+ * (:419-429, :477-483).  inBin: optional per-event on-the-fly bin flag
+ * (the reference's eventMeta + otfBin test, :411-416).  maxNmbEvents <= 0
+ * uses all events.
+ */
+int pwa_integral_integrate(pwa_integral* I, uint32_t nWaves, const char* const* waveNames, const void* amps,
+                           uint64_t nEvents, uint32_t nSubAmps, int ampType, int memory, const double* weights,
+                           uint64_t nWeights, const uint8_t* inBin, int64_t maxNmbEvents, int precision);
+/* addEvent (ampIntegralMatrix.cc:280-297): amps = nWaves complex128 in wave order */
+int pwa_integral_add_event(pwa_integral* I, const double* amps);
+/* element (ampIntegralMatrix.cc:238-252): raw sum / nmbEvents */
+int pwa_integral_element(const pwa_integral* I, uint32_t i, uint32_t j, double* re, double* im);
+/* matrix() (ampIntegralMatrix.h:114-117): raw sums, nWaves x nWaves complex128 row-major */
+int pwa_integral_matrix(const pwa_integral* I, double* out);
+int pwa_integral_set_matrix(pwa_integral* I, const double* in);
+/* nmbWaves / nmbEvents / setNmbEvents (ampIntegralMatrix.h:99-103) */
+int pwa_integral_nmb_waves(const pwa_integral* I, uint32_t* n);
+int pwa_integral_nmb_events(const pwa_integral* I, uint64_t* n);
+int pwa_integral_set_nmb_events(pwa_integral* I, uint64_t n);
+/* waveIndex / waveName (ampIntegralMatrix.cc:195-216) */
+int pwa_integral_wave_name(const pwa_integral* I, uint32_t i, char* buf, uint32_t bufLen);
+int pwa_integral_wave_index(const pwa_integral* I, const char* name, uint32_t* index);
+/* operator+= / -= / *= / /= (ampIntegralMatrix.cc:126-185) */
+int pwa_integral_add(pwa_integral* I, const pwa_integral* other);
+int pwa_integral_subtract(pwa_integral* I, const pwa_integral* other);
+int pwa_integral_scale(pwa_integral* I, double factor);
+int pwa_integral_divide(pwa_integral* I, double factor);
+/* renormalize (ampIntegralMatrix.cc:492-500) */
+int pwa_integral_renormalize(pwa_integral* I, uint64_t nmbEventsRenorm);
+/* writeAscii / readAscii (ampIntegralMatrix.cc:503-570, file variants :573-608) */
+int pwa_integral_read_ascii(pwa_integral* I, const char* path);
+int pwa_integral_write_ascii(const pwa_integral* I, const char* path);
+
+/* ------------------------------------------------------------------------ */
+/* pwaLikelihood                                                              */
+/* ------------------------------------------------------------------------ */
+/* pwaLikelihood() (pwaLikelihood.cc:133-160); binds to the current CUDA device */
+int pwa_likelihood_create(pwa_likelihood** out);
+/* ~pwaLikelihood (pwaLikelihood.cc:163-167) */
+int pwa_likelihood_destroy(pwa_likelihood* L);
+/* useNormalizedAmps (pwaLikelihood.h:210) */
+int pwa_likelihood_use_normalized_amps(pwa_likelihood* L, int flag);
+/* setPriorType / setCauchyWidth (pwaLikelihood.h:212-215) */
+int pwa_likelihood_set_prior_type(pwa_likelihood* L, int priorType);
+int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double width);
+/* engine options without reference counterpart: CUDA stream of all launches,
+ * cross-event reduction mode */
+int pwa_likelihood_set_stream(pwa_likelihood* L, void* cudaStream);
+int pwa_likelihood_set_reduction(pwa_likelihood* L, int reduction);
+/*
+ * init (pwaLikelihood.cc:1050-1063 with readWaveList :1443-1484 and
+ * buildParDataStruct :1487-1556).  The reference takes wave descriptions and
+ * derives each wave's reflectivity from its decay topology; here the
+ * reflectivity (+1 / -1) is passed directly, in wave-list order.
+ */
+int pwa_likelihood_init(pwa_likelihood* L, uint32_t nWaves, const char* const* waveNames,
+                        const int32_t* reflectivities, const double* thresholds, uint32_t rank,
+                        double massBinCenter);
+/* addNormIntegral (pwaLikelihood.cc:1066-1083) */
+int pwa_likelihood_add_norm_integral(pwa_likelihood* L, const pwa_integral* normMatrix);
+/* addAccIntegral (pwaLikelihood.cc:1086-1107); like the reference it sets the
+ * argument's nmbEvents to the number of generated events */
+int pwa_likelihood_add_acc_integral(pwa_likelihood* L, pwa_integral* accMatrix, uint64_t accEventsOverride);
+/* addAmplitude (pwaLikelihood.cc:1110-1288): one wave's decay amplitudes for
+ * all data events, from host or device memory; normalised on upload */
+int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const void* amps, uint64_t nEvents,
+                                 int ampType, int memory);
+/* finishInit (pwaLikelihood.cc:1291-1388) */
+int pwa_likelihood_finish_init(pwa_likelihood* L);
+
+/* accessors (pwaLikelihood.h:188-196, :163) */
+int pwa_likelihood_nmb_pars(const pwa_likelihood* L, uint32_t* n);       /* NDim() */
+int pwa_likelihood_nmb_pars_fixed(const pwa_likelihood* L, uint32_t* n);
+int pwa_likelihood_nmb_events(const pwa_likelihood* L, uint64_t* n);
+int pwa_likelihood_rank(const pwa_likelihood* L, uint32_t* r);
+/* nmbWaves(reflectivity): 0 = all, > 0 positive, < 0 negative (pwaLikelihood.cc:1015-1024) */
+int pwa_likelihood_nmb_waves(const pwa_likelihood* L, int reflectivity, uint32_t* n);
+/* parameter(i) (pwaLikelihood.h:114-150): name as fitParameter::parName() */
+int pwa_likelihood_parameter(const pwa_likelihood* L, uint32_t i, char* nameBuf, uint32_t bufLen, int* fixed,
+                             int* realPart, int32_t* rank, double* threshold);
+/* totAcc of the acceptance integral (pwaLikelihood.cc:1100) */
+int pwa_likelihood_tot_acc(const pwa_likelihood* L, double* totAcc);
+
+/* FdF (pwaLikelihood.cc:170-315): f and the full-length gradient */
+int pwa_likelihood_fdf(pwa_likelihood* L, const double* par, double* f, double* grad);
+/* DoEval (pwaLikelihood.cc:318-435) */
+int pwa_likelihood_doeval(pwa_likelihood* L, const double* par, double* f);
+/* Gradient (pwaLikelihood.cc:474-636) */
+int pwa_likelihood_gradient(pwa_likelihood* L, const double* par, double* grad);
+/* DoDerivative (pwaLikelihood.cc:438-471): cached gradient if par equals the
+ * last evaluated point, else a full FdF */
+int pwa_likelihood_doderivative(pwa_likelihood* L, const double* par, uint32_t index, double* d);
+/* nPoints parameter vectors [nPoints][P] -> f[nPoints], grad[nPoints][P];
+ * one FdF per point, launched back to back on the handle's stream */
+int pwa_likelihood_fdf_batch(pwa_likelihood* L, uint32_t nPoints, const double* par, double* f, double* grad);
+/* Device-resident FdF for device-side minimisers and graph capture: reads
+ * P doubles at dPar, writes dOut[0] = f, dOut[1..P] = gradient, asynchronously
+ * on `stream` (NULL = the handle's stream).  withGradient = 0 gives DoEval. */
+int pwa_likelihood_fdf_device(pwa_likelihood* L, const double* dPar, double* dOut, int withGradient, void* stream);
+/* Hessian (pwaLikelihood.cc:639-859): P x P row-major */
+int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* hessian);
+/* CovarianceMatrix(hessian) (pwaLikelihood.cc:929-981) */
+int pwa_likelihood_covariance_matrix(const pwa_likelihood* L, const double* hessian, double* covariance);
+/* CorrectParamSigns (pwaLikelihood.cc:984-1010) */
+int pwa_likelihood_correct_param_signs(const pwa_likelihood* L, const double* par, double* out);
+/* getIntegralMatrices (pwaLikelihood.cc:1579-1622): norm and acc as
+ * n x n complex128 (n = nmbWaves + withFlat), phaseSpace as n doubles */
+int pwa_likelihood_integral_matrices(const pwa_likelihood* L, double* norm, double* acc, double* phaseSpace,
+                                     int withFlat);
+/* buildProdAmpArrays (pwaLikelihood.cc:1626-1665): production amplitudes
+ * (complex128, count = parameters without the flat imaginary slots) and
+ * their parameter index pairs (im = -1 for real amplitudes); returns the count
+ * in *nAmps.  Buffers must hold P entries. */
+int pwa_likelihood_build_prod_amp_arrays(const pwa_likelihood* L, const double* par, double* prodAmps,
+                                         int32_t* parIndices, uint32_t* nAmps, int withFlat);
+/* functionCallInfo (pwaLikelihood.h:88-106): calls, total / event-loop /
+ * normalisation seconds per call type */
+int pwa_likelihood_func_call_info(const pwa_likelihood* L, int call, uint64_t* nCalls, double* totalTime,
+                                  double* funcTime, double* normTime);
+int pwa_likelihood_reset_func_call_info(pwa_likelihood* L);
+/* Engine instrumentation without reference counterpart: when enabled, every
+ * evaluation records CUDA events on its launch stream before the fused event
+ * kernel, between it and the finalize kernel, and after the finalize kernel.
+ * pwa_likelihood_kernel_times waits for the recorded events, returns the summed
+ * durations in milliseconds and the number of timed evaluations, and clears
+ * the record.  At most 65536 evaluations are recorded between two reads. */
+int pwa_likelihood_set_timing(pwa_likelihood* L, int enable);
+int pwa_likelihood_kernel_times(pwa_likelihood* L, double* eventKernelMs, double* finalizeMs, uint64_t* nTimed);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* PWA_GB300_H */

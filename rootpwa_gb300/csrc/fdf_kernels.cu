@@ -1,0 +1,681 @@
+// fdf_kernels.cu -- fused extended-likelihood value + gradient for sm_103a.
+//
+// One pass over the complex64 amplitude store computes, for every data event i,
+//   S_{r,e,i} = sum_{w in e} V_{r,w} A_{w,i}            (coherent sum, FP32)
+//   L_i       = sum_{r,e} |S_{r,e,i}|^2 + V_flat^2
+//   c_i       = -2 / L_i
+//   G_{r,w}  += c_i S_{r,e(w),i} conj(A_{w,i})          (FP32 per tile, FP64 across tiles)
+// plus -sum ln L_i and sum c_i, which is the event term of
+// partialWaveFit/pwaLikelihood.cc:209-244 (FdF), :361-375 (DoEval) and
+// :547-577 (Gradient).  A second small kernel sums the per-block partials in
+// FP64, adds the normalisation term (:254-273), the half-Cauchy prior
+// (:278-297) and maps the result onto the parameter layout (:1714-1731).
+//
+// Kernel structure (one persistent CTA per SM, 512 threads):
+//   * event tiles of E events x W waves are staged in shared memory by
+//     cp.async.bulk copies (one per wave row, issued by one warp) completing
+//     on an mbarrier; `stages` tiles are in flight;
+//   * phase 1: 512/E threads per event each sum a slice of the waves; the
+//     slices are combined per event, giving L_i, c_i and T_{r,e,i} = c_i S;
+//   * phase 2: warp j owns a contiguous range of waves, each lane a fixed set
+//     of event pairs; per tile the lane sums conj(A) T over its events in FP32
+//     and a warp reduce-scatter leaves every lane one (slot, re/im) value,
+//     which it adds to its FP64 (or compensated FP32) accumulator.
+// Every mbarrier wait is bounded (about a second); on expiry the CTA sets a
+// device error flag, waits (again bounded) for its own copies and returns.
+
+#include "pwa_internal.h"
+
+#include <algorithm>
+
+namespace pwa {
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbarInit(uint64_t* bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbarArriveExpectTx(uint64_t* bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
+	             : "memory");
+}
+
+__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\t"
+	    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+	    "selp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(smemAddr(bar)), "r"(parity)
+	    : "memory");
+	return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long globalTimer()
+{
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Bounded wait for the phase with the given parity to complete.
+__device__ bool mbarWaitBounded(uint64_t* bar, uint32_t parity)
+{
+	if (mbarTryWait(bar, parity))
+		return true;
+	const unsigned long long t0 = globalTimer();
+	while (true) {
+		if (mbarTryWait(bar, parity))
+			return true;
+		if (globalTimer() - t0 > kWaitLimitNs)
+			return false;
+	}
+}
+
+__device__ __forceinline__ void bulkCopyG2S(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 smemAddr(dst)),
+	             "l"(src), "r"(bytes), "r"(smemAddr(bar))
+	             : "memory");
+}
+
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ float warpSum(float v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1)
+		v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+__device__ __forceinline__ double warpSumD(double v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1)
+		v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// Warp reduce-scatter of 32 values held by every lane: afterwards x[0] of
+// lane l holds the sum over all lanes of value index l.
+__device__ __forceinline__ float reduceScatter32(float* x, int lane)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const bool up = (lane & o) != 0;
+#pragma unroll
+		for (int k = 0; k < o; ++k) {
+			const float send = up ? x[k] : x[k + o];
+			const float keep = up ? x[k + o] : x[k];
+			x[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+		}
+	}
+	return x[0];
+}
+
+__device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
+{
+	const float y = x - c;
+	const float t = s + y;
+	c = (t - s) - y;
+	s = t;
+}
+
+// Shared-memory layout of the main kernel (byte offsets from the dynamic base).
+struct SmemLayout {
+	size_t tiles, vs, sp, ts, bars, total;
+};
+
+__host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
+{
+	// every region starts on a 128-byte boundary (float4 and bulk-copy targets)
+	const int H = kThreads / E;
+	auto up = [](size_t x) { return (x + 127) & ~(size_t)127; };
+	SmemLayout L;
+	L.tiles = 0;
+	L.vs = up((size_t)stages * W * E * 8);
+	L.sp = up(L.vs + (size_t)W * R * 8);
+	L.ts = up(L.sp + (size_t)H * R * 2 * E * 8);
+	L.bars = up(L.ts + (size_t)R * 2 * E * 8);
+	L.total = L.bars + (size_t)stages * 8;
+	return L;
+}
+
+template <int R, int E, int WPW>
+__global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, const int stages)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	constexpr int H = kThreads / E;          // threads per event in phase 1
+	constexpr int NV = WPW * R * 2;          // phase-2 values per lane
+	constexpr int NQ = (NV + 31) / 32;       // rounds of 32
+	constexpr int NVP = NQ * 32;
+	constexpr int EPAIRS = E / 64;           // event pairs per lane per tile
+
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int W = a.W, W0 = a.W0;
+	const SmemLayout lay = smemLayout(W, R, E, stages);
+	float2* tiles = reinterpret_cast<float2*>(smem + lay.tiles);
+	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);
+	float2* Sp = reinterpret_cast<float2*>(smem + lay.sp);
+	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
+	__shared__ double redLL[kWarps], redC[kWarps];
+
+	// production amplitudes V[w][r] as FP32 complex
+	for (int k = tid; k < W * R; k += kThreads) {
+		const int w = k / R, r = k - w * R;
+		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
+		Vs[k] = make_float2(ir >= 0 ? (float)a.par[ir] : 0.f, ii >= 0 ? (float)a.par[ii] : 0.f);
+	}
+	const double flatD = a.par[a.P - 1];
+	const float flat2 = (float)(flatD * flatD);
+
+	const uint64_t nTiles = (a.nEvents + E - 1) / E;
+	const uint64_t first = blockIdx.x, stride = gridDim.x;
+	const uint64_t myTiles = (first < nTiles) ? (nTiles - 1 - first) / stride + 1 : 0;
+	const uint32_t stageBytes = (uint32_t)W * E * 8u;
+
+	if (tid == 0) {
+		for (int s = 0; s < stages; ++s)
+			mbarInit(&bars[s], 1);
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+
+	// issue tile k (local index) into stage s; executed by all lanes of warp 0
+	auto issue = [&](uint64_t k, int s) {
+		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
+		float2* dst = tiles + (size_t)s * W * E;
+		if (lane == 0)
+			mbarArriveExpectTx(&bars[s], stageBytes);
+		__syncwarp();
+		for (int w = lane; w < W; w += 32)
+			bulkCopyG2S(dst + (size_t)w * E, a.amps + (size_t)w * a.nPad + e0, E * 8u, &bars[s]);
+	};
+	if (warp == 0) {
+		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
+			issue((uint64_t)s, s);
+	}
+	uint64_t issued = ((uint64_t)stages < myTiles) ? (uint64_t)stages : myTiles;
+
+	// phase-1 role
+	const int pe = tid % E, ph = tid / E;
+	const int pwb = ph * W / H, pwe = (ph + 1) * W / H;
+	// phase-2 role
+	const int wpwa = (W + kWarps - 1) / kWarps;
+	const int wBase = warp * wpwa;
+	const int nWarpWaves = max(0, min(wpwa, W - wBase));
+
+	double accLL = 0., accC = 0.;
+	float kLL = 0.f, kLLc = 0.f, kC = 0.f, kCc = 0.f;
+	double accG[NQ];
+	float kG[NQ], kGc[NQ];
+#pragma unroll
+	for (int q = 0; q < NQ; ++q) {
+		accG[q] = 0.;
+		kG[q] = 0.f;
+		kGc[q] = 0.f;
+	}
+
+	bool failed = false;
+	uint64_t k = 0;
+	for (; k < myTiles; ++k) {
+		const int s = (int)(k % (uint64_t)stages);
+		const uint32_t parity = (uint32_t)((k / (uint64_t)stages) & 1ull);
+		const bool ok = mbarWaitBounded(&bars[s], parity);
+		if (!__syncthreads_and(ok)) {
+			failed = true;
+			break;
+		}
+		const float2* tile = tiles + (size_t)s * W * E;
+		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
+
+		// ---- phase 1: partial coherent sums over a slice of the waves ----
+		{
+			float2 S[R][2];
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				S[r][0] = make_float2(0.f, 0.f);
+				S[r][1] = make_float2(0.f, 0.f);
+			}
+			const int m = min(pwe, W0);
+			for (int w = pwb; w < m; ++w) {
+				const float2 av = tile[(size_t)w * E + pe];
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const float2 v = Vs[w * R + r];
+					S[r][0].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, S[r][0].x));
+					S[r][0].y = fmaf(v.x, av.y, fmaf(v.y, av.x, S[r][0].y));
+				}
+			}
+			for (int w = max(pwb, W0); w < pwe; ++w) {
+				const float2 av = tile[(size_t)w * E + pe];
+#pragma unroll
+				for (int r = 0; r < R; ++r) {
+					const float2 v = Vs[w * R + r];
+					S[r][1].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, S[r][1].x));
+					S[r][1].y = fmaf(v.x, av.y, fmaf(v.y, av.x, S[r][1].y));
+				}
+			}
+#pragma unroll
+			for (int r = 0; r < R; ++r) {
+				Sp[((ph * R + r) * 2 + 0) * E + pe] = S[r][0];
+				Sp[((ph * R + r) * 2 + 1) * E + pe] = S[r][1];
+			}
+		}
+		__syncthreads();
+
+		// ---- combine: L_i, c_i, T = c_i S ----
+		if (tid < E) {
+			float L = flat2;
+			float2 S[R][2];
+#pragma unroll
+			for (int r = 0; r < R; ++r)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					float2 acc = Sp[((0 * R + r) * 2 + e) * E + tid];
+#pragma unroll
+					for (int h = 1; h < H; ++h) {
+						const float2 p = Sp[((h * R + r) * 2 + e) * E + tid];
+						acc.x += p.x;
+						acc.y += p.y;
+					}
+					S[r][e] = acc;
+					L = fmaf(acc.x, acc.x, fmaf(acc.y, acc.y, L));
+				}
+			const bool valid = (e0 + (uint64_t)tid) < a.nEvents;
+			const float c = valid ? -2.f / L : 0.f;
+			float ll = valid ? -logf(L) : 0.f;
+			if (a.withGrad) {
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+#pragma unroll
+					for (int e = 0; e < 2; ++e)
+						Ts[(r * 2 + e) * E + tid] = make_float2(c * S[r][e].x, c * S[r][e].y);
+			}
+			ll = warpSum(ll);
+			const float cs = warpSum(c);
+			if (lane == 0) {
+				if (a.reduction == 0) {
+					accLL += (double)ll;
+					accC += (double)cs;
+				} else {
+					kahanAdd(kLL, kLLc, ll);
+					kahanAdd(kC, kCc, cs);
+				}
+			}
+		}
+		__syncthreads();
+
+		// ---- phase 2: gradient contraction over the tile ----
+		if (a.withGrad) {
+			float part[NVP];
+#pragma unroll
+			for (int v = 0; v < NVP; ++v)
+				part[v] = 0.f;
+#pragma unroll
+			for (int pp = 0; pp < EPAIRS; ++pp) {
+				const int ev = 2 * lane + 64 * pp;
+				float4 t[R][2];
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+#pragma unroll
+					for (int e = 0; e < 2; ++e)
+						t[r][e] = *reinterpret_cast<const float4*>(&Ts[(r * 2 + e) * E + ev]);
+#pragma unroll
+				for (int wi = 0; wi < WPW; ++wi) {
+					if (wi < nWarpWaves) {
+						const int w = wBase + wi;
+						const float4 av = *reinterpret_cast<const float4*>(&tile[(size_t)w * E + ev]);
+						const bool pos = (w >= W0);
+#pragma unroll
+						for (int r = 0; r < R; ++r) {
+							const float4 tt = pos ? t[r][1] : t[r][0];
+							// conj(a0) t0 + conj(a1) t1
+							float re = part[(wi * R + r) * 2 + 0];
+							float im = part[(wi * R + r) * 2 + 1];
+							re = fmaf(av.x, tt.x, re);
+							re = fmaf(av.y, tt.y, re);
+							re = fmaf(av.z, tt.z, re);
+							re = fmaf(av.w, tt.w, re);
+							im = fmaf(av.x, tt.y, im);
+							im = fmaf(-av.y, tt.x, im);
+							im = fmaf(av.z, tt.w, im);
+							im = fmaf(-av.w, tt.z, im);
+							part[(wi * R + r) * 2 + 0] = re;
+							part[(wi * R + r) * 2 + 1] = im;
+						}
+					}
+				}
+			}
+#pragma unroll
+			for (int q = 0; q < NQ; ++q) {
+				const float v = reduceScatter32(&part[q * 32], lane);
+				if (a.reduction == 0)
+					accG[q] += (double)v;
+				else
+					kahanAdd(kG[q], kGc[q], v);
+			}
+		}
+		__syncthreads();  // stage s and Ts are free again
+
+		if (warp == 0 && k + (uint64_t)stages < myTiles) {
+			fenceProxyAsync();
+			issue(k + (uint64_t)stages, s);
+		}
+		if (k + (uint64_t)stages < myTiles)
+			++issued;
+	}
+
+	if (failed) {
+		// let our own copies in flight land before the CTA exits (bounded)
+		if (tid == 0) {
+			atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+			for (uint64_t j = k; j < issued; ++j) {
+				const int s = (int)(j % (uint64_t)stages);
+				mbarWaitBounded(&bars[s], (uint32_t)((j / (uint64_t)stages) & 1ull));
+			}
+		}
+		return;
+	}
+
+	// ---- epilogue: per-block partials ----
+	double* out = a.partials + (size_t)blockIdx.x * a.nPartial;
+	if (lane == 0) {
+		if (a.reduction == 0) {
+			redLL[warp] = accLL;
+			redC[warp] = accC;
+		} else {
+			redLL[warp] = (double)kLL - (double)kLLc;
+			redC[warp] = (double)kC - (double)kCc;
+		}
+	}
+	__syncthreads();
+	if (tid == 0) {
+		double ll = 0., cs = 0.;
+		for (int wv = 0; wv < E / 32; ++wv) {
+			ll += redLL[wv];
+			cs += redC[wv];
+		}
+		out[0] = ll;
+		out[1] = cs;
+	}
+	if (a.withGrad) {
+#pragma unroll
+		for (int q = 0; q < NQ; ++q) {
+			const int vi = q * 32 + lane;
+			if (vi < NV) {
+				const int wi = vi / (2 * R);
+				const int rem = vi - wi * 2 * R;
+				const int r = rem >> 1, comp = rem & 1;
+				if (wi < nWarpWaves) {
+					const int w = wBase + wi;
+					const double v = (a.reduction == 0) ? accG[q] : ((double)kG[q] - (double)kGc[q]);
+					out[2 + (r * W + w) * 2 + comp] = v;
+				}
+			}
+		}
+	}
+}
+
+constexpr int kFinWarps = 8;
+
+__global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArgs f)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int g = blockIdx.x * kFinWarps + warp;
+	const int nSlots = f.R * f.W;
+	const double twice = 2. * f.nEvt;
+	const double flat = f.par[f.P - 1];
+	__shared__ double sNorm[kFinWarps], sPrior[kFinWarps];
+	__shared__ int sLast;
+	double normv = 0., priorv = 0.;
+	if (g < nSlots) {
+		const int r = g / f.W, w = g - r * f.W;
+		const int pos = (w >= f.W0) ? 1 : 0;
+		const int off = pos ? f.W0 : 0;
+		const int We = pos ? f.W - f.W0 : f.W0;
+		const int i = w - off;
+		const int ire = f.slotRe[g], iim = f.slotIm[g];
+		const double vr = ire >= 0 ? f.par[ire] : 0., vi = iim >= 0 ? f.par[iim] : 0.;
+		double gre = 0., gim = 0.;
+		if (f.withGrad)
+			for (int b = lane; b < f.nBlocks; b += 32) {
+				gre += f.partials[(size_t)b * f.nPartial + 2 + 2 * g];
+				gim += f.partials[(size_t)b * f.nPartial + 3 + 2 * g];
+			}
+		// D_i = sum_j V_j conj(I_ij) over waves of the same reflectivity
+		const double* Ib = f.accI + (pos ? 2 * (size_t)f.W0 * f.W0 : 0) + 2 * (size_t)i * We;
+		double dre = 0., dim = 0.;
+		for (int j = lane; j < We; j += 32) {
+			const int sj = r * f.W + off + j;
+			const int jr = f.slotRe[sj], ji = f.slotIm[sj];
+			const double ur = jr >= 0 ? f.par[jr] : 0., ui = ji >= 0 ? f.par[ji] : 0.;
+			const double Ir = Ib[2 * j], Ii = Ib[2 * j + 1];
+			dre += ur * Ir + ui * Ii;
+			dim += ui * Ir - ur * Ii;
+		}
+		gre = warpSumD(gre);
+		gim = warpSumD(gim);
+		dre = warpSumD(dre);
+		dim = warpSumD(dim);
+		if (lane == 0) {
+			normv = vr * dre + vi * dim;  // Re(V_i conj(D_i))
+			double pre = 0., pim = 0.;
+			if (f.prior == 1) {
+				const double rr = hypot(vr, vi);
+				const double g2 = f.cauchyWidth * f.cauchyWidth;
+				const double cf = 1. / (1. + (rr * rr) / g2);
+				const double cd = (-2. * rr * g2) / ((g2 + rr * rr) * (g2 + rr * rr));
+				const double fac = (1. / (rr * cf)) * cd;
+				priorv = -log(cf);
+				pre = fac * vr;
+				pim = fac * vi;
+			}
+			if (f.withGrad) {
+				if (ire >= 0)
+					f.out[1 + ire] = gre + twice * dre - pre;
+				if (iim >= 0)
+					f.out[1 + iim] = gim + twice * dim - pim;
+			}
+		}
+	} else if (g == nSlots) {
+		double ll = 0., cs = 0.;
+		for (int b = lane; b < f.nBlocks; b += 32) {
+			ll += f.partials[(size_t)b * f.nPartial + 0];
+			cs += f.partials[(size_t)b * f.nPartial + 1];
+		}
+		ll = warpSumD(ll);
+		cs = warpSumD(cs);
+		if (lane == 0) {
+			if (f.withGrad)
+				f.out[f.P] = flat * cs + twice * flat * f.totAcc;
+			f.scratch[2 * gridDim.x] = ll;
+		}
+	}
+	if (lane == 0) {
+		sNorm[warp] = normv;
+		sPrior[warp] = priorv;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double n = 0., p = 0.;
+		for (int wv = 0; wv < kFinWarps; ++wv) {
+			n += sNorm[wv];
+			p += sPrior[wv];
+		}
+		f.scratch[2 * blockIdx.x] = n;
+		f.scratch[2 * blockIdx.x + 1] = p;
+		__threadfence();
+		const unsigned t = atomicAdd(f.ticket, 1u);
+		sLast = (t == gridDim.x - 1) ? 1 : 0;
+	}
+	__syncthreads();
+	if (sLast && warp == 0) {
+		__threadfence();
+		const volatile double* sc = f.scratch;
+		double n = 0., p = 0.;
+		for (int b = lane; b < (int)gridDim.x; b += 32) {
+			n += sc[2 * b];
+			p += sc[2 * b + 1];
+		}
+		n = warpSumD(n);
+		p = warpSumD(p);
+		if (lane == 0) {
+			const double ll = sc[2 * gridDim.x];
+			f.out[0] = ll + f.nEvt * (n + flat * flat * f.totAcc) + p;
+			f.out[f.P + 1] = (double)(*(const volatile unsigned*)f.devErr);
+			*f.ticket = 0u;
+		}
+	}
+}
+
+__global__ void convertRowKernel(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor,
+                                 unsigned* nonzero)
+{
+	bool any = false;
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+		double re, im;
+		if (srcIsDouble) {
+			const double2 v = reinterpret_cast<const double2*>(src)[i];
+			re = v.x;
+			im = v.y;
+		} else {
+			const float2 v = reinterpret_cast<const float2*>(src)[i];
+			re = v.x;
+			im = v.y;
+		}
+		any = any || re != 0. || im != 0.;
+		dst[i] = make_float2((float)(re / divisor), (float)(im / divisor));
+	}
+	if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0)
+		atomicOr(nonzero, 1u);
+}
+
+template <int R, int E, int WPW>
+int launchVariant(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
+{
+	auto kern = fdfMainKernel<R, E, WPW>;
+	// raise the dynamic shared-memory limit once per variant (not a stream
+	// operation, so it is kept out of the launches captured into graphs)
+	static size_t configured = 0;
+	if (p.smemBytes > configured) {
+		const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smemBytes);
+		if (e != cudaSuccess)
+			return cudaCheck(e, "cudaFuncSetAttribute(fdf)");
+		configured = p.smemBytes;
+	}
+	kern<<<p.blocks, kThreads, p.smemBytes, s>>>(a, p.stages);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "fdf kernel launch");
+}
+
+template <int R>
+int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
+{
+	if (p.E == 128) {
+		switch (p.wpw) {
+		case 2: return launchVariant<R, 128, 2>(p, a, s);
+		case 4: return launchVariant<R, 128, 4>(p, a, s);
+		case 8: return launchVariant<R, 128, 8>(p, a, s);
+		default: break;
+		}
+	} else if (p.E == 64) {
+		switch (p.wpw) {
+		case 8: return launchVariant<R, 64, 8>(p, a, s);
+		case 14: return launchVariant<R, 64, 14>(p, a, s);
+		default: break;
+		}
+	}
+	return setError(kErrUnsupported, "no FdF kernel variant for this tile/wave bucket");
+}
+
+}  // namespace
+
+int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan)
+{
+	if (R < 1 || R > 4)
+		return setError(kErrUnsupported, "FdF kernel supports rank 1..4");
+	if (W < 1)
+		return setError(kErrArg, "no waves");
+	const int wpwa = (W + kWarps - 1) / kWarps;
+	int wpw;
+	if (wpwa <= 2) wpw = 2;
+	else if (wpwa <= 4) wpw = 4;
+	else if (wpwa <= 8) wpw = 8;
+	else if (wpwa <= 14) wpw = 14;
+	else return setError(kErrUnsupported, "FdF kernel supports at most 224 waves");
+	if (R * wpw > 32)
+		return setError(kErrUnsupported, "rank x waves-per-warp beyond the compiled register budget");
+	// prefer E = 128 with >= 2 stages; fall back to E = 64
+	int E = (wpw <= 8) ? 128 : 64;
+	int stages = 0;
+	for (int tries = 0; tries < 2 && stages == 0; ++tries) {
+		for (int st = 4; st >= 2; --st) {
+			if (smemLayout(W, R, E, st).total + 512 <= maxSmem) {
+				stages = st;
+				break;
+			}
+		}
+		if (stages == 0) {
+			if (E == 128 && wpw == 8) {
+				E = 64;
+			} else {
+				break;
+			}
+		}
+	}
+	if (stages == 0)
+		return setError(kErrUnsupported, "amplitude tile does not fit in shared memory");
+	plan->E = E;
+	plan->stages = stages;
+	plan->wpw = wpw;
+	const uint64_t nTiles = (nEvents + E - 1) / E;
+	plan->blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
+	plan->smemBytes = smemLayout(W, R, E, stages).total;
+	return kOk;
+}
+
+int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
+{
+	switch (a.R) {
+	case 1: return launchR<1>(p, a, s);
+	case 2: return launchR<2>(p, a, s);
+	case 3: return launchR<3>(p, a, s);
+	case 4: return launchR<4>(p, a, s);
+	default: return setError(kErrUnsupported, "FdF kernel supports rank 1..4");
+	}
+}
+
+int finalizeBlocks(int R, int W) { return (R * W + 1 + kFinWarps - 1) / kFinWarps; }
+
+int launchFinalize(const FinArgs& a, int finBlocks, cudaStream_t s)
+{
+	fdfFinalizeKernel<<<finBlocks, kFinWarps * 32, 0, s>>>(a);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "fdf finalize launch");
+}
+
+int launchConvertRow(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor, unsigned* nonzero,
+                     cudaStream_t s)
+{
+	const int threads = 256;
+	const int blocks = (int)std::min<uint64_t>((n + threads - 1) / threads, 4096);
+	convertRowKernel<<<std::max(blocks, 1), threads, 0, s>>>(src, srcIsDouble, dst, n, divisor, nonzero);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "convert row launch");
+}
+
+}  // namespace pwa

@@ -1,0 +1,1778 @@
+// pwa_host.cpp -- host side of the GB300 extended-likelihood engine: the
+// C ABI of include/pwa_gb300.h over two C++ objects that mirror ROOTPWA's
+// rpwa::ampIntegralMatrix and rpwa::pwaLikelihood<complex<double>>.
+//
+// Setup (wave list, parameter layout, integral reordering and rescaling,
+// amplitude normalisation) follows the reference line by line in FP64 on the
+// host; every per-event loop runs in the CUDA kernels of this directory.
+
+#include "../../include/pwa_gb300.h"
+#include "pwa_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <map>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+typedef std::complex<double> cplx;
+
+namespace {
+thread_local std::string g_lastError;
+std::atomic<uint64_t> g_launches{0};
+}  // namespace
+
+namespace pwa {
+
+int setError(int code, const std::string& msg)
+{
+	if (code != kOk)
+		g_lastError = msg;
+	return code;
+}
+
+int cudaCheck(cudaError_t e, const char* what)
+{
+	if (e == cudaSuccess)
+		return kOk;
+	cudaGetLastError();  // clear the sticky-free error state of the runtime
+	return setError(e == cudaErrorMemoryAllocation ? kErrOom : kErrCuda,
+	                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void countLaunches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+// device allocation owned by a handle
+struct DevBuf {
+	void* p = nullptr;
+	size_t bytes = 0;
+	DevBuf() = default;
+	DevBuf(const DevBuf&) = delete;
+	DevBuf& operator=(const DevBuf&) = delete;
+	~DevBuf() { release(); }
+	int alloc(size_t b, const char* what)
+	{
+		release();
+		if (b == 0)
+			return kOk;
+		const cudaError_t e = cudaMalloc(&p, b);
+		if (e != cudaSuccess) {
+			p = nullptr;
+			return cudaCheck(e, what);
+		}
+		bytes = b;
+		return kOk;
+	}
+	int ensure(size_t b, const char* what) { return (bytes >= b && p) ? kOk : alloc(b, what); }
+	void release()
+	{
+		if (p)
+			cudaFree(p);
+		p = nullptr;
+		bytes = 0;
+	}
+	template <typename T>
+	T* as() const
+	{
+		return static_cast<T*>(p);
+	}
+};
+
+// page-locked host staging buffer
+struct PinnedBuf {
+	void* p = nullptr;
+	size_t bytes = 0;
+	PinnedBuf() = default;
+	PinnedBuf(const PinnedBuf&) = delete;
+	PinnedBuf& operator=(const PinnedBuf&) = delete;
+	~PinnedBuf() { release(); }
+	int ensure(size_t b, const char* what)
+	{
+		if (p && bytes >= b)
+			return kOk;
+		release();
+		const cudaError_t e = cudaMallocHost(&p, b);
+		if (e != cudaSuccess) {
+			p = nullptr;
+			return cudaCheck(e, what);
+		}
+		bytes = b;
+		return kOk;
+	}
+	void release()
+	{
+		if (p)
+			cudaFreeHost(p);
+		p = nullptr;
+		bytes = 0;
+	}
+	template <typename T>
+	T* as() const
+	{
+		return static_cast<T*>(p);
+	}
+};
+
+#define PWA_TRY(expr)                 \
+	do {                              \
+		const int _st = (expr);       \
+		if (_st != kOk)               \
+			return _st;               \
+	} while (0)
+
+int deviceInfo(int* dev, int* sms, size_t* smem)
+{
+	PWA_TRY(cudaCheck(cudaGetDevice(dev), "cudaGetDevice"));
+	PWA_TRY(cudaCheck(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, *dev), "SM count"));
+	int optin = 0;
+	PWA_TRY(cudaCheck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, *dev), "smem"));
+	*smem = (size_t)optin;
+	return kOk;
+}
+
+std::string fmtDouble(double v)
+{
+	char buf[64];
+	std::snprintf(buf, sizeof(buf), "%.16e", v);
+	return buf;
+}
+
+}  // namespace
+}  // namespace pwa
+
+using namespace pwa;
+
+// ===========================================================================
+// ampIntegralMatrix
+// ===========================================================================
+struct pwa_integral {
+	uint32_t nWaves = 0;
+	uint64_t nEvents = 0;
+	std::vector<std::string> names;
+	std::vector<cplx> sums;  // raw sums [i][j]
+
+	int index(const std::string& n) const
+	{
+		for (size_t i = 0; i < names.size(); ++i)
+			if (names[i] == n)
+				return (int)i;
+		return -1;
+	}
+	bool sameWaveSet(const pwa_integral& o) const
+	{
+		if (o.nWaves != nWaves)
+			return false;
+		for (const auto& n : names)
+			if (o.index(n) < 0)
+				return false;
+		return true;
+	}
+};
+
+namespace {
+
+// Sums the GPU Gram kernel for integrate().
+int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, int ampType, int memory,
+                 const std::vector<double>& weightK, uint64_t K, int precision, std::vector<cplx>& out)
+{
+	int dev, sms;
+	size_t smem;
+	PWA_TRY(deviceInfo(&dev, &sms, &smem));
+	cudaStream_t s = nullptr;
+	PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream"));
+	struct StreamGuard {
+		cudaStream_t s;
+		~StreamGuard() { cudaStreamDestroy(s); }
+	} guard{s};
+
+	// device inputs may still be written by the caller's streams
+	if (memory == PWA_MEMORY_DEVICE)
+		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device amplitudes"));
+	const uint64_t ldIn = nEvents * nSub;
+	const bool wantDouble = (precision == PWA_PRECISION_FP64 && ampType == PWA_COMPLEX128);
+	DevBuf dIn, dConv, dW, dPart, dOut, dErr;
+	const float2* a32 = nullptr;
+	const double2* a64 = nullptr;
+	uint64_t ldK = ldIn;
+	if (memory == PWA_MEMORY_DEVICE) {
+		if (ampType == PWA_COMPLEX64) {
+			a32 = static_cast<const float2*>(amps);
+		} else if (wantDouble) {
+			a64 = static_cast<const double2*>(amps);
+		} else {
+			PWA_TRY(dConv.alloc((size_t)W * K * sizeof(float2), "integral conversion buffer"));
+			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
+			for (uint32_t w = 0; w < W; ++w)
+				PWA_TRY(launchConvertRow(static_cast<const double2*>(amps) + (size_t)w * ldIn, 1,
+				                         dConv.as<float2>() + (size_t)w * K, K, 1.0, dErr.as<unsigned>(), s));
+			a32 = dConv.as<float2>();
+			ldK = K;
+		}
+	} else {
+		const size_t elem = (ampType == PWA_COMPLEX64) ? sizeof(float2) : sizeof(double2);
+		PWA_TRY(dIn.alloc((size_t)W * K * elem, "integral amplitude buffer"));
+		PWA_TRY(cudaCheck(cudaMemcpy2DAsync(dIn.p, K * elem, amps, ldIn * elem, K * elem, W, cudaMemcpyHostToDevice, s),
+		                  "integral amplitude upload"));
+		ldK = K;
+		if (ampType == PWA_COMPLEX64) {
+			a32 = dIn.as<float2>();
+		} else if (wantDouble) {
+			a64 = dIn.as<double2>();
+		} else {
+			PWA_TRY(dConv.alloc((size_t)W * K * sizeof(float2), "integral conversion buffer"));
+			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
+			for (uint32_t w = 0; w < W; ++w)
+				PWA_TRY(launchConvertRow(dIn.as<double2>() + (size_t)w * K, 1, dConv.as<float2>() + (size_t)w * K, K, 1.0,
+				                         dErr.as<unsigned>(), s));
+			a32 = dConv.as<float2>();
+		}
+	}
+	if (!weightK.empty()) {
+		PWA_TRY(dW.alloc(weightK.size() * sizeof(double), "weights"));
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(dW.p, weightK.data(), weightK.size() * sizeof(double),
+		                                  cudaMemcpyHostToDevice, s),
+		                  "weight upload"));
+	}
+	PWA_TRY(dOut.alloc((size_t)W * W * 2 * sizeof(double), "integral output"));
+	if (!dErr.p)
+		PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(dErr.p, 0, sizeof(unsigned), s), "memset"));
+
+	GramArgs g{};
+	g.amps = a32;
+	g.amps64 = a64;
+	g.K = K;
+	g.ldK = ldK;
+	g.W = (int)W;
+	g.weightK = weightK.empty() ? nullptr : dW.as<double>();
+	g.devErr = dErr.as<unsigned>();
+	int st = kErrUnsupported;
+	if (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3 || precision == PWA_PRECISION_BF16X3) {
+		const size_t scratch = (size_t)2 * sms * 2 * 128 * 256;  // per-CTA partial tiles, upper bound
+		PWA_TRY(dPart.alloc(scratch * sizeof(double), "gram partials"));
+		st = launchGramTc(g, precision, sms, s, dOut.as<double>(), dPart.as<double>(), scratch);
+		if (st != kOk)
+			return st;
+	} else {
+		const int tps = ((int)W + 63) / 64;
+		const int nTiles = tps * (tps + 1) / 2;
+		int chunks = std::max(1, (4 * sms + nTiles - 1) / nTiles);
+		const uint64_t maxChunks = std::max<uint64_t>(1, K / 64);
+		chunks = (int)std::min<uint64_t>((uint64_t)chunks, maxChunks);
+		g.chunks = chunks;
+		PWA_TRY(dPart.alloc((size_t)chunks * W * W * 2 * sizeof(double), "gram partials"));
+		PWA_TRY(cudaCheck(cudaMemsetAsync(dPart.p, 0, dPart.bytes, s), "memset"));
+		g.partials = dPart.as<double>();
+		PWA_TRY(launchGramSimt(g, precision, s));
+		PWA_TRY(launchGramReduce(g.partials, chunks, (int)W, dOut.as<double>(), 0, s));
+	}
+	std::vector<double> host((size_t)W * W * 2);
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(host.data(), dOut.p, host.size() * sizeof(double), cudaMemcpyDeviceToHost, s),
+	                  "integral download"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "integral sync"));
+	out.resize((size_t)W * W);
+	for (size_t k = 0; k < out.size(); ++k)
+		out[k] = cplx(host[2 * k], host[2 * k + 1]);
+	return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pwa_abi_version(void) { return PWA_GB300_ABI_VERSION; }
+const char* pwa_last_error(void) { return g_lastError.c_str(); }
+uint64_t pwa_kernel_launch_count(void) { return g_launches.load(); }
+
+int pwa_integral_create(pwa_integral** out)
+{
+	if (!out)
+		return setError(kErrArg, "null output pointer");
+	try {
+		*out = new pwa_integral();
+	} catch (const std::bad_alloc&) {
+		return setError(kErrOom, "host allocation failed");
+	}
+	return kOk;
+}
+
+int pwa_integral_destroy(pwa_integral* I)
+{
+	delete I;
+	return kOk;
+}
+
+int pwa_integral_copy(pwa_integral* dst, const pwa_integral* src)
+{
+	if (!dst || !src)
+		return setError(kErrArg, "null integral");
+	if (dst != src)
+		*dst = *src;
+	return kOk;
+}
+
+int pwa_integral_set_wave_names(pwa_integral* I, uint32_t n, const char* const* names)
+{
+	if (!I || (!names && n))
+		return setError(kErrArg, "null argument");
+	if (I->nWaves > 0) {
+		if (n != I->nWaves)
+			return setError(kErrState, "integral matrix was already initialized with a different number of waves");
+		for (uint32_t i = 0; i < n; ++i)
+			if (I->names[i] != names[i])
+				return setError(kErrState, "integral matrix was already initialized with different wave names");
+		return kOk;
+	}
+	I->names.assign(names, names + n);
+	I->nWaves = n;
+	I->sums.assign((size_t)n * n, cplx(0, 0));
+	return kOk;
+}
+
+int pwa_integral_integrate(pwa_integral* I, uint32_t nWaves, const char* const* waveNames, const void* amps,
+                           uint64_t nEvents, uint32_t nSubAmps, int ampType, int memory, const double* weights,
+                           uint64_t nWeights, const uint8_t* inBin, int64_t maxNmbEvents, int precision)
+{
+	if (!I || !waveNames || !amps)
+		return setError(kErrArg, "null argument");
+	if (nWaves == 0)
+		return setError(kErrArg, "did not receive any amplitudes; cannot calculate integral");
+	if (nEvents == 0)
+		return setError(kErrArg, "amplitudes contain no values; cannot calculate integral");
+	if (nSubAmps == 0)
+		return setError(kErrArg, "amplitude object does not contain any amplitude values");
+	if (ampType != PWA_COMPLEX64 && ampType != PWA_COMPLEX128)
+		return setError(kErrArg, "unknown amplitude type");
+	if (memory != PWA_MEMORY_HOST && memory != PWA_MEMORY_DEVICE)
+		return setError(kErrArg, "unknown memory kind");
+	if (precision < PWA_PRECISION_FP64 || precision > PWA_PRECISION_BF16X3)
+		return setError(kErrArg, "unknown precision");
+	// wave-name bookkeeping as ampIntegralMatrix.cc:310-330
+	if (I->names.empty()) {
+		I->names.assign(waveNames, waveNames + nWaves);
+		I->nWaves = nWaves;
+	} else {
+		if (I->names.size() != nWaves)
+			return setError(kErrState, "integral matrix was already initialized with a different number of waves");
+		for (uint32_t i = 0; i < nWaves; ++i)
+			if (I->names[i] != waveNames[i])
+				return setError(kErrState, "integral matrix was already initialized with different wave names");
+	}
+	const uint64_t nProc = (maxNmbEvents <= 0) ? nEvents : std::min<uint64_t>(nEvents, (uint64_t)maxNmbEvents);
+	// event selection and weights (ampIntegralMatrix.cc:408-429): the weight
+	// stream is consumed by events that pass the bin cut, in order
+	std::vector<double> weightK;
+	uint64_t counter = 0, wIdx = 0, lastK = nProc;
+	bool success = true;
+	double wsum = 0., wcomp = 0.;  // compensated sum of 1/w
+	const bool useWeight = (weights != nullptr);
+	if (useWeight || inBin) {
+		weightK.assign(nProc * nSubAmps, 0.);
+		for (uint64_t ev = 0; ev < nProc; ++ev) {
+			if (inBin && !inBin[ev])
+				continue;
+			++counter;
+			double w = 1.;
+			if (useWeight) {
+				if (wIdx >= nWeights) {
+					success = false;
+					lastK = ev;
+					break;
+				}
+				w = weights[wIdx++];
+			}
+			const double weight = 1. / w;
+			const double y = weight - wcomp, t = wsum + y;
+			wcomp = (t - wsum) - y;
+			wsum = t;
+			for (uint32_t s = 0; s < nSubAmps; ++s)
+				weightK[ev * nSubAmps + s] = useWeight ? weight : 1.;
+		}
+	} else {
+		counter = nProc;
+		wsum = (double)nProc;
+	}
+	const uint64_t K = nProc * nSubAmps;
+	std::vector<cplx> result;
+	if (lastK > 0 && counter > 0)
+		PWA_TRY(gramOnDevice(nWaves, amps, nEvents, nSubAmps, ampType, memory, weightK, K, precision, result));
+	else
+		result.assign((size_t)nWaves * nWaves, cplx(0, 0));
+	I->nEvents = counter;
+	I->sums = result;
+	if (useWeight && counter > 0) {
+		const double weightNorm = wsum / (double)counter;
+		for (auto& v : I->sums)
+			v *= 1. / weightNorm;
+	}
+	if (!success)
+		return setError(kErrIo, "weight stream shorter than the number of selected events; integration stopped");
+	return kOk;
+}
+
+int pwa_integral_add_event(pwa_integral* I, const double* amps)
+{
+	if (!I || !amps)
+		return setError(kErrArg, "null argument");
+	const uint32_t n = I->nWaves;
+	for (uint32_t i = 0; i < n; ++i) {
+		const cplx a(amps[2 * i], amps[2 * i + 1]);
+		for (uint32_t j = 0; j < n; ++j)
+			I->sums[(size_t)i * n + j] += a * std::conj(cplx(amps[2 * j], amps[2 * j + 1]));
+	}
+	++I->nEvents;
+	return kOk;
+}
+
+int pwa_integral_element(const pwa_integral* I, uint32_t i, uint32_t j, double* re, double* im)
+{
+	if (!I || !re || !im)
+		return setError(kErrArg, "null argument");
+	if (i >= I->nWaves || j >= I->nWaves)
+		return setError(kErrArg, "wave index out of range");
+	const cplx v = I->sums[(size_t)i * I->nWaves + j] / (double)I->nEvents;
+	*re = v.real();
+	*im = v.imag();
+	return kOk;
+}
+
+int pwa_integral_matrix(const pwa_integral* I, double* out)
+{
+	if (!I || !out)
+		return setError(kErrArg, "null argument");
+	for (size_t k = 0; k < I->sums.size(); ++k) {
+		out[2 * k] = I->sums[k].real();
+		out[2 * k + 1] = I->sums[k].imag();
+	}
+	return kOk;
+}
+
+int pwa_integral_set_matrix(pwa_integral* I, const double* in)
+{
+	if (!I || !in)
+		return setError(kErrArg, "null argument");
+	for (size_t k = 0; k < I->sums.size(); ++k)
+		I->sums[k] = cplx(in[2 * k], in[2 * k + 1]);
+	return kOk;
+}
+
+int pwa_integral_nmb_waves(const pwa_integral* I, uint32_t* n)
+{
+	if (!I || !n)
+		return setError(kErrArg, "null argument");
+	*n = I->nWaves;
+	return kOk;
+}
+
+int pwa_integral_nmb_events(const pwa_integral* I, uint64_t* n)
+{
+	if (!I || !n)
+		return setError(kErrArg, "null argument");
+	*n = I->nEvents;
+	return kOk;
+}
+
+int pwa_integral_set_nmb_events(pwa_integral* I, uint64_t n)
+{
+	if (!I)
+		return setError(kErrArg, "null argument");
+	I->nEvents = n;
+	return kOk;
+}
+
+int pwa_integral_wave_name(const pwa_integral* I, uint32_t i, char* buf, uint32_t len)
+{
+	if (!I || !buf || len == 0)
+		return setError(kErrArg, "null argument");
+	if (i >= I->names.size())
+		return setError(kErrArg, "wave index out of range");
+	std::snprintf(buf, len, "%s", I->names[i].c_str());
+	return kOk;
+}
+
+int pwa_integral_wave_index(const pwa_integral* I, const char* name, uint32_t* index)
+{
+	if (!I || !name || !index)
+		return setError(kErrArg, "null argument");
+	const int k = I->index(name);
+	if (k < 0)
+		return setError(kErrArg, std::string("cannot find wave '") + name + "' in integral matrix");
+	*index = (uint32_t)k;
+	return kOk;
+}
+
+static int integralCombine(pwa_integral* I, const pwa_integral* o, double sign)
+{
+	if (!I || !o)
+		return setError(kErrArg, "null argument");
+	if (!I->sameWaveSet(*o))
+		return setError(kErrArg, "the two integral matrices have different wave sets");
+	const uint32_t n = I->nWaves;
+	for (uint32_t i = 0; i < n; ++i) {
+		const int oi = o->index(I->names[i]);
+		for (uint32_t j = 0; j < n; ++j) {
+			const int oj = o->index(I->names[j]);
+			I->sums[(size_t)i * n + j] += sign * o->sums[(size_t)oi * n + oj];
+		}
+	}
+	if (sign > 0)
+		I->nEvents += o->nEvents;
+	else
+		I->nEvents -= o->nEvents;
+	return kOk;
+}
+
+int pwa_integral_add(pwa_integral* I, const pwa_integral* o) { return integralCombine(I, o, 1.); }
+int pwa_integral_subtract(pwa_integral* I, const pwa_integral* o) { return integralCombine(I, o, -1.); }
+
+int pwa_integral_scale(pwa_integral* I, double f)
+{
+	if (!I)
+		return setError(kErrArg, "null argument");
+	for (auto& v : I->sums)
+		v *= f;
+	I->nEvents = (uint64_t)((double)I->nEvents * f);
+	return kOk;
+}
+
+int pwa_integral_divide(pwa_integral* I, double f)
+{
+	if (!I)
+		return setError(kErrArg, "null argument");
+	for (auto& v : I->sums)
+		v /= f;
+	I->nEvents = (uint64_t)((double)I->nEvents / f);
+	return kOk;
+}
+
+int pwa_integral_renormalize(pwa_integral* I, uint64_t n)
+{
+	if (!I)
+		return setError(kErrArg, "null argument");
+	if (I->nEvents == 0)
+		return setError(kErrState, "integral has no events");
+	PWA_TRY(pwa_integral_scale(I, (double)n / (double)I->nEvents));
+	I->nEvents = n;
+	return kOk;
+}
+
+int pwa_integral_read_ascii(pwa_integral* I, const char* path)
+{
+	if (!I || !path)
+		return setError(kErrArg, "null argument");
+	std::ifstream in(path);
+	if (!in)
+		return setError(kErrIo, std::string("cannot open file '") + path + "' for reading of integral matrix");
+	uint32_t nw;
+	uint64_t ne;
+	if (!(in >> nw >> ne))
+		return setError(kErrIo, "could not read number of waves and events");
+	uint32_t nr, nc;
+	if (!(in >> nr >> nc))
+		return setError(kErrIo, "could not read number of rows and columns");
+	std::vector<cplx> m((size_t)nr * nc);
+	for (uint32_t i = 0; i < nr; ++i)
+		for (uint32_t j = 0; j < nc; ++j)
+			if (!(in >> m[(size_t)i * nc + j]) || in.eof())
+				return setError(kErrIo, "could not read integral values; stream seems truncated");
+	uint32_t mapSize;
+	in >> mapSize;
+	if (mapSize != nw)
+		return setError(kErrIo, "mismatch between integral dimensions and number of wave names");
+	std::vector<std::string> names(nw);
+	while (mapSize > 0 && in) {
+		std::string name;
+		uint32_t idx;
+		if (!(in >> name >> idx))
+			return setError(kErrIo, "could not read wave name -> index map; stream seems truncated");
+		if (idx >= nw)
+			return setError(kErrIo, "wave index out of range in wave name -> index map");
+		names[idx] = name;
+		--mapSize;
+	}
+	I->nWaves = nw;
+	I->nEvents = ne;
+	I->sums = m;
+	I->names = names;
+	return kOk;
+}
+
+int pwa_integral_write_ascii(const pwa_integral* I, const char* path)
+{
+	if (!I || !path)
+		return setError(kErrArg, "null argument");
+	std::ofstream out(path);
+	if (!out)
+		return setError(kErrIo, std::string("cannot open file '") + path + "' for writing of integral matrix");
+	out << I->nWaves << "\n" << I->nEvents << "\n" << I->nWaves << " " << I->nWaves << "\n";
+	for (uint32_t i = 0; i < I->nWaves; ++i) {
+		for (uint32_t j = 0; j < I->nWaves; ++j) {
+			const cplx& v = I->sums[(size_t)i * I->nWaves + j];
+			out << "(" << fmtDouble(v.real()) << "," << fmtDouble(v.imag()) << ")\t";
+		}
+		out << "\n";
+	}
+	out << I->names.size() << "\n";
+	for (uint32_t i = 0; i < I->nWaves; ++i)
+		out << I->names[i] << " " << i << "\n";
+	return out.good() ? kOk : setError(kErrIo, "problems writing integral to ASCII file");
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// pwaLikelihood
+// ===========================================================================
+namespace {
+
+struct ParInfo {
+	std::string waveName;
+	int rank = 0;
+	double threshold = 0.;
+	bool fixed = false;
+	bool realPart = true;
+};
+
+struct CallInfo {
+	uint64_t nCalls = 0;
+	double total = 0., func = 0., norm = 0.;
+};
+
+double seconds()
+{
+	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct pwa_likelihood {
+	int device = 0, numSMs = 0;
+	size_t maxSmem = 0;
+	cudaStream_t stream = nullptr;
+	bool ownStream = false;
+	bool streamSet = false;  // the caller chose the stream (possibly the default stream)
+
+	bool useNormalizedAmps = true;
+	int priorType = PWA_PRIOR_FLAT;
+	double cauchyWidth = 0.5;
+	int reduction = PWA_REDUCE_FP64;
+
+	uint32_t nW[2] = {0, 0}, nWmax = 0, rank = 1;
+	std::vector<std::string> names[2];
+	std::vector<double> thres[2];
+	std::map<std::string, std::pair<uint32_t, uint32_t> > waveIdx;
+
+	uint32_t nPars = 0;
+	std::vector<ParInfo> pars;
+	std::vector<int> slotRe, slotIm;  // [rank][W], global wave order (negative first)
+
+	std::vector<cplx> normM, accM;  // [2][nWmax][2][nWmax]
+	uint64_t numbAccEvents = 0;
+	double totAcc = 0.;
+	std::vector<double> psInt;
+
+	uint64_t nEvents = 0, nPad = 0;
+	DevBuf amps;
+	std::vector<char> added[2];
+
+	bool initialized = false, normAdded = false, accAdded = false, finished = false;
+
+	// evaluation resources
+	FdfPlan plan;
+	int finBlocks = 0;
+	DevBuf dSlotRe, dSlotIm, dAccI, dPartials, dFinScratch, dTicket, dErr, dPar, dOut, dFlag;
+	PinnedBuf hPar, hOut;
+	cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
+	std::vector<double> parCache, derivCache;
+	bool cacheValid = false;
+	CallInfo info[5];
+
+	// per-evaluation kernel timing (pwa_likelihood_set_timing)
+	bool timing = false;
+	std::vector<cudaEvent_t> timingEvents;  // 3 per evaluation
+	size_t nTimed = 0;
+
+	uint32_t W() const { return nW[0] + nW[1]; }
+	uint32_t gw(uint32_t e, uint32_t w) const { return e == 0 ? w : nW[0] + w; }
+	size_t mIdx(uint32_t e1, uint32_t i, uint32_t e2, uint32_t j) const
+	{
+		return (((size_t)e1 * nWmax + i) * 2 + e2) * nWmax + j;
+	}
+
+	~pwa_likelihood()
+	{
+		for (auto& e : ev)
+			if (e)
+				cudaEventDestroy(e);
+		for (auto& e : timingEvents)
+			cudaEventDestroy(e);
+		if (ownStream && stream)
+			cudaStreamDestroy(stream);
+	}
+};
+
+namespace {
+
+int checkFinished(const pwa_likelihood* L)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (!L->finished)
+		return setError(kErrState, "pwaLikelihood::finishInit has not been called");
+	return kOk;
+}
+
+// Binds the handle to the current CUDA device on first device use (setup of
+// the wave set and parameter layout is pure host work).
+int ensureDevice(pwa_likelihood* L)
+{
+	if (L->numSMs > 0)
+		return kOk;
+	PWA_TRY(deviceInfo(&L->device, &L->numSMs, &L->maxSmem));
+	if (!L->streamSet) {
+		PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "stream create"));
+		L->ownStream = true;
+		L->streamSet = true;
+	}
+	for (auto& e : L->ev)
+		if (!e)
+			PWA_TRY(cudaCheck(cudaEventCreate(&e), "event create"));
+	return kOk;
+}
+
+// copyFromParArray (pwaLikelihood.cc:1682-1710), host FP64
+void fromPar(const pwa_likelihood* L, const double* par, std::vector<cplx>& V, double& flat)
+{
+	const uint32_t W = L->W();
+	V.assign((size_t)L->rank * W, cplx(0, 0));
+	for (uint32_t r = 0; r < L->rank; ++r)
+		for (uint32_t g = 0; g < W; ++g) {
+			const int ir = L->slotRe[r * W + g], ii = L->slotIm[r * W + g];
+			V[(size_t)r * W + g] = cplx(ir >= 0 ? par[ir] : 0., ii >= 0 ? par[ii] : 0.);
+		}
+	flat = par[L->nPars - 1];
+}
+
+// copyToParArray (pwaLikelihood.cc:1716-1731)
+void toPar(const pwa_likelihood* L, const std::vector<cplx>& V, double flat, double* out)
+{
+	const uint32_t W = L->W();
+	for (uint32_t r = 0; r < L->rank; ++r)
+		for (uint32_t g = 0; g < W; ++g) {
+			const int ir = L->slotRe[r * W + g], ii = L->slotIm[r * W + g];
+			if (ir >= 0)
+				out[ir] = V[(size_t)r * W + g].real();
+			if (ii >= 0)
+				out[ii] = V[(size_t)r * W + g].imag();
+		}
+	out[L->nPars - 1] = flat;
+}
+
+// Launches the fused event kernel and the finalize kernel: dPar -> dOut.
+int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad, cudaStream_t s,
+               cudaEvent_t between = nullptr)
+{
+	FdfArgs a{};
+	a.amps = L->amps.as<float2>();
+	a.nEvents = L->nEvents;
+	a.nPad = L->nPad;
+	a.W0 = (int)L->nW[0];
+	a.W = (int)L->W();
+	a.R = (int)L->rank;
+	a.P = (int)L->nPars;
+	a.par = dPar;
+	a.slotRe = L->dSlotRe.as<int>();
+	a.slotIm = L->dSlotIm.as<int>();
+	a.partials = L->dPartials.as<double>();
+	a.nPartial = 2 + 2 * a.R * a.W;
+	a.devErr = L->dErr.as<unsigned>();
+	a.withGrad = withGrad;
+	a.reduction = L->reduction;
+	cudaEvent_t* te = nullptr;
+	if (L->timing && 3 * (L->nTimed + 1) <= L->timingEvents.size()) {
+		te = &L->timingEvents[3 * L->nTimed];
+		++L->nTimed;
+		cudaEventRecord(te[0], s);
+	}
+	PWA_TRY(launchFdf(L->plan, a, s));
+	if (between)
+		cudaEventRecord(between, s);
+	if (te)
+		cudaEventRecord(te[1], s);
+	FinArgs f{};
+	f.partials = a.partials;
+	f.nBlocks = L->plan.blocks;
+	f.nPartial = a.nPartial;
+	f.par = dPar;
+	f.P = a.P;
+	f.W0 = a.W0;
+	f.W = a.W;
+	f.R = a.R;
+	f.slotRe = a.slotRe;
+	f.slotIm = a.slotIm;
+	f.accI = L->dAccI.as<double>();
+	f.nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
+	f.totAcc = L->totAcc;
+	f.prior = L->priorType;
+	f.cauchyWidth = L->cauchyWidth;
+	f.withGrad = withGrad;
+	f.scratch = L->dFinScratch.as<double>();
+	f.ticket = L->dTicket.as<unsigned>();
+	f.devErr = L->dErr.as<unsigned>();
+	f.out = dOut;
+	PWA_TRY(launchFinalize(f, L->finBlocks, s));
+	if (te)
+		cudaEventRecord(te[2], s);
+	return kOk;
+}
+
+// Host-buffer evaluation: par (host) -> f, grad (host).
+int hostEval(pwa_likelihood* L, const double* par, double* f, double* grad, int withGrad, int call)
+{
+	PWA_TRY(checkFinished(L));
+	const double t0 = seconds();
+	const uint32_t P = L->nPars;
+	std::memcpy(L->hPar.as<double>(), par, P * sizeof(double));
+	cudaStream_t s = L->stream;
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dPar.p, L->hPar.p, P * sizeof(double), cudaMemcpyHostToDevice, s), "H2D par"));
+	cudaEventRecord(L->ev[0], s);
+	PWA_TRY(launchEval(L, L->dPar.as<double>(), L->dOut.as<double>(), withGrad, s, L->ev[1]));
+	cudaEventRecord(L->ev[2], s);
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->hOut.p, L->dOut.p, (P + 2) * sizeof(double), cudaMemcpyDeviceToHost, s),
+	                  "D2H result"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "FdF sync"));
+	const double* out = L->hOut.as<double>();
+	if (out[P + 1] != 0.) {
+		cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s);
+		cudaStreamSynchronize(s);
+		return setError(kErrTimeout, "a bounded device-side wait expired in the FdF kernel");
+	}
+	if (f)
+		*f = out[0];
+	if (withGrad && grad)
+		std::memcpy(grad, out + 1, P * sizeof(double));
+	if (withGrad) {
+		L->parCache.assign(par, par + P);
+		L->derivCache.assign(out + 1, out + 1 + P);
+		L->cacheValid = true;
+	}
+	float ms1 = 0.f, ms2 = 0.f;
+	cudaEventElapsedTime(&ms1, L->ev[0], L->ev[1]);
+	cudaEventElapsedTime(&ms2, L->ev[1], L->ev[2]);
+	CallInfo& ci = L->info[call];
+	++ci.nCalls;
+	ci.func += ms1 * 1e-3;
+	ci.norm += ms2 * 1e-3;
+	ci.total += seconds() - t0;
+	return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pwa_likelihood_create(pwa_likelihood** out)
+{
+	if (!out)
+		return setError(kErrArg, "null output pointer");
+	try {
+		*out = new pwa_likelihood();
+	} catch (const std::bad_alloc&) {
+		return setError(kErrOom, "host allocation failed");
+	}
+	return kOk;
+}
+
+int pwa_likelihood_destroy(pwa_likelihood* L)
+{
+	if (L) {
+		if (L->stream)
+			cudaStreamSynchronize(L->stream);
+		delete L;
+	}
+	return kOk;
+}
+
+int pwa_likelihood_use_normalized_amps(pwa_likelihood* L, int flag)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	L->useNormalizedAmps = flag != 0;
+	return kOk;
+}
+
+int pwa_likelihood_set_prior_type(pwa_likelihood* L, int p)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (p != PWA_PRIOR_FLAT && p != PWA_PRIOR_HALF_CAUCHY)
+		return setError(kErrArg, "unknown prior type");
+	L->priorType = p;
+	return kOk;
+}
+
+int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double w)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	L->cauchyWidth = w;
+	return kOk;
+}
+
+int pwa_likelihood_set_stream(pwa_likelihood* L, void* s)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	L->streamSet = true;
+	if (L->ownStream && L->stream) {
+		cudaStreamSynchronize(L->stream);
+		cudaStreamDestroy(L->stream);
+	}
+	// NULL selects the CUDA default stream
+	L->ownStream = false;
+	L->stream = static_cast<cudaStream_t>(s);
+	return kOk;
+}
+
+int pwa_likelihood_set_reduction(pwa_likelihood* L, int r)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (r != PWA_REDUCE_FP64 && r != PWA_REDUCE_KAHAN_FP32)
+		return setError(kErrArg, "unknown reduction mode");
+	L->reduction = r;
+	return kOk;
+}
+
+// readWaveList + buildParDataStruct (pwaLikelihood.cc:1445-1556)
+int pwa_likelihood_init(pwa_likelihood* L, uint32_t n, const char* const* names, const int32_t* refl,
+                        const double* thresholds, uint32_t rank, double massBinCenter)
+{
+	if (!L || (!names && n) || (!refl && n))
+		return setError(kErrArg, "null argument");
+	if (L->initialized)
+		return setError(kErrState, "likelihood already initialized");
+	if (rank == 0)
+		return setError(kErrArg, "rank must be at least 1");
+	for (uint32_t i = 0; i < n; ++i) {
+		if (refl[i] != 1 && refl[i] != -1)
+			return setError(kErrArg, "reflectivity must be +1 or -1");
+		const uint32_t e = refl[i] > 0 ? 1 : 0;
+		if (L->waveIdx.count(names[i]))
+			return setError(kErrArg, std::string("duplicate wave '") + names[i] + "'");
+		L->waveIdx[names[i]] = std::make_pair(e, L->nW[e]);
+		++L->nW[e];
+		L->names[e].push_back(names[i]);
+		L->thres[e].push_back(thresholds ? thresholds[i] : 0.);
+	}
+	if (L->nW[0] + L->nW[1] == 0)
+		return setError(kErrArg, "no wave info");
+	L->nWmax = std::max(L->nW[0], L->nW[1]);
+	L->rank = rank;
+	L->added[0].assign(L->nWmax, 0);
+	L->added[1].assign(L->nWmax, 0);
+	uint32_t P = 0;
+	for (uint32_t r = 0; r < rank; ++r) {
+		const int pos = (int)L->nW[1] - (int)r, neg = (int)L->nW[0] - (int)r;
+		P += 2 * (std::max(pos - 1, 0) + std::max(neg - 1, 0));
+		if (pos > 0)
+			++P;
+		if (neg > 0)
+			++P;
+	}
+	P += 1;
+	L->nPars = P;
+	L->pars.assign(P, ParInfo());
+	const uint32_t W = L->W();
+	L->slotRe.assign((size_t)rank * W, -1);
+	L->slotIm.assign((size_t)rank * W, -1);
+	uint32_t p = 0;
+	for (uint32_t r = 0; r < rank; ++r)
+		for (uint32_t e = 0; e < 2; ++e)
+			for (uint32_t w = 0; w < L->nW[e]; ++w) {
+				const double th = L->thres[e][w];
+				const bool fixed = (th != 0 && th >= massBinCenter);
+				const size_t slot = (size_t)r * W + L->gw(e, w);
+				if (w < r)
+					continue;
+				ParInfo pi;
+				pi.waveName = L->names[e][w];
+				pi.rank = (int)r;
+				pi.threshold = th;
+				pi.fixed = fixed;
+				pi.realPart = true;
+				L->pars[p] = pi;
+				L->slotRe[slot] = (int)p;
+				if (w == r) {
+					p += 1;
+				} else {
+					pi.realPart = false;
+					L->pars[p + 1] = pi;
+					L->slotIm[slot] = (int)p + 1;
+					p += 2;
+				}
+			}
+	ParInfo flat;
+	flat.waveName = "flat";
+	L->pars[p] = flat;
+	L->initialized = true;
+	return kOk;
+}
+
+namespace {
+// reorderIntegralMatrix (pwaLikelihood.cc:1562-1576): same-reflectivity blocks only
+int reorder(const pwa_likelihood* L, const pwa_integral* I, std::vector<cplx>& out)
+{
+	out.assign((size_t)2 * L->nWmax * 2 * L->nWmax, cplx(0, 0));
+	for (uint32_t e = 0; e < 2; ++e)
+		for (uint32_t i = 0; i < L->nW[e]; ++i) {
+			const int a = I->index(L->names[e][i]);
+			if (a < 0)
+				return setError(kErrArg, "cannot find wave '" + L->names[e][i] + "' in integral matrix");
+			for (uint32_t j = 0; j < L->nW[e]; ++j) {
+				const int b = I->index(L->names[e][j]);
+				if (b < 0)
+					return setError(kErrArg, "cannot find wave '" + L->names[e][j] + "' in integral matrix");
+				out[L->mIdx(e, i, e, j)] = I->sums[(size_t)a * I->nWaves + b] / (double)I->nEvents;
+			}
+		}
+	return kOk;
+}
+}  // namespace
+
+int pwa_likelihood_add_norm_integral(pwa_likelihood* L, const pwa_integral* I)
+{
+	if (!L || !I)
+		return setError(kErrArg, "null argument");
+	if (!L->initialized)
+		return setError(kErrState, "likelihood not initialized; call init() before addNormIntegral()");
+	PWA_TRY(reorder(L, I, L->normM));
+	L->numbAccEvents = I->nEvents;
+	L->normAdded = true;
+	return kOk;
+}
+
+int pwa_likelihood_add_acc_integral(pwa_likelihood* L, pwa_integral* I, uint64_t accEventsOverride)
+{
+	if (!L || !I)
+		return setError(kErrArg, "null argument");
+	if (!L->normAdded)
+		return setError(kErrState,
+		                "normalization integral not added before acceptance integral; call addNormIntegral() first");
+	L->numbAccEvents = accEventsOverride == 0 ? L->numbAccEvents : accEventsOverride;
+	L->totAcc = (double)I->nEvents / (double)L->numbAccEvents;
+	I->nEvents = L->numbAccEvents;
+	PWA_TRY(reorder(L, I, L->accM));
+	L->accAdded = true;
+	return kOk;
+}
+
+int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const void* amps, uint64_t n, int ampType,
+                                 int memory)
+{
+	if (!L || !waveName || !amps)
+		return setError(kErrArg, "null argument");
+	if (!L->accAdded)
+		return setError(kErrState, "no acceptance integral found; call addAccIntegral() before addAmplitude()");
+	if (ampType != PWA_COMPLEX64 && ampType != PWA_COMPLEX128)
+		return setError(kErrArg, "unknown amplitude type");
+	if (memory != PWA_MEMORY_HOST && memory != PWA_MEMORY_DEVICE)
+		return setError(kErrArg, "unknown memory kind");
+	if (L->finished)
+		return setError(kErrState, "finishInit() already called");
+	auto it = L->waveIdx.find(waveName);
+	if (it == L->waveIdx.end())
+		return setError(kErrArg, std::string("requested to add decay amplitudes for wave '") + waveName +
+		                             "' which is not in wavelist");
+	if (n == 0)
+		return setError(kErrArg, "no events to load");
+	PWA_TRY(ensureDevice(L));
+	cudaStream_t s = L->stream;
+	if (L->nEvents == 0) {
+		L->nEvents = n;
+		L->nPad = (n + 127) / 128 * 128;
+		PWA_TRY(L->amps.alloc((size_t)L->W() * L->nPad * sizeof(float2), "amplitude store"));
+		PWA_TRY(cudaCheck(cudaMemsetAsync(L->amps.p, 0, L->amps.bytes, s), "amplitude store memset"));
+		PWA_TRY(L->dFlag.alloc(sizeof(unsigned), "flag"));
+	}
+	if (n != L->nEvents)
+		return setError(kErrArg, "size mismatch in amplitude arrays");
+	const uint32_t e = it->second.first, w = it->second.second;
+	const cplx normInt = L->normM[L->mIdx(e, w, e, w)];
+	bool fixPar = (L->accM[L->mIdx(e, w, e, w)] == 0.);
+	const double divisor = (L->useNormalizedAmps && normInt != 0.) ? std::sqrt(normInt.real()) : 1.;
+	float2* row = L->amps.as<float2>() + (size_t)L->gw(e, w) * L->nPad;
+	bool anyNonZero = false;
+	if (memory == PWA_MEMORY_HOST) {
+		// convert in FP64 on the host, upload through a pinned staging buffer
+		const size_t chunk = 1 << 20;
+		PinnedBuf stage;
+		PWA_TRY(stage.ensure(chunk * sizeof(float2), "staging"));
+		for (uint64_t b = 0; b < n; b += chunk) {
+			const uint64_t m = std::min<uint64_t>(chunk, n - b);
+			float2* dst = stage.as<float2>();
+			for (uint64_t i = 0; i < m; ++i) {
+				double re, im;
+				if (ampType == PWA_COMPLEX128) {
+					re = static_cast<const double*>(amps)[2 * (b + i)];
+					im = static_cast<const double*>(amps)[2 * (b + i) + 1];
+				} else {
+					re = static_cast<const float*>(amps)[2 * (b + i)];
+					im = static_cast<const float*>(amps)[2 * (b + i) + 1];
+				}
+				anyNonZero = anyNonZero || re != 0. || im != 0.;
+				dst[i] = make_float2((float)(re / divisor), (float)(im / divisor));
+			}
+			PWA_TRY(cudaCheck(cudaMemcpyAsync(row + b, dst, m * sizeof(float2), cudaMemcpyHostToDevice, s),
+			                  "amplitude upload"));
+			PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "amplitude upload sync"));
+		}
+	} else {
+		// the caller's streams may still be writing the device amplitudes
+		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device amplitudes"));
+		PWA_TRY(cudaCheck(cudaMemsetAsync(L->dFlag.p, 0, sizeof(unsigned), s), "memset"));
+		PWA_TRY(launchConvertRow(amps, ampType == PWA_COMPLEX128 ? 1 : 0, row, n, divisor, L->dFlag.as<unsigned>(), s));
+		unsigned flag = 0;
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(&flag, L->dFlag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "flag"));
+		PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "amplitude convert sync"));
+		anyNonZero = flag != 0;
+	}
+	if (L->useNormalizedAmps && normInt == 0. && anyNonZero)
+		return setError(kErrArg, std::string("normalization integral for wave '") + waveName +
+		                             "' is zero, but the amplitude is not");
+	if (anyNonZero)
+		fixPar = false;
+	if (fixPar)
+		for (auto& p : L->pars)
+			if (p.waveName == waveName)
+				p.fixed = true;
+	L->added[e][w] = 1;
+	return kOk;
+}
+
+int pwa_likelihood_finish_init(pwa_likelihood* L)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (!L->accAdded)
+		return setError(kErrState, "integrals not added");
+	for (uint32_t e = 0; e < 2; ++e)
+		for (uint32_t w = 0; w < L->nW[e]; ++w)
+			if (!L->added[e][w])
+				return setError(kErrState, "not all expected amplitudes were added to the likelihood ('" +
+				                               L->names[e][w] + "')");
+	// phase-space integrals and rescaling (pwaLikelihood.cc:1303-1335)
+	L->psInt.assign((size_t)2 * L->nWmax, 0.);
+	for (uint32_t e = 0; e < 2; ++e)
+		for (uint32_t w = 0; w < L->nW[e]; ++w)
+			L->psInt[e * L->nWmax + w] = std::sqrt(L->normM[L->mIdx(e, w, e, w)].real());
+	if (L->useNormalizedAmps) {
+		for (uint32_t e1 = 0; e1 < 2; ++e1)
+			for (uint32_t i = 0; i < L->nW[e1]; ++i) {
+				double ni = std::sqrt(L->normM[L->mIdx(e1, i, e1, i)].real());
+				if (ni == 0)
+					ni = 1;
+				for (uint32_t e2 = 0; e2 < 2; ++e2)
+					for (uint32_t j = 0; j < L->nW[e2]; ++j) {
+						double nj = std::sqrt(L->normM[L->mIdx(e2, j, e2, j)].real());
+						if (nj == 0)
+							nj = 1;
+						if (e1 != e2 || i != j)
+							L->normM[L->mIdx(e1, i, e2, j)] /= ni * nj;
+						L->accM[L->mIdx(e1, i, e2, j)] /= ni * nj;
+					}
+			}
+		for (uint32_t e = 0; e < 2; ++e)
+			for (uint32_t w = 0; w < L->nW[e]; ++w)
+				if (L->normM[L->mIdx(e, w, e, w)] != 0.)
+					L->normM[L->mIdx(e, w, e, w)] = 1.;
+	}
+	// device-side evaluation resources
+	PWA_TRY(ensureDevice(L));
+	const uint32_t W = L->W();
+	PWA_TRY(planFdf((int)W, (int)L->rank, L->nEvents, L->numSMs, L->maxSmem, &L->plan));
+	L->finBlocks = finalizeBlocks((int)L->rank, (int)W);
+	const size_t nSlot = (size_t)L->rank * W;
+	const size_t nPartial = 2 + 2 * nSlot;
+	PWA_TRY(L->dSlotRe.alloc(nSlot * sizeof(int), "slot map"));
+	PWA_TRY(L->dSlotIm.alloc(nSlot * sizeof(int), "slot map"));
+	PWA_TRY(L->dPartials.alloc((size_t)L->plan.blocks * nPartial * sizeof(double), "partials"));
+	PWA_TRY(L->dFinScratch.alloc((size_t)(2 * L->finBlocks + 2) * sizeof(double), "finalize scratch"));
+	PWA_TRY(L->dTicket.alloc(sizeof(unsigned), "ticket"));
+	PWA_TRY(L->dErr.alloc(sizeof(unsigned), "error flag"));
+	PWA_TRY(L->dPar.alloc(L->nPars * sizeof(double), "parameters"));
+	PWA_TRY(L->dOut.alloc((L->nPars + 2) * sizeof(double), "result"));
+	PWA_TRY(L->hPar.ensure(L->nPars * sizeof(double), "pinned parameters"));
+	PWA_TRY(L->hOut.ensure((L->nPars + 2) * sizeof(double), "pinned result"));
+	std::vector<double> accI;
+	for (uint32_t e = 0; e < 2; ++e)
+		for (uint32_t i = 0; i < L->nW[e]; ++i)
+			for (uint32_t j = 0; j < L->nW[e]; ++j) {
+				const cplx v = L->accM[L->mIdx(e, i, e, j)];
+				accI.push_back(v.real());
+				accI.push_back(v.imag());
+			}
+	PWA_TRY(L->dAccI.alloc(std::max<size_t>(accI.size(), 2) * sizeof(double), "acceptance integral"));
+	cudaStream_t s = L->stream;
+	if (!accI.empty())
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dAccI.p, accI.data(), accI.size() * sizeof(double),
+		                                  cudaMemcpyHostToDevice, s),
+		                  "acc upload"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dSlotRe.p, L->slotRe.data(), nSlot * sizeof(int), cudaMemcpyHostToDevice, s),
+	                  "slot upload"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dSlotIm.p, L->slotIm.data(), nSlot * sizeof(int), cudaMemcpyHostToDevice, s),
+	                  "slot upload"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dTicket.p, 0, sizeof(unsigned), s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s), "memset"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "finishInit sync"));
+	L->finished = true;
+	return kOk;
+}
+
+int pwa_likelihood_nmb_pars(const pwa_likelihood* L, uint32_t* n)
+{
+	if (!L || !n)
+		return setError(kErrArg, "null argument");
+	*n = L->nPars;
+	return kOk;
+}
+
+int pwa_likelihood_nmb_pars_fixed(const pwa_likelihood* L, uint32_t* n)
+{
+	if (!L || !n)
+		return setError(kErrArg, "null argument");
+	uint32_t k = 0;
+	for (const auto& p : L->pars)
+		k += p.fixed ? 1 : 0;
+	*n = k;
+	return kOk;
+}
+
+int pwa_likelihood_nmb_events(const pwa_likelihood* L, uint64_t* n)
+{
+	if (!L || !n)
+		return setError(kErrArg, "null argument");
+	*n = L->nEvents;
+	return kOk;
+}
+
+int pwa_likelihood_rank(const pwa_likelihood* L, uint32_t* r)
+{
+	if (!L || !r)
+		return setError(kErrArg, "null argument");
+	*r = L->rank;
+	return kOk;
+}
+
+int pwa_likelihood_nmb_waves(const pwa_likelihood* L, int refl, uint32_t* n)
+{
+	if (!L || !n)
+		return setError(kErrArg, "null argument");
+	*n = (refl == 0) ? L->W() : (refl > 0 ? L->nW[1] : L->nW[0]);
+	return kOk;
+}
+
+int pwa_likelihood_parameter(const pwa_likelihood* L, uint32_t i, char* nameBuf, uint32_t bufLen, int* fixed,
+                             int* realPart, int32_t* rank, double* threshold)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (i >= L->nPars)
+		return setError(kErrArg, "parameter index out of range");
+	const ParInfo& p = L->pars[i];
+	if (nameBuf && bufLen) {
+		// fitParameter::parName (pwaLikelihood.cc:107-122)
+		std::ostringstream o;
+		o << "V";
+		if (p.waveName != "flat")
+			o << p.rank;
+		o << "_" << p.waveName << (p.realPart ? "_RE" : "_IM");
+		std::snprintf(nameBuf, bufLen, "%s", o.str().c_str());
+	}
+	if (fixed)
+		*fixed = p.fixed ? 1 : 0;
+	if (realPart)
+		*realPart = p.realPart ? 1 : 0;
+	if (rank)
+		*rank = p.rank;
+	if (threshold)
+		*threshold = p.threshold;
+	return kOk;
+}
+
+int pwa_likelihood_tot_acc(const pwa_likelihood* L, double* t)
+{
+	if (!L || !t)
+		return setError(kErrArg, "null argument");
+	*t = L->totAcc;
+	return kOk;
+}
+
+int pwa_likelihood_fdf(pwa_likelihood* L, const double* par, double* f, double* grad)
+{
+	if (!par || !f || !grad)
+		return setError(kErrArg, "null argument");
+	return hostEval(L, par, f, grad, 1, PWA_CALL_FDF);
+}
+
+int pwa_likelihood_doeval(pwa_likelihood* L, const double* par, double* f)
+{
+	if (!par || !f)
+		return setError(kErrArg, "null argument");
+	return hostEval(L, par, f, nullptr, 0, PWA_CALL_DOEVAL);
+}
+
+int pwa_likelihood_gradient(pwa_likelihood* L, const double* par, double* grad)
+{
+	if (!par || !grad)
+		return setError(kErrArg, "null argument");
+	return hostEval(L, par, nullptr, grad, 1, PWA_CALL_GRADIENT);
+}
+
+int pwa_likelihood_doderivative(pwa_likelihood* L, const double* par, uint32_t index, double* d)
+{
+	PWA_TRY(checkFinished(L));
+	if (!par || !d)
+		return setError(kErrArg, "null argument");
+	if (index >= L->nPars)
+		return setError(kErrArg, "derivative index out of range");
+	++L->info[PWA_CALL_DODERIVATIVE].nCalls;
+	if (L->cacheValid && std::equal(par, par + L->nPars, L->parCache.begin())) {
+		*d = L->derivCache[index];
+		return kOk;
+	}
+	std::vector<double> g(L->nPars);
+	double f;
+	PWA_TRY(hostEval(L, par, &f, g.data(), 1, PWA_CALL_FDF));
+	*d = g[index];
+	return kOk;
+}
+
+int pwa_likelihood_fdf_batch(pwa_likelihood* L, uint32_t nPoints, const double* par, double* f, double* grad)
+{
+	PWA_TRY(checkFinished(L));
+	if (!par || !f || !grad)
+		return setError(kErrArg, "null argument");
+	if (nPoints == 0)
+		return kOk;
+	const uint32_t P = L->nPars;
+	const double t0 = seconds();
+	PWA_TRY(L->dPar.ensure((size_t)nPoints * P * sizeof(double), "batch parameters"));
+	PWA_TRY(L->dOut.ensure((size_t)nPoints * (P + 2) * sizeof(double), "batch results"));
+	PWA_TRY(L->hPar.ensure((size_t)nPoints * P * sizeof(double), "pinned batch parameters"));
+	PWA_TRY(L->hOut.ensure((size_t)nPoints * (P + 2) * sizeof(double), "pinned batch results"));
+	std::memcpy(L->hPar.p, par, (size_t)nPoints * P * sizeof(double));
+	cudaStream_t s = L->stream;
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dPar.p, L->hPar.p, (size_t)nPoints * P * sizeof(double),
+	                                  cudaMemcpyHostToDevice, s),
+	                  "H2D batch"));
+	for (uint32_t k = 0; k < nPoints; ++k)
+		PWA_TRY(launchEval(L, L->dPar.as<double>() + (size_t)k * P, L->dOut.as<double>() + (size_t)k * (P + 2), 1, s));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->hOut.p, L->dOut.p, (size_t)nPoints * (P + 2) * sizeof(double),
+	                                  cudaMemcpyDeviceToHost, s),
+	                  "D2H batch"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "batch sync"));
+	const double* out = L->hOut.as<double>();
+	for (uint32_t k = 0; k < nPoints; ++k) {
+		if (out[(size_t)k * (P + 2) + P + 1] != 0.) {
+			cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s);
+			cudaStreamSynchronize(s);
+			return setError(kErrTimeout, "a bounded device-side wait expired in the FdF kernel");
+		}
+		f[k] = out[(size_t)k * (P + 2)];
+		std::memcpy(grad + (size_t)k * P, out + (size_t)k * (P + 2) + 1, P * sizeof(double));
+	}
+	CallInfo& ci = L->info[PWA_CALL_FDF];
+	ci.nCalls += nPoints;
+	ci.total += seconds() - t0;
+	return kOk;
+}
+
+int pwa_likelihood_fdf_device(pwa_likelihood* L, const double* dPar, double* dOut, int withGradient, void* stream)
+{
+	PWA_TRY(checkFinished(L));
+	if (!dPar || !dOut)
+		return setError(kErrArg, "null argument");
+	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : L->stream;
+	return launchEval(L, dPar, dOut, withGradient ? 1 : 0, s);
+}
+
+int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* H)
+{
+	PWA_TRY(checkFinished(L));
+	if (!par || !H)
+		return setError(kErrArg, "null argument");
+	const double t0 = seconds();
+	const uint32_t P = L->nPars, W = L->W(), R = L->rank;
+	const uint32_t nS = R * W, nY1 = 2 * nS + 1, nY2 = W + 1;
+	cudaStream_t s = L->stream;
+	// event slabs sized so that the [d; conj d; 1] columns stay below ~1 GB
+	uint64_t slab = (uint64_t)1 << 30;
+	slab /= (uint64_t)nY1 * sizeof(float2);
+	slab = std::max<uint64_t>(1024, std::min<uint64_t>(slab, (L->nEvents + 63) / 64 * 64));
+	const int tps = ((int)nY1 + 63) / 64;
+	const int nTiles = tps * (tps + 1) / 2;
+	int chunks = std::max(1, (4 * L->numSMs + nTiles - 1) / nTiles);
+	chunks = (int)std::min<uint64_t>((uint64_t)chunks, std::max<uint64_t>(1, slab / 64));
+	DevBuf dY1, dY2, dW1, dW2, dPart, dG1, dG2, dHP;
+	PWA_TRY(dY1.alloc((size_t)nY1 * slab * sizeof(float2), "hessian operand"));
+	PWA_TRY(dY2.alloc((size_t)nY2 * slab * sizeof(float2), "hessian operand"));
+	PWA_TRY(dW1.alloc(slab * sizeof(double), "hessian weights"));
+	PWA_TRY(dW2.alloc(slab * sizeof(double), "hessian weights"));
+	PWA_TRY(dPart.alloc((size_t)chunks * nY1 * nY1 * 2 * sizeof(double), "hessian partials"));
+	PWA_TRY(dG1.alloc((size_t)nY1 * nY1 * 2 * sizeof(double), "hessian gram"));
+	PWA_TRY(dG2.alloc((size_t)nY2 * nY2 * 2 * sizeof(double), "hessian gram"));
+	PWA_TRY(dHP.alloc(P * sizeof(double), "hessian parameters"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(dHP.p, par, P * sizeof(double), cudaMemcpyHostToDevice, s), "H2D par"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(dG1.p, 0, dG1.bytes, s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(dG2.p, 0, dG2.bytes, s), "memset"));
+	for (uint64_t e0 = 0; e0 < L->nEvents; e0 += slab) {
+		const uint64_t K = std::min<uint64_t>(slab, L->nEvents - e0);
+		PWA_TRY(launchHessPrep(L->amps.as<float2>(), L->nEvents, L->nPad, e0, slab, (int)L->nW[0], (int)W, (int)R,
+		                       (int)P, dHP.as<double>(), L->dSlotRe.as<int>(), L->dSlotIm.as<int>(), dY1.as<float2>(),
+		                       dY2.as<float2>(), dW1.as<double>(), dW2.as<double>(), s));
+		const int ck = (int)std::min<uint64_t>((uint64_t)chunks, std::max<uint64_t>(1, K / 64));
+		GramArgs g{};
+		g.K = K;
+		g.ldK = slab;
+		g.partials = dPart.as<double>();
+		g.chunks = ck;
+		g.amps = dY1.as<float2>();
+		g.W = (int)nY1;
+		g.weightK = dW1.as<double>();
+		PWA_TRY(launchGramSimt(g, PWA_PRECISION_FP32, s));
+		PWA_TRY(launchGramReduce(g.partials, ck, (int)nY1, dG1.as<double>(), 1, s));
+		g.amps = dY2.as<float2>();
+		g.W = (int)nY2;
+		g.weightK = dW2.as<double>();
+		PWA_TRY(launchGramSimt(g, PWA_PRECISION_FP32, s));
+		PWA_TRY(launchGramReduce(g.partials, ck, (int)nY2, dG2.as<double>(), 1, s));
+	}
+	std::vector<double> G1((size_t)nY1 * nY1 * 2), G2((size_t)nY2 * nY2 * 2);
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(G1.data(), dG1.p, G1.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(G2.data(), dG2.p, G2.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "hessian sync"));
+	auto g1 = [&](uint32_t a, uint32_t b) { return cplx(G1[((size_t)a * nY1 + b) * 2], G1[((size_t)a * nY1 + b) * 2 + 1]); };
+	auto g2 = [&](uint32_t a, uint32_t b) { return cplx(G2[((size_t)a * nY2 + b) * 2], G2[((size_t)a * nY2 + b) * 2 + 1]); };
+
+	// assemble the reference's [slot][slot][3] blocks (pwaLikelihood.cc:736-800)
+	std::vector<cplx> V;
+	double flat;
+	fromPar(L, par, V, flat);
+	const double nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
+	const double twice = 2. * nEvt;
+	std::vector<double> h((size_t)nS * nS * 3);
+	for (uint32_t si = 0; si < nS; ++si) {
+		const uint32_t ri = si / W, gi = si % W, ei = gi < L->nW[0] ? 0 : 1;
+		for (uint32_t sj = 0; sj < nS; ++sj) {
+			const uint32_t rj = sj / W, gj = sj % W, ej = gj < L->nW[0] ? 0 : 1;
+			const cplx Gd = g1(si, sj), Gn = g1(si, nS + sj);
+			double h0 = 0.5 * (Gd.real() + Gn.real());
+			double h1 = 0.5 * (Gn.imag() - Gd.imag());
+			double h2 = 0.5 * (Gd.real() - Gn.real());
+			if (ri == rj && ei == ej) {
+				const cplx M = g2(gi, gj);
+				const uint32_t li = gi - (ei ? L->nW[0] : 0), lj = gj - (ej ? L->nW[0] : 0);
+				const cplx I = L->accM[L->mIdx(ei, li, ei, lj)];
+				h0 += -M.real() + I.real() * twice;
+				h1 += -M.imag() + I.imag() * twice;
+				h2 += -M.real() + I.real() * twice;
+			}
+			double* hh = &h[((size_t)si * nS + sj) * 3];
+			hh[0] = h0;
+			hh[1] = h1;
+			hh[2] = h2;
+		}
+	}
+	std::vector<cplx> flatTerms(nS);
+	for (uint32_t si = 0; si < nS; ++si)
+		flatTerms[si] = flat * g1(si, 2 * nS);
+	double hFlat = flat * flat * g1(2 * nS, 2 * nS).real() - g2(W, W).real() + twice * L->totAcc;
+	if (L->priorType == PWA_PRIOR_HALF_CAUCHY) {
+		// pwaLikelihood.cc:766-798
+		const double gw = L->cauchyWidth, g2w = gw * gw;
+		for (uint32_t si = 0; si < nS; ++si) {
+			const cplx v = V[si];
+			const double rr = std::abs(v);
+			const double cf = 1. / (1. + (rr * rr) / g2w);
+			const double cd = (-2. * rr * g2w) / ((g2w + rr * rr) * (g2w + rr * rr));
+			const double cd2 = g2w / ((g2w + rr * rr) * (g2w + rr * rr)) * (-2. + 8. * rr * rr / (g2w + rr * rr));
+			const double a1 = cd2 / (cf * rr * rr);
+			const double a2 = cd * cd / (cf * cf * rr * rr);
+			const double a3 = cd / (cf * rr);
+			const double a4 = cd / (cf * rr * rr * rr);
+			const double a124 = a1 - a2 - a4;
+			double* hh = &h[((size_t)si * nS + si) * 3];
+			hh[0] -= a124 * v.real() * v.real() + a3;
+			hh[1] -= a124 * v.real() * v.imag();
+			hh[2] -= a124 * v.imag() * v.imag() + a3;
+		}
+	}
+	// map onto the parameter layout (pwaLikelihood.cc:802-850)
+	std::fill(H, H + (size_t)P * P, 0.);
+	for (uint32_t si = 0; si < nS; ++si) {
+		const int r1 = L->slotRe[si], i1 = L->slotIm[si];
+		if (r1 < 0 || L->pars[r1].fixed)
+			continue;
+		for (uint32_t sj = 0; sj < nS; ++sj) {
+			const int r2 = L->slotRe[sj], i2 = L->slotIm[sj];
+			if (r2 < 0 || L->pars[r2].fixed)
+				continue;
+			H[(size_t)r1 * P + r2] = h[((size_t)si * nS + sj) * 3 + 0];
+			if (i2 >= 0)
+				H[(size_t)r1 * P + i2] = h[((size_t)si * nS + sj) * 3 + 1];
+			if (i1 >= 0)
+				H[(size_t)i1 * P + r2] = h[((size_t)sj * nS + si) * 3 + 1];
+			if (i1 >= 0 && i2 >= 0)
+				H[(size_t)i1 * P + i2] = h[((size_t)si * nS + sj) * 3 + 2];
+		}
+		H[(size_t)r1 * P + P - 1] = flatTerms[si].real();
+		H[(size_t)(P - 1) * P + r1] = flatTerms[si].real();
+		if (i1 >= 0) {
+			H[(size_t)i1 * P + P - 1] = flatTerms[si].imag();
+			H[(size_t)(P - 1) * P + i1] = flatTerms[si].imag();
+		}
+	}
+	H[(size_t)(P - 1) * P + P - 1] = hFlat;
+	CallInfo& ci = L->info[PWA_CALL_HESSIAN];
+	++ci.nCalls;
+	ci.total += seconds() - t0;
+	return kOk;
+}
+
+int pwa_likelihood_covariance_matrix(const pwa_likelihood* L, const double* H, double* C)
+{
+	PWA_TRY(checkFinished(L));
+	if (!H || !C)
+		return setError(kErrArg, "null argument");
+	// invert the free-parameter block (pwaLikelihood.cc:929-981); Gauss-Jordan
+	// with partial pivoting in FP64 on the host (P x P, once per fit)
+	const uint32_t P = L->nPars;
+	std::vector<uint32_t> fr;
+	for (uint32_t i = 0; i < P; ++i)
+		if (!L->pars[i].fixed)
+			fr.push_back(i);
+	const size_t n = fr.size();
+	std::vector<double> a(n * n), inv(n * n, 0.);
+	for (size_t i = 0; i < n; ++i) {
+		for (size_t j = 0; j < n; ++j)
+			a[i * n + j] = H[(size_t)fr[i] * P + fr[j]];
+		inv[i * n + i] = 1.;
+	}
+	for (size_t c = 0; c < n; ++c) {
+		size_t piv = c;
+		for (size_t r = c + 1; r < n; ++r)
+			if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c]))
+				piv = r;
+		if (a[piv * n + c] == 0.)
+			return setError(kErrNumerical, "Hessian is singular");
+		if (piv != c)
+			for (size_t k = 0; k < n; ++k) {
+				std::swap(a[c * n + k], a[piv * n + k]);
+				std::swap(inv[c * n + k], inv[piv * n + k]);
+			}
+		const double d = a[c * n + c];
+		for (size_t k = 0; k < n; ++k) {
+			a[c * n + k] /= d;
+			inv[c * n + k] /= d;
+		}
+		for (size_t r = 0; r < n; ++r) {
+			if (r == c)
+				continue;
+			const double fct = a[r * n + c];
+			if (fct == 0.)
+				continue;
+			for (size_t k = 0; k < n; ++k) {
+				a[r * n + k] -= fct * a[c * n + k];
+				inv[r * n + k] -= fct * inv[c * n + k];
+			}
+		}
+	}
+	std::fill(C, C + (size_t)P * P, 0.);
+	for (size_t i = 0; i < n; ++i)
+		for (size_t j = 0; j < n; ++j)
+			C[(size_t)fr[i] * P + fr[j]] = inv[i * n + j];
+	return kOk;
+}
+
+int pwa_likelihood_correct_param_signs(const pwa_likelihood* L, const double* par, double* out)
+{
+	if (!L || !par || !out)
+		return setError(kErrArg, "null argument");
+	if (!L->initialized)
+		return setError(kErrState, "likelihood not initialized");
+	// pwaLikelihood.cc:986-1010
+	std::vector<cplx> V;
+	double flat;
+	fromPar(L, par, V, flat);
+	if (flat < 0)
+		flat *= -1;
+	const uint32_t W = L->W();
+	for (uint32_t r = 0; r < L->rank; ++r)
+		for (uint32_t e = 0; e < 2; ++e) {
+			if (r >= L->nW[e])
+				continue;  // anchor wave absent in this reflectivity: V == 0, nothing to flip
+			const cplx anchor = V[(size_t)r * W + L->gw(e, r)];
+			if (anchor.real() < 0 && anchor.imag() == 0)
+				for (uint32_t w = 0; w < L->nW[e]; ++w)
+					V[(size_t)r * W + L->gw(e, w)] *= -1;
+		}
+	toPar(L, V, flat, out);
+	return kOk;
+}
+
+int pwa_likelihood_integral_matrices(const pwa_likelihood* L, double* norm, double* acc, double* ps, int withFlat)
+{
+	PWA_TRY(checkFinished(L));
+	if (!norm || !acc || !ps)
+		return setError(kErrArg, "null argument");
+	const uint32_t n = L->W(), sz = n + (withFlat ? 1 : 0);
+	std::fill(norm, norm + 2 * (size_t)sz * sz, 0.);
+	std::fill(acc, acc + 2 * (size_t)sz * sz, 0.);
+	std::fill(ps, ps + sz, 0.);
+	uint32_t ii = 0;
+	for (uint32_t e1 = 0; e1 < 2; ++e1)
+		for (uint32_t i = 0; i < L->nW[e1]; ++i, ++ii) {
+			ps[ii] = L->psInt[e1 * L->nWmax + i];
+			uint32_t jj = 0;
+			for (uint32_t e2 = 0; e2 < 2; ++e2)
+				for (uint32_t j = 0; j < L->nW[e2]; ++j, ++jj) {
+					const cplx nv = L->normM[L->mIdx(e1, i, e2, j)], av = L->accM[L->mIdx(e1, i, e2, j)];
+					norm[2 * ((size_t)ii * sz + jj)] = nv.real();
+					norm[2 * ((size_t)ii * sz + jj) + 1] = nv.imag();
+					acc[2 * ((size_t)ii * sz + jj)] = av.real();
+					acc[2 * ((size_t)ii * sz + jj) + 1] = av.imag();
+				}
+		}
+	if (withFlat) {
+		norm[2 * ((size_t)n * sz + n)] = 1.;
+		acc[2 * ((size_t)n * sz + n)] = L->totAcc;
+		ps[n] = 1.;
+	}
+	return kOk;
+}
+
+int pwa_likelihood_build_prod_amp_arrays(const pwa_likelihood* L, const double* par, double* prodAmps,
+                                         int32_t* parIndices, uint32_t* nAmps, int withFlat)
+{
+	if (!L || !par || !prodAmps || !parIndices || !nAmps)
+		return setError(kErrArg, "null argument");
+	if (!L->initialized)
+		return setError(kErrState, "likelihood not initialized");
+	// pwaLikelihood.cc:1626-1665
+	uint32_t p = 0, k = 0;
+	for (uint32_t r = 0; r < L->rank; ++r)
+		for (uint32_t e = 0; e < 2; ++e)
+			for (uint32_t w = 0; w < L->nW[e]; ++w) {
+				if (w < r)
+					continue;
+				double re, im;
+				if (w == r) {
+					parIndices[2 * k] = (int32_t)p;
+					parIndices[2 * k + 1] = -1;
+					re = par[p];
+					im = 0;
+					p += 1;
+				} else {
+					parIndices[2 * k] = (int32_t)p;
+					parIndices[2 * k + 1] = (int32_t)p + 1;
+					re = par[p];
+					im = par[p + 1];
+					p += 2;
+				}
+				prodAmps[2 * k] = re;
+				prodAmps[2 * k + 1] = im;
+				++k;
+			}
+	if (withFlat) {
+		prodAmps[2 * k] = par[p];
+		prodAmps[2 * k + 1] = 0.;
+		parIndices[2 * k] = (int32_t)p;
+		parIndices[2 * k + 1] = -1;
+		++k;
+	}
+	*nAmps = k;
+	return kOk;
+}
+
+int pwa_likelihood_func_call_info(const pwa_likelihood* L, int call, uint64_t* nCalls, double* total, double* func,
+                                  double* norm)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (call < 0 || call > PWA_CALL_HESSIAN)
+		return setError(kErrArg, "unknown call type");
+	const CallInfo& c = L->info[call];
+	if (nCalls)
+		*nCalls = c.nCalls;
+	if (total)
+		*total = c.total;
+	if (func)
+		*func = c.func;
+	if (norm)
+		*norm = c.norm;
+	return kOk;
+}
+
+int pwa_likelihood_set_timing(pwa_likelihood* L, int enable)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (enable && L->timingEvents.empty()) {
+		PWA_TRY(ensureDevice(L));
+		const size_t n = 3 * 65536;
+		L->timingEvents.resize(n, nullptr);
+		for (auto& e : L->timingEvents)
+			PWA_TRY(cudaCheck(cudaEventCreate(&e), "timing event create"));
+	}
+	L->timing = enable != 0;
+	L->nTimed = 0;
+	return kOk;
+}
+
+int pwa_likelihood_kernel_times(pwa_likelihood* L, double* mainMs, double* finMs, uint64_t* nTimed)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	double a = 0., b = 0.;
+	if (L->nTimed > 0)
+		PWA_TRY(cudaCheck(cudaEventSynchronize(L->timingEvents[3 * L->nTimed - 1]), "timing sync"));
+	for (size_t k = 0; k < L->nTimed; ++k) {
+		float x = 0.f, y = 0.f;
+		PWA_TRY(cudaCheck(cudaEventElapsedTime(&x, L->timingEvents[3 * k], L->timingEvents[3 * k + 1]), "elapsed"));
+		PWA_TRY(cudaCheck(cudaEventElapsedTime(&y, L->timingEvents[3 * k + 1], L->timingEvents[3 * k + 2]), "elapsed"));
+		a += x;
+		b += y;
+	}
+	if (mainMs)
+		*mainMs = a;
+	if (finMs)
+		*finMs = b;
+	if (nTimed)
+		*nTimed = L->nTimed;
+	L->nTimed = 0;
+	return kOk;
+}
+
+int pwa_likelihood_reset_func_call_info(pwa_likelihood* L)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	for (auto& c : L->info)
+		c = CallInfo();
+	return kOk;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// pwa_internal.h -- declarations shared by the host library and the CUDA
+// kernels of the GB300 extended-likelihood engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+namespace pwa {
+
+// status codes (same values as enum pwa_status in include/pwa_gb300.h)
+enum {
+	kOk = 0,
+	kErrArg = 1,
+	kErrState = 2,
+	kErrCuda = 3,
+	kErrOom = 4,
+	kErrTimeout = 5,
+	kErrIo = 6,
+	kErrUnsupported = 7,
+	kErrNumerical = 8
+};
+
+// records the calling thread's last error; returns code
+int setError(int code, const std::string& msg);
+// checks a CUDA runtime result; records and returns kErrCuda on failure
+int cudaCheck(cudaError_t e, const char* what);
+// counts kernel launches (reported through pwa_kernel_launch_count)
+void countLaunches(uint64_t n);
+
+// Device-side error flags written by bounded waits.
+enum { kDevErrTimeout = 1 };
+
+// ---------------------------------------------------------------------------
+// Fused FdF / DoEval
+// ---------------------------------------------------------------------------
+// Amplitude store: complex64 structure-of-arrays [wave][nPad]; waves of
+// negative reflectivity first (W0 of them), then positive; rows zero-padded
+// to nPad (a multiple of 128 events).
+struct FdfPlan {
+	int E = 128;        // events per tile
+	int stages = 2;     // shared-memory pipeline depth
+	int wpw = 2;        // wave bucket per warp (template)
+	int blocks = 0;     // grid size (persistent, <= #SMs)
+	size_t smemBytes = 0;
+};
+
+struct FdfArgs {
+	const float2* amps;
+	uint64_t nEvents;
+	uint64_t nPad;
+	int W0, W, R, P;
+	const double* par;       // device, [P]
+	const int* slotRe;       // device, [R*W] parameter index of Re(V_rw) or -1
+	const int* slotIm;       // device, [R*W] parameter index of Im(V_rw) or -1
+	double* partials;        // device, [blocks][nPartial]
+	int nPartial;            // 2 + 2*R*W
+	unsigned* devErr;        // device error flags
+	int withGrad;
+	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32
+};
+
+struct FinArgs {
+	const double* partials;
+	int nBlocks, nPartial;
+	const double* par;
+	int P, W0, W, R;
+	const int* slotRe;
+	const int* slotIm;
+	const double* accI;      // device, per reflectivity e: W_e x W_e complex128 (re, im) row-major, e=0 block first
+	double nEvt, totAcc;
+	int prior;
+	double cauchyWidth;
+	int withGrad;
+	double* scratch;         // device, [2*gridDim + 2]
+	unsigned* ticket;        // device counter, zero between launches
+	const unsigned* devErr;  // device error flags of the main kernel
+	double* out;             // device, [P + 2]: f, gradient, device error status
+};
+
+// Chooses tile size, pipeline depth and grid; returns kErrUnsupported for
+// shapes outside the compiled variants.
+int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan);
+int launchFdf(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
+int launchFinalize(const FinArgs& args, int finBlocks, cudaStream_t s);
+int finalizeBlocks(int R, int W);
+
+// Converts one wave of amplitudes (complex64 or complex128, device memory)
+// into the complex64 store row, divided by `divisor` in FP64; sets *nonzero
+// to 1 if any amplitude is non-zero.
+int launchConvertRow(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor, unsigned* nonzero,
+                     cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Hessian event term
+// ---------------------------------------------------------------------------
+// For events [e0, e0 + slab) writes, per event t (column of the slab):
+//   Y1 rows [0, nS):      d_s = S_{r(s),e(s)} conj(A_{w(s)})   (nS = R*W slots)
+//   Y1 rows [nS, 2nS):    conj(d_s)
+//   Y1 row 2nS:           1
+//   Y2 rows [0, W):       A_w;   Y2 row W: 1
+//   w1 = f^2, w2 = f with f = 2 / L (0 beyond nEvents)
+// so that the weighted Gram matrices of Y1 and Y2 give every event sum of the
+// analytic Hessian (partialWaveFit/pwaLikelihood.cc:676-735).
+int launchHessPrep(const float2* amps, uint64_t nEvents, uint64_t nPad, uint64_t e0, uint64_t slab, int W0, int W,
+                   int R, int P, const double* par, const int* slotRe, const int* slotIm, float2* Y1, float2* Y2,
+                   double* w1, double* w2, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Integral matrix (Gram) kernels
+// ---------------------------------------------------------------------------
+struct GramArgs {
+	const float2* amps;     // [W][K] complex64 (K = events x subamps), row stride ldK (elements)
+	const double2* amps64;  // [W][K] complex128 alternative (FP64 precision)
+	uint64_t K;
+	uint64_t ldK;
+	int W;
+	const double* weightK;  // optional per-K weight (1/w, already expanded over subamps), or null
+	double* partials;       // [chunks][W*W*2]
+	int chunks;
+	unsigned* devErr;
+};
+int launchGramSimt(const GramArgs& a, int precision, cudaStream_t s);
+// out = (accumulate ? out : 0) + sum of chunk partials, mirrored to the lower triangle
+int launchGramReduce(const double* partials, int chunks, int W, double* out, int accumulate, cudaStream_t s);
+// tcgen05 tensor-core Gram; returns kErrUnsupported when the shape has no variant
+int launchGramTc(const GramArgs& a, int precision, int numSMs, cudaStream_t s, double* out, double* scratch,
+                 size_t scratchDoubles);
+
+}  // namespace pwa

@@ -1,0 +1,185 @@
+"""CPU tests of the C ABI: the library loads and exports every declared
+symbol, the host-side logic (integral bookkeeping and ASCII I/O, wave list,
+parameter layout, sign convention) matches the oracle, and device work fails
+loudly when no GPU is present."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import rootpwa_gb300 as R
+from rootpwa_gb300 import _native as N
+from rootpwa_gb300 import synth
+from oracle.oracle import OracleIntegral, OracleLikelihood
+from test_oracle import split_ascii
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_library_exports_every_declared_symbol():
+    lib = N.lib()
+    declared = N.header_symbols()
+    assert len(declared) >= 50
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    # and every binding signature refers to a declared function
+    assert set(N.SIGNATURES) <= set(declared)
+    assert lib.pwa_abi_version() == 1
+
+
+def test_read_write_ascii_fixture(tmp_path):
+    src = os.path.join(GOLDEN, "testIntegral.int")
+    I = R.ampIntegralMatrix()
+    I.readAscii(src)
+    assert I.nmbWaves() == 41 and I.nmbEvents() == 20000
+    out = tmp_path / "rt.int"
+    I.writeAscii(out)
+    assert split_ascii(out.read_text()) == split_ascii(open(src).read())
+    O = OracleIntegral()
+    assert O.read_ascii(src)
+    assert np.array_equal(I.matrix(), O.raw())
+    assert I.waveNames() == O.wave_names()
+    name = I.waveName(7)
+    assert I.waveIndex(name) == 7
+    assert I.element(name, I.waveName(3)) == O.element(7, 3)
+
+
+def test_read_ascii_rejects_truncated(tmp_path):
+    src = open(os.path.join(GOLDEN, "testIntegral.int")).read()
+    bad = tmp_path / "bad.int"
+    bad.write_text(src[:2000])
+    I = R.ampIntegralMatrix()
+    with pytest.raises(R.PwaError) as e:
+        I.readAscii(bad)
+    assert e.value.status == 6
+    with pytest.raises(R.PwaError):
+        I.readAscii(tmp_path / "does_not_exist.int")
+
+
+def test_integral_arithmetic_and_add_event():
+    rng = np.random.default_rng(11)
+    A = rng.standard_normal((5, 30)) + 1j * rng.standard_normal((5, 30))
+    names = ["a", "b", "c", "d", "e"]
+    I = R.ampIntegralMatrix()
+    I.setWaveNames(names)
+    O = OracleIntegral()
+    O.set_wave_names(names)
+    for e in range(30):
+        I.addEvent(A[:, e])
+        O.add_event(A[:, e])
+    assert I.nmbEvents() == 30
+    assert np.array_equal(I.matrix(), O.raw())
+    J = R.ampIntegralMatrix(I)
+    J += I
+    assert J.nmbEvents() == 60 and np.allclose(J.matrix(), 2 * I.matrix(), rtol=1e-15)
+    J -= I
+    assert J.nmbEvents() == 30
+    J *= 2.0
+    assert J.nmbEvents() == 60
+    J /= 2.0
+    J.renormalize(90)
+    assert J.nmbEvents() == 90 and np.allclose(J.matrix(), 3 * I.matrix(), rtol=1e-14)
+    # wave sets must match for +=
+    K = R.ampIntegralMatrix()
+    K.setWaveNames(["a", "b", "c", "d", "x"])
+    with pytest.raises(R.PwaError):
+        J += K
+    # a second setWaveNames with other names is refused (ampIntegralMatrix.cc:255-277)
+    with pytest.raises(R.PwaError):
+        I.setWaveNames(["q"] * 5)
+
+
+def _layout_pair(n_neg, n_pos, rank, thresholds=None, mass=0.0):
+    names, refl = synth.wave_names(n_neg, n_pos)
+    L = R.pwaLikelihood()
+    L.init(names, refl, thresholds, rank, mass)
+    O = OracleLikelihood()
+    assert O.init(names, refl, thresholds, rank, mass)
+    return L, O, names
+
+
+@pytest.mark.parametrize("n_neg,n_pos,rank", [(0, 15, 1), (7, 80, 2), (2, 5, 3), (1, 1, 1), (3, 0, 2), (4, 4, 4)])
+def test_parameter_layout_matches_oracle(n_neg, n_pos, rank):
+    """buildParDataStruct (pwaLikelihood.cc:1489-1556) and parName (:107-122)."""
+    L, O, names = _layout_pair(n_neg, n_pos, rank)
+    assert L.nmbPars() == O.nmbPars() == synth.n_pars(n_neg, n_pos, rank)
+    for k in range(L.nmbPars()):
+        assert L.parameter(k)["name"] == O.parName(k)
+    assert L.parameter(L.nmbPars() - 1)["name"] == "V_flat_RE"
+    assert L.nmbWaves() == n_neg + n_pos
+    assert L.nmbWaves(+1) == n_pos and L.nmbWaves(-1) == n_neg
+    assert L.rank() == rank
+
+
+def test_threshold_fixing():
+    th = [0.0, 1.5, 2.0, 0.0, 1.0]
+    L, O, names = _layout_pair(2, 3, 1, thresholds=th, mass=1.7)
+    fixed = [L.parameter(k)["fixed"] for k in range(L.nmbPars())]
+    assert fixed == [O.parFixed(k) for k in range(O.nmbPars())]
+    # only the positive-reflectivity anchor (threshold 2.0 >= 1.7) is fixed: one real parameter
+    assert L.nmbParsFixed() == O.nmbParsFixed() == 1
+    assert any(fixed)
+
+
+def test_correct_param_signs_and_prod_amps_match_oracle():
+    L, O, names = _layout_pair(3, 6, 2)
+    rng = np.random.default_rng(1)
+    for _ in range(5):
+        p = rng.standard_normal(L.nmbPars())
+        p[0] = -abs(p[0])
+        p[-1] = -abs(p[-1])
+        assert np.array_equal(L.CorrectParamSigns(p), O.CorrectParamSigns(p))
+    amps, idx = L.buildProdAmpArrays(p, withFlat=True)
+    assert idx[-1] == (L.nmbPars() - 1, -1)
+    assert amps[-1] == p[-1]
+    assert len(amps) == sum(1 for k in range(L.nmbPars()) if L.parameter(k)["realPart"])
+
+
+def test_setup_order_is_enforced():
+    """addNormIntegral before init, addAcc before addNorm, evaluation before
+    finishInit are refused as in pwaLikelihood.cc:1066-1107, :177-180."""
+    names, refl = synth.wave_names(0, 3)
+    I = R.ampIntegralMatrix()
+    I.setWaveNames(names)
+    L = R.pwaLikelihood()
+    with pytest.raises(R.PwaError) as e:
+        L.addNormIntegral(I)
+    assert e.value.status == 2
+    L.init(names, refl, None, 1, 0.0)
+    with pytest.raises(R.PwaError):
+        L.addAccIntegral(I)
+    with pytest.raises(R.PwaError) as e:
+        L.FdF(np.zeros(L.nmbPars()))
+    assert e.value.status == 2
+    with pytest.raises(R.PwaError):
+        R.pwaLikelihood().init(["a", "a"], [1, 1])
+    with pytest.raises(R.PwaError):
+        R.pwaLikelihood().init(["a"], [0])
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-GPU failure path")
+def test_device_work_fails_loudly_without_gpu():
+    w = synth.make_workload("compass15", n_data=50, n_mc=50)
+    L = R.pwaLikelihood()
+    L.init(w["names"], w["refl"], None, 1, 0.0)
+    I = R.ampIntegralMatrix()
+    I.setWaveNames(w["names"])
+    I.setMatrix(np.eye(15))
+    I.setNmbEvents(10)
+    L.addNormIntegral(I)
+    L.addAccIntegral(I)
+    with pytest.raises(R.PwaError) as e:
+        L.addAmplitude(w["names"][0], w["data"][0])
+    assert e.value.status == 3
+    J = R.ampIntegralMatrix()
+    with pytest.raises(R.PwaError):
+        J.integrate(w["names"], w["mc"])

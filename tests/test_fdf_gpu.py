@@ -1,0 +1,222 @@
+"""GPU parity of the fused FdF / DoEval / Gradient kernels against the FP64
+oracle (partialWaveFit/pwaLikelihood.cc:170-636).
+
+Tolerances (FP32 contraction, FP64 cross-tile and cross-block reductions):
+function value relative 1e-6, gradient max-abs error relative to the largest
+gradient component 1e-6."""
+import os
+
+import numpy as np
+import pytest
+
+import rootpwa_gb300 as R
+from rootpwa_gb300 import synth
+import helpers
+from helpers import F_RTOL, G_NORMWISE, normwise, rel
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def pair(w, **kw):
+    """Oracle and GPU likelihoods on identical integrals (the oracle's)."""
+    norm, acc = helpers.oracle_integrals(w)
+    gn = helpers.copy_oracle_integral_to_gpu(norm)
+    ga = helpers.copy_oracle_integral_to_gpu(acc)
+    O = helpers.build_oracle(w, norm, acc, **kw)
+    G = helpers.build_gpu(w, gn, ga, **kw)
+    return O, G
+
+
+def check_point(O, G, p, frtol=F_RTOL, gtol=G_NORMWISE):
+    f0, g0 = O.FdF(p)
+    f1, g1 = G.FdF(p)
+    assert rel(f1, f0) < frtol, (f1, f0)
+    assert normwise(g1, g0) < gtol, normwise(g1, g0)
+    return f0, g0, f1, g1
+
+
+def test_golden_compass15():
+    from golden.make_golden import GOLDEN_WORKLOADS
+    gold = np.load(os.path.join(GOLDEN, "oracle_compass15_seed0.npz"))
+    w = synth.make_workload(**GOLDEN_WORKLOADS["compass15_seed0"])
+    gn = R.ampIntegralMatrix()
+    gn.setWaveNames(w["names"])
+    gn.setMatrix(gold["norm_raw"])
+    gn.setNmbEvents(int(gold["norm_n"]))
+    ga = R.ampIntegralMatrix()
+    ga.setWaveNames(w["names"])
+    ga.setMatrix(gold["acc_raw"])
+    ga.setNmbEvents(int(gold["acc_n"]))
+    G = helpers.build_gpu(w, gn, ga)
+    f, g = G.FdF(w["par"])
+    assert rel(f, float(gold["f"])) < F_RTOL
+    assert normwise(g, gold["grad"]) < G_NORMWISE
+    assert rel(G.DoEval(w["par"]), float(gold["doeval"])) < F_RTOL
+    assert G.totAcc() == pytest.approx(float(gold["tot_acc"]), rel=1e-15)
+
+
+def test_golden_compass88_small():
+    from golden.make_golden import GOLDEN_WORKLOADS
+    gold = np.load(os.path.join(GOLDEN, "oracle_compass88_small_seed1.npz"))
+    w = synth.make_workload(**GOLDEN_WORKLOADS["compass88_small_seed1"])
+    gn = R.ampIntegralMatrix()
+    gn.setWaveNames(w["names"])
+    gn.setMatrix(gold["norm_raw"])
+    gn.setNmbEvents(int(gold["norm_n"]))
+    ga = R.ampIntegralMatrix()
+    ga.setWaveNames(w["names"])
+    ga.setMatrix(gold["acc_raw"])
+    ga.setNmbEvents(int(gold["acc_n"]))
+    G = helpers.build_gpu(w, gn, ga)
+    f, g = G.FdF(w["par"])
+    assert rel(f, float(gold["f"])) < F_RTOL
+    assert normwise(g, gold["grad"]) < G_NORMWISE
+
+
+@pytest.mark.parametrize("n_neg,n_pos,rank,n_data", [
+    (0, 15, 1, 20_000),      # compass15 shape
+    (7, 80, 2, 30_001),      # compass88 shape, ragged tail
+    (7, 80, 2, 1),           # a single event
+    (3, 5, 1, 127),          # less than one tile
+    (2, 9, 3, 129),          # rank above the negative wave count
+    (5, 0, 2, 1000),         # negative reflectivity only
+    (1, 1, 1, 256),          # one wave per reflectivity
+    (20, 120, 1, 4099),      # 140 waves -> 64-event tiles
+    (10, 54, 4, 3000),       # rank 4
+    (0, 200, 1, 2000),       # 200 waves
+])
+def test_shapes_against_oracle(n_neg, n_pos, rank, n_data):
+    names, refl = synth.wave_names(n_neg, n_pos)
+    rng = np.random.default_rng(n_data + 31 * rank)
+    model = synth.AmplitudeModel(n_neg + n_pos, 4, rng)
+    w = dict(names=names, refl=refl, rank=rank, data=model.draw(rng, n_data), mc=model.draw(rng, 3000),
+             accepted=rng.random(3000) < 0.6, par=rng.standard_normal(synth.n_pars(n_neg, n_pos, rank)))
+    O, G = pair(w)
+    check_point(O, G, w["par"])
+    # a second point on the same handle (no stale state)
+    check_point(O, G, 0.5 * w["par"][::-1].copy())
+
+
+def test_doeval_gradient_doderivative_consistent():
+    w = synth.make_workload("compass88", seed=3, n_data=9000, n_mc=4000)
+    O, G = pair(w)
+    p = w["par"]
+    f, g = G.FdF(p)
+    assert G.DoEval(p) == f           # same kernels, same order: bitwise
+    assert np.array_equal(G.Gradient(p), g)
+    assert G.DoDerivative(p, 5) == g[5]   # cached
+    q = p * 1.01
+    d = G.DoDerivative(q, 7)
+    assert d == pytest.approx(O.Gradient(q)[7], rel=1e-5, abs=1e-6 * np.max(np.abs(g)))
+    info = G.funcCallInfo(0)
+    assert info["nmbCalls"] >= 2 and info["funcTime"] > 0
+
+
+def test_deterministic_and_batch():
+    w = synth.make_workload("compass88", seed=4, n_data=20000, n_mc=4000)
+    O, G = pair(w)
+    p = w["par"]
+    f1, g1 = G.FdF(p)
+    f2, g2 = G.FdF(p)
+    assert f1 == f2 and np.array_equal(g1, g2)
+    pts = np.stack([p, 0.3 * p, -p, p + 0.1])
+    fb, gb = G.FdFBatch(pts)
+    for k in range(len(pts)):
+        fk, gk = G.FdF(pts[k])
+        assert fb[k] == fk and np.array_equal(gb[k], gk)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "kahan_fp32"])
+def test_reduction_modes(mode):
+    w = synth.make_workload("compass88", seed=5, n_data=50000, n_mc=4000)
+    O, G = pair(w)
+    G.setReduction(mode)
+    check_point(O, G, w["par"])
+
+
+def test_options_prior_unnormalised_thresholds_override():
+    w = synth.make_workload("compass15", seed=6, n_data=5000, n_mc=8000)
+    th = np.zeros(15)
+    th[3] = 2.5
+    th[9] = 1.0
+    kw = dict(use_normalized=False, prior=1, cauchy_width=0.7, thresholds=th, mass_bin_center=2.0,
+              acc_override=12345)
+    O, G = pair(w, **kw)
+    assert [G.parameter(k)["fixed"] for k in range(G.nmbPars())] == [O.parFixed(k) for k in range(O.nmbPars())]
+    check_point(O, G, w["par"])
+    assert G.totAcc() == pytest.approx(O.totAcc(), rel=1e-15)
+
+
+def test_zero_amplitude_wave_is_fixed():
+    """addAmplitude fixes the parameters of an all-zero wave whose acceptance
+    diagonal is zero (pwaLikelihood.cc:1300-1334)."""
+    w = synth.make_workload("compass15", seed=8, n_data=2000, n_mc=3000)
+    w["mc"][4] = 0
+    w["data"][4] = 0
+    O, G = pair(w)
+    assert [G.parameter(k)["fixed"] for k in range(G.nmbPars())] == [O.parFixed(k) for k in range(O.nmbPars())]
+    assert G.nmbParsFixed() == O.nmbParsFixed() == 2
+    check_point(O, G, w["par"])
+
+
+def test_complex128_host_and_device_input():
+    torch = pytest.importorskip("torch")
+    w = synth.make_workload("compass88", seed=9, n_data=7000, n_mc=3000)
+    norm, acc = helpers.oracle_integrals(w)
+    O = helpers.build_oracle(w, norm, acc)
+    G64 = helpers.build_gpu(w, helpers.copy_oracle_integral_to_gpu(norm), helpers.copy_oracle_integral_to_gpu(acc),
+                            amps=w["data"].astype(np.complex128))
+    dev = torch.from_numpy(w["data"]).cuda()
+    Gd = helpers.build_gpu(w, helpers.copy_oracle_integral_to_gpu(norm), helpers.copy_oracle_integral_to_gpu(acc),
+                           amps=dev)
+    f0, g0 = O.FdF(w["par"])
+    for G in (G64, Gd):
+        f, g = G.FdF(w["par"])
+        assert rel(f, f0) < F_RTOL and normwise(g, g0) < G_NORMWISE
+
+
+def test_device_resident_fdf_and_graph_capture():
+    torch = pytest.importorskip("torch")
+    w = synth.make_workload("compass88", seed=10, n_data=12000, n_mc=3000)
+    O, G = pair(w)
+    P = G.nmbPars()
+    s = torch.cuda.Stream()
+    G.setStream(s.cuda_stream)
+    dpar = torch.from_numpy(w["par"]).cuda()
+    dout = torch.zeros(P + 2, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    G.FdFDevice(dpar.data_ptr(), dout.data_ptr(), True, s.cuda_stream)
+    s.synchronize()
+    f0, g0 = O.FdF(w["par"])
+    out = dout.cpu().numpy()
+    assert out[P + 1] == 0.0
+    assert rel(out[0], f0) < F_RTOL and normwise(out[1:P + 1], g0) < G_NORMWISE
+    # the same two launches captured in a CUDA graph and replayed
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        G.FdFDevice(dpar.data_ptr(), dout.data_ptr(), True, s.cuda_stream)
+    dout.zero_()
+    dpar.mul_(0.5)
+    graph.replay()
+    torch.cuda.synchronize()
+    f1, g1 = O.FdF(0.5 * w["par"])
+    out = dout.cpu().numpy()
+    assert rel(out[0], f1) < F_RTOL and normwise(out[1:P + 1], g1) < G_NORMWISE
+
+
+def test_error_paths_on_gpu():
+    w = synth.make_workload("compass15", seed=12, n_data=300, n_mc=600)
+    norm, acc = helpers.oracle_integrals(w)
+    G = R.pwaLikelihood()
+    G.init(w["names"], w["refl"], None, 1, 0.0)
+    G.addNormIntegral(helpers.copy_oracle_integral_to_gpu(norm))
+    G.addAccIntegral(helpers.copy_oracle_integral_to_gpu(acc))
+    G.addAmplitude(w["names"][0], w["data"][0])
+    with pytest.raises(R.PwaError):
+        G.addAmplitude(w["names"][1], w["data"][1][:100])   # size mismatch
+    with pytest.raises(R.PwaError):
+        G.addAmplitude("not_a_wave", w["data"][1])
+    with pytest.raises(R.PwaError) as e:
+        G.finishInit()                                        # waves missing
+    assert e.value.status == 2

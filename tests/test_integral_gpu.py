@@ -1,0 +1,110 @@
+"""GPU parity of the integral-matrix Gram kernels against the FP64 oracle's
+ampIntegralMatrix::integrate (decayAmplitude/ampIntegralMatrix.cc:300-489).
+
+Tolerance: max |I - I_ref| / max |I_ref| below 1e-12 for the FP64 variant,
+1e-6 for FP32 (SIMT) and the split-precision tensor-core variants, 5e-3 for
+single-pass TF32."""
+import numpy as np
+import pytest
+
+import rootpwa_gb300 as R
+from rootpwa_gb300 import synth
+from oracle.oracle import OracleIntegral
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "fp32": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-6, "tf32": 5e-3}
+
+
+def maxrel(m, ref):
+    return float(np.max(np.abs(m - ref)) / np.max(np.abs(ref)))
+
+
+def integrate_or_skip(I, *args, **kw):
+    try:
+        I.integrate(*args, **kw)
+    except R.PwaError as e:
+        if e.status == 7 and kw.get("precision") in ("tf32", "tf32x3", "bf16x3"):
+            pytest.skip("tensor-core variant not built for this shape: %s" % e)
+        raise
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "tf32x3", "bf16x3", "tf32"])
+@pytest.mark.parametrize("nw,ne", [(15, 100_000), (87, 20_011), (1, 777), (65, 4096), (130, 3000)])
+def test_integrate_against_oracle(precision, nw, ne):
+    rng = np.random.default_rng(nw * 1000 + ne)
+    model = synth.AmplitudeModel(nw, 4 if nw > 4 else 0, rng)
+    A = model.draw(rng, ne)
+    names = ["w%03d" % k for k in range(nw)]
+    O = OracleIntegral()
+    assert O.integrate(names, A.astype(np.complex128))
+    I = R.ampIntegralMatrix()
+    integrate_or_skip(I, names, A, precision=precision)
+    assert I.nmbEvents() == O.nmb_events() == ne
+    m, ref = I.matrix(), O.raw()
+    assert maxrel(m, ref) < TOL[precision], maxrel(m, ref)
+    assert np.array_equal(m, m.conj().T)          # exactly Hermitian
+    assert np.all(np.imag(np.diag(m)) == 0)
+
+
+def test_fp64_with_complex128_input_is_near_exact():
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((20, 5000)) + 1j * rng.standard_normal((20, 5000))
+    names = ["w%d" % k for k in range(20)]
+    O = OracleIntegral()
+    O.integrate(names, A)
+    I = R.ampIntegralMatrix()
+    I.integrate(names, A, precision="fp64")
+    assert maxrel(I.matrix(), O.raw()) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_weights_bins_max_events_subamps(precision):
+    rng = np.random.default_rng(2)
+    A = (rng.standard_normal((9, 4000, 2)) + 1j * rng.standard_normal((9, 4000, 2))).astype(np.complex64)
+    sel = rng.random(4000) < 0.7
+    wts = rng.uniform(0.2, 3.0, int(sel.sum()))
+    names = ["w%d" % k for k in range(9)]
+    O = OracleIntegral()
+    assert O.integrate(names, A.astype(np.complex128), weights=wts, in_bin=sel, max_nmb_events=3500)
+    I = R.ampIntegralMatrix()
+    I.integrate(names, A, weights=wts, inBin=sel, maxNmbEvents=3500, precision=precision, nmbSubAmps=2)
+    assert I.nmbEvents() == O.nmb_events()
+    assert maxrel(I.matrix(), O.raw()) < TOL[precision]
+
+
+def test_device_input_and_accumulation():
+    torch = pytest.importorskip("torch")
+    w = synth.make_workload("compass88", seed=3, n_data=10, n_mc=30000)
+    names = w["names"]
+    d = torch.from_numpy(w["mc"]).cuda()
+    I = R.ampIntegralMatrix()
+    I.integrate(names, d, precision="fp32")
+    O = OracleIntegral()
+    O.integrate(names, w["mc"].astype(np.complex128))
+    assert maxrel(I.matrix(), O.raw()) < 1e-6
+    # files combine with += (pyInterface/module/_integrals.py:50-52)
+    J = R.ampIntegralMatrix()
+    J.integrate(names, w["mc"][:, :10000], precision="fp32")
+    K = R.ampIntegralMatrix()
+    K.integrate(names, w["mc"][:, 10000:], precision="fp32")
+    J += K
+    assert J.nmbEvents() == 30000
+    assert maxrel(J.matrix(), O.raw()) < 1e-6
+
+
+def test_gpu_integrals_feed_the_likelihood():
+    """The acceptance/normalisation integrals built on the GPU give the same
+    likelihood as the oracle's integrals."""
+    w = synth.make_workload("compass15", seed=4, n_data=3000, n_mc=100_000)
+    gn, ga = helpers.gpu_integrals(w, "fp32")
+    G = helpers.build_gpu(w, gn, ga)
+    O = helpers.build_oracle(w)
+    f0, g0 = O.FdF(w["par"])
+    f1, g1 = G.FdF(w["par"])
+    assert helpers.rel(f1, f0) < 1e-6
+    assert helpers.normwise(g1, g0) < 1e-5
+    # addAccIntegral set the acceptance integral's event count to the generated count
+    assert ga.nmbEvents() == 100_000
+    assert G.totAcc() == pytest.approx(O.totAcc(), rel=1e-15)
