@@ -281,7 +281,6 @@ def run_gb300(args):
         if i % 200 == 0:
             stream.synchronize()
     stream.synchronize()
-    L.setTiming(True)
     launches0 = lib.pwa_kernel_launch_count()
     if world > 1:
         torch.distributed.barrier()
@@ -295,10 +294,15 @@ def run_gb300(args):
     ev1.synchronize()
     torch.cuda.synchronize()
     launches = lib.pwa_kernel_launch_count() - launches0
-    clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
+    # the same steps once more with CUDA events around each of the two
+    # kernels (on the launch stream) for the per-kernel durations
+    L.setTiming(True)
+    for i in range(args.steps):
+        step(i)
     main_ms, fin_ms, n_timed = L.kernelTimes()
     L.setTiming(False)
+    clocks = sampler.stop()
     out = d_out.cpu().numpy()
     assert np.all(out[:, P + 1] == 0.0), "device error flag set"
     assert np.all(np.isfinite(out[:, :P + 1]))
@@ -376,7 +380,8 @@ def run_gb300(args):
                            "waves": 88, "rank": RANK, "events": args.n_data, "parameters": P,
                            "mc_events": args.n_mc, "reduction": args.reduction,
                            "l2": "inputs (%.0f MB) larger than L2 (129 MB); no flush" % (alg_bytes / 1e6),
-                           "entry": "pwa_likelihood_fdf_device (parameters and results in HBM)"},
+                           "entry": "pwa_likelihood_fdf_device (parameters and results in HBM)",
+                           "plan": dict(zip(("tile_events", "stages", "blocks"), L.plan()))},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": P * 8,
                         "d2h_bytes_per_step": (P + 2) * 8, "entry": "pwa_likelihood_fdf (host buffers)"},
                 "gpu_launches": int(launches), "launches_per_step": launches / args.steps,

@@ -15,12 +15,17 @@
 //   * event tiles of E events x W waves are staged in shared memory by
 //     cp.async.bulk copies (one per wave row, issued by one warp) completing
 //     on an mbarrier; `stages` tiles are in flight;
-//   * phase 1: 512/E threads per event each sum a slice of the waves; the
-//     slices are combined per event, giving L_i, c_i and T_{r,e,i} = c_i S;
+//   * phase 1: each warp owns E/16 events of the tile, 32/(E/16) lanes per
+//     event sum interleaved slices of the waves and combine them with warp
+//     shuffles, giving L_i, c_i and T_{r,e,i} = c_i S (double-buffered, so
+//     one block barrier per tile suffices);
 //   * phase 2: warp j owns a contiguous range of waves, each lane a fixed set
-//     of event pairs; per tile the lane sums conj(A) T over its events in FP32
-//     and a warp reduce-scatter leaves every lane one (slot, re/im) value,
-//     which it adds to its FP64 (or compensated FP32) accumulator.
+//     of event pairs; the lane sums conj(A) T over its events in FP32 for
+//     kFold tiles, then a warp reduce-scatter leaves every lane one
+//     (slot, re/im) value, which it adds to its FP64 (or compensated FP32)
+//     accumulator;
+//   * the last warp to finish with a stage (shared-memory counter) refills it
+//     with the tile `stages` ahead.
 // Every mbarrier wait is bounded (about a second); on expiry the CTA sets a
 // device error flag, waits (again bounded) for its own copies and returns.
 
@@ -92,6 +97,11 @@ __device__ __forceinline__ void bulkCopyG2S(void* dst, const void* src, uint32_t
 
 __device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Programmatic dependent launch: wait until the preceding grid in the stream
+// has completed and its memory is visible; allow the next grid to launch.
+__device__ __forceinline__ void gridDependencyWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void gridDependencyTrigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ float warpSum(float v)
 {
 #pragma unroll
@@ -134,45 +144,59 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
 }
 
 // Shared-memory layout of the main kernel (byte offsets from the dynamic base).
+// A tile holds W rows of E complex64 amplitudes; rows are padded by
+// 8 * (E / kWarps) bytes so that the phase-1 access (lanes split over
+// 32 / (E / kWarps) wave slices and E / kWarps events) touches every bank
+// pair at most once per 256 bytes.
 struct SmemLayout {
-	size_t tiles, vs, sp, ts, bars, total;
+	size_t rowStride;  // bytes per wave row
+	size_t tiles, vs, ts, bars, done, total;
 };
 
 __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
 {
-	// every region starts on a 128-byte boundary (float4 and bulk-copy targets)
-	const int H = kThreads / E;
 	auto up = [](size_t x) { return (x + 127) & ~(size_t)127; };
 	SmemLayout L;
+	L.rowStride = (size_t)E * 8 + 8 * (size_t)(E / kWarps);
 	L.tiles = 0;
-	L.vs = up((size_t)stages * W * E * 8);
-	L.sp = up(L.vs + (size_t)W * R * 8);
-	L.ts = up(L.sp + (size_t)H * R * 2 * E * 8);
-	L.bars = up(L.ts + (size_t)R * 2 * E * 8);
-	L.total = L.bars + (size_t)stages * 8;
+	L.vs = up((size_t)stages * W * L.rowStride);
+	L.ts = up(L.vs + (size_t)W * R * 8);
+	L.bars = up(L.ts + 2 * (size_t)R * 2 * E * 8);
+	L.done = L.bars + (size_t)stages * 8;
+	L.total = L.done + (size_t)stages * 4;
 	return L;
 }
+
+// Tiles whose gradient partials are summed in FP32 before the warp
+// reduce-scatter folds them into the FP64 (or compensated) accumulators.
+constexpr int kFold = 4;
 
 template <int R, int E, int WPW>
 __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, const int stages)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
-	constexpr int H = kThreads / E;          // threads per event in phase 1
+	constexpr int EPW = E / kWarps;          // events per warp in phase 1
+	constexpr int H = 32 / EPW;              // lanes (wave slices) per event
 	constexpr int NV = WPW * R * 2;          // phase-2 values per lane
 	constexpr int NQ = (NV + 31) / 32;       // rounds of 32
 	constexpr int NVP = NQ * 32;
 	constexpr int EPAIRS = E / 64;           // event pairs per lane per tile
+	static_assert(EPW * kWarps == E && H * EPW == 32, "tile shape");
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const int W = a.W, W0 = a.W0;
 	const SmemLayout lay = smemLayout(W, R, E, stages);
+	const int rowF2 = (int)(lay.rowStride / 8);  // row stride in float2
 	float2* tiles = reinterpret_cast<float2*>(smem + lay.tiles);
 	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);
-	float2* Sp = reinterpret_cast<float2*>(smem + lay.sp);
-	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);
+	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);  // [2][R][2][E]
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
+	unsigned* done = reinterpret_cast<unsigned*>(smem + lay.done);
 	__shared__ double redLL[kWarps], redC[kWarps];
 
+	// the parameters may be written by the preceding grid (device-side minimiser)
+	gridDependencyWait();
+	gridDependencyTrigger();
 	// production amplitudes V[w][r] as FP32 complex
 	for (int k = tid; k < W * R; k += kThreads) {
 		const int w = k / R, r = k - w * R;
@@ -185,41 +209,45 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	const uint64_t nTiles = (a.nEvents + E - 1) / E;
 	const uint64_t first = blockIdx.x, stride = gridDim.x;
 	const uint64_t myTiles = (first < nTiles) ? (nTiles - 1 - first) / stride + 1 : 0;
-	const uint32_t stageBytes = (uint32_t)W * E * 8u;
+	const uint32_t rowBytes = E * 8u;
+	const uint32_t stageBytes = (uint32_t)W * rowBytes;
 
 	if (tid == 0) {
-		for (int s = 0; s < stages; ++s)
+		for (int s = 0; s < stages; ++s) {
 			mbarInit(&bars[s], 1);
+			done[s] = 0u;
+		}
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
 	__syncthreads();
 
-	// issue tile k (local index) into stage s; executed by all lanes of warp 0
+	// issue tile k (local index) into stage s; executed by all lanes of one warp
 	auto issue = [&](uint64_t k, int s) {
 		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
-		float2* dst = tiles + (size_t)s * W * E;
+		float2* dst = tiles + (size_t)s * W * rowF2;
 		if (lane == 0)
 			mbarArriveExpectTx(&bars[s], stageBytes);
 		__syncwarp();
 		for (int w = lane; w < W; w += 32)
-			bulkCopyG2S(dst + (size_t)w * E, a.amps + (size_t)w * a.nPad + e0, E * 8u, &bars[s]);
+			bulkCopyG2S(dst + (size_t)w * rowF2, a.amps + (size_t)w * a.nPad + e0, rowBytes, &bars[s]);
 	};
 	if (warp == 0) {
 		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
 			issue((uint64_t)s, s);
 	}
-	uint64_t issued = ((uint64_t)stages < myTiles) ? (uint64_t)stages : myTiles;
 
-	// phase-1 role
-	const int pe = tid % E, ph = tid / E;
-	const int pwb = ph * W / H, pwe = (ph + 1) * W / H;
-	// phase-2 role
+	// phase-1 role: event pe of the tile, wave slice ph (waves w = ph mod H)
+	const int pm = lane / H, ph = lane - pm * H;
+	const int pe = warp * EPW + pm;
+	const int wStart1 = W0 + (((ph - W0) % H) + H) % H;  // first positive-reflectivity wave of this slice
+	// phase-2 role: warp owns waves [wBase, wBase + nWarpWaves)
 	const int wpwa = (W + kWarps - 1) / kWarps;
 	const int wBase = warp * wpwa;
 	const int nWarpWaves = max(0, min(wpwa, W - wBase));
 
 	double accLL = 0., accC = 0.;
 	float kLL = 0.f, kLLc = 0.f, kC = 0.f, kCc = 0.f;
+	float llPart = 0.f, cPart = 0.f;
 	double accG[NQ];
 	float kG[NQ], kGc[NQ];
 #pragma unroll
@@ -228,21 +256,22 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		kG[q] = 0.f;
 		kGc[q] = 0.f;
 	}
+	float part[NVP];
+#pragma unroll
+	for (int v = 0; v < NVP; ++v)
+		part[v] = 0.f;
 
 	bool failed = false;
 	uint64_t k = 0;
 	for (; k < myTiles; ++k) {
 		const int s = (int)(k % (uint64_t)stages);
 		const uint32_t parity = (uint32_t)((k / (uint64_t)stages) & 1ull);
-		const bool ok = mbarWaitBounded(&bars[s], parity);
-		if (!__syncthreads_and(ok)) {
-			failed = true;
-			break;
-		}
-		const float2* tile = tiles + (size_t)s * W * E;
+		const bool timedOut = !mbarWaitBounded(&bars[s], parity);
+		const float2* tile = tiles + (size_t)s * W * rowF2;
 		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
+		float2* T = Ts + (size_t)(k & 1ull) * R * 2 * E;
 
-		// ---- phase 1: partial coherent sums over a slice of the waves ----
+		// ---- phase 1: coherent sums, combined across the H lanes of an event ----
 		{
 			float2 S[R][2];
 #pragma unroll
@@ -250,9 +279,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				S[r][0] = make_float2(0.f, 0.f);
 				S[r][1] = make_float2(0.f, 0.f);
 			}
-			const int m = min(pwe, W0);
-			for (int w = pwb; w < m; ++w) {
-				const float2 av = tile[(size_t)w * E + pe];
+			for (int w = ph; w < W0; w += H) {
+				const float2 av = tile[(size_t)w * rowF2 + pe];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					const float2 v = Vs[w * R + r];
@@ -260,8 +288,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					S[r][0].y = fmaf(v.x, av.y, fmaf(v.y, av.x, S[r][0].y));
 				}
 			}
-			for (int w = max(pwb, W0); w < pwe; ++w) {
-				const float2 av = tile[(size_t)w * E + pe];
+			for (int w = wStart1; w < W; w += H) {
+				const float2 av = tile[(size_t)w * rowF2 + pe];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					const float2 v = Vs[w * R + r];
@@ -269,62 +297,41 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					S[r][1].y = fmaf(v.x, av.y, fmaf(v.y, av.x, S[r][1].y));
 				}
 			}
-#pragma unroll
-			for (int r = 0; r < R; ++r) {
-				Sp[((ph * R + r) * 2 + 0) * E + pe] = S[r][0];
-				Sp[((ph * R + r) * 2 + 1) * E + pe] = S[r][1];
-			}
-		}
-		__syncthreads();
-
-		// ---- combine: L_i, c_i, T = c_i S ----
-		if (tid < E) {
 			float L = flat2;
-			float2 S[R][2];
 #pragma unroll
 			for (int r = 0; r < R; ++r)
 #pragma unroll
 				for (int e = 0; e < 2; ++e) {
-					float2 acc = Sp[((0 * R + r) * 2 + e) * E + tid];
 #pragma unroll
-					for (int h = 1; h < H; ++h) {
-						const float2 p = Sp[((h * R + r) * 2 + e) * E + tid];
-						acc.x += p.x;
-						acc.y += p.y;
+					for (int o = 1; o < H; o <<= 1) {
+						S[r][e].x += __shfl_xor_sync(0xffffffffu, S[r][e].x, o);
+						S[r][e].y += __shfl_xor_sync(0xffffffffu, S[r][e].y, o);
 					}
-					S[r][e] = acc;
-					L = fmaf(acc.x, acc.x, fmaf(acc.y, acc.y, L));
+					L = fmaf(S[r][e].x, S[r][e].x, fmaf(S[r][e].y, S[r][e].y, L));
 				}
-			const bool valid = (e0 + (uint64_t)tid) < a.nEvents;
+			const bool valid = (e0 + (uint64_t)pe) < a.nEvents;
 			const float c = valid ? -2.f / L : 0.f;
-			float ll = valid ? -logf(L) : 0.f;
-			if (a.withGrad) {
+			if (ph == 0) {
+				if (valid)
+					llPart += -logf(L);
+				cPart += c;
+				if (a.withGrad) {
 #pragma unroll
-				for (int r = 0; r < R; ++r)
+					for (int r = 0; r < R; ++r)
 #pragma unroll
-					for (int e = 0; e < 2; ++e)
-						Ts[(r * 2 + e) * E + tid] = make_float2(c * S[r][e].x, c * S[r][e].y);
-			}
-			ll = warpSum(ll);
-			const float cs = warpSum(c);
-			if (lane == 0) {
-				if (a.reduction == 0) {
-					accLL += (double)ll;
-					accC += (double)cs;
-				} else {
-					kahanAdd(kLL, kLLc, ll);
-					kahanAdd(kC, kCc, cs);
+						for (int e = 0; e < 2; ++e)
+							T[(r * 2 + e) * E + pe] = make_float2(c * S[r][e].x, c * S[r][e].y);
 				}
 			}
 		}
-		__syncthreads();
+		// the only block barrier per tile: T complete (and a uniform exit on timeout)
+		if (__syncthreads_or(timedOut)) {
+			failed = true;
+			break;
+		}
 
 		// ---- phase 2: gradient contraction over the tile ----
 		if (a.withGrad) {
-			float part[NVP];
-#pragma unroll
-			for (int v = 0; v < NVP; ++v)
-				part[v] = 0.f;
 #pragma unroll
 			for (int pp = 0; pp < EPAIRS; ++pp) {
 				const int ev = 2 * lane + 64 * pp;
@@ -333,12 +340,12 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				for (int r = 0; r < R; ++r)
 #pragma unroll
 					for (int e = 0; e < 2; ++e)
-						t[r][e] = *reinterpret_cast<const float4*>(&Ts[(r * 2 + e) * E + ev]);
+						t[r][e] = *reinterpret_cast<const float4*>(&T[(r * 2 + e) * E + ev]);
 #pragma unroll
 				for (int wi = 0; wi < WPW; ++wi) {
 					if (wi < nWarpWaves) {
 						const int w = wBase + wi;
-						const float4 av = *reinterpret_cast<const float4*>(&tile[(size_t)w * E + ev]);
+						const float4 av = *reinterpret_cast<const float4*>(&tile[(size_t)w * rowF2 + ev]);
 						const bool pos = (w >= W0);
 #pragma unroll
 						for (int r = 0; r < R; ++r) {
@@ -360,30 +367,62 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					}
 				}
 			}
-#pragma unroll
-			for (int q = 0; q < NQ; ++q) {
-				const float v = reduceScatter32(&part[q * 32], lane);
-				if (a.reduction == 0)
-					accG[q] += (double)v;
-				else
-					kahanAdd(kG[q], kGc[q], v);
+		}
+
+		// stage s is no longer read by this warp; the last warp to finish
+		// with it refills it with tile k + stages
+		__syncwarp();
+		unsigned prev = 0;
+		if (lane == 0) {
+			__threadfence_block();
+			prev = atomicAdd(&done[s], 1u);
+		}
+		prev = __shfl_sync(0xffffffffu, prev, 0);
+		if (prev == (unsigned)(kWarps - 1)) {
+			if (lane == 0)
+				atomicExch(&done[s], 0u);
+			if (k + (uint64_t)stages < myTiles) {
+				fenceProxyAsync();
+				issue(k + (uint64_t)stages, s);
 			}
 		}
-		__syncthreads();  // stage s and Ts are free again
 
-		if (warp == 0 && k + (uint64_t)stages < myTiles) {
-			fenceProxyAsync();
-			issue(k + (uint64_t)stages, s);
+		// fold the FP32 tile partials every kFold tiles and after the last tile
+		if ((k + 1) % kFold == 0 || k + 1 == myTiles) {
+			const float ll = warpSum(llPart), cs = warpSum(cPart);
+			llPart = 0.f;
+			cPart = 0.f;
+			if (lane == 0) {
+				if (a.reduction == 0) {
+					accLL += (double)ll;
+					accC += (double)cs;
+				} else {
+					kahanAdd(kLL, kLLc, ll);
+					kahanAdd(kC, kCc, cs);
+				}
+			}
+			if (a.withGrad) {
+#pragma unroll
+				for (int q = 0; q < NQ; ++q) {
+					const float v = reduceScatter32(&part[q * 32], lane);
+					if (a.reduction == 0)
+						accG[q] += (double)v;
+					else
+						kahanAdd(kG[q], kGc[q], v);
+				}
+#pragma unroll
+				for (int v = 0; v < NVP; ++v)
+					part[v] = 0.f;
+			}
 		}
-		if (k + (uint64_t)stages < myTiles)
-			++issued;
 	}
 
 	if (failed) {
-		// let our own copies in flight land before the CTA exits (bounded)
+		// let our own copies in flight land before the CTA exits (bounded):
+		// tiles up to k - 1 + stages have been issued
 		if (tid == 0) {
 			atomicOr(a.devErr, (unsigned)kDevErrTimeout);
-			for (uint64_t j = k; j < issued; ++j) {
+			for (uint64_t j = k; j < k + (uint64_t)stages && j < myTiles; ++j) {
 				const int s = (int)(j % (uint64_t)stages);
 				mbarWaitBounded(&bars[s], (uint32_t)((j / (uint64_t)stages) & 1ull));
 			}
@@ -391,8 +430,12 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		return;
 	}
 
-	// ---- epilogue: per-block partials ----
-	double* out = a.partials + (size_t)blockIdx.x * a.nPartial;
+	// ---- epilogue: per-block partials, slot-major [nPartial][gridDim] ----
+	// (the previous grid's finalize kernel may still read the partials when
+	// this grid starts early under programmatic dependent launch)
+	gridDependencyWait();
+	double* out = a.partials + blockIdx.x;
+	const size_t ps = gridDim.x;
 	if (lane == 0) {
 		if (a.reduction == 0) {
 			redLL[warp] = accLL;
@@ -405,12 +448,12 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	__syncthreads();
 	if (tid == 0) {
 		double ll = 0., cs = 0.;
-		for (int wv = 0; wv < E / 32; ++wv) {
+		for (int wv = 0; wv < kWarps; ++wv) {
 			ll += redLL[wv];
 			cs += redC[wv];
 		}
 		out[0] = ll;
-		out[1] = cs;
+		out[ps] = cs;
 	}
 	if (a.withGrad) {
 #pragma unroll
@@ -423,7 +466,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				if (wi < nWarpWaves) {
 					const int w = wBase + wi;
 					const double v = (a.reduction == 0) ? accG[q] : ((double)kG[q] - (double)kGc[q]);
-					out[2 + (r * W + w) * 2 + comp] = v;
+					out[(size_t)(2 + (r * W + w) * 2 + comp) * ps] = v;
 				}
 			}
 		}
@@ -441,6 +484,9 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 	const double flat = f.par[f.P - 1];
 	__shared__ double sNorm[kFinWarps], sPrior[kFinWarps];
 	__shared__ int sLast;
+	gridDependencyWait();
+	gridDependencyTrigger();
+	const size_t ps = f.nBlocks;
 	double normv = 0., priorv = 0.;
 	if (g < nSlots) {
 		const int r = g / f.W, w = g - r * f.W;
@@ -453,8 +499,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 		double gre = 0., gim = 0.;
 		if (f.withGrad)
 			for (int b = lane; b < f.nBlocks; b += 32) {
-				gre += f.partials[(size_t)b * f.nPartial + 2 + 2 * g];
-				gim += f.partials[(size_t)b * f.nPartial + 3 + 2 * g];
+				gre += f.partials[(size_t)(2 + 2 * g) * ps + b];
+				gim += f.partials[(size_t)(3 + 2 * g) * ps + b];
 			}
 		// D_i = sum_j V_j conj(I_ij) over waves of the same reflectivity
 		const double* Ib = f.accI + (pos ? 2 * (size_t)f.W0 * f.W0 : 0) + 2 * (size_t)i * We;
@@ -494,8 +540,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 	} else if (g == nSlots) {
 		double ll = 0., cs = 0.;
 		for (int b = lane; b < f.nBlocks; b += 32) {
-			ll += f.partials[(size_t)b * f.nPartial + 0];
-			cs += f.partials[(size_t)b * f.nPartial + 1];
+			ll += f.partials[b];
+			cs += f.partials[ps + b];
 		}
 		ll = warpSumD(ll);
 		cs = warpSumD(cs);
@@ -577,9 +623,19 @@ int launchVariant(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 			return cudaCheck(e, "cudaFuncSetAttribute(fdf)");
 		configured = p.smemBytes;
 	}
-	kern<<<p.blocks, kThreads, p.smemBytes, s>>>(a, p.stages);
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(p.blocks);
+	cfg.blockDim = dim3(kThreads);
+	cfg.dynamicSmemBytes = p.smemBytes;
+	cfg.stream = s;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, a, p.stages);
 	countLaunches(1);
-	return cudaCheck(cudaGetLastError(), "fdf kernel launch");
+	return cudaCheck(e, "fdf kernel launch");
 }
 
 template <int R>
@@ -594,6 +650,8 @@ int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 		}
 	} else if (p.E == 64) {
 		switch (p.wpw) {
+		case 2: return launchVariant<R, 64, 2>(p, a, s);
+		case 4: return launchVariant<R, 64, 4>(p, a, s);
 		case 8: return launchVariant<R, 64, 8>(p, a, s);
 		case 14: return launchVariant<R, 64, 14>(p, a, s);
 		default: break;
@@ -604,8 +662,9 @@ int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 
 }  // namespace
 
-int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan)
+int planCandidates(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out)
 {
+	out->clear();
 	if (R < 1 || R > 4)
 		return setError(kErrUnsupported, "FdF kernel supports rank 1..4");
 	if (W < 1)
@@ -619,32 +678,36 @@ int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan*
 	else return setError(kErrUnsupported, "FdF kernel supports at most 224 waves");
 	if (R * wpw > 32)
 		return setError(kErrUnsupported, "rank x waves-per-warp beyond the compiled register budget");
-	// prefer E = 128 with >= 2 stages; fall back to E = 64
-	int E = (wpw <= 8) ? 128 : 64;
-	int stages = 0;
-	for (int tries = 0; tries < 2 && stages == 0; ++tries) {
-		for (int st = 4; st >= 2; --st) {
-			if (smemLayout(W, R, E, st).total + 512 <= maxSmem) {
-				stages = st;
+	const int tileSizes[2] = {128, 64};
+	for (int E : tileSizes) {
+		if (E == 128 && wpw > 8)
+			continue;  // no compiled variant
+		for (int st = 2; st <= 4; ++st) {
+			if (smemLayout(W, R, E, st).total + 1024 > maxSmem)
 				break;
-			}
-		}
-		if (stages == 0) {
-			if (E == 128 && wpw == 8) {
-				E = 64;
-			} else {
-				break;
-			}
+			FdfPlan p;
+			p.E = E;
+			p.stages = st;
+			p.wpw = wpw;
+			const uint64_t nTiles = (nEvents + E - 1) / E;
+			p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
+			p.smemBytes = smemLayout(W, R, E, st).total;
+			out->push_back(p);
 		}
 	}
-	if (stages == 0)
+	if (out->empty())
 		return setError(kErrUnsupported, "amplitude tile does not fit in shared memory");
-	plan->E = E;
-	plan->stages = stages;
-	plan->wpw = wpw;
-	const uint64_t nTiles = (nEvents + E - 1) / E;
-	plan->blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
-	plan->smemBytes = smemLayout(W, R, E, stages).total;
+	return kOk;
+}
+
+int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan)
+{
+	// default without tuning: the largest tile with two stages, else the deepest pipeline
+	std::vector<FdfPlan> c;
+	const int st = planCandidates(W, R, nEvents, numSMs, maxSmem, &c);
+	if (st != kOk)
+		return st;
+	*plan = c.front();
 	return kOk;
 }
 
@@ -663,9 +726,18 @@ int finalizeBlocks(int R, int W) { return (R * W + 1 + kFinWarps - 1) / kFinWarp
 
 int launchFinalize(const FinArgs& a, int finBlocks, cudaStream_t s)
 {
-	fdfFinalizeKernel<<<finBlocks, kFinWarps * 32, 0, s>>>(a);
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(finBlocks);
+	cfg.blockDim = dim3(kFinWarps * 32);
+	cfg.stream = s;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	const cudaError_t e = cudaLaunchKernelEx(&cfg, fdfFinalizeKernel, a);
 	countLaunches(1);
-	return cudaCheck(cudaGetLastError(), "fdf finalize launch");
+	return cudaCheck(e, "fdf finalize launch");
 }
 
 int launchConvertRow(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor, unsigned* nonzero,

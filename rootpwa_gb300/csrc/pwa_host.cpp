@@ -22,6 +22,7 @@
 #include <new>
 #include <sstream>
 #include <string>
+#include <tuple>
 #include <vector>
 
 typedef std::complex<double> cplx;
@@ -689,6 +690,7 @@ struct pwa_likelihood {
 	bool initialized = false, normAdded = false, accAdded = false, finished = false;
 
 	// evaluation resources
+	bool autotune = true;
 	FdfPlan plan;
 	int finBlocks = 0;
 	DevBuf dSlotRe, dSlotIm, dAccI, dPartials, dFinScratch, dTicket, dErr, dPar, dOut, dFlag;
@@ -881,6 +883,68 @@ int hostEval(pwa_likelihood* L, const double* par, double* f, double* grad, int 
 
 }  // namespace
 
+namespace {
+
+// Plans chosen by the autotuner, per (waves, negative waves, rank, event-count
+// class) in this process.
+struct TuneKey {
+	uint32_t W, W0, R, evClass;
+	bool operator<(const TuneKey& o) const
+	{
+		return std::tie(W, W0, R, evClass) < std::tie(o.W, o.W0, o.R, o.evClass);
+	}
+};
+std::map<TuneKey, std::pair<int, int> > g_tuned;  // -> (E, stages)
+
+// Times every candidate (tile size, pipeline depth) on the handle's own data
+// with a fixed parameter point and keeps the fastest.
+int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
+{
+	uint32_t evClass = 0;
+	for (uint64_t n = L->nEvents; n > 1; n >>= 1)
+		++evClass;
+	const TuneKey key{L->W(), L->nW[0], L->rank, evClass};
+	auto it = g_tuned.find(key);
+	if (it != g_tuned.end()) {
+		for (const auto& c : cands)
+			if (c.E == it->second.first && c.stages == it->second.second)
+				L->plan = c;
+		return kOk;
+	}
+	cudaStream_t s = L->stream;
+	std::vector<double> p(L->nPars, 0.5);
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dPar.p, p.data(), p.size() * sizeof(double), cudaMemcpyHostToDevice, s),
+	                  "autotune parameters"));
+	float best = 1e30f;
+	FdfPlan bestPlan = cands.front();
+	for (const auto& c : cands) {
+		L->plan = c;
+		for (int i = 0; i < 2; ++i)
+			PWA_TRY(launchEval(L, L->dPar.as<double>(), L->dOut.as<double>(), 1, s));
+		PWA_TRY(cudaCheck(cudaEventRecord(L->ev[0], s), "event"));
+		for (int i = 0; i < 5; ++i)
+			PWA_TRY(launchEval(L, L->dPar.as<double>(), L->dOut.as<double>(), 1, s));
+		PWA_TRY(cudaCheck(cudaEventRecord(L->ev[2], s), "event"));
+		PWA_TRY(cudaCheck(cudaEventSynchronize(L->ev[2]), "autotune sync"));
+		float ms = 0.f;
+		PWA_TRY(cudaCheck(cudaEventElapsedTime(&ms, L->ev[0], L->ev[2]), "elapsed"));
+		if (ms < best) {
+			best = ms;
+			bestPlan = c;
+		}
+	}
+	L->plan = bestPlan;
+	g_tuned[key] = std::make_pair(bestPlan.E, bestPlan.stages);
+	// the tuning runs leave no device error behind
+	unsigned err = 0;
+	PWA_TRY(cudaCheck(cudaMemcpy(&err, L->dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "error flag"));
+	if (err != 0)
+		return setError(kErrTimeout, "a bounded device-side wait expired while tuning the FdF kernel");
+	return kOk;
+}
+
+}  // namespace
+
 extern "C" {
 
 int pwa_likelihood_create(pwa_likelihood** out)
@@ -943,6 +1007,26 @@ int pwa_likelihood_set_stream(pwa_likelihood* L, void* s)
 	// NULL selects the CUDA default stream
 	L->ownStream = false;
 	L->stream = static_cast<cudaStream_t>(s);
+	return kOk;
+}
+
+int pwa_likelihood_set_autotune(pwa_likelihood* L, int enable)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	L->autotune = enable != 0;
+	return kOk;
+}
+
+int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, int* blocks)
+{
+	PWA_TRY(checkFinished(L));
+	if (tileEvents)
+		*tileEvents = L->plan.E;
+	if (stages)
+		*stages = L->plan.stages;
+	if (blocks)
+		*blocks = L->plan.blocks;
 	return kOk;
 }
 
@@ -1202,13 +1286,18 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	// device-side evaluation resources
 	PWA_TRY(ensureDevice(L));
 	const uint32_t W = L->W();
-	PWA_TRY(planFdf((int)W, (int)L->rank, L->nEvents, L->numSMs, L->maxSmem, &L->plan));
+	std::vector<FdfPlan> cands;
+	PWA_TRY(planCandidates((int)W, (int)L->rank, L->nEvents, L->numSMs, L->maxSmem, &cands));
+	L->plan = cands.front();
+	int maxBlocks = 1;
+	for (const auto& c : cands)
+		maxBlocks = std::max(maxBlocks, c.blocks);
 	L->finBlocks = finalizeBlocks((int)L->rank, (int)W);
 	const size_t nSlot = (size_t)L->rank * W;
 	const size_t nPartial = 2 + 2 * nSlot;
 	PWA_TRY(L->dSlotRe.alloc(nSlot * sizeof(int), "slot map"));
 	PWA_TRY(L->dSlotIm.alloc(nSlot * sizeof(int), "slot map"));
-	PWA_TRY(L->dPartials.alloc((size_t)L->plan.blocks * nPartial * sizeof(double), "partials"));
+	PWA_TRY(L->dPartials.alloc((size_t)maxBlocks * nPartial * sizeof(double), "partials"));
 	PWA_TRY(L->dFinScratch.alloc((size_t)(2 * L->finBlocks + 2) * sizeof(double), "finalize scratch"));
 	PWA_TRY(L->dTicket.alloc(sizeof(unsigned), "ticket"));
 	PWA_TRY(L->dErr.alloc(sizeof(unsigned), "error flag"));
@@ -1237,6 +1326,8 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dTicket.p, 0, sizeof(unsigned), s), "memset"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s), "memset"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "finishInit sync"));
+	if (L->autotune && cands.size() > 1 && L->nEvents >= 65536)
+		PWA_TRY(autotunePlan(L, cands));
 	L->finished = true;
 	return kOk;
 }

@@ -236,6 +236,16 @@ class pwaLikelihood:
         m = {"fp64": N.REDUCE_FP64, "kahan_fp32": N.REDUCE_KAHAN_FP32}[mode] if isinstance(mode, str) else int(mode)
         N.call("pwa_likelihood_set_reduction", self._h, m)
 
+    def setAutotune(self, enable=True):
+        """Time the compiled FdF kernel plans at finishInit and keep the fastest (default on)."""
+        N.call("pwa_likelihood_set_autotune", self._h, int(bool(enable)))
+
+    def plan(self):
+        """(events per tile, pipeline stages, grid blocks) of the FdF kernel in use."""
+        e, s, b = C.c_int(), C.c_int(), C.c_int()
+        N.call("pwa_likelihood_plan", self._h, C.byref(e), C.byref(s), C.byref(b))
+        return e.value, s.value, b.value
+
     # -- setup (order as _likelihood.py:17-71) -------------------------------
     def init(self, waveNames, reflectivities, thresholds=None, rank=1, massBinCenter=0.0):
         n = len(waveNames)

@@ -44,6 +44,16 @@ def gpu_integrals(w, precision="fp32"):
     return norm, acc
 
 
+def integral_pairs(w):
+    """(oracle norm, oracle acc, GPU norm, GPU acc) holding identical sums.
+
+    The GPU copies are taken before any likelihood sees the integrals: like
+    the reference, addAccIntegral overwrites the acceptance integral's event
+    count (pwaLikelihood.cc:1099-1101)."""
+    norm, acc = oracle_integrals(w)
+    return norm, acc, copy_oracle_integral_to_gpu(norm), copy_oracle_integral_to_gpu(acc)
+
+
 def copy_oracle_integral_to_gpu(oi):
     """Product integral object holding exactly the oracle's sums."""
     import rootpwa_gb300 as R

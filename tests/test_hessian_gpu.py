@@ -13,9 +13,9 @@ pytestmark = pytest.mark.gpu
 
 
 def pair(w, **kw):
-    norm, acc = helpers.oracle_integrals(w)
+    norm, acc, gn, ga = helpers.integral_pairs(w)
     O = helpers.build_oracle(w, norm, acc, **kw)
-    G = helpers.build_gpu(w, helpers.copy_oracle_integral_to_gpu(norm), helpers.copy_oracle_integral_to_gpu(acc), **kw)
+    G = helpers.build_gpu(w, gn, ga, **kw)
     return O, G
 
 
