@@ -150,7 +150,7 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
 // pair at most once per 256 bytes.
 struct SmemLayout {
 	size_t rowStride;  // bytes per wave row
-	size_t tiles, vs, ts, bars, done, total;
+	size_t tiles, vs, ts, tsw, bars, done, total;
 };
 
 __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
@@ -160,11 +160,56 @@ __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages
 	L.rowStride = (size_t)E * 8 + 8 * (size_t)(E / kWarps);
 	L.tiles = 0;
 	L.vs = up((size_t)stages * W * L.rowStride);
-	L.ts = up(L.vs + (size_t)W * R * 8);
-	L.bars = up(L.ts + 2 * (size_t)R * 2 * E * 8);
+	L.ts = up(L.vs + (size_t)W * R * 16);
+	L.tsw = up(L.ts + 2 * (size_t)R * 2 * E * 8);
+	L.bars = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
 	L.done = L.bars + (size_t)stages * 8;
 	L.total = L.done + (size_t)stages * 4;
 	return L;
+}
+
+// Phase-2 wave ownership: nNeg warps share the W0 negative-reflectivity
+// waves (wn each), the other warps the positive ones (wp each), so that every
+// warp works on one reflectivity only; returns the largest per-warp count.
+__host__ __device__ inline int waveSplit(int W0, int W, int* nNeg, int* wn, int* wp)
+{
+	const int W1 = W - W0;
+	int best = 1 << 30, bn = 0;
+	if (W0 == 0 || W1 == 0) {
+		bn = (W0 == 0) ? 0 : kWarps;
+		best = (W0 == 0) ? (W1 + kWarps - 1) / kWarps : (W0 + kWarps - 1) / kWarps;
+	} else {
+		for (int n = 1; n < kWarps; ++n) {
+			const int m = max((W0 + n - 1) / n, (W1 + kWarps - n - 1) / (kWarps - n));
+			if (m < best) {
+				best = m;
+				bn = n;
+			}
+		}
+	}
+	*nNeg = bn;
+	*wn = bn ? (W0 + bn - 1) / bn : 0;
+	*wp = (bn < kWarps) ? (W1 + kWarps - bn - 1) / (kWarps - bn) : 0;
+	return best;
+}
+
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
+{
+	float2 d;
+	asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+	    "mov.b64 ra, {%2, %3};\n\t"
+	    "mov.b64 rb, {%4, %5};\n\t"
+	    "mov.b64 rc, {%6, %7};\n\t"
+	    "fma.rn.f32x2 rd, ra, rb, rc;\n\t"
+	    "mov.b64 {%0, %1}, rd;\n\t}"
+	    : "=f"(d.x), "=f"(d.y)
+	    : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+	return d;
+}
+
+__device__ __forceinline__ void prefetchL2(const void* src, uint32_t bytes)
+{
+	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
 // Tiles whose gradient partials are summed in FP32 before the warp
@@ -188,8 +233,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	const SmemLayout lay = smemLayout(W, R, E, stages);
 	const int rowF2 = (int)(lay.rowStride / 8);  // row stride in float2
 	float2* tiles = reinterpret_cast<float2*>(smem + lay.tiles);
-	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);
-	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);  // [2][R][2][E]
+	float4* V4 = reinterpret_cast<float4*>(smem + lay.vs);      // [W][R] (vx, vx, vy, vy)
+	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);      // [2][R][2][E] c S
+	float2* Tsw = reinterpret_cast<float2*>(smem + lay.tsw);    // [2][R][2][E] c S, re/im swapped
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	unsigned* done = reinterpret_cast<unsigned*>(smem + lay.done);
 	__shared__ double redLL[kWarps], redC[kWarps];
@@ -197,11 +243,11 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	// the parameters may be written by the preceding grid (device-side minimiser)
 	gridDependencyWait();
 	gridDependencyTrigger();
-	// production amplitudes V[w][r] as FP32 complex
 	for (int k = tid; k < W * R; k += kThreads) {
 		const int w = k / R, r = k - w * R;
 		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
-		Vs[k] = make_float2(ir >= 0 ? (float)a.par[ir] : 0.f, ii >= 0 ? (float)a.par[ii] : 0.f);
+		const float vx = ir >= 0 ? (float)a.par[ir] : 0.f, vy = ii >= 0 ? (float)a.par[ii] : 0.f;
+		V4[k] = make_float4(vx, vx, vy, vy);
 	}
 	const double flatD = a.par[a.P - 1];
 	const float flat2 = (float)(flatD * flatD);
@@ -221,6 +267,14 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	}
 	__syncthreads();
 
+	// L2 prefetch of tile k (rows spread over the lanes of one warp)
+	auto prefetch = [&](uint64_t k) {
+		if (k < myTiles) {
+			const uint64_t e0 = (first + k * stride) * (uint64_t)E;
+			for (int w = lane; w < W; w += 32)
+				prefetchL2(a.amps + (size_t)w * a.nPad + e0, rowBytes);
+		}
+	};
 	// issue tile k (local index) into stage s; executed by all lanes of one warp
 	auto issue = [&](uint64_t k, int s) {
 		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
@@ -234,16 +288,20 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	if (warp == 0) {
 		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
 			issue((uint64_t)s, s);
+		prefetch((uint64_t)stages);
 	}
 
 	// phase-1 role: event pe of the tile, wave slice ph (waves w = ph mod H)
 	const int pm = lane / H, ph = lane - pm * H;
 	const int pe = warp * EPW + pm;
 	const int wStart1 = W0 + (((ph - W0) % H) + H) % H;  // first positive-reflectivity wave of this slice
-	// phase-2 role: warp owns waves [wBase, wBase + nWarpWaves)
-	const int wpwa = (W + kWarps - 1) / kWarps;
-	const int wBase = warp * wpwa;
-	const int nWarpWaves = max(0, min(wpwa, W - wBase));
+	// phase-2 role: the warp owns waves [wBase, wBase + nWarpWaves) of reflectivity wRefl
+	int nNegWarps, wn, wp;
+	waveSplit(W0, W, &nNegWarps, &wn, &wp);
+	const int wRefl = (warp < nNegWarps) ? 0 : 1;
+	const int wBase = wRefl == 0 ? warp * wn : W0 + (warp - nNegWarps) * wp;
+	const int wEnd = wRefl == 0 ? min(W0, wBase + wn) : min(W, wBase + wp);
+	const int nWarpWaves = max(0, wEnd - wBase);
 
 	double accLL = 0., accC = 0.;
 	float kLL = 0.f, kLLc = 0.f, kC = 0.f, kCc = 0.f;
@@ -256,10 +314,15 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		kG[q] = 0.f;
 		kGc[q] = 0.f;
 	}
-	float part[NVP];
+	// P = sum a (.) t, Q = sum a (.) t_swapped  ->  G = (P.x + P.y, Q.x - Q.y)
+	float2 Pp[WPW][R], Qp[WPW][R];
 #pragma unroll
-	for (int v = 0; v < NVP; ++v)
-		part[v] = 0.f;
+	for (int wi = 0; wi < WPW; ++wi)
+#pragma unroll
+		for (int r = 0; r < R; ++r) {
+			Pp[wi][r] = make_float2(0.f, 0.f);
+			Qp[wi][r] = make_float2(0.f, 0.f);
+		}
 
 	bool failed = false;
 	uint64_t k = 0;
@@ -270,38 +333,47 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		const float2* tile = tiles + (size_t)s * W * rowF2;
 		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
 		float2* T = Ts + (size_t)(k & 1ull) * R * 2 * E;
+		float2* Tw = Tsw + (size_t)(k & 1ull) * R * 2 * E;
 
 		// ---- phase 1: coherent sums, combined across the H lanes of an event ----
 		{
-			float2 S[R][2];
+			// X = sum (vx, vx) (.) a, Y = sum (vy, vy) (.) a  ->  S = (X.x - Y.y, X.y + Y.x)
+			float2 X[R][2], Y[R][2];
 #pragma unroll
-			for (int r = 0; r < R; ++r) {
-				S[r][0] = make_float2(0.f, 0.f);
-				S[r][1] = make_float2(0.f, 0.f);
-			}
+			for (int r = 0; r < R; ++r)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					X[r][e] = make_float2(0.f, 0.f);
+					Y[r][e] = make_float2(0.f, 0.f);
+				}
+			const float2* col = tile + pe;
+#pragma unroll 4
 			for (int w = ph; w < W0; w += H) {
-				const float2 av = tile[(size_t)w * rowF2 + pe];
+				const float2 av = col[(size_t)w * rowF2];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					const float2 v = Vs[w * R + r];
-					S[r][0].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, S[r][0].x));
-					S[r][0].y = fmaf(v.x, av.y, fmaf(v.y, av.x, S[r][0].y));
+					const float4 v = V4[w * R + r];
+					X[r][0] = ffma2(make_float2(v.x, v.y), av, X[r][0]);
+					Y[r][0] = ffma2(make_float2(v.z, v.w), av, Y[r][0]);
 				}
 			}
+#pragma unroll 4
 			for (int w = wStart1; w < W; w += H) {
-				const float2 av = tile[(size_t)w * rowF2 + pe];
+				const float2 av = col[(size_t)w * rowF2];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					const float2 v = Vs[w * R + r];
-					S[r][1].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, S[r][1].x));
-					S[r][1].y = fmaf(v.x, av.y, fmaf(v.y, av.x, S[r][1].y));
+					const float4 v = V4[w * R + r];
+					X[r][1] = ffma2(make_float2(v.x, v.y), av, X[r][1]);
+					Y[r][1] = ffma2(make_float2(v.z, v.w), av, Y[r][1]);
 				}
 			}
+			float2 S[R][2];
 			float L = flat2;
 #pragma unroll
 			for (int r = 0; r < R; ++r)
 #pragma unroll
 				for (int e = 0; e < 2; ++e) {
+					S[r][e] = make_float2(X[r][e].x - Y[r][e].y, X[r][e].y + Y[r][e].x);
 #pragma unroll
 					for (int o = 1; o < H; o <<= 1) {
 						S[r][e].x += __shfl_xor_sync(0xffffffffu, S[r][e].x, o);
@@ -319,8 +391,11 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 #pragma unroll
 					for (int r = 0; r < R; ++r)
 #pragma unroll
-						for (int e = 0; e < 2; ++e)
-							T[(r * 2 + e) * E + pe] = make_float2(c * S[r][e].x, c * S[r][e].y);
+						for (int e = 0; e < 2; ++e) {
+							const float tx = c * S[r][e].x, ty = c * S[r][e].y;
+							T[(r * 2 + e) * E + pe] = make_float2(tx, ty);
+							Tw[(r * 2 + e) * E + pe] = make_float2(ty, tx);
+						}
 				}
 			}
 		}
@@ -330,39 +405,28 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			break;
 		}
 
-		// ---- phase 2: gradient contraction over the tile ----
+		// ---- phase 2: gradient contraction over the tile, one reflectivity per warp ----
 		if (a.withGrad) {
 #pragma unroll
 			for (int pp = 0; pp < EPAIRS; ++pp) {
 				const int ev = 2 * lane + 64 * pp;
-				float4 t[R][2];
+				float4 t[R], tw[R];
 #pragma unroll
-				for (int r = 0; r < R; ++r)
-#pragma unroll
-					for (int e = 0; e < 2; ++e)
-						t[r][e] = *reinterpret_cast<const float4*>(&T[(r * 2 + e) * E + ev]);
+				for (int r = 0; r < R; ++r) {
+					t[r] = *reinterpret_cast<const float4*>(&T[(r * 2 + wRefl) * E + ev]);
+					tw[r] = *reinterpret_cast<const float4*>(&Tw[(r * 2 + wRefl) * E + ev]);
+				}
 #pragma unroll
 				for (int wi = 0; wi < WPW; ++wi) {
 					if (wi < nWarpWaves) {
-						const int w = wBase + wi;
-						const float4 av = *reinterpret_cast<const float4*>(&tile[(size_t)w * rowF2 + ev]);
-						const bool pos = (w >= W0);
+						const float4 av = *reinterpret_cast<const float4*>(&tile[(size_t)(wBase + wi) * rowF2 + ev]);
+						const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
 #pragma unroll
 						for (int r = 0; r < R; ++r) {
-							const float4 tt = pos ? t[r][1] : t[r][0];
-							// conj(a0) t0 + conj(a1) t1
-							float re = part[(wi * R + r) * 2 + 0];
-							float im = part[(wi * R + r) * 2 + 1];
-							re = fmaf(av.x, tt.x, re);
-							re = fmaf(av.y, tt.y, re);
-							re = fmaf(av.z, tt.z, re);
-							re = fmaf(av.w, tt.w, re);
-							im = fmaf(av.x, tt.y, im);
-							im = fmaf(-av.y, tt.x, im);
-							im = fmaf(av.z, tt.w, im);
-							im = fmaf(-av.w, tt.z, im);
-							part[(wi * R + r) * 2 + 0] = re;
-							part[(wi * R + r) * 2 + 1] = im;
+							Pp[wi][r] = ffma2(a0, make_float2(t[r].x, t[r].y), Pp[wi][r]);
+							Pp[wi][r] = ffma2(a1, make_float2(t[r].z, t[r].w), Pp[wi][r]);
+							Qp[wi][r] = ffma2(a0, make_float2(tw[r].x, tw[r].y), Qp[wi][r]);
+							Qp[wi][r] = ffma2(a1, make_float2(tw[r].z, tw[r].w), Qp[wi][r]);
 						}
 					}
 				}
@@ -370,7 +434,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		}
 
 		// stage s is no longer read by this warp; the last warp to finish
-		// with it refills it with tile k + stages
+		// with it refills it with tile k + stages and prefetches the next one
 		__syncwarp();
 		unsigned prev = 0;
 		if (lane == 0) {
@@ -384,6 +448,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			if (k + (uint64_t)stages < myTiles) {
 				fenceProxyAsync();
 				issue(k + (uint64_t)stages, s);
+				prefetch(k + (uint64_t)stages + 1);
 			}
 		}
 
@@ -402,6 +467,19 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				}
 			}
 			if (a.withGrad) {
+				float part[NVP];
+#pragma unroll
+				for (int wi = 0; wi < WPW; ++wi)
+#pragma unroll
+					for (int r = 0; r < R; ++r) {
+						part[(wi * R + r) * 2 + 0] = Pp[wi][r].x + Pp[wi][r].y;
+						part[(wi * R + r) * 2 + 1] = Qp[wi][r].x - Qp[wi][r].y;
+						Pp[wi][r] = make_float2(0.f, 0.f);
+						Qp[wi][r] = make_float2(0.f, 0.f);
+					}
+#pragma unroll
+				for (int v = NV; v < NVP; ++v)
+					part[v] = 0.f;
 #pragma unroll
 				for (int q = 0; q < NQ; ++q) {
 					const float v = reduceScatter32(&part[q * 32], lane);
@@ -410,9 +488,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					else
 						kahanAdd(kG[q], kGc[q], v);
 				}
-#pragma unroll
-				for (int v = 0; v < NVP; ++v)
-					part[v] = 0.f;
 			}
 		}
 	}
@@ -645,6 +720,7 @@ int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 		switch (p.wpw) {
 		case 2: return launchVariant<R, 128, 2>(p, a, s);
 		case 4: return launchVariant<R, 128, 4>(p, a, s);
+		case 6: return launchVariant<R, 128, 6>(p, a, s);
 		case 8: return launchVariant<R, 128, 8>(p, a, s);
 		default: break;
 		}
@@ -652,6 +728,7 @@ int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 		switch (p.wpw) {
 		case 2: return launchVariant<R, 64, 2>(p, a, s);
 		case 4: return launchVariant<R, 64, 4>(p, a, s);
+		case 6: return launchVariant<R, 64, 6>(p, a, s);
 		case 8: return launchVariant<R, 64, 8>(p, a, s);
 		case 14: return launchVariant<R, 64, 14>(p, a, s);
 		default: break;
@@ -662,17 +739,19 @@ int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 
 }  // namespace
 
-int planCandidates(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out)
+int planCandidates(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out)
 {
 	out->clear();
 	if (R < 1 || R > 4)
 		return setError(kErrUnsupported, "FdF kernel supports rank 1..4");
 	if (W < 1)
 		return setError(kErrArg, "no waves");
-	const int wpwa = (W + kWarps - 1) / kWarps;
+	int nNeg, wn, wp;
+	const int wpwa = waveSplit(W0, W, &nNeg, &wn, &wp);
 	int wpw;
 	if (wpwa <= 2) wpw = 2;
 	else if (wpwa <= 4) wpw = 4;
+	else if (wpwa <= 6) wpw = 6;
 	else if (wpwa <= 8) wpw = 8;
 	else if (wpwa <= 14) wpw = 14;
 	else return setError(kErrUnsupported, "FdF kernel supports at most 224 waves");
@@ -700,11 +779,11 @@ int planCandidates(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, s
 	return kOk;
 }
 
-int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan)
+int planFdf(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan)
 {
 	// default without tuning: the largest tile with two stages, else the deepest pipeline
 	std::vector<FdfPlan> c;
-	const int st = planCandidates(W, R, nEvents, numSMs, maxSmem, &c);
+	const int st = planCandidates(W0, W, R, nEvents, numSMs, maxSmem, &c);
 	if (st != kOk)
 		return st;
 	*plan = c.front();

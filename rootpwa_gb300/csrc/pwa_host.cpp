@@ -1287,7 +1287,7 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	PWA_TRY(ensureDevice(L));
 	const uint32_t W = L->W();
 	std::vector<FdfPlan> cands;
-	PWA_TRY(planCandidates((int)W, (int)L->rank, L->nEvents, L->numSMs, L->maxSmem, &cands));
+	PWA_TRY(planCandidates((int)L->nW[0], (int)W, (int)L->rank, L->nEvents, L->numSMs, L->maxSmem, &cands));
 	L->plan = cands.front();
 	int maxBlocks = 1;
 	for (const auto& c : cands)

@@ -82,9 +82,9 @@ struct FinArgs {
 
 // Chooses tile size, pipeline depth and grid; returns kErrUnsupported for
 // shapes outside the compiled variants.
-int planFdf(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan);
+int planFdf(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan);
 // All compiled (tile size, pipeline depth) plans that fit, for the autotuner.
-int planCandidates(int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out);
+int planCandidates(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out);
 int launchFdf(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
 int launchFinalize(const FinArgs& args, int finBlocks, cudaStream_t s);
 int finalizeBlocks(int R, int W);
