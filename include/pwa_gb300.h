@@ -152,12 +152,14 @@ int pwa_likelihood_set_stream(pwa_likelihood* L, void* cudaStream);
 int pwa_likelihood_set_reduction(pwa_likelihood* L, int reduction);
 /* autotuner (no reference counterpart; the reference's CUDA path sized its
  * grid by an occupancy heuristic, cuda/likelihoodInterface.cu:304-360):
- * when enabled (default), finishInit times every compiled (tile size,
- * pipeline depth) plan of the FdF kernel on the handle's data and keeps the
- * fastest; the choice is cached per shape for the process.  pwa_likelihood_plan
- * reports the plan in use. */
+ * when enabled (default), finishInit times every compiled pipeline depth of
+ * the FdF kernel on the handle's data and keeps the fastest; the choice is
+ * cached per shape for the process.  pwa_likelihood_plan reports the plan in
+ * use (events per tile = the amplitude store's block size, 128 or 64). */
 int pwa_likelihood_set_autotune(pwa_likelihood* L, int enable);
 int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, int* blocks);
+/* selects the pipeline depth by hand after finishInit (2..4 as shared memory allows) */
+int pwa_likelihood_set_plan(pwa_likelihood* L, int stages);
 /*
  * init (pwaLikelihood.cc:1050-1063 with readWaveList :1443-1484 and
  * buildParDataStruct :1487-1556).  The reference takes wave descriptions and

@@ -144,10 +144,8 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
 }
 
 // Shared-memory layout of the main kernel (byte offsets from the dynamic base).
-// A tile holds W rows of E complex64 amplitudes; rows are padded by
-// 8 * (E / kWarps) bytes so that the phase-1 access (lanes split over
-// 32 / (E / kWarps) wave slices and E / kWarps events) touches every bank
-// pair at most once per 256 bytes.
+// A stage holds one store block: W rows of E complex64 amplitudes, in the
+// store's rotated order (storeIndex), moved by a single bulk copy.
 struct SmemLayout {
 	size_t rowStride;  // bytes per wave row
 	size_t tiles, vs, ts, tsw, bars, done, total;
@@ -157,10 +155,10 @@ __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages
 {
 	auto up = [](size_t x) { return (x + 127) & ~(size_t)127; };
 	SmemLayout L;
-	L.rowStride = (size_t)E * 8 + 8 * (size_t)(E / kWarps);
+	L.rowStride = (size_t)E * 8;
 	L.tiles = 0;
 	L.vs = up((size_t)stages * W * L.rowStride);
-	L.ts = up(L.vs + (size_t)W * R * 16);
+	L.ts = up(L.vs + (size_t)W * R * 8);
 	L.tsw = up(L.ts + 2 * (size_t)R * 2 * E * 8);
 	L.bars = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
 	L.done = L.bars + (size_t)stages * 8;
@@ -207,9 +205,18 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
 	return d;
 }
 
-__device__ __forceinline__ void prefetchL2(const void* src, uint32_t bytes)
+// shared-memory loads through 32-bit shared-window addresses
+__device__ __forceinline__ float2 lds64(uint32_t addr)
 {
-	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+	float2 v;
+	asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+	return v;
+}
+__device__ __forceinline__ float4 lds128(uint32_t addr)
+{
+	float4 v;
+	asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+	return v;
 }
 
 // Tiles whose gradient partials are summed in FP32 before the warp
@@ -231,9 +238,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const int W = a.W, W0 = a.W0;
 	const SmemLayout lay = smemLayout(W, R, E, stages);
-	const int rowF2 = (int)(lay.rowStride / 8);  // row stride in float2
 	float2* tiles = reinterpret_cast<float2*>(smem + lay.tiles);
-	float4* V4 = reinterpret_cast<float4*>(smem + lay.vs);      // [W][R] (vx, vx, vy, vy)
+	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);      // [W][R] (vx, vy)
 	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);      // [2][R][2][E] c S
 	float2* Tsw = reinterpret_cast<float2*>(smem + lay.tsw);    // [2][R][2][E] c S, re/im swapped
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
@@ -246,8 +252,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	for (int k = tid; k < W * R; k += kThreads) {
 		const int w = k / R, r = k - w * R;
 		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
-		const float vx = ir >= 0 ? (float)a.par[ir] : 0.f, vy = ii >= 0 ? (float)a.par[ii] : 0.f;
-		V4[k] = make_float4(vx, vx, vy, vy);
+		Vs[k] = make_float2(ir >= 0 ? (float)a.par[ir] : 0.f, ii >= 0 ? (float)a.par[ii] : 0.f);
 	}
 	const double flatD = a.par[a.P - 1];
 	const float flat2 = (float)(flatD * flatD);
@@ -255,8 +260,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	const uint64_t nTiles = (a.nEvents + E - 1) / E;
 	const uint64_t first = blockIdx.x, stride = gridDim.x;
 	const uint64_t myTiles = (first < nTiles) ? (nTiles - 1 - first) / stride + 1 : 0;
-	const uint32_t rowBytes = E * 8u;
-	const uint32_t stageBytes = (uint32_t)W * rowBytes;
+	const uint32_t stageBytes = (uint32_t)W * E * 8u;
 
 	if (tid == 0) {
 		for (int s = 0; s < stages; ++s) {
@@ -267,28 +271,17 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	}
 	__syncthreads();
 
-	// L2 prefetch of tile k (rows spread over the lanes of one warp)
-	auto prefetch = [&](uint64_t k) {
-		if (k < myTiles) {
-			const uint64_t e0 = (first + k * stride) * (uint64_t)E;
-			for (int w = lane; w < W; w += 32)
-				prefetchL2(a.amps + (size_t)w * a.nPad + e0, rowBytes);
-		}
-	};
-	// issue tile k (local index) into stage s; executed by all lanes of one warp
+	// issue store block (tile) k (local index) into stage s: one bulk copy
 	auto issue = [&](uint64_t k, int s) {
-		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
-		float2* dst = tiles + (size_t)s * W * rowF2;
-		if (lane == 0)
+		if (lane == 0) {
+			const float2* src = a.amps + (first + k * stride) * (uint64_t)W * E;
 			mbarArriveExpectTx(&bars[s], stageBytes);
-		__syncwarp();
-		for (int w = lane; w < W; w += 32)
-			bulkCopyG2S(dst + (size_t)w * rowF2, a.amps + (size_t)w * a.nPad + e0, rowBytes, &bars[s]);
+			bulkCopyG2S(tiles + (size_t)s * W * E, src, stageBytes, &bars[s]);
+		}
 	};
 	if (warp == 0) {
 		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
 			issue((uint64_t)s, s);
-		prefetch((uint64_t)stages);
 	}
 
 	// phase-1 role: event pe of the tile, wave slice ph (waves w = ph mod H)
@@ -330,41 +323,42 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		const int s = (int)(k % (uint64_t)stages);
 		const uint32_t parity = (uint32_t)((k / (uint64_t)stages) & 1ull);
 		const bool timedOut = !mbarWaitBounded(&bars[s], parity);
-		const float2* tile = tiles + (size_t)s * W * rowF2;
+		const float2* tile = tiles + (size_t)s * W * E;
 		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
 		float2* T = Ts + (size_t)(k & 1ull) * R * 2 * E;
 		float2* Tw = Tsw + (size_t)(k & 1ull) * R * 2 * E;
 
 		// ---- phase 1: coherent sums, combined across the H lanes of an event ----
 		{
-			// X = sum (vx, vx) (.) a, Y = sum (vy, vy) (.) a  ->  S = (X.x - Y.y, X.y + Y.x)
-			float2 X[R][2], Y[R][2];
+			float2 Sa[R][2];
 #pragma unroll
-			for (int r = 0; r < R; ++r)
-#pragma unroll
-				for (int e = 0; e < 2; ++e) {
-					X[r][e] = make_float2(0.f, 0.f);
-					Y[r][e] = make_float2(0.f, 0.f);
-				}
-			const float2* col = tile + pe;
+			for (int r = 0; r < R; ++r) {
+				Sa[r][0] = make_float2(0.f, 0.f);
+				Sa[r][1] = make_float2(0.f, 0.f);
+			}
+			// every row this lane reads has the same rotation (w = ph mod H)
+			const int rot1 = EPW * (ph % (16 / EPW));
+			const uint32_t colAddr = smemAddr(tile + ((pe + rot1) & (E - 1)));
+			const uint32_t vAddr = smemAddr(Vs);
+			const uint32_t rowB = (uint32_t)lay.rowStride;
 #pragma unroll 4
 			for (int w = ph; w < W0; w += H) {
-				const float2 av = col[(size_t)w * rowF2];
+				const float2 av = lds64(colAddr + (uint32_t)w * rowB);
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					const float4 v = V4[w * R + r];
-					X[r][0] = ffma2(make_float2(v.x, v.y), av, X[r][0]);
-					Y[r][0] = ffma2(make_float2(v.z, v.w), av, Y[r][0]);
+					const float2 v = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
+					Sa[r][0].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, Sa[r][0].x));
+					Sa[r][0].y = fmaf(v.x, av.y, fmaf(v.y, av.x, Sa[r][0].y));
 				}
 			}
 #pragma unroll 4
 			for (int w = wStart1; w < W; w += H) {
-				const float2 av = col[(size_t)w * rowF2];
+				const float2 av = lds64(colAddr + (uint32_t)w * rowB);
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					const float4 v = V4[w * R + r];
-					X[r][1] = ffma2(make_float2(v.x, v.y), av, X[r][1]);
-					Y[r][1] = ffma2(make_float2(v.z, v.w), av, Y[r][1]);
+					const float2 v = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
+					Sa[r][1].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, Sa[r][1].x));
+					Sa[r][1].y = fmaf(v.x, av.y, fmaf(v.y, av.x, Sa[r][1].y));
 				}
 			}
 			float2 S[R][2];
@@ -373,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			for (int r = 0; r < R; ++r)
 #pragma unroll
 				for (int e = 0; e < 2; ++e) {
-					S[r][e] = make_float2(X[r][e].x - Y[r][e].y, X[r][e].y + Y[r][e].x);
+					S[r][e] = Sa[r][e];
 #pragma unroll
 					for (int o = 1; o < H; o <<= 1) {
 						S[r][e].x += __shfl_xor_sync(0xffffffffu, S[r][e].x, o);
@@ -413,13 +407,16 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				float4 t[R], tw[R];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					t[r] = *reinterpret_cast<const float4*>(&T[(r * 2 + wRefl) * E + ev]);
-					tw[r] = *reinterpret_cast<const float4*>(&Tw[(r * 2 + wRefl) * E + ev]);
+					t[r] = lds128(smemAddr(&T[(r * 2 + wRefl) * E + ev]));
+					tw[r] = lds128(smemAddr(&Tw[(r * 2 + wRefl) * E + ev]));
 				}
+				const uint32_t tAddr = smemAddr(tile);
 #pragma unroll
 				for (int wi = 0; wi < WPW; ++wi) {
 					if (wi < nWarpWaves) {
-						const float4 av = *reinterpret_cast<const float4*>(&tile[(size_t)(wBase + wi) * rowF2 + ev]);
+						const int w = wBase + wi;
+						const int pos = (ev + EPW * (w % (16 / EPW))) & (E - 1);
+						const float4 av = lds128(tAddr + (uint32_t)(w * E + pos) * 8u);
 						const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
 #pragma unroll
 						for (int r = 0; r < R; ++r) {
@@ -434,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		}
 
 		// stage s is no longer read by this warp; the last warp to finish
-		// with it refills it with tile k + stages and prefetches the next one
+		// with it refills it with tile k + stages
 		__syncwarp();
 		unsigned prev = 0;
 		if (lane == 0) {
@@ -448,7 +445,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			if (k + (uint64_t)stages < myTiles) {
 				fenceProxyAsync();
 				issue(k + (uint64_t)stages, s);
-				prefetch(k + (uint64_t)stages + 1);
 			}
 		}
 
@@ -556,12 +552,18 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 	const int g = blockIdx.x * kFinWarps + warp;
 	const int nSlots = f.R * f.W;
 	const double twice = 2. * f.nEvt;
-	const double flat = f.par[f.P - 1];
 	__shared__ double sNorm[kFinWarps], sPrior[kFinWarps];
 	__shared__ int sLast;
+	extern __shared__ double2 sV[];  // [R * W] production amplitudes (FP64)
 	gridDependencyWait();
 	gridDependencyTrigger();
+	const double flat = f.par[f.P - 1];
 	const size_t ps = f.nBlocks;
+	for (int k = threadIdx.x; k < nSlots; k += blockDim.x) {
+		const int kr = f.slotRe[k], ki = f.slotIm[k];
+		sV[k] = make_double2(kr >= 0 ? f.par[kr] : 0., ki >= 0 ? f.par[ki] : 0.);
+	}
+	__syncthreads();
 	double normv = 0., priorv = 0.;
 	if (g < nSlots) {
 		const int r = g / f.W, w = g - r * f.W;
@@ -570,7 +572,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 		const int We = pos ? f.W - f.W0 : f.W0;
 		const int i = w - off;
 		const int ire = f.slotRe[g], iim = f.slotIm[g];
-		const double vr = ire >= 0 ? f.par[ire] : 0., vi = iim >= 0 ? f.par[iim] : 0.;
+		const double vr = sV[g].x, vi = sV[g].y;
 		double gre = 0., gim = 0.;
 		if (f.withGrad)
 			for (int b = lane; b < f.nBlocks; b += 32) {
@@ -581,9 +583,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 		const double* Ib = f.accI + (pos ? 2 * (size_t)f.W0 * f.W0 : 0) + 2 * (size_t)i * We;
 		double dre = 0., dim = 0.;
 		for (int j = lane; j < We; j += 32) {
-			const int sj = r * f.W + off + j;
-			const int jr = f.slotRe[sj], ji = f.slotIm[sj];
-			const double ur = jr >= 0 ? f.par[jr] : 0., ui = ji >= 0 ? f.par[ji] : 0.;
+			const double2 u = sV[r * f.W + off + j];
+			const double ur = u.x, ui = u.y;
 			const double Ir = Ib[2 * j], Ii = Ib[2 * j + 1];
 			dre += ur * Ir + ui * Ii;
 			dim += ui * Ir - ur * Ii;
@@ -663,8 +664,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArg
 	}
 }
 
-__global__ void convertRowKernel(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor,
-                                 unsigned* nonzero)
+__global__ void convertRowKernel(const void* src, int srcIsDouble, float2* store, uint32_t W, uint32_t w, uint32_t B,
+                                 uint64_t n, double divisor, unsigned* nonzero)
 {
 	bool any = false;
 	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -679,10 +680,18 @@ __global__ void convertRowKernel(const void* src, int srcIsDouble, float2* dst, 
 			im = v.y;
 		}
 		any = any || re != 0. || im != 0.;
-		dst[i] = make_float2((float)(re / divisor), (float)(im / divisor));
+		store[storeIndex(w, i, W, B)] = make_float2((float)(re / divisor), (float)(im / divisor));
 	}
 	if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0)
 		atomicOr(nonzero, 1u);
+}
+
+__global__ void convertPlainKernel(const double2* src, float2* dst, uint64_t n)
+{
+	for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+		const double2 v = src[i];
+		dst[i] = make_float2((float)v.x, (float)v.y);
+	}
 }
 
 template <int R, int E, int WPW>
@@ -739,7 +748,13 @@ int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 
 }  // namespace
 
-int planCandidates(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out)
+int chooseStoreBlock(int W, int R, size_t maxSmem)
+{
+	return (smemLayout(W, R, 128, 2).total + 1024 <= maxSmem) ? 128 : 64;
+}
+
+int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, size_t maxSmem,
+                   std::vector<FdfPlan>* out)
 {
 	out->clear();
 	if (R < 1 || R > 4)
@@ -757,36 +772,25 @@ int planCandidates(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t ma
 	else return setError(kErrUnsupported, "FdF kernel supports at most 224 waves");
 	if (R * wpw > 32)
 		return setError(kErrUnsupported, "rank x waves-per-warp beyond the compiled register budget");
-	const int tileSizes[2] = {128, 64};
-	for (int E : tileSizes) {
-		if (E == 128 && wpw > 8)
-			continue;  // no compiled variant
-		for (int st = 2; st <= 4; ++st) {
-			if (smemLayout(W, R, E, st).total + 1024 > maxSmem)
-				break;
-			FdfPlan p;
-			p.E = E;
-			p.stages = st;
-			p.wpw = wpw;
-			const uint64_t nTiles = (nEvents + E - 1) / E;
-			p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
-			p.smemBytes = smemLayout(W, R, E, st).total;
-			out->push_back(p);
-		}
+	if (B != 128 && B != 64)
+		return setError(kErrArg, "store block must be 64 or 128 events");
+	for (int st = 1; st <= 4; ++st) {
+		if (smemLayout(W, R, B, st).total + 1024 > maxSmem)
+			break;
+		FdfPlan p;
+		p.E = B;
+		p.stages = st;
+		p.wpw = wpw;
+		const uint64_t nTiles = (nEvents + B - 1) / B;
+		p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
+		p.smemBytes = smemLayout(W, R, B, st).total;
+		out->push_back(p);
 	}
 	if (out->empty())
 		return setError(kErrUnsupported, "amplitude tile does not fit in shared memory");
-	return kOk;
-}
-
-int planFdf(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan)
-{
-	// default without tuning: the largest tile with two stages, else the deepest pipeline
-	std::vector<FdfPlan> c;
-	const int st = planCandidates(W0, W, R, nEvents, numSMs, maxSmem, &c);
-	if (st != kOk)
-		return st;
-	*plan = c.front();
+	// a single stage does not overlap copy and compute: drop it when deeper pipelines fit
+	if (out->size() > 1)
+		out->erase(out->begin());
 	return kOk;
 }
 
@@ -799,6 +803,15 @@ int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 	case 4: return launchR<4>(p, a, s);
 	default: return setError(kErrUnsupported, "FdF kernel supports rank 1..4");
 	}
+}
+
+int launchConvertPlain(const void* src, float2* dst, uint64_t n, cudaStream_t s)
+{
+	const int threads = 256;
+	const int blocks = (int)std::min<uint64_t>((n + threads - 1) / threads, 4096);
+	convertPlainKernel<<<std::max(blocks, 1), threads, 0, s>>>(static_cast<const double2*>(src), dst, n);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "convert launch");
 }
 
 int finalizeBlocks(int R, int W) { return (R * W + 1 + kFinWarps - 1) / kFinWarps; }
@@ -814,17 +827,18 @@ int launchFinalize(const FinArgs& a, int finBlocks, cudaStream_t s)
 	attr[0].val.programmaticStreamSerializationAllowed = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
+	cfg.dynamicSmemBytes = (size_t)a.R * a.W * sizeof(double2);
 	const cudaError_t e = cudaLaunchKernelEx(&cfg, fdfFinalizeKernel, a);
 	countLaunches(1);
 	return cudaCheck(e, "fdf finalize launch");
 }
 
-int launchConvertRow(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor, unsigned* nonzero,
-                     cudaStream_t s)
+int launchConvertRow(const void* src, int srcIsDouble, float2* store, uint32_t W, uint32_t w, uint32_t B, uint64_t n,
+                     double divisor, unsigned* nonzero, cudaStream_t s)
 {
 	const int threads = 256;
 	const int blocks = (int)std::min<uint64_t>((n + threads - 1) / threads, 4096);
-	convertRowKernel<<<std::max(blocks, 1), threads, 0, s>>>(src, srcIsDouble, dst, n, divisor, nonzero);
+	convertRowKernel<<<std::max(blocks, 1), threads, 0, s>>>(src, srcIsDouble, store, W, w, B, n, divisor, nonzero);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "convert row launch");
 }

@@ -22,7 +22,7 @@ namespace {
 
 constexpr int kMaxRW = 1024;  // rank x waves held in shared memory
 
-__global__ void __launch_bounds__(256) hessPrepKernel(const float2* __restrict__ amps, uint64_t nEvents, uint64_t nPad,
+__global__ void __launch_bounds__(256) hessPrepKernel(const float2* __restrict__ amps, uint64_t nEvents, uint32_t B,
                                                       uint64_t e0, uint64_t slab, int W0, int W, int R, int P,
                                                       const double* __restrict__ par, const int* __restrict__ slotRe,
                                                       const int* __restrict__ slotIm, float2* Y1, float2* Y2,
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) hessPrepKernel(const float2* __restrict__
 		for (int r = 0; r < R; ++r) {
 			float2 S0 = make_float2(0.f, 0.f), S1 = make_float2(0.f, 0.f);
 			for (int w = 0; w < W; ++w) {
-				const float2 a = amps[(size_t)w * nPad + col];
+				const float2 a = amps[storeIndex((uint32_t)w, col, (uint32_t)W, B)];
 				const float2 v = Vs[r * W + w];
 				float2& S = (w < W0) ? S0 : S1;
 				S.x = fmaf(v.x, a.x, fmaf(-v.y, a.y, S.x));
@@ -62,14 +62,14 @@ __global__ void __launch_bounds__(256) hessPrepKernel(const float2* __restrict__
 		for (int r = 0; r < R; ++r) {
 			float2 S0 = make_float2(0.f, 0.f), S1 = make_float2(0.f, 0.f);
 			for (int w = 0; w < W; ++w) {
-				const float2 a = amps[(size_t)w * nPad + col];
+				const float2 a = amps[storeIndex((uint32_t)w, col, (uint32_t)W, B)];
 				const float2 v = Vs[r * W + w];
 				float2& S = (w < W0) ? S0 : S1;
 				S.x = fmaf(v.x, a.x, fmaf(-v.y, a.y, S.x));
 				S.y = fmaf(v.x, a.y, fmaf(v.y, a.x, S.y));
 			}
 			for (int w = 0; w < W; ++w) {
-				const float2 a = amps[(size_t)w * nPad + col];
+				const float2 a = amps[storeIndex((uint32_t)w, col, (uint32_t)W, B)];
 				const float2 S = (w < W0) ? S0 : S1;
 				// S conj(a)
 				const float2 d = make_float2(S.x * a.x + S.y * a.y, S.y * a.x - S.x * a.y);
@@ -79,14 +79,14 @@ __global__ void __launch_bounds__(256) hessPrepKernel(const float2* __restrict__
 		}
 		Y1[(size_t)(2 * nS) * slab + t] = make_float2(1.f, 0.f);
 		for (int w = 0; w < W; ++w)
-			Y2[(size_t)w * slab + t] = amps[(size_t)w * nPad + col];
+			Y2[(size_t)w * slab + t] = amps[storeIndex((uint32_t)w, col, (uint32_t)W, B)];
 		Y2[(size_t)W * slab + t] = make_float2(1.f, 0.f);
 	}
 }
 
 }  // namespace
 
-int launchHessPrep(const float2* amps, uint64_t nEvents, uint64_t nPad, uint64_t e0, uint64_t slab, int W0, int W,
+int launchHessPrep(const float2* amps, uint64_t nEvents, uint32_t B, uint64_t e0, uint64_t slab, int W0, int W,
                    int R, int P, const double* par, const int* slotRe, const int* slotIm, float2* Y1, float2* Y2,
                    double* w1, double* w2, cudaStream_t s)
 {
@@ -94,7 +94,7 @@ int launchHessPrep(const float2* amps, uint64_t nEvents, uint64_t nPad, uint64_t
 		return setError(kErrUnsupported, "Hessian kernel supports rank x waves <= 1024");
 	const int threads = 256;
 	const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((slab + threads - 1) / threads, 8192));
-	hessPrepKernel<<<blocks, threads, 0, s>>>(amps, nEvents, nPad, e0, slab, W0, W, R, P, par, slotRe, slotIm, Y1, Y2,
+	hessPrepKernel<<<blocks, threads, 0, s>>>(amps, nEvents, B, e0, slab, W0, W, R, P, par, slotRe, slotIm, Y1, Y2,
 	                                          w1, w2);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "hessian prep launch");

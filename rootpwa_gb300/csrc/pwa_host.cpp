@@ -215,8 +215,8 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 			PWA_TRY(dConv.alloc((size_t)W * K * sizeof(float2), "integral conversion buffer"));
 			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
 			for (uint32_t w = 0; w < W; ++w)
-				PWA_TRY(launchConvertRow(static_cast<const double2*>(amps) + (size_t)w * ldIn, 1,
-				                         dConv.as<float2>() + (size_t)w * K, K, 1.0, dErr.as<unsigned>(), s));
+				PWA_TRY(launchConvertPlain(static_cast<const double2*>(amps) + (size_t)w * ldIn,
+				                           dConv.as<float2>() + (size_t)w * K, K, s));
 			a32 = dConv.as<float2>();
 			ldK = K;
 		}
@@ -233,9 +233,7 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		} else {
 			PWA_TRY(dConv.alloc((size_t)W * K * sizeof(float2), "integral conversion buffer"));
 			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
-			for (uint32_t w = 0; w < W; ++w)
-				PWA_TRY(launchConvertRow(dIn.as<double2>() + (size_t)w * K, 1, dConv.as<float2>() + (size_t)w * K, K, 1.0,
-				                         dErr.as<unsigned>(), s));
+			PWA_TRY(launchConvertPlain(dIn.as<double2>(), dConv.as<float2>(), (uint64_t)W * K, s));
 			a32 = dConv.as<float2>();
 		}
 	}
@@ -683,8 +681,9 @@ struct pwa_likelihood {
 	double totAcc = 0.;
 	std::vector<double> psInt;
 
-	uint64_t nEvents = 0, nPad = 0;
-	DevBuf amps;
+	uint64_t nEvents = 0;
+	uint32_t storeB = 128;  // events per store block (storeIndex)
+	DevBuf amps, ampTmp;
 	std::vector<char> added[2];
 
 	bool initialized = false, normAdded = false, accAdded = false, finished = false;
@@ -789,7 +788,6 @@ int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad
 	FdfArgs a{};
 	a.amps = L->amps.as<float2>();
 	a.nEvents = L->nEvents;
-	a.nPad = L->nPad;
 	a.W0 = (int)L->nW[0];
 	a.W = (int)L->W();
 	a.R = (int)L->rank;
@@ -894,7 +892,7 @@ struct TuneKey {
 		return std::tie(W, W0, R, evClass) < std::tie(o.W, o.W0, o.R, o.evClass);
 	}
 };
-std::map<TuneKey, std::pair<int, int> > g_tuned;  // -> (E, stages)
+std::map<TuneKey, int> g_tuned;  // -> pipeline stages
 
 // Times every candidate (tile size, pipeline depth) on the handle's own data
 // with a fixed parameter point and keeps the fastest.
@@ -907,7 +905,7 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 	auto it = g_tuned.find(key);
 	if (it != g_tuned.end()) {
 		for (const auto& c : cands)
-			if (c.E == it->second.first && c.stages == it->second.second)
+			if (c.stages == it->second)
 				L->plan = c;
 		return kOk;
 	}
@@ -934,7 +932,7 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 		}
 	}
 	L->plan = bestPlan;
-	g_tuned[key] = std::make_pair(bestPlan.E, bestPlan.stages);
+	g_tuned[key] = bestPlan.stages;
 	// the tuning runs leave no device error behind
 	unsigned err = 0;
 	PWA_TRY(cudaCheck(cudaMemcpy(&err, L->dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "error flag"));
@@ -1028,6 +1026,20 @@ int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, i
 	if (blocks)
 		*blocks = L->plan.blocks;
 	return kOk;
+}
+
+int pwa_likelihood_set_plan(pwa_likelihood* L, int stages)
+{
+	PWA_TRY(checkFinished(L));
+	std::vector<FdfPlan> cands;
+	PWA_TRY(planCandidates((int)L->nW[0], (int)L->W(), (int)L->rank, (int)L->storeB, L->nEvents, L->numSMs, L->maxSmem,
+	                       &cands));
+	for (const auto& c : cands)
+		if (c.stages == stages) {
+			L->plan = c;
+			return kOk;
+		}
+	return setError(kErrUnsupported, "no compiled FdF plan with this pipeline depth");
 }
 
 int pwa_likelihood_set_reduction(pwa_likelihood* L, int r)
@@ -1186,8 +1198,9 @@ int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const 
 	cudaStream_t s = L->stream;
 	if (L->nEvents == 0) {
 		L->nEvents = n;
-		L->nPad = (n + 127) / 128 * 128;
-		PWA_TRY(L->amps.alloc((size_t)L->W() * L->nPad * sizeof(float2), "amplitude store"));
+		L->storeB = (uint32_t)chooseStoreBlock((int)L->W(), (int)L->rank, L->maxSmem);
+		const uint64_t nBlocks = (n + L->storeB - 1) / L->storeB;
+		PWA_TRY(L->amps.alloc((size_t)nBlocks * L->W() * L->storeB * sizeof(float2), "amplitude store"));
 		PWA_TRY(cudaCheck(cudaMemsetAsync(L->amps.p, 0, L->amps.bytes, s), "amplitude store memset"));
 		PWA_TRY(L->dFlag.alloc(sizeof(unsigned), "flag"));
 	}
@@ -1197,13 +1210,16 @@ int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const 
 	const cplx normInt = L->normM[L->mIdx(e, w, e, w)];
 	bool fixPar = (L->accM[L->mIdx(e, w, e, w)] == 0.);
 	const double divisor = (L->useNormalizedAmps && normInt != 0.) ? std::sqrt(normInt.real()) : 1.;
-	float2* row = L->amps.as<float2>() + (size_t)L->gw(e, w) * L->nPad;
+	const uint32_t gwave = L->gw(e, w);
 	bool anyNonZero = false;
 	if (memory == PWA_MEMORY_HOST) {
 		// convert in FP64 on the host, upload through a pinned staging buffer
+		// into a contiguous device row, then scatter it into the tiled store
 		const size_t chunk = 1 << 20;
 		PinnedBuf stage;
 		PWA_TRY(stage.ensure(chunk * sizeof(float2), "staging"));
+		PWA_TRY(L->ampTmp.ensure(n * sizeof(float2), "amplitude row"));
+		float2* row = L->ampTmp.as<float2>();
 		for (uint64_t b = 0; b < n; b += chunk) {
 			const uint64_t m = std::min<uint64_t>(chunk, n - b);
 			float2* dst = stage.as<float2>();
@@ -1223,11 +1239,15 @@ int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const 
 			                  "amplitude upload"));
 			PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "amplitude upload sync"));
 		}
+		PWA_TRY(launchConvertRow(row, 0, L->amps.as<float2>(), L->W(), gwave, L->storeB, n, 1.0, L->dFlag.as<unsigned>(),
+		                         s));
+		PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "amplitude scatter sync"));
 	} else {
 		// the caller's streams may still be writing the device amplitudes
 		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device amplitudes"));
 		PWA_TRY(cudaCheck(cudaMemsetAsync(L->dFlag.p, 0, sizeof(unsigned), s), "memset"));
-		PWA_TRY(launchConvertRow(amps, ampType == PWA_COMPLEX128 ? 1 : 0, row, n, divisor, L->dFlag.as<unsigned>(), s));
+		PWA_TRY(launchConvertRow(amps, ampType == PWA_COMPLEX128 ? 1 : 0, L->amps.as<float2>(), L->W(), gwave, L->storeB, n,
+		                         divisor, L->dFlag.as<unsigned>(), s));
 		unsigned flag = 0;
 		PWA_TRY(cudaCheck(cudaMemcpyAsync(&flag, L->dFlag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "flag"));
 		PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "amplitude convert sync"));
@@ -1287,8 +1307,10 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	PWA_TRY(ensureDevice(L));
 	const uint32_t W = L->W();
 	std::vector<FdfPlan> cands;
-	PWA_TRY(planCandidates((int)L->nW[0], (int)W, (int)L->rank, L->nEvents, L->numSMs, L->maxSmem, &cands));
+	PWA_TRY(planCandidates((int)L->nW[0], (int)W, (int)L->rank, (int)L->storeB, L->nEvents, L->numSMs, L->maxSmem,
+	                       &cands));
 	L->plan = cands.front();
+	L->ampTmp.release();
 	int maxBlocks = 1;
 	for (const auto& c : cands)
 		maxBlocks = std::max(maxBlocks, c.blocks);
@@ -1531,7 +1553,7 @@ int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* H)
 	PWA_TRY(cudaCheck(cudaMemsetAsync(dG2.p, 0, dG2.bytes, s), "memset"));
 	for (uint64_t e0 = 0; e0 < L->nEvents; e0 += slab) {
 		const uint64_t K = std::min<uint64_t>(slab, L->nEvents - e0);
-		PWA_TRY(launchHessPrep(L->amps.as<float2>(), L->nEvents, L->nPad, e0, slab, (int)L->nW[0], (int)W, (int)R,
+		PWA_TRY(launchHessPrep(L->amps.as<float2>(), L->nEvents, L->storeB, e0, slab, (int)L->nW[0], (int)W, (int)R,
 		                       (int)P, dHP.as<double>(), L->dSlotRe.as<int>(), L->dSlotIm.as<int>(), dY1.as<float2>(),
 		                       dY2.as<float2>(), dW1.as<double>(), dW2.as<double>(), s));
 		const int ck = (int)std::min<uint64_t>((uint64_t)chunks, std::max<uint64_t>(1, K / 64));

@@ -34,13 +34,29 @@ void countLaunches(uint64_t n);
 enum { kDevErrTimeout = 1 };
 
 // ---------------------------------------------------------------------------
+// Amplitude store
+// ---------------------------------------------------------------------------
+// complex64 amplitudes in blocks of B events (B = 128, or 64 for wide wave
+// sets).  Block b holds the W wave rows of its B events contiguously (waves of
+// negative reflectivity first), so one bulk copy moves one tile.  Row w keeps
+// event b*B + p at position (p + rot(w)) mod B with
+// rot(w) = (B/16) * (w mod (256/B)): the rotation spreads the rows that one
+// warp reads together in the FdF kernel's first phase over all shared-memory
+// banks.  The last block is zero-padded.
+__host__ __device__ inline uint64_t storeIndex(uint32_t w, uint64_t e, uint32_t W, uint32_t B)
+{
+	const uint64_t b = e / B;
+	const uint32_t p = (uint32_t)(e - b * B);
+	const uint32_t epw = B / 16;
+	const uint32_t rot = epw * (w % (16 / epw));
+	return (b * W + w) * B + ((p + rot) & (B - 1));
+}
+
+// ---------------------------------------------------------------------------
 // Fused FdF / DoEval
 // ---------------------------------------------------------------------------
-// Amplitude store: complex64 structure-of-arrays [wave][nPad]; waves of
-// negative reflectivity first (W0 of them), then positive; rows zero-padded
-// to nPad (a multiple of 128 events).
 struct FdfPlan {
-	int E = 128;        // events per tile
+	int E = 128;        // events per tile (= store block)
 	int stages = 2;     // shared-memory pipeline depth
 	int wpw = 2;        // wave bucket per warp (template)
 	int blocks = 0;     // grid size (persistent, <= #SMs)
@@ -48,9 +64,8 @@ struct FdfPlan {
 };
 
 struct FdfArgs {
-	const float2* amps;
+	const float2* amps;      // tiled store (storeIndex)
 	uint64_t nEvents;
-	uint64_t nPad;
 	int W0, W, R, P;
 	const double* par;       // device, [P]
 	const int* slotRe;       // device, [R*W] parameter index of Re(V_rw) or -1
@@ -80,20 +95,23 @@ struct FinArgs {
 	double* out;             // device, [P + 2]: f, gradient, device error status
 };
 
-// Chooses tile size, pipeline depth and grid; returns kErrUnsupported for
-// shapes outside the compiled variants.
-int planFdf(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, FdfPlan* plan);
-// All compiled (tile size, pipeline depth) plans that fit, for the autotuner.
-int planCandidates(int W0, int W, int R, uint64_t nEvents, int numSMs, size_t maxSmem, std::vector<FdfPlan>* out);
+// Store block size for a wave set: 128 when two 128-event tiles fit in shared
+// memory, else 64.
+int chooseStoreBlock(int W, int R, size_t maxSmem);
+// All compiled pipeline depths for tiles of B events that fit, for the autotuner.
+int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, size_t maxSmem,
+                   std::vector<FdfPlan>* out);
 int launchFdf(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
 int launchFinalize(const FinArgs& args, int finBlocks, cudaStream_t s);
 int finalizeBlocks(int R, int W);
 
-// Converts one wave of amplitudes (complex64 or complex128, device memory)
-// into the complex64 store row, divided by `divisor` in FP64; sets *nonzero
+// Converts one wave w of amplitudes (complex64 or complex128, device memory)
+// into the tiled complex64 store, divided by `divisor` in FP64; sets *nonzero
 // to 1 if any amplitude is non-zero.
-int launchConvertRow(const void* src, int srcIsDouble, float2* dst, uint64_t n, double divisor, unsigned* nonzero,
-                     cudaStream_t s);
+int launchConvertRow(const void* src, int srcIsDouble, float2* store, uint32_t W, uint32_t w, uint32_t B, uint64_t n,
+                     double divisor, unsigned* nonzero, cudaStream_t s);
+// Converts amplitudes to complex64 rows [wave][event] of a plain array (integral input).
+int launchConvertPlain(const void* src, float2* dst, uint64_t n, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Hessian event term
@@ -106,7 +124,7 @@ int launchConvertRow(const void* src, int srcIsDouble, float2* dst, uint64_t n, 
 //   w1 = f^2, w2 = f with f = 2 / L (0 beyond nEvents)
 // so that the weighted Gram matrices of Y1 and Y2 give every event sum of the
 // analytic Hessian (partialWaveFit/pwaLikelihood.cc:676-735).
-int launchHessPrep(const float2* amps, uint64_t nEvents, uint64_t nPad, uint64_t e0, uint64_t slab, int W0, int W,
+int launchHessPrep(const float2* amps, uint64_t nEvents, uint32_t B, uint64_t e0, uint64_t slab, int W0, int W,
                    int R, int P, const double* par, const int* slotRe, const int* slotIm, float2* Y1, float2* Y2,
                    double* w1, double* w2, cudaStream_t s);
 

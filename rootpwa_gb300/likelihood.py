@@ -246,6 +246,10 @@ class pwaLikelihood:
         N.call("pwa_likelihood_plan", self._h, C.byref(e), C.byref(s), C.byref(b))
         return e.value, s.value, b.value
 
+    def setPlan(self, stages):
+        """Select the FdF kernel pipeline depth by hand (after finishInit)."""
+        N.call("pwa_likelihood_set_plan", self._h, int(stages))
+
     # -- setup (order as _likelihood.py:17-71) -------------------------------
     def init(self, waveNames, reflectivities, thresholds=None, rank=1, massBinCenter=0.0):
         n = len(waveNames)
