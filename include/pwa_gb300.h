@@ -232,11 +232,13 @@ int pwa_likelihood_func_call_info(const pwa_likelihood* L, int call, uint64_t* n
                                   double* funcTime, double* normTime);
 int pwa_likelihood_reset_func_call_info(pwa_likelihood* L);
 /* Engine instrumentation without reference counterpart: when enabled, every
- * evaluation records CUDA events on its launch stream before the fused event
- * kernel, between it and the finalize kernel, and after the finalize kernel.
- * pwa_likelihood_kernel_times waits for the recorded events, returns the summed
- * durations in milliseconds and the number of timed evaluations, and clears
- * the record.  At most 65536 evaluations are recorded between two reads. */
+ * evaluation records CUDA events on its launch stream before and after the
+ * fused FdF kernel (one launch per evaluation, the normalisation term and the
+ * cross-block sums included).  pwa_likelihood_kernel_times waits for the
+ * recorded events, returns the summed kernel duration in milliseconds
+ * (finalizeMs is always 0: there is no second kernel) and the number of timed
+ * evaluations, and clears the record.  At most 65536 evaluations are recorded
+ * between two reads. */
 int pwa_likelihood_set_timing(pwa_likelihood* L, int enable);
 int pwa_likelihood_kernel_times(pwa_likelihood* L, double* eventKernelMs, double* finalizeMs, uint64_t* nTimed);
 

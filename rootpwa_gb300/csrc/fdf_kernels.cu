@@ -7,27 +7,34 @@
 //   G_{r,w}  += c_i S_{r,e(w),i} conj(A_{w,i})          (FP32 per tile, FP64 across tiles)
 // plus -sum ln L_i and sum c_i, which is the event term of
 // partialWaveFit/pwaLikelihood.cc:209-244 (FdF), :361-375 (DoEval) and
-// :547-577 (Gradient).  A second small kernel sums the per-block partials in
-// FP64, adds the normalisation term (:254-273), the half-Cauchy prior
-// (:278-297) and maps the result onto the parameter layout (:1714-1731).
+// :547-577 (Gradient).  The same kernel adds the normalisation term
+// (:254-273) and the half-Cauchy prior (:278-297) in FP64, sums the blocks'
+// partials in FP64 and writes f and the gradient in the parameter layout
+// (:1714-1731): one launch per evaluation.
 //
 // Kernel structure (one persistent CTA per SM, 512 threads):
-//   * event tiles of E events x W waves are staged in shared memory by
-//     cp.async.bulk copies (one per wave row, issued by one warp) completing
-//     on an mbarrier; `stages` tiles are in flight;
+//   * the store keeps each block of E events contiguous (storeIndex), so one
+//     cp.async.bulk copy moves a tile into shared memory, completing on an
+//     mbarrier; `stages` tiles are in flight;
+//   * while the first tiles load, every CTA computes the normalisation and
+//     prior terms of a few slots in FP64;
 //   * phase 1: each warp owns E/16 events of the tile, 32/(E/16) lanes per
 //     event sum interleaved slices of the waves and combine them with warp
 //     shuffles, giving L_i, c_i and T_{r,e,i} = c_i S (double-buffered, so
 //     one block barrier per tile suffices);
-//   * phase 2: warp j owns a contiguous range of waves, each lane a fixed set
-//     of event pairs; the lane sums conj(A) T over its events in FP32 for
-//     kFold tiles, then a warp reduce-scatter leaves every lane one
-//     (slot, re/im) value, which it adds to its FP64 (or compensated FP32)
-//     accumulator;
+//   * phase 2: warp j owns a contiguous range of waves of one reflectivity,
+//     each lane a fixed set of event pairs; the lane sums conj(A) T over its
+//     events with packed FP32x2 FMA for kFold tiles, then a warp
+//     reduce-scatter leaves every lane one (slot, re/im) value, which it adds
+//     to its FP64 (or compensated FP32) accumulator;
 //   * the last warp to finish with a stage (shared-memory counter) refills it
-//     with the tile `stages` ahead.
+//     with the tile `stages` ahead;
+//   * the tail sums the CTAs' partials in two deterministic levels (groups of
+//     kTailGroup CTAs in index order, then the groups in order), picked by
+//     arrival counters, so results are bitwise reproducible.
 // Every mbarrier wait is bounded (about a second); on expiry the CTA sets a
-// device error flag, waits (again bounded) for its own copies and returns.
+// device error flag, waits (again bounded) for its own copies and completes
+// the tail, and the host discards the result.
 
 #include "pwa_internal.h"
 
@@ -148,7 +155,7 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
 // store's rotated order (storeIndex), moved by a single bulk copy.
 struct SmemLayout {
 	size_t rowStride;  // bytes per wave row
-	size_t tiles, vs, ts, tsw, bars, done, total;
+	size_t tiles, vs, v64, ts, tsw, tot, bars, done, total;
 };
 
 __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
@@ -158,9 +165,11 @@ __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages
 	L.rowStride = (size_t)E * 8;
 	L.tiles = 0;
 	L.vs = up((size_t)stages * W * L.rowStride);
-	L.ts = up(L.vs + (size_t)W * R * 8);
+	L.v64 = up(L.vs + (size_t)W * R * 8);
+	L.ts = up(L.v64 + (size_t)W * R * 16);
 	L.tsw = up(L.ts + 2 * (size_t)R * 2 * E * 8);
-	L.bars = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
+	L.tot = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
+	L.bars = up(L.tot + (2 + 2 * (size_t)R * W) * 8);
 	L.done = L.bars + (size_t)stages * 8;
 	L.total = L.done + (size_t)stages * 4;
 	return L;
@@ -221,7 +230,9 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 
 // Tiles whose gradient partials are summed in FP32 before the warp
 // reduce-scatter folds them into the FP64 (or compensated) accumulators.
-constexpr int kFold = 4;
+constexpr int kFold = 8;
+// blocks per group of the two-level cross-block sum
+constexpr int kTailGroup = 12;
 
 template <int R, int E, int WPW>
 __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, const int stages)
@@ -242,9 +253,12 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);      // [W][R] (vx, vy)
 	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);      // [2][R][2][E] c S
 	float2* Tsw = reinterpret_cast<float2*>(smem + lay.tsw);    // [2][R][2][E] c S, re/im swapped
+	double2* V64 = reinterpret_cast<double2*>(smem + lay.v64);  // [R][W] FP64, slot order
+	double* sTot = reinterpret_cast<double*>(smem + lay.tot);     // [nPartial] totals (final block)
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	unsigned* done = reinterpret_cast<unsigned*>(smem + lay.done);
 	__shared__ double redLL[kWarps], redC[kWarps];
+	__shared__ unsigned sLast;
 
 	// the parameters may be written by the preceding grid (device-side minimiser)
 	gridDependencyWait();
@@ -252,7 +266,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	for (int k = tid; k < W * R; k += kThreads) {
 		const int w = k / R, r = k - w * R;
 		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
-		Vs[k] = make_float2(ir >= 0 ? (float)a.par[ir] : 0.f, ii >= 0 ? (float)a.par[ii] : 0.f);
+		const double vr = ir >= 0 ? a.par[ir] : 0., vi = ii >= 0 ? a.par[ii] : 0.;
+		Vs[k] = make_float2((float)vr, (float)vi);
+		V64[r * W + w] = make_double2(vr, vi);
 	}
 	const double flatD = a.par[a.P - 1];
 	const float flat2 = (float)(flatD * flatD);
@@ -282,6 +298,52 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	if (warp == 0) {
 		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
 			issue((uint64_t)s, s);
+	}
+
+	// Normalisation and prior terms (pwaLikelihood.cc:254-297) do not depend on
+	// the events: every block computes them in FP64 for the slots
+	// s = blockIdx.x + j * gridDim.x (warp j mod 16) while its first tiles
+	// load.  Per slot: D = sum_j V_j conj(I_ij) over the same reflectivity,
+	// Re(V_i conj(D)), and the half-Cauchy value and gradient.
+	{
+		const int nSlots = R * W;
+		const double g2 = a.cauchyWidth * a.cauchyWidth;
+		for (int j = warp; (int)blockIdx.x + j * (int)gridDim.x < nSlots; j += kWarps) {
+			const int sl = (int)blockIdx.x + j * (int)gridDim.x;
+			const int r = sl / W, g = sl - r * W;
+			const int pos = (g >= W0) ? 1 : 0;
+			const int off = pos ? W0 : 0, We = pos ? W - W0 : W0, i = g - off;
+			const double* Ib = a.accI + (pos ? 2 * (size_t)W0 * W0 : 0) + 2 * (size_t)i * We;
+			double dre = 0., dim = 0.;
+			for (int q = lane; q < We; q += 32) {
+				const double2 u = V64[r * W + off + q];
+				const double Ir = Ib[2 * q], Ii = Ib[2 * q + 1];
+				dre += u.x * Ir + u.y * Ii;  // V_q conj(I_iq)
+				dim += u.y * Ir - u.x * Ii;
+			}
+			dre = warpSumD(dre);
+			dim = warpSumD(dim);
+			if (lane == 0) {
+				const double2 v = V64[sl];
+				double priorv = 0., pre = 0., pim = 0.;
+				if (a.prior == 1) {
+					const double rr = hypot(v.x, v.y);
+					const double cf = 1. / (1. + (rr * rr) / g2);
+					const double cd = (-2. * rr * g2) / ((g2 + rr * rr) * (g2 + rr * rr));
+					const double fac = (1. / (rr * cf)) * cd;
+					priorv = -log(cf);
+					pre = fac * v.x;
+					pim = fac * v.y;
+				}
+				double* ns = a.normScr + (size_t)sl * 6;
+				ns[0] = dre;
+				ns[1] = dim;
+				ns[2] = v.x * dre + v.y * dim;  // Re(V_i conj(D_i))
+				ns[3] = priorv;
+				ns[4] = pre;
+				ns[5] = pim;
+			}
+		}
 	}
 
 	// phase-1 role: event pe of the tile, wave slice ph (waves w = ph mod H)
@@ -341,24 +403,42 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			const uint32_t colAddr = smemAddr(tile + ((pe + rot1) & (E - 1)));
 			const uint32_t vAddr = smemAddr(Vs);
 			const uint32_t rowB = (uint32_t)lay.rowStride;
+			// V of two consecutive ranks in one 128-bit load; the address
+			// (w * R + r) * 8 is 16-byte aligned only for even R
+			auto loadV = [&](int w, float2 (&v)[R]) {
+				if ((R & 1) == 0) {
+#pragma unroll
+					for (int r = 0; r + 1 < R; r += 2) {
+						const float4 q = lds128(vAddr + (uint32_t)(w * R + r) * 8u);
+						v[r] = make_float2(q.x, q.y);
+						v[r + 1] = make_float2(q.z, q.w);
+					}
+				} else {
+#pragma unroll
+					for (int r = 0; r < R; ++r)
+						v[r] = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
+				}
+			};
 #pragma unroll 4
 			for (int w = ph; w < W0; w += H) {
 				const float2 av = lds64(colAddr + (uint32_t)w * rowB);
+				float2 v[R];
+				loadV(w, v);
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					const float2 v = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
-					Sa[r][0].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, Sa[r][0].x));
-					Sa[r][0].y = fmaf(v.x, av.y, fmaf(v.y, av.x, Sa[r][0].y));
+					Sa[r][0].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sa[r][0].x));
+					Sa[r][0].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sa[r][0].y));
 				}
 			}
 #pragma unroll 4
 			for (int w = wStart1; w < W; w += H) {
 				const float2 av = lds64(colAddr + (uint32_t)w * rowB);
+				float2 v[R];
+				loadV(w, v);
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					const float2 v = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
-					Sa[r][1].x = fmaf(v.x, av.x, fmaf(-v.y, av.y, Sa[r][1].x));
-					Sa[r][1].y = fmaf(v.x, av.y, fmaf(v.y, av.x, Sa[r][1].y));
+					Sa[r][1].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sa[r][1].x));
+					Sa[r][1].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sa[r][1].y));
 				}
 			}
 			float2 S[R][2];
@@ -489,8 +569,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	}
 
 	if (failed) {
-		// let our own copies in flight land before the CTA exits (bounded):
-		// tiles up to k - 1 + stages have been issued
+		// let our own copies in flight land (bounded): tiles up to
+		// k - 1 + stages have been issued; the partials of this block are
+		// incomplete and the error flag tells the host to discard the result
 		if (tid == 0) {
 			atomicOr(a.devErr, (unsigned)kDevErrTimeout);
 			for (uint64_t j = k; j < k + (uint64_t)stages && j < myTiles; ++j) {
@@ -498,15 +579,17 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				mbarWaitBounded(&bars[s], (uint32_t)((j / (uint64_t)stages) & 1ull));
 			}
 		}
-		return;
 	}
 
-	// ---- epilogue: per-block partials, slot-major [nPartial][gridDim] ----
-	// (the previous grid's finalize kernel may still read the partials when
-	// this grid starts early under programmatic dependent launch)
+	// ---- epilogue: block partials [gridDim][nPartial], then a deterministic
+	// two-level sum: the last block of each group of kTailGroup blocks sums
+	// its members in index order, the last group sums the groups in order and
+	// writes f and the gradient (no further kernel) ----
+	// (the previous launch's tail may still read the partials when this grid
+	// starts early under programmatic dependent launch)
 	gridDependencyWait();
-	double* out = a.partials + blockIdx.x;
-	const size_t ps = gridDim.x;
+	const int nP = a.nPartial;
+	double* myPart = a.partials + (size_t)blockIdx.x * nP;
 	if (lane == 0) {
 		if (a.reduction == 0) {
 			redLL[warp] = accLL;
@@ -523,8 +606,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			ll += redLL[wv];
 			cs += redC[wv];
 		}
-		out[0] = ll;
-		out[ps] = cs;
+		myPart[0] = ll;
+		myPart[1] = cs;
 	}
 	if (a.withGrad) {
 #pragma unroll
@@ -537,129 +620,72 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				if (wi < nWarpWaves) {
 					const int w = wBase + wi;
 					const double v = (a.reduction == 0) ? accG[q] : ((double)kG[q] - (double)kGc[q]);
-					out[(size_t)(2 + (r * W + w) * 2 + comp) * ps] = v;
+					myPart[2 + (r * W + w) * 2 + comp] = v;
 				}
 			}
 		}
 	}
-}
-
-constexpr int kFinWarps = 8;
-
-__global__ void __launch_bounds__(kFinWarps * 32) fdfFinalizeKernel(const FinArgs f)
-{
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const int g = blockIdx.x * kFinWarps + warp;
-	const int nSlots = f.R * f.W;
-	const double twice = 2. * f.nEvt;
-	__shared__ double sNorm[kFinWarps], sPrior[kFinWarps];
-	__shared__ int sLast;
-	extern __shared__ double2 sV[];  // [R * W] production amplitudes (FP64)
-	gridDependencyWait();
-	gridDependencyTrigger();
-	const double flat = f.par[f.P - 1];
-	const size_t ps = f.nBlocks;
-	for (int k = threadIdx.x; k < nSlots; k += blockDim.x) {
-		const int kr = f.slotRe[k], ki = f.slotIm[k];
-		sV[k] = make_double2(kr >= 0 ? f.par[kr] : 0., ki >= 0 ? f.par[ki] : 0.);
+	__threadfence();
+	__syncthreads();
+	const int grp = (int)blockIdx.x / kTailGroup;
+	const int g0 = grp * kTailGroup, g1 = min((int)gridDim.x, g0 + kTailGroup);
+	const int nGroups = ((int)gridDim.x + kTailGroup - 1) / kTailGroup;
+	if (tid == 0)
+		sLast = (atomicAdd(&a.counters[grp], 1u) == (unsigned)(g1 - g0 - 1)) ? 1u : 0u;
+	__syncthreads();
+	if (!sLast)
+		return;
+	__threadfence();
+	const int nUsed = a.withGrad ? nP : 2;
+	for (int v = tid; v < nUsed; v += kThreads) {
+		double acc = 0.;
+		for (int b = g0; b < g1; ++b)
+			acc += __ldcg(a.partials + (size_t)b * nP + v);
+		a.groupSums[(size_t)grp * nP + v] = acc;
+	}
+	__threadfence();
+	__syncthreads();
+	if (tid == 0) {
+		a.counters[grp] = 0u;  // ready for the next launch
+		sLast = (atomicAdd(&a.counters[nGroups], 1u) == (unsigned)(nGroups - 1)) ? 1u : 0u;
 	}
 	__syncthreads();
-	double normv = 0., priorv = 0.;
-	if (g < nSlots) {
-		const int r = g / f.W, w = g - r * f.W;
-		const int pos = (w >= f.W0) ? 1 : 0;
-		const int off = pos ? f.W0 : 0;
-		const int We = pos ? f.W - f.W0 : f.W0;
-		const int i = w - off;
-		const int ire = f.slotRe[g], iim = f.slotIm[g];
-		const double vr = sV[g].x, vi = sV[g].y;
-		double gre = 0., gim = 0.;
-		if (f.withGrad)
-			for (int b = lane; b < f.nBlocks; b += 32) {
-				gre += f.partials[(size_t)(2 + 2 * g) * ps + b];
-				gim += f.partials[(size_t)(3 + 2 * g) * ps + b];
-			}
-		// D_i = sum_j V_j conj(I_ij) over waves of the same reflectivity
-		const double* Ib = f.accI + (pos ? 2 * (size_t)f.W0 * f.W0 : 0) + 2 * (size_t)i * We;
-		double dre = 0., dim = 0.;
-		for (int j = lane; j < We; j += 32) {
-			const double2 u = sV[r * f.W + off + j];
-			const double ur = u.x, ui = u.y;
-			const double Ir = Ib[2 * j], Ii = Ib[2 * j + 1];
-			dre += ur * Ir + ui * Ii;
-			dim += ui * Ir - ur * Ii;
-		}
-		gre = warpSumD(gre);
-		gim = warpSumD(gim);
-		dre = warpSumD(dre);
-		dim = warpSumD(dim);
-		if (lane == 0) {
-			normv = vr * dre + vi * dim;  // Re(V_i conj(D_i))
-			double pre = 0., pim = 0.;
-			if (f.prior == 1) {
-				const double rr = hypot(vr, vi);
-				const double g2 = f.cauchyWidth * f.cauchyWidth;
-				const double cf = 1. / (1. + (rr * rr) / g2);
-				const double cd = (-2. * rr * g2) / ((g2 + rr * rr) * (g2 + rr * rr));
-				const double fac = (1. / (rr * cf)) * cd;
-				priorv = -log(cf);
-				pre = fac * vr;
-				pim = fac * vi;
-			}
-			if (f.withGrad) {
-				if (ire >= 0)
-					f.out[1 + ire] = gre + twice * dre - pre;
-				if (iim >= 0)
-					f.out[1 + iim] = gim + twice * dim - pim;
-			}
-		}
-	} else if (g == nSlots) {
-		double ll = 0., cs = 0.;
-		for (int b = lane; b < f.nBlocks; b += 32) {
-			ll += f.partials[b];
-			cs += f.partials[ps + b];
-		}
-		ll = warpSumD(ll);
-		cs = warpSumD(cs);
-		if (lane == 0) {
-			if (f.withGrad)
-				f.out[f.P] = flat * cs + twice * flat * f.totAcc;
-			f.scratch[2 * gridDim.x] = ll;
-		}
-	}
-	if (lane == 0) {
-		sNorm[warp] = normv;
-		sPrior[warp] = priorv;
+	if (!sLast)
+		return;
+	__threadfence();
+	for (int v = tid; v < nUsed; v += kThreads) {
+		double acc = 0.;
+		for (int gg = 0; gg < nGroups; ++gg)
+			acc += __ldcg(a.groupSums + (size_t)gg * nP + v);
+		sTot[v] = acc;
 	}
 	__syncthreads();
-	if (threadIdx.x == 0) {
+	const double nEvt = a.nEvt, twice = 2. * a.nEvt;
+	const int nSlots = R * W;
+	if (a.withGrad) {
+		for (int sl = tid; sl < nSlots; sl += kThreads) {
+			const double* ns = a.normScr + (size_t)sl * 6;
+			const int ire = a.slotRe[sl], iim = a.slotIm[sl];
+			if (ire >= 0)
+				a.out[1 + ire] = sTot[2 + 2 * sl] + twice * __ldcg(ns + 0) - __ldcg(ns + 4);
+			if (iim >= 0)
+				a.out[1 + iim] = sTot[3 + 2 * sl] + twice * __ldcg(ns + 1) - __ldcg(ns + 5);
+		}
+	}
+	if (warp == 0) {
 		double n = 0., p = 0.;
-		for (int wv = 0; wv < kFinWarps; ++wv) {
-			n += sNorm[wv];
-			p += sPrior[wv];
-		}
-		f.scratch[2 * blockIdx.x] = n;
-		f.scratch[2 * blockIdx.x + 1] = p;
-		__threadfence();
-		const unsigned t = atomicAdd(f.ticket, 1u);
-		sLast = (t == gridDim.x - 1) ? 1 : 0;
-	}
-	__syncthreads();
-	if (sLast && warp == 0) {
-		__threadfence();
-		const volatile double* sc = f.scratch;
-		double n = 0., p = 0.;
-		for (int b = lane; b < (int)gridDim.x; b += 32) {
-			n += sc[2 * b];
-			p += sc[2 * b + 1];
+		for (int sl = lane; sl < nSlots; sl += 32) {
+			n += __ldcg(a.normScr + (size_t)sl * 6 + 2);
+			p += __ldcg(a.normScr + (size_t)sl * 6 + 3);
 		}
 		n = warpSumD(n);
 		p = warpSumD(p);
 		if (lane == 0) {
-			const double ll = sc[2 * gridDim.x];
-			f.out[0] = ll + f.nEvt * (n + flat * flat * f.totAcc) + p;
-			f.out[f.P + 1] = (double)(*(const volatile unsigned*)f.devErr);
-			*f.ticket = 0u;
+			a.out[0] = sTot[0] + nEvt * (n + flatD * flatD * a.totAcc) + p;
+			if (a.withGrad)
+				a.out[a.P] = flatD * sTot[1] + twice * flatD * a.totAcc;
+			a.out[a.P + 1] = (double)(*(const volatile unsigned*)a.devErr);
+			a.counters[nGroups] = 0u;
 		}
 	}
 }
@@ -794,6 +820,8 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 	return kOk;
 }
 
+int fdfTailGroups(int blocks) { return (blocks + kTailGroup - 1) / kTailGroup; }
+
 int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {
 	switch (a.R) {
@@ -812,25 +840,6 @@ int launchConvertPlain(const void* src, float2* dst, uint64_t n, cudaStream_t s)
 	convertPlainKernel<<<std::max(blocks, 1), threads, 0, s>>>(static_cast<const double2*>(src), dst, n);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "convert launch");
-}
-
-int finalizeBlocks(int R, int W) { return (R * W + 1 + kFinWarps - 1) / kFinWarps; }
-
-int launchFinalize(const FinArgs& a, int finBlocks, cudaStream_t s)
-{
-	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3(finBlocks);
-	cfg.blockDim = dim3(kFinWarps * 32);
-	cfg.stream = s;
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-	attr[0].val.programmaticStreamSerializationAllowed = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
-	cfg.dynamicSmemBytes = (size_t)a.R * a.W * sizeof(double2);
-	const cudaError_t e = cudaLaunchKernelEx(&cfg, fdfFinalizeKernel, a);
-	countLaunches(1);
-	return cudaCheck(e, "fdf finalize launch");
 }
 
 int launchConvertRow(const void* src, int srcIsDouble, float2* store, uint32_t W, uint32_t w, uint32_t B, uint64_t n,

@@ -691,8 +691,7 @@ struct pwa_likelihood {
 	// evaluation resources
 	bool autotune = true;
 	FdfPlan plan;
-	int finBlocks = 0;
-	DevBuf dSlotRe, dSlotIm, dAccI, dPartials, dFinScratch, dTicket, dErr, dPar, dOut, dFlag;
+	DevBuf dSlotRe, dSlotIm, dAccI, dPartials, dGroupSums, dNormScr, dCounters, dErr, dPar, dOut, dFlag;
 	PinnedBuf hPar, hOut;
 	cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
@@ -781,9 +780,9 @@ void toPar(const pwa_likelihood* L, const std::vector<cplx>& V, double flat, dou
 	out[L->nPars - 1] = flat;
 }
 
-// Launches the fused event kernel and the finalize kernel: dPar -> dOut.
+// Launches the fused FdF kernel: dPar -> dOut (f, gradient, device status).
 int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad, cudaStream_t s,
-               cudaEvent_t between = nullptr)
+               cudaEvent_t after = nullptr)
 {
 	FdfArgs a{};
 	a.amps = L->amps.as<float2>();
@@ -795,46 +794,31 @@ int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad
 	a.par = dPar;
 	a.slotRe = L->dSlotRe.as<int>();
 	a.slotIm = L->dSlotIm.as<int>();
-	a.partials = L->dPartials.as<double>();
-	a.nPartial = 2 + 2 * a.R * a.W;
-	a.devErr = L->dErr.as<unsigned>();
+	a.accI = L->dAccI.as<double>();
+	a.nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
+	a.totAcc = L->totAcc;
+	a.prior = L->priorType;
+	a.cauchyWidth = L->cauchyWidth;
 	a.withGrad = withGrad;
 	a.reduction = L->reduction;
+	a.partials = L->dPartials.as<double>();
+	a.nPartial = 2 + 2 * a.R * a.W;
+	a.groupSums = L->dGroupSums.as<double>();
+	a.normScr = L->dNormScr.as<double>();
+	a.counters = L->dCounters.as<unsigned>();
+	a.devErr = L->dErr.as<unsigned>();
+	a.out = dOut;
 	cudaEvent_t* te = nullptr;
-	if (L->timing && 3 * (L->nTimed + 1) <= L->timingEvents.size()) {
-		te = &L->timingEvents[3 * L->nTimed];
+	if (L->timing && 2 * (L->nTimed + 1) <= L->timingEvents.size()) {
+		te = &L->timingEvents[2 * L->nTimed];
 		++L->nTimed;
 		cudaEventRecord(te[0], s);
 	}
 	PWA_TRY(launchFdf(L->plan, a, s));
-	if (between)
-		cudaEventRecord(between, s);
+	if (after)
+		cudaEventRecord(after, s);
 	if (te)
 		cudaEventRecord(te[1], s);
-	FinArgs f{};
-	f.partials = a.partials;
-	f.nBlocks = L->plan.blocks;
-	f.nPartial = a.nPartial;
-	f.par = dPar;
-	f.P = a.P;
-	f.W0 = a.W0;
-	f.W = a.W;
-	f.R = a.R;
-	f.slotRe = a.slotRe;
-	f.slotIm = a.slotIm;
-	f.accI = L->dAccI.as<double>();
-	f.nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
-	f.totAcc = L->totAcc;
-	f.prior = L->priorType;
-	f.cauchyWidth = L->cauchyWidth;
-	f.withGrad = withGrad;
-	f.scratch = L->dFinScratch.as<double>();
-	f.ticket = L->dTicket.as<unsigned>();
-	f.devErr = L->dErr.as<unsigned>();
-	f.out = dOut;
-	PWA_TRY(launchFinalize(f, L->finBlocks, s));
-	if (te)
-		cudaEventRecord(te[2], s);
 	return kOk;
 }
 
@@ -849,7 +833,6 @@ int hostEval(pwa_likelihood* L, const double* par, double* f, double* grad, int 
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dPar.p, L->hPar.p, P * sizeof(double), cudaMemcpyHostToDevice, s), "H2D par"));
 	cudaEventRecord(L->ev[0], s);
 	PWA_TRY(launchEval(L, L->dPar.as<double>(), L->dOut.as<double>(), withGrad, s, L->ev[1]));
-	cudaEventRecord(L->ev[2], s);
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->hOut.p, L->dOut.p, (P + 2) * sizeof(double), cudaMemcpyDeviceToHost, s),
 	                  "D2H result"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "FdF sync"));
@@ -868,13 +851,11 @@ int hostEval(pwa_likelihood* L, const double* par, double* f, double* grad, int 
 		L->derivCache.assign(out + 1, out + 1 + P);
 		L->cacheValid = true;
 	}
-	float ms1 = 0.f, ms2 = 0.f;
+	float ms1 = 0.f;
 	cudaEventElapsedTime(&ms1, L->ev[0], L->ev[1]);
-	cudaEventElapsedTime(&ms2, L->ev[1], L->ev[2]);
 	CallInfo& ci = L->info[call];
 	++ci.nCalls;
-	ci.func += ms1 * 1e-3;
-	ci.norm += ms2 * 1e-3;
+	ci.func += ms1 * 1e-3;  // the fused kernel includes the normalisation term
 	ci.total += seconds() - t0;
 	return kOk;
 }
@@ -922,10 +903,10 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 		PWA_TRY(cudaCheck(cudaEventRecord(L->ev[0], s), "event"));
 		for (int i = 0; i < 5; ++i)
 			PWA_TRY(launchEval(L, L->dPar.as<double>(), L->dOut.as<double>(), 1, s));
-		PWA_TRY(cudaCheck(cudaEventRecord(L->ev[2], s), "event"));
-		PWA_TRY(cudaCheck(cudaEventSynchronize(L->ev[2]), "autotune sync"));
+		PWA_TRY(cudaCheck(cudaEventRecord(L->ev[1], s), "event"));
+		PWA_TRY(cudaCheck(cudaEventSynchronize(L->ev[1]), "autotune sync"));
 		float ms = 0.f;
-		PWA_TRY(cudaCheck(cudaEventElapsedTime(&ms, L->ev[0], L->ev[2]), "elapsed"));
+		PWA_TRY(cudaCheck(cudaEventElapsedTime(&ms, L->ev[0], L->ev[1]), "elapsed"));
 		if (ms < best) {
 			best = ms;
 			bestPlan = c;
@@ -1314,14 +1295,15 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	int maxBlocks = 1;
 	for (const auto& c : cands)
 		maxBlocks = std::max(maxBlocks, c.blocks);
-	L->finBlocks = finalizeBlocks((int)L->rank, (int)W);
 	const size_t nSlot = (size_t)L->rank * W;
 	const size_t nPartial = 2 + 2 * nSlot;
+	const int nGroups = fdfTailGroups(maxBlocks);
 	PWA_TRY(L->dSlotRe.alloc(nSlot * sizeof(int), "slot map"));
 	PWA_TRY(L->dSlotIm.alloc(nSlot * sizeof(int), "slot map"));
 	PWA_TRY(L->dPartials.alloc((size_t)maxBlocks * nPartial * sizeof(double), "partials"));
-	PWA_TRY(L->dFinScratch.alloc((size_t)(2 * L->finBlocks + 2) * sizeof(double), "finalize scratch"));
-	PWA_TRY(L->dTicket.alloc(sizeof(unsigned), "ticket"));
+	PWA_TRY(L->dGroupSums.alloc((size_t)nGroups * nPartial * sizeof(double), "group sums"));
+	PWA_TRY(L->dNormScr.alloc(nSlot * 6 * sizeof(double), "normalisation terms"));
+	PWA_TRY(L->dCounters.alloc((size_t)(nGroups + 1) * sizeof(unsigned), "tail counters"));
 	PWA_TRY(L->dErr.alloc(sizeof(unsigned), "error flag"));
 	PWA_TRY(L->dPar.alloc(L->nPars * sizeof(double), "parameters"));
 	PWA_TRY(L->dOut.alloc((L->nPars + 2) * sizeof(double), "result"));
@@ -1345,7 +1327,7 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	                  "slot upload"));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dSlotIm.p, L->slotIm.data(), nSlot * sizeof(int), cudaMemcpyHostToDevice, s),
 	                  "slot upload"));
-	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dTicket.p, 0, sizeof(unsigned), s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dCounters.p, 0, L->dCounters.bytes, s), "memset"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s), "memset"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "finishInit sync"));
 	if (L->autotune && cands.size() > 1 && L->nEvents >= 65536)
@@ -1845,7 +1827,7 @@ int pwa_likelihood_set_timing(pwa_likelihood* L, int enable)
 		return setError(kErrArg, "null likelihood");
 	if (enable && L->timingEvents.empty()) {
 		PWA_TRY(ensureDevice(L));
-		const size_t n = 3 * 65536;
+		const size_t n = 2 * 65536;
 		L->timingEvents.resize(n, nullptr);
 		for (auto& e : L->timingEvents)
 			PWA_TRY(cudaCheck(cudaEventCreate(&e), "timing event create"));
@@ -1861,13 +1843,11 @@ int pwa_likelihood_kernel_times(pwa_likelihood* L, double* mainMs, double* finMs
 		return setError(kErrArg, "null likelihood");
 	double a = 0., b = 0.;
 	if (L->nTimed > 0)
-		PWA_TRY(cudaCheck(cudaEventSynchronize(L->timingEvents[3 * L->nTimed - 1]), "timing sync"));
+		PWA_TRY(cudaCheck(cudaEventSynchronize(L->timingEvents[2 * L->nTimed - 1]), "timing sync"));
 	for (size_t k = 0; k < L->nTimed; ++k) {
-		float x = 0.f, y = 0.f;
-		PWA_TRY(cudaCheck(cudaEventElapsedTime(&x, L->timingEvents[3 * k], L->timingEvents[3 * k + 1]), "elapsed"));
-		PWA_TRY(cudaCheck(cudaEventElapsedTime(&y, L->timingEvents[3 * k + 1], L->timingEvents[3 * k + 2]), "elapsed"));
+		float x = 0.f;
+		PWA_TRY(cudaCheck(cudaEventElapsedTime(&x, L->timingEvents[2 * k], L->timingEvents[2 * k + 1]), "elapsed"));
 		a += x;
-		b += y;
 	}
 	if (mainMs)
 		*mainMs = a;

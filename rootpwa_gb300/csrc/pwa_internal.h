@@ -70,30 +70,23 @@ struct FdfArgs {
 	const double* par;       // device, [P]
 	const int* slotRe;       // device, [R*W] parameter index of Re(V_rw) or -1
 	const int* slotIm;       // device, [R*W] parameter index of Im(V_rw) or -1
-	double* partials;        // device, [blocks][nPartial]
-	int nPartial;            // 2 + 2*R*W
-	unsigned* devErr;        // device error flags
-	int withGrad;
-	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32
-};
-
-struct FinArgs {
-	const double* partials;
-	int nBlocks, nPartial;
-	const double* par;
-	int P, W0, W, R;
-	const int* slotRe;
-	const int* slotIm;
 	const double* accI;      // device, per reflectivity e: W_e x W_e complex128 (re, im) row-major, e=0 block first
-	double nEvt, totAcc;
-	int prior;
+	double nEvt, totAcc;     // normalisation factor (1 or N) and total acceptance
+	int prior;               // 0 flat, 1 half-Cauchy
 	double cauchyWidth;
 	int withGrad;
-	double* scratch;         // device, [2*gridDim + 2]
-	unsigned* ticket;        // device counter, zero between launches
-	const unsigned* devErr;  // device error flags of the main kernel
+	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32
+	double* partials;        // device, [blocks][nPartial]
+	int nPartial;            // 2 + 2*R*W
+	double* groupSums;       // device, [ceil(blocks/12)][nPartial]
+	double* normScr;         // device, [R*W][6] normalisation / prior terms per slot
+	unsigned* counters;      // device, [ceil(blocks/12) + 1], zero between launches
+	unsigned* devErr;        // device error flags
 	double* out;             // device, [P + 2]: f, gradient, device error status
 };
+
+// Number of groups of the FdF kernel's cross-block sum for a grid.
+int fdfTailGroups(int blocks);
 
 // Store block size for a wave set: 128 when two 128-event tiles fit in shared
 // memory, else 64.
@@ -102,8 +95,6 @@ int chooseStoreBlock(int W, int R, size_t maxSmem);
 int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, size_t maxSmem,
                    std::vector<FdfPlan>* out);
 int launchFdf(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
-int launchFinalize(const FinArgs& args, int finBlocks, cudaStream_t s);
-int finalizeBlocks(int R, int W);
 
 // Converts one wave w of amplitudes (complex64 or complex128, device memory)
 // into the tiled complex64 store, divided by `divisor` in FP64; sets *nonzero
