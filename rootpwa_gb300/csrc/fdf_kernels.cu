@@ -16,8 +16,8 @@
 //   * the store keeps each block of E events contiguous (storeIndex), so one
 //     cp.async.bulk copy moves a tile into shared memory, completing on an
 //     mbarrier; `stages` tiles are in flight;
-//   * while the first tiles load, every CTA computes the normalisation and
-//     prior terms of a few slots in FP64;
+//   * after its event loop every CTA computes the normalisation and prior
+//     terms of a few slots in FP64;
 //   * phase 1: each warp owns E/16 events of the tile, 32/(E/16) lanes per
 //     event sum interleaved slices of the waves and combine them with warp
 //     shuffles, giving L_i, c_i and T_{r,e,i} = c_i S (double-buffered, so
@@ -29,9 +29,9 @@
 //     to its FP64 (or compensated FP32) accumulator;
 //   * the last warp to finish with a stage (shared-memory counter) refills it
 //     with the tile `stages` ahead;
-//   * the tail sums the CTAs' partials in two deterministic levels (groups of
-//     kTailGroup CTAs in index order, then the groups in order), picked by
-//     arrival counters, so results are bitwise reproducible.
+//   * the CTAs' partials are summed exactly in 128-bit fixed point with
+//     integer atomics (order-independent, so results are bitwise
+//     reproducible); the last CTA to arrive writes f and the gradient.
 // Every mbarrier wait is bounded (about a second); on expiry the CTA sets a
 // device error flag, waits (again bounded) for its own copies and completes
 // the tail, and the host discards the result.
@@ -155,7 +155,7 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
 // store's rotated order (storeIndex), moved by a single bulk copy.
 struct SmemLayout {
 	size_t rowStride;  // bytes per wave row
-	size_t tiles, vs, v64, ts, tsw, tot, bars, done, total;
+	size_t tiles, vs, ts, tsw, bars, done, total;
 };
 
 __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
@@ -165,11 +165,9 @@ __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages
 	L.rowStride = (size_t)E * 8;
 	L.tiles = 0;
 	L.vs = up((size_t)stages * W * L.rowStride);
-	L.v64 = up(L.vs + (size_t)W * R * 8);
-	L.ts = up(L.v64 + (size_t)W * R * 16);
+	L.ts = up(L.vs + (size_t)W * R * 8);
 	L.tsw = up(L.ts + 2 * (size_t)R * 2 * E * 8);
-	L.tot = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
-	L.bars = up(L.tot + (2 + 2 * (size_t)R * W) * 8);
+	L.bars = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
 	L.done = L.bars + (size_t)stages * 8;
 	L.total = L.done + (size_t)stages * 4;
 	return L;
@@ -231,8 +229,137 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 // Tiles whose gradient partials are summed in FP32 before the warp
 // reduce-scatter folds them into the FP64 (or compensated) accumulators.
 constexpr int kFold = 8;
-// blocks per group of the two-level cross-block sum
-constexpr int kTailGroup = 12;
+
+
+// Normalisation and prior terms of the slots s = blockIdx.x + j * gridDim.x
+// (warp j mod 16) in FP64, computed at the end of each block's event loop: D = sum_j V_j conj(I_ij) over the same
+// reflectivity, Re(V_i conj(D)), and the half-Cauchy value and gradient
+// (pwaLikelihood.cc:254-297); written to a.normScr.
+__device__ __noinline__ void fdfNormTerms(const FdfArgs& a, int warp, int lane)
+{
+	auto V = [&](int sl) {
+		const int ir = a.slotRe[sl], ii = a.slotIm[sl];
+		return make_double2(ir >= 0 ? a.par[ir] : 0., ii >= 0 ? a.par[ii] : 0.);
+	};
+	const int W = a.W, W0 = a.W0, R = a.R;
+	const int nSlots = R * W;
+	const double g2 = a.cauchyWidth * a.cauchyWidth;
+	for (int j = warp; (int)blockIdx.x + j * (int)gridDim.x < nSlots; j += kWarps) {
+		const int sl = (int)blockIdx.x + j * (int)gridDim.x;
+		const int r = sl / W, g = sl - r * W;
+		const int pos = (g >= W0) ? 1 : 0;
+		const int off = pos ? W0 : 0, We = pos ? W - W0 : W0, i = g - off;
+		const double* Ib = a.accI + (pos ? 2 * (size_t)W0 * W0 : 0) + 2 * (size_t)i * We;
+		double dre = 0., dim = 0.;
+		for (int q = lane; q < We; q += 32) {
+			const double2 u = V(r * W + off + q);
+			const double Ir = Ib[2 * q], Ii = Ib[2 * q + 1];
+			dre += u.x * Ir + u.y * Ii;  // V_q conj(I_iq)
+			dim += u.y * Ir - u.x * Ii;
+		}
+		dre = warpSumD(dre);
+		dim = warpSumD(dim);
+		if (lane == 0) {
+			const double2 v = V(sl);
+			double priorv = 0., pre = 0., pim = 0.;
+			if (a.prior == 1) {
+				const double rr = hypot(v.x, v.y);
+				const double cf = 1. / (1. + (rr * rr) / g2);
+				const double cd = (-2. * rr * g2) / ((g2 + rr * rr) * (g2 + rr * rr));
+				const double fac = (1. / (rr * cf)) * cd;
+				priorv = -log(cf);
+				pre = fac * v.x;
+				pim = fac * v.y;
+			}
+			double* ns = a.normScr + (size_t)sl * 6;
+			ns[0] = dre;
+			ns[1] = dim;
+			ns[2] = v.x * dre + v.y * dim;  // Re(V_i conj(D_i))
+			ns[3] = priorv;
+			ns[4] = pre;
+			ns[5] = pim;
+		}
+	}
+}
+
+// Exact cross-block sums: a value x is added to a 128-bit two's-complement
+// fixed-point accumulator (64 integer, 64 fraction bits) as
+// floor(x) * 2^64 + frac(x) * 2^64 with two 64-bit integer atomics and a
+// carry.  Integer addition is associative, so the totals do not depend on the
+// order in which the blocks arrive (bitwise reproducible), and they are exact
+// up to the conversion of each x below 2^-64.
+// Values outside the fixed-point range (|x| >= 2^63, inf, NaN) go to an FP64
+// accumulator instead: inf and NaN propagate the same way in any order.
+__device__ __forceinline__ void fixedAdd(unsigned long long* acc, double* nf, double x)
+{
+	if (!(fabs(x) < 9.0e18)) {
+		atomicAdd(nf, x);
+		return;
+	}
+	const double fl = floor(x);
+	const unsigned long long hi = (unsigned long long)(long long)fl;
+	const unsigned long long lo = __double2ull_rz((x - fl) * 18446744073709551616.0);  // frac * 2^64
+	const unsigned long long old = atomicAdd(acc, lo);
+	const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
+	atomicAdd(acc + 1, hi + carry);
+}
+
+__device__ __forceinline__ double fixedRead(const unsigned long long* acc, const double* nf)
+{
+	const unsigned long long lo = __ldcg(acc), hi = __ldcg(acc + 1);
+	return ((double)(long long)hi + (double)lo * 5.42101086242752217e-20) + __ldcg(nf);  // lo * 2^-64
+}
+
+// The last block to arrive reads the exact totals, adds the normalisation and
+// prior terms and writes f and the gradient in the parameter layout
+// (pwaLikelihood.cc:300-304, :1716-1731), then clears the accumulators for
+// the next launch.
+__device__ __noinline__ void fdfTail(const FdfArgs& a, unsigned* sLast, double flatD, int tid, int warp, int lane)
+{
+	__threadfence();
+	__syncthreads();
+	if (tid == 0)
+		*sLast = (atomicAdd(a.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+	__syncthreads();
+	if (!*sLast)
+		return;
+	__threadfence();
+	const double nEvt = a.nEvt, twice = 2. * a.nEvt;
+	const int nSlots = a.R * a.W;
+	if (a.withGrad) {
+		for (int sl = tid; sl < nSlots; sl += kThreads) {
+			const double* ns = a.normScr + (size_t)sl * 6;
+			const int ire = a.slotRe[sl], iim = a.slotIm[sl];
+			if (ire >= 0)
+				a.out[1 + ire] = fixedRead(a.fixAcc + 2 * (2 + 2 * sl), a.nfAcc + 2 + 2 * sl) + twice * __ldcg(ns + 0) - __ldcg(ns + 4);
+			if (iim >= 0)
+				a.out[1 + iim] = fixedRead(a.fixAcc + 2 * (3 + 2 * sl), a.nfAcc + 3 + 2 * sl) + twice * __ldcg(ns + 1) - __ldcg(ns + 5);
+		}
+	}
+	if (warp == 0) {
+		double n = 0., p = 0.;
+		for (int sl = lane; sl < nSlots; sl += 32) {
+			n += __ldcg(a.normScr + (size_t)sl * 6 + 2);
+			p += __ldcg(a.normScr + (size_t)sl * 6 + 3);
+		}
+		n = warpSumD(n);
+		p = warpSumD(p);
+		if (lane == 0) {
+			a.out[0] = fixedRead(a.fixAcc, a.nfAcc) + nEvt * (n + flatD * flatD * a.totAcc) + p;
+			if (a.withGrad)
+				a.out[a.P] = flatD * fixedRead(a.fixAcc + 2, a.nfAcc + 1) + twice * flatD * a.totAcc;
+			a.out[a.P + 1] = (double)(*(const volatile unsigned*)a.devErr);
+		}
+	}
+	__syncthreads();
+	const int nUsed = a.withGrad ? a.nPartial : 2;
+	for (int v = tid; v < 2 * nUsed; v += kThreads)
+		a.fixAcc[v] = 0ull;
+	for (int v = tid; v < nUsed; v += kThreads)
+		a.nfAcc[v] = 0.;
+	if (tid == 0)
+		*a.counter = 0u;
+}
 
 template <int R, int E, int WPW>
 __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, const int stages)
@@ -253,12 +380,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);      // [W][R] (vx, vy)
 	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);      // [2][R][2][E] c S
 	float2* Tsw = reinterpret_cast<float2*>(smem + lay.tsw);    // [2][R][2][E] c S, re/im swapped
-	double2* V64 = reinterpret_cast<double2*>(smem + lay.v64);  // [R][W] FP64, slot order
-	double* sTot = reinterpret_cast<double*>(smem + lay.tot);     // [nPartial] totals (final block)
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	unsigned* done = reinterpret_cast<unsigned*>(smem + lay.done);
 	__shared__ double redLL[kWarps], redC[kWarps];
-	__shared__ unsigned sLast;
 
 	// the parameters may be written by the preceding grid (device-side minimiser)
 	gridDependencyWait();
@@ -268,7 +392,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
 		const double vr = ir >= 0 ? a.par[ir] : 0., vi = ii >= 0 ? a.par[ii] : 0.;
 		Vs[k] = make_float2((float)vr, (float)vi);
-		V64[r * W + w] = make_double2(vr, vi);
 	}
 	const double flatD = a.par[a.P - 1];
 	const float flat2 = (float)(flatD * flatD);
@@ -298,52 +421,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	if (warp == 0) {
 		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
 			issue((uint64_t)s, s);
-	}
-
-	// Normalisation and prior terms (pwaLikelihood.cc:254-297) do not depend on
-	// the events: every block computes them in FP64 for the slots
-	// s = blockIdx.x + j * gridDim.x (warp j mod 16) while its first tiles
-	// load.  Per slot: D = sum_j V_j conj(I_ij) over the same reflectivity,
-	// Re(V_i conj(D)), and the half-Cauchy value and gradient.
-	{
-		const int nSlots = R * W;
-		const double g2 = a.cauchyWidth * a.cauchyWidth;
-		for (int j = warp; (int)blockIdx.x + j * (int)gridDim.x < nSlots; j += kWarps) {
-			const int sl = (int)blockIdx.x + j * (int)gridDim.x;
-			const int r = sl / W, g = sl - r * W;
-			const int pos = (g >= W0) ? 1 : 0;
-			const int off = pos ? W0 : 0, We = pos ? W - W0 : W0, i = g - off;
-			const double* Ib = a.accI + (pos ? 2 * (size_t)W0 * W0 : 0) + 2 * (size_t)i * We;
-			double dre = 0., dim = 0.;
-			for (int q = lane; q < We; q += 32) {
-				const double2 u = V64[r * W + off + q];
-				const double Ir = Ib[2 * q], Ii = Ib[2 * q + 1];
-				dre += u.x * Ir + u.y * Ii;  // V_q conj(I_iq)
-				dim += u.y * Ir - u.x * Ii;
-			}
-			dre = warpSumD(dre);
-			dim = warpSumD(dim);
-			if (lane == 0) {
-				const double2 v = V64[sl];
-				double priorv = 0., pre = 0., pim = 0.;
-				if (a.prior == 1) {
-					const double rr = hypot(v.x, v.y);
-					const double cf = 1. / (1. + (rr * rr) / g2);
-					const double cd = (-2. * rr * g2) / ((g2 + rr * rr) * (g2 + rr * rr));
-					const double fac = (1. / (rr * cf)) * cd;
-					priorv = -log(cf);
-					pre = fac * v.x;
-					pim = fac * v.y;
-				}
-				double* ns = a.normScr + (size_t)sl * 6;
-				ns[0] = dre;
-				ns[1] = dim;
-				ns[2] = v.x * dre + v.y * dim;  // Re(V_i conj(D_i))
-				ns[3] = priorv;
-				ns[4] = pre;
-				ns[5] = pim;
-			}
-		}
 	}
 
 	// phase-1 role: event pe of the tile, wave slice ph (waves w = ph mod H)
@@ -581,15 +658,17 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		}
 	}
 
-	// ---- epilogue: block partials [gridDim][nPartial], then a deterministic
-	// two-level sum: the last block of each group of kTailGroup blocks sums
-	// its members in index order, the last group sums the groups in order and
-	// writes f and the gradient (no further kernel) ----
-	// (the previous launch's tail may still read the partials when this grid
-	// starts early under programmatic dependent launch)
+	// Normalisation and prior terms (pwaLikelihood.cc:254-297) do not depend on
+	// the events: every block computes a few slots after its event loop, so
+	// blocks with one tile fewer absorb the work (separate function so that
+	// the event loop keeps its own register allocation)
+	fdfNormTerms(a, warp, lane);
+
+	// ---- epilogue: the block's partials go into the exact fixed-point
+	// accumulators; the last block writes the results ----
+	// (the previous launch's tail may still read the accumulators when this
+	// grid starts early under programmatic dependent launch)
 	gridDependencyWait();
-	const int nP = a.nPartial;
-	double* myPart = a.partials + (size_t)blockIdx.x * nP;
 	if (lane == 0) {
 		if (a.reduction == 0) {
 			redLL[warp] = accLL;
@@ -606,8 +685,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			ll += redLL[wv];
 			cs += redC[wv];
 		}
-		myPart[0] = ll;
-		myPart[1] = cs;
+		fixedAdd(a.fixAcc + 0, a.nfAcc + 0, ll);
+		fixedAdd(a.fixAcc + 2, a.nfAcc + 1, cs);
 	}
 	if (a.withGrad) {
 #pragma unroll
@@ -620,74 +699,14 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				if (wi < nWarpWaves) {
 					const int w = wBase + wi;
 					const double v = (a.reduction == 0) ? accG[q] : ((double)kG[q] - (double)kGc[q]);
-					myPart[2 + (r * W + w) * 2 + comp] = v;
+					const int slotVal = 2 + (r * W + w) * 2 + comp;
+					fixedAdd(a.fixAcc + 2 * slotVal, a.nfAcc + slotVal, v);
 				}
 			}
 		}
 	}
-	__threadfence();
-	__syncthreads();
-	const int grp = (int)blockIdx.x / kTailGroup;
-	const int g0 = grp * kTailGroup, g1 = min((int)gridDim.x, g0 + kTailGroup);
-	const int nGroups = ((int)gridDim.x + kTailGroup - 1) / kTailGroup;
-	if (tid == 0)
-		sLast = (atomicAdd(&a.counters[grp], 1u) == (unsigned)(g1 - g0 - 1)) ? 1u : 0u;
-	__syncthreads();
-	if (!sLast)
-		return;
-	__threadfence();
-	const int nUsed = a.withGrad ? nP : 2;
-	for (int v = tid; v < nUsed; v += kThreads) {
-		double acc = 0.;
-		for (int b = g0; b < g1; ++b)
-			acc += __ldcg(a.partials + (size_t)b * nP + v);
-		a.groupSums[(size_t)grp * nP + v] = acc;
-	}
-	__threadfence();
-	__syncthreads();
-	if (tid == 0) {
-		a.counters[grp] = 0u;  // ready for the next launch
-		sLast = (atomicAdd(&a.counters[nGroups], 1u) == (unsigned)(nGroups - 1)) ? 1u : 0u;
-	}
-	__syncthreads();
-	if (!sLast)
-		return;
-	__threadfence();
-	for (int v = tid; v < nUsed; v += kThreads) {
-		double acc = 0.;
-		for (int gg = 0; gg < nGroups; ++gg)
-			acc += __ldcg(a.groupSums + (size_t)gg * nP + v);
-		sTot[v] = acc;
-	}
-	__syncthreads();
-	const double nEvt = a.nEvt, twice = 2. * a.nEvt;
-	const int nSlots = R * W;
-	if (a.withGrad) {
-		for (int sl = tid; sl < nSlots; sl += kThreads) {
-			const double* ns = a.normScr + (size_t)sl * 6;
-			const int ire = a.slotRe[sl], iim = a.slotIm[sl];
-			if (ire >= 0)
-				a.out[1 + ire] = sTot[2 + 2 * sl] + twice * __ldcg(ns + 0) - __ldcg(ns + 4);
-			if (iim >= 0)
-				a.out[1 + iim] = sTot[3 + 2 * sl] + twice * __ldcg(ns + 1) - __ldcg(ns + 5);
-		}
-	}
-	if (warp == 0) {
-		double n = 0., p = 0.;
-		for (int sl = lane; sl < nSlots; sl += 32) {
-			n += __ldcg(a.normScr + (size_t)sl * 6 + 2);
-			p += __ldcg(a.normScr + (size_t)sl * 6 + 3);
-		}
-		n = warpSumD(n);
-		p = warpSumD(p);
-		if (lane == 0) {
-			a.out[0] = sTot[0] + nEvt * (n + flatD * flatD * a.totAcc) + p;
-			if (a.withGrad)
-				a.out[a.P] = flatD * sTot[1] + twice * flatD * a.totAcc;
-			a.out[a.P + 1] = (double)(*(const volatile unsigned*)a.devErr);
-			a.counters[nGroups] = 0u;
-		}
-	}
+	__shared__ unsigned sLast;
+	fdfTail(a, &sLast, flatD, tid, warp, lane);
 }
 
 __global__ void convertRowKernel(const void* src, int srcIsDouble, float2* store, uint32_t W, uint32_t w, uint32_t B,
@@ -819,8 +838,6 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 		out->erase(out->begin());
 	return kOk;
 }
-
-int fdfTailGroups(int blocks) { return (blocks + kTailGroup - 1) / kTailGroup; }
 
 int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {

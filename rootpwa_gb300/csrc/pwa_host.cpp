@@ -691,7 +691,7 @@ struct pwa_likelihood {
 	// evaluation resources
 	bool autotune = true;
 	FdfPlan plan;
-	DevBuf dSlotRe, dSlotIm, dAccI, dPartials, dGroupSums, dNormScr, dCounters, dErr, dPar, dOut, dFlag;
+	DevBuf dSlotRe, dSlotIm, dAccI, dFixAcc, dNfAcc, dNormScr, dCounter, dErr, dPar, dOut, dFlag;
 	PinnedBuf hPar, hOut;
 	cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
@@ -801,11 +801,11 @@ int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad
 	a.cauchyWidth = L->cauchyWidth;
 	a.withGrad = withGrad;
 	a.reduction = L->reduction;
-	a.partials = L->dPartials.as<double>();
 	a.nPartial = 2 + 2 * a.R * a.W;
-	a.groupSums = L->dGroupSums.as<double>();
+	a.fixAcc = L->dFixAcc.as<unsigned long long>();
+	a.nfAcc = L->dNfAcc.as<double>();
 	a.normScr = L->dNormScr.as<double>();
-	a.counters = L->dCounters.as<unsigned>();
+	a.counter = L->dCounter.as<unsigned>();
 	a.devErr = L->dErr.as<unsigned>();
 	a.out = dOut;
 	cudaEvent_t* te = nullptr;
@@ -1292,18 +1292,14 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	                       &cands));
 	L->plan = cands.front();
 	L->ampTmp.release();
-	int maxBlocks = 1;
-	for (const auto& c : cands)
-		maxBlocks = std::max(maxBlocks, c.blocks);
 	const size_t nSlot = (size_t)L->rank * W;
 	const size_t nPartial = 2 + 2 * nSlot;
-	const int nGroups = fdfTailGroups(maxBlocks);
 	PWA_TRY(L->dSlotRe.alloc(nSlot * sizeof(int), "slot map"));
 	PWA_TRY(L->dSlotIm.alloc(nSlot * sizeof(int), "slot map"));
-	PWA_TRY(L->dPartials.alloc((size_t)maxBlocks * nPartial * sizeof(double), "partials"));
-	PWA_TRY(L->dGroupSums.alloc((size_t)nGroups * nPartial * sizeof(double), "group sums"));
+	PWA_TRY(L->dFixAcc.alloc(nPartial * 2 * sizeof(unsigned long long), "fixed-point accumulators"));
+	PWA_TRY(L->dNfAcc.alloc(nPartial * sizeof(double), "non-finite accumulators"));
 	PWA_TRY(L->dNormScr.alloc(nSlot * 6 * sizeof(double), "normalisation terms"));
-	PWA_TRY(L->dCounters.alloc((size_t)(nGroups + 1) * sizeof(unsigned), "tail counters"));
+	PWA_TRY(L->dCounter.alloc(sizeof(unsigned), "arrival counter"));
 	PWA_TRY(L->dErr.alloc(sizeof(unsigned), "error flag"));
 	PWA_TRY(L->dPar.alloc(L->nPars * sizeof(double), "parameters"));
 	PWA_TRY(L->dOut.alloc((L->nPars + 2) * sizeof(double), "result"));
@@ -1327,7 +1323,9 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	                  "slot upload"));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dSlotIm.p, L->slotIm.data(), nSlot * sizeof(int), cudaMemcpyHostToDevice, s),
 	                  "slot upload"));
-	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dCounters.p, 0, L->dCounters.bytes, s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dCounter.p, 0, L->dCounter.bytes, s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dFixAcc.p, 0, L->dFixAcc.bytes, s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dNfAcc.p, 0, L->dNfAcc.bytes, s), "memset"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s), "memset"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "finishInit sync"));
 	if (L->autotune && cands.size() > 1 && L->nEvents >= 65536)

@@ -76,17 +76,14 @@ struct FdfArgs {
 	double cauchyWidth;
 	int withGrad;
 	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32
-	double* partials;        // device, [blocks][nPartial]
-	int nPartial;            // 2 + 2*R*W
-	double* groupSums;       // device, [ceil(blocks/12)][nPartial]
+	int nPartial;            // 2 + 2*R*W summed values (LL, sum c, gradient re/im per slot)
+	unsigned long long* fixAcc;  // device, [nPartial][2] 128-bit fixed-point totals, zero between launches
+	double* nfAcc;           // device, [nPartial] totals of values outside the fixed-point range, zero between launches
 	double* normScr;         // device, [R*W][6] normalisation / prior terms per slot
-	unsigned* counters;      // device, [ceil(blocks/12) + 1], zero between launches
+	unsigned* counter;       // device, arrival counter, zero between launches
 	unsigned* devErr;        // device error flags
 	double* out;             // device, [P + 2]: f, gradient, device error status
 };
-
-// Number of groups of the FdF kernel's cross-block sum for a grid.
-int fdfTailGroups(int blocks);
 
 // Store block size for a wave set: 128 when two 128-event tiles fit in shared
 // memory, else 64.

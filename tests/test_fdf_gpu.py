@@ -253,3 +253,20 @@ def test_autotuned_plan_matches_oracle():
     check_point(O, G, w["par"])
     G2 = helpers.build_gpu(w, *helpers.integral_pairs(w)[2:])
     assert G2.plan() == (E, stages, blocks)   # cached per shape
+
+
+def test_zero_intensity_event_gives_non_finite_value():
+    """An event with all amplitudes zero and a zero flat amplitude has L_i = 0.
+    The reference's compensated sum turns the -log 0 = inf sample into NaN on
+    the next addition (c = (inf - s) - inf), and its gradient is NaN
+    (-(2/0) * 0).  The engine must report a non-finite value and gradient as
+    well (it keeps +inf), not wrap around in its fixed-point sums."""
+    w = synth.make_workload("compass15", seed=14, n_data=3000, n_mc=3000)
+    w["data"][:, 17] = 0
+    O, G = pair(w)
+    p = w["par"].copy()
+    p[-1] = 0.0
+    f0, g0 = O.FdF(p)
+    f1, g1 = G.FdF(p)
+    assert not np.isfinite(f0) and not np.isfinite(f1)
+    assert np.array_equal(np.isfinite(g1), np.isfinite(g0))
