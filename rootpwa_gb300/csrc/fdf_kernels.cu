@@ -155,7 +155,7 @@ __device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
 // store's rotated order (storeIndex), moved by a single bulk copy.
 struct SmemLayout {
 	size_t rowStride;  // bytes per wave row
-	size_t tiles, vs, ts, tsw, bars, done, total;
+	size_t tiles, vs, v64, ts, tsw, bars, done, total;
 };
 
 __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
@@ -165,7 +165,8 @@ __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages
 	L.rowStride = (size_t)E * 8;
 	L.tiles = 0;
 	L.vs = up((size_t)stages * W * L.rowStride);
-	L.ts = up(L.vs + (size_t)W * R * 8);
+	L.v64 = up(L.vs + (size_t)W * R * 8);
+	L.ts = up(L.v64 + (size_t)W * R * 16);
 	L.tsw = up(L.ts + 2 * (size_t)R * 2 * E * 8);
 	L.bars = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
 	L.done = L.bars + (size_t)stages * 8;
@@ -231,36 +232,130 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 constexpr int kFold = 8;
 
 
-// Normalisation and prior terms of the slots s = blockIdx.x + j * gridDim.x
-// (warp j mod 16) in FP64, computed at the end of each block's event loop: D = sum_j V_j conj(I_ij) over the same
-// reflectivity, Re(V_i conj(D)), and the half-Cauchy value and gradient
-// (pwaLikelihood.cc:254-297); written to a.normScr.
-__device__ __noinline__ void fdfNormTerms(const FdfArgs& a, int warp, int lane)
+// Exact cross-block sums: a value x is truncated to a 128-bit two's-
+// complement fixed-point number X = trunc(x * 2^64) (64 integer, 64 fraction
+// bits), split into four 32-bit limbs; each limb is added to its own 64-bit
+// counter with a fire-and-forget atomic (no carries: a counter cannot
+// overflow for fewer than 2^32 additions).  Integer addition is associative,
+// so the totals do not depend on the order in which blocks arrive (bitwise
+// reproducible).  The conversion uses integer operations on the IEEE-754
+// fields only.  The last block propagates the carries once.
+//
+// Layout of the accumulators: [replica][limb][value] (the last block reads a
+// limb of consecutive values with coalesced loads).
+constexpr int kLimbs = 4;
+
+// Number of replicas of the accumulators: block b adds into replica
+// b % kReplicas, which divides the atomic contention per address.
+constexpr int kReplicas = 8;
+
+// Adds x to value slot `acc` (limb stride `ls` words).  Values outside the
+// fixed-point range (|x| >= 2^63, inf, NaN) go to an FP64 accumulator
+// instead: inf and NaN propagate the same way in any order.
+__device__ __forceinline__ void fixedAdd(unsigned long long* acc, size_t ls, double* nf, double x)
 {
-	auto V = [&](int sl) {
-		const int ir = a.slotRe[sl], ii = a.slotIm[sl];
-		return make_double2(ir >= 0 ? a.par[ir] : 0., ii >= 0 ? a.par[ii] : 0.);
-	};
+	const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+	const int e = (int)((b >> 52) & 0x7ffull);
+	if (e >= 1023 + 63) {  // |x| >= 2^63, inf or NaN
+		atomicAdd(nf, x);
+		return;
+	}
+	// |x| = m 2^(e - 1075); X = m 2^sh with sh = e - 1075 + 64
+	const unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+	const int sh = e - 1011;
+	if (e == 0 || sh <= -53)  // zero, subnormal or below 2^-64
+		return;
+	unsigned long long lo, hi;
+	if (sh >= 64) {
+		lo = 0ull;
+		hi = m << (sh - 64);
+	} else if (sh > 0) {
+		lo = m << sh;
+		hi = m >> (64 - sh);
+	} else {
+		lo = m >> (-sh);
+		hi = 0ull;
+	}
+	if (b >> 63) {  // two's-complement negation of hi:lo
+		lo = ~lo + 1ull;
+		hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+	}
+	const unsigned long long l0 = lo & 0xffffffffull, l1 = lo >> 32, l2 = hi & 0xffffffffull, l3 = hi >> 32;
+	if (l0)
+		atomicAdd(acc, l0);
+	if (l1)
+		atomicAdd(acc + ls, l1);
+	if (l2)
+		atomicAdd(acc + 2 * ls, l2);
+	if (l3)
+		atomicAdd(acc + 3 * ls, l3);
+}
+
+// Exact sum of the kReplicas replicas (replica stride `rs`, limb stride `ls`
+// words) of one value slot with the carries propagated, converted to FP64,
+// plus its out-of-range part; clears the slot for the next launch.
+__device__ __forceinline__ double fixedTake(unsigned long long* acc, size_t rs, size_t ls, double* nf)
+{
+	unsigned long long l[kLimbs] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+	for (int q = 0; q < kReplicas; ++q)
+#pragma unroll
+		for (int k = 0; k < kLimbs; ++k) {
+			unsigned long long* p = acc + q * rs + k * ls;
+			l[k] += __ldcg(p);
+			__stcg(p, 0ull);
+		}
+	// carries: the value is limb3:limb2:limb1:limb0 in base 2^32
+	l[1] += l[0] >> 32;
+	l[2] += l[1] >> 32;
+	l[3] += l[2] >> 32;
+	const unsigned long long lo = (l[0] & 0xffffffffull) | (l[1] << 32);
+	const unsigned long long hi = (l[2] & 0xffffffffull) | (l[3] << 32);
+	const double out = __ldcg(nf);
+	__stcg(nf, 0.);
+	return ((double)(long long)hi + (double)lo * 5.42101086242752217e-20) + out;  // lo * 2^-64
+}
+
+// Normalisation and prior terms (pwaLikelihood.cc:254-297) of a share of
+// the slots in FP64: D = sum_j V_j conj(I_ij) over the same reflectivity and
+// the half-Cauchy value and gradient; nEvt Re(V_i conj(D)) + prior goes into
+// value slot 0 (LL) and 2 nEvt D - prior gradient into the slot's gradient
+// values, so that the exact cross-block sums carry them.  The slots go to the
+// blocks with one tile fewer than the others (they finish a tile earlier), or
+// to all blocks when every block has the same number of tiles; warp j of a
+// block takes its j-th slot.
+__device__ __forceinline__ void fdfNormTerms(const FdfArgs& a, const double2* V64, uint64_t nTiles,
+                                             unsigned long long* myAcc, size_t ls, int warp, int lane)
+{
 	const int W = a.W, W0 = a.W0, R = a.R;
 	const int nSlots = R * W;
+	const int grid = (int)gridDim.x;
+	const int rem = (int)(nTiles % (uint64_t)grid);
+	// blocks b >= rem have one tile fewer when rem > 0
+	const int first = (rem > 0 && nTiles > (uint64_t)grid) ? rem : 0;
+	const int nb = grid - first;
+	if ((int)blockIdx.x < first)
+		return;
+	const int me = (int)blockIdx.x - first;
 	const double g2 = a.cauchyWidth * a.cauchyWidth;
-	for (int j = warp; (int)blockIdx.x + j * (int)gridDim.x < nSlots; j += kWarps) {
-		const int sl = (int)blockIdx.x + j * (int)gridDim.x;
+	for (int j = warp; me + j * nb < nSlots; j += kWarps) {
+		const int sl = me + j * nb;
 		const int r = sl / W, g = sl - r * W;
 		const int pos = (g >= W0) ? 1 : 0;
 		const int off = pos ? W0 : 0, We = pos ? W - W0 : W0, i = g - off;
 		const double* Ib = a.accI + (pos ? 2 * (size_t)W0 * W0 : 0) + 2 * (size_t)i * We;
 		double dre = 0., dim = 0.;
+#pragma unroll 4
 		for (int q = lane; q < We; q += 32) {
-			const double2 u = V(r * W + off + q);
-			const double Ir = Ib[2 * q], Ii = Ib[2 * q + 1];
+			const double2 u = V64[r * W + off + q];
+			const double Ir = __ldg(Ib + 2 * q), Ii = __ldg(Ib + 2 * q + 1);
 			dre += u.x * Ir + u.y * Ii;  // V_q conj(I_iq)
 			dim += u.y * Ir - u.x * Ii;
 		}
 		dre = warpSumD(dre);
 		dim = warpSumD(dim);
 		if (lane == 0) {
-			const double2 v = V(sl);
+			const double2 v = V64[sl];
 			double priorv = 0., pre = 0., pim = 0.;
 			if (a.prior == 1) {
 				const double rr = hypot(v.x, v.y);
@@ -271,50 +366,24 @@ __device__ __noinline__ void fdfNormTerms(const FdfArgs& a, int warp, int lane)
 				pre = fac * v.x;
 				pim = fac * v.y;
 			}
-			double* ns = a.normScr + (size_t)sl * 6;
-			ns[0] = dre;
-			ns[1] = dim;
-			ns[2] = v.x * dre + v.y * dim;  // Re(V_i conj(D_i))
-			ns[3] = priorv;
-			ns[4] = pre;
-			ns[5] = pim;
+			const double twice = 2. * a.nEvt;
+			// Re(V_i conj(D_i))
+			fixedAdd(myAcc, ls, a.nfAcc, a.nEvt * (v.x * dre + v.y * dim) + priorv);
+			if (a.withGrad) {
+				fixedAdd(myAcc + 2 + 2 * sl, ls, a.nfAcc + 2 + 2 * sl, twice * dre - pre);
+				fixedAdd(myAcc + 3 + 2 * sl, ls, a.nfAcc + 3 + 2 * sl, twice * dim - pim);
+			}
 		}
 	}
 }
 
-// Exact cross-block sums: a value x is added to a 128-bit two's-complement
-// fixed-point accumulator (64 integer, 64 fraction bits) as
-// floor(x) * 2^64 + frac(x) * 2^64 with two 64-bit integer atomics and a
-// carry.  Integer addition is associative, so the totals do not depend on the
-// order in which the blocks arrive (bitwise reproducible), and they are exact
-// up to the conversion of each x below 2^-64.
-// Values outside the fixed-point range (|x| >= 2^63, inf, NaN) go to an FP64
-// accumulator instead: inf and NaN propagate the same way in any order.
-__device__ __forceinline__ void fixedAdd(unsigned long long* acc, double* nf, double x)
-{
-	if (!(fabs(x) < 9.0e18)) {
-		atomicAdd(nf, x);
-		return;
-	}
-	const double fl = floor(x);
-	const unsigned long long hi = (unsigned long long)(long long)fl;
-	const unsigned long long lo = __double2ull_rz((x - fl) * 18446744073709551616.0);  // frac * 2^64
-	const unsigned long long old = atomicAdd(acc, lo);
-	const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
-	atomicAdd(acc + 1, hi + carry);
-}
-
-__device__ __forceinline__ double fixedRead(const unsigned long long* acc, const double* nf)
-{
-	const unsigned long long lo = __ldcg(acc), hi = __ldcg(acc + 1);
-	return ((double)(long long)hi + (double)lo * 5.42101086242752217e-20) + __ldcg(nf);  // lo * 2^-64
-}
-
-// The last block to arrive reads the exact totals, adds the normalisation and
-// prior terms and writes f and the gradient in the parameter layout
-// (pwaLikelihood.cc:300-304, :1716-1731), then clears the accumulators for
-// the next launch.
-__device__ __noinline__ void fdfTail(const FdfArgs& a, unsigned* sLast, double flatD, int tid, int warp, int lane)
+// The last block to arrive reads the exact totals and writes f and the
+// gradient in the parameter layout (pwaLikelihood.cc:300-304, :1716-1731),
+// clearing the accumulators for the next launch as it reads them: one value
+// slot per thread.  Value slot 0 holds LL plus the normalisation and prior
+// terms, 1 sum c, 2 + 2 s (+1) the gradient re (im) of production-amplitude
+// slot s.
+__device__ __forceinline__ void fdfTail(const FdfArgs& a, unsigned* sLast, double flatD, int tid)
 {
 	__threadfence();
 	__syncthreads();
@@ -324,41 +393,24 @@ __device__ __noinline__ void fdfTail(const FdfArgs& a, unsigned* sLast, double f
 	if (!*sLast)
 		return;
 	__threadfence();
-	const double nEvt = a.nEvt, twice = 2. * a.nEvt;
-	const int nSlots = a.R * a.W;
-	if (a.withGrad) {
-		for (int sl = tid; sl < nSlots; sl += kThreads) {
-			const double* ns = a.normScr + (size_t)sl * 6;
-			const int ire = a.slotRe[sl], iim = a.slotIm[sl];
-			if (ire >= 0)
-				a.out[1 + ire] = fixedRead(a.fixAcc + 2 * (2 + 2 * sl), a.nfAcc + 2 + 2 * sl) + twice * __ldcg(ns + 0) - __ldcg(ns + 4);
-			if (iim >= 0)
-				a.out[1 + iim] = fixedRead(a.fixAcc + 2 * (3 + 2 * sl), a.nfAcc + 3 + 2 * sl) + twice * __ldcg(ns + 1) - __ldcg(ns + 5);
-		}
-	}
-	if (warp == 0) {
-		double n = 0., p = 0.;
-		for (int sl = lane; sl < nSlots; sl += 32) {
-			n += __ldcg(a.normScr + (size_t)sl * 6 + 2);
-			p += __ldcg(a.normScr + (size_t)sl * 6 + 3);
-		}
-		n = warpSumD(n);
-		p = warpSumD(p);
-		if (lane == 0) {
-			a.out[0] = fixedRead(a.fixAcc, a.nfAcc) + nEvt * (n + flatD * flatD * a.totAcc) + p;
+	const size_t ls = (size_t)a.nPartial, rs = (size_t)kLimbs * ls;
+	const double twice = 2. * a.nEvt;
+	const int nVals = a.withGrad ? a.nPartial : 2;
+	for (int v = tid; v < nVals; v += kThreads) {
+		const unsigned err = (v == 0) ? *(const volatile unsigned*)a.devErr : 0u;
+		const int idx = (v < 2) ? -1 : (((v & 1) == 0) ? a.slotRe[(v - 2) >> 1] : a.slotIm[(v - 2) >> 1]);
+		const double x = fixedTake(a.fixAcc + v, rs, ls, a.nfAcc + v);
+		if (v == 0) {
+			a.out[0] = x + a.nEvt * flatD * flatD * a.totAcc;
+			a.out[a.P + 1] = (double)err;
+			*a.counter = 0u;
+		} else if (v == 1) {
 			if (a.withGrad)
-				a.out[a.P] = flatD * fixedRead(a.fixAcc + 2, a.nfAcc + 1) + twice * flatD * a.totAcc;
-			a.out[a.P + 1] = (double)(*(const volatile unsigned*)a.devErr);
+				a.out[a.P] = flatD * x + twice * flatD * a.totAcc;
+		} else if (idx >= 0) {
+			a.out[1 + idx] = x;
 		}
 	}
-	__syncthreads();
-	const int nUsed = a.withGrad ? a.nPartial : 2;
-	for (int v = tid; v < 2 * nUsed; v += kThreads)
-		a.fixAcc[v] = 0ull;
-	for (int v = tid; v < nUsed; v += kThreads)
-		a.nfAcc[v] = 0.;
-	if (tid == 0)
-		*a.counter = 0u;
 }
 
 template <int R, int E, int WPW>
@@ -378,23 +430,11 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	const SmemLayout lay = smemLayout(W, R, E, stages);
 	float2* tiles = reinterpret_cast<float2*>(smem + lay.tiles);
 	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);      // [W][R] (vx, vy)
+	double2* V64 = reinterpret_cast<double2*>(smem + lay.v64);  // [R][W] FP64, slot order
 	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);      // [2][R][2][E] c S
 	float2* Tsw = reinterpret_cast<float2*>(smem + lay.tsw);    // [2][R][2][E] c S, re/im swapped
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	unsigned* done = reinterpret_cast<unsigned*>(smem + lay.done);
-	__shared__ double redLL[kWarps], redC[kWarps];
-
-	// the parameters may be written by the preceding grid (device-side minimiser)
-	gridDependencyWait();
-	gridDependencyTrigger();
-	for (int k = tid; k < W * R; k += kThreads) {
-		const int w = k / R, r = k - w * R;
-		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
-		const double vr = ir >= 0 ? a.par[ir] : 0., vi = ii >= 0 ? a.par[ii] : 0.;
-		Vs[k] = make_float2((float)vr, (float)vi);
-	}
-	const double flatD = a.par[a.P - 1];
-	const float flat2 = (float)(flatD * flatD);
 
 	const uint64_t nTiles = (a.nEvents + E - 1) / E;
 	const uint64_t first = blockIdx.x, stride = gridDim.x;
@@ -418,10 +458,26 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			bulkCopyG2S(tiles + (size_t)s * W * E, src, stageBytes, &bars[s]);
 		}
 	};
+	// the amplitude store does not change after finishInit (which
+	// synchronises), so the first stages load while the preceding grid ends
 	if (warp == 0) {
 		for (int s = 0; s < stages && (uint64_t)s < myTiles; ++s)
 			issue((uint64_t)s, s);
 	}
+
+	// the parameters may be written by the preceding grid (device-side minimiser)
+	gridDependencyWait();
+	gridDependencyTrigger();
+	for (int k = tid; k < W * R; k += kThreads) {
+		const int w = k / R, r = k - w * R;
+		const int ir = a.slotRe[r * W + w], ii = a.slotIm[r * W + w];
+		const double vr = ir >= 0 ? a.par[ir] : 0., vi = ii >= 0 ? a.par[ii] : 0.;
+		Vs[k] = make_float2((float)vr, (float)vi);
+		V64[r * W + w] = make_double2(vr, vi);
+	}
+	const double flatD = a.par[a.P - 1];
+	const float flat2 = (float)(flatD * flatD);
+	__syncthreads();
 
 	// phase-1 role: event pe of the tile, wave slice ph (waves w = ph mod H)
 	const int pm = lane / H, ph = lane - pm * H;
@@ -658,35 +714,21 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		}
 	}
 
-	// Normalisation and prior terms (pwaLikelihood.cc:254-297) do not depend on
-	// the events: every block computes a few slots after its event loop, so
-	// blocks with one tile fewer absorb the work (separate function so that
-	// the event loop keeps its own register allocation)
-	fdfNormTerms(a, warp, lane);
-
 	// ---- epilogue: the block's partials go into the exact fixed-point
 	// accumulators; the last block writes the results ----
-	// (the previous launch's tail may still read the accumulators when this
-	// grid starts early under programmatic dependent launch)
+	// (the previous launch's tail may still read the accumulators and the
+	// slot scratch when this grid starts early under programmatic dependent
+	// launch)
 	gridDependencyWait();
+
+	const size_t ls = (size_t)a.nPartial;
+	unsigned long long* myAcc = a.fixAcc + (blockIdx.x % kReplicas) * (size_t)kLimbs * ls;
+	// normalisation and prior terms do not depend on the events: blocks with
+	// one tile fewer compute them after their event loop
+	fdfNormTerms(a, V64, nTiles, myAcc, ls, warp, lane);
 	if (lane == 0) {
-		if (a.reduction == 0) {
-			redLL[warp] = accLL;
-			redC[warp] = accC;
-		} else {
-			redLL[warp] = (double)kLL - (double)kLLc;
-			redC[warp] = (double)kC - (double)kCc;
-		}
-	}
-	__syncthreads();
-	if (tid == 0) {
-		double ll = 0., cs = 0.;
-		for (int wv = 0; wv < kWarps; ++wv) {
-			ll += redLL[wv];
-			cs += redC[wv];
-		}
-		fixedAdd(a.fixAcc + 0, a.nfAcc + 0, ll);
-		fixedAdd(a.fixAcc + 2, a.nfAcc + 1, cs);
+		fixedAdd(myAcc + 0, ls, a.nfAcc + 0, (a.reduction == 0) ? accLL : (double)kLL - (double)kLLc);
+		fixedAdd(myAcc + 1, ls, a.nfAcc + 1, (a.reduction == 0) ? accC : (double)kC - (double)kCc);
 	}
 	if (a.withGrad) {
 #pragma unroll
@@ -700,13 +742,13 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					const int w = wBase + wi;
 					const double v = (a.reduction == 0) ? accG[q] : ((double)kG[q] - (double)kGc[q]);
 					const int slotVal = 2 + (r * W + w) * 2 + comp;
-					fixedAdd(a.fixAcc + 2 * slotVal, a.nfAcc + slotVal, v);
+					fixedAdd(myAcc + slotVal, ls, a.nfAcc + slotVal, v);
 				}
 			}
 		}
 	}
 	__shared__ unsigned sLast;
-	fdfTail(a, &sLast, flatD, tid, warp, lane);
+	fdfTail(a, &sLast, flatD, tid);
 }
 
 __global__ void convertRowKernel(const void* src, int srcIsDouble, float2* store, uint32_t W, uint32_t w, uint32_t B,
@@ -838,6 +880,8 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 		out->erase(out->begin());
 	return kOk;
 }
+
+size_t fdfAccumulatorWords(int nPartial) { return (size_t)kReplicas * kLimbs * (size_t)nPartial; }
 
 int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {

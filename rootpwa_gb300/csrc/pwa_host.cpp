@@ -691,7 +691,7 @@ struct pwa_likelihood {
 	// evaluation resources
 	bool autotune = true;
 	FdfPlan plan;
-	DevBuf dSlotRe, dSlotIm, dAccI, dFixAcc, dNfAcc, dNormScr, dCounter, dErr, dPar, dOut, dFlag;
+	DevBuf dSlotRe, dSlotIm, dAccI, dFixAcc, dNfAcc, dCounter, dErr, dPar, dOut, dFlag;
 	PinnedBuf hPar, hOut;
 	cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
@@ -804,7 +804,6 @@ int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad
 	a.nPartial = 2 + 2 * a.R * a.W;
 	a.fixAcc = L->dFixAcc.as<unsigned long long>();
 	a.nfAcc = L->dNfAcc.as<double>();
-	a.normScr = L->dNormScr.as<double>();
 	a.counter = L->dCounter.as<unsigned>();
 	a.devErr = L->dErr.as<unsigned>();
 	a.out = dOut;
@@ -1296,9 +1295,8 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	const size_t nPartial = 2 + 2 * nSlot;
 	PWA_TRY(L->dSlotRe.alloc(nSlot * sizeof(int), "slot map"));
 	PWA_TRY(L->dSlotIm.alloc(nSlot * sizeof(int), "slot map"));
-	PWA_TRY(L->dFixAcc.alloc(nPartial * 2 * sizeof(unsigned long long), "fixed-point accumulators"));
+	PWA_TRY(L->dFixAcc.alloc(fdfAccumulatorWords((int)nPartial) * sizeof(unsigned long long), "fixed-point accumulators"));
 	PWA_TRY(L->dNfAcc.alloc(nPartial * sizeof(double), "non-finite accumulators"));
-	PWA_TRY(L->dNormScr.alloc(nSlot * 6 * sizeof(double), "normalisation terms"));
 	PWA_TRY(L->dCounter.alloc(sizeof(unsigned), "arrival counter"));
 	PWA_TRY(L->dErr.alloc(sizeof(unsigned), "error flag"));
 	PWA_TRY(L->dPar.alloc(L->nPars * sizeof(double), "parameters"));

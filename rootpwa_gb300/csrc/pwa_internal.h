@@ -77,9 +77,8 @@ struct FdfArgs {
 	int withGrad;
 	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32
 	int nPartial;            // 2 + 2*R*W summed values (LL, sum c, gradient re/im per slot)
-	unsigned long long* fixAcc;  // device, [nPartial][2] 128-bit fixed-point totals, zero between launches
+	unsigned long long* fixAcc;  // device, fdfAccumulatorWords(nPartial) 128-bit fixed-point totals, zero between launches
 	double* nfAcc;           // device, [nPartial] totals of values outside the fixed-point range, zero between launches
-	double* normScr;         // device, [R*W][6] normalisation / prior terms per slot
 	unsigned* counter;       // device, arrival counter, zero between launches
 	unsigned* devErr;        // device error flags
 	double* out;             // device, [P + 2]: f, gradient, device error status
@@ -92,6 +91,8 @@ int chooseStoreBlock(int W, int R, size_t maxSmem);
 int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, size_t maxSmem,
                    std::vector<FdfPlan>* out);
 int launchFdf(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
+// 64-bit words of the FdF kernel's fixed-point accumulators (all replicas).
+size_t fdfAccumulatorWords(int nPartial);
 
 // Converts one wave w of amplitudes (complex64 or complex128, device memory)
 // into the tiled complex64 store, divided by `divisor` in FP64; sets *nonzero
