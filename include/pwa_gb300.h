@@ -133,6 +133,27 @@ int pwa_integral_renormalize(pwa_integral* I, uint64_t nmbEventsRenorm);
 /* writeAscii / readAscii (ampIntegralMatrix.cc:503-570, file variants :573-608) */
 int pwa_integral_read_ascii(pwa_integral* I, const char* path);
 int pwa_integral_write_ascii(const pwa_integral* I, const char* path);
+/*
+ * No reference counterpart: the raw sums of integrate()'s Gram product
+ * (ampIntegralMatrix.cc:408-469), I_ij = sum_k w_k A_ik conj(A_jk), from
+ * device memory to device memory, allocating nothing.  amps: complex64
+ * [nWaves][ldK] on the current device (nK events used per row); weights:
+ * NULL or nK doubles on the device; out: nWaves x nWaves complex128
+ * row-major on the device, full Hermitian matrix of raw sums (divide by the
+ * event count for element()).  precision: PWA_PRECISION_FP64 or
+ * PWA_PRECISION_FP32 (SIMT kernels).  Asynchronous on `stream`.
+ * Partial sums go to a fixed 8 MiB device array (no cudaMalloc, no cudaFree,
+ * no host synchronisation), for callers that must not allocate, e.g. one
+ * integral per kinematic bin issued back to back on several streams, where a
+ * cudaFree would synchronise the whole device.  Limits: nWaves <= 256
+ * (PWA_GRAM_NOALLOC_MAX_WAVES); larger sets return PWA_ERROR_INVALID_ARGUMENT.  The first
+ * call on a device (that device current) resolves the array's address and
+ * has to precede any stream capture.  Calls that overlap in time share the
+ * array and race: order them on one stream.
+ */
+#define PWA_GRAM_NOALLOC_MAX_WAVES 256
+int pwa_gram_device_noalloc(const void* amps, uint64_t nK, uint64_t ldK, uint32_t nWaves, const double* weights,
+                            int precision, double* out, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* pwaLikelihood                                                              */

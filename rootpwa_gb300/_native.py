@@ -68,6 +68,7 @@ SIGNATURES = {
     "pwa_integral_renormalize": (i, [vp, u64]),
     "pwa_integral_read_ascii": (i, [vp, cc]),
     "pwa_integral_write_ascii": (i, [vp, cc]),
+    "pwa_gram_device_noalloc": (i, [vp, u64, u64, u32, vp, i, vp, vp]),
     "pwa_likelihood_create": (i, [pvp]),
     "pwa_likelihood_destroy": (i, [vp]),
     "pwa_likelihood_use_normalized_amps": (i, [vp, i]),
