@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	constexpr int NQ = (NV + 31) / 32;       // rounds of 32
 	constexpr int NVP = NQ * 32;
 	constexpr int EPAIRS = E / 64;           // event pairs per lane per tile
-	static_assert(EPW * kWarps == E && H * EPW == 32, "tile shape");
+	static_assert(EPW * kWarps == E && H * EPW == 32 && H == 512 / E, "tile shape");
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const int W = a.W, W0 = a.W0;
@@ -532,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				Sa[r][1] = make_float2(0.f, 0.f);
 			}
 			// every row this lane reads has the same rotation (w = ph mod H)
-			const int rot1 = EPW * (ph % (16 / EPW));
+			const int rot1 = (int)storeRot((uint32_t)ph, (uint32_t)E);  // 512 / E == H
 			const uint32_t colAddr = smemAddr(tile + ((pe + rot1) & (E - 1)));
 			const uint32_t vAddr = smemAddr(Vs);
 			const uint32_t rowB = (uint32_t)lay.rowStride;
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				for (int wi = 0; wi < WPW; ++wi) {
 					if (wi < nWarpWaves) {
 						const int w = wBase + wi;
-						const int pos = (ev + EPW * (w % (16 / EPW))) & (E - 1);
+						const int pos = (ev + (int)storeRot((uint32_t)w, (uint32_t)E)) & (E - 1);
 						const float4 av = lds128(tAddr + (uint32_t)(w * E + pos) * 8u);
 						const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
 #pragma unroll

@@ -40,16 +40,19 @@ enum { kDevErrTimeout = 1 };
 // sets).  Block b holds the W wave rows of its B events contiguously (waves of
 // negative reflectivity first), so one bulk copy moves one tile.  Row w keeps
 // event b*B + p at position (p + rot(w)) mod B with
-// rot(w) = (B/16) * (w mod (256/B)): the rotation spreads the rows that one
-// warp reads together in the FdF kernel's first phase over all shared-memory
-// banks.  The last block is zero-padded.
+// rot(w) = (B/32) * (w mod (512/B)).  In the FdF kernel's first phase a
+// half-warp reads 512/B consecutive rows (w mod 512/B = 0, 1, ...) at the
+// same B/32 events; the rotation puts those pieces at distinct offsets
+// (B/32 events = 32 bytes apart for B = 128), so they fall on distinct
+// shared-memory banks.  Rotations are even, so event pairs (p, p+1) with p
+// even never wrap.  The last block is zero-padded.
+__host__ __device__ inline uint32_t storeRot(uint32_t w, uint32_t B) { return (B / 32) * (w % (512 / B)); }
+
 __host__ __device__ inline uint64_t storeIndex(uint32_t w, uint64_t e, uint32_t W, uint32_t B)
 {
 	const uint64_t b = e / B;
 	const uint32_t p = (uint32_t)(e - b * B);
-	const uint32_t epw = B / 16;
-	const uint32_t rot = epw * (w % (16 / epw));
-	return (b * W + w) * B + ((p + rot) & (B - 1));
+	return (b * W + w) * B + ((p + storeRot(w, B)) & (B - 1));
 }
 
 // ---------------------------------------------------------------------------
