@@ -1,11 +1,569 @@
-// gram_tc.cu -- tensor-core (tcgen05) Gram kernel for the integral matrices.
+// gram_tc.cu -- tcgen05 tensor-core Gram kernel for the integral matrices.
+//
+// Computes the raw sums of ampIntegralMatrix::integrate
+// (decayAmplitude/ampIntegralMatrix.cc:408-469)
+//   I_ij = sum_k w_k A_{i,k} conj(A_{j,k})
+// from real products of the planar parts Ar = Re A, Ai = Im A (one column per
+// event k):
+//   Re I = Ar Ar^T + Ai Ai^T,   Im I = D - D^T with D = Ai Ar^T.
+// Weights enter as sqrt(w_k) on both sides (the host passes w_k >= 0).
+//
+// One persistent CTA per SM owns a contiguous range of events.  Per tile of
+// 32 events:
+//   - one TMA load brings the complex64 rows [W][32] (interleaved re, im)
+//     into a raw shared-memory stage (warp 8);
+//   - eight converter warps split re / im into the planar operand in the
+//     canonical K-major 128-byte-swizzled layout, Ar in rows 0..127 and Ai in
+//     rows 128..255 (TF32: one plane rounded to TF32; TF32x3: hi = tf32(x),
+//     lo = tf32(x - hi)), weighted;
+//   - one thread of warp 9 issues tcgen05.mma kind::tf32 (M = 128, N = W
+//     rounded up to 16, K = 8 per instruction) into two FP32 accumulators
+//     (Re, D) in tensor memory; TF32x3 adds the cross products hi lo^T and
+//     lo hi^T before hi hi^T.
+// The tensor cores add into FP32 accumulators with truncation, so a long
+// chain of accumulations drifts towards zero by a fraction of an ulp per
+// instruction.  The accumulators therefore start from zero every `period`
+// tiles, and four drain warps (10..13) add them into a second pair of FP32
+// accumulators in tensor memory with round-to-nearest additions; cross
+// products come first in each tile so that their truncation acts on small
+// partial sums.  At the end the drain warps store the CTA's FP32 partials; a
+// second kernel sums the partials of all CTAs in FP64 in a fixed order and
+// assembles the Hermitian matrix.
+//
+// Every wait on an mbarrier is bounded (1 s of globaltimer): on expiry the
+// CTA records kDevErrTimeout, stops issuing work, waits (bounded) for its own
+// TMA copies and MMAs in flight and frees its tensor memory before it exits.
+
 #include "pwa_internal.h"
 
-namespace pwa {
+#include <cuda.h>
 
-int launchGramTc(const GramArgs&, int, int, cudaStream_t, double*, double*, size_t)
+#include <algorithm>
+#include <mutex>
+
+namespace pwa {
+namespace {
+
+#define PWA_CHECK_RET(expr)     \
+	do {                        \
+		const int _st = (expr); \
+		if (_st != kOk)         \
+			return _st;         \
+	} while (0)
+
+constexpr int kKT = 32;                   // events per tile (128-byte swizzle row of TF32)
+constexpr int kConvWarps = 8;             // converter warps 0..7
+constexpr int kTmaWarp = kConvWarps;      // warp 8
+constexpr int kMmaWarp = kConvWarps + 1;  // warp 9
+constexpr int kDrainWarp0 = kConvWarps + 2;  // warps 10..13 (one warpgroup)
+constexpr int kThreadsTc = (kConvWarps + 6) * 32;
+constexpr int kOpBufs = 2;
+constexpr int kTmemCols = 512;
+constexpr uint32_t kPlaneBytes = 256u * 128u;  // Ar rows 0..127, Ai rows 128..255
+constexpr unsigned long long kWaitNs = 1000000000ull;
+
+struct TcArgs {
+	uint64_t K;         // events (columns)
+	int W;              // waves (<= 128)
+	int N;              // MMA N: W rounded up to 16
+	int planes;         // 1 (TF32) or 2 (TF32x3: hi, lo)
+	int stages;         // raw TMA stages
+	int period;         // tiles between drains of the accumulators
+	uint64_t tilesTotal;
+	const double* weightK;  // per event, or null
+	float* partials;        // [grid][2 (Re, D)][128][N]
+	unsigned* devErr;
+};
+
+__device__ __forceinline__ uint32_t sAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long nowNs()
 {
-	return setError(kErrUnsupported, "tensor-core Gram kernel not available in this build");
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+__device__ __forceinline__ void barInit(uint64_t* b, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sAddr(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void barArrive(uint64_t* b)
+{
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(sAddr(b)) : "memory");
+}
+
+__device__ __forceinline__ void barExpectTx(uint64_t* b, uint32_t bytes)
+{
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(sAddr(b)),
+	             "r"(bytes)
+	             : "memory");
+}
+
+__device__ __forceinline__ bool barTry(uint64_t* b, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(sAddr(b)), "r"(parity)
+	    : "memory");
+	return ok != 0;
+}
+
+// bounded wait for the completion of phase `parity`
+__device__ bool barWait(uint64_t* b, uint32_t parity)
+{
+	if (barTry(b, parity))
+		return true;
+	const unsigned long long t0 = nowNs();
+	while (!barTry(b, parity))
+		if (nowNs() - t0 > kWaitNs)
+			return false;
+	return true;
+}
+
+__device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
+{
+	asm volatile(
+	    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+	        sAddr(dst)),
+	    "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(sAddr(bar))
+	    : "memory");
+}
+
+__device__ __forceinline__ float tf32Round(float x)
+{
+	uint32_t r;
+	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+	return __uint_as_float(r);
+}
+
+// K-major, 128-byte swizzle shared-memory matrix descriptor (tcgen05 format):
+// start address >> 4 at [0,14), leading byte offset >> 4 at [16,30) (unused
+// for swizzled K-major layouts), stride byte offset >> 4 at [32,46) = 1024 B
+// between groups of 8 rows, version 1 at [46,48), swizzle mode 2 (128 B) at
+// [61,64).
+__device__ __forceinline__ uint64_t smemDesc(uint32_t addr)
+{
+	return (uint64_t)((addr & 0x3ffffu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+	       ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// instruction descriptor of kind::tf32: D format F32 at [4,6), A and B
+// format TF32 (2) at [7,10) and [10,13), both K-major, N >> 3 at [17,23),
+// M >> 4 at [24,29)
+__host__ __device__ constexpr uint32_t idescTf32(int M, int N)
+{
+	return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mmaTf32(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dTmem),
+	    "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(acc)
+	    : "memory");
+}
+
+__device__ __forceinline__ void mmaCommit(uint64_t* bar)
+{
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(sAddr(bar))
+	             : "memory");
+}
+
+// byte offset of element (row r, column k < 32) in a K-major 128-byte
+// swizzled TF32 tile: 8-row groups of 1024 B, 16-byte chunks XOR row % 8
+__device__ __forceinline__ uint32_t swzOffset(int r, int k)
+{
+	return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + (k & 3) * 4);
+}
+
+__device__ __forceinline__ void tmemLd16(uint32_t taddr, uint32_t (&r)[16])
+{
+	asm volatile(
+	    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+	    "%15}, [%16];"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+	      "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+	    : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmemSt16(uint32_t taddr, const uint32_t (&r)[16])
+{
+	asm volatile(
+	    "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+	    "%15, %16};" ::"r"(taddr),
+	    "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+	    "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+	    : "memory");
+}
+
+__global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_constant__ CUtensorMap map, const TcArgs a)
+{
+	extern __shared__ __align__(1024) unsigned char smemRaw[];
+	unsigned char* smem =
+	    reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
+	const int W = a.W, N = a.N;
+	const uint32_t rawBytes = (uint32_t)W * 256u;
+	const uint32_t rawStride = (rawBytes + 1023u) & ~1023u;
+	unsigned char* ops = smem;                                            // [kOpBufs][planes][256 rows x 128 B]
+	unsigned char* raw = ops + (size_t)kOpBufs * a.planes * kPlaneBytes;  // [stages][W][64 floats]
+	uint64_t* bars = reinterpret_cast<uint64_t*>(raw + (size_t)a.stages * rawStride);
+	uint64_t* rawFull = bars;
+	uint64_t* rawEmpty = bars + a.stages;
+	uint64_t* opFull = bars + 2 * a.stages;
+	uint64_t* opEmpty = opFull + kOpBufs;
+	uint64_t* drainReady = opEmpty + kOpBufs;
+	uint64_t* drainDone = drainReady + 1;
+	uint64_t* mmaFinal = drainDone + 1;
+	uint32_t* tmemHolder = reinterpret_cast<uint32_t*>(mmaFinal + 1);
+	__shared__ unsigned sFail;
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const uint64_t t0 = (uint64_t)blockIdx.x * a.tilesTotal / gridDim.x;
+	const uint64_t t1 = (uint64_t)(blockIdx.x + 1) * a.tilesTotal / gridDim.x;
+	const int nT = (int)(t1 - t0);
+	const int nDrains = (nT + a.period - 1) / a.period;
+
+	if (tid == 0) {
+		for (int s = 0; s < a.stages; ++s) {
+			barInit(&rawFull[s], 1);
+			barInit(&rawEmpty[s], kConvWarps);
+		}
+		for (int b = 0; b < kOpBufs; ++b) {
+			barInit(&opFull[b], kConvWarps);
+			barInit(&opEmpty[b], 1);
+		}
+		barInit(drainReady, 1);
+		barInit(drainDone, 4);
+		barInit(mmaFinal, 1);
+		sFail = 0u;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	if (warp == kMmaWarp) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sAddr(tmemHolder)),
+		             "r"(kTmemCols)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	// rows W..127 (Ar) and 128+W..255 (Ai) of every operand plane stay zero
+	if (warp < kConvWarps) {
+		const int padWords = (128 - W) * 32;
+		for (int b = 0; b < kOpBufs * a.planes; ++b)
+			for (int h = 0; h < 2; ++h) {
+				uint32_t* p = reinterpret_cast<uint32_t*>(ops + (size_t)b * kPlaneBytes + (size_t)(h * 128 + W) * 128);
+				for (int i = tid; i < padWords; i += kConvWarps * 32)
+					p[i] = 0u;
+			}
+		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = *tmemHolder;
+	// tensor-memory columns: working Re [0, N), D [N, 2N); sums Re [2N, 3N), D [3N, 4N)
+
+	if (warp == kTmaWarp) {
+		// ---- producer: one TMA load per tile ----
+		if (lane == 0) {
+			asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map)) : "memory");
+			int issued = 0;
+			for (int t = 0; t < nT; ++t) {
+				const int s = t % a.stages;
+				if (t >= a.stages && !barWait(&rawEmpty[s], (uint32_t)(((t / a.stages) - 1) & 1))) {
+					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+					sFail = 1u;
+					break;
+				}
+				if (*(volatile unsigned*)&sFail)
+					break;
+				barExpectTx(&rawFull[s], rawBytes);
+				tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * kKT), 0, &rawFull[s]);
+				++issued;
+			}
+			// the copies of this CTA land before it exits
+			for (int t = (issued > a.stages ? issued - a.stages : 0); t < issued; ++t)
+				barWait(&rawFull[t % a.stages], (uint32_t)((t / a.stages) & 1));
+		}
+	} else if (warp == kMmaWarp) {
+		// ---- MMA issuer ----
+		if (lane == 0) {
+			const uint32_t idesc = idescTf32(128, N);
+			const uint32_t opBase = sAddr(ops);
+			const uint32_t accRe = tmem, accD = tmem + (uint32_t)N;
+			bool freshRe = true, freshD = true;
+			// one product over the tile: acc += A B^T, 4 instructions of K = 8
+			auto product = [&](uint32_t acc, bool& fresh, uint32_t aOp, uint32_t bOp) {
+				for (int kk = 0; kk < kKT / 8; ++kk) {
+					mmaTf32(acc, smemDesc(aOp + (uint32_t)kk * 32u), smemDesc(bOp + (uint32_t)kk * 32u), idesc,
+					        fresh ? 0u : 1u);
+					fresh = false;
+				}
+			};
+			for (int t = 0; t < nT; ++t) {
+				const int b = t % kOpBufs;
+				if (t > 0 && t % a.period == 0) {
+					// the drain of the previous period has read the working accumulators
+					if (!barWait(drainDone, (uint32_t)(((t / a.period) - 1) & 1))) {
+						atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+						sFail = 1u;
+						break;
+					}
+					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+					freshRe = freshD = true;
+				}
+				if (!barWait(&opFull[b], (uint32_t)((t / kOpBufs) & 1))) {
+					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+					sFail = 1u;
+					break;
+				}
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				const uint32_t hi = opBase + (uint32_t)b * a.planes * kPlaneBytes;
+				const uint32_t arH = hi, aiH = hi + 16384u;
+				if (a.planes == 2) {
+					const uint32_t arL = hi + kPlaneBytes, aiL = arL + 16384u;
+					product(accRe, freshRe, arH, arL);
+					product(accRe, freshRe, arL, arH);
+					product(accRe, freshRe, aiH, aiL);
+					product(accRe, freshRe, aiL, aiH);
+					product(accD, freshD, aiH, arL);
+					product(accD, freshD, aiL, arH);
+				}
+				product(accRe, freshRe, arH, arH);
+				product(accRe, freshRe, aiH, aiH);
+				product(accD, freshD, aiH, arH);
+				mmaCommit(&opEmpty[b]);
+				if ((t + 1) % a.period == 0 || t + 1 == nT)
+					mmaCommit(drainReady);
+			}
+			// all MMAs of this CTA complete before tensor memory is freed
+			mmaCommit(mmaFinal);
+			if (!barWait(mmaFinal, 0u))
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+		}
+	} else if (warp >= kDrainWarp0) {
+		// ---- drain: sums += working accumulators (round to nearest) ----
+		const int q = warp & 3;  // lane quarter of tensor memory
+		const uint32_t rowBase = tmem + ((uint32_t)(q * 32) << 16);
+		bool ok = true;
+		for (int d = 0; d < nDrains; ++d) {
+			if (!barWait(drainReady, (uint32_t)(d & 1))) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				ok = false;
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			for (int c = 0; c < 2 * N; c += 16) {
+				uint32_t w[16], s[16];
+				tmemLd16(rowBase + (uint32_t)c, w);
+				if (d > 0)
+					tmemLd16(rowBase + (uint32_t)(2 * N + c), s);
+				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+				if (d > 0)
+#pragma unroll
+					for (int i = 0; i < 16; ++i)
+						w[i] = __float_as_uint(__uint_as_float(w[i]) + __uint_as_float(s[i]));
+				tmemSt16(rowBase + (uint32_t)(2 * N + c), w);
+			}
+			asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+			__syncwarp();
+			if (lane == 0)
+				barArrive(drainDone);
+		}
+		if (ok) {
+			// partials of this CTA: [2][128][N], rows < W
+			const int row = q * 32 + lane;
+			for (int c = 0; c < 2 * N; c += 16) {
+				uint32_t r[16];
+				tmemLd16(rowBase + (uint32_t)(2 * N + c), r);
+				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+				if (row < W) {
+					const int part = c / N, col = c - part * N;
+					float4* d4 = reinterpret_cast<float4*>(
+					    a.partials + (((size_t)blockIdx.x * 2 + part) * 128 + row) * N + col);
+#pragma unroll
+					for (int i = 0; i < 4; ++i)
+						d4[i] = make_float4(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1]),
+						                    __uint_as_float(r[4 * i + 2]), __uint_as_float(r[4 * i + 3]));
+				}
+			}
+		}
+	} else {
+		// ---- converters: raw interleaved rows -> planar swizzled operand ----
+		const int sub = lane >> 4, p = lane & 15;  // wave of the pair, event pair
+		for (int t = 0; t < nT; ++t) {
+			const int s = t % a.stages, b = t % kOpBufs;
+			if (!barWait(&rawFull[s], (uint32_t)((t / a.stages) & 1)) ||
+			    (t >= kOpBufs && !barWait(&opEmpty[b], (uint32_t)(((t / kOpBufs) - 1) & 1)))) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				sFail = 1u;
+				break;
+			}
+			const float* rs = reinterpret_cast<const float*>(raw + (size_t)s * rawStride);
+			unsigned char* hiP = ops + (size_t)b * a.planes * kPlaneBytes;
+			unsigned char* loP = hiP + kPlaneBytes;
+			const uint64_t k0 = (t0 + t) * (uint64_t)kKT + 2u * p;
+			float w0 = 1.f, w1 = 1.f;
+			if (a.weightK) {
+				w0 = (k0 < a.K) ? sqrtf((float)a.weightK[k0]) : 0.f;
+				w1 = (k0 + 1 < a.K) ? sqrtf((float)a.weightK[k0 + 1]) : 0.f;
+			}
+			for (int w = 2 * warp + sub; w < W; w += 2 * kConvWarps) {
+				const float4 v = *reinterpret_cast<const float4*>(rs + w * 64 + 4 * p);
+				const float re0 = v.x * w0, im0 = v.y * w0, re1 = v.z * w1, im1 = v.w * w1;
+				const uint32_t oRe = swzOffset(w, 2 * p), oIm = swzOffset(128 + w, 2 * p);
+				const float2 hre = make_float2(tf32Round(re0), tf32Round(re1));
+				const float2 him = make_float2(tf32Round(im0), tf32Round(im1));
+				*reinterpret_cast<float2*>(hiP + oRe) = hre;
+				*reinterpret_cast<float2*>(hiP + oIm) = him;
+				if (a.planes == 2) {
+					*reinterpret_cast<float2*>(loP + oRe) =
+					    make_float2(tf32Round(re0 - hre.x), tf32Round(re1 - hre.y));
+					*reinterpret_cast<float2*>(loP + oIm) =
+					    make_float2(tf32Round(im0 - him.x), tf32Round(im1 - him.y));
+				}
+			}
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+			__syncwarp();
+			if (lane == 0) {
+				barArrive(&rawEmpty[s]);
+				barArrive(&opFull[b]);
+			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	if (warp == kMmaWarp) {
+		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+	}
+}
+
+// FP64 sum of the CTAs' partials in CTA order; assembles the Hermitian matrix
+// (upper triangle from Re and D, lower mirrored, real diagonal).
+__global__ void gramTcReduceKernel(const float* partials, int grid, int W, int N, double* out)
+{
+	const int n = W * W;
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+		const int i = e / W, j = e - i * W;
+		if (i > j)
+			continue;
+		double re = 0., im = 0.;
+		for (int c = 0; c < grid; ++c) {
+			const float* Re = partials + (size_t)c * 2 * 128 * N;
+			const float* D = Re + (size_t)128 * N;
+			re += (double)Re[(size_t)i * N + j];
+			im += (double)D[(size_t)i * N + j] - (double)D[(size_t)j * N + i];
+		}
+		if (i == j)
+			im = 0.;
+		out[(size_t)e * 2] = re;
+		out[(size_t)e * 2 + 1] = im;
+		out[((size_t)j * W + i) * 2] = re;
+		out[((size_t)j * W + i) * 2 + 1] = -im;
+	}
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encodeTiled(EncodeTiledFn* fn)
+{
+	static std::mutex m;
+	static EncodeTiledFn cached = nullptr;
+	std::lock_guard<std::mutex> lock(m);
+	if (!cached) {
+		void* p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+		if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+			return setError(kErrCuda, "cuTensorMapEncodeTiled is not available from the driver");
+		cached = reinterpret_cast<EncodeTiledFn>(p);
+	}
+	*fn = cached;
+	return kOk;
+}
+
+}  // namespace
+
+size_t gramTcScratchFloats(int W, int numSMs)
+{
+	const int N = ((W + 15) / 16) * 16;
+	return (size_t)numSMs * 2 * 128 * N;
+}
+
+int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, double* out, double* scratch,
+                 size_t scratchDoubles)
+{
+	if (precision != 2 && precision != 3)
+		return setError(kErrUnsupported, "tensor-core Gram: precision must be TF32 or TF32x3");
+	if (g.amps64 || !g.amps)
+		return setError(kErrUnsupported, "tensor-core Gram: complex64 amplitudes required");
+	if (g.W < 1 || g.W > 128)
+		return setError(kErrUnsupported, "tensor-core Gram supports 1..128 waves");
+	if ((g.ldK & 1ull) || (reinterpret_cast<uintptr_t>(g.amps) & 15u))
+		return setError(kErrUnsupported, "tensor-core Gram needs an even row stride and a 16-byte aligned base");
+	if (g.K == 0)
+		return setError(kErrArg, "tensor-core Gram: no events");
+	int dev = 0;
+	PWA_CHECK_RET(cudaCheck(cudaGetDevice(&dev), "cudaGetDevice"));
+	int maxSmem = 0;
+	PWA_CHECK_RET(cudaCheck(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem"));
+
+	TcArgs a{};
+	a.K = g.K;
+	a.W = g.W;
+	a.N = ((g.W + 15) / 16) * 16;
+	a.planes = (precision == 3) ? 2 : 1;
+	a.period = (precision == 3) ? 1 : 8;
+	a.tilesTotal = (g.K + kKT - 1) / kKT;
+	a.weightK = g.weightK;
+	a.devErr = g.devErr;
+	const size_t rawStride = ((size_t)g.W * 256 + 1023) & ~size_t(1023);
+	const size_t fixed = 1024 /* alignment */ + (size_t)kOpBufs * a.planes * kPlaneBytes + 256 /* barriers */;
+	a.stages = 4;
+	while (a.stages > 2 && fixed + a.stages * rawStride > (size_t)maxSmem)
+		--a.stages;
+	size_t smemBytes = fixed + a.stages * rawStride;
+	if (smemBytes > (size_t)maxSmem)
+		return setError(kErrUnsupported, "tensor-core Gram: shared memory too small for this wave count");
+	// one CTA per SM: each CTA allocates all 512 tensor-memory columns
+	smemBytes = std::max(smemBytes, (size_t)maxSmem / 2 + 2048);
+	const int grid = (int)std::min<uint64_t>((uint64_t)numSMs, a.tilesTotal);
+	const size_t need = (size_t)grid * 2 * 128 * a.N;
+	if (need > scratchDoubles * 2)
+		return setError(kErrArg, "tensor-core Gram: scratch too small");
+	a.partials = reinterpret_cast<float*>(scratch);
+
+	EncodeTiledFn enc = nullptr;
+	PWA_CHECK_RET(encodeTiled(&enc));
+	CUtensorMap map;
+	const cuuint64_t dims[2] = {(cuuint64_t)(2 * g.K), (cuuint64_t)g.W};
+	const cuuint64_t strides[1] = {(cuuint64_t)(g.ldK * 8)};
+	const cuuint32_t box[2] = {64u, (cuuint32_t)g.W};
+	const cuuint32_t estr[2] = {1u, 1u};
+	const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(g.amps), dims, strides, box,
+	                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+	                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	if (cr != CUDA_SUCCESS)
+		return setError(kErrCuda, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
+
+	PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                             (int)smemBytes),
+	                        "gram TC smem attribute"));
+	gramTcKernel<<<grid, kThreadsTc, smemBytes, s>>>(map, a);
+	countLaunches(1);
+	PWA_CHECK_RET(cudaCheck(cudaGetLastError(), "gram TC launch"));
+	const int n = g.W * g.W;
+	const int blocks = std::max(1, std::min(1024, (n + 255) / 256));
+	gramTcReduceKernel<<<blocks, 256, 0, s>>>(a.partials, grid, g.W, a.N, out);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "gram TC reduce launch");
 }
 
 }  // namespace pwa

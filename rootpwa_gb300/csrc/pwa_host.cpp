@@ -202,6 +202,10 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device amplitudes"));
 	const uint64_t ldIn = nEvents * nSub;
 	const bool wantDouble = (precision == PWA_PRECISION_FP64 && ampType == PWA_COMPLEX128);
+	const bool tensorCore = (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3);
+	// the tensor-core kernel reads rows with TMA: even row stride (16-byte
+	// multiple) and a 16-byte aligned base
+	const uint64_t ldPad = tensorCore ? (K + (K & 1ull)) : K;
 	DevBuf dIn, dConv, dW, dPart, dOut, dErr;
 	const float2* a32 = nullptr;
 	const double2* a64 = nullptr;
@@ -209,35 +213,49 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 	if (memory == PWA_MEMORY_DEVICE) {
 		if (ampType == PWA_COMPLEX64) {
 			a32 = static_cast<const float2*>(amps);
+			if (tensorCore && ((ldIn & 1ull) || (reinterpret_cast<uintptr_t>(amps) & 15u))) {
+				PWA_TRY(dConv.alloc((size_t)W * ldPad * sizeof(float2), "integral alignment buffer"));
+				PWA_TRY(cudaCheck(cudaMemcpy2DAsync(dConv.p, ldPad * sizeof(float2), amps, ldIn * sizeof(float2),
+				                                    K * sizeof(float2), W, cudaMemcpyDeviceToDevice, s),
+				                  "integral amplitude realignment"));
+				a32 = dConv.as<float2>();
+				ldK = ldPad;
+			}
 		} else if (wantDouble) {
 			a64 = static_cast<const double2*>(amps);
 		} else {
-			PWA_TRY(dConv.alloc((size_t)W * K * sizeof(float2), "integral conversion buffer"));
+			PWA_TRY(dConv.alloc((size_t)W * ldPad * sizeof(float2), "integral conversion buffer"));
 			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
 			for (uint32_t w = 0; w < W; ++w)
 				PWA_TRY(launchConvertPlain(static_cast<const double2*>(amps) + (size_t)w * ldIn,
-				                           dConv.as<float2>() + (size_t)w * K, K, s));
+				                           dConv.as<float2>() + (size_t)w * ldPad, K, s));
 			a32 = dConv.as<float2>();
-			ldK = K;
+			ldK = ldPad;
 		}
 	} else {
 		const size_t elem = (ampType == PWA_COMPLEX64) ? sizeof(float2) : sizeof(double2);
-		PWA_TRY(dIn.alloc((size_t)W * K * elem, "integral amplitude buffer"));
-		PWA_TRY(cudaCheck(cudaMemcpy2DAsync(dIn.p, K * elem, amps, ldIn * elem, K * elem, W, cudaMemcpyHostToDevice, s),
+		PWA_TRY(dIn.alloc((size_t)W * ldPad * elem, "integral amplitude buffer"));
+		PWA_TRY(cudaCheck(cudaMemcpy2DAsync(dIn.p, ldPad * elem, amps, ldIn * elem, K * elem, W,
+		                                    cudaMemcpyHostToDevice, s),
 		                  "integral amplitude upload"));
-		ldK = K;
+		ldK = ldPad;
 		if (ampType == PWA_COMPLEX64) {
 			a32 = dIn.as<float2>();
 		} else if (wantDouble) {
 			a64 = dIn.as<double2>();
 		} else {
-			PWA_TRY(dConv.alloc((size_t)W * K * sizeof(float2), "integral conversion buffer"));
+			PWA_TRY(dConv.alloc((size_t)W * ldPad * sizeof(float2), "integral conversion buffer"));
 			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
-			PWA_TRY(launchConvertPlain(dIn.as<double2>(), dConv.as<float2>(), (uint64_t)W * K, s));
+			PWA_TRY(launchConvertPlain(dIn.as<double2>(), dConv.as<float2>(), (uint64_t)W * ldPad, s));
 			a32 = dConv.as<float2>();
 		}
 	}
 	if (!weightK.empty()) {
+		// the tensor-core kernel weights both operands by sqrt(w)
+		if (tensorCore)
+			for (double v : weightK)
+				if (!(v >= 0.))
+					return setError(kErrUnsupported, "tensor-core Gram needs non-negative event weights");
 		PWA_TRY(dW.alloc(weightK.size() * sizeof(double), "weights"));
 		PWA_TRY(cudaCheck(cudaMemcpyAsync(dW.p, weightK.data(), weightK.size() * sizeof(double),
 		                                  cudaMemcpyHostToDevice, s),
@@ -257,12 +275,14 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 	g.weightK = weightK.empty() ? nullptr : dW.as<double>();
 	g.devErr = dErr.as<unsigned>();
 	int st = kErrUnsupported;
-	if (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3 || precision == PWA_PRECISION_BF16X3) {
-		const size_t scratch = (size_t)2 * sms * 2 * 128 * 256;  // per-CTA partial tiles, upper bound
+	if (tensorCore) {
+		const size_t scratch = gramTcScratchFloats((int)W, sms) / 2 + 1;  // doubles holding the FP32 partials
 		PWA_TRY(dPart.alloc(scratch * sizeof(double), "gram partials"));
 		st = launchGramTc(g, precision, sms, s, dOut.as<double>(), dPart.as<double>(), scratch);
 		if (st != kOk)
 			return st;
+	} else if (precision == PWA_PRECISION_BF16X3) {
+		return setError(kErrUnsupported, "BF16 split-precision tensor-core Gram kernel not available in this build");
 	} else {
 		const int tps = ((int)W + 63) / 64;
 		const int nTiles = tps * (tps + 1) / 2;
@@ -277,9 +297,13 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		PWA_TRY(launchGramReduce(g.partials, chunks, (int)W, dOut.as<double>(), 0, s));
 	}
 	std::vector<double> host((size_t)W * W * 2);
+	unsigned devErr = 0;
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(host.data(), dOut.p, host.size() * sizeof(double), cudaMemcpyDeviceToHost, s),
 	                  "integral download"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(&devErr, dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "flag download"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "integral sync"));
+	if (devErr)
+		return setError(kErrTimeout, "integral kernel: a bounded device-side wait expired");
 	out.resize((size_t)W * W);
 	for (size_t k = 0; k < out.size(); ++k)
 		out[k] = cplx(host[2 * k], host[2 * k + 1]);

@@ -140,5 +140,7 @@ int launchGramReduce(const double* partials, int chunks, int W, double* out, int
 // tcgen05 tensor-core Gram; returns kErrUnsupported when the shape has no variant
 int launchGramTc(const GramArgs& a, int precision, int numSMs, cudaStream_t s, double* out, double* scratch,
                  size_t scratchDoubles);
+// FP32 words of per-CTA partial Grams launchGramTc needs
+size_t gramTcScratchFloats(int W, int numSMs);
 
 }  // namespace pwa
