@@ -263,6 +263,47 @@ int pwa_likelihood_reset_func_call_info(pwa_likelihood* L);
 int pwa_likelihood_set_timing(pwa_likelihood* L, int enable);
 int pwa_likelihood_kernel_times(pwa_likelihood* L, double* eventKernelMs, double* finalizeMs, uint64_t* nTimed);
 
+/* ------------------------------------------------------------------------ */
+/* Batched multibin x multistart fits (no reference counterpart: the          */
+/* reference fits one bin per process, pwaFit.py:18,51-57, and its start      */
+/* points one after another, _fit.py:131-165)                                 */
+/* ------------------------------------------------------------------------ */
+typedef struct pwa_multibin pwa_multibin;
+/* L-BFGS status of a problem (one bin x one start point) */
+enum pwa_lbfgs_status { PWA_LBFGS_ACTIVE = 0, PWA_LBFGS_SEARCHING = 1, PWA_LBFGS_CONVERGED = 2,
+                        PWA_LBFGS_MAX_ITER = 3, PWA_LBFGS_STALLED = 4, PWA_LBFGS_FAILED = 5 };
+int pwa_multibin_create(pwa_multibin** out);
+int pwa_multibin_destroy(pwa_multibin* M);
+/* adds a bin: a likelihood after finishInit (rank 1, one reflectivity, at
+ * most 64 waves; every bin the same wave set and layout) with nStarts start
+ * points; the likelihood must outlive the batch.  Problems are numbered bin
+ * by bin, start by start. */
+int pwa_multibin_add_bin(pwa_multibin* M, pwa_likelihood* L, uint32_t nStarts);
+/* startGroup: starts evaluated together per amplitude tile (8 or 32);
+ * L-BFGS memory; convergence when |grad| <= gtolAbs + gtolRel * max(1, |f|);
+ * iteration limit per problem */
+int pwa_multibin_set_options(pwa_multibin* M, uint32_t startGroup, uint32_t lbfgsMemory, double gtolAbs,
+                             double gtolRel, uint32_t maxIter);
+/* tiles of 128 events per work item for bins of < 64, < 512 and >= 512 tiles */
+int pwa_multibin_set_chunks(pwa_multibin* M, const uint32_t* tilesPerItem);
+int pwa_multibin_chunks(const pwa_multibin* M, uint32_t* tilesPerItem);
+/* autotuner: per bin size class in turn, the tiles per item with the fastest
+ * evaluation sweep at x [Q][P] */
+int pwa_multibin_autotune(pwa_multibin* M, const double* x);
+int pwa_multibin_nmb_problems(const pwa_multibin* M, uint32_t* nProblems);
+int pwa_multibin_nmb_pars(const pwa_multibin* M, uint32_t* nPars);
+/* FdF of every problem: x [Q][P] -> f [Q], grad [Q][P] (host buffers) */
+int pwa_multibin_fdf(pwa_multibin* M, const double* x, double* f, double* grad);
+/* device time of one evaluation sweep of all problems at x (mean of reps) */
+int pwa_multibin_sweep_ms(pwa_multibin* M, const double* x, uint32_t reps, double* ms);
+/* L-BFGS of every problem from x0 [Q][P]: sweeps (one batched FdF + one
+ * L-BFGS step for all active problems) run until no problem is active or
+ * maxSweeps; with useGraph the sweeps are replayed from a CUDA graph of
+ * sweepsPerGraph sweeps.  Outputs (host, any may be NULL): x [Q][P], f, gnorm,
+ * status (pwa_lbfgs_status), iterations [Q], sweeps run. */
+int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t sweepsPerGraph, uint32_t maxSweeps,
+                     double* x, double* f, double* gnorm, int32_t* status, uint32_t* iterations, uint32_t* sweeps);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -69,6 +69,18 @@ SIGNATURES = {
     "pwa_integral_read_ascii": (i, [vp, cc]),
     "pwa_integral_write_ascii": (i, [vp, cc]),
     "pwa_gram_device_noalloc": (i, [vp, u64, u64, u32, vp, i, vp, vp]),
+    "pwa_multibin_create": (i, [pvp]),
+    "pwa_multibin_destroy": (i, [vp]),
+    "pwa_multibin_add_bin": (i, [vp, vp, u32]),
+    "pwa_multibin_set_options": (i, [vp, u32, u32, C.c_double, C.c_double, u32]),
+    "pwa_multibin_set_chunks": (i, [vp, C.POINTER(u32)]),
+    "pwa_multibin_chunks": (i, [vp, C.POINTER(u32)]),
+    "pwa_multibin_autotune": (i, [vp, pd]),
+    "pwa_multibin_nmb_problems": (i, [vp, C.POINTER(u32)]),
+    "pwa_multibin_nmb_pars": (i, [vp, C.POINTER(u32)]),
+    "pwa_multibin_fdf": (i, [vp, pd, pd, pd]),
+    "pwa_multibin_sweep_ms": (i, [vp, pd, u32, pd]),
+    "pwa_multibin_fit": (i, [vp, pd, i, u32, u32, pd, pd, pd, C.POINTER(i32), C.POINTER(u32), C.POINTER(u32)]),
     "pwa_likelihood_create": (i, [pvp]),
     "pwa_likelihood_destroy": (i, [vp]),
     "pwa_likelihood_use_normalized_amps": (i, [vp, i]),

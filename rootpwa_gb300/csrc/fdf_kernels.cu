@@ -37,6 +37,7 @@
 // the tail, and the host discards the result.
 
 #include "pwa_internal.h"
+#include "device_common.cuh"
 
 #include <algorithm>
 
@@ -45,110 +46,6 @@ namespace {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s
-
-__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbarInit(uint64_t* bar, uint32_t count)
-{
-	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbarArriveExpectTx(uint64_t* bar, uint32_t bytes)
-{
-	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
-	             : "memory");
-}
-
-__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, uint32_t parity)
-{
-	uint32_t ok;
-	asm volatile(
-	    "{\n\t.reg .pred p;\n\t"
-	    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-	    "selp.u32 %0, 1, 0, p;\n\t}"
-	    : "=r"(ok)
-	    : "r"(smemAddr(bar)), "r"(parity)
-	    : "memory");
-	return ok != 0;
-}
-
-__device__ __forceinline__ unsigned long long globalTimer()
-{
-	unsigned long long t;
-	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-	return t;
-}
-
-// Bounded wait for the phase with the given parity to complete.
-__device__ bool mbarWaitBounded(uint64_t* bar, uint32_t parity)
-{
-	if (mbarTryWait(bar, parity))
-		return true;
-	const unsigned long long t0 = globalTimer();
-	while (true) {
-		if (mbarTryWait(bar, parity))
-			return true;
-		if (globalTimer() - t0 > kWaitLimitNs)
-			return false;
-	}
-}
-
-__device__ __forceinline__ void bulkCopyG2S(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-	                 smemAddr(dst)),
-	             "l"(src), "r"(bytes), "r"(smemAddr(bar))
-	             : "memory");
-}
-
-__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// Programmatic dependent launch: wait until the preceding grid in the stream
-// has completed and its memory is visible; allow the next grid to launch.
-__device__ __forceinline__ void gridDependencyWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void gridDependencyTrigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
-__device__ __forceinline__ float warpSum(float v)
-{
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1)
-		v += __shfl_xor_sync(0xffffffffu, v, o);
-	return v;
-}
-
-__device__ __forceinline__ double warpSumD(double v)
-{
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1)
-		v += __shfl_xor_sync(0xffffffffu, v, o);
-	return v;
-}
-
-// Warp reduce-scatter of 32 values held by every lane: afterwards x[0] of
-// lane l holds the sum over all lanes of value index l.
-__device__ __forceinline__ float reduceScatter32(float* x, int lane)
-{
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) {
-		const bool up = (lane & o) != 0;
-#pragma unroll
-		for (int k = 0; k < o; ++k) {
-			const float send = up ? x[k] : x[k + o];
-			const float keep = up ? x[k + o] : x[k];
-			x[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-		}
-	}
-	return x[0];
-}
-
-__device__ __forceinline__ void kahanAdd(float& s, float& c, float x)
-{
-	const float y = x - c;
-	const float t = s + y;
-	c = (t - s) - y;
-	s = t;
-}
 
 // Shared-memory layout of the main kernel (byte offsets from the dynamic base).
 // A stage holds one store block: W rows of E complex64 amplitudes, in the
@@ -197,34 +94,6 @@ __host__ __device__ inline int waveSplit(int W0, int W, int* nNeg, int* wn, int*
 	*wn = bn ? (W0 + bn - 1) / bn : 0;
 	*wp = (bn < kWarps) ? (W1 + kWarps - bn - 1) / (kWarps - bn) : 0;
 	return best;
-}
-
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
-{
-	float2 d;
-	asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
-	    "mov.b64 ra, {%2, %3};\n\t"
-	    "mov.b64 rb, {%4, %5};\n\t"
-	    "mov.b64 rc, {%6, %7};\n\t"
-	    "fma.rn.f32x2 rd, ra, rb, rc;\n\t"
-	    "mov.b64 {%0, %1}, rd;\n\t}"
-	    : "=f"(d.x), "=f"(d.y)
-	    : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-	return d;
-}
-
-// shared-memory loads through 32-bit shared-window addresses
-__device__ __forceinline__ float2 lds64(uint32_t addr)
-{
-	float2 v;
-	asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
-	return v;
-}
-__device__ __forceinline__ float4 lds128(uint32_t addr)
-{
-	float4 v;
-	asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
-	return v;
 }
 
 // Tiles whose gradient partials are summed in FP32 before the warp

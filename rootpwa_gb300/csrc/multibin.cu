@@ -1,0 +1,666 @@
+// multibin.cu -- batched FdF over many kinematic bins x many start points,
+// its per-problem finish (cross-item sums, normalisation and prior terms) and
+// a batched L-BFGS step, for whole multibin multi-start fits on the GPU.
+//
+// A "problem" is one (bin, start point) pair with its own parameter vector in
+// the pwaLikelihood layout (partialWaveFit/pwaLikelihood.cc:1487-1556).  All
+// bins share the wave set (rank 1, one reflectivity).  One sweep evaluates
+// every active problem at its trial point:
+//   fdfBatchKernel   -- persistent blocks walk a list of work items
+//                       (bin, group of SG starts, range of 128-event tiles);
+//                       each tile is loaded once by a bulk copy and used for all
+//                       SG starts: phase 1 forms S_{s,e} = sum_w V_{s,w} A_{w,e},
+//                       L = |S|^2 + V_flat^2, -ln L and c S (c = -2/L); phase 2
+//                       G_{s,w} += sum_e c S_{s,e} conj(A_{w,e});
+//                       per-thread FP32 (compensated for -ln L and c) over up
+//                       to 8 tiles, then FP64; FP64 partials per item;
+//   batchFinishKernel -- one warp per problem: sums the items' partials in item
+//                       order (deterministic), adds nEvt (Re V^H I^acc V +
+//                       V_flat^2 eta) and the half-Cauchy prior in FP64
+//                       (pwaLikelihood.cc:254-297) and writes f and the gradient;
+//   lbfgsKernel      -- one warp per problem: backtracking line search
+//                       (Armijo, or the approximate Wolfe conditions of Hager
+//                       and Zhang near the rounding floor of f) and the L-BFGS
+//                       two-loop recursion in FP64.
+// The launches of one sweep are stream-ordered and capture into a CUDA graph;
+// converged problems drop out (their items exit at once).
+
+#include "pwa_internal.h"
+#include "device_common.cuh"
+
+#include <algorithm>
+
+namespace pwa {
+namespace {
+
+constexpr int kBThreads = 256;
+constexpr int kBE = 128;     // events per tile (the amplitude store's block)
+constexpr int kBFold = 8;    // tiles summed in FP32 before the FP64 fold
+
+struct BatchSmem {
+	size_t stages, vs, ts, flat, bars, total;
+};
+
+__host__ __device__ inline BatchSmem batchSmem(int W, int SG)
+{
+	BatchSmem L{};
+	auto up = [](size_t x) { return (x + 127) & ~size_t(127); };
+	L.stages = 0;
+	L.vs = up((size_t)2 * W * kBE * 8);
+	L.ts = up(L.vs + (size_t)W * SG * 16);
+	L.flat = up(L.ts + (size_t)2 * kBE * SG * 8);
+	L.bars = up(L.flat + (size_t)SG * 4);
+	L.total = L.bars + 2 * 8 + 128;
+	return L;
+}
+
+// SG starts per group; phase 1: SPT starts x EPT events per thread;
+// phase 2: SPT2 starts x WPT waves per thread (waves < 64).
+template <int SG, int SPT, int EPT, int SPT2, int WPT>
+__global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a)
+{
+	static_assert((SG / SPT) * (kBE / EPT) == kBThreads, "phase-1 mapping");
+	static_assert((SG / SPT2) * (64 / WPT) == kBThreads, "phase-2 mapping");
+	static_assert(EPT % 2 == 0 && SPT2 % 2 == 0 && SPT % 2 == 0, "paired loads");
+	extern __shared__ __align__(128) unsigned char smem[];
+	const int W = a.W, P = a.P;
+	const BatchSmem lay = batchSmem(W, SG);
+	float2* stages = reinterpret_cast<float2*>(smem + lay.stages);  // [2][W][kBE]
+	float4* Vs = reinterpret_cast<float4*>(smem + lay.vs);          // [W][SG] (vx, vx, vy, vy)
+	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);          // [2][kBE][SG] c S
+	float* flat2 = reinterpret_cast<float*>(smem + lay.flat);       // [SG]
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
+	__shared__ double redLL[kBThreads / 32][SG], redC[kBThreads / 32][SG];
+
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint32_t tileBytes = (uint32_t)W * kBE * 8u;
+	// phase-1 role
+	const int sq = tid % (SG / SPT), eq = tid / (SG / SPT);
+	const int s1 = sq * SPT, e1 = eq * EPT;
+	// phase-2 role
+	const int sp = tid % (SG / SPT2), wg = tid / (SG / SPT2);
+	const int s2 = sp * SPT2, w2 = wg * WPT;
+
+	if (tid == 0) {
+		mbarInit(&bars[0], 1);
+		mbarInit(&bars[1], 1);
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+	uint32_t phase[2] = {0u, 0u};
+	bool failed = false;
+
+	for (int item = blockIdx.x; item < a.nItems && !failed; item += gridDim.x) {
+		const BatchItem it = a.items[item];
+		const BinDesc bin = a.bins[it.bin];
+		const int q0 = bin.q0 + it.group * SG;
+		const int ns = min(SG, bin.nStarts - it.group * SG);
+		const int act = (tid < ns) ? a.active[q0 + tid] : 0;
+		if (!__syncthreads_or(act))
+			continue;
+		// production amplitudes of the group's starts
+		for (int k = tid; k < W * SG; k += kBThreads) {
+			const int w = k / SG, s = k - w * SG;
+			float vr = 0.f, vi = 0.f;
+			if (s < ns) {
+				const double* x = a.x + (size_t)(q0 + s) * P;
+				const int ir = a.slotRe[w], ii = a.slotIm[w];
+				vr = ir >= 0 ? (float)x[ir] : 0.f;
+				vi = ii >= 0 ? (float)x[ii] : 0.f;
+			}
+			Vs[k] = make_float4(vr, vr, vi, vi);
+		}
+		for (int s = tid; s < SG; s += kBThreads) {
+			const double f = (s < ns) ? a.x[(size_t)(q0 + s) * P + P - 1] : 0.;
+			flat2[s] = (float)(f * f);
+		}
+		const int nt = (int)(it.t1 - it.t0);
+		const uint32_t ph0[2] = {phase[0], phase[1]};
+		if (tid == 0) {
+			fenceProxyAsync();
+			for (int k = 0; k < 2 && k < nt; ++k) {
+				mbarArriveExpectTx(&bars[k], tileBytes);
+				bulkCopyG2S(stages + (size_t)k * W * kBE, bin.amps + (size_t)(it.t0 + k) * W * kBE, tileBytes,
+				            &bars[k]);
+			}
+		}
+		__syncthreads();
+
+		// accumulators
+		double llD[SPT], csD[SPT];
+		float llF[SPT], csF[SPT], llK[SPT], csK[SPT];  // compensated FP32 sums
+#pragma unroll
+		for (int i = 0; i < SPT; ++i) {
+			llD[i] = csD[i] = 0.;
+			llF[i] = csF[i] = llK[i] = csK[i] = 0.f;
+		}
+		double gD[SPT2][WPT][2];
+		float2 Pp[SPT2][WPT], Qp[SPT2][WPT];
+#pragma unroll
+		for (int i = 0; i < SPT2; ++i)
+#pragma unroll
+			for (int j = 0; j < WPT; ++j) {
+				gD[i][j][0] = gD[i][j][1] = 0.;
+				Pp[i][j] = Qp[i][j] = make_float2(0.f, 0.f);
+			}
+
+		int k = 0;
+		for (; k < nt; ++k) {
+			const int st = k & 1;
+			const bool ok = mbarWaitBounded(&bars[st], phase[st]);
+			phase[st] ^= 1u;
+			const float2* tile = stages + (size_t)st * W * kBE;
+			const uint32_t tileAddr = smemAddr(tile);
+			float2* T = Ts + (size_t)(k & 1) * kBE * SG;
+			const uint64_t ev0 = (uint64_t)(it.t0 + k) * kBE;
+
+			// ---- phase 1: S, L, -ln L, c S ----
+			{
+				float2 U[SPT][EPT], Z[SPT][EPT];
+#pragma unroll
+				for (int i = 0; i < SPT; ++i)
+#pragma unroll
+					for (int j = 0; j < EPT; ++j)
+						U[i][j] = Z[i][j] = make_float2(0.f, 0.f);
+				const uint32_t vAddr = smemAddr(Vs) + (uint32_t)s1 * 16u;
+				for (int w = 0; w < W; ++w) {
+					const int pos = (e1 + (int)storeRot((uint32_t)w, kBE)) & (kBE - 1);
+					float2 av[EPT];
+#pragma unroll
+					for (int j = 0; j < EPT; j += 2) {
+						const float4 q = lds128(tileAddr + (uint32_t)(w * kBE + pos + j) * 8u);
+						av[j] = make_float2(q.x, q.y);
+						av[j + 1] = make_float2(q.z, q.w);
+					}
+#pragma unroll
+					for (int i = 0; i < SPT; ++i) {
+						const float4 v = lds128(vAddr + (uint32_t)(w * SG + i) * 16u);
+						const float2 vx = make_float2(v.x, v.y), vy = make_float2(v.z, v.w);
+#pragma unroll
+						for (int j = 0; j < EPT; ++j) {
+							U[i][j] = ffma2(av[j], vx, U[i][j]);
+							Z[i][j] = ffma2(av[j], vy, Z[i][j]);
+						}
+					}
+				}
+#pragma unroll
+				for (int j = 0; j < EPT; ++j) {
+					const bool valid = ev0 + (uint64_t)(e1 + j) < bin.nEvents;
+#pragma unroll
+					for (int i = 0; i < SPT; i += 2) {
+						float2 ts[2];
+#pragma unroll
+						for (int h = 0; h < 2; ++h) {
+							const float sx = U[i + h][j].x - Z[i + h][j].y, sy = U[i + h][j].y + Z[i + h][j].x;
+							const float L = fmaf(sx, sx, fmaf(sy, sy, flat2[s1 + i + h]));
+							const float c = valid ? -2.f / L : 0.f;
+							if (valid)
+								kahanAdd(llF[i + h], llK[i + h], -logf(L));
+							kahanAdd(csF[i + h], csK[i + h], c);
+							ts[h] = make_float2(c * sx, c * sy);
+						}
+						*reinterpret_cast<float4*>(&T[(e1 + j) * SG + s1 + i]) =
+						    make_float4(ts[0].x, ts[0].y, ts[1].x, ts[1].y);
+					}
+				}
+			}
+			// T complete; phase 2 of the previous tile is done by every thread
+			if (__syncthreads_or(!ok)) {
+				failed = true;
+				break;
+			}
+			if (tid == 0 && k >= 1 && k + 1 < nt) {
+				fenceProxyAsync();
+				const int ns2 = (k + 1) & 1;
+				mbarArriveExpectTx(&bars[ns2], tileBytes);
+				bulkCopyG2S(stages + (size_t)ns2 * W * kBE, bin.amps + (size_t)(it.t0 + k + 1) * W * kBE, tileBytes,
+				            &bars[ns2]);
+			}
+
+			// ---- phase 2: G += sum_e c S conj(A) ----
+			if (w2 < W) {
+				const uint32_t tAddr = smemAddr(T) + (uint32_t)s2 * 8u;
+				int rot[WPT];
+#pragma unroll
+				for (int j = 0; j < WPT; ++j)
+					rot[j] = (int)storeRot((uint32_t)(w2 + j), kBE);
+				for (int e = 0; e < kBE; ++e) {
+					float2 t[SPT2];
+#pragma unroll
+					for (int i = 0; i < SPT2; i += 2) {
+						const float4 q = lds128(tAddr + (uint32_t)(e * SG + i) * 8u);
+						t[i] = make_float2(q.x, q.y);
+						t[i + 1] = make_float2(q.z, q.w);
+					}
+#pragma unroll
+					for (int j = 0; j < WPT; ++j) {
+						const int w = min(w2 + j, W - 1);
+						const float2 av = lds64(tileAddr + (uint32_t)(w * kBE + ((e + rot[j]) & (kBE - 1))) * 8u);
+						const float2 aw = make_float2(av.y, av.x);
+#pragma unroll
+						for (int i = 0; i < SPT2; ++i) {
+							Pp[i][j] = ffma2(t[i], av, Pp[i][j]);  // (tx ax, ty ay)
+							Qp[i][j] = ffma2(t[i], aw, Qp[i][j]);  // (tx ay, ty ax)
+						}
+					}
+				}
+			}
+			// fold the FP32 partials into FP64
+			if ((k + 1) % kBFold == 0 || k + 1 == nt) {
+#pragma unroll
+				for (int i = 0; i < SPT; ++i) {
+					llD[i] += (double)llF[i] - (double)llK[i];
+					csD[i] += (double)csF[i] - (double)csK[i];
+					llF[i] = csF[i] = llK[i] = csK[i] = 0.f;
+				}
+#pragma unroll
+				for (int i = 0; i < SPT2; ++i)
+#pragma unroll
+					for (int j = 0; j < WPT; ++j) {
+						gD[i][j][0] += (double)(Pp[i][j].x + Pp[i][j].y);
+						gD[i][j][1] += (double)(Qp[i][j].y - Qp[i][j].x);
+						Pp[i][j] = Qp[i][j] = make_float2(0.f, 0.f);
+					}
+			}
+		}
+		if (failed) {
+			if (tid == 0) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				// copies of this item still in flight land before the block
+				// exits: tiles k .. max(1, k) were issued and not consumed
+				for (int j = k; j <= max(1, k) && j < nt; ++j)
+					mbarWaitBounded(&bars[j & 1], ph0[j & 1] ^ (uint32_t)((j >> 1) & 1));
+			}
+			break;
+		}
+
+		// ---- partials of this item: [SG][2 + 2W] FP64 ----
+		const int NV = 2 + 2 * W;
+		double* out = a.partials + (size_t)item * SG * NV;
+		// LL and sum c per start: lanes that share sq differ in eq
+#pragma unroll
+		for (int i = 0; i < SPT; ++i) {
+			double l = llD[i], c = csD[i];
+			for (int o = SG / SPT; o < 32; o <<= 1) {
+				l += __shfl_xor_sync(0xffffffffu, l, o);
+				c += __shfl_xor_sync(0xffffffffu, c, o);
+			}
+			if (lane < SG / SPT) {
+				redLL[warp][s1 + i] = l;
+				redC[warp][s1 + i] = c;
+			}
+		}
+		if (w2 < W) {
+#pragma unroll
+			for (int i = 0; i < SPT2; ++i)
+#pragma unroll
+				for (int j = 0; j < WPT; ++j)
+					if (w2 + j < W) {
+						out[(size_t)(s2 + i) * NV + 2 + 2 * (w2 + j)] = gD[i][j][0];
+						out[(size_t)(s2 + i) * NV + 3 + 2 * (w2 + j)] = gD[i][j][1];
+					}
+		}
+		__syncthreads();
+		for (int s = tid; s < SG; s += kBThreads) {
+			double l = 0., c = 0.;
+			for (int wv = 0; wv < kBThreads / 32; ++wv) {
+				l += redLL[wv][s];
+				c += redC[wv][s];
+			}
+			out[(size_t)s * NV] = l;
+			out[(size_t)s * NV + 1] = c;
+		}
+		__syncthreads();
+	}
+}
+
+__device__ __forceinline__ double warpAllSum(double v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1)
+		v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// One warp per problem: f and gradient from the items' partials plus the
+// normalisation and prior terms.
+__global__ void batchFinishKernel(const FinishBatchArgs a)
+{
+	const int q = (int)((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5);
+	const int lane = threadIdx.x & 31;
+	if (q >= a.Q || !a.active[q])
+		return;
+	const int W = a.W, P = a.P, NV = 2 + 2 * W;
+	const ProblemDesc pd = a.problems[q];
+	const BinDesc bin = a.bins[pd.bin];
+	const double* x = a.x + (size_t)q * P;
+	double* g = a.g + (size_t)q * P;
+	const double nEvt = bin.nEvt, twice = 2. * bin.nEvt;
+	const double flat = x[P - 1];
+	// event sums, in item order
+	double fLL = 0., fC = 0.;
+	for (int v = lane; v < NV; v += 32) {
+		double acc = 0.;
+		for (int i = pd.item0; i < pd.item1; ++i)
+			acc += a.partials[((size_t)i * a.SG + pd.slot) * NV + v];
+		if (v == 0)
+			fLL = acc;
+		else if (v == 1)
+			fC = acc;
+		else {
+			const int w = (v - 2) >> 1, comp = (v - 2) & 1;
+			const int idx = comp ? a.slotIm[w] : a.slotRe[w];
+			if (idx >= 0)
+				g[idx] = acc;
+		}
+	}
+	fLL = __shfl_sync(0xffffffffu, fLL, 0);
+	fC = __shfl_sync(0xffffffffu, fC, 1);
+	__syncwarp();
+	// normalisation: D_i = sum_j V_j conj(I_ij); prior
+	double norm = 0., prior = 0.;
+	const double g2 = a.cauchyWidth * a.cauchyWidth;
+	for (int i = lane; i < W; i += 32) {
+		const int ri = a.slotRe[i], ii = a.slotIm[i];
+		const double vr = ri >= 0 ? x[ri] : 0., vi = ii >= 0 ? x[ii] : 0.;
+		double dre = 0., dim = 0.;
+		const double* Ib = bin.accI + (size_t)2 * i * W;
+		for (int j = 0; j < W; ++j) {
+			const int rj = a.slotRe[j], ij = a.slotIm[j];
+			const double ur = rj >= 0 ? x[rj] : 0., ui = ij >= 0 ? x[ij] : 0.;
+			const double Ir = Ib[2 * j], Ii = Ib[2 * j + 1];
+			dre += ur * Ir + ui * Ii;
+			dim += ui * Ir - ur * Ii;
+		}
+		norm += vr * dre + vi * dim;
+		double pre = 0., pim = 0.;
+		if (a.prior == 1) {
+			const double rr = hypot(vr, vi);
+			const double cf = 1. / (1. + (rr * rr) / g2);
+			const double cd = (-2. * rr * g2) / ((g2 + rr * rr) * (g2 + rr * rr));
+			const double fac = (1. / (rr * cf)) * cd;
+			prior += -log(cf);
+			pre = fac * vr;
+			pim = fac * vi;
+		}
+		if (ri >= 0)
+			g[ri] += twice * dre - pre;
+		if (ii >= 0)
+			g[ii] += twice * dim - pim;
+	}
+	norm = warpAllSum(norm);
+	prior = warpAllSum(prior);
+	if (lane == 0) {
+		a.f[q] = fLL + nEvt * (norm + flat * flat * bin.totAcc) + prior;
+		g[P - 1] = flat * fC + twice * flat * bin.totAcc;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// batched L-BFGS (one warp per problem, FP64)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double wdot(const double* a, const double* b, int n, int lane)
+{
+	double s = 0.;
+	for (int i = lane; i < n; i += 32)
+		s += a[i] * b[i];
+	return warpAllSum(s);
+}
+
+__global__ void lbfgsKernel(const LbfgsArgs a)
+{
+	const int q = (int)((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5);
+	const int lane = threadIdx.x & 31;
+	if (q >= a.Q)
+		return;
+	const int st = a.status[q];
+	if (st != kLbfgsInit && st != kLbfgsSearch)
+		return;
+	const int P = a.P, m = a.m;
+	double* x = a.x + (size_t)q * P;    // accepted point
+	double* g = a.g + (size_t)q * P;
+	double* d = a.d + (size_t)q * P;
+	double* xt = a.xt + (size_t)q * P;  // trial point (evaluated in this sweep)
+	const double* gt = a.gt + (size_t)q * P;
+	double* S = a.S + (size_t)q * m * P;
+	double* Y = a.Y + (size_t)q * m * P;
+	double* rho = a.rho + (size_t)q * m;
+	double* alph = a.alphaBuf + (size_t)q * m;
+	const double ft = a.ft[q];
+	bool accept = false;
+	if (st == kLbfgsInit) {
+		accept = isfinite(ft);
+		if (!accept) {
+			if (lane == 0)
+				a.status[q] = kLbfgsFailed;
+			return;
+		}
+	} else {
+		// sufficient decrease (Armijo), or the approximate Wolfe conditions of
+		// Hager and Zhang (value within a relative 1e-8 of f, directional
+		// derivative between 0.9 g.d and -0.8 g.d), which stay decisive when
+		// the decrease is below the rounding noise of f near a minimum
+		const double gd = wdot(g, d, P, lane);
+		const double gtd = wdot(gt, d, P, lane);
+		const double f0 = a.f[q];
+		const bool armijo = ft <= f0 + 1e-4 * a.step[q] * gd;
+		const bool approxWolfe = ft <= f0 + 1e-8 * fmax(1., fabs(f0)) && gtd >= 0.9 * gd && gtd <= -0.8 * gd;
+		accept = isfinite(ft) && (armijo || approxWolfe);
+	}
+	if (!accept) {
+		// backtrack
+		const int nb = a.nBack[q] + 1;
+		const double step = a.step[q] * 0.5;
+		if (nb > 40) {
+			if (a.hist[q] > 0) {
+				// restart once from steepest descent at the accepted point
+				const double gn = sqrt(wdot(g, g, P, lane));
+				for (int i = lane; i < P; i += 32) {
+					d[i] = -g[i] / fmax(gn, 1e-300);
+					xt[i] = x[i] + d[i];
+				}
+				if (lane == 0) {
+					a.hist[q] = 0;
+					a.head[q] = 0;
+					a.nBack[q] = 0;
+					a.step[q] = 1.;
+				}
+				return;
+			}
+			if (lane == 0)
+				a.status[q] = kLbfgsStalled;
+			return;
+		}
+		for (int i = lane; i < P; i += 32)
+			xt[i] = x[i] + step * d[i];
+		if (lane == 0) {
+			a.nBack[q] = nb;
+			a.step[q] = step;
+		}
+		return;
+	}
+	// accept the trial point: update the history with s = xt - x, y = gt - g
+	int hist = a.hist[q], head = a.head[q];
+	if (st == kLbfgsSearch) {
+		double sy = 0., yy = 0., ss = 0.;
+		for (int i = lane; i < P; i += 32) {
+			const double si = xt[i] - x[i], yi = gt[i] - g[i];
+			sy += si * yi;
+			yy += yi * yi;
+			ss += si * si;
+		}
+		sy = warpAllSum(sy);
+		yy = warpAllSum(yy);
+		ss = warpAllSum(ss);
+		if (sy > 1e-12 * sqrt(ss * yy)) {
+			const int slot = (head + hist) % m;
+			for (int i = lane; i < P; i += 32) {
+				S[(size_t)slot * P + i] = xt[i] - x[i];
+				Y[(size_t)slot * P + i] = gt[i] - g[i];
+			}
+			if (lane == 0) {
+				rho[slot] = 1. / sy;
+				a.gamma[q] = sy / yy;
+			}
+			if (hist < m)
+				++hist;
+			else
+				head = (head + 1) % m;
+		}
+	}
+	__syncwarp();
+	for (int i = lane; i < P; i += 32) {
+		x[i] = xt[i];
+		g[i] = gt[i];
+	}
+	__syncwarp();
+	const double fNew = ft;
+	const double gnorm = sqrt(wdot(g, g, P, lane));
+	const int iter = a.iter[q] + (st == kLbfgsSearch ? 1 : 0);
+	if (lane == 0) {
+		a.f[q] = fNew;
+		a.gnorm[q] = gnorm;
+		a.iter[q] = iter;
+		a.hist[q] = hist;
+		a.head[q] = head;
+	}
+	if (gnorm <= a.gtolAbs + a.gtolRel * fmax(1., fabs(fNew))) {
+		if (lane == 0)
+			a.status[q] = kLbfgsConverged;
+		return;
+	}
+	if (iter >= a.maxIter) {
+		if (lane == 0)
+			a.status[q] = kLbfgsMaxIter;
+		return;
+	}
+	// two-loop recursion: d = -H g
+	for (int i = lane; i < P; i += 32)
+		d[i] = -g[i];
+	__syncwarp();
+	for (int k = hist - 1; k >= 0; --k) {
+		const int slot = (head + k) % m;
+		const double al = rho[slot] * wdot(S + (size_t)slot * P, d, P, lane);
+		if (lane == 0)
+			alph[k] = al;
+		for (int i = lane; i < P; i += 32)
+			d[i] -= al * Y[(size_t)slot * P + i];
+		__syncwarp();
+	}
+	const double gamma = hist > 0 ? a.gamma[q] : 1. / fmax(gnorm, 1e-300);
+	for (int i = lane; i < P; i += 32)
+		d[i] *= gamma;
+	__syncwarp();
+	for (int k = 0; k < hist; ++k) {
+		const int slot = (head + k) % m;
+		const double be = rho[slot] * wdot(Y + (size_t)slot * P, d, P, lane);
+		const double al = __shfl_sync(0xffffffffu, lane == 0 ? alph[k] : 0., 0);
+		for (int i = lane; i < P; i += 32)
+			d[i] += (al - be) * S[(size_t)slot * P + i];
+		__syncwarp();
+	}
+	const double gd = wdot(g, d, P, lane);
+	if (!(gd < 0.)) {
+		// not a descent direction: restart from steepest descent
+		for (int i = lane; i < P; i += 32)
+			d[i] = -g[i] / fmax(gnorm, 1e-300);
+		if (lane == 0) {
+			a.hist[q] = 0;
+			a.head[q] = 0;
+		}
+		__syncwarp();
+	}
+	for (int i = lane; i < P; i += 32)
+		xt[i] = x[i] + d[i];
+	if (lane == 0) {
+		a.step[q] = 1.;
+		a.nBack[q] = 0;
+		a.status[q] = kLbfgsSearch;
+	}
+}
+
+__global__ void countActiveKernel(const int* status, int Q, int* active, unsigned* nActive)
+{
+	for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x) {
+		const int a = (status[q] == kLbfgsInit || status[q] == kLbfgsSearch) ? 1 : 0;
+		active[q] = a;
+		if (a)
+			atomicAdd(nActive, 1u);
+	}
+}
+
+template <int SG, int SPT, int EPT, int SPT2, int WPT>
+int configureBatchT(int W)
+{
+	const BatchSmem lay = batchSmem(W, SG);
+	return cudaCheck(cudaFuncSetAttribute(fdfBatchKernel<SG, SPT, EPT, SPT2, WPT>,
+	                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total),
+	                 "batch smem attribute");
+}
+
+template <int SG, int SPT, int EPT, int SPT2, int WPT>
+int launchBatchT(const BatchArgs& a, int grid, cudaStream_t s)
+{
+	const BatchSmem lay = batchSmem(a.W, SG);
+	fdfBatchKernel<SG, SPT, EPT, SPT2, WPT><<<grid, kBThreads, lay.total, s>>>(a);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "batch FdF launch");
+}
+
+}  // namespace
+
+size_t batchSmemBytes(int W, int SG) { return batchSmem(W, SG).total; }
+
+int configureBatchFdf(int W, int SG, size_t maxSmem)
+{
+	if (W < 1 || W > 64)
+		return setError(kErrUnsupported, "batched FdF supports 1..64 waves");
+	if (batchSmem(W, SG).total > maxSmem)
+		return setError(kErrUnsupported, "batched FdF: shared memory too small for this wave set");
+	if (SG == 32)
+		return configureBatchT<32, 4, 4, 4, 2>(W);
+	if (SG == 8)
+		return configureBatchT<8, 2, 2, 2, 1>(W);
+	return setError(kErrUnsupported, "batched FdF: start-group size must be 8 or 32");
+}
+
+int launchBatchFdf(const BatchArgs& a, int grid, cudaStream_t s)
+{
+	if (a.W < 1 || a.W > 64)
+		return setError(kErrUnsupported, "batched FdF supports 1..64 waves");
+	if (a.SG == 32)
+		return launchBatchT<32, 4, 4, 4, 2>(a, grid, s);
+	if (a.SG == 8)
+		return launchBatchT<8, 2, 2, 2, 1>(a, grid, s);
+	return setError(kErrUnsupported, "batched FdF: start-group size must be 8 or 32");
+}
+
+int launchBatchFinish(const FinishBatchArgs& a, cudaStream_t s)
+{
+	const int threads = 256;
+	const int blocks = (int)((a.Q * 32ull + threads - 1) / threads);
+	batchFinishKernel<<<std::max(blocks, 1), threads, 0, s>>>(a);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "batch finish launch");
+}
+
+int launchLbfgs(const LbfgsArgs& a, cudaStream_t s)
+{
+	const int threads = 256;
+	const int blocks = (int)((a.Q * 32ull + threads - 1) / threads);
+	lbfgsKernel<<<std::max(blocks, 1), threads, 0, s>>>(a);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "L-BFGS launch");
+}
+
+int launchCountActive(const int* status, int Q, int* active, unsigned* nActive, cudaStream_t s)
+{
+	PWA_CHECK(cudaCheck(cudaMemsetAsync(nActive, 0, sizeof(unsigned), s), "memset"));
+	const int threads = 256;
+	const int blocks = std::min(1024, std::max(1, (Q + threads - 1) / threads));
+	countActiveKernel<<<blocks, threads, 0, s>>>(status, Q, active, nActive);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "count launch");
+}
+
+}  // namespace pwa

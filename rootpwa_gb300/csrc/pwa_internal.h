@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+struct pwa_likelihood;
+
 namespace pwa {
 
 // status codes (same values as enum pwa_status in include/pwa_gb300.h)
@@ -22,6 +24,13 @@ enum {
 	kErrUnsupported = 7,
 	kErrNumerical = 8
 };
+
+#define PWA_CHECK(expr)         \
+	do {                        \
+		const int _st = (expr); \
+		if (_st != 0)           \
+			return _st;         \
+	} while (0)
 
 // records the calling thread's last error; returns code
 int setError(int code, const std::string& msg);
@@ -142,5 +151,87 @@ int launchGramTc(const GramArgs& a, int precision, int numSMs, cudaStream_t s, d
                  size_t scratchDoubles);
 // FP32 words of per-CTA partial Grams launchGramTc needs
 size_t gramTcScratchFloats(int W, int numSMs);
+
+// ---------------------------------------------------------------------------
+// Read-only view of a finished likelihood's device data (multibin batches)
+// ---------------------------------------------------------------------------
+struct LikelihoodView {
+	const float2* amps;       // tiled store
+	uint64_t nEvents;
+	uint32_t storeB;
+	int W0, W, R, P;
+	std::vector<int> slotRe, slotIm;  // host copies, [R*W]
+	const double* accI;       // device, reordered acceptance blocks
+	double nEvt, totAcc;
+	int prior;
+	double cauchyWidth;
+	int device;
+};
+int likelihoodView(const pwa_likelihood* L, LikelihoodView* v);
+
+// ---------------------------------------------------------------------------
+// Batched multibin x multistart FdF and L-BFGS (multibin.cu)
+// ---------------------------------------------------------------------------
+struct BinDesc {
+	const float2* amps;  // tiled store of the bin (B = 128)
+	uint64_t nEvents;
+	const double* accI;  // W x W complex128 acceptance integral (one reflectivity)
+	double nEvt, totAcc;
+	int q0;              // first problem of the bin
+	int nStarts;
+};
+struct BatchItem {
+	int bin, group;      // starts [group * SG, ...) of the bin
+	uint32_t t0, t1;     // tiles [t0, t1) of the bin
+};
+struct ProblemDesc {
+	int bin, slot;       // slot within its start group
+	int item0, item1;    // items of its (bin, group)
+};
+struct BatchArgs {
+	const BinDesc* bins;
+	const BatchItem* items;
+	int nItems;
+	int W, P, SG;
+	const int* slotRe;   // [W] parameter index of Re V_w or -1 (rank 1)
+	const int* slotIm;
+	const double* x;     // [Q][P] trial points
+	const int* active;   // [Q]
+	double* partials;    // [nItems][SG][2 + 2W]
+	unsigned* devErr;
+};
+struct FinishBatchArgs {
+	const BinDesc* bins;
+	const ProblemDesc* problems;
+	int Q, W, P, SG;
+	const int* slotRe;
+	const int* slotIm;
+	const double* x;
+	const int* active;
+	const double* partials;
+	int prior;
+	double cauchyWidth;
+	double* f;           // [Q]
+	double* g;           // [Q][P]
+};
+enum { kLbfgsInit = 0, kLbfgsSearch = 1, kLbfgsConverged = 2, kLbfgsMaxIter = 3, kLbfgsStalled = 4, kLbfgsFailed = 5 };
+struct LbfgsArgs {
+	int Q, P, m, maxIter;
+	double gtolAbs, gtolRel;
+	double *x, *g, *d, *xt;        // [Q][P]
+	const double* ft;              // [Q] trial values
+	const double* gt;              // [Q][P] trial gradients
+	double *f, *gnorm, *step, *gamma;  // [Q]
+	double *S, *Y;                 // [Q][m][P]
+	double *rho, *alphaBuf;        // [Q][m]
+	int *status, *iter, *nBack, *hist, *head;  // [Q]
+};
+size_t batchSmemBytes(int W, int SG);
+// sets the kernel's shared-memory limit (before any launch or stream capture)
+int configureBatchFdf(int W, int SG, size_t maxSmem);
+int launchBatchFdf(const BatchArgs& a, int grid, cudaStream_t s);
+int launchBatchFinish(const FinishBatchArgs& a, cudaStream_t s);
+int launchLbfgs(const LbfgsArgs& a, cudaStream_t s);
+int launchCountActive(const int* status, int Q, int* active, unsigned* nActive, cudaStream_t s);
 
 }  // namespace pwa
