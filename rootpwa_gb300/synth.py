@@ -114,3 +114,43 @@ def make_workload(name="compass15", seed=0, n_data=None, n_mc=None, rank=None, a
     par = rng.standard_normal(P)
     return dict(name=name, names=names, refl=refl, rank=cfg["rank"], data=data, mc=mc, accepted=accepted,
                 par=par, n_neg=cfg["n_neg"], n_pos=cfg["n_pos"])
+
+
+# ---------------------------------------------------------------------------
+# Multibin workloads: bins whose data follow the model intensity of a known
+# production-amplitude vector
+# ---------------------------------------------------------------------------
+def multibin_event_counts(n_bins=400, median=40_000, sigma_ln=1.0, lo=2_000, hi=400_000, seed=0):
+    """Events per bin: LogNormal(ln median, sigma_ln) truncated to [lo, hi]
+    (draws outside the range are redrawn)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = np.empty(n_bins, dtype=np.int64)
+    k = 0
+    while k < n_bins:
+        n = int(round(np.exp(rng.normal(np.log(median), sigma_ln))))
+        if lo <= n <= hi:
+            out[k] = n
+            k += 1
+    return out
+
+
+def true_production_amplitudes(n_waves, rng):
+    """V_true: re/im ~ N(0, 1) per wave, flat amplitude |N(0, 1)|."""
+    v = rng.standard_normal(n_waves) + 1j * rng.standard_normal(n_waves)
+    return v.astype(np.complex128), float(abs(rng.standard_normal()))
+
+
+def draw_bin_device(model, v_true, flat, n_events, seed, pool_factor=4, device="cuda"):
+    """Data events of one bin, importance-resampled from phase-space draws in
+    proportion to the rank-1 intensity |sum_w V_w A_w|^2 + flat^2 (multinomial
+    resampling with replacement from a pool of pool_factor * n_events draws).
+    Returns complex64 [wave][event] on the device."""
+    import torch
+    pool = draw_device(model, pool_factor * n_events, seed=seed, device=device)
+    v = torch.from_numpy(v_true.astype(np.complex64)).to(device)
+    s = v @ pool
+    inten = (s.real * s.real + s.imag * s.imag + flat * flat).float()
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed) + 7919)
+    idx = torch.multinomial(inten, n_events, replacement=True, generator=g)
+    return pool[:, idx].contiguous()
