@@ -304,6 +304,32 @@ int pwa_multibin_sweep_ms(pwa_multibin* M, const double* x, uint32_t reps, doubl
 int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t sweepsPerGraph, uint32_t maxSweeps,
                      double* x, double* f, double* gnorm, int32_t* status, uint32_t* iterations, uint32_t* sweeps);
 
+/* ------------------------------------------------------------------------ */
+/* Learned warm start (no reference counterpart): a 3-layer perceptron        */
+/* nIn -> nHidden1 -> nHidden2 -> nOut with relu, BF16 weights and            */
+/* activations, FP32 accumulation and FP32 master weights, trained with Adam  */
+/* on the mean squared error.  Parameters are laid out W1 [nHidden1][nIn], b1,*/
+/* W2 [nHidden2][nHidden1], b2, W3 [nOut][nHidden2], b3 (FP32).               */
+/* ------------------------------------------------------------------------ */
+typedef struct pwa_mlp pwa_mlp;
+/* He-normal weights from `seed`, zero biases */
+int pwa_mlp_create(pwa_mlp** out, uint32_t nIn, uint32_t nHidden1, uint32_t nHidden2, uint32_t nOut, uint64_t seed);
+int pwa_mlp_destroy(pwa_mlp* net);
+int pwa_mlp_nmb_params(const pwa_mlp* net, uint64_t* n);
+int pwa_mlp_get_params(const pwa_mlp* net, float* params);
+/* sets the FP32 master weights (and their BF16 copy); resets Adam's moments */
+int pwa_mlp_set_params(pwa_mlp* net, const float* params);
+/* Y [B][nOut] = net(X [B][nIn]) (host buffers; X is rounded to BF16) */
+int pwa_mlp_forward(pwa_mlp* net, const float* X, uint32_t B, float* Y);
+/* mean squared error of net(X) against T [B][nOut] and its gradient in the
+ * parameter layout (host buffers; loss and grad may be NULL) */
+int pwa_mlp_gradient(pwa_mlp* net, const float* X, const float* T, uint32_t B, double* loss, float* grad);
+/* Adam (lr, betas 0.9 / 0.999) over `epochs` shuffled passes of mini-batches
+ * of `batch` samples; lossHistory [epochs] (may be NULL) gets the mean batch
+ * loss of each epoch */
+int pwa_mlp_train(pwa_mlp* net, const float* X, const float* T, uint64_t nSamples, uint32_t batch, uint32_t epochs,
+                  float lr, uint64_t seed, double* lossHistory);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

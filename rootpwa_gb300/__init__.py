@@ -7,3 +7,4 @@ libpwa_gb300.so behind the C ABI of include/pwa_gb300.h.
 from ._native import PwaError, lib  # noqa: F401
 from .likelihood import ampIntegralMatrix, pwaLikelihood  # noqa: F401
 from .multibin import pwaMultibin  # noqa: F401
+from .warmstart import pwaMLP  # noqa: F401

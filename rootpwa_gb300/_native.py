@@ -80,6 +80,14 @@ SIGNATURES = {
     "pwa_multibin_nmb_pars": (i, [vp, C.POINTER(u32)]),
     "pwa_multibin_fdf": (i, [vp, pd, pd, pd]),
     "pwa_multibin_sweep_ms": (i, [vp, pd, u32, pd]),
+    "pwa_mlp_create": (i, [pvp, u32, u32, u32, u32, u64]),
+    "pwa_mlp_destroy": (i, [vp]),
+    "pwa_mlp_nmb_params": (i, [vp, C.POINTER(u64)]),
+    "pwa_mlp_get_params": (i, [vp, C.POINTER(C.c_float)]),
+    "pwa_mlp_set_params": (i, [vp, C.POINTER(C.c_float)]),
+    "pwa_mlp_forward": (i, [vp, C.POINTER(C.c_float), u32, C.POINTER(C.c_float)]),
+    "pwa_mlp_gradient": (i, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), u32, pd, C.POINTER(C.c_float)]),
+    "pwa_mlp_train": (i, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), u64, u32, u32, C.c_float, u64, pd]),
     "pwa_multibin_fit": (i, [vp, pd, i, u32, u32, pd, pd, pd, C.POINTER(i32), C.POINTER(u32), C.POINTER(u32)]),
     "pwa_likelihood_create": (i, [pvp]),
     "pwa_likelihood_destroy": (i, [vp]),

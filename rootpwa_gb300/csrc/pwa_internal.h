@@ -234,4 +234,32 @@ int launchBatchFinish(const FinishBatchArgs& a, cudaStream_t s);
 int launchLbfgs(const LbfgsArgs& a, cudaStream_t s);
 int launchCountActive(const int* status, int Q, int* active, unsigned* nActive, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Warm-start network kernels (mlp.cu)
+// ---------------------------------------------------------------------------
+// C[M][N] = sum_k A(m, k) B(k, n) (+ bias[n], relu, relu mask), BF16 operands
+// A(m, k) = A[m * lda_m + k * lda_k], B(k, n) = B[k * ldb_k + n * ldb_n]
+struct MlpGemm {
+	int M, N, K;
+	const uint16_t* A;
+	size_t lda_m, lda_k;
+	int aContigK;        // 1 when lda_k == 1 (load order along k)
+	const uint16_t* B;
+	size_t ldb_k, ldb_n;
+	int bContigK;        // 1 when ldb_k == 1
+	const float* bias;   // [N] or null
+	int relu;
+	const uint16_t* mask;  // BF16 [M][N]: zero the output where mask <= 0, or null
+	float* C32;          // FP32 [M][N] or null
+	uint16_t* C16;       // BF16 [M][N] or null
+};
+int launchMlpGemm(const MlpGemm& g, cudaStream_t s);
+int launchColSum(const float* X, int M, int N, float* out, cudaStream_t s);
+int launchMse(const float* Y, const float* T, int n, float scale, float* dY32, uint16_t* dY16, double* loss,
+              cudaStream_t s);
+int launchAdam(float* w, const float* g, float* m, float* v, uint16_t* w16, size_t n, float lr, float b1, float b2,
+               float eps, float c1, float c2, cudaStream_t s);
+int launchToBf16(const float* x, uint16_t* y, size_t n, cudaStream_t s);
+int launchGatherRows(const void* src, const uint32_t* idx, int rows, size_t rowBytes, void* dst, cudaStream_t s);
+
 }  // namespace pwa

@@ -1,0 +1,166 @@
+"""Learned warm start for multibin fits.
+
+A 3-layer perceptron (pwa_mlp_*, hand-written CUDA kernels, BF16 with FP32
+accumulation) maps a bin's data-averaged moment matrix
+    M_ij = < a_i conj(a_j) >_data,  a = (A_w / sqrt(N_ww), 1)
+(the normalised decay amplitudes of the likelihood plus the flat wave, all
+real and imaginary parts) and log N to the production amplitudes at the
+likelihood minimum, V / sqrt(N) (real and imaginary parts of the waves and
+the flat wave).  The plain fit always refines the prediction; random start
+points remain the fallback.  There is no reference counterpart: ROOTPWA
+starts its fits from random amplitudes (pwaFit.cc:231-257).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _pf(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class pwaMLP:
+    """nIn -> nHidden1 -> nHidden2 -> nOut perceptron on the GPU."""
+
+    def __init__(self, nIn, nHidden1=512, nHidden2=512, nOut=102, seed=0):
+        h = C.c_void_p()
+        N.call("pwa_mlp_create", C.byref(h), int(nIn), int(nHidden1), int(nHidden2), int(nOut), int(seed))
+        self._h = h
+        self.shape = (int(nIn), int(nHidden1), int(nHidden2), int(nOut))
+        # input standardisation (set by fit_standardisation)
+        self.mu = np.zeros(nIn, dtype=np.float32)
+        self.sd = np.ones(nIn, dtype=np.float32)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and N._lib is not None:
+            N.lib().pwa_mlp_destroy(h)
+            self._h = None
+
+    def nmbParams(self):
+        n = C.c_uint64()
+        N.call("pwa_mlp_nmb_params", self._h, C.byref(n))
+        return n.value
+
+    def params(self):
+        p = np.zeros(self.nmbParams(), dtype=np.float32)
+        N.call("pwa_mlp_get_params", self._h, _pf(p))
+        return p
+
+    def setParams(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nmbParams()
+        N.call("pwa_mlp_set_params", self._h, _pf(p))
+
+    def _X(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        assert X.ndim == 2 and X.shape[1] == self.shape[0]
+        return X
+
+    def forward(self, X):
+        X = self._X(X)
+        Y = np.zeros((X.shape[0], self.shape[3]), dtype=np.float32)
+        N.call("pwa_mlp_forward", self._h, _pf(X), X.shape[0], _pf(Y))
+        return Y
+
+    def gradient(self, X, T):
+        """(mean squared error, gradient in the parameter layout)."""
+        X = self._X(X)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = C.c_double()
+        g = np.zeros(self.nmbParams(), dtype=np.float32)
+        N.call("pwa_mlp_gradient", self._h, _pf(X), _pf(T), X.shape[0], C.byref(loss), _pf(g))
+        return loss.value, g
+
+    def train(self, X, T, batch=256, epochs=50, lr=1e-3, seed=0):
+        """Adam on standardised inputs; returns the mean loss of each epoch."""
+        X = self._X(X)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        hist = np.zeros(epochs)
+        N.call("pwa_mlp_train", self._h, _pf(X), _pf(T), X.shape[0], int(batch), int(epochs), float(lr), int(seed),
+               hist.ctypes.data_as(C.POINTER(C.c_double)))
+        return hist
+
+    # -- standardised use ------------------------------------------------------
+    def fit_standardisation(self, F):
+        self.mu = F.mean(axis=0).astype(np.float32)
+        self.sd = (F.std(axis=0) + 1e-6).astype(np.float32)
+
+    def standardise(self, F):
+        return ((F - self.mu) / self.sd).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# features and targets
+# ---------------------------------------------------------------------------
+def moment_features(names, data, norm_diag, precision="tf32x3"):
+    """Features of one bin: the real and imaginary parts of the moment matrix
+    of (A_w / sqrt(N_ww), 1) over the data events and log N.
+
+    data: complex64 [W][N] device array (torch); norm_diag: the
+    normalisation integral's diagonal per event (element(w, w))."""
+    import torch
+    from .likelihood import ampIntegralMatrix
+    W, n = data.shape
+    ext = torch.cat([data, torch.ones((1, n), dtype=data.dtype, device=data.device)], dim=0).contiguous()
+    I = ampIntegralMatrix()
+    I.integrate(list(names) + ["flat"], ext, precision=precision)
+    M = I.matrix() / n
+    s = np.concatenate([1.0 / np.sqrt(np.asarray(norm_diag, dtype=np.float64)), [1.0]])
+    M = M * s[:, None] * s[None, :]
+    return np.concatenate([M.real.ravel(), M.imag.ravel(), [np.log(n)]]).astype(np.float32)
+
+
+def prod_amp_indices(L):
+    """Parameter indices (re, im or -1) of the production amplitudes and the
+    flat wave, in wave order (pwaLikelihood::buildProdAmpArrays)."""
+    _, idx = L.buildProdAmpArrays(np.zeros(L.nmbPars()), withFlat=True)
+    return idx
+
+
+def params_to_complex(L, x):
+    idx = prod_amp_indices(L)
+    return np.array([(x[r] if r >= 0 else 0.0) + 1j * (x[i] if i >= 0 else 0.0) for r, i in idx])
+
+
+def complex_to_params(L, v):
+    """Parameter vector from complex amplitudes (waves then flat), rotated so
+    that the first wave is real and positive (the layout's convention)."""
+    idx = prod_amp_indices(L)
+    v = np.asarray(v, dtype=np.complex128)
+    ph = np.exp(-1j * np.angle(v[0])) if abs(v[0]) > 0 else 1.0
+    v = v.copy()
+    v[:-1] *= ph
+    v[-1] = abs(v[-1])
+    x = np.zeros(L.nmbPars())
+    for (r, i), c in zip(idx, v):
+        if r >= 0:
+            x[r] = c.real
+        if i >= 0:
+            x[i] = c.imag
+    return x
+
+
+def targets_from_params(L, x, n_events):
+    v = params_to_complex(L, L.CorrectParamSigns(x)) / np.sqrt(n_events)
+    return np.concatenate([v.real, v.imag]).astype(np.float32)
+
+
+def params_from_targets(L, y, n_events):
+    k = len(y) // 2
+    v = (np.asarray(y[:k], dtype=np.float64) + 1j * np.asarray(y[k:], dtype=np.float64)) * np.sqrt(n_events)
+    return complex_to_params(L, v)
+
+
+def start_from_truth(L, v_true, flat, n_events):
+    """The true amplitudes mapped to the likelihood's normalisation: each wave
+    scaled by sqrt(N_ww) (normalised amplitudes), all scaled so that the
+    expected number of accepted events equals n_events."""
+    normM, accM, _ = L.integralMatrices(withFlat=False)
+    d = np.sqrt(np.real(np.diag(normM)))
+    v = np.asarray(v_true) * d
+    expected = np.real(np.conj(v) @ (accM @ v)) + flat * flat * L.totAcc()
+    s = np.sqrt(n_events / max(expected, 1e-300))
+    return complex_to_params(L, np.concatenate([v * s, [flat * s]]))
