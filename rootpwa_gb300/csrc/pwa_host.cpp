@@ -2653,14 +2653,15 @@ int pwa_mlp_get_params(const pwa_mlp* N, float* out)
 {
 	if (!N || !out)
 		return setError(kErrArg, "null argument");
-	return cudaCheck(cudaMemcpy(out, N->params.p, N->nPar * 4, cudaMemcpyDeviceToHost), "download");
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(out, N->params.p, N->nPar * 4, cudaMemcpyDeviceToHost, N->stream), "download"));
+	return cudaCheck(cudaStreamSynchronize(N->stream), "MLP parameters");
 }
 
 int pwa_mlp_set_params(pwa_mlp* N, const float* in)
 {
 	if (!N || !in)
 		return setError(kErrArg, "null argument");
-	PWA_TRY(cudaCheck(cudaMemcpy(N->params.p, in, N->nPar * 4, cudaMemcpyHostToDevice), "upload"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(N->params.p, in, N->nPar * 4, cudaMemcpyHostToDevice, N->stream), "upload"));
 	PWA_TRY(launchToBf16(N->params.as<float>(), N->w16.as<uint16_t>(), N->nPar, N->stream));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(N->adamM.p, 0, N->nPar * 4, N->stream), "memset"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(N->adamV.p, 0, N->nPar * 4, N->stream), "memset"));
@@ -2687,10 +2688,12 @@ int pwa_mlp_gradient(pwa_mlp* N, const float* X, const float* T, uint32_t B, dou
 	PWA_TRY(mlpForward(N, (int)B));
 	PWA_TRY(mlpBackward(N, (int)B));
 	if (loss)
-		PWA_TRY(cudaCheck(cudaMemcpy(loss, N->loss.p, sizeof(double), cudaMemcpyDeviceToHost), "download"));
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(loss, N->loss.p, sizeof(double), cudaMemcpyDeviceToHost, N->stream),
+		                  "download"));
 	if (grad)
-		PWA_TRY(cudaCheck(cudaMemcpy(grad, N->grads.p, N->nPar * 4, cudaMemcpyDeviceToHost), "download"));
-	return kOk;
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(grad, N->grads.p, N->nPar * 4, cudaMemcpyDeviceToHost, N->stream),
+		                  "download"));
+	return cudaCheck(cudaStreamSynchronize(N->stream), "MLP gradient");
 }
 
 int pwa_mlp_train(pwa_mlp* N, const float* X, const float* T, uint64_t nSamples, uint32_t batch, uint32_t epochs,
@@ -2735,7 +2738,8 @@ int pwa_mlp_train(pwa_mlp* N, const float* X, const float* T, uint64_t nSamples,
 			PWA_TRY(mlpForward(N, B));
 			PWA_TRY(mlpBackward(N, B));
 			double l = 0.;
-			PWA_TRY(cudaCheck(cudaMemcpy(&l, N->loss.p, sizeof(double), cudaMemcpyDeviceToHost), "download"));
+			PWA_TRY(cudaCheck(cudaMemcpyAsync(&l, N->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s), "download"));
+			PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "MLP step"));
 			epochLoss += l;
 			PWA_TRY(mlpAdam(N, lr));
 		}

@@ -164,3 +164,32 @@ def start_from_truth(L, v_true, flat, n_events):
     expected = np.real(np.conj(v) @ (accM @ v)) + flat * flat * L.totAcc()
     s = np.sqrt(n_events / max(expected, 1e-300))
     return complex_to_params(L, np.concatenate([v * s, [flat * s]]))
+
+
+def augment_phases(F, Y, n_waves, copies, rng):
+    """Training-set augmentation by per-wave phase rotations.
+
+    When the phase-space amplitudes of each wave are distributed invariantly
+    under a phase rotation, rotating wave w by theta_w maps a bin's moments
+    to M_ij exp(i (theta_i - theta_j)) and its minimum to
+    V_w exp(i (theta_0 - theta_w)) (the first wave stays real, the flat wave
+    is unchanged).  Returns the original rows followed by `copies` rotated
+    copies of each."""
+    n = n_waves + 1
+    F = np.asarray(F, dtype=np.float64)
+    Y = np.asarray(Y, dtype=np.float64)
+    M = (F[:, :n * n] + 1j * F[:, n * n:2 * n * n]).reshape(-1, n, n)
+    v = Y[:, :n] + 1j * Y[:, n:2 * n]
+    outF, outY = [F], [Y]
+    for _ in range(copies):
+        th = np.zeros((len(F), n))
+        th[:, :n_waves] = rng.uniform(0, 2 * np.pi, (len(F), n_waves))
+        e = np.exp(1j * th)
+        M2 = M * e[:, :, None] * np.conj(e)[:, None, :]
+        rot = np.exp(1j * (th[:, :1] - th))
+        rot[:, -1] = 1.0
+        v2 = v * rot
+        outF.append(np.concatenate([M2.real.reshape(len(F), -1), M2.imag.reshape(len(F), -1), F[:, 2 * n * n:]],
+                                   axis=1))
+        outY.append(np.concatenate([v2.real, v2.imag], axis=1))
+    return np.concatenate(outF).astype(np.float32), np.concatenate(outY).astype(np.float32)

@@ -42,8 +42,8 @@ def test_training_reduces_loss():
     X = rng.standard_normal((2048, 20)).astype(np.float32)
     T = np.tanh(X @ A).astype(np.float32)
     net = R.pwaMLP(20, 64, 64, 6, seed=1)
-    hist = net.train(X, T, batch=128, epochs=30, lr=3e-3)
-    assert hist[-1] < 0.1 * hist[0]
+    hist = net.train(X, T, batch=128, epochs=100, lr=3e-3)
+    assert hist[-1] < 0.05 * hist[0]
 
 
 def _bins(n_bins, names, model, norm, acc, rng, seed0, lo=2000, hi=8000):
@@ -91,11 +91,11 @@ def test_warm_start_gains_over_random_starts():
     x0 = np.stack([WS.start_from_truth(b["L"], b["vt"], b["flat"], b["n"]) for b in train])
     res = fit(train, x0, 1)
     Y = np.stack([WS.targets_from_params(b["L"], res["x"][k], b["n"]) for k, b in enumerate(train)])
-    F = features(train)
+    F, Y = WS.augment_phases(features(train), Y, len(names), 64, np.random.default_rng(1))
     net = R.pwaMLP(F.shape[1], 128, 128, Y.shape[1], seed=4)
     net.fit_standardisation(F)
-    hist = net.train(net.standardise(F), Y, batch=64, epochs=300, lr=1e-3)
-    assert hist[-1] < 0.2 * hist[0]
+    hist = net.train(net.standardise(F), Y, batch=64, epochs=30, lr=1e-3)
+    assert hist[-1] < 0.05 * hist[0]
     # test bins: warm start vs random starts
     Yp = net.forward(net.standardise(features(test)))
     xw = np.stack([WS.params_from_targets(b["L"], Yp[k], b["n"]) for k, b in enumerate(test)])
@@ -104,8 +104,14 @@ def test_warm_start_gains_over_random_starts():
     xr = np.random.default_rng(9).standard_normal((len(test) * S, xw.shape[1]))
     rand = fit(test, xr, S)
     best = rand["f"].reshape(len(test), S).min(axis=1)
+    # the single warm start reaches the best minimum of 8 random starts
     same = np.abs(warm["f"] - best) <= 1e-6 * np.abs(best)
     assert same.mean() >= 0.9, same
-    it_w = np.median(warm["iterations"])
-    it_r = np.median(rand["iterations"])
-    assert it_w < 0.6 * it_r, (it_w, it_r)
+    # its start point is much closer to that minimum than random points
+    d_w = np.linalg.norm(xw - warm["x"], axis=1) / np.linalg.norm(warm["x"], axis=1)
+    d_r = np.linalg.norm(xr - rand["x"], axis=1) / np.linalg.norm(rand["x"], axis=1)
+    assert np.median(d_w) < 0.5 * np.median(d_r), (np.median(d_w), np.median(d_r))
+    # fewer iterations per start, and far fewer in total than the multi-start
+    it_w, it_r = np.median(warm["iterations"]), np.median(rand["iterations"])
+    assert it_w < 0.8 * it_r, (it_w, it_r)
+    assert warm["iterations"].sum() < 0.2 * rand["iterations"].sum()
