@@ -55,6 +55,14 @@ def parse():
                     help="arithmetic of the normalisation / acceptance integrals (set-up, not timed)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
+    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin"],
+                    help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
+                         "learned warm start")
+    ap.add_argument("--bins", type=int, default=400, help="multibin: kinematic bins (100 mass x 4 t')")
+    ap.add_argument("--starts", type=int, default=64, help="multibin: random start points of the plain fit")
+    ap.add_argument("--train-bins", type=int, default=20_000, help="multibin: synthetic training bins")
+    ap.add_argument("--augment", type=int, default=3, help="multibin: phase-rotated copies per training bin")
+    ap.add_argument("--epochs", type=int, default=30, help="multibin: training epochs")
     return ap.parse_args()
 
 
@@ -396,10 +404,154 @@ def run_gb300(args):
     return 0
 
 
+def run_multibin(args):
+    """Whole multibin fit (100 mass x 4 t' bins, 50 positive-reflectivity waves
+    + flat, rank 1): the plain fit from `starts` random start points per bin
+    against the learned warm start (moments -> network -> 1 warm + 4 random
+    start points), both refined by the batched GPU L-BFGS.  Data of each bin
+    follow the model intensity of known amplitudes; normalisation and
+    acceptance integrals from 5x as many phase-space events per bin."""
+    import torch
+    import rootpwa_gb300 as R
+    from rootpwa_gb300 import synth
+    from rootpwa_gb300 import warmstart as WS
+    W = 50
+    names, _ = synth.wave_names(0, W)
+    counts = synth.multibin_event_counts(n_bins=args.bins, seed=0)
+    model = synth.AmplitudeModel(W, 0, np.random.Generator(np.random.PCG64(5)))
+    rng = np.random.default_rng(1)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter()
+    bins = []
+    for b, n in enumerate(counts):
+        n = int(n)
+        vt, fl = synth.true_production_amplitudes(W, rng)
+        data = synth.draw_bin_device(model, vt, fl, n, seed=1000 + b)
+        mc = synth.draw_device(model, 5 * n, seed=2_000_000 + b)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(3_000_000 + b)
+        accepted = (torch.rand(5 * n, generator=g, device="cuda") < 0.6).to(torch.uint8).cpu().numpy()
+        norm = R.ampIntegralMatrix()
+        norm.integrate(names, mc, precision="tf32x3")
+        acc = R.ampIntegralMatrix()
+        acc.integrate(names, mc, inBin=accepted, precision="tf32x3")
+        del mc
+        diag = np.real(np.diag(norm.matrix())) / norm.nmbEvents()
+        L = R.pwaLikelihood()
+        L.init(names, [1] * W, None, 1, 0.0)
+        L.addNormIntegral(norm)
+        L.addAccIntegral(acc)
+        for k, nm in enumerate(names):
+            L.addAmplitude(nm, data[k])
+        L.finishInit()
+        bins.append(dict(L=L, n=n, data=data, diag=diag))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    P = bins[0]["L"].nmbPars()
+
+    # ---- training set (method-generated pairs) and network training ----
+    t0 = time.perf_counter()
+    tmc = synth.draw_device(model, 4_000_000, seed=77)
+    tnorm = R.ampIntegralMatrix()
+    tnorm.integrate(names, tmc, precision="tf32x3")
+    tacc = R.ampIntegralMatrix()
+    tacc.integrate(names, tmc, inBin=(torch.rand(4_000_000, device="cuda") < 0.6).to(torch.uint8).cpu().numpy(),
+                   precision="tf32x3")
+    del tmc
+    tcounts = synth.multibin_event_counts(n_bins=args.train_bins, seed=11)
+
+    def draw_bin(vt, fl, n, k):
+        return synth.draw_bin_device(model, vt, fl, n, seed=10_000_000 + k)
+
+    F, Y, _ = WS.generate_training_set(names, draw_bin, tnorm, tacc, tcounts, np.random.default_rng(12), chunk=500)
+    gen_s = time.perf_counter() - t0
+    Fa, Ya = WS.augment_phases(F, Y, W, args.augment, np.random.default_rng(13))
+    t0 = time.perf_counter()
+    net = R.pwaMLP(Fa.shape[1], 512, 512, Ya.shape[1], seed=14)
+    net.fit_standardisation(Fa)
+    hist = net.train(net.standardise(Fa), Ya, batch=256, epochs=args.epochs, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    del Fa, Ya
+
+    # ---- plain multi-start fit ----
+    S = args.starts
+    Mp = R.pwaMultibin()
+    Mp.setOptions(startGroup=32 if S > 8 else 8, gtolRel=1e-9, maxIter=5000)
+    for bn in bins:
+        Mp.addBin(bn["L"], S)
+    x0 = np.random.default_rng(21).standard_normal((len(bins) * S, P))
+    Mp.autotune(x0)
+    sweep_ms = Mp.sweepMs(x0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rp = Mp.fit(x0)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+
+    # ---- learned warm start: features + inference + 1 warm + 4 random starts ----
+    Sw = 5
+    Mw = R.pwaMultibin()
+    Mw.setOptions(startGroup=8, gtolRel=1e-9, maxIter=5000)
+    for bn in bins:
+        Mw.addBin(bn["L"], Sw)
+    xr = np.random.default_rng(22).standard_normal((len(bins) * Sw, P))
+    Mw.autotune(xr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Fe = np.stack([WS.moment_features(names, bn["data"], bn["diag"]) for bn in bins])
+    Yp = net.forward(net.standardise(Fe))
+    xw = xr.copy()
+    for b, bn in enumerate(bins):
+        xw[b * Sw] = WS.params_from_targets(bn["L"], Yp[b], bn["n"])
+    rw = Mw.fit(xw)
+    torch.cuda.synchronize()
+    learned_s = time.perf_counter() - t0
+
+    fp = rp["f"].reshape(len(bins), S)
+    fw = rw["f"].reshape(len(bins), Sw)
+    fstar = np.minimum(fp.min(axis=1), fw.min(axis=1))
+    tol = 1e-6 * np.abs(fstar)
+    reach_p = float(np.mean(fp.min(axis=1) <= fstar + tol))
+    reach_w = float(np.mean(fw.min(axis=1) <= fstar + tol))
+    warm_alone = float(np.mean(fw[:, 0] <= fstar + tol))
+    # fitted-V agreement in units of the parameter errors (Hessian of 16 bins)
+    verr = []
+    for b in range(0, len(bins), max(1, len(bins) // 16)):
+        L = bins[b]["L"]
+        xa = L.CorrectParamSigns(rp["x"][b * S + int(np.argmin(fp[b]))])
+        xb = L.CorrectParamSigns(rw["x"][b * Sw + int(np.argmin(fw[b]))])
+        if abs(fp[b].min() - fw[b].min()) > tol[b]:
+            continue
+        cov = L.CovarianceMatrix(xa)
+        sig = np.sqrt(np.maximum(np.diag(cov), 1e-300))
+        verr.append(float(np.max(np.abs(xa - xb) / sig)))
+    line = {"metric": "multibin fit wall time, learned warm start vs plain multi-start", "value": learned_s,
+            "unit": "s", "higher_is_better": False, "n_gpus": 1, "impl": "gb300",
+            "plain_s": plain_s, "speedup_vs_plain": plain_s / learned_s, "data": "synthetic",
+            "config": {"workload": "%d bins x 50 waves + flat, rank 1, %d data events (log-normal per bin), "
+                                   "MC 5x per bin" % (len(bins), int(counts.sum())),
+                       "starts_plain": S, "starts_learned": Sw, "gtol": "1e-9 x max(1, |f|)",
+                       "network": "5203-512-512-102 BF16/FP32, %d training bins x %d copies, %d epochs" %
+                                  (args.train_bins, args.augment + 1, args.epochs)},
+            "reached_global_min": {"plain": reach_p, "learned": reach_w, "warm_start_alone": warm_alone},
+            "v_error_sigma_max": max(verr) if verr else None, "v_error_bins": len(verr),
+            "sweeps": {"plain": rp["sweeps"], "learned": rw["sweeps"]},
+            "full_sweep_ms_plain": sweep_ms,
+            "status_counts": {"plain": np.bincount(rp["status"], minlength=6).tolist(),
+                              "learned": np.bincount(rw["status"], minlength=6).tolist()},
+            "training": {"generate_s": gen_s, "train_s": train_s, "loss_first": float(hist[0]),
+                         "loss_last": float(hist[-1])},
+            "setup_s": setup_s}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "multibin":
+        return run_multibin(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -154,16 +154,66 @@ def params_from_targets(L, y, n_events):
     return complex_to_params(L, v)
 
 
-def start_from_truth(L, v_true, flat, n_events):
-    """The true amplitudes mapped to the likelihood's normalisation: each wave
-    scaled by sqrt(N_ww) (normalised amplitudes), all scaled so that the
-    expected number of accepted events equals n_events."""
-    normM, accM, _ = L.integralMatrices(withFlat=False)
-    d = np.sqrt(np.real(np.diag(normM)))
-    v = np.asarray(v_true) * d
+def start_from_truth(L, v_true, flat, n_events, norm_diag):
+    """The true amplitudes in the likelihood's normalisation: each wave
+    scaled by sqrt(N_ww) (norm_diag: the normalisation integral's diagonal
+    per event, as the likelihood divides the amplitudes by it), all scaled so
+    that the expected number of accepted events equals n_events."""
+    _, accM, _ = L.integralMatrices(withFlat=False)  # normalised acceptance integral
+    v = np.asarray(v_true) * np.sqrt(np.asarray(norm_diag, dtype=np.float64))
     expected = np.real(np.conj(v) @ (accM @ v)) + flat * flat * L.totAcc()
     s = np.sqrt(n_events / max(expected, 1e-300))
     return complex_to_params(L, np.concatenate([v * s, [flat * s]]))
+
+
+def generate_training_set(names, draw_bin, norm, acc, counts, rng, chunk=1000, precision="tf32x3",
+                          gtolRel=1e-8, maxIter=3000):
+    """Training pairs (features, targets) produced by the method itself.
+
+    For each bin k: true amplitudes V_true (re/im ~ N(0, 1)) and a flat
+    amplitude are drawn, draw_bin(v_true, flat, counts[k], k) returns the
+    bin's data amplitudes (complex64 [W][N] on the device, drawn in
+    proportion to the model intensity), a likelihood is built with the shared
+    normalisation and acceptance integrals, and the plain batched L-BFGS fits
+    it from the true amplitudes; the target is the minimum (CorrectParamSigns
+    convention, divided by sqrt(N)) and the features the data moments.
+    Returns (F [n][(W+1)^2 * 2 + 1], Y [n][2 (W+1)], V_true [n][W])."""
+    from .likelihood import ampIntegralMatrix, pwaLikelihood
+    from .multibin import pwaMultibin
+    diag = np.real(np.diag(norm.matrix())) / norm.nmbEvents()
+    F, Y, VT = [], [], []
+    for c0 in range(0, len(counts), chunk):
+        bins = []
+        for k in range(c0, min(len(counts), c0 + chunk)):
+            vt, fl = synth_true(len(names), rng)
+            n = int(counts[k])
+            data = draw_bin(vt, fl, n, k)
+            L = pwaLikelihood()
+            L.init(names, [1] * len(names), None, 1, 0.0)
+            L.addNormIntegral(ampIntegralMatrix(norm))
+            L.addAccIntegral(ampIntegralMatrix(acc))
+            for w, nm in enumerate(names):
+                L.addAmplitude(nm, data[w])
+            L.finishInit()
+            F.append(moment_features(names, data, diag, precision))
+            del data
+            bins.append((L, vt, fl, n))
+        M = pwaMultibin()
+        M.setOptions(startGroup=8, gtolRel=gtolRel, maxIter=maxIter)
+        for L, _, _, _ in bins:
+            M.addBin(L, 1)
+        x0 = np.stack([start_from_truth(L, vt, fl, n, diag) for L, vt, fl, n in bins])
+        res = M.fit(x0)
+        for k, (L, vt, fl, n) in enumerate(bins):
+            Y.append(targets_from_params(L, res["x"][k], n))
+            VT.append(vt)
+        del M, bins
+    return np.stack(F), np.stack(Y), np.stack(VT)
+
+
+def synth_true(n_waves, rng):
+    v = rng.standard_normal(n_waves) + 1j * rng.standard_normal(n_waves)
+    return v, float(abs(rng.standard_normal()))
 
 
 def augment_phases(F, Y, n_waves, copies, rng):

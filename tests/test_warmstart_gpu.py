@@ -88,7 +88,7 @@ def test_warm_start_gains_over_random_starts():
     train = _bins(400, names, model, norm, acc, rng, 1000)
     test = _bins(24, names, model, norm, acc, rng, 5000)
     # labels: minima reached from the true amplitudes
-    x0 = np.stack([WS.start_from_truth(b["L"], b["vt"], b["flat"], b["n"]) for b in train])
+    x0 = np.stack([WS.start_from_truth(b["L"], b["vt"], b["flat"], b["n"], diag) for b in train])
     res = fit(train, x0, 1)
     Y = np.stack([WS.targets_from_params(b["L"], res["x"][k], b["n"]) for k, b in enumerate(train)])
     F, Y = WS.augment_phases(features(train), Y, len(names), 64, np.random.default_rng(1))
