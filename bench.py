@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--train-bins", type=int, default=20_000, help="multibin: synthetic training bins")
     ap.add_argument("--augment", type=int, default=3, help="multibin: phase-rotated copies per training bin")
     ap.add_argument("--epochs", type=int, default=30, help="multibin: training epochs")
+    ap.add_argument("--gtol-rel", type=float, default=1e-10,
+                    help="multibin: L-BFGS stops when |grad| <= 1e-6 + gtol_rel * max(1, |f|)")
     return ap.parse_args()
 
 
@@ -476,7 +478,7 @@ def run_multibin(args):
     # ---- plain multi-start fit ----
     S = args.starts
     Mp = R.pwaMultibin()
-    Mp.setOptions(startGroup=32 if S > 8 else 8, gtolRel=1e-9, maxIter=5000)
+    Mp.setOptions(startGroup=32 if S > 8 else 8, gtolAbs=1e-6, gtolRel=args.gtol_rel, maxIter=5000)
     for bn in bins:
         Mp.addBin(bn["L"], S)
     x0 = np.random.default_rng(21).standard_normal((len(bins) * S, P))
@@ -491,7 +493,7 @@ def run_multibin(args):
     # ---- learned warm start: features + inference + 1 warm + 4 random starts ----
     Sw = 5
     Mw = R.pwaMultibin()
-    Mw.setOptions(startGroup=8, gtolRel=1e-9, maxIter=5000)
+    Mw.setOptions(startGroup=8, gtolAbs=1e-6, gtolRel=args.gtol_rel, maxIter=5000)
     for bn in bins:
         Mw.addBin(bn["L"], Sw)
     xr = np.random.default_rng(22).standard_normal((len(bins) * Sw, P))
@@ -530,7 +532,7 @@ def run_multibin(args):
             "plain_s": plain_s, "speedup_vs_plain": plain_s / learned_s, "data": "synthetic",
             "config": {"workload": "%d bins x 50 waves + flat, rank 1, %d data events (log-normal per bin), "
                                    "MC 5x per bin" % (len(bins), int(counts.sum())),
-                       "starts_plain": S, "starts_learned": Sw, "gtol": "1e-9 x max(1, |f|)",
+                       "starts_plain": S, "starts_learned": Sw, "gtol": "1e-6 + %g x max(1, |f|)" % args.gtol_rel,
                        "network": "5203-512-512-102 BF16/FP32, %d training bins x %d copies, %d epochs" %
                                   (args.train_bins, args.augment + 1, args.epochs)},
             "reached_global_min": {"plain": reach_p, "learned": reach_w, "warm_start_alone": warm_alone},
