@@ -167,6 +167,12 @@ int pwa_likelihood_use_normalized_amps(pwa_likelihood* L, int flag);
 /* setPriorType / setCauchyWidth (pwaLikelihood.h:212-215) */
 int pwa_likelihood_set_prior_type(pwa_likelihood* L, int priorType);
 int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double width);
+/* No reference counterpart: event-sharded evaluation across processes (one
+ * likelihood per process over a contiguous share of the data events).  Only
+ * the root shard adds the normalisation term (with nEvt = totalEvents when
+ * the amplitudes are not normalised) and the prior; the sum of all shards'
+ * f and gradients (one all-reduce of P + 1 doubles) is the full FdF. */
+int pwa_likelihood_set_shard(pwa_likelihood* L, uint64_t totalEvents, int root);
 /* engine options without reference counterpart: CUDA stream of all launches,
  * cross-event reduction mode */
 int pwa_likelihood_set_stream(pwa_likelihood* L, void* cudaStream);

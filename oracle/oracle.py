@@ -56,6 +56,7 @@ def lib():
             "oracle_lik_create": (vp, []),
             "oracle_lik_destroy": (None, [vp]),
             "oracle_lik_set_options": (None, [vp, i, i, d]),
+            "oracle_lik_set_shard": (None, [vp, ul, i]),
             "oracle_lik_init": (i, [vp, u, C.POINTER(C.c_char_p), C.POINTER(C.c_int), pd, u, d]),
             "oracle_lik_add_norm_integral": (i, [vp, vp]),
             "oracle_lik_add_acc_integral": (i, [vp, vp, ul]),
@@ -183,6 +184,9 @@ class OracleLikelihood:
         if getattr(self, "_h", None):
             lib().oracle_lik_destroy(self._h)
             self._h = None
+
+    def set_shard(self, total_events, root):
+        lib().oracle_lik_set_shard(self._h, int(total_events), 1 if root else 0)
 
     def init(self, names, refl, thresholds=None, rank=1, mass_bin_center=0.0):
         r = (C.c_int * len(names))(*[int(x) for x in refl])

@@ -100,6 +100,17 @@ struct OracleLikelihood {
 	bool   useNormalizedAmps = true;   // pwaLikelihood.cc:147
 	int    priorType = 0;              // 0 = FLAT, 1 = HALF_CAUCHY
 	double cauchyWidth = 0.5;          // pwaLikelihood.cc:149
+	// event shard: only the root shard adds normalisation and prior (the
+	// product's pwa_likelihood_set_shard; no reference counterpart)
+	bool   shardSet = false, shardRoot = true;
+	unsigned long shardTotal = 0;
+	double normFactor() const
+	{
+		if (shardSet && !shardRoot) return 0.;
+		if (useNormalizedAmps) return 1.;
+		return (double)(shardSet ? shardTotal : nEvents);
+	}
+	int effPrior() const { return (shardSet && !shardRoot) ? 0 : priorType; }
 
 	// wave set
 	unsigned int nW[2] = {0, 0};       // [0] = negative, [1] = positive reflectivity
@@ -422,7 +433,7 @@ struct OracleLikelihood {
 
 		// normalisation, pwaLikelihood.cc:254-273
 		kahan<double> normAcc;
-		const double nEvt = useNormalizedAmps ? 1. : (double)nEvents;
+		const double nEvt = normFactor();
 		const double twice = 2 * nEvt;
 		for (unsigned r = 0; r < rank; ++r)
 			for (unsigned e = 0; e < 2; ++e)
@@ -440,7 +451,7 @@ struct OracleLikelihood {
 
 		// prior, pwaLikelihood.cc:278-297
 		double prior = 0.;
-		if (priorType == 1)
+		if (effPrior() == 1)
 			for (unsigned r = 0; r < rank; ++r)
 				for (unsigned e = 0; e < 2; ++e)
 					for (unsigned w = 0; w < nW[e]; ++w) {
@@ -522,7 +533,7 @@ struct OracleLikelihood {
 		for (size_t k = 0; k < nSlot; ++k) flatTerms[k] = flatTermsAcc[k].sum();
 		double hFlat = hFlatAcc.sum();
 
-		const double nEvt = useNormalizedAmps ? 1. : (double)nEvents;
+		const double nEvt = normFactor();
 		const double twice = 2 * nEvt;
 		for (unsigned r = 0; r < rank; ++r)
 			for (unsigned e = 0; e < 2; ++e)
@@ -536,7 +547,7 @@ struct OracleLikelihood {
 					}
 		hFlat += twice * totAcc;
 
-		if (priorType == 1)
+		if (effPrior() == 1)
 			for (unsigned r = 0; r < rank; ++r)
 				for (unsigned e = 0; e < 2; ++e)
 					for (unsigned w = 0; w < nW[e]; ++w) {
@@ -883,6 +894,13 @@ void oracle_lik_set_options(void* h, int useNormalizedAmps, int priorType, doubl
 	L.useNormalizedAmps = useNormalizedAmps != 0;
 	L.priorType = priorType;
 	L.cauchyWidth = cauchyWidth;
+}
+void oracle_lik_set_shard(void* h, unsigned long totalEvents, int root)
+{
+	OracleLikelihood& L = *(OracleLikelihood*)h;
+	L.shardSet = true;
+	L.shardTotal = totalEvents;
+	L.shardRoot = root != 0;
 }
 int oracle_lik_init(void* h, unsigned n, const char* const* names, const int* refl, const double* thres,
                     unsigned rank, double massBinCenter)

@@ -94,6 +94,7 @@ SIGNATURES = {
     "pwa_likelihood_use_normalized_amps": (i, [vp, i]),
     "pwa_likelihood_set_prior_type": (i, [vp, i]),
     "pwa_likelihood_set_cauchy_width": (i, [vp, C.c_double]),
+    "pwa_likelihood_set_shard": (i, [vp, u64, i]),
     "pwa_likelihood_set_stream": (i, [vp, vp]),
     "pwa_likelihood_set_reduction": (i, [vp, i]),
     "pwa_likelihood_set_autotune": (i, [vp, i]),

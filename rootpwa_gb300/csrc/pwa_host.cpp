@@ -690,6 +690,10 @@ struct pwa_likelihood {
 
 	bool useNormalizedAmps = true;
 	int priorType = PWA_PRIOR_FLAT;
+	// event shard (pwa_likelihood_set_shard): only the root shard adds the
+	// normalisation and prior terms, with the total event count
+	bool shardSet = false, shardRoot = true;
+	uint64_t shardTotal = 0;
 	double cauchyWidth = 0.5;
 	int reduction = PWA_REDUCE_FP64;
 
@@ -760,6 +764,19 @@ int checkFinished(const pwa_likelihood* L)
 	return kOk;
 }
 
+// nEvt of the normalisation term (pwaLikelihood.cc:257): 1 with normalised
+// amplitudes, else the number of data events; zero on non-root shards
+double normFactor(const pwa_likelihood* L)
+{
+	if (L->shardSet && !L->shardRoot)
+		return 0.;
+	if (L->useNormalizedAmps)
+		return 1.;
+	return (double)(L->shardSet ? L->shardTotal : L->nEvents);
+}
+
+int priorOf(const pwa_likelihood* L) { return (L->shardSet && !L->shardRoot) ? PWA_PRIOR_FLAT : L->priorType; }
+
 // Binds the handle to the current CUDA device on first device use (setup of
 // the wave set and parameter layout is pure host work).
 int ensureDevice(pwa_likelihood* L)
@@ -821,9 +838,9 @@ int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad
 	a.slotRe = L->dSlotRe.as<int>();
 	a.slotIm = L->dSlotIm.as<int>();
 	a.accI = L->dAccI.as<double>();
-	a.nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
+	a.nEvt = normFactor(L);
 	a.totAcc = L->totAcc;
-	a.prior = L->priorType;
+	a.prior = priorOf(L);
 	a.cauchyWidth = L->cauchyWidth;
 	a.withGrad = withGrad;
 	a.reduction = L->reduction;
@@ -996,6 +1013,17 @@ int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double w)
 	if (!L)
 		return setError(kErrArg, "null likelihood");
 	L->cauchyWidth = w;
+	return kOk;
+}
+
+int pwa_likelihood_set_shard(pwa_likelihood* L, uint64_t totalEvents, int root)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	L->shardSet = true;
+	L->shardTotal = totalEvents;
+	L->shardRoot = root != 0;
+	L->cacheValid = false;
 	return kOk;
 }
 
@@ -1588,7 +1616,7 @@ int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* H)
 	std::vector<cplx> V;
 	double flat;
 	fromPar(L, par, V, flat);
-	const double nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
+	const double nEvt = normFactor(L);
 	const double twice = 2. * nEvt;
 	std::vector<double> h((size_t)nS * nS * 3);
 	for (uint32_t si = 0; si < nS; ++si) {
@@ -1617,7 +1645,7 @@ int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* H)
 	for (uint32_t si = 0; si < nS; ++si)
 		flatTerms[si] = flat * g1(si, 2 * nS);
 	double hFlat = flat * flat * g1(2 * nS, 2 * nS).real() - g2(W, W).real() + twice * L->totAcc;
-	if (L->priorType == PWA_PRIOR_HALF_CAUCHY) {
+	if (priorOf(L) == PWA_PRIOR_HALF_CAUCHY) {
 		// pwaLikelihood.cc:766-798
 		const double gw = L->cauchyWidth, g2w = gw * gw;
 		for (uint32_t si = 0; si < nS; ++si) {
@@ -1910,9 +1938,9 @@ int likelihoodView(const pwa_likelihood* L, LikelihoodView* v)
 	v->slotRe = L->slotRe;
 	v->slotIm = L->slotIm;
 	v->accI = L->dAccI.as<double>();
-	v->nEvt = L->useNormalizedAmps ? 1. : (double)L->nEvents;
+	v->nEvt = normFactor(L);
 	v->totAcc = L->totAcc;
-	v->prior = L->priorType;
+	v->prior = priorOf(L);
 	v->cauchyWidth = L->cauchyWidth;
 	v->device = L->device;
 	return kOk;

@@ -219,6 +219,12 @@ class pwaLikelihood:
     def setPriorType(self, prior):
         N.call("pwa_likelihood_set_prior_type", self._h, int(prior))
 
+    def setShard(self, totalEvents, root):
+        """Event-sharded evaluation: this likelihood holds one share of the
+        events; only the root shard adds the normalisation and prior terms
+        (no reference counterpart; see rootpwa_gb300.sharded)."""
+        N.call("pwa_likelihood_set_shard", self._h, int(totalEvents), 1 if root else 0)
+
     def setCauchyWidth(self, width):
         N.call("pwa_likelihood_set_cauchy_width", self._h, float(width))
 

@@ -270,3 +270,34 @@ def test_zero_intensity_event_gives_non_finite_value():
     f1, g1 = G.FdF(p)
     assert not np.isfinite(f0) and not np.isfinite(f1)
     assert np.array_equal(np.isfinite(g1), np.isfinite(g0))
+
+
+@pytest.mark.parametrize("use_normalized,prior", [(True, 0), (False, 0), (True, 1)])
+def test_event_shards_sum_to_full_fdf(use_normalized, prior):
+    """pwa_likelihood_set_shard: two shard likelihoods over contiguous halves
+    of the events sum to the full FdF (FP32 contractions: 1e-6 / 1e-5)."""
+    from rootpwa_gb300.sharded import shard_range
+    w = synth.make_workload("compass15", seed=4, n_data=20001, n_mc=5000)
+    norm, acc = helpers.gpu_integrals(w)
+    full = helpers.build_gpu(w, R.ampIntegralMatrix(norm), R.ampIntegralMatrix(acc), use_normalized=use_normalized,
+                             prior=prior)
+    N = w["data"].shape[1]
+    f, g = 0.0, 0.0
+    for k in range(2):
+        b, e = shard_range(N, k, 2)
+        L = R.pwaLikelihood()
+        L.useNormalizedAmps(use_normalized)
+        if prior:
+            L.setPriorType(prior)
+        L.setShard(N, k == 0)
+        L.init(w["names"], w["refl"], None, w["rank"], 0.0)
+        L.addNormIntegral(R.ampIntegralMatrix(norm))
+        L.addAccIntegral(R.ampIntegralMatrix(acc))
+        for j, n in enumerate(w["names"]):
+            L.addAmplitude(n, np.ascontiguousarray(w["data"][j, b:e]))
+        L.finishInit()
+        fk, gk = L.FdF(w["par"])
+        f, g = f + fk, g + gk
+    f0, g0 = full.FdF(w["par"])
+    assert helpers.rel(f, f0) < 1e-6
+    assert helpers.normwise(g, g0) < 1e-5
