@@ -55,9 +55,11 @@ def parse():
                     help="arithmetic of the normalisation / acceptance integrals (set-up, not timed)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
-    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin"],
+    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision"],
                     help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
-                         "learned warm start")
+                         "learned warm start; precision: error of each arithmetic variant against FP64")
+    ap.add_argument("--oracle-mc", type=int, default=200_000,
+                    help="precision: MC events of the integrals compared with the CPU FP64 oracle")
     ap.add_argument("--bins", type=int, default=400, help="multibin: kinematic bins (100 mass x 4 t')")
     ap.add_argument("--starts", type=int, default=64, help="multibin: random start points of the plain fit")
     ap.add_argument("--train-bins", type=int, default=20_000, help="multibin: synthetic training bins")
@@ -548,8 +550,120 @@ def run_multibin(args):
     return 0
 
 
+def run_precision(args):
+    """Precision sweep on the production shapes (87 waves + flat, rank 2): the
+    integral matrix in FP64 / FP32 (SIMT) / TF32 / TF32x3 (tensor cores), the
+    FdF with FP64 or compensated-FP32 cross-tile reductions, and the effect of
+    each integral variant on LL and gradient; errors against FP64 (the CPU
+    oracle, and the GPU FP64 kernels at full size)."""
+    import torch
+    import rootpwa_gb300 as R
+    from rootpwa_gb300 import synth
+    from oracle.oracle import OracleIntegral, OracleLikelihood
+    names, refl = synth.wave_names(N_NEG, N_POS)
+    W = len(names)
+    rng = np.random.Generator(np.random.PCG64(1))
+    model = synth.AmplitudeModel(W, 8, rng)
+    P = synth.n_pars(N_NEG, N_POS, RANK)
+    par = rng.standard_normal(P)
+    precs = ["fp32", "tf32", "tf32x3"]
+
+    def maxrel(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    out = {}
+    # integrals against the CPU FP64 oracle (smaller MC sample)
+    mcs = model.draw(np.random.Generator(np.random.PCG64(2)), args.oracle_mc)
+    oi = OracleIntegral()
+    assert oi.integrate(names, mcs.astype(np.complex128))
+    ref = oi.raw()
+    out["integral_vs_oracle"] = {"mc_events": args.oracle_mc}
+    for p in ["fp64"] + precs:
+        I = R.ampIntegralMatrix()
+        I.integrate(names, mcs, precision=p)
+        out["integral_vs_oracle"][p] = maxrel(I.matrix(), ref)
+    # integrals at full size against the GPU FP64 kernel
+    mc = synth.draw_device(model, args.n_mc, seed=1011)
+    ints = {}
+    for p in ["fp64"] + precs:
+        I = R.ampIntegralMatrix()
+        I.integrate(names, mc, precision=p)
+        ints[p] = I
+    out["integral_vs_fp64"] = {"mc_events": args.n_mc}
+    for p in precs:
+        out["integral_vs_fp64"][p] = maxrel(ints[p].matrix(), ints["fp64"].matrix())
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2011)
+    accepted = (torch.rand(args.n_mc, generator=g, device="cuda") < 0.6).to(torch.uint8).cpu().numpy()
+    accs = {}
+    for p in ["fp64"] + precs:
+        J = R.ampIntegralMatrix()
+        J.integrate(names, mc, inBin=accepted, precision=p)
+        accs[p] = J
+    del mc
+    data = synth.draw_device(model, args.n_data, seed=11)
+    host = data.cpu().numpy()
+
+    def copy(I):
+        C_ = R.ampIntegralMatrix(I)
+        return C_
+
+    def oracle_copy(I):
+        o = OracleIntegral()
+        o.set_wave_names(I.waveNames())
+        o.set_raw(I.matrix())
+        o.set_nmb_events(I.nmbEvents())
+        return o
+
+    # FP64 oracle likelihood with the FP64 integrals
+    O = OracleLikelihood()
+    assert O.init(names, refl, None, RANK, 0.0)
+    assert O.addNormIntegral(oracle_copy(ints["fp64"])) and O.addAccIntegral(oracle_copy(accs["fp64"]))
+    for k, n in enumerate(names):
+        assert O.addAmplitude(n, host[k].astype(np.complex128))
+    assert O.finishInit()
+    f0, g0 = O.FdF(par, threads=cpu_threads())
+    out["fdf_vs_oracle"] = {"events": args.n_data}
+    for red in ["fp64", "kahan_fp32"]:
+        L = R.pwaLikelihood()
+        L.init(names, refl, None, RANK, 0.0)
+        L.addNormIntegral(copy(ints["fp64"]))
+        L.addAccIntegral(copy(accs["fp64"]))
+        for k, n in enumerate(names):
+            L.addAmplitude(n, data[k])
+        L.finishInit()
+        L.setReduction(red)
+        f, gg = L.FdF(par)
+        out["fdf_vs_oracle"][red] = {"ll_rel": abs(f - f0) / abs(f0),
+                                     "grad_normwise": float(np.max(np.abs(gg - g0)) / np.max(np.abs(g0)))}
+    # effect of the integral arithmetic on LL and gradient (GPU FdF, FP64 reductions)
+    out["fdf_integral_variant"] = {}
+    base = None
+    for p in ["fp64"] + precs:
+        L = R.pwaLikelihood()
+        L.init(names, refl, None, RANK, 0.0)
+        L.addNormIntegral(copy(ints[p]))
+        L.addAccIntegral(copy(accs[p]))
+        for k, n in enumerate(names):
+            L.addAmplitude(n, data[k])
+        L.finishInit()
+        f, gg = L.FdF(par)
+        if base is None:
+            base = (f, gg)
+        else:
+            out["fdf_integral_variant"][p] = {"ll_rel": abs(f - base[0]) / abs(base[0]),
+                                              "grad_normwise": float(np.max(np.abs(gg - base[1])) /
+                                                                     np.max(np.abs(base[1])))}
+    line = {"metric": "precision sweep (errors against FP64)", "workload": "compass88: 87 waves + flat, rank 2, "
+            "%d data / %d MC events" % (args.n_data, args.n_mc), "data": "synthetic", "results": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "precision":
+        return run_precision(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "multibin":
