@@ -541,8 +541,10 @@ def run_multibin(args):
             "v_error_sigma_max": max(verr) if verr else None, "v_error_bins": len(verr),
             "sweeps": {"plain": rp["sweeps"], "learned": rw["sweeps"]},
             "full_sweep_ms_plain": sweep_ms,
-            "status_counts": {"plain": np.bincount(rp["status"], minlength=6).tolist(),
-                              "learned": np.bincount(rw["status"], minlength=6).tolist()},
+            "status_counts": {"plain": np.bincount(rp["status"], minlength=7).tolist(),
+                              "learned": np.bincount(rw["status"], minlength=7).tolist(),
+                              "order": ["active", "searching", "converged", "max_iter", "stalled", "failed",
+                                        "floor"]},
             "training": {"generate_s": gen_s, "train_s": train_s, "loss_first": float(hist[0]),
                          "loss_last": float(hist[-1])},
             "setup_s": setup_s}

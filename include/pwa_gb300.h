@@ -277,7 +277,8 @@ int pwa_likelihood_kernel_times(pwa_likelihood* L, double* eventKernelMs, double
 typedef struct pwa_multibin pwa_multibin;
 /* L-BFGS status of a problem (one bin x one start point) */
 enum pwa_lbfgs_status { PWA_LBFGS_ACTIVE = 0, PWA_LBFGS_SEARCHING = 1, PWA_LBFGS_CONVERGED = 2,
-                        PWA_LBFGS_MAX_ITER = 3, PWA_LBFGS_STALLED = 4, PWA_LBFGS_FAILED = 5 };
+                        PWA_LBFGS_MAX_ITER = 3, PWA_LBFGS_STALLED = 4, PWA_LBFGS_FAILED = 5,
+                        PWA_LBFGS_FLOOR = 6 /* gradient norm stopped improving (rounding floor) */ };
 int pwa_multibin_create(pwa_multibin** out);
 int pwa_multibin_destroy(pwa_multibin* M);
 /* adds a bin: a likelihood after finishInit (rank 1, one reflectivity, at
@@ -290,6 +291,9 @@ int pwa_multibin_add_bin(pwa_multibin* M, pwa_likelihood* L, uint32_t nStarts);
  * iteration limit per problem */
 int pwa_multibin_set_options(pwa_multibin* M, uint32_t startGroup, uint32_t lbfgsMemory, double gtolAbs,
                              double gtolRel, uint32_t maxIter);
+/* a problem stops with PWA_LBFGS_FLOOR when its gradient norm has not
+ * improved by 1% for this many iterations (default 50, 0 = never) */
+int pwa_multibin_set_floor_window(pwa_multibin* M, uint32_t iterations);
 /* tiles of 128 events per work item for bins of < 64, < 512 and >= 512 tiles */
 int pwa_multibin_set_chunks(pwa_multibin* M, const uint32_t* tilesPerItem);
 int pwa_multibin_chunks(const pwa_multibin* M, uint32_t* tilesPerItem);

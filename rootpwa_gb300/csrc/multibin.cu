@@ -529,6 +529,20 @@ __global__ void lbfgsKernel(const LbfgsArgs a)
 			a.status[q] = kLbfgsConverged;
 		return;
 	}
+	// rounding floor: the gradient norm has not improved by 1% for
+	// floorWindow iterations (FP32 contractions bound how small it gets)
+	if (a.floorWindow > 0) {
+		if (st == kLbfgsInit || gnorm < 0.99 * a.gBest[q]) {
+			if (lane == 0) {
+				a.gBest[q] = gnorm;
+				a.itBest[q] = iter;
+			}
+		} else if (iter - a.itBest[q] >= a.floorWindow) {
+			if (lane == 0)
+				a.status[q] = kLbfgsFloor;
+			return;
+		}
+	}
 	if (iter >= a.maxIter) {
 		if (lane == 0)
 			a.status[q] = kLbfgsMaxIter;

@@ -1969,7 +1969,7 @@ struct pwa_multibin {
 
 	// options
 	int SG = 32;
-	uint32_t m = 8, maxIter = 5000;
+	uint32_t m = 8, maxIter = 5000, floorWindow = 50;
 	double gtolAbs = 0., gtolRel = 1e-6;
 	uint32_t chunkTiles[3] = {16, 16, 16};  // tiles per work item, by bin size class
 
@@ -1977,8 +1977,8 @@ struct pwa_multibin {
 	bool built = false;
 	int Q = 0, nItems = 0;
 	DevBuf dBins, dItems, dProblems, dSlotRe, dSlotIm, dPartials, dErr;
-	DevBuf dX, dXt, dG, dGt, dD, dF, dFt, dGnorm, dStep, dGamma, dS, dY, dRho, dAlpha;
-	DevBuf dStatus, dIter, dNBack, dHist, dHead, dActive, dNActive;
+	DevBuf dX, dXt, dG, dGt, dD, dF, dFt, dGnorm, dStep, dGamma, dGBest, dS, dY, dRho, dAlpha;
+	DevBuf dStatus, dIter, dNBack, dHist, dHead, dItBest, dActive, dNActive;
 	PinnedBuf hCount;
 
 	~pwa_multibin()
@@ -2038,13 +2038,13 @@ int buildBatch(pwa_multibin* M)
 	PWA_TRY(M->dErr.alloc(sizeof(unsigned), "flag"));
 	for (DevBuf* b : {&M->dX, &M->dXt, &M->dG, &M->dGt, &M->dD})
 		PWA_TRY(b->alloc(Q * P * sizeof(double), "multibin vectors"));
-	for (DevBuf* b : {&M->dF, &M->dFt, &M->dGnorm, &M->dStep, &M->dGamma})
+	for (DevBuf* b : {&M->dF, &M->dFt, &M->dGnorm, &M->dStep, &M->dGamma, &M->dGBest})
 		PWA_TRY(b->alloc(Q * sizeof(double), "multibin scalars"));
 	PWA_TRY(M->dS.alloc(Q * M->m * P * sizeof(double), "L-BFGS history"));
 	PWA_TRY(M->dY.alloc(Q * M->m * P * sizeof(double), "L-BFGS history"));
 	PWA_TRY(M->dRho.alloc(Q * M->m * sizeof(double), "L-BFGS history"));
 	PWA_TRY(M->dAlpha.alloc(Q * M->m * sizeof(double), "L-BFGS history"));
-	for (DevBuf* b : {&M->dStatus, &M->dIter, &M->dNBack, &M->dHist, &M->dHead, &M->dActive})
+	for (DevBuf* b : {&M->dStatus, &M->dIter, &M->dNBack, &M->dHist, &M->dHead, &M->dItBest, &M->dActive})
 		PWA_TRY(b->alloc(Q * sizeof(int), "multibin state"));
 	PWA_TRY(M->dNActive.alloc(sizeof(unsigned), "counter"));
 	PWA_TRY(M->hCount.ensure(sizeof(unsigned), "counter"));
@@ -2121,6 +2121,9 @@ LbfgsArgs lbfgsArgs(pwa_multibin* M)
 	l.gnorm = M->dGnorm.as<double>();
 	l.step = M->dStep.as<double>();
 	l.gamma = M->dGamma.as<double>();
+	l.gBest = M->dGBest.as<double>();
+	l.itBest = M->dItBest.as<int>();
+	l.floorWindow = (int)M->floorWindow;
 	l.S = M->dS.as<double>();
 	l.Y = M->dY.as<double>();
 	l.rho = M->dRho.as<double>();
@@ -2254,6 +2257,14 @@ int pwa_multibin_set_options(pwa_multibin* M, uint32_t startGroup, uint32_t lbfg
 	return kOk;
 }
 
+int pwa_multibin_set_floor_window(pwa_multibin* M, uint32_t iterations)
+{
+	if (!M)
+		return setError(kErrArg, "null handle");
+	M->floorWindow = iterations;
+	return kOk;
+}
+
 int pwa_multibin_set_chunks(pwa_multibin* M, const uint32_t* tilesPerItem)
 {
 	if (!M || !tilesPerItem)
@@ -2359,7 +2370,7 @@ int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t s
 	const size_t Q = (size_t)M->Q, P = (size_t)M->P;
 	cudaStream_t s = M->stream;
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dX.p, x0, Q * P * sizeof(double), cudaMemcpyHostToDevice, s), "upload"));
-	for (DevBuf* b : {&M->dStatus, &M->dIter, &M->dNBack, &M->dHist, &M->dHead})
+	for (DevBuf* b : {&M->dStatus, &M->dIter, &M->dNBack, &M->dHist, &M->dHead, &M->dItBest})
 		PWA_TRY(cudaCheck(cudaMemsetAsync(b->p, 0, Q * sizeof(int), s), "memset"));
 	PWA_TRY(startSweep(M, x0));
 	const uint32_t per = std::max<uint32_t>(1, sweepsPerGraph);

@@ -214,17 +214,19 @@ struct FinishBatchArgs {
 	double* f;           // [Q]
 	double* g;           // [Q][P]
 };
-enum { kLbfgsInit = 0, kLbfgsSearch = 1, kLbfgsConverged = 2, kLbfgsMaxIter = 3, kLbfgsStalled = 4, kLbfgsFailed = 5 };
+enum { kLbfgsInit = 0, kLbfgsSearch = 1, kLbfgsConverged = 2, kLbfgsMaxIter = 3, kLbfgsStalled = 4, kLbfgsFailed = 5,
+       kLbfgsFloor = 6 };
 struct LbfgsArgs {
 	int Q, P, m, maxIter;
+	int floorWindow;               // iterations without a 1% better gradient norm -> kLbfgsFloor (0: off)
 	double gtolAbs, gtolRel;
 	double *x, *g, *d, *xt;        // [Q][P]
 	const double* ft;              // [Q] trial values
 	const double* gt;              // [Q][P] trial gradients
-	double *f, *gnorm, *step, *gamma;  // [Q]
+	double *f, *gnorm, *step, *gamma, *gBest;  // [Q]
 	double *S, *Y;                 // [Q][m][P]
 	double *rho, *alphaBuf;        // [Q][m]
-	int *status, *iter, *nBack, *hist, *head;  // [Q]
+	int *status, *iter, *nBack, *hist, *head, *itBest;  // [Q]
 };
 size_t batchSmemBytes(int W, int SG);
 // sets the kernel's shared-memory limit (before any launch or stream capture)

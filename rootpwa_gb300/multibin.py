@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _native as N
 
-STATUS = {0: "active", 1: "searching", 2: "converged", 3: "max_iter", 4: "stalled", 5: "failed"}
+STATUS = {0: "active", 1: "searching", 2: "converged", 3: "max_iter", 4: "stalled", 5: "failed", 6: "floor"}
 
 
 def _pd(a):
@@ -47,6 +47,11 @@ class pwaMultibin:
     def setOptions(self, startGroup=32, lbfgsMemory=8, gtolAbs=0.0, gtolRel=1e-6, maxIter=5000):
         N.call("pwa_multibin_set_options", self._h, int(startGroup), int(lbfgsMemory), float(gtolAbs),
                float(gtolRel), int(maxIter))
+
+    def setFloorWindow(self, iterations):
+        """Stop a problem whose gradient norm has not improved by 1% for this
+        many iterations (status 'floor'; 0 disables)."""
+        N.call("pwa_multibin_set_floor_window", self._h, int(iterations))
 
     def setChunks(self, tiles):
         arr = (C.c_uint32 * 3)(*[int(t) for t in tiles])
