@@ -502,19 +502,34 @@ def run_multibin(args):
     Mw.autotune(xr)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    Fe = np.stack([WS.moment_features(names, bn["data"], bn["diag"]) for bn in bins])
+    Fe = WS.moment_features_batch([bn["data"] for bn in bins], [bn["diag"] for bn in bins])
+    t_feat = time.perf_counter()
     Yp = net.forward(net.standardise(Fe))
     xw = xr.copy()
     for b, bn in enumerate(bins):
         xw[b * Sw] = WS.params_from_targets(bn["L"], Yp[b], bn["n"])
+    t_inf = time.perf_counter()
     rw = Mw.fit(xw)
     torch.cuda.synchronize()
     learned_s = time.perf_counter() - t0
+    breakdown = {"features_s": t_feat - t0, "inference_s": t_inf - t_feat, "fit_s": time.perf_counter() - t_inf}
 
     fp = rp["f"].reshape(len(bins), S)
     fw = rw["f"].reshape(len(bins), Sw)
     fstar = np.minimum(fp.min(axis=1), fw.min(axis=1))
     tol = 1e-6 * np.abs(fstar)
+
+    def time_to_global(Mx, starts, offset):
+        # first check at which every bin has a start within 1e-6 of its global minimum
+        t, f = Mx.trace()
+        for k in range(len(t)):
+            best = np.nanmin(f[k].reshape(len(bins), starts), axis=1)
+            if np.all(best <= fstar + tol):
+                return offset + float(t[k])
+        return None
+
+    ttg_plain = time_to_global(Mp, S, 0.0)
+    ttg_learned = time_to_global(Mw, Sw, breakdown["features_s"] + breakdown["inference_s"])
     reach_p = float(np.mean(fp.min(axis=1) <= fstar + tol))
     reach_w = float(np.mean(fw.min(axis=1) <= fstar + tol))
     warm_alone = float(np.mean(fw[:, 0] <= fstar + tol))
@@ -529,9 +544,14 @@ def run_multibin(args):
         cov = L.CovarianceMatrix(xa)
         sig = np.sqrt(np.maximum(np.diag(cov), 1e-300))
         verr.append(float(np.max(np.abs(xa - xb) / sig)))
-    line = {"metric": "multibin fit wall time, learned warm start vs plain multi-start", "value": learned_s,
-            "unit": "s", "higher_is_better": False, "n_gpus": 1, "impl": "gb300",
-            "plain_s": plain_s, "speedup_vs_plain": plain_s / learned_s, "data": "synthetic",
+    line = {"metric": "multibin fit: GPU wall time to reach every bin's global-minimum LL (1e-6 relative), "
+                      "learned warm start", "value": ttg_learned, "unit": "s", "higher_is_better": False,
+            "n_gpus": 1, "impl": "gb300",
+            "plain_time_to_global_s": ttg_plain,
+            "speedup_time_to_global": (ttg_plain / ttg_learned) if (ttg_plain and ttg_learned) else None,
+            "full_fit_s": {"learned": learned_s, "plain": plain_s, "speedup": plain_s / learned_s},
+            "learned_breakdown": breakdown,
+            "data": "synthetic",
             "config": {"workload": "%d bins x 50 waves + flat, rank 1, %d data events (log-normal per bin), "
                                    "MC 5x per bin" % (len(bins), int(counts.sum())),
                        "starts_plain": S, "starts_learned": Sw, "gtol": "1e-6 + %g x max(1, |f|)" % args.gtol_rel,

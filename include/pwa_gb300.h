@@ -291,6 +291,10 @@ int pwa_multibin_add_bin(pwa_multibin* M, pwa_likelihood* L, uint32_t nStarts);
  * iteration limit per problem */
 int pwa_multibin_set_options(pwa_multibin* M, uint32_t startGroup, uint32_t lbfgsMemory, double gtolAbs,
                              double gtolRel, uint32_t maxIter);
+/* trace of the last fit: at each check (every sweepsPerGraph sweeps) the
+ * seconds since the fit started and the accepted f of every problem
+ * (f [check][Q]); returns the number of checks (copies at most maxChecks) */
+int pwa_multibin_trace(const pwa_multibin* M, uint32_t maxChecks, double* seconds, double* f, uint32_t* nChecks);
 /* a problem stops with PWA_LBFGS_FLOOR when its gradient norm has not
  * improved by 1% for this many iterations (default 50, 0 = never) */
 int pwa_multibin_set_floor_window(pwa_multibin* M, uint32_t iterations);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "pwa_multibin_set_options": (i, [vp, u32, u32, C.c_double, C.c_double, u32]),
     "pwa_multibin_set_chunks": (i, [vp, C.POINTER(u32)]),
     "pwa_multibin_set_floor_window": (i, [vp, u32]),
+    "pwa_multibin_trace": (i, [vp, u32, pd, pd, C.POINTER(u32)]),
     "pwa_multibin_chunks": (i, [vp, C.POINTER(u32)]),
     "pwa_multibin_autotune": (i, [vp, pd]),
     "pwa_multibin_nmb_problems": (i, [vp, C.POINTER(u32)]),

@@ -62,12 +62,18 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 	static_assert((SG / SPT) * (kBE / EPT) == kBThreads, "phase-1 mapping");
 	static_assert((SG / SPT2) * (64 / WPT) == kBThreads, "phase-2 mapping");
 	static_assert(EPT % 2 == 0 && SPT2 % 2 == 0 && SPT % 2 == 0, "paired loads");
+	static_assert(SPT == SPT2, "both phases group the starts in the same quads");
+	constexpr int NQ = SG / SPT;  // start groups of SPT (phase-1 sq, phase-2 sp)
 	extern __shared__ __align__(128) unsigned char smem[];
 	const int W = a.W, P = a.P;
 	const BatchSmem lay = batchSmem(W, SG);
 	float2* stages = reinterpret_cast<float2*>(smem + lay.stages);  // [2][W][kBE]
-	float4* Vs = reinterpret_cast<float4*>(smem + lay.vs);          // [W][SG] (vx, vx, vy, vy)
-	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);          // [2][kBE][SG] c S
+	// V of start s = q * SPT + i at [w][i][q] (vx, vx, vy, vy): a quarter-warp
+	// (q = 0..7) reads 128 contiguous bytes
+	float4* Vs = reinterpret_cast<float4*>(smem + lay.vs);
+	// c S of the start pair (q * SPT + 2h, +1) of event e at 16-byte chunk
+	// e * SG / 2 + h * NQ + q: again contiguous over q for both phases
+	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);          // [2][kBE][SG]
 	float* flat2 = reinterpret_cast<float*>(smem + lay.flat);       // [SG]
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	__shared__ double redLL[kBThreads / 32][SG], redC[kBThreads / 32][SG];
@@ -108,7 +114,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 				vr = ir >= 0 ? (float)x[ir] : 0.f;
 				vi = ii >= 0 ? (float)x[ii] : 0.f;
 			}
-			Vs[k] = make_float4(vr, vr, vi, vi);
+			Vs[w * SG + (s % SPT) * NQ + s / SPT] = make_float4(vr, vr, vi, vi);
 		}
 		for (int s = tid; s < SG; s += kBThreads) {
 			const double f = (s < ns) ? a.x[(size_t)(q0 + s) * P + P - 1] : 0.;
@@ -162,7 +168,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 #pragma unroll
 					for (int j = 0; j < EPT; ++j)
 						U[i][j] = Z[i][j] = make_float2(0.f, 0.f);
-				const uint32_t vAddr = smemAddr(Vs) + (uint32_t)s1 * 16u;
+				const uint32_t vAddr = smemAddr(Vs) + (uint32_t)sq * 16u;
 				for (int w = 0; w < W; ++w) {
 					const int pos = (e1 + (int)storeRot((uint32_t)w, kBE)) & (kBE - 1);
 					float2 av[EPT];
@@ -174,7 +180,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 					}
 #pragma unroll
 					for (int i = 0; i < SPT; ++i) {
-						const float4 v = lds128(vAddr + (uint32_t)(w * SG + i) * 16u);
+						const float4 v = lds128(vAddr + (uint32_t)(w * SG + i * NQ) * 16u);
 						const float2 vx = make_float2(v.x, v.y), vy = make_float2(v.z, v.w);
 #pragma unroll
 						for (int j = 0; j < EPT; ++j) {
@@ -199,7 +205,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 							kahanAdd(csF[i + h], csK[i + h], c);
 							ts[h] = make_float2(c * sx, c * sy);
 						}
-						*reinterpret_cast<float4*>(&T[(e1 + j) * SG + s1 + i]) =
+						*reinterpret_cast<float4*>(&T[2 * ((e1 + j) * (SG / 2) + (i / 2) * NQ + sq)]) =
 						    make_float4(ts[0].x, ts[0].y, ts[1].x, ts[1].y);
 					}
 				}
@@ -219,7 +225,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 
 			// ---- phase 2: G += sum_e c S conj(A) ----
 			if (w2 < W) {
-				const uint32_t tAddr = smemAddr(T) + (uint32_t)s2 * 8u;
+				const uint32_t tAddr = smemAddr(T) + (uint32_t)sp * 16u;
 				int rot[WPT];
 #pragma unroll
 				for (int j = 0; j < WPT; ++j)
@@ -228,7 +234,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 					float2 t[SPT2];
 #pragma unroll
 					for (int i = 0; i < SPT2; i += 2) {
-						const float4 q = lds128(tAddr + (uint32_t)(e * SG + i) * 8u);
+						const float4 q = lds128(tAddr + (uint32_t)(e * (SG / 2) + (i / 2) * NQ) * 16u);
 						t[i] = make_float2(q.x, q.y);
 						t[i + 1] = make_float2(q.z, q.w);
 					}

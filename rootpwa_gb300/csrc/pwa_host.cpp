@@ -1980,6 +1980,8 @@ struct pwa_multibin {
 	DevBuf dX, dXt, dG, dGt, dD, dF, dFt, dGnorm, dStep, dGamma, dGBest, dS, dY, dRho, dAlpha;
 	DevBuf dStatus, dIter, dNBack, dHist, dHead, dItBest, dActive, dNActive;
 	PinnedBuf hCount;
+	// per check of the last fit: elapsed seconds and every problem's current f
+	std::vector<double> traceT, traceF;
 
 	~pwa_multibin()
 	{
@@ -2257,6 +2259,20 @@ int pwa_multibin_set_options(pwa_multibin* M, uint32_t startGroup, uint32_t lbfg
 	return kOk;
 }
 
+int pwa_multibin_trace(const pwa_multibin* M, uint32_t maxChecks, double* seconds, double* f, uint32_t* nChecks)
+{
+	if (!M || !nChecks)
+		return setError(kErrArg, "null argument");
+	const size_t n = M->traceT.size();
+	*nChecks = (uint32_t)n;
+	const size_t k = std::min<size_t>(n, maxChecks);
+	if (seconds)
+		std::copy(M->traceT.begin(), M->traceT.begin() + k, seconds);
+	if (f && M->Q > 0)
+		std::copy(M->traceF.begin(), M->traceF.begin() + k * (size_t)M->Q, f);
+	return kOk;
+}
+
 int pwa_multibin_set_floor_window(pwa_multibin* M, uint32_t iterations)
 {
 	if (!M)
@@ -2395,6 +2411,10 @@ int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t s
 	uint32_t done = 0;
 	unsigned* nAct = static_cast<unsigned*>(M->hCount.p);
 	int st = kOk;
+	M->traceT.clear();
+	M->traceF.clear();
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "fit start"));
+	const double t0 = seconds();
 	while (done < maxSweeps) {
 		if (exec)
 			st = cudaCheck(cudaGraphLaunch(exec, s), "graph launch");
@@ -2407,6 +2427,14 @@ int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t s
 		st = cudaCheck(cudaMemcpyAsync(nAct, M->dNActive.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "count");
 		if (st == kOk)
 			st = cudaCheck(cudaStreamSynchronize(s), "fit sync");
+		if (st == kOk) {
+			// trace: elapsed time and the accepted f of every problem
+			M->traceT.push_back(seconds() - t0);
+			const size_t o = M->traceF.size();
+			M->traceF.resize(o + Q);
+			st = cudaCheck(cudaMemcpy(M->traceF.data() + o, M->dF.p, Q * sizeof(double), cudaMemcpyDeviceToHost),
+			               "trace");
+		}
 		if (st != kOk || *nAct == 0)
 			break;
 	}

@@ -99,6 +99,15 @@ class pwaMultibin:
         N.call("pwa_multibin_sweep_ms", self._h, _pd(x), int(reps), C.byref(ms))
         return ms.value
 
+    def trace(self):
+        """(seconds [checks], f [checks][Q]) recorded by the last fit."""
+        n = C.c_uint32()
+        N.call("pwa_multibin_trace", self._h, 0, None, None, C.byref(n))
+        t = np.zeros(n.value)
+        f = np.zeros((n.value, self.nmbProblems()))
+        N.call("pwa_multibin_trace", self._h, n.value, _pd(t), _pd(f), C.byref(n))
+        return t, f
+
     def fit(self, x0, useGraph=True, sweepsPerGraph=25, maxSweeps=1_000_000):
         """L-BFGS of every problem from x0; returns a dict with x, f, gnorm,
         status, iterations and sweeps."""

@@ -113,6 +113,40 @@ def moment_features(names, data, norm_diag, precision="tf32x3"):
     return np.concatenate([M.real.ravel(), M.imag.ravel(), [np.log(n)]]).astype(np.float32)
 
 
+def moment_features_batch(datas, norm_diags):
+    """moment_features of many bins at once, from device amplitudes in place:
+    the W x W sums A conj(A)^T of each bin by the allocation-free Gram entry
+    point (pwa_gram_device_noalloc, FP32, all bins ordered on one stream),
+    the sums of A by a device reduction, one download at the end."""
+    import torch
+    W = datas[0].shape[0]
+    nb = len(datas)
+    gram = torch.empty((nb, W, W), dtype=torch.complex128, device=datas[0].device)
+    sums = torch.empty((nb, W), dtype=torch.complex128, device=datas[0].device)
+    stream = torch.cuda.current_stream()
+    for b, d in enumerate(datas):
+        assert d.is_contiguous() and d.dtype == torch.complex64
+        n = d.shape[1]
+        N.call("pwa_gram_device_noalloc", C.c_void_p(d.data_ptr()), n, n, W, None, 1,
+               C.c_void_p(gram[b].data_ptr()), C.c_void_p(stream.cuda_stream))
+        sums[b] = d.sum(dim=1).to(torch.complex128)
+    G = gram.cpu().numpy()
+    S = sums.cpu().numpy()
+    F = []
+    for b, d in enumerate(datas):
+        n = d.shape[1]
+        M = np.empty((W + 1, W + 1), dtype=np.complex128)
+        M[:W, :W] = G[b]
+        M[:W, W] = S[b]
+        M[W, :W] = np.conj(S[b])
+        M[W, W] = n
+        M /= n
+        sc = np.concatenate([1.0 / np.sqrt(np.asarray(norm_diags[b], dtype=np.float64)), [1.0]])
+        M = M * sc[:, None] * sc[None, :]
+        F.append(np.concatenate([M.real.ravel(), M.imag.ravel(), [np.log(n)]]))
+    return np.asarray(F, dtype=np.float32)
+
+
 def prod_amp_indices(L):
     """Parameter indices (re, im or -1) of the production amplitudes and the
     flat wave, in wave order (pwaLikelihood::buildProdAmpArrays)."""

@@ -76,7 +76,11 @@ def test_warm_start_gains_over_random_starts():
     diag = np.real(np.diag(norm.matrix())) / norm.nmbEvents()
 
     def features(bins):
-        return np.stack([WS.moment_features(names, b["data"], diag) for b in bins])
+        F = np.stack([WS.moment_features(names, b["data"], diag) for b in bins])
+        # the batched, allocation-free path gives the same features
+        Fb = WS.moment_features_batch([b["data"] for b in bins], [diag] * len(bins))
+        assert np.max(np.abs(Fb - F)) <= 1e-5 * np.max(np.abs(F))
+        return F
 
     def fit(bins, x0, starts):
         M = R.pwaMultibin()
