@@ -488,7 +488,7 @@ def run_multibin(args):
     sweep_ms = Mp.sweepMs(x0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    rp = Mp.fit(x0)
+    rp = Mp.fit(x0, sweepsPerGraph=10)
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
 
@@ -500,6 +500,9 @@ def run_multibin(args):
         Mw.addBin(bn["L"], Sw)
     xr = np.random.default_rng(22).standard_normal((len(bins) * Sw, P))
     Mw.autotune(xr)
+    # one-time kernel loading of the feature and inference paths, outside the timed region
+    WS.moment_features_batch([bins[0]["data"]], [bins[0]["diag"]])
+    net.forward(np.zeros((1, net.shape[0]), dtype=np.float32))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     Fe = WS.moment_features_batch([bn["data"] for bn in bins], [bn["diag"] for bn in bins])
@@ -509,7 +512,7 @@ def run_multibin(args):
     for b, bn in enumerate(bins):
         xw[b * Sw] = WS.params_from_targets(bn["L"], Yp[b], bn["n"])
     t_inf = time.perf_counter()
-    rw = Mw.fit(xw)
+    rw = Mw.fit(xw, sweepsPerGraph=10)
     torch.cuda.synchronize()
     learned_s = time.perf_counter() - t0
     breakdown = {"features_s": t_feat - t0, "inference_s": t_inf - t_feat, "fit_s": time.perf_counter() - t_inf}
