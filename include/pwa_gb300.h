@@ -205,6 +205,39 @@ int pwa_likelihood_add_acc_integral(pwa_likelihood* L, pwa_integral* accMatrix, 
  * all data events, from host or device memory; normalised on upload */
 int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const void* amps, uint64_t nEvents,
                                  int ampType, int memory);
+/* setOnTheFlyBinning (pwaLikelihood.cc:1391-1440): keep only the events of
+ * the data file whose binning variables all satisfy lower[v] <= x_v <
+ * upper[v], in file order.  binVars[v] points to nFileEvents doubles (host or
+ * device memory); the selection runs on the GPU.  Call after
+ * addAccIntegral() and before addAmplitude(); addAmplitude() then takes the
+ * whole file's nFileEvents amplitudes and keeps the selected ones. */
+int pwa_likelihood_set_otf_binning(pwa_likelihood* L, uint32_t nVars, const double* lower, const double* upper,
+                                   const double* const* binVars, uint64_t nFileEvents, int memory);
+/* number of data events selected by the on-the-fly binning (0 when unset) */
+int pwa_likelihood_otf_selected(const pwa_likelihood* L, uint64_t* nSelected);
+/* Raw amplitude files.  No reference counterpart as a format: they replace
+ * the per-wave ROOT trees of amplitudeTreeLeaf objects
+ * (storageFormats/amplitudeTreeLeaf.h:51-118) read by addAmplitude
+ * (pwaLikelihood.cc:1110-1288) and the event-metadata binning variables read
+ * by setOnTheFlyBinning (pwaLikelihood.cc:1391-1440).  One file holds N
+ * events of one event file: W complex64 amplitude rows (one per wave, the
+ * wave's N values contiguous) and V float64 binning-variable rows, after a
+ * header with the names; the data block starts at a 4096-byte boundary.
+ * amps is [nWaves][nEvents] complex64 and vars [nVars][nEvents] float64,
+ * both host memory. */
+int pwa_ampfile_write(const char* path, uint32_t nWaves, const char* const* waveNames, uint64_t nEvents,
+                      const void* amps, uint32_t nVars, const char* const* varNames, const double* vars);
+int pwa_ampfile_info(const char* path, uint32_t* nWaves, uint64_t* nEvents, uint32_t* nVars);
+/* name of wave i (isVariable = 0) or of binning variable i (isVariable = 1) */
+int pwa_ampfile_name(const char* path, int isVariable, uint32_t i, char* buf, uint32_t bufLen);
+/* addAmplitude for every wave of the wave list from amplitude files, the
+ * files' events concatenated in the order given, with on-the-fly binning on
+ * the named variables when nBinVars > 0 (lower <= x < upper for each).  The
+ * files are streamed through pinned buffers into device memory; the
+ * selection and gather run on the GPU.  Call after addAccIntegral() and
+ * before finishInit(), instead of addAmplitude(). */
+int pwa_likelihood_load_amp_files(pwa_likelihood* L, uint32_t nFiles, const char* const* paths, uint32_t nBinVars,
+                                  const char* const* binVarNames, const double* lower, const double* upper);
 /* finishInit (pwaLikelihood.cc:1291-1388) */
 int pwa_likelihood_finish_init(pwa_likelihood* L);
 

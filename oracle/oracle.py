@@ -57,6 +57,8 @@ def lib():
             "oracle_lik_destroy": (None, [vp]),
             "oracle_lik_set_options": (None, [vp, i, i, d]),
             "oracle_lik_set_shard": (None, [vp, ul, i]),
+            "oracle_lik_set_otf_binning": (i, [vp, u, pd, pd, C.POINTER(C.c_void_p), ul]),
+            "oracle_lik_otf_selected": (ul, [vp]),
             "oracle_lik_init": (i, [vp, u, C.POINTER(C.c_char_p), C.POINTER(C.c_int), pd, u, d]),
             "oracle_lik_add_norm_integral": (i, [vp, vp]),
             "oracle_lik_add_acc_integral": (i, [vp, vp, ul]),
@@ -187,6 +189,19 @@ class OracleLikelihood:
 
     def set_shard(self, total_events, root):
         lib().oracle_lik_set_shard(self._h, int(total_events), 1 if root else 0)
+
+    def setOnTheFlyBinning(self, boundaries, bin_vars):
+        """pwaLikelihood::setOnTheFlyBinning (pwaLikelihood.cc:1391-1440)."""
+        names = list(boundaries)
+        lo = np.array([boundaries[k][0] for k in names], dtype=np.float64)
+        hi = np.array([boundaries[k][1] for k in names], dtype=np.float64)
+        cols = [np.ascontiguousarray(bin_vars[k], dtype=np.float64) for k in names]
+        n = len(cols[0]) if cols else 0
+        ptrs = (C.c_void_p * max(1, len(cols)))(*[c.ctypes.data for c in cols])
+        return bool(lib().oracle_lik_set_otf_binning(self._h, len(names), _pd(lo), _pd(hi), ptrs, n))
+
+    def otfSelected(self):
+        return int(lib().oracle_lik_otf_selected(self._h))
 
     def init(self, names, refl, thresholds=None, rank=1, mass_bin_center=0.0):
         r = (C.c_int * len(names))(*[int(x) for x in refl])

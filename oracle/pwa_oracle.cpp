@@ -111,6 +111,29 @@ struct OracleLikelihood {
 		return (double)(shardSet ? shardTotal : nEvents);
 	}
 	int effPrior() const { return (shardSet && !shardRoot) ? 0 : priorType; }
+	// on-the-fly binning (pwaLikelihood.cc:1391-1440): file indices of the
+	// events with lower <= x < upper for every binning variable
+	bool otfSet = false;
+	unsigned long otfFileEvents = 0;
+	std::vector<unsigned long> otfIdx;
+	bool setOtf(unsigned nVars, const double* lower, const double* upper, const double* const* vars,
+	            unsigned long nFile)
+	{
+		if (nEvents != 0 or nFile == 0)
+			return false;
+		otfSet = true;
+		otfFileEvents = nFile;
+		otfIdx.clear();
+		for (unsigned long i = 0; i < nFile; ++i) {
+			bool use = true;
+			for (unsigned v = 0; v < nVars; ++v)
+				if (vars[v][i] < lower[v] or vars[v][i] >= upper[v])
+					use = false;
+			if (use)
+				otfIdx.push_back(i);
+		}
+		return true;
+	}
 
 	// wave set
 	unsigned int nW[2] = {0, 0};       // [0] = negative, [1] = positive reflectivity
@@ -250,6 +273,18 @@ struct OracleLikelihood {
 	{
 		if (not accAdded or n == 0)
 			return false;
+		std::vector<double> sel;
+		if (otfSet) {
+			if (n != otfFileEvents or otfIdx.empty())
+				return false;
+			sel.resize(2 * otfIdx.size());
+			for (size_t k = 0; k < otfIdx.size(); ++k) {
+				sel[2 * k] = a[2 * otfIdx[k]];
+				sel[2 * k + 1] = a[2 * otfIdx[k] + 1];
+			}
+			a = sel.data();
+			n = otfIdx.size();
+		}
 		auto it = waveParams.find(name);
 		if (it == waveParams.end())
 			return false;
@@ -902,6 +937,12 @@ void oracle_lik_set_shard(void* h, unsigned long totalEvents, int root)
 	L.shardTotal = totalEvents;
 	L.shardRoot = root != 0;
 }
+int oracle_lik_set_otf_binning(void* h, unsigned nVars, const double* lower, const double* upper,
+                               const double* const* vars, unsigned long nFile)
+{
+	return ((OracleLikelihood*)h)->setOtf(nVars, lower, upper, vars, nFile) ? 1 : 0;
+}
+unsigned long oracle_lik_otf_selected(void* h) { return ((OracleLikelihood*)h)->otfIdx.size(); }
 int oracle_lik_init(void* h, unsigned n, const char* const* names, const int* refl, const double* thres,
                     unsigned rank, double massBinCenter)
 {

@@ -8,3 +8,4 @@ from ._native import PwaError, lib  # noqa: F401
 from .likelihood import ampIntegralMatrix, pwaLikelihood  # noqa: F401
 from .multibin import pwaMultibin  # noqa: F401
 from .warmstart import pwaMLP  # noqa: F401
+from .ampfile import ampFileInfo, readAmplitudeFile, writeAmplitudeFile  # noqa: F401

@@ -97,6 +97,12 @@ SIGNATURES = {
     "pwa_likelihood_set_prior_type": (i, [vp, i]),
     "pwa_likelihood_set_cauchy_width": (i, [vp, C.c_double]),
     "pwa_likelihood_set_shard": (i, [vp, u64, i]),
+    "pwa_likelihood_set_otf_binning": (i, [vp, u32, pd, pd, C.POINTER(vp), u64, i]),
+    "pwa_likelihood_otf_selected": (i, [vp, C.POINTER(u64)]),
+    "pwa_likelihood_load_amp_files": (i, [vp, u32, C.POINTER(C.c_char_p), u32, C.POINTER(C.c_char_p), pd, pd]),
+    "pwa_ampfile_write": (i, [C.c_char_p, u32, C.POINTER(C.c_char_p), u64, vp, u32, C.POINTER(C.c_char_p), pd]),
+    "pwa_ampfile_info": (i, [C.c_char_p, C.POINTER(u32), C.POINTER(u64), C.POINTER(u32)]),
+    "pwa_ampfile_name": (i, [C.c_char_p, i, u32, C.c_char_p, u32]),
     "pwa_likelihood_set_stream": (i, [vp, vp]),
     "pwa_likelihood_set_reduction": (i, [vp, i]),
     "pwa_likelihood_set_autotune": (i, [vp, i]),

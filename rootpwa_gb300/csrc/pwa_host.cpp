@@ -713,6 +713,10 @@ struct pwa_likelihood {
 
 	uint64_t nEvents = 0;
 	uint32_t storeB = 128;  // events per store block (storeIndex)
+	// on-the-fly binning: indices of the selected events of the data file
+	bool otfSet = false;
+	uint64_t otfFileEvents = 0, otfSelected = 0;
+	DevBuf otfIdx;
 	DevBuf amps, ampTmp;
 	std::vector<char> added[2];
 
@@ -1016,6 +1020,149 @@ int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double w)
 	return kOk;
 }
 
+int pwa_likelihood_set_otf_binning(pwa_likelihood* L, uint32_t nVars, const double* lower, const double* upper,
+                                   const double* const* binVars, uint64_t nFileEvents, int memory)
+{
+	if (!L || (nVars && (!lower || !upper || !binVars)))
+		return setError(kErrArg, "null argument");
+	if (!L->initialized)
+		return setError(kErrState, "likelihood not initialized");
+	if (L->finished || L->nEvents != 0)
+		return setError(kErrState, "setOnTheFlyBinning must come before addAmplitude()");
+	if (nVars > (uint32_t)kOtfMaxVars)
+		return setError(kErrArg, "at most 8 binning variables");
+	if (nFileEvents == 0)
+		return setError(kErrArg, "no events in the data file");
+	if (memory != PWA_MEMORY_HOST && memory != PWA_MEMORY_DEVICE)
+		return setError(kErrArg, "unknown memory kind");
+	PWA_TRY(ensureDevice(L));
+	cudaStream_t s = L->stream;
+	OtfArgs a{};
+	a.nVars = (int)nVars;
+	a.n = nFileEvents;
+	for (uint32_t v = 0; v < nVars; ++v) {
+		a.lower[v] = lower[v];
+		a.upper[v] = upper[v];
+	}
+	DevBuf vars, counts, offsets;
+	PWA_TRY(vars.alloc(std::max<uint64_t>(1, nVars) * nFileEvents * sizeof(double), "binning variables"));
+	if (memory == PWA_MEMORY_DEVICE)
+		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device binning variables"));
+	for (uint32_t v = 0; v < nVars; ++v)
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(vars.as<double>() + (size_t)v * nFileEvents, binVars[v],
+		                                  nFileEvents * sizeof(double),
+		                                  memory == PWA_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+		                                  s),
+		                  "binning variable upload"));
+	a.vars = vars.as<double>();
+	const uint64_t blocks = (nFileEvents + kOtfChunk - 1) / kOtfChunk;
+	PWA_TRY(counts.alloc(blocks * sizeof(unsigned), "OTF counts"));
+	PWA_TRY(launchOtfCount(a, counts.as<unsigned>(), s));
+	std::vector<unsigned> hc(blocks);
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(hc.data(), counts.p, blocks * sizeof(unsigned), cudaMemcpyDeviceToHost, s),
+	                  "OTF counts"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "OTF counts"));
+	std::vector<unsigned long long> off(blocks);
+	unsigned long long total = 0;
+	for (uint64_t b = 0; b < blocks; ++b) {
+		off[b] = total;
+		total += hc[b];
+	}
+	L->otfSet = true;
+	L->otfFileEvents = nFileEvents;
+	L->otfSelected = total;
+	if (total > 0) {
+		PWA_TRY(offsets.alloc(blocks * sizeof(unsigned long long), "OTF offsets"));
+		PWA_TRY(L->otfIdx.alloc(total * sizeof(unsigned long long), "OTF indices"));
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(offsets.p, off.data(), blocks * sizeof(unsigned long long),
+		                                  cudaMemcpyHostToDevice, s),
+		                  "OTF offsets"));
+		PWA_TRY(launchOtfCompact(a, offsets.as<unsigned long long>(), L->otfIdx.as<unsigned long long>(), s));
+	}
+	return cudaCheck(cudaStreamSynchronize(s), "OTF binning");
+}
+
+int pwa_likelihood_load_amp_files(pwa_likelihood* L, uint32_t nFiles, const char* const* paths, uint32_t nBinVars,
+                                  const char* const* binVarNames, const double* lower, const double* upper)
+{
+	if (!L || !paths || nFiles == 0 || (nBinVars && (!binVarNames || !lower || !upper)))
+		return setError(kErrArg, "null argument");
+	if (!L->accAdded)
+		return setError(kErrState, "no acceptance integral found; call addAccIntegral() before loading amplitudes");
+	if (L->finished || L->nEvents != 0 || L->otfSet)
+		return setError(kErrState, "amplitudes or a binning were already added");
+	if (nBinVars > (uint32_t)kOtfMaxVars)
+		return setError(kErrArg, "at most 8 binning variables");
+	std::vector<AmpFile> files(nFiles);
+	uint64_t total = 0;
+	for (uint32_t f = 0; f < nFiles; ++f) {
+		if (!paths[f])
+			return setError(kErrArg, "null path");
+		PWA_TRY(ampFileOpen(paths[f], files[f]));
+		total += files[f].nEvents;
+	}
+	if (total == 0)
+		return setError(kErrArg, "the amplitude files hold no events");
+	auto find = [](const std::vector<std::string>& v, const std::string& name) -> int {
+		for (size_t i = 0; i < v.size(); ++i)
+			if (v[i] == name)
+				return (int)i;
+		return -1;
+	};
+	// every wave of the wave list must be in every file: finishInit refuses a
+	// wave without amplitudes (pwaLikelihood.cc:1295-1302)
+	std::vector<std::string> waves;
+	for (const auto& kv : L->waveIdx)
+		waves.push_back(kv.first);
+	for (const auto& f : files)
+		for (const auto& w : waves)
+			if (find(f.waves, w) < 0)
+				return setError(kErrArg, "could not find amplitude for wave '" + w + "' in file '" + f.path + "'");
+	PWA_TRY(ensureDevice(L));
+	cudaStream_t s = L->stream;
+	if (nBinVars) {
+		DevBuf vars;
+		PWA_TRY(vars.alloc(nBinVars * total * sizeof(double), "binning variables"));
+		std::vector<const double*> cols(nBinVars);
+		for (uint32_t v = 0; v < nBinVars; ++v) {
+			if (!binVarNames[v])
+				return setError(kErrArg, "null binning variable name");
+			uint64_t at = 0;
+			for (const auto& f : files) {
+				const int k = find(f.vars, binVarNames[v]);
+				if (k < 0)
+					return setError(kErrArg, std::string("binning variable '") + binVarNames[v] + "' is not in file '" +
+					                             f.path + "'");
+				PWA_TRY(ampFileToDevice(f, f.varOffset((uint32_t)k), f.nEvents * sizeof(double),
+				                        vars.as<double>() + (size_t)v * total + at, s));
+				at += f.nEvents;
+			}
+			cols[v] = vars.as<double>() + (size_t)v * total;
+		}
+		PWA_TRY(pwa_likelihood_set_otf_binning(L, nBinVars, lower, upper, cols.data(), total, PWA_MEMORY_DEVICE));
+	}
+	DevBuf row;
+	PWA_TRY(row.alloc(total * sizeof(float2), "amplitude row"));
+	for (const auto& w : waves) {
+		uint64_t at = 0;
+		for (const auto& f : files) {
+			const int k = find(f.waves, w);
+			PWA_TRY(ampFileToDevice(f, f.waveOffset((uint32_t)k), f.nEvents * sizeof(float2), row.as<float2>() + at, s));
+			at += f.nEvents;
+		}
+		PWA_TRY(pwa_likelihood_add_amplitude(L, w.c_str(), row.p, total, PWA_COMPLEX64, PWA_MEMORY_DEVICE));
+	}
+	return kOk;
+}
+
+int pwa_likelihood_otf_selected(const pwa_likelihood* L, uint64_t* nSelected)
+{
+	if (!L || !nSelected)
+		return setError(kErrArg, "null argument");
+	*nSelected = L->otfSet ? L->otfSelected : 0;
+	return kOk;
+}
+
 int pwa_likelihood_set_shard(pwa_likelihood* L, uint64_t totalEvents, int root)
 {
 	if (!L)
@@ -1230,6 +1377,29 @@ int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const 
 		return setError(kErrArg, "no events to load");
 	PWA_TRY(ensureDevice(L));
 	cudaStream_t s = L->stream;
+	// on-the-fly binning: keep the selected events of the file, in order
+	DevBuf otfFull, otfSel;
+	if (L->otfSet) {
+		if (n != L->otfFileEvents)
+			return setError(kErrArg, "amplitude array length differs from the event count of the on-the-fly binning");
+		if (L->otfSelected == 0)
+			return setError(kErrArg, "no event of the data file is in the on-the-fly bin");
+		const int elem = (ampType == PWA_COMPLEX128) ? 16 : 8;
+		const void* src = amps;
+		if (memory == PWA_MEMORY_HOST) {
+			PWA_TRY(otfFull.alloc(n * elem, "amplitude upload"));
+			PWA_TRY(cudaCheck(cudaMemcpyAsync(otfFull.p, amps, n * elem, cudaMemcpyHostToDevice, s), "upload"));
+			src = otfFull.p;
+		} else {
+			PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device amplitudes"));
+		}
+		PWA_TRY(otfSel.alloc(L->otfSelected * elem, "selected amplitudes"));
+		PWA_TRY(launchOtfGather(src, L->otfIdx.as<unsigned long long>(), L->otfSelected, elem, otfSel.p, s));
+		PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "OTF gather"));
+		amps = otfSel.p;
+		memory = PWA_MEMORY_DEVICE;
+		n = L->otfSelected;
+	}
 	if (L->nEvents == 0) {
 		L->nEvents = n;
 		L->storeB = (uint32_t)chooseStoreBlock((int)L->W(), (int)L->rank, L->maxSmem);

@@ -264,4 +264,43 @@ int launchAdam(float* w, const float* g, float* m, float* v, uint16_t* w16, size
 int launchToBf16(const float* x, uint16_t* y, size_t n, cudaStream_t s);
 int launchGatherRows(const void* src, const uint32_t* idx, int rows, size_t rowBytes, void* dst, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// On-the-fly event binning (otf_kernels.cu)
+// ---------------------------------------------------------------------------
+constexpr int kOtfMaxVars = 8;
+constexpr int kOtfChunk = 4096;  // events per block of the selection kernels
+struct OtfArgs {
+	int nVars;
+	double lower[kOtfMaxVars], upper[kOtfMaxVars];
+	const double* vars;  // device, [nVars][n]
+	uint64_t n;
+};
+int launchOtfCount(const OtfArgs& a, unsigned* counts, cudaStream_t s);
+int launchOtfCompact(const OtfArgs& a, const unsigned long long* offsets, unsigned long long* idx, cudaStream_t s);
+int launchOtfGather(const void* src, const unsigned long long* idx, uint64_t n, int elemBytes, void* dst,
+                    cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Raw amplitude files (ampfile.cpp)
+// ---------------------------------------------------------------------------
+struct AmpFile {
+	std::string path;
+	int fd = -1;
+	uint32_t nWaves = 0, nVars = 0;
+	uint64_t nEvents = 0, dataOffset = 0;
+	std::vector<std::string> waves, vars;
+	AmpFile() = default;
+	AmpFile(const AmpFile&) = delete;
+	AmpFile& operator=(const AmpFile&) = delete;
+	AmpFile(AmpFile&& o) noexcept { *this = std::move(o); }
+	AmpFile& operator=(AmpFile&& o) noexcept;
+	~AmpFile();
+	uint64_t waveOffset(uint32_t w) const { return dataOffset + (uint64_t)w * nEvents * 8; }
+	uint64_t varOffset(uint32_t v) const { return dataOffset + ((uint64_t)nWaves + v) * nEvents * 8; }
+};
+// opens and validates an amplitude file (header, name table, file size)
+int ampFileOpen(const char* path, AmpFile& f);
+// file bytes [offset, offset + bytes) -> device memory (synchronises s)
+int ampFileToDevice(const AmpFile& f, uint64_t offset, uint64_t bytes, void* dst, cudaStream_t s);
+
 }  // namespace pwa

@@ -219,6 +219,60 @@ class pwaLikelihood:
     def setPriorType(self, prior):
         N.call("pwa_likelihood_set_prior_type", self._h, int(prior))
 
+    def setOnTheFlyBinning(self, boundaries, binVars):
+        """setOnTheFlyBinning (pwaLikelihood.cc:1391-1440).  boundaries:
+        {name: (lower, upper)}; binVars: {name: per-event values of the data
+        file} (numpy or CUDA arrays, all of the file's length).  Events with
+        lower <= x < upper for every variable are kept, in file order;
+        addAmplitude then takes whole-file amplitude arrays."""
+        names = list(boundaries)
+        lo = np.array([boundaries[k][0] for k in names], dtype=np.float64)
+        hi = np.array([boundaries[k][1] for k in names], dtype=np.float64)
+        keep, ptrs, n, mem = [], [], None, None
+        for k in names:
+            v = binVars[k]
+            cai = getattr(v, "__cuda_array_interface__", None)
+            if cai is not None:
+                if not cai["typestr"].endswith("f8"):
+                    raise TypeError("device binning variables must be float64")
+                if cai.get("strides") not in (None, (8,)):
+                    raise ValueError("device binning variables must be contiguous")
+                ptrs.append(cai["data"][0])
+                m, size = N.MEMORY_DEVICE, int(np.prod(cai["shape"]))
+            else:
+                a = np.ascontiguousarray(v, dtype=np.float64)
+                keep.append(a)
+                ptrs.append(a.ctypes.data)
+                m, size = N.MEMORY_HOST, a.size
+            if n is None:
+                n, mem = size, m
+            elif size != n or m != mem:
+                raise ValueError("binning variables must have one length and one residence")
+        arr = (C.c_void_p * max(1, len(ptrs)))(*ptrs)
+        N.call("pwa_likelihood_set_otf_binning", self._h, len(names), _pd(lo), _pd(hi), arr, int(n), mem)
+
+    def loadAmplitudeFiles(self, paths, boundaries=None):
+        """addAmplitude for every wave of the wave list from raw amplitude
+        files (rootpwa_gb300.ampfile), their events concatenated in the
+        order given, with on-the-fly binning {variable: (lower, upper)} on
+        the files' binning variables when boundaries are given."""
+        if isinstance(paths, (str, bytes)) or hasattr(paths, "__fspath__"):
+            paths = [paths]
+        ps = [str(p).encode() for p in paths]
+        boundaries = boundaries or {}
+        names = list(boundaries)
+        lo = np.array([boundaries[k][0] for k in names] or [0.0], dtype=np.float64)
+        hi = np.array([boundaries[k][1] for k in names] or [0.0], dtype=np.float64)
+        pa = (C.c_char_p * len(ps))(*ps)
+        na = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        N.call("pwa_likelihood_load_amp_files", self._h, len(ps), pa, len(names), na, _pd(lo), _pd(hi))
+        return True
+
+    def otfSelected(self):
+        n = C.c_uint64()
+        N.call("pwa_likelihood_otf_selected", self._h, C.byref(n))
+        return n.value
+
     def setShard(self, totalEvents, root):
         """Event-sharded evaluation: this likelihood holds one share of the
         events; only the root shard adds the normalisation and prior terms
