@@ -187,6 +187,11 @@ int pwa_likelihood_set_autotune(pwa_likelihood* L, int enable);
 int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, int* blocks);
 /* selects the pipeline depth by hand after finishInit (2..4 as shared memory allows) */
 int pwa_likelihood_set_plan(pwa_likelihood* L, int stages);
+/* kernel variant of the coherent-sum phase: 1 or 2 events per lane (two
+ * events share each V load and use packed FP32x2 FMAs); 0 keeps the current
+ * one.  The autotuner times both. */
+int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events);
+int pwa_likelihood_plan_variant(const pwa_likelihood* L, int* phase1Events);
 /*
  * init (pwaLikelihood.cc:1050-1063 with readWaveList :1443-1484 and
  * buildParDataStruct :1487-1556).  The reference takes wave descriptions and

@@ -108,6 +108,8 @@ SIGNATURES = {
     "pwa_likelihood_set_autotune": (i, [vp, i]),
     "pwa_likelihood_plan": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
     "pwa_likelihood_set_plan": (i, [vp, i]),
+    "pwa_likelihood_set_plan_variant": (i, [vp, i, i]),
+    "pwa_likelihood_plan_variant": (i, [vp, C.POINTER(C.c_int)]),
     "pwa_likelihood_init": (i, [vp, u32, C.POINTER(cc), C.POINTER(i32), pd, u32, C.c_double]),
     "pwa_likelihood_add_norm_integral": (i, [vp, vp]),
     "pwa_likelihood_add_acc_integral": (i, [vp, vp, u64]),

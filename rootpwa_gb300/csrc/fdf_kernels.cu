@@ -282,7 +282,7 @@ __device__ __forceinline__ void fdfTail(const FdfArgs& a, unsigned* sLast, doubl
 	}
 }
 
-template <int R, int E, int WPW>
+template <int R, int E, int WPW, int NE>
 __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, const int stages)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -359,6 +359,18 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	const int wBase = wRefl == 0 ? warp * wn : W0 + (warp - nNegWarps) * wp;
 	const int wEnd = wRefl == 0 ? min(W0, wBase + wn) : min(W, wBase + wp);
 	const int nWarpWaves = max(0, wEnd - wBase);
+	// tile-invariant phase-2 addresses: byte offset of this lane's first event
+	// pair in row wBase + wi of a stage (the second pair, 64 events on, is at
+	// offset ^ 512: adding 64 modulo 128 flips one bit of the position), and
+	// of its first pair in the T buffers
+	static_assert(EPAIRS == 1 || (EPAIRS == 2 && E == 128), "phase-2 event pairs");
+	uint32_t aOff[WPW];
+#pragma unroll
+	for (int wi = 0; wi < WPW; ++wi) {
+		const int w = min(wBase + wi, W - 1);
+		aOff[wi] = (uint32_t)(w * E + ((2 * lane + (int)storeRot((uint32_t)w, (uint32_t)E)) & (E - 1))) * 8u;
+	}
+	const uint32_t tOff = (uint32_t)(wRefl * E + 2 * lane) * 8u;
 
 	double accLL = 0., accC = 0.;
 	float kLL = 0.f, kLLc = 0.f, kC = 0.f, kCc = 0.f;
@@ -383,26 +395,26 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 
 	bool failed = false;
 	uint64_t k = 0;
-	for (; k < myTiles; ++k) {
-		const int s = (int)(k % (uint64_t)stages);
-		const uint32_t parity = (uint32_t)((k / (uint64_t)stages) & 1ull);
+	// stage, phase parity and first event of tile k, advanced incrementally
+	// (no division by the runtime stage count inside the loop)
+	int s = 0;
+	uint32_t parity = 0;
+	uint64_t e0 = first * (uint64_t)E;
+	for (; k < myTiles; ++k, e0 += stride * (uint64_t)E) {
+		if (k != 0 && ++s == stages) {
+			s = 0;
+			parity ^= 1u;
+		}
 		const bool timedOut = !mbarWaitBounded(&bars[s], parity);
 		const float2* tile = tiles + (size_t)s * W * E;
-		const uint64_t e0 = (first + k * stride) * (uint64_t)E;
 		float2* T = Ts + (size_t)(k & 1ull) * R * 2 * E;
 		float2* Tw = Tsw + (size_t)(k & 1ull) * R * 2 * E;
 
-		// ---- phase 1: coherent sums, combined across the H lanes of an event ----
+		// ---- phase 1: coherent sums, combined across the lanes of an event ----
 		{
-			float2 Sa[R][2];
-#pragma unroll
-			for (int r = 0; r < R; ++r) {
-				Sa[r][0] = make_float2(0.f, 0.f);
-				Sa[r][1] = make_float2(0.f, 0.f);
-			}
-			// every row this lane reads has the same rotation (w = ph mod H)
-			const int rot1 = (int)storeRot((uint32_t)ph, (uint32_t)E);  // 512 / E == H
-			const uint32_t colAddr = smemAddr(tile + ((pe + rot1) & (E - 1)));
+			float2 S[R][2];
+			int pe1;       // the event whose sums this lane holds after the combination
+			bool writer;   // one lane per event writes its results
 			const uint32_t vAddr = smemAddr(Vs);
 			const uint32_t rowB = (uint32_t)lay.rowStride;
 			// V of two consecutive ranks in one 128-bit load; the address
@@ -421,45 +433,135 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 						v[r] = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
 				}
 			};
-#pragma unroll 4
-			for (int w = ph; w < W0; w += H) {
-				const float2 av = lds64(colAddr + (uint32_t)w * rowB);
-				float2 v[R];
-				loadV(w, v);
+			if constexpr (NE == 1) {
+				float2 Sa[R][2];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					Sa[r][0].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sa[r][0].x));
-					Sa[r][0].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sa[r][0].y));
+					Sa[r][0] = make_float2(0.f, 0.f);
+					Sa[r][1] = make_float2(0.f, 0.f);
 				}
-			}
+				// every row this lane reads has the same rotation (w = ph mod H)
+				const int rot1 = (int)storeRot((uint32_t)ph, (uint32_t)E);  // 512 / E == H
+				const uint32_t colAddr = smemAddr(tile + ((pe + rot1) & (E - 1)));
 #pragma unroll 4
-			for (int w = wStart1; w < W; w += H) {
-				const float2 av = lds64(colAddr + (uint32_t)w * rowB);
-				float2 v[R];
-				loadV(w, v);
+				for (int w = ph; w < W0; w += H) {
+					const float2 av = lds64(colAddr + (uint32_t)w * rowB);
+					float2 v[R];
+					loadV(w, v);
 #pragma unroll
-				for (int r = 0; r < R; ++r) {
-					Sa[r][1].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sa[r][1].x));
-					Sa[r][1].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sa[r][1].y));
+					for (int r = 0; r < R; ++r) {
+						Sa[r][0].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sa[r][0].x));
+						Sa[r][0].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sa[r][0].y));
+					}
 				}
+#pragma unroll 4
+				for (int w = wStart1; w < W; w += H) {
+					const float2 av = lds64(colAddr + (uint32_t)w * rowB);
+					float2 v[R];
+					loadV(w, v);
+#pragma unroll
+					for (int r = 0; r < R; ++r) {
+						Sa[r][1].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sa[r][1].x));
+						Sa[r][1].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sa[r][1].y));
+					}
+				}
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+#pragma unroll
+					for (int e = 0; e < 2; ++e) {
+						S[r][e] = Sa[r][e];
+#pragma unroll
+						for (int o = 1; o < H; o <<= 1) {
+							S[r][e].x += __shfl_xor_sync(0xffffffffu, S[r][e].x, o);
+							S[r][e].y += __shfl_xor_sync(0xffffffffu, S[r][e].y, o);
+						}
+					}
+				pe1 = pe;
+				writer = ph == 0;
+			} else {
+				// two consecutive events per lane: one 128-bit load brings a
+				// wave's amplitudes of both, and each V load serves both.
+				// Quarter-warp q holds PQ adjacent event pairs x QPH wave
+				// slices with distinct rotations, so its eight 16-byte loads
+				// cover all 32 banks once.
+				constexpr int PPW = EPW / 2;  // event pairs per warp
+				constexpr int H2 = 32 / PPW;  // lanes (wave slices) per pair
+				constexpr int PQ = E / 64;    // pairs per quarter-warp
+				constexpr int QPH = 8 / PQ;   // wave slices per quarter-warp
+				static_assert(PQ * QPH == 8 && 2 * PQ == PPW && 2 * QPH == H2, "two-event phase-1 shape");
+				const int phLo = lane & (QPH - 1);
+				const int pm2 = ((lane >> 3) & 1) * PQ + ((lane / QPH) & (PQ - 1));
+				const int ph2 = phLo + QPH * (lane >> 4);
+				const int pe0 = warp * EPW + 2 * pm2;
+				// H2 is a multiple of 512 / E: one rotation for all rows of the slice
+				const int rot1 = (int)storeRot((uint32_t)ph2, (uint32_t)E);
+				const uint32_t colAddr = smemAddr(tile + ((pe0 + rot1) & (E - 1)));
+				// P = sum (ax vx, ay vy), Q = sum (ay vx, ax vy) per (rank,
+				// event), one set per reflectivity: Re S = P.x - P.y,
+				// Im S = Q.x + Q.y
+				auto mac = [&](int w, float2 (&P)[R][2], float2 (&Q)[R][2]) {
+					const float4 av = lds128(colAddr + (uint32_t)w * rowB);
+					float2 v[R];
+					loadV(w, v);
+					const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
+					const float2 s0 = make_float2(av.y, av.x), s1 = make_float2(av.w, av.z);
+#pragma unroll
+					for (int r = 0; r < R; ++r) {
+						P[r][0] = ffma2(a0, v[r], P[r][0]);
+						Q[r][0] = ffma2(s0, v[r], Q[r][0]);
+						P[r][1] = ffma2(a1, v[r], P[r][1]);
+						Q[r][1] = ffma2(s1, v[r], Q[r][1]);
+					}
+				};
+				float2 P0[R][2], Q0[R][2], P1[R][2], Q1[R][2];
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+#pragma unroll
+					for (int j = 0; j < 2; ++j) {
+						P0[r][j] = Q0[r][j] = P1[r][j] = Q1[r][j] = make_float2(0.f, 0.f);
+					}
+#pragma unroll 2
+				for (int w = ph2; w < W0; w += H2)
+					mac(w, P0, Q0);
+				const int wS1 = W0 + (((ph2 - W0) % H2) + H2) % H2;
+#pragma unroll 4
+				for (int w = wS1; w < W; w += H2)
+					mac(w, P1, Q1);
+				// both events' sums, then a reduce-scatter over the slice bit 16
+				// (lanes with that bit keep the second event) and a
+				// butterfly over the remaining slice bits
+				const int mine = (lane >> 4) & 1;
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+#pragma unroll
+					for (int e = 0; e < 2; ++e) {
+						const float2 (&P)[R][2] = e ? P1 : P0;
+						const float2 (&Q)[R][2] = e ? Q1 : Q0;
+						const float2 sA = make_float2(P[r][0].x - P[r][0].y, Q[r][0].x + Q[r][0].y);
+						const float2 sB = make_float2(P[r][1].x - P[r][1].y, Q[r][1].x + Q[r][1].y);
+						float2 keep = mine ? sB : sA;
+						const float2 send = mine ? sA : sB;
+						keep.x += __shfl_xor_sync(0xffffffffu, send.x, 16);
+						keep.y += __shfl_xor_sync(0xffffffffu, send.y, 16);
+#pragma unroll
+						for (int o = 1; o < QPH; o <<= 1) {
+							keep.x += __shfl_xor_sync(0xffffffffu, keep.x, o);
+							keep.y += __shfl_xor_sync(0xffffffffu, keep.y, o);
+						}
+						S[r][e] = keep;
+					}
+				pe1 = pe0 + mine;
+				writer = phLo == 0;
 			}
-			float2 S[R][2];
 			float L = flat2;
 #pragma unroll
 			for (int r = 0; r < R; ++r)
 #pragma unroll
-				for (int e = 0; e < 2; ++e) {
-					S[r][e] = Sa[r][e];
-#pragma unroll
-					for (int o = 1; o < H; o <<= 1) {
-						S[r][e].x += __shfl_xor_sync(0xffffffffu, S[r][e].x, o);
-						S[r][e].y += __shfl_xor_sync(0xffffffffu, S[r][e].y, o);
-					}
+				for (int e = 0; e < 2; ++e)
 					L = fmaf(S[r][e].x, S[r][e].x, fmaf(S[r][e].y, S[r][e].y, L));
-				}
-			const bool valid = (e0 + (uint64_t)pe) < a.nEvents;
+			const bool valid = (e0 + (uint64_t)pe1) < a.nEvents;
 			const float c = valid ? -2.f / L : 0.f;
-			if (ph == 0) {
+			if (writer) {
 				if (valid)
 					llPart += -logf(L);
 				cPart += c;
@@ -469,8 +571,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 #pragma unroll
 						for (int e = 0; e < 2; ++e) {
 							const float tx = c * S[r][e].x, ty = c * S[r][e].y;
-							T[(r * 2 + e) * E + pe] = make_float2(tx, ty);
-							Tw[(r * 2 + e) * E + pe] = make_float2(ty, tx);
+							T[(r * 2 + e) * E + pe1] = make_float2(tx, ty);
+							Tw[(r * 2 + e) * E + pe1] = make_float2(ty, tx);
 						}
 				}
 			}
@@ -483,22 +585,20 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 
 		// ---- phase 2: gradient contraction over the tile, one reflectivity per warp ----
 		if (a.withGrad) {
+			const uint32_t tAddr = smemAddr(tile);
+			const uint32_t tBase = smemAddr(T) + tOff, twBase = smemAddr(Tw) + tOff;
 #pragma unroll
 			for (int pp = 0; pp < EPAIRS; ++pp) {
-				const int ev = 2 * lane + 64 * pp;
 				float4 t[R], tw[R];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					t[r] = lds128(smemAddr(&T[(r * 2 + wRefl) * E + ev]));
-					tw[r] = lds128(smemAddr(&Tw[(r * 2 + wRefl) * E + ev]));
+					t[r] = lds128(tBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u);
+					tw[r] = lds128(twBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u);
 				}
-				const uint32_t tAddr = smemAddr(tile);
 #pragma unroll
 				for (int wi = 0; wi < WPW; ++wi) {
 					if (wi < nWarpWaves) {
-						const int w = wBase + wi;
-						const int pos = (ev + (int)storeRot((uint32_t)w, (uint32_t)E)) & (E - 1);
-						const float4 av = lds128(tAddr + (uint32_t)(w * E + pos) * 8u);
+						const float4 av = lds128(tAddr + (aOff[wi] ^ (uint32_t)(pp * 512)));
 						const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
 #pragma unroll
 						for (int r = 0; r < R; ++r) {
@@ -650,10 +750,10 @@ __global__ void convertPlainKernel(const double2* src, float2* dst, uint64_t n)
 	}
 }
 
-template <int R, int E, int WPW>
+template <int R, int E, int WPW, int NE>
 int launchVariant(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {
-	auto kern = fdfMainKernel<R, E, WPW>;
+	auto kern = fdfMainKernel<R, E, WPW, NE>;
 	// raise the dynamic shared-memory limit once per variant (not a stream
 	// operation, so it is kept out of the launches captured into graphs)
 	static size_t configured = 0;
@@ -678,28 +778,34 @@ int launchVariant(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 	return cudaCheck(e, "fdf kernel launch");
 }
 
-template <int R>
-int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
+template <int R, int NE>
+int launchRN(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {
 	if (p.E == 128) {
 		switch (p.wpw) {
-		case 2: return launchVariant<R, 128, 2>(p, a, s);
-		case 4: return launchVariant<R, 128, 4>(p, a, s);
-		case 6: return launchVariant<R, 128, 6>(p, a, s);
-		case 8: return launchVariant<R, 128, 8>(p, a, s);
+		case 2: return launchVariant<R, 128, 2, NE>(p, a, s);
+		case 4: return launchVariant<R, 128, 4, NE>(p, a, s);
+		case 6: return launchVariant<R, 128, 6, NE>(p, a, s);
+		case 8: return launchVariant<R, 128, 8, NE>(p, a, s);
 		default: break;
 		}
 	} else if (p.E == 64) {
 		switch (p.wpw) {
-		case 2: return launchVariant<R, 64, 2>(p, a, s);
-		case 4: return launchVariant<R, 64, 4>(p, a, s);
-		case 6: return launchVariant<R, 64, 6>(p, a, s);
-		case 8: return launchVariant<R, 64, 8>(p, a, s);
-		case 14: return launchVariant<R, 64, 14>(p, a, s);
+		case 2: return launchVariant<R, 64, 2, NE>(p, a, s);
+		case 4: return launchVariant<R, 64, 4, NE>(p, a, s);
+		case 6: return launchVariant<R, 64, 6, NE>(p, a, s);
+		case 8: return launchVariant<R, 64, 8, NE>(p, a, s);
+		case 14: return launchVariant<R, 64, 14, NE>(p, a, s);
 		default: break;
 		}
 	}
 	return setError(kErrUnsupported, "no FdF kernel variant for this tile/wave bucket");
+}
+
+template <int R>
+int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
+{
+	return p.phase1Events == 2 ? launchRN<R, 2>(p, a, s) : launchRN<R, 1>(p, a, s);
 }
 
 }  // namespace
@@ -740,13 +846,17 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 		const uint64_t nTiles = (nEvents + B - 1) / B;
 		p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
 		p.smemBytes = smemLayout(W, R, B, st).total;
-		out->push_back(p);
+		// one event per lane first (the default without autotuning), then two
+		for (int ne : {1, 2}) {
+			p.phase1Events = ne;
+			out->push_back(p);
+		}
 	}
 	if (out->empty())
 		return setError(kErrUnsupported, "amplitude tile does not fit in shared memory");
 	// a single stage does not overlap copy and compute: drop it when deeper pipelines fit
-	if (out->size() > 1)
-		out->erase(out->begin());
+	if (out->size() > 2)
+		out->erase(out->begin(), out->begin() + 2);
 	return kOk;
 }
 

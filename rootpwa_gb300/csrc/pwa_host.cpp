@@ -919,7 +919,7 @@ struct TuneKey {
 		return std::tie(W, W0, R, evClass) < std::tie(o.W, o.W0, o.R, o.evClass);
 	}
 };
-std::map<TuneKey, int> g_tuned;  // -> pipeline stages
+std::map<TuneKey, std::pair<int, int> > g_tuned;  // -> (pipeline stages, phase-1 events per lane)
 
 // Times every candidate (tile size, pipeline depth) on the handle's own data
 // with a fixed parameter point and keeps the fastest.
@@ -932,7 +932,7 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 	auto it = g_tuned.find(key);
 	if (it != g_tuned.end()) {
 		for (const auto& c : cands)
-			if (c.stages == it->second)
+			if (c.stages == it->second.first && c.phase1Events == it->second.second)
 				L->plan = c;
 		return kOk;
 	}
@@ -959,7 +959,7 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 		}
 	}
 	L->plan = bestPlan;
-	g_tuned[key] = bestPlan.stages;
+	g_tuned[key] = std::make_pair(bestPlan.stages, bestPlan.phase1Events);
 	// the tuning runs leave no device error behind
 	unsigned err = 0;
 	PWA_TRY(cudaCheck(cudaMemcpy(&err, L->dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "error flag"));
@@ -1211,16 +1211,32 @@ int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, i
 
 int pwa_likelihood_set_plan(pwa_likelihood* L, int stages)
 {
+	return pwa_likelihood_set_plan_variant(L, stages, 0);
+}
+
+int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events)
+{
 	PWA_TRY(checkFinished(L));
+	if (phase1Events != 0 && phase1Events != 1 && phase1Events != 2)
+		return setError(kErrArg, "phase-1 events per lane must be 1 or 2 (0: keep)");
+	const int ne = phase1Events ? phase1Events : L->plan.phase1Events;
 	std::vector<FdfPlan> cands;
 	PWA_TRY(planCandidates((int)L->nW[0], (int)L->W(), (int)L->rank, (int)L->storeB, L->nEvents, L->numSMs, L->maxSmem,
 	                       &cands));
 	for (const auto& c : cands)
-		if (c.stages == stages) {
+		if (c.stages == stages && c.phase1Events == ne) {
 			L->plan = c;
 			return kOk;
 		}
 	return setError(kErrUnsupported, "no compiled FdF plan with this pipeline depth");
+}
+
+int pwa_likelihood_plan_variant(const pwa_likelihood* L, int* phase1Events)
+{
+	PWA_TRY(checkFinished(L));
+	if (phase1Events)
+		*phase1Events = L->plan.phase1Events;
+	return kOk;
 }
 
 int pwa_likelihood_set_reduction(pwa_likelihood* L, int r)

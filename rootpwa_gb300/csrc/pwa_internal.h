@@ -71,6 +71,7 @@ struct FdfPlan {
 	int E = 128;        // events per tile (= store block)
 	int stages = 2;     // shared-memory pipeline depth
 	int wpw = 2;        // wave bucket per warp (template)
+	int phase1Events = 2;  // events per lane in the coherent-sum phase (1 or 2)
 	int blocks = 0;     // grid size (persistent, <= #SMs)
 	size_t smemBytes = 0;
 };

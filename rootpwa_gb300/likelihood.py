@@ -306,9 +306,16 @@ class pwaLikelihood:
         N.call("pwa_likelihood_plan", self._h, C.byref(e), C.byref(s), C.byref(b))
         return e.value, s.value, b.value
 
-    def setPlan(self, stages):
-        """Select the FdF kernel pipeline depth by hand (after finishInit)."""
-        N.call("pwa_likelihood_set_plan", self._h, int(stages))
+    def setPlan(self, stages, phase1Events=0):
+        """Select the FdF kernel pipeline depth and coherent-sum variant (1 or
+        2 events per lane; 0 keeps the current one) by hand (after finishInit)."""
+        N.call("pwa_likelihood_set_plan_variant", self._h, int(stages), int(phase1Events))
+
+    def planVariant(self):
+        """Events per lane of the FdF kernel's coherent-sum phase (1 or 2)."""
+        v = C.c_int()
+        N.call("pwa_likelihood_plan_variant", self._h, C.byref(v))
+        return v.value
 
     # -- setup (order as _likelihood.py:17-71) -------------------------------
     def init(self, waveNames, reflectivities, thresholds=None, rank=1, massBinCenter=0.0):

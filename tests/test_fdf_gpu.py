@@ -100,11 +100,16 @@ def test_shapes_against_oracle(n_neg, n_pos, rank, n_data):
     # comparison measures the kernels and not the conditioning (see below)
     w = stress_workload(n_neg, n_pos, rank, n_data, flat=1.0)
     O, G = pair(w)
-    check_point(O, G, w["par"])
-    # a second point on the same handle (no stale state)
-    q = 0.5 * w["par"][::-1].copy()
-    q[-1] = -0.8
-    check_point(O, G, q)
+    stages = G.plan()[1]
+    # both coherent-sum variants (one and two events per lane)
+    for ne in (1, 2):
+        G.setPlan(stages, ne)
+        assert G.planVariant() == ne
+        check_point(O, G, w["par"])
+        # a second point on the same handle (no stale state)
+        q = 0.5 * w["par"][::-1].copy()
+        q[-1] = -0.8
+        check_point(O, G, q)
 
 
 def test_ill_conditioned_point():
