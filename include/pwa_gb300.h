@@ -188,8 +188,8 @@ int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, i
 /* selects the pipeline depth by hand after finishInit (2..4 as shared memory allows) */
 int pwa_likelihood_set_plan(pwa_likelihood* L, int stages);
 /* kernel variant of the coherent-sum phase: 1 or 2 events per lane (two
- * events share each V load and use packed FP32x2 FMAs); 0 keeps the current
- * one.  The autotuner times both. */
+ * adjacent events share each V load and one 128-bit amplitude load); 0
+ * keeps the current one.  The autotuner times both. */
 int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events);
 int pwa_likelihood_plan_variant(const pwa_likelihood* L, int* phase1Events);
 /*

@@ -21,7 +21,9 @@
 //   * phase 1: each warp owns E/16 events of the tile, 32/(E/16) lanes per
 //     event sum interleaved slices of the waves and combine them with warp
 //     shuffles, giving L_i, c_i and T_{r,e,i} = c_i S (double-buffered, so
-//     one block barrier per tile suffices);
+//     one block barrier per tile suffices).  Variant NE = 2 gives each lane
+//     two adjacent events (one 128-bit amplitude load and one V load per
+//     wave serve both; 17 % fewer shared-memory wavefronts per tile);
 //   * phase 2: warp j owns a contiguous range of waves of one reflectivity,
 //     each lane a fixed set of event pairs; the lane sums conj(A) T over its
 //     events with packed FP32x2 FMA for kFold tiles, then a warp
@@ -496,51 +498,44 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				// H2 is a multiple of 512 / E: one rotation for all rows of the slice
 				const int rot1 = (int)storeRot((uint32_t)ph2, (uint32_t)E);
 				const uint32_t colAddr = smemAddr(tile + ((pe0 + rot1) & (E - 1)));
-				// P = sum (ax vx, ay vy), Q = sum (ay vx, ax vy) per (rank,
-				// event), one set per reflectivity: Re S = P.x - P.y,
-				// Im S = Q.x + Q.y
-				auto mac = [&](int w, float2 (&P)[R][2], float2 (&Q)[R][2]) {
+				// coherent sums of both events, FP32 FMA chains as in the
+				// one-event variant: S[r][ev] per reflectivity
+				auto mac = [&](int w, float2 (&Sx)[R][2]) {
 					const float4 av = lds128(colAddr + (uint32_t)w * rowB);
 					float2 v[R];
 					loadV(w, v);
-					const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
-					const float2 s0 = make_float2(av.y, av.x), s1 = make_float2(av.w, av.z);
 #pragma unroll
 					for (int r = 0; r < R; ++r) {
-						P[r][0] = ffma2(a0, v[r], P[r][0]);
-						Q[r][0] = ffma2(s0, v[r], Q[r][0]);
-						P[r][1] = ffma2(a1, v[r], P[r][1]);
-						Q[r][1] = ffma2(s1, v[r], Q[r][1]);
+						Sx[r][0].x = fmaf(v[r].x, av.x, fmaf(-v[r].y, av.y, Sx[r][0].x));
+						Sx[r][0].y = fmaf(v[r].x, av.y, fmaf(v[r].y, av.x, Sx[r][0].y));
+						Sx[r][1].x = fmaf(v[r].x, av.z, fmaf(-v[r].y, av.w, Sx[r][1].x));
+						Sx[r][1].y = fmaf(v[r].x, av.w, fmaf(v[r].y, av.z, Sx[r][1].y));
 					}
 				};
-				float2 P0[R][2], Q0[R][2], P1[R][2], Q1[R][2];
+				float2 S0[R][2], S1[R][2];
 #pragma unroll
 				for (int r = 0; r < R; ++r)
 #pragma unroll
-					for (int j = 0; j < 2; ++j) {
-						P0[r][j] = Q0[r][j] = P1[r][j] = Q1[r][j] = make_float2(0.f, 0.f);
-					}
+					for (int j = 0; j < 2; ++j)
+						S0[r][j] = S1[r][j] = make_float2(0.f, 0.f);
 #pragma unroll 2
 				for (int w = ph2; w < W0; w += H2)
-					mac(w, P0, Q0);
+					mac(w, S0);
 				const int wS1 = W0 + (((ph2 - W0) % H2) + H2) % H2;
 #pragma unroll 4
 				for (int w = wS1; w < W; w += H2)
-					mac(w, P1, Q1);
-				// both events' sums, then a reduce-scatter over the slice bit 16
-				// (lanes with that bit keep the second event) and a
-				// butterfly over the remaining slice bits
+					mac(w, S1);
+				// a reduce-scatter over the slice bit 16 (lanes with that bit
+				// keep the second event) and a butterfly over the remaining
+				// slice bits
 				const int mine = (lane >> 4) & 1;
 #pragma unroll
 				for (int r = 0; r < R; ++r)
 #pragma unroll
 					for (int e = 0; e < 2; ++e) {
-						const float2 (&P)[R][2] = e ? P1 : P0;
-						const float2 (&Q)[R][2] = e ? Q1 : Q0;
-						const float2 sA = make_float2(P[r][0].x - P[r][0].y, Q[r][0].x + Q[r][0].y);
-						const float2 sB = make_float2(P[r][1].x - P[r][1].y, Q[r][1].x + Q[r][1].y);
-						float2 keep = mine ? sB : sA;
-						const float2 send = mine ? sA : sB;
+						const float2 (&Se)[R][2] = e ? S1 : S0;
+						float2 keep = mine ? Se[r][1] : Se[r][0];
+						const float2 send = mine ? Se[r][0] : Se[r][1];
 						keep.x += __shfl_xor_sync(0xffffffffu, send.x, 16);
 						keep.y += __shfl_xor_sync(0xffffffffu, send.y, 16);
 #pragma unroll
@@ -846,8 +841,10 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 		const uint64_t nTiles = (nEvents + B - 1) / B;
 		p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
 		p.smemBytes = smemLayout(W, R, B, st).total;
-		// one event per lane first (the default without autotuning), then two
-		for (int ne : {1, 2}) {
+		// the default without autotuning first: two events per lane up to
+		// rank 2, one beyond (where two would spill registers)
+		const int order[2] = {R <= 2 ? 2 : 1, R <= 2 ? 1 : 2};
+		for (int ne : order) {
 			p.phase1Events = ne;
 			out->push_back(p);
 		}
