@@ -395,7 +395,8 @@ def run_gb300(args):
                            "mc_events": args.n_mc, "reduction": args.reduction,
                            "l2": "inputs (%.0f MB) larger than L2 (129 MB); no flush" % (alg_bytes / 1e6),
                            "entry": "pwa_likelihood_fdf_device (parameters and results in HBM)",
-                           "plan": dict(zip(("tile_events", "stages", "blocks"), L.plan()))},
+                           "plan": dict(zip(("tile_events", "stages", "blocks"), L.plan()),
+                                        phase1_events_per_lane=L.planVariant())},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": P * 8,
                         "d2h_bytes_per_step": (P + 2) * 8, "entry": "pwa_likelihood_fdf (host buffers)"},
                 "gpu_launches": int(launches), "launches_per_step": launches / args.steps,
