@@ -398,7 +398,9 @@ def run_gb300(args):
                            "plan": dict(zip(("tile_events", "stages", "blocks"), L.plan()),
                                         phase1_events_per_lane=L.planVariant())},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": P * 8,
-                        "d2h_bytes_per_step": (P + 2) * 8, "entry": "pwa_likelihood_fdf (host buffers)"},
+                        "d2h_bytes_per_step": (P + 2) * 8,
+                        "entry": "pwa_likelihood_fdf (host buffers, staged through mapped pinned memory that "
+                                 "the kernel reads and writes directly)"},
                 "gpu_launches": int(launches), "launches_per_step": launches / args.steps,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "extra": {"integral_norm_s": integral_s, "integral_precision": args.integral_precision,

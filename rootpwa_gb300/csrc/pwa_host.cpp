@@ -100,17 +100,25 @@ struct PinnedBuf {
 	PinnedBuf(const PinnedBuf&) = delete;
 	PinnedBuf& operator=(const PinnedBuf&) = delete;
 	~PinnedBuf() { release(); }
-	int ensure(size_t b, const char* what)
+	void* dev = nullptr;  // device view of a mapped buffer
+	int ensure(size_t b, const char* what, bool mapped = false)
 	{
-		if (p && bytes >= b)
+		if (p && bytes >= b && (!mapped || dev))
 			return kOk;
 		release();
-		const cudaError_t e = cudaMallocHost(&p, b);
+		const cudaError_t e = mapped ? cudaHostAlloc(&p, b, cudaHostAllocMapped) : cudaMallocHost(&p, b);
 		if (e != cudaSuccess) {
 			p = nullptr;
 			return cudaCheck(e, what);
 		}
 		bytes = b;
+		if (mapped) {
+			const cudaError_t e2 = cudaHostGetDevicePointer(&dev, p, 0);
+			if (e2 != cudaSuccess) {
+				release();
+				return cudaCheck(e2, what);
+			}
+		}
 		return kOk;
 	}
 	void release()
@@ -118,6 +126,7 @@ struct PinnedBuf {
 		if (p)
 			cudaFreeHost(p);
 		p = nullptr;
+		dev = nullptr;
 		bytes = 0;
 	}
 	template <typename T>
@@ -874,13 +883,16 @@ int hostEval(pwa_likelihood* L, const double* par, double* f, double* grad, int 
 	PWA_TRY(checkFinished(L));
 	const double t0 = seconds();
 	const uint32_t P = L->nPars;
+	// the kernel reads the parameters from and writes the results to mapped
+	// pinned host memory: one launch and one synchronisation per call, no
+	// separate copies (a previous call's kernel has finished: it was waited for)
+	PWA_TRY(L->hPar.ensure(P * sizeof(double), "pinned parameters", true));
+	PWA_TRY(L->hOut.ensure((P + 2) * sizeof(double), "pinned result", true));
 	std::memcpy(L->hPar.as<double>(), par, P * sizeof(double));
 	cudaStream_t s = L->stream;
-	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dPar.p, L->hPar.p, P * sizeof(double), cudaMemcpyHostToDevice, s), "H2D par"));
 	cudaEventRecord(L->ev[0], s);
-	PWA_TRY(launchEval(L, L->dPar.as<double>(), L->dOut.as<double>(), withGrad, s, L->ev[1]));
-	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->hOut.p, L->dOut.p, (P + 2) * sizeof(double), cudaMemcpyDeviceToHost, s),
-	                  "D2H result"));
+	PWA_TRY(launchEval(L, static_cast<const double*>(L->hPar.dev), static_cast<double*>(L->hOut.dev), withGrad, s,
+	                   L->ev[1]));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "FdF sync"));
 	const double* out = L->hOut.as<double>();
 	if (out[P + 1] != 0.) {
@@ -1547,8 +1559,10 @@ int pwa_likelihood_finish_init(pwa_likelihood* L)
 	PWA_TRY(L->dErr.alloc(sizeof(unsigned), "error flag"));
 	PWA_TRY(L->dPar.alloc(L->nPars * sizeof(double), "parameters"));
 	PWA_TRY(L->dOut.alloc((L->nPars + 2) * sizeof(double), "result"));
-	PWA_TRY(L->hPar.ensure(L->nPars * sizeof(double), "pinned parameters"));
-	PWA_TRY(L->hOut.ensure((L->nPars + 2) * sizeof(double), "pinned result"));
+	// mapped: the host-buffer entry points let the kernel read the
+	// parameters from and write the results to host memory directly
+	PWA_TRY(L->hPar.ensure(L->nPars * sizeof(double), "pinned parameters", true));
+	PWA_TRY(L->hOut.ensure((L->nPars + 2) * sizeof(double), "pinned result", true));
 	std::vector<double> accI;
 	for (uint32_t e = 0; e < 2; ++e)
 		for (uint32_t i = 0; i < L->nW[e]; ++i)
@@ -1708,8 +1722,8 @@ int pwa_likelihood_fdf_batch(pwa_likelihood* L, uint32_t nPoints, const double* 
 	const double t0 = seconds();
 	PWA_TRY(L->dPar.ensure((size_t)nPoints * P * sizeof(double), "batch parameters"));
 	PWA_TRY(L->dOut.ensure((size_t)nPoints * (P + 2) * sizeof(double), "batch results"));
-	PWA_TRY(L->hPar.ensure((size_t)nPoints * P * sizeof(double), "pinned batch parameters"));
-	PWA_TRY(L->hOut.ensure((size_t)nPoints * (P + 2) * sizeof(double), "pinned batch results"));
+	PWA_TRY(L->hPar.ensure((size_t)nPoints * P * sizeof(double), "pinned batch parameters", true));
+	PWA_TRY(L->hOut.ensure((size_t)nPoints * (P + 2) * sizeof(double), "pinned batch results", true));
 	std::memcpy(L->hPar.p, par, (size_t)nPoints * P * sizeof(double));
 	cudaStream_t s = L->stream;
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(L->dPar.p, L->hPar.p, (size_t)nPoints * P * sizeof(double),
