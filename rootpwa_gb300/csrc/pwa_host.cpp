@@ -1235,8 +1235,8 @@ int pwa_likelihood_set_plan(pwa_likelihood* L, int stages)
 int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events)
 {
 	PWA_TRY(checkFinished(L));
-	if (phase1Events != 0 && phase1Events != 1 && phase1Events != 2)
-		return setError(kErrArg, "phase-1 events per lane must be 1 or 2 (0: keep)");
+	if (phase1Events < 0 || phase1Events > 3)
+		return setError(kErrArg, "FdF kernel variant must be 1 or 2 (events per lane), 3 (fused gradient) or 0 (keep)");
 	const int ne = phase1Events ? phase1Events : L->plan.phase1Events;
 	std::vector<FdfPlan> cands;
 	PWA_TRY(planCandidates((int)L->nW[0], (int)L->W(), (int)L->rank, (int)L->storeB, L->nEvents, L->numSMs, L->maxSmem,

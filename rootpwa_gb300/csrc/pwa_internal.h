@@ -71,7 +71,7 @@ struct FdfPlan {
 	int E = 128;        // events per tile (= store block)
 	int stages = 2;     // shared-memory pipeline depth
 	int wpw = 2;        // wave bucket per warp (template)
-	int phase1Events = 2;  // events per lane in the coherent-sum phase (1 or 2)
+	int phase1Events = 2;  // events per lane in the coherent-sum phase (1 or 2; 3: fused-gradient variant)
 	int blocks = 0;     // grid size (persistent, <= #SMs)
 	size_t smemBytes = 0;
 };
@@ -106,6 +106,11 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 int launchFdf(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
 // 64-bit words of the FdF kernel's fixed-point accumulators (all replicas).
 size_t fdfAccumulatorWords(int nPartial);
+// Fused-gradient FdF variant (fdf_fused.cu, plan phase1Events == 3):
+// 128-event tiles, rank 1 or 2, at most 16 negative and 104 positive waves.
+// Dynamic shared memory it needs for `stages` stages, 0 when unsupported.
+size_t fusedFdfSmem(int W0, int W, int R, int stages);
+int launchFdfFused(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
 
 // Converts one wave w of amplitudes (complex64 or complex128, device memory)
 // into the tiled complex64 store, divided by `divisor` in FP64; sets *nonzero

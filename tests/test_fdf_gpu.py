@@ -101,8 +101,15 @@ def test_shapes_against_oracle(n_neg, n_pos, rank, n_data):
     w = stress_workload(n_neg, n_pos, rank, n_data, flat=1.0)
     O, G = pair(w)
     stages = G.plan()[1]
-    # both coherent-sum variants (one and two events per lane)
-    for ne in (1, 2):
+    # every kernel variant the shape supports: one or two events per lane in
+    # the coherent-sum phase, and the fused-gradient kernel (rank <= 2,
+    # 128-event tiles)
+    fused_ok = rank <= 2 and G.plan()[0] == 128 and n_neg <= 16 and 1 <= n_pos <= 104
+    for ne in (1, 2, 3):
+        if ne == 3 and not fused_ok:
+            with pytest.raises(R.PwaError):
+                G.setPlan(stages, ne)
+            continue
         G.setPlan(stages, ne)
         assert G.planVariant() == ne
         check_point(O, G, w["par"])
@@ -110,6 +117,10 @@ def test_shapes_against_oracle(n_neg, n_pos, rank, n_data):
         q = 0.5 * w["par"][::-1].copy()
         q[-1] = -0.8
         check_point(O, G, q)
+        # value-only and gradient-only launches of the same variant agree bitwise
+        f, g = G.FdF(q)
+        assert G.DoEval(q) == f
+        assert np.array_equal(G.Gradient(q), g)
 
 
 def test_ill_conditioned_point():
