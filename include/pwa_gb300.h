@@ -357,6 +357,22 @@ int pwa_multibin_sweep_ms(pwa_multibin* M, const double* x, uint32_t reps, doubl
  * status (pwa_lbfgs_status), iterations [Q], sweeps run. */
 int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t sweepsPerGraph, uint32_t maxSweeps,
                      double* x, double* f, double* gnorm, int32_t* status, uint32_t* iterations, uint32_t* sweeps);
+/* Checkpoint / resume of a batched fit (no reference counterpart; the
+ * reference appends each finished fit to a ROOT tree, pwaFit.py:101-130).
+ * The fit state (iterates, trial points, gradients, L-BFGS histories and
+ * per-problem counters) lives on the device; save_state writes it to a file
+ * (through path.tmp and a rename), load_state reads it back into a batch
+ * with the same bins, starts and options, and resume continues the sweeps
+ * from it, giving the same results bit for bit as a fit that was never
+ * interrupted.  set_checkpoint makes fit/resume write the file every
+ * `everySweeps` sweeps, between graph launches (0 switches it off). */
+int pwa_multibin_save_state(pwa_multibin* M, const char* path);
+int pwa_multibin_load_state(pwa_multibin* M, const char* path);
+int pwa_multibin_resume(pwa_multibin* M, int useGraph, uint32_t sweepsPerGraph, uint32_t maxSweeps, double* x,
+                        double* f, double* gnorm, int32_t* status, uint32_t* iterations, uint32_t* sweeps);
+int pwa_multibin_set_checkpoint(pwa_multibin* M, const char* path, uint32_t everySweeps);
+/* sweeps run since the fit started (including those before a saved state) */
+int pwa_multibin_sweeps_done(const pwa_multibin* M, uint32_t* sweeps);
 
 /* ------------------------------------------------------------------------ */
 /* Learned warm start (no reference counterpart): a 3-layer perceptron        */

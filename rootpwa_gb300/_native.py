@@ -91,6 +91,11 @@ SIGNATURES = {
     "pwa_mlp_gradient": (i, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), u32, pd, C.POINTER(C.c_float)]),
     "pwa_mlp_train": (i, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), u64, u32, u32, C.c_float, u64, pd]),
     "pwa_multibin_fit": (i, [vp, pd, i, u32, u32, pd, pd, pd, C.POINTER(i32), C.POINTER(u32), C.POINTER(u32)]),
+    "pwa_multibin_resume": (i, [vp, i, u32, u32, pd, pd, pd, C.POINTER(i32), C.POINTER(u32), C.POINTER(u32)]),
+    "pwa_multibin_save_state": (i, [vp, C.c_char_p]),
+    "pwa_multibin_load_state": (i, [vp, C.c_char_p]),
+    "pwa_multibin_set_checkpoint": (i, [vp, C.c_char_p, u32]),
+    "pwa_multibin_sweeps_done": (i, [vp, C.POINTER(u32)]),
     "pwa_likelihood_create": (i, [pvp]),
     "pwa_likelihood_destroy": (i, [vp]),
     "pwa_likelihood_use_normalized_amps": (i, [vp, i]),

@@ -2188,6 +2188,12 @@ struct pwa_multibin {
 	PinnedBuf hCount;
 	// per check of the last fit: elapsed seconds and every problem's current f
 	std::vector<double> traceT, traceF;
+	// the device holds a fit state that pwa_multibin_resume can continue
+	bool stateValid = false;
+	uint32_t sweepsDone = 0;
+	// checkpoint file written every checkpointEvery sweeps of a fit (0: none)
+	std::string checkpointPath;
+	uint32_t checkpointEvery = 0;
 
 	~pwa_multibin()
 	{
@@ -2367,6 +2373,7 @@ int ensureBuilt(pwa_multibin* M) { return M->built ? kOk : buildBatch(M); }
 // uploads trial points and marks every problem active
 int startSweep(pwa_multibin* M, const double* x)
 {
+	M->stateValid = false;  // the trial points and active flags are overwritten
 	const size_t Q = (size_t)M->Q, P = (size_t)M->P;
 	cudaStream_t s = M->stream;
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dXt.p, x, Q * P * sizeof(double), cudaMemcpyHostToDevice, s), "upload"));
@@ -2374,6 +2381,191 @@ int startSweep(pwa_multibin* M, const double* x)
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dActive.p, ones.data(), Q * sizeof(int), cudaMemcpyHostToDevice, s), "upload"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(M->dErr.p, 0, sizeof(unsigned), s), "memset"));
 	return cudaCheck(cudaStreamSynchronize(s), "upload sync");
+}
+
+// The device buffers that hold a batched fit's state, in file order: the
+// iterates, trial points, gradients, directions, scalars, L-BFGS histories
+// and per-problem counters.  Everything else is rebuilt from the bins.
+std::vector<DevBuf*> stateBuffers(pwa_multibin* M)
+{
+	return {&M->dX,     &M->dXt,    &M->dG,     &M->dGt,    &M->dD,     &M->dF,    &M->dFt,    &M->dGnorm,
+	        &M->dStep,  &M->dGamma, &M->dGBest, &M->dS,     &M->dY,     &M->dRho,  &M->dAlpha, &M->dStatus,
+	        &M->dIter,  &M->dNBack, &M->dHist,  &M->dHead,  &M->dItBest, &M->dActive};
+}
+
+constexpr char kStateMagic[8] = {'R', 'P', 'W', 'A', 'M', 'B', 'S', '1'};
+
+// Checkpoint file: magic, u32 Q, P, m, number of bins, sweeps done, then per
+// bin u64 events and u32 starts (checked on load), then every state buffer
+// as u64 byte count + bytes.  Written to path + ".tmp" and renamed, so a
+// crash while writing leaves the previous checkpoint intact.
+int saveState(pwa_multibin* M, const std::string& path)
+{
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(M->stream), "checkpoint sync"));
+	const std::string tmp = path + ".tmp";
+	FILE* fp = std::fopen(tmp.c_str(), "wb");
+	if (!fp)
+		return setError(kErrIo, "cannot create checkpoint '" + tmp + "'");
+	bool ok = std::fwrite(kStateMagic, 1, 8, fp) == 8;
+	const uint32_t head[5] = {(uint32_t)M->Q, (uint32_t)M->P, M->m, (uint32_t)M->bins.size(), M->sweepsDone};
+	ok = ok && std::fwrite(head, sizeof(head), 1, fp) == 1;
+	for (const auto& B : M->bins) {
+		const uint64_t n = B.v.nEvents;
+		ok = ok && std::fwrite(&n, 8, 1, fp) == 1 && std::fwrite(&B.nStarts, 4, 1, fp) == 1;
+	}
+	std::vector<unsigned char> host;
+	int st = kOk;
+	for (DevBuf* b : stateBuffers(M)) {
+		if (!ok)
+			break;
+		const uint64_t n = b->bytes;
+		host.resize(n);
+		st = cudaCheck(cudaMemcpy(host.data(), b->p, n, cudaMemcpyDeviceToHost), "checkpoint download");
+		if (st != kOk)
+			break;
+		ok = std::fwrite(&n, 8, 1, fp) == 1 && std::fwrite(host.data(), 1, n, fp) == n;
+	}
+	ok = (std::fclose(fp) == 0) && ok;
+	if (st != kOk) {
+		std::remove(tmp.c_str());
+		return st;
+	}
+	if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) {
+		std::remove(tmp.c_str());
+		return setError(kErrIo, "cannot write checkpoint '" + path + "'");
+	}
+	return kOk;
+}
+
+int loadState(pwa_multibin* M, const std::string& path)
+{
+	FILE* fp = std::fopen(path.c_str(), "rb");
+	if (!fp)
+		return setError(kErrIo, "cannot open checkpoint '" + path + "'");
+	auto fail = [&](const std::string& why) {
+		std::fclose(fp);
+		return setError(kErrIo, "checkpoint '" + path + "': " + why);
+	};
+	char magic[8];
+	uint32_t head[5];
+	if (std::fread(magic, 1, 8, fp) != 8 || std::memcmp(magic, kStateMagic, 8) != 0)
+		return fail("not a multibin checkpoint");
+	if (std::fread(head, sizeof(head), 1, fp) != 1)
+		return fail("truncated header");
+	if (head[0] != (uint32_t)M->Q || head[1] != (uint32_t)M->P || head[2] != M->m || head[3] != M->bins.size())
+		return fail("problem count, parameter count, history length or bin count differs from this batch");
+	for (const auto& B : M->bins) {
+		uint64_t n = 0;
+		uint32_t starts = 0;
+		if (std::fread(&n, 8, 1, fp) != 1 || std::fread(&starts, 4, 1, fp) != 1)
+			return fail("truncated bin table");
+		if (n != B.v.nEvents || starts != B.nStarts)
+			return fail("bin events or starts differ from this batch");
+	}
+	std::vector<unsigned char> host;
+	for (DevBuf* b : stateBuffers(M)) {
+		uint64_t n = 0;
+		if (std::fread(&n, 8, 1, fp) != 1 || n != b->bytes)
+			return fail("state buffer size differs");
+		host.resize(n);
+		if (std::fread(host.data(), 1, n, fp) != n)
+			return fail("truncated state buffer");
+		const int st = cudaCheck(cudaMemcpy(b->p, host.data(), n, cudaMemcpyHostToDevice), "checkpoint upload");
+		if (st != kOk) {
+			std::fclose(fp);
+			return st;
+		}
+	}
+	std::fclose(fp);
+	M->sweepsDone = head[4];
+	M->stateValid = true;
+	return kOk;
+}
+
+// Runs fit sweeps from the current device state until no problem is active
+// or maxSweeps more sweeps have run; writes the checkpoint file between
+// graph launches when one is set.
+int runFit(pwa_multibin* M, int useGraph, uint32_t sweepsPerGraph, uint32_t maxSweeps, double* x, double* f,
+           double* gnorm, int32_t* status, uint32_t* iterations, uint32_t* sweeps)
+{
+	const size_t Q = (size_t)M->Q, P = (size_t)M->P;
+	cudaStream_t s = M->stream;
+	const uint32_t per = std::max<uint32_t>(1, sweepsPerGraph);
+	cudaGraphExec_t exec = nullptr;
+	if (useGraph) {
+		cudaGraph_t g = nullptr;
+		PWA_TRY(cudaCheck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture"));
+		int st = kOk;
+		for (uint32_t i = 0; i < per && st == kOk; ++i)
+			st = fitSweep(M);
+		const cudaError_t ce = cudaStreamEndCapture(s, &g);
+		if (st != kOk) {
+			if (g)
+				cudaGraphDestroy(g);
+			return st;
+		}
+		PWA_TRY(cudaCheck(ce, "end capture"));
+		const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+		cudaGraphDestroy(g);
+		PWA_TRY(cudaCheck(ie, "graph instantiate"));
+	}
+	uint32_t done = 0, lastCheckpoint = M->sweepsDone;
+	unsigned* nAct = static_cast<unsigned*>(M->hCount.p);
+	int st = kOk;
+	M->traceT.clear();
+	M->traceF.clear();
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "fit start"));
+	const double t0 = seconds();
+	while (done < maxSweeps) {
+		if (exec)
+			st = cudaCheck(cudaGraphLaunch(exec, s), "graph launch");
+		else
+			for (uint32_t i = 0; i < per && st == kOk; ++i)
+				st = fitSweep(M);
+		if (st != kOk)
+			break;
+		done += per;
+		M->sweepsDone += per;
+		st = cudaCheck(cudaMemcpyAsync(nAct, M->dNActive.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "count");
+		if (st == kOk)
+			st = cudaCheck(cudaStreamSynchronize(s), "fit sync");
+		if (st == kOk) {
+			// trace: elapsed time and the accepted f of every problem
+			M->traceT.push_back(seconds() - t0);
+			const size_t o = M->traceF.size();
+			M->traceF.resize(o + Q);
+			st = cudaCheck(cudaMemcpy(M->traceF.data() + o, M->dF.p, Q * sizeof(double), cudaMemcpyDeviceToHost),
+			               "trace");
+		}
+		if (st == kOk && M->checkpointEvery > 0 && M->sweepsDone - lastCheckpoint >= M->checkpointEvery) {
+			st = saveState(M, M->checkpointPath);
+			lastCheckpoint = M->sweepsDone;
+		}
+		if (st != kOk || *nAct == 0)
+			break;
+	}
+	if (exec)
+		cudaGraphExecDestroy(exec);
+	PWA_TRY(st);
+	if (sweeps)
+		*sweeps = done;
+	if (x)
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(x, M->dX.p, Q * P * sizeof(double), cudaMemcpyDeviceToHost, s), "download"));
+	if (f)
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(f, M->dF.p, Q * sizeof(double), cudaMemcpyDeviceToHost, s), "download"));
+	if (gnorm)
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(gnorm, M->dGnorm.p, Q * sizeof(double), cudaMemcpyDeviceToHost, s),
+		                  "download"));
+	if (status)
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(status, M->dStatus.p, Q * sizeof(int), cudaMemcpyDeviceToHost, s),
+		                  "download"));
+	std::vector<int> it(Q);
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(it.data(), M->dIter.p, Q * sizeof(int), cudaMemcpyDeviceToHost, s), "download"));
+	PWA_TRY(checkDevErr(M));
+	if (iterations)
+		for (size_t q = 0; q < Q; ++q)
+			iterations[q] = (uint32_t)it[q];
+	return kOk;
 }
 
 // Times one evaluation sweep (all problems active) in milliseconds.
@@ -2444,6 +2636,7 @@ int pwa_multibin_add_bin(pwa_multibin* M, pwa_likelihood* L, uint32_t nStarts)
 	}
 	M->bins.push_back(pwa_multibin::Bin{L, v, nStarts});
 	M->built = false;
+	M->stateValid = false;
 	return kOk;
 }
 
@@ -2462,6 +2655,7 @@ int pwa_multibin_set_options(pwa_multibin* M, uint32_t startGroup, uint32_t lbfg
 	M->gtolRel = gtolRel;
 	M->maxIter = maxIter;
 	M->built = false;
+	M->stateValid = false;
 	return kOk;
 }
 
@@ -2497,6 +2691,7 @@ int pwa_multibin_set_chunks(pwa_multibin* M, const uint32_t* tilesPerItem)
 	for (int c = 0; c < 3; ++c)
 		M->chunkTiles[c] = tilesPerItem[c];
 	M->built = false;
+	M->stateValid = false;
 	return kOk;
 }
 
@@ -2568,6 +2763,7 @@ int pwa_multibin_autotune(pwa_multibin* M, const double* x)
 		for (uint32_t t : cand) {
 			M->chunkTiles[c] = t;
 			M->built = false;
+			M->stateValid = false;
 			PWA_TRY(ensureBuilt(M));
 			PWA_TRY(startSweep(M, x));
 			float ms = 0.f;
@@ -2579,6 +2775,7 @@ int pwa_multibin_autotune(pwa_multibin* M, const double* x)
 		}
 		M->chunkTiles[c] = best;
 		M->built = false;
+		M->stateValid = false;
 	}
 	return ensureBuilt(M);
 }
@@ -2591,80 +2788,60 @@ int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t s
 	PWA_TRY(ensureBuilt(M));
 	const size_t Q = (size_t)M->Q, P = (size_t)M->P;
 	cudaStream_t s = M->stream;
+	M->stateValid = false;
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dX.p, x0, Q * P * sizeof(double), cudaMemcpyHostToDevice, s), "upload"));
 	for (DevBuf* b : {&M->dStatus, &M->dIter, &M->dNBack, &M->dHist, &M->dHead, &M->dItBest})
 		PWA_TRY(cudaCheck(cudaMemsetAsync(b->p, 0, Q * sizeof(int), s), "memset"));
 	PWA_TRY(startSweep(M, x0));
-	const uint32_t per = std::max<uint32_t>(1, sweepsPerGraph);
-	cudaGraphExec_t exec = nullptr;
-	if (useGraph) {
-		cudaGraph_t g = nullptr;
-		PWA_TRY(cudaCheck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture"));
-		int st = kOk;
-		for (uint32_t i = 0; i < per && st == kOk; ++i)
-			st = fitSweep(M);
-		const cudaError_t ce = cudaStreamEndCapture(s, &g);
-		if (st != kOk) {
-			if (g)
-				cudaGraphDestroy(g);
-			return st;
-		}
-		PWA_TRY(cudaCheck(ce, "end capture"));
-		const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
-		cudaGraphDestroy(g);
-		PWA_TRY(cudaCheck(ie, "graph instantiate"));
-	}
-	uint32_t done = 0;
-	unsigned* nAct = static_cast<unsigned*>(M->hCount.p);
-	int st = kOk;
-	M->traceT.clear();
-	M->traceF.clear();
-	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "fit start"));
-	const double t0 = seconds();
-	while (done < maxSweeps) {
-		if (exec)
-			st = cudaCheck(cudaGraphLaunch(exec, s), "graph launch");
-		else
-			for (uint32_t i = 0; i < per && st == kOk; ++i)
-				st = fitSweep(M);
-		if (st != kOk)
-			break;
-		done += per;
-		st = cudaCheck(cudaMemcpyAsync(nAct, M->dNActive.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "count");
-		if (st == kOk)
-			st = cudaCheck(cudaStreamSynchronize(s), "fit sync");
-		if (st == kOk) {
-			// trace: elapsed time and the accepted f of every problem
-			M->traceT.push_back(seconds() - t0);
-			const size_t o = M->traceF.size();
-			M->traceF.resize(o + Q);
-			st = cudaCheck(cudaMemcpy(M->traceF.data() + o, M->dF.p, Q * sizeof(double), cudaMemcpyDeviceToHost),
-			               "trace");
-		}
-		if (st != kOk || *nAct == 0)
-			break;
-	}
-	if (exec)
-		cudaGraphExecDestroy(exec);
-	PWA_TRY(st);
-	if (sweeps)
-		*sweeps = done;
-	if (x)
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(x, M->dX.p, Q * P * sizeof(double), cudaMemcpyDeviceToHost, s), "download"));
-	if (f)
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(f, M->dF.p, Q * sizeof(double), cudaMemcpyDeviceToHost, s), "download"));
-	if (gnorm)
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(gnorm, M->dGnorm.p, Q * sizeof(double), cudaMemcpyDeviceToHost, s),
-		                  "download"));
-	if (status)
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(status, M->dStatus.p, Q * sizeof(int), cudaMemcpyDeviceToHost, s),
-		                  "download"));
-	std::vector<int> it(Q);
-	PWA_TRY(cudaCheck(cudaMemcpyAsync(it.data(), M->dIter.p, Q * sizeof(int), cudaMemcpyDeviceToHost, s), "download"));
-	PWA_TRY(checkDevErr(M));
-	if (iterations)
-		for (size_t q = 0; q < Q; ++q)
-			iterations[q] = (uint32_t)it[q];
+	M->sweepsDone = 0;
+	M->stateValid = true;
+	return runFit(M, useGraph, sweepsPerGraph, maxSweeps, x, f, gnorm, status, iterations, sweeps);
+}
+
+int pwa_multibin_resume(pwa_multibin* M, int useGraph, uint32_t sweepsPerGraph, uint32_t maxSweeps, double* x,
+                        double* f, double* gnorm, int32_t* status, uint32_t* iterations, uint32_t* sweeps)
+{
+	if (!M)
+		return setError(kErrArg, "null argument");
+	if (!M->built || !M->stateValid)
+		return setError(kErrState, "multibin: no fit state to resume (run a fit or load a saved state first)");
+	PWA_TRY(cudaCheck(cudaMemsetAsync(M->dErr.p, 0, sizeof(unsigned), M->stream), "memset"));
+	return runFit(M, useGraph, sweepsPerGraph, maxSweeps, x, f, gnorm, status, iterations, sweeps);
+}
+
+int pwa_multibin_set_checkpoint(pwa_multibin* M, const char* path, uint32_t everySweeps)
+{
+	if (!M)
+		return setError(kErrArg, "null argument");
+	if (everySweeps > 0 && (!path || !*path))
+		return setError(kErrArg, "multibin: checkpoint path missing");
+	M->checkpointPath = everySweeps > 0 ? path : "";
+	M->checkpointEvery = everySweeps;
+	return kOk;
+}
+
+int pwa_multibin_save_state(pwa_multibin* M, const char* path)
+{
+	if (!M || !path)
+		return setError(kErrArg, "null argument");
+	if (!M->built || !M->stateValid)
+		return setError(kErrState, "multibin: no fit state to save");
+	return saveState(M, path);
+}
+
+int pwa_multibin_load_state(pwa_multibin* M, const char* path)
+{
+	if (!M || !path)
+		return setError(kErrArg, "null argument");
+	PWA_TRY(ensureBuilt(M));
+	return loadState(M, path);
+}
+
+int pwa_multibin_sweeps_done(const pwa_multibin* M, uint32_t* sweeps)
+{
+	if (!M || !sweeps)
+		return setError(kErrArg, "null argument");
+	*sweeps = M->stateValid ? M->sweepsDone : 0;
 	return kOk;
 }
 

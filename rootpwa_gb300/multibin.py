@@ -123,3 +123,35 @@ class pwaMultibin:
                _pd(x), _pd(f), _pd(gn), st.ctypes.data_as(C.POINTER(C.c_int32)),
                it.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(sw))
         return dict(x=x, f=f, gnorm=gn, status=st, iterations=it, sweeps=sw.value)
+
+    def resume(self, useGraph=True, sweepsPerGraph=25, maxSweeps=1_000_000):
+        """Continues the fit held on the device (after fit() stopped at
+        maxSweeps, or after loadState); same outputs as fit()."""
+        Q, P = self.nmbProblems(), self.nmbPars()
+        x = np.zeros((Q, P))
+        f = np.zeros(Q)
+        gn = np.zeros(Q)
+        st = np.zeros(Q, dtype=np.int32)
+        it = np.zeros(Q, dtype=np.uint32)
+        sw = C.c_uint32()
+        N.call("pwa_multibin_resume", self._h, 1 if useGraph else 0, int(sweepsPerGraph), int(maxSweeps),
+               _pd(x), _pd(f), _pd(gn), st.ctypes.data_as(C.POINTER(C.c_int32)),
+               it.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(sw))
+        return dict(x=x, f=f, gnorm=gn, status=st, iterations=it, sweeps=sw.value)
+
+    def saveState(self, path):
+        """Writes the device-side fit state to a checkpoint file."""
+        N.call("pwa_multibin_save_state", self._h, str(path).encode())
+
+    def loadState(self, path):
+        """Reads a checkpoint written for a batch with the same bins, starts and options."""
+        N.call("pwa_multibin_load_state", self._h, str(path).encode())
+
+    def setCheckpoint(self, path, everySweeps):
+        """fit()/resume() write the checkpoint file every `everySweeps` sweeps (0: off)."""
+        N.call("pwa_multibin_set_checkpoint", self._h, str(path).encode() if path else None, int(everySweeps))
+
+    def sweepsDone(self):
+        v = C.c_uint32()
+        N.call("pwa_multibin_sweeps_done", self._h, C.byref(v))
+        return v.value
