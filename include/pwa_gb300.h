@@ -245,6 +245,11 @@ int pwa_ampfile_name(const char* path, int isVariable, uint32_t i, char* buf, ui
  * before finishInit(), instead of addAmplitude(). */
 int pwa_likelihood_load_amp_files(pwa_likelihood* L, uint32_t nFiles, const char* const* paths, uint32_t nBinVars,
                                   const char* const* binVarNames, const double* lower, const double* upper);
+/* Test hook (no reference counterpart): after n further device allocations
+ * of the library, every allocation fails with PWA_ERROR_OUT_OF_MEMORY
+ * without calling the CUDA allocator; n < 0 switches it off.  Exercises the
+ * error paths of setup without exhausting a GPU. */
+int pwa_debug_fail_alloc_after(int64_t n);
 /* finishInit (pwaLikelihood.cc:1291-1388) */
 int pwa_likelihood_finish_init(pwa_likelihood* L);
 

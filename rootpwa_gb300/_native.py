@@ -104,6 +104,7 @@ SIGNATURES = {
     "pwa_likelihood_set_shard": (i, [vp, u64, i]),
     "pwa_likelihood_set_otf_binning": (i, [vp, u32, pd, pd, C.POINTER(vp), u64, i]),
     "pwa_likelihood_otf_selected": (i, [vp, C.POINTER(u64)]),
+    "pwa_debug_fail_alloc_after": (i, [i64]),
     "pwa_likelihood_load_amp_files": (i, [vp, u32, C.POINTER(C.c_char_p), u32, C.POINTER(C.c_char_p), pd, pd]),
     "pwa_ampfile_write": (i, [C.c_char_p, u32, C.POINTER(C.c_char_p), u64, vp, u32, C.POINTER(C.c_char_p), pd]),
     "pwa_ampfile_info": (i, [C.c_char_p, C.POINTER(u32), C.POINTER(u64), C.POINTER(u32)]),

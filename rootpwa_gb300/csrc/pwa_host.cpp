@@ -57,6 +57,11 @@ void countLaunches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relax
 namespace {
 
 // device allocation owned by a handle
+// Test hook: after this many further device allocations, every allocation
+// fails with PWA_ERROR_OUT_OF_MEMORY before it reaches cudaMalloc (negative:
+// off).  Host-side fault injection for the error paths.
+std::atomic<long> g_failAllocAfter{-1};
+
 struct DevBuf {
 	void* p = nullptr;
 	size_t bytes = 0;
@@ -69,6 +74,10 @@ struct DevBuf {
 		release();
 		if (b == 0)
 			return kOk;
+		if (g_failAllocAfter.load() >= 0 && g_failAllocAfter.fetch_sub(1) <= 0) {
+			g_failAllocAfter.store(0);
+			return setError(kErrOom, std::string(what) + ": injected allocation failure");
+		}
 		const cudaError_t e = cudaMalloc(&p, b);
 		if (e != cudaSuccess) {
 			p = nullptr;
@@ -1170,6 +1179,12 @@ int pwa_likelihood_load_amp_files(pwa_likelihood* L, uint32_t nFiles, const char
 		}
 		PWA_TRY(pwa_likelihood_add_amplitude(L, w.c_str(), row.p, total, PWA_COMPLEX64, PWA_MEMORY_DEVICE));
 	}
+	return kOk;
+}
+
+int pwa_debug_fail_alloc_after(int64_t n)
+{
+	g_failAllocAfter.store(n < 0 ? -1 : (long)n);
 	return kOk;
 }
 

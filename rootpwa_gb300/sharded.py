@@ -18,19 +18,44 @@ def shard_range(n_events, rank, world):
     return b, b + per + (1 if rank < extra else 0)
 
 
+class ShardFailure(RuntimeError):
+    """Another rank of the shard group reported a failure."""
+
+
 class ShardedFdF:
     """FdF of the whole data set from the rank-local shard `local` (any
-    object with FdF(par) -> (f, grad)); collective over `group`."""
+    object with FdF(par) -> (f, grad)); collective over `group`.
 
-    def __init__(self, local, group=None, device="cpu"):
+    Failure detection on the host: with a torch.distributed `store`, a rank
+    whose local evaluation raises records itself under FAILED_KEY before it
+    re-raises, and every rank checks that key before it enters the
+    all-reduce, so the others stop with ShardFailure instead of waiting in a
+    collective the failed rank never joins.  Without a store, the process
+    group's own timeout ends that collective with an error."""
+
+    FAILED_KEY = "pwa_shard_failed"
+
+    def __init__(self, local, group=None, device="cpu", store=None):
         self.local = local
         self.group = group
         self.device = device
+        self.store = store
+
+    def _check_peers(self):
+        if self.store is not None and self.store.check([self.FAILED_KEY]):
+            raise ShardFailure("shard rank %s failed" % self.store.get(self.FAILED_KEY).decode())
 
     def FdF(self, par):
         import torch
         import torch.distributed as dist
-        f, g = self.local.FdF(par)
+        self._check_peers()
+        try:
+            f, g = self.local.FdF(par)
+        except Exception:
+            if self.store is not None:
+                self.store.set(self.FAILED_KEY, str(dist.get_rank(self.group)))
+            raise
+        self._check_peers()
         buf = torch.from_numpy(np.concatenate([[f], np.asarray(g, dtype=np.float64)])).to(self.device)
         dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=self.group)
         out = buf.cpu().numpy()
