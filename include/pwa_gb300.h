@@ -245,6 +245,17 @@ int pwa_ampfile_name(const char* path, int isVariable, uint32_t i, char* buf, ui
  * before finishInit(), instead of addAmplitude(). */
 int pwa_likelihood_load_amp_files(pwa_likelihood* L, uint32_t nFiles, const char* const* paths, uint32_t nBinVars,
                                   const char* const* binVarNames, const double* lower, const double* upper);
+/* Autotuner cache (no reference counterpart; the reference picks its grid
+ * by an occupancy heuristic, cuda/likelihoodInterface.cu:304-360).  The FdF
+ * plans the autotuner measured in this process (per wave count, negative
+ * waves, rank and event-count class) are written to / merged from a JSON
+ * file tagged with the device name; a likelihood whose shape is in the cache
+ * takes the cached plan at finishInit without timing runs.  Loading a cache
+ * measured on another device model is refused. */
+int pwa_autotune_cache_save(const char* path);
+int pwa_autotune_cache_load(const char* path);
+int pwa_autotune_cache_clear(void);
+int pwa_autotune_cache_size(uint32_t* n);
 /* Test hook (no reference counterpart): after n further device allocations
  * of the library, every allocation fails with PWA_ERROR_OUT_OF_MEMORY
  * without calling the CUDA allocator; n < 0 switches it off.  Exercises the

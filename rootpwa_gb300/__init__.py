@@ -9,3 +9,4 @@ from .likelihood import ampIntegralMatrix, pwaLikelihood  # noqa: F401
 from .multibin import pwaMultibin  # noqa: F401
 from .warmstart import pwaMLP  # noqa: F401
 from .ampfile import ampFileInfo, readAmplitudeFile, writeAmplitudeFile  # noqa: F401
+from . import autotune  # noqa: F401

@@ -9,7 +9,10 @@ import os
 import re
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libpwa_gb300.so")
+# PWA_GB300_DEBUG=1 selects the build with shared-memory bounds checks
+# (rootpwa_gb300.build.build_debug())
+LIB_PATH = os.path.join(_HERE, "libpwa_gb300_debug.so" if os.environ.get("PWA_GB300_DEBUG") == "1"
+                        else "libpwa_gb300.so")
 HEADER = os.path.join(os.path.dirname(_HERE), "include", "pwa_gb300.h")
 
 SUCCESS = 0
@@ -105,6 +108,10 @@ SIGNATURES = {
     "pwa_likelihood_set_otf_binning": (i, [vp, u32, pd, pd, C.POINTER(vp), u64, i]),
     "pwa_likelihood_otf_selected": (i, [vp, C.POINTER(u64)]),
     "pwa_debug_fail_alloc_after": (i, [i64]),
+    "pwa_autotune_cache_save": (i, [C.c_char_p]),
+    "pwa_autotune_cache_load": (i, [C.c_char_p]),
+    "pwa_autotune_cache_clear": (i, []),
+    "pwa_autotune_cache_size": (i, [C.POINTER(u32)]),
     "pwa_likelihood_load_amp_files": (i, [vp, u32, C.POINTER(C.c_char_p), u32, C.POINTER(C.c_char_p), pd, pd]),
     "pwa_ampfile_write": (i, [C.c_char_p, u32, C.POINTER(C.c_char_p), u64, vp, u32, C.POINTER(C.c_char_p), pd]),
     "pwa_ampfile_info": (i, [C.c_char_p, C.POINTER(u32), C.POINTER(u64), C.POINTER(u32)]),

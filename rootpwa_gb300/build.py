@@ -72,6 +72,50 @@ def build(force=False, ptxas_verbose=False, verbose=False):
     return LIB
 
 
+LIB_DEBUG = os.path.join(HERE, "libpwa_gb300_debug.so")
+BUILD_DEBUG = os.path.join(HERE, "_build_debug")
+# translation units rebuilt with the shared-memory bounds checks compiled in
+DEBUG_SOURCES = ("fdf_kernels.cu", "fdf_fused.cu")
+
+
+def build_debug():
+    """libpwa_gb300_debug.so: the release objects, except the FdF kernels,
+    which are compiled with -DPWA_DEBUG_CHECKS (every shared-memory access
+    checked against its region; a failed check sets a device error flag and
+    skips the access).  Loaded instead of the release library when the
+    environment has PWA_GB300_DEBUG=1."""
+    build()
+    os.makedirs(BUILD_DEBUG, exist_ok=True)
+    objs = []
+    todo = []
+    for src in sources():
+        name = os.path.basename(src)
+        if name in DEBUG_SOURCES:
+            obj = os.path.join(BUILD_DEBUG, name + ".o")
+            if not (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
+                    and os.path.getmtime(obj) >= _headers_mtime()):
+                todo.append((src, obj))
+            objs.append(obj)
+        else:
+            objs.append(os.path.join(BUILD, name + ".o"))
+
+    def comp(job):
+        src, obj = job
+        cmd = [_nvcc()] + ARCH + FLAGS + ["-DPWA_DEBUG_CHECKS", "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(todo))) as ex:
+        list(ex.map(comp, todo))
+    if not os.path.exists(LIB_DEBUG) or any(os.path.getmtime(o) > os.path.getmtime(LIB_DEBUG) for o in objs):
+        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB_DEBUG] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    return LIB_DEBUG
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, ptxas_verbose="-v" in sys.argv, verbose=True)
     print(LIB)

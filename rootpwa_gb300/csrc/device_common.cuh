@@ -14,6 +14,23 @@ constexpr unsigned long long kWaitLimitNs = 1000000000ull;
 
 __device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// Bounds checks of shared-memory accesses for the debug build (compiled with
+// -DPWA_DEBUG_CHECKS, the stand-in for a memory checker): an access of
+// `bytes` at shared address `addr` must lie in [lo, hi); otherwise the flag
+// kDevErrBounds (2) is set in *err and the caller skips the access.  In the
+// release build the check is the constant true and costs nothing.
+#ifdef PWA_DEBUG_CHECKS
+__device__ __forceinline__ bool smemInBounds(uint32_t addr, uint32_t bytes, uint32_t lo, uint32_t hi, unsigned* err)
+{
+	if (addr >= lo && addr + bytes <= hi && (addr & (bytes - 1u)) == 0u)
+		return true;
+	atomicOr(err, 2u);
+	return false;
+}
+#else
+__device__ __forceinline__ bool smemInBounds(uint32_t, uint32_t, uint32_t, uint32_t, unsigned*) { return true; }
+#endif
+
 __device__ __forceinline__ void mbarInit(uint64_t* bar, uint32_t count)
 {
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
@@ -141,6 +158,17 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 	float4 v;
 	asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
 	return v;
+}
+
+// loads with the debug build's bounds check against [lo, hi)
+__device__ __forceinline__ float2 lds64c(uint32_t addr, uint32_t lo, uint32_t hi, unsigned* err)
+{
+	return smemInBounds(addr, 8u, lo, hi, err) ? lds64(addr) : make_float2(0.f, 0.f);
+}
+
+__device__ __forceinline__ float4 lds128c(uint32_t addr, uint32_t lo, uint32_t hi, unsigned* err)
+{
+	return smemInBounds(addr, 16u, lo, hi, err) ? lds128(addr) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 }  // namespace pwa

@@ -164,18 +164,19 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 
 	// V of two consecutive ranks in one 128-bit load where the address is
 	// 16-byte aligned (even R)
+	const uint32_t vHi = vBase + (uint32_t)((W + 1) * R) * 8u;  // debug-build bounds
 	auto loadV = [&](uint32_t addr, float2 (&v)[R]) {
 		if ((R & 1) == 0) {
 #pragma unroll
 			for (int r = 0; r + 1 < R; r += 2) {
-				const float4 q = lds128(addr + (uint32_t)r * 8u);
+				const float4 q = lds128c(addr + (uint32_t)r * 8u, vBase, vHi, a.devErr);
 				v[r] = make_float2(q.x, q.y);
 				v[r + 1] = make_float2(q.z, q.w);
 			}
 		} else {
 #pragma unroll
 			for (int r = 0; r < R; ++r)
-				v[r] = lds64(addr + (uint32_t)r * 8u);
+				v[r] = lds64c(addr + (uint32_t)r * 8u, vBase, vHi, a.devErr);
 		}
 	};
 	// S[r][j] += V_r A of event j of the pair
@@ -229,6 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 			break;
 		}
 		const uint32_t tAddr = smemAddr(tiles + (size_t)s * W * E);
+		const uint32_t tHi = tAddr + stageBytes;  // debug-build bounds
 
 		// ---- coherent sums of the pair over this lane's waves ----
 		float2 S0[R][2], S1[R][2];
@@ -239,14 +241,14 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 				S0[r][j] = S1[r][j] = make_float2(0.f, 0.f);
 #pragma unroll
 		for (int j = 0; j < NEG; ++j) {
-			const float4 av = lds128(tAddr + rowNeg(j));
+			const float4 av = lds128c(tAddr + rowNeg(j), tAddr, tHi, a.devErr);
 			float2 v[R];
 			loadV(vNegA(j), v);
 			mac(av, v, S0);
 		}
 #pragma unroll
 		for (int j = 0; j < POS; ++j) {
-			const float4 av = lds128(tAddr + rowPos(j));
+			const float4 av = lds128c(tAddr + rowPos(j), tAddr, tHi, a.devErr);
 			float2 v[R];
 			loadV(vPosA(j), v);
 			mac(av, v, S1);
@@ -297,12 +299,12 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 				}
 #pragma unroll
 			for (int j = 0; j < NEG; ++j) {
-				const float4 av = lds128(tAddr + rowNeg(j));
+				const float4 av = lds128c(tAddr + rowNeg(j), tAddr, tHi, a.devErr);
 				gmac(av, T0[0], T1[0], Gn[j]);
 			}
 #pragma unroll
 			for (int j = 0; j < POS; ++j) {
-				const float4 av = lds128(tAddr + rowPos(j));
+				const float4 av = lds128c(tAddr + rowPos(j), tAddr, tHi, a.devErr);
 				gmac(av, T0[1], T1[1], Gp[j]);
 			}
 		}
@@ -354,7 +356,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 						gy += __shfl_xor_sync(0xffffffffu, gy, 4);
 						gx += __shfl_xor_sync(0xffffffffu, gx, 8);
 						gy += __shfl_xor_sync(0xffffffffu, gy, 8);
-						if (NEG > 0 && pm2 == 0 && j < n0) {
+						if (NEG > 0 && pm2 == 0 && j < n0 &&
+						    smemInBounds(smemAddr(Gw + (r * W + ph2 + 8 * j) * 2), 16u, smemAddr(Gw), smemAddr(Gw + nG),
+						                 a.devErr)) {
 							const int w = ph2 + 8 * j;
 							Gw[(r * W + w) * 2] += (double)gx;
 							Gw[(r * W + w) * 2 + 1] += (double)gy;
@@ -370,7 +374,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 						gy += __shfl_xor_sync(0xffffffffu, gy, 4);
 						gx += __shfl_xor_sync(0xffffffffu, gx, 8);
 						gy += __shfl_xor_sync(0xffffffffu, gy, 8);
-						if (POS > 0 && pm2 == 0 && j < n1) {
+						if (POS > 0 && pm2 == 0 && j < n1 &&
+						    smemInBounds(smemAddr(Gw + (r * W + wS1 + 8 * j) * 2), 16u, smemAddr(Gw), smemAddr(Gw + nG),
+						                 a.devErr)) {
 							const int w = wS1 + 8 * j;
 							Gw[(r * W + w) * 2] += (double)gx;
 							Gw[(r * W + w) * 2 + 1] += (double)gy;

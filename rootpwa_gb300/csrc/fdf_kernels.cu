@@ -227,6 +227,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		}
 		const bool timedOut = !mbarWaitBounded(&bars[s], parity);
 		const float2* tile = tiles + (size_t)s * W * E;
+		// shared-memory regions for the debug build's bounds checks
+		const uint32_t tLo = smemAddr(tile), tHi = tLo + stageBytes;
 		float2* T = Ts + (size_t)(k & 1ull) * R * 2 * E;
 		float2* Tw = Tsw + (size_t)(k & 1ull) * R * 2 * E;
 
@@ -236,6 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			int pe1;       // the event whose sums this lane holds after the combination
 			bool writer;   // one lane per event writes its results
 			const uint32_t vAddr = smemAddr(Vs);
+			const uint32_t vHi = vAddr + (uint32_t)(W * R) * 8u;
 			const uint32_t rowB = (uint32_t)lay.rowStride;
 			// V of two consecutive ranks in one 128-bit load; the address
 			// (w * R + r) * 8 is 16-byte aligned only for even R
@@ -243,14 +246,14 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				if ((R & 1) == 0) {
 #pragma unroll
 					for (int r = 0; r + 1 < R; r += 2) {
-						const float4 q = lds128(vAddr + (uint32_t)(w * R + r) * 8u);
+						const float4 q = lds128c(vAddr + (uint32_t)(w * R + r) * 8u, vAddr, vHi, a.devErr);
 						v[r] = make_float2(q.x, q.y);
 						v[r + 1] = make_float2(q.z, q.w);
 					}
 				} else {
 #pragma unroll
 					for (int r = 0; r < R; ++r)
-						v[r] = lds64(vAddr + (uint32_t)(w * R + r) * 8u);
+						v[r] = lds64c(vAddr + (uint32_t)(w * R + r) * 8u, vAddr, vHi, a.devErr);
 				}
 			};
 			if constexpr (NE == 1) {
@@ -265,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				const uint32_t colAddr = smemAddr(tile + ((pe + rot1) & (E - 1)));
 #pragma unroll 4
 				for (int w = ph; w < W0; w += H) {
-					const float2 av = lds64(colAddr + (uint32_t)w * rowB);
+					const float2 av = lds64c(colAddr + (uint32_t)w * rowB, tLo, tHi, a.devErr);
 					float2 v[R];
 					loadV(w, v);
 #pragma unroll
@@ -276,7 +279,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				}
 #pragma unroll 4
 				for (int w = wStart1; w < W; w += H) {
-					const float2 av = lds64(colAddr + (uint32_t)w * rowB);
+					const float2 av = lds64c(colAddr + (uint32_t)w * rowB, tLo, tHi, a.devErr);
 					float2 v[R];
 					loadV(w, v);
 #pragma unroll
@@ -319,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				// coherent sums of both events, FP32 FMA chains as in the
 				// one-event variant: S[r][ev] per reflectivity
 				auto mac = [&](int w, float2 (&Sx)[R][2]) {
-					const float4 av = lds128(colAddr + (uint32_t)w * rowB);
+					const float4 av = lds128c(colAddr + (uint32_t)w * rowB, tLo, tHi, a.devErr);
 					float2 v[R];
 					loadV(w, v);
 #pragma unroll
@@ -384,8 +387,11 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 #pragma unroll
 						for (int e = 0; e < 2; ++e) {
 							const float tx = c * S[r][e].x, ty = c * S[r][e].y;
-							T[(r * 2 + e) * E + pe1] = make_float2(tx, ty);
-							Tw[(r * 2 + e) * E + pe1] = make_float2(ty, tx);
+							const int ti = (r * 2 + e) * E + pe1;
+							if (smemInBounds(smemAddr(T + ti), 8u, smemAddr(T), smemAddr(T + R * 2 * E), a.devErr)) {
+								T[ti] = make_float2(tx, ty);
+								Tw[ti] = make_float2(ty, tx);
+							}
 						}
 				}
 			}
@@ -405,13 +411,15 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				float4 t[R], tw[R];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
-					t[r] = lds128(tBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u);
-					tw[r] = lds128(twBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u);
+					t[r] = lds128c(tBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u, smemAddr(T),
+					               smemAddr(T + R * 2 * E), a.devErr);
+					tw[r] = lds128c(twBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u, smemAddr(Tw),
+					                smemAddr(Tw + R * 2 * E), a.devErr);
 				}
 #pragma unroll
 				for (int wi = 0; wi < WPW; ++wi) {
 					if (wi < nWarpWaves) {
-						const float4 av = lds128(tAddr + (aOff[wi] ^ (uint32_t)(pp * 512)));
+						const float4 av = lds128c(tAddr + (aOff[wi] ^ (uint32_t)(pp * 512)), tLo, tHi, a.devErr);
 						const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
 #pragma unroll
 						for (int r = 0; r < R; ++r) {

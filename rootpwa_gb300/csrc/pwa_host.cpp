@@ -20,6 +20,7 @@
 #include <limits>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <random>
 #include <sstream>
@@ -905,8 +906,11 @@ int hostEval(pwa_likelihood* L, const double* par, double* f, double* grad, int 
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "FdF sync"));
 	const double* out = L->hOut.as<double>();
 	if (out[P + 1] != 0.) {
+		const unsigned flags = (unsigned)out[P + 1];
 		cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s);
 		cudaStreamSynchronize(s);
+		if (flags & kDevErrBounds)
+			return setError(kErrNumerical, "debug build: a shared-memory access of the FdF kernel failed its bounds check");
 		return setError(kErrTimeout, "a bounded device-side wait expired in the FdF kernel");
 	}
 	if (f)
@@ -940,7 +944,36 @@ struct TuneKey {
 		return std::tie(W, W0, R, evClass) < std::tie(o.W, o.W0, o.R, o.evClass);
 	}
 };
-std::map<TuneKey, std::pair<int, int> > g_tuned;  // -> (pipeline stages, phase-1 events per lane)
+std::map<TuneKey, std::pair<int, int> > g_tuned;  // -> (pipeline stages, kernel variant)
+std::mutex g_tunedMutex;
+
+bool tunedLookup(const TuneKey& key, std::pair<int, int>* v)
+{
+	std::lock_guard<std::mutex> lock(g_tunedMutex);
+	auto it = g_tuned.find(key);
+	if (it == g_tuned.end())
+		return false;
+	*v = it->second;
+	return true;
+}
+
+void tunedStore(const TuneKey& key, std::pair<int, int> v)
+{
+	std::lock_guard<std::mutex> lock(g_tunedMutex);
+	g_tuned[key] = v;
+}
+
+// name of the current CUDA device, empty without one
+std::string deviceName()
+{
+	int dev = 0;
+	cudaDeviceProp prop;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+		cudaGetLastError();
+		return std::string();
+	}
+	return std::string(prop.name);
+}
 
 // Times every candidate (tile size, pipeline depth) on the handle's own data
 // with a fixed parameter point and keeps the fastest.
@@ -950,10 +983,10 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 	for (uint64_t n = L->nEvents; n > 1; n >>= 1)
 		++evClass;
 	const TuneKey key{L->W(), L->nW[0], L->rank, evClass};
-	auto it = g_tuned.find(key);
-	if (it != g_tuned.end()) {
+	std::pair<int, int> known;
+	if (tunedLookup(key, &known)) {
 		for (const auto& c : cands)
-			if (c.stages == it->second.first && c.phase1Events == it->second.second)
+			if (c.stages == known.first && c.phase1Events == known.second)
 				L->plan = c;
 		return kOk;
 	}
@@ -986,7 +1019,7 @@ int autotunePlan(pwa_likelihood* L, const std::vector<FdfPlan>& cands)
 			bestPlan = cands[ci];
 		}
 	L->plan = bestPlan;
-	g_tuned[key] = std::make_pair(bestPlan.stages, bestPlan.phase1Events);
+	tunedStore(key, std::make_pair(bestPlan.stages, bestPlan.phase1Events));
 	// the tuning runs leave no device error behind
 	unsigned err = 0;
 	PWA_TRY(cudaCheck(cudaMemcpy(&err, L->dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "error flag"));
@@ -1179,6 +1212,99 @@ int pwa_likelihood_load_amp_files(pwa_likelihood* L, uint32_t nFiles, const char
 		}
 		PWA_TRY(pwa_likelihood_add_amplitude(L, w.c_str(), row.p, total, PWA_COMPLEX64, PWA_MEMORY_DEVICE));
 	}
+	return kOk;
+}
+
+// Autotuner cache file: JSON with the device it was measured on and one
+// object per tuned FdF shape, one per line:
+//   {"device": "<name>", "fdf_plans": [
+//   {"waves": W, "negative_waves": W0, "rank": R, "event_class": c, "stages": s, "variant": v},
+//   ...]}
+int pwa_autotune_cache_save(const char* path)
+{
+	if (!path)
+		return setError(kErrArg, "null path");
+	std::map<TuneKey, std::pair<int, int> > snap;
+	{
+		std::lock_guard<std::mutex> lock(g_tunedMutex);
+		snap = g_tuned;
+	}
+	std::string dev = deviceName();
+	for (char& c : dev)
+		if (c == '"' || c == '\\')
+			c = '_';
+	FILE* fp = std::fopen(path, "w");
+	if (!fp)
+		return setError(kErrIo, std::string("cannot create '") + path + "'");
+	std::fprintf(fp, "{\"device\": \"%s\", \"fdf_plans\": [\n", dev.c_str());
+	size_t k = 0;
+	for (const auto& kv : snap)
+		std::fprintf(fp,
+		             "{\"waves\": %u, \"negative_waves\": %u, \"rank\": %u, \"event_class\": %u, \"stages\": %d, "
+		             "\"variant\": %d}%s\n",
+		             kv.first.W, kv.first.W0, kv.first.R, kv.first.evClass, kv.second.first, kv.second.second,
+		             ++k < snap.size() ? "," : "");
+	std::fprintf(fp, "]}\n");
+	if (std::fclose(fp) != 0)
+		return setError(kErrIo, std::string("cannot write '") + path + "'");
+	return kOk;
+}
+
+int pwa_autotune_cache_load(const char* path)
+{
+	if (!path)
+		return setError(kErrArg, "null path");
+	std::ifstream in(path);
+	if (!in)
+		return setError(kErrIo, std::string("cannot open '") + path + "'");
+	std::string line;
+	if (!std::getline(in, line))
+		return setError(kErrIo, std::string("'") + path + "' is empty");
+	const std::string tag = "{\"device\": \"";
+	const size_t q = line.find('"', tag.size());
+	if (line.compare(0, tag.size(), tag) != 0 || q == std::string::npos)
+		return setError(kErrIo, std::string("'") + path + "' is not an autotuner cache");
+	const std::string fileDev = line.substr(tag.size(), q - tag.size());
+	std::string dev = deviceName();
+	for (char& c : dev)
+		if (c == '"' || c == '\\')
+			c = '_';
+	if (!dev.empty() && !fileDev.empty() && dev != fileDev)
+		return setError(kErrArg, "autotuner cache '" + std::string(path) + "' was measured on " + fileDev +
+		                             ", this device is " + dev);
+	std::map<TuneKey, std::pair<int, int> > read;
+	while (std::getline(in, line)) {
+		if (line.compare(0, 2, "]}") == 0)
+			break;
+		unsigned W, W0, R, ev;
+		int st, var;
+		if (std::sscanf(line.c_str(),
+		                "{\"waves\": %u, \"negative_waves\": %u, \"rank\": %u, \"event_class\": %u, \"stages\": %d, "
+		                "\"variant\": %d}",
+		                &W, &W0, &R, &ev, &st, &var) != 6 ||
+		    st < 1 || st > 4 || var < 1 || var > 3 || W0 > W || R < 1)
+			return setError(kErrIo, std::string("'") + path + "': malformed entry: " + line);
+		read[TuneKey{W, W0, R, ev}] = std::make_pair(st, var);
+	}
+	std::lock_guard<std::mutex> lock(g_tunedMutex);
+	for (const auto& kv : read)
+		g_tuned[kv.first] = kv.second;
+	return kOk;
+}
+
+int pwa_autotune_cache_clear(void)
+{
+	std::lock_guard<std::mutex> lock(g_tunedMutex);
+	g_tuned.clear();
+	return kOk;
+}
+
+int pwa_autotune_cache_size(uint32_t* n)
+{
+	if (!n)
+		return setError(kErrArg, "null argument");
+	std::lock_guard<std::mutex> lock(g_tunedMutex);
+	*n = (uint32_t)g_tuned.size();
 	return kOk;
 }
 

@@ -39,8 +39,10 @@ int cudaCheck(cudaError_t e, const char* what);
 // counts kernel launches (reported through pwa_kernel_launch_count)
 void countLaunches(uint64_t n);
 
-// Device-side error flags written by bounded waits.
-enum { kDevErrTimeout = 1 };
+// Device-side error flags: a bounded wait expired; a shared-memory access
+// failed its bounds check (builds with PWA_DEBUG_CHECKS only; the access is
+// skipped).
+enum { kDevErrTimeout = 1, kDevErrBounds = 2 };
 
 // ---------------------------------------------------------------------------
 // Amplitude store
