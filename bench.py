@@ -65,9 +65,21 @@ def parse():
     ap.add_argument("--train-bins", type=int, default=20_000, help="multibin: synthetic training bins")
     ap.add_argument("--augment", type=int, default=3, help="multibin: phase-rotated copies per training bin")
     ap.add_argument("--epochs", type=int, default=30, help="multibin: training epochs")
+    ap.add_argument("--metrics-log", default=None,
+                    help="also append the JSON line (with a UTC time stamp) to this JSON-lines file")
     ap.add_argument("--gtol-rel", type=float, default=1e-10,
                     help="multibin: L-BFGS stops when |grad| <= 1e-6 + gtol_rel * max(1, |f|)")
     return ap.parse_args()
+
+
+def emit(line, args):
+    """Prints the result line; with --metrics-log also appends it, time-stamped,
+    to a JSON-lines metrics file."""
+    print(json.dumps(line))
+    if getattr(args, "metrics_log", None):
+        rec = dict(line, time_utc=time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()))
+        with open(args.metrics_log, "a") as f:
+            f.write(json.dumps(rec) + "\n")
 
 
 def dist_env():
@@ -214,7 +226,7 @@ def run_reference(args):
                        "waves": 88, "rank": RANK, "events": args.n_data, "parameters": len(par)},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    emit(line, args)
     return 0
 
 
@@ -405,7 +417,7 @@ def run_gb300(args):
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "extra": {"integral_norm_s": integral_s, "integral_precision": args.integral_precision,
                           "mc_events": args.n_mc}}
-        print(json.dumps(line))
+        emit(line, args)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -574,7 +586,7 @@ def run_multibin(args):
             "training": {"generate_s": gen_s, "train_s": train_s, "loss_first": float(hist[0]),
                          "loss_last": float(hist[-1])},
             "setup_s": setup_s}
-    print(json.dumps(line))
+    emit(line, args)
     return 0
 
 
@@ -684,7 +696,7 @@ def run_precision(args):
                                                                      np.max(np.abs(base[1])))}
     line = {"metric": "precision sweep (errors against FP64)", "workload": "compass88: 87 waves + flat, rank 2, "
             "%d data / %d MC events" % (args.n_data, args.n_mc), "data": "synthetic", "results": out}
-    print(json.dumps(line))
+    emit(line, args)
     return 0
 
 
