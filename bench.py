@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--n-data", type=int, default=1_000_000)
     ap.add_argument("--n-mc", type=int, default=5_000_000)
     ap.add_argument("--reduction", default="fp64", choices=["fp64", "kahan_fp32"])
-    ap.add_argument("--integral-precision", default="tf32x3", choices=["fp64", "fp32", "tf32", "tf32x3"],
+    ap.add_argument("--integral-precision", default="tf32x3", choices=["fp64", "fp32", "tf32", "tf32x3", "bf16x3"],
                     help="arithmetic of the normalisation / acceptance integrals (set-up, not timed)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
@@ -606,7 +606,7 @@ def run_precision(args):
     model = synth.AmplitudeModel(W, 8, rng)
     P = synth.n_pars(N_NEG, N_POS, RANK)
     par = rng.standard_normal(P)
-    precs = ["fp32", "tf32", "tf32x3"]
+    precs = ["fp32", "tf32", "tf32x3", "bf16x3"]
 
     def maxrel(a, b):
         return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
@@ -625,10 +625,21 @@ def run_precision(args):
     # integrals at full size against the GPU FP64 kernel
     mc = synth.draw_device(model, args.n_mc, seed=1011)
     ints = {}
+    out["integral_ms"] = {"mc_events": args.n_mc, "timing": "host-timed integrate() of device-resident "
+                          "amplitudes, best of 3 after one warm-up call"}
     for p in ["fp64"] + precs:
         I = R.ampIntegralMatrix()
         I.integrate(names, mc, precision=p)
         ints[p] = I
+        best = 1e30
+        for _ in range(3):
+            J = R.ampIntegralMatrix()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            J.integrate(names, mc, precision=p)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        out["integral_ms"][p] = best * 1e3
     out["integral_vs_fp64"] = {"mc_events": args.n_mc}
     for p in precs:
         out["integral_vs_fp64"][p] = maxrel(ints[p].matrix(), ints["fp64"].matrix())

@@ -20,6 +20,9 @@
 //     rounded up to 16, K = 8 per instruction) into two FP32 accumulators
 //     (Re, D) in tensor memory; TF32x3 adds the cross products hi lo^T and
 //     lo hi^T before hi hi^T.
+// BF16x3 uses tiles of 64 events (one 128-byte swizzle row of BF16), hi =
+// bf16(x), lo = bf16(x - hi), and tcgen05.mma kind::f16 with BF16 operands
+// (K = 16 per instruction) for the same three products.
 // The tensor cores add into FP32 accumulators with truncation, so a long
 // chain of accumulations drifts towards zero by a fraction of an ulp per
 // instruction.  The accumulators therefore start from zero every `period`
@@ -37,6 +40,7 @@
 #include "pwa_internal.h"
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <mutex>
@@ -52,6 +56,7 @@ namespace {
 	} while (0)
 
 constexpr int kKT = 32;                   // events per tile (128-byte swizzle row of TF32)
+constexpr int kKTB = 64;                  // events per tile of the BF16 variant (128-byte row of BF16)
 constexpr int kConvWarps = 8;             // converter warps 0..7
 constexpr int kTmaWarp = kConvWarps;      // warp 8
 constexpr int kMmaWarp = kConvWarps + 1;  // warp 9
@@ -66,7 +71,9 @@ struct TcArgs {
 	uint64_t K;         // events (columns)
 	int W;              // waves (<= 128)
 	int N;              // MMA N: W rounded up to 16
-	int planes;         // 1 (TF32) or 2 (TF32x3: hi, lo)
+	int planes;         // 1 (TF32) or 2 (TF32x3, BF16x3: hi, lo)
+	int bf16;           // BF16 operands (kind::f16), 64-event tiles
+	int kt;             // events per tile: kKT or kKTB
 	int stages;         // raw TMA stages
 	int period;         // tiles between drains of the accumulators
 	uint64_t tilesTotal;
@@ -159,6 +166,23 @@ __host__ __device__ constexpr uint32_t idescTf32(int M, int N)
 	return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// instruction descriptor of kind::f16 with BF16 operands: D format F32 at
+// [4,6), A and B format BF16 (1) at [7,10) and [10,13), both K-major,
+// N >> 3 at [17,23), M >> 4 at [24,29)
+__host__ __device__ constexpr uint32_t idescBf16(int M, int N)
+{
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mmaBf16(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dTmem),
+	    "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(acc)
+	    : "memory");
+}
+
 __device__ __forceinline__ void mmaTf32(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, uint32_t acc)
 {
 	asm volatile(
@@ -179,6 +203,20 @@ __device__ __forceinline__ void mmaCommit(uint64_t* bar)
 __device__ __forceinline__ uint32_t swzOffset(int r, int k)
 {
 	return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + (k & 3) * 4);
+}
+
+// the same for BF16 elements (k < 64): 8 elements per 16-byte chunk
+__device__ __forceinline__ uint32_t swzOffset16(int r, int k)
+{
+	return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 3) ^ (r & 7)) & 7) << 4) + (k & 7) * 2);
+}
+
+// BF16 bits of x rounded to nearest even, and the FP32 value of those bits
+__device__ __forceinline__ uint32_t bf16Bits(float x, float* back)
+{
+	const __nv_bfloat16 h = __float2bfloat16_rn(x);
+	*back = __bfloat162float(h);
+	return (uint32_t)__bfloat16_as_ushort(h);
 }
 
 __device__ __forceinline__ void tmemLd16(uint32_t taddr, uint32_t (&r)[16])
@@ -207,7 +245,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 	unsigned char* smem =
 	    reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
 	const int W = a.W, N = a.N;
-	const uint32_t rawBytes = (uint32_t)W * 256u;
+	const uint32_t rawBytes = (uint32_t)W * (uint32_t)a.kt * 8u;
 	const uint32_t rawStride = (rawBytes + 1023u) & ~1023u;
 	unsigned char* ops = smem;                                            // [kOpBufs][planes][256 rows x 128 B]
 	unsigned char* raw = ops + (size_t)kOpBufs * a.planes * kPlaneBytes;  // [stages][W][64 floats]
@@ -281,7 +319,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 				if (*(volatile unsigned*)&sFail)
 					break;
 				barExpectTx(&rawFull[s], rawBytes);
-				tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * kKT), 0, &rawFull[s]);
+				tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, &rawFull[s]);
 				++issued;
 			}
 			// the copies of this CTA land before it exits
@@ -291,15 +329,20 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 	} else if (warp == kMmaWarp) {
 		// ---- MMA issuer ----
 		if (lane == 0) {
-			const uint32_t idesc = idescTf32(128, N);
+			const uint32_t idesc = a.bf16 ? idescBf16(128, N) : idescTf32(128, N);
 			const uint32_t opBase = sAddr(ops);
 			const uint32_t accRe = tmem, accD = tmem + (uint32_t)N;
 			bool freshRe = true, freshD = true;
-			// one product over the tile: acc += A B^T, 4 instructions of K = 8
+			// one product over the tile: acc += A B^T, 4 instructions of 32
+			// bytes of K (8 TF32 or 16 BF16 elements)
 			auto product = [&](uint32_t acc, bool& fresh, uint32_t aOp, uint32_t bOp) {
-				for (int kk = 0; kk < kKT / 8; ++kk) {
-					mmaTf32(acc, smemDesc(aOp + (uint32_t)kk * 32u), smemDesc(bOp + (uint32_t)kk * 32u), idesc,
-					        fresh ? 0u : 1u);
+				for (int kk = 0; kk < 4; ++kk) {
+					if (a.bf16)
+						mmaBf16(acc, smemDesc(aOp + (uint32_t)kk * 32u), smemDesc(bOp + (uint32_t)kk * 32u), idesc,
+						        fresh ? 0u : 1u);
+					else
+						mmaTf32(acc, smemDesc(aOp + (uint32_t)kk * 32u), smemDesc(bOp + (uint32_t)kk * 32u), idesc,
+						        fresh ? 0u : 1u);
 					fresh = false;
 				}
 			};
@@ -406,6 +449,42 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 			const float* rs = reinterpret_cast<const float*>(raw + (size_t)s * rawStride);
 			unsigned char* hiP = ops + (size_t)b * a.planes * kPlaneBytes;
 			unsigned char* loP = hiP + kPlaneBytes;
+			if (a.bf16) {
+				// four events per lane: raw row of 64 (re, im) pairs -> BF16 hi, lo
+				const uint64_t kb = (t0 + t) * (uint64_t)kKTB + 4u * p;
+				float wq[4] = {1.f, 1.f, 1.f, 1.f};
+				if (a.weightK)
+#pragma unroll
+					for (int q = 0; q < 4; ++q)
+						wq[q] = (kb + q < a.K) ? sqrtf((float)a.weightK[kb + q]) : 0.f;
+				for (int w = 2 * warp + sub; w < W; w += 2 * kConvWarps) {
+					const float4 v0 = *reinterpret_cast<const float4*>(rs + w * 128 + 8 * p);
+					const float4 v1 = *reinterpret_cast<const float4*>(rs + w * 128 + 8 * p + 4);
+					const float re[4] = {v0.x * wq[0], v0.z * wq[1], v1.x * wq[2], v1.z * wq[3]};
+					const float im[4] = {v0.y * wq[0], v0.w * wq[1], v1.y * wq[2], v1.w * wq[3]};
+					uint32_t hr[4], hm[4], lr[4], lm[4];
+#pragma unroll
+					for (int q = 0; q < 4; ++q) {
+						float br, bm, dummy;
+						hr[q] = bf16Bits(re[q], &br);
+						hm[q] = bf16Bits(im[q], &bm);
+						lr[q] = bf16Bits(re[q] - br, &dummy);
+						lm[q] = bf16Bits(im[q] - bm, &dummy);
+					}
+					const uint32_t oRe = swzOffset16(w, 4 * p), oIm = swzOffset16(128 + w, 4 * p);
+					*reinterpret_cast<uint2*>(hiP + oRe) = make_uint2(hr[0] | (hr[1] << 16), hr[2] | (hr[3] << 16));
+					*reinterpret_cast<uint2*>(hiP + oIm) = make_uint2(hm[0] | (hm[1] << 16), hm[2] | (hm[3] << 16));
+					*reinterpret_cast<uint2*>(loP + oRe) = make_uint2(lr[0] | (lr[1] << 16), lr[2] | (lr[3] << 16));
+					*reinterpret_cast<uint2*>(loP + oIm) = make_uint2(lm[0] | (lm[1] << 16), lm[2] | (lm[3] << 16));
+				}
+				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+				__syncwarp();
+				if (lane == 0) {
+					barArrive(&rawEmpty[s]);
+					barArrive(&opFull[b]);
+				}
+				continue;
+			}
 			const uint64_t k0 = (t0 + t) * (uint64_t)kKT + 2u * p;
 			float w0 = 1.f, w1 = 1.f;
 			if (a.weightK) {
@@ -500,8 +579,8 @@ size_t gramTcScratchFloats(int W, int numSMs)
 int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, double* out, double* scratch,
                  size_t scratchDoubles)
 {
-	if (precision != 2 && precision != 3)
-		return setError(kErrUnsupported, "tensor-core Gram: precision must be TF32 or TF32x3");
+	if (precision != 2 && precision != 3 && precision != 4)
+		return setError(kErrUnsupported, "tensor-core Gram: precision must be TF32, TF32x3 or BF16x3");
 	if (g.amps64 || !g.amps)
 		return setError(kErrUnsupported, "tensor-core Gram: complex64 amplitudes required");
 	if (g.W < 1 || g.W > 128)
@@ -519,15 +598,17 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	a.K = g.K;
 	a.W = g.W;
 	a.N = ((g.W + 15) / 16) * 16;
-	a.planes = (precision == 3) ? 2 : 1;
-	a.period = (precision == 3) ? 1 : 8;
-	a.tilesTotal = (g.K + kKT - 1) / kKT;
+	a.planes = (precision == 2) ? 1 : 2;
+	a.period = (precision == 2) ? 8 : 1;
+	a.bf16 = (precision == 4) ? 1 : 0;
+	a.kt = a.bf16 ? kKTB : kKT;
+	a.tilesTotal = (g.K + a.kt - 1) / a.kt;
 	a.weightK = g.weightK;
 	a.devErr = g.devErr;
-	const size_t rawStride = ((size_t)g.W * 256 + 1023) & ~size_t(1023);
+	const size_t rawStride = ((size_t)g.W * a.kt * 8 + 1023) & ~size_t(1023);
 	const size_t fixed = 1024 /* alignment */ + (size_t)kOpBufs * a.planes * kPlaneBytes + 256 /* barriers */;
 	a.stages = 4;
-	while (a.stages > 2 && fixed + a.stages * rawStride > (size_t)maxSmem)
+	while (a.stages > 1 && fixed + a.stages * rawStride > (size_t)maxSmem)
 		--a.stages;
 	size_t smemBytes = fixed + a.stages * rawStride;
 	if (smemBytes > (size_t)maxSmem)
@@ -545,7 +626,7 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	CUtensorMap map;
 	const cuuint64_t dims[2] = {(cuuint64_t)(2 * g.K), (cuuint64_t)g.W};
 	const cuuint64_t strides[1] = {(cuuint64_t)(g.ldK * 8)};
-	const cuuint32_t box[2] = {64u, (cuuint32_t)g.W};
+	const cuuint32_t box[2] = {(cuuint32_t)(2 * a.kt), (cuuint32_t)g.W};
 	const cuuint32_t estr[2] = {1u, 1u};
 	const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(g.amps), dims, strides, box,
 	                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,

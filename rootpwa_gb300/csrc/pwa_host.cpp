@@ -223,7 +223,8 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device amplitudes"));
 	const uint64_t ldIn = nEvents * nSub;
 	const bool wantDouble = (precision == PWA_PRECISION_FP64 && ampType == PWA_COMPLEX128);
-	const bool tensorCore = (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3);
+	const bool tensorCore = (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3 ||
+	                         precision == PWA_PRECISION_BF16X3);
 	// the tensor-core kernel reads rows with TMA: even row stride (16-byte
 	// multiple) and a 16-byte aligned base
 	const uint64_t ldPad = tensorCore ? (K + (K & 1ull)) : K;
@@ -302,8 +303,6 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		st = launchGramTc(g, precision, sms, s, dOut.as<double>(), dPart.as<double>(), scratch);
 		if (st != kOk)
 			return st;
-	} else if (precision == PWA_PRECISION_BF16X3) {
-		return setError(kErrUnsupported, "BF16 split-precision tensor-core Gram kernel not available in this build");
 	} else {
 		const int tps = ((int)W + 63) / 64;
 		const int nTiles = tps * (tps + 1) / 2;

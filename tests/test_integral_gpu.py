@@ -2,8 +2,9 @@
 ampIntegralMatrix::integrate (decayAmplitude/ampIntegralMatrix.cc:300-489).
 
 Tolerance: max |I - I_ref| / max |I_ref| below 1e-12 for the FP64 variant,
-1e-6 for FP32 (SIMT) and the split-precision tensor-core variants, 5e-3 for
-single-pass TF32."""
+1e-6 for FP32 (SIMT) and TF32x3, 1e-5 for BF16x3 (hi hi + hi lo + lo hi with
+8-bit halves leaves out lo lo, about 2^-16 of a product, one-signed on the
+diagonal: 3e-6 measured), 5e-3 for single-pass TF32."""
 import numpy as np
 import pytest
 
@@ -14,7 +15,7 @@ import helpers
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-12, "fp32": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-6, "tf32": 5e-3}
+TOL = {"fp64": 1e-12, "fp32": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-5, "tf32": 5e-3}
 
 
 def maxrel(m, ref):
