@@ -55,7 +55,7 @@ def parse():
                     help="arithmetic of the normalisation / acceptance integrals (set-up, not timed)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
-    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision"],
+    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision", "next"],
                     help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
                          "learned warm start; precision: error of each arithmetic variant against FP64")
     ap.add_argument("--oracle-mc", type=int, default=200_000,
@@ -711,10 +711,140 @@ def run_precision(args):
     return 0
 
 
+def run_next(args):
+    """Measurements of the rows after the FdF path: the GPU Hessian at the
+    88-wave shapes (against the FP64 oracle's on a sample), loading a raw
+    amplitude file with on-the-fly binning, and the selection alone."""
+    import shutil
+    import torch
+    import rootpwa_gb300 as R
+    from rootpwa_gb300 import synth
+    from oracle.oracle import OracleIntegral, OracleLikelihood
+    names, refl = synth.wave_names(N_NEG, N_POS)
+    W = len(names)
+    rng = np.random.Generator(np.random.PCG64(1))
+    model = synth.AmplitudeModel(W, 8, rng)
+    P = synth.n_pars(N_NEG, N_POS, RANK)
+    par = rng.standard_normal(P)
+    out = {}
+
+    def host_best(fn, reps=3):
+        fn()
+        best = 1e30
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    # ---- Hessian (pwaLikelihood.cc:639-859) ----
+    mc = model.draw(np.random.Generator(np.random.PCG64(2)), 100_000)
+    oi = OracleIntegral()
+    assert oi.integrate(names, mc.astype(np.complex128))
+
+    def gpu_int():
+        I = R.ampIntegralMatrix()
+        I.setWaveNames(names)
+        I.setMatrix(oi.raw())
+        I.setNmbEvents(oi.nmb_events())
+        return I
+
+    def gpu_lik(d):
+        L = R.pwaLikelihood()
+        L.init(names, refl, None, RANK, 0.0)
+        L.addNormIntegral(gpu_int())
+        L.addAccIntegral(gpu_int())
+        for k, n in enumerate(names):
+            L.addAmplitude(n, d[k])
+        L.finishInit()
+        return L
+
+    data = synth.draw_device(model, args.n_data, seed=11)
+    L = gpu_lik(data)
+    t_h = host_best(lambda: L.Hessian(par))
+    n_sample = 20_000
+    sample = data[:, :n_sample].cpu().numpy()
+    O = OracleLikelihood()
+    assert O.init(names, refl, None, RANK, 0.0)
+    assert O.addNormIntegral(oi) and O.addAccIntegral(oi)
+    for k, n in enumerate(names):
+        assert O.addAmplitude(n, sample[k].astype(np.complex128))
+    assert O.finishInit()
+    t0 = time.perf_counter()
+    H0 = O.Hessian(par)
+    t_o = time.perf_counter() - t0
+    Hs = gpu_lik(torch.from_numpy(sample).cuda()).Hessian(par)
+    out["hessian"] = {
+        "events": args.n_data, "parameters": P,
+        "gpu_s": t_h,
+        "oracle_single_thread_s_per_event": t_o / n_sample,
+        "oracle_single_thread_s_extrapolated": t_o / n_sample * args.n_data,
+        "max_rel_err_vs_oracle_on_%d_events" % n_sample: float(np.max(np.abs(Hs - H0)) / np.max(np.abs(H0))),
+        "timing": "host-timed Hessian() call, best of 3 after one warm-up; oracle timed once on the sample",
+    }
+    del L
+    torch.cuda.empty_cache()
+
+    # ---- raw amplitude file + on-the-fly binning (pwaLikelihood.cc:1110-1288, :1391-1440) ----
+    tmp = tempfile.mkdtemp(prefix="pwa_amp_")
+    try:
+        host = data.cpu().numpy()
+        g = np.random.Generator(np.random.PCG64(3))
+        mass = g.uniform(0.5, 2.5, args.n_data)
+        tprime = g.exponential(0.3, args.n_data)
+        path = os.path.join(tmp, "events.amp")
+        R.writeAmplitudeFile(path, names, host, {"mass": mass, "tPrime": tprime})
+        nbytes = os.path.getsize(path)
+        bounds = {"mass": (1.0, 1.5), "tPrime": (0.1, 1.0)}
+
+        def load():
+            Lf = R.pwaLikelihood()
+            Lf.init(names, refl, None, RANK, 0.0)
+            Lf.addNormIntegral(gpu_int())
+            Lf.addAccIntegral(gpu_int())
+            Lf.loadAmplitudeFiles([path], bounds)
+            Lf.finishInit()
+            return Lf
+        Lf = load()
+        sel = Lf.otfSelected()
+        keep = (mass >= 1.0) & (mass < 1.5) & (tprime >= 0.1) & (tprime < 1.0)
+        assert sel == int(keep.sum())
+        t_load = host_best(load)
+        dcols = {"mass": torch.from_numpy(mass).cuda(), "tPrime": torch.from_numpy(tprime).cuda()}
+
+        def select():
+            Ls = R.pwaLikelihood()
+            Ls.init(names, refl, None, RANK, 0.0)
+            Ls.addNormIntegral(gpu_int())
+            Ls.addAccIntegral(gpu_int())
+            Ls.setOnTheFlyBinning(bounds, dcols)
+        t_sel = host_best(select)
+        out["amplitude_file"] = {
+            "file_bytes": nbytes, "events": args.n_data, "selected": sel,
+            "load_s": t_load, "load_GBps": nbytes / t_load / 1e9,
+            "note": "file in the page cache (loaded once before timing); load = setup of a likelihood from the "
+                    "file with the selection, finishInit included",
+            "selection_s": t_sel,
+            "selection_note": "likelihood init + both integrals + GPU selection over %d device-resident events "
+                              "x 2 variables" % args.n_data,
+        }
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    line = {"metric": "rows after the FdF path: Hessian, amplitude-file ingestion with on-the-fly binning",
+            "workload": "compass88: 87 waves + flat, rank 2, %d events" % args.n_data, "data": "synthetic",
+            "results": out}
+    emit(line, args)
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "next":
+        return run_next(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "multibin":
