@@ -53,7 +53,7 @@ namespace {
 // store's rotated order (storeIndex), moved by a single bulk copy.
 struct SmemLayout {
 	size_t rowStride;  // bytes per wave row
-	size_t tiles, vs, v64, ts, tsw, bars, done, total;
+	size_t tiles, vs, v64, ts, bars, done, total;
 };
 
 __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages)
@@ -65,8 +65,7 @@ __host__ __device__ inline SmemLayout smemLayout(int W, int R, int E, int stages
 	L.vs = up((size_t)stages * W * L.rowStride);
 	L.v64 = up(L.vs + (size_t)W * R * 8);
 	L.ts = up(L.v64 + (size_t)W * R * 16);
-	L.tsw = up(L.ts + 2 * (size_t)R * 2 * E * 8);
-	L.bars = up(L.tsw + 2 * (size_t)R * 2 * E * 8);
+	L.bars = up(L.ts + 2 * (size_t)R * 2 * E * 8);
 	L.done = L.bars + (size_t)stages * 8;
 	L.total = L.done + (size_t)stages * 4;
 	return L;
@@ -121,7 +120,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 	float2* Vs = reinterpret_cast<float2*>(smem + lay.vs);      // [W][R] (vx, vy)
 	double2* V64 = reinterpret_cast<double2*>(smem + lay.v64);  // [R][W] FP64, slot order
 	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);      // [2][R][2][E] c S
-	float2* Tsw = reinterpret_cast<float2*>(smem + lay.tsw);    // [2][R][2][E] c S, re/im swapped
 	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	unsigned* done = reinterpret_cast<unsigned*>(smem + lay.done);
 
@@ -230,7 +228,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		// shared-memory regions for the debug build's bounds checks
 		const uint32_t tLo = smemAddr(tile), tHi = tLo + stageBytes;
 		float2* T = Ts + (size_t)(k & 1ull) * R * 2 * E;
-		float2* Tw = Tsw + (size_t)(k & 1ull) * R * 2 * E;
 
 		// ---- phase 1: coherent sums, combined across the lanes of an event ----
 		{
@@ -390,7 +387,6 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 							const int ti = (r * 2 + e) * E + pe1;
 							if (smemInBounds(smemAddr(T + ti), 8u, smemAddr(T), smemAddr(T + R * 2 * E), a.devErr)) {
 								T[ti] = make_float2(tx, ty);
-								Tw[ti] = make_float2(ty, tx);
 							}
 						}
 				}
@@ -405,16 +401,15 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		// ---- phase 2: gradient contraction over the tile, one reflectivity per warp ----
 		if (a.withGrad) {
 			const uint32_t tAddr = smemAddr(tile);
-			const uint32_t tBase = smemAddr(T) + tOff, twBase = smemAddr(Tw) + tOff;
+			const uint32_t tBase = smemAddr(T) + tOff;
 #pragma unroll
 			for (int pp = 0; pp < EPAIRS; ++pp) {
-				float4 t[R], tw[R];
+				float4 t[R];
 #pragma unroll
 				for (int r = 0; r < R; ++r) {
 					t[r] = lds128c(tBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u, smemAddr(T),
 					               smemAddr(T + R * 2 * E), a.devErr);
-					tw[r] = lds128c(twBase + (uint32_t)(r * 2 * E + 64 * pp) * 8u, smemAddr(Tw),
-					                smemAddr(Tw + R * 2 * E), a.devErr);
+
 				}
 #pragma unroll
 				for (int wi = 0; wi < WPW; ++wi) {
@@ -425,8 +420,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 						for (int r = 0; r < R; ++r) {
 							Pp[wi][r] = ffma2(a0, make_float2(t[r].x, t[r].y), Pp[wi][r]);
 							Pp[wi][r] = ffma2(a1, make_float2(t[r].z, t[r].w), Pp[wi][r]);
-							Qp[wi][r] = ffma2(a0, make_float2(tw[r].x, tw[r].y), Qp[wi][r]);
-							Qp[wi][r] = ffma2(a1, make_float2(tw[r].z, tw[r].w), Qp[wi][r]);
+							// the swapped (ty, tx) pairs come from registers
+							Qp[wi][r] = ffma2(a0, make_float2(t[r].y, t[r].x), Qp[wi][r]);
+							Qp[wi][r] = ffma2(a1, make_float2(t[r].w, t[r].z), Qp[wi][r]);
 						}
 					}
 				}
