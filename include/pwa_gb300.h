@@ -187,11 +187,12 @@ int pwa_likelihood_set_autotune(pwa_likelihood* L, int enable);
 int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, int* blocks);
 /* selects the pipeline depth by hand after finishInit (2..4 as shared memory allows) */
 int pwa_likelihood_set_plan(pwa_likelihood* L, int stages);
-/* FdF kernel variant: 1 or 2 events per lane in the coherent-sum phase (two
- * adjacent events share each V load and one 128-bit amplitude load), 3 the
- * fused-gradient kernel (each warp contracts its own events' gradient from
- * registers; rank <= 2, 128-event tiles); 0 keeps the current one.  The
- * autotuner times all that fit. */
+/* FdF kernel variant: 1, 2 or 4 events per lane in the coherent-sum phase
+ * (adjacent events share each V load; 2 and 4 read them with 128-bit loads;
+ * 4 needs rank <= 2 and 128-event tiles), 3 the fused-gradient kernel (each
+ * warp contracts its own events' gradient from registers; rank <= 2,
+ * 128-event tiles); 0 keeps the current one.  The autotuner times all that
+ * fit. */
 int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events);
 int pwa_likelihood_plan_variant(const pwa_likelihood* L, int* phase1Events);
 /*

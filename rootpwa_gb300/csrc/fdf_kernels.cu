@@ -298,6 +298,83 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					}
 				pe1 = pe;
 				writer = ph == 0;
+			} else if constexpr (NE == 4) {
+				// four consecutive events per lane, 16 wave slices per quad of
+				// events: each V load serves four events.  A lane reads its
+				// quad as two 16-byte halves; lanes of the second quad of the
+				// warp read the upper half first, so that each quarter-warp
+				// (2 quads x 4 slices with distinct store rotations) covers
+				// all 32 banks once in both loads.
+				static_assert(E == 128, "four events per lane need 128-event tiles");
+				const int kLo = lane & 3, quad = (lane >> 2) & 1, sHi = (lane >> 3) & 3;
+				const int ph4 = kLo + 4 * sHi;          // wave slice: waves w = ph4 mod 16
+				const int pe0 = warp * EPW + 4 * quad;  // the quad's first event
+				const int rot1 = (int)storeRot((uint32_t)ph4, (uint32_t)E);
+				const uint32_t colA = smemAddr(tile + ((pe0 + rot1) & (E - 1)));
+				// slot 0 = the half loaded first (events pe0 + 2 quad, + 1)
+				const uint32_t off0 = colA + 16u * (uint32_t)quad, off1 = colA + 16u * (uint32_t)(1 - quad);
+				auto mac4 = [&](int w, float2 (&Sx)[2][2][R]) {
+					const float4 p0 = lds128c(off0 + (uint32_t)w * rowB, tLo, tHi, a.devErr);
+					const float4 p1 = lds128c(off1 + (uint32_t)w * rowB, tLo, tHi, a.devErr);
+					float2 v[R];
+					loadV(w, v);
+#pragma unroll
+					for (int r = 0; r < R; ++r) {
+						Sx[0][0][r].x = fmaf(v[r].x, p0.x, fmaf(-v[r].y, p0.y, Sx[0][0][r].x));
+						Sx[0][0][r].y = fmaf(v[r].x, p0.y, fmaf(v[r].y, p0.x, Sx[0][0][r].y));
+						Sx[0][1][r].x = fmaf(v[r].x, p0.z, fmaf(-v[r].y, p0.w, Sx[0][1][r].x));
+						Sx[0][1][r].y = fmaf(v[r].x, p0.w, fmaf(v[r].y, p0.z, Sx[0][1][r].y));
+						Sx[1][0][r].x = fmaf(v[r].x, p1.x, fmaf(-v[r].y, p1.y, Sx[1][0][r].x));
+						Sx[1][0][r].y = fmaf(v[r].x, p1.y, fmaf(v[r].y, p1.x, Sx[1][0][r].y));
+						Sx[1][1][r].x = fmaf(v[r].x, p1.z, fmaf(-v[r].y, p1.w, Sx[1][1][r].x));
+						Sx[1][1][r].y = fmaf(v[r].x, p1.w, fmaf(v[r].y, p1.z, Sx[1][1][r].y));
+					}
+				};
+				float2 SN[2][2][R], SP[2][2][R];  // [slot][event of the slot][rank], per reflectivity
+#pragma unroll
+				for (int q = 0; q < 2; ++q)
+#pragma unroll
+					for (int j = 0; j < 2; ++j)
+#pragma unroll
+						for (int r = 0; r < R; ++r)
+							SN[q][j][r] = SP[q][j][r] = make_float2(0.f, 0.f);
+#pragma unroll 1
+				for (int w = ph4; w < W0; w += 16)
+					mac4(w, SN);
+				const int wS1 = W0 + (((ph4 - W0) % 16) + 16) % 16;
+#pragma unroll 1
+				for (int w = wS1; w < W; w += 16)
+					mac4(w, SP);
+				// reduce-scatter over lane bit 16 (slot) and bit 8 (event of
+				// the slot), butterfly over bits 0-1: the lane ends with the
+				// sums of event pe0 + 2 (bs ^ quad) + be
+				const int bs = (lane >> 4) & 1, be = (lane >> 3) & 1;
+#pragma unroll
+				for (int r = 0; r < R; ++r)
+#pragma unroll
+					for (int e = 0; e < 2; ++e) {
+						const float2 (&Se)[2][2][R] = e ? SP : SN;
+						float2 k0 = bs ? Se[1][0][r] : Se[0][0][r];
+						float2 k1 = bs ? Se[1][1][r] : Se[0][1][r];
+						const float2 s0 = bs ? Se[0][0][r] : Se[1][0][r];
+						const float2 s1 = bs ? Se[0][1][r] : Se[1][1][r];
+						k0.x += __shfl_xor_sync(0xffffffffu, s0.x, 16);
+						k0.y += __shfl_xor_sync(0xffffffffu, s0.y, 16);
+						k1.x += __shfl_xor_sync(0xffffffffu, s1.x, 16);
+						k1.y += __shfl_xor_sync(0xffffffffu, s1.y, 16);
+						float2 keep = be ? k1 : k0;
+						const float2 send = be ? k0 : k1;
+						keep.x += __shfl_xor_sync(0xffffffffu, send.x, 8);
+						keep.y += __shfl_xor_sync(0xffffffffu, send.y, 8);
+#pragma unroll
+						for (int o = 1; o < 4; o <<= 1) {
+							keep.x += __shfl_xor_sync(0xffffffffu, keep.x, o);
+							keep.y += __shfl_xor_sync(0xffffffffu, keep.y, o);
+						}
+						S[r][e] = keep;
+					}
+				pe1 = pe0 + 2 * (bs ^ quad) + be;
+				writer = kLo == 0;
 			} else {
 				// two consecutive events per lane: one 128-bit load brings a
 				// wave's amplitudes of both, and each V load serves both.
@@ -606,14 +683,16 @@ int launchRN(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 		case 8: return launchVariant<R, 128, 8, NE>(p, a, s);
 		default: break;
 		}
-	} else if (p.E == 64) {
-		switch (p.wpw) {
-		case 2: return launchVariant<R, 64, 2, NE>(p, a, s);
-		case 4: return launchVariant<R, 64, 4, NE>(p, a, s);
-		case 6: return launchVariant<R, 64, 6, NE>(p, a, s);
-		case 8: return launchVariant<R, 64, 8, NE>(p, a, s);
-		case 14: return launchVariant<R, 64, 14, NE>(p, a, s);
-		default: break;
+	} else if constexpr (NE != 4) {  // four events per lane: 128-event tiles only
+		if (p.E == 64) {
+			switch (p.wpw) {
+			case 2: return launchVariant<R, 64, 2, NE>(p, a, s);
+			case 4: return launchVariant<R, 64, 4, NE>(p, a, s);
+			case 6: return launchVariant<R, 64, 6, NE>(p, a, s);
+			case 8: return launchVariant<R, 64, 8, NE>(p, a, s);
+			case 14: return launchVariant<R, 64, 14, NE>(p, a, s);
+			default: break;
+			}
 		}
 	}
 	return setError(kErrUnsupported, "no FdF kernel variant for this tile/wave bucket");
@@ -622,6 +701,10 @@ int launchRN(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 template <int R>
 int launchR(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {
+	if constexpr (R <= 2) {
+		if (p.phase1Events == 4)
+			return launchRN<R, 4>(p, a, s);
+	}
 	return p.phase1Events == 2 ? launchRN<R, 2>(p, a, s) : launchRN<R, 1>(p, a, s);
 }
 
@@ -664,9 +747,12 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 		p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, nTiles));
 		p.smemBytes = smemLayout(W, R, B, st).total;
 		// the default without autotuning first: two events per lane up to
-		// rank 2, one beyond (where two would spill registers)
-		const int order[2] = {R <= 2 ? 2 : 1, R <= 2 ? 1 : 2};
+		// rank 2, one beyond (where two would spill registers); four events
+		// per lane (128-event tiles, rank <= 2) is timed by the autotuner
+		const int order[3] = {R <= 2 ? 2 : 1, R <= 2 ? 1 : 2, (R <= 2 && B == 128) ? 4 : 0};
 		for (int ne : order) {
+			if (ne == 0)
+				continue;
 			p.phase1Events = ne;
 			out->push_back(p);
 		}
@@ -674,8 +760,9 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 	if (out->empty())
 		return setError(kErrUnsupported, "amplitude tile does not fit in shared memory");
 	// a single stage does not overlap copy and compute: drop it when deeper pipelines fit
-	if (out->size() > 2)
-		out->erase(out->begin(), out->begin() + 2);
+	const size_t perStage = (R <= 2 && B == 128) ? 3 : 2;
+	if (out->size() > perStage)
+		out->erase(out->begin(), out->begin() + perStage);
 	// the fused-gradient variant, with two or more stages where it fits
 	if (B == 128)
 		for (int st = 2; st <= 4; ++st) {

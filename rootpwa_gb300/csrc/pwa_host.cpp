@@ -1281,7 +1281,7 @@ int pwa_autotune_cache_load(const char* path)
 		                "{\"waves\": %u, \"negative_waves\": %u, \"rank\": %u, \"event_class\": %u, \"stages\": %d, "
 		                "\"variant\": %d}",
 		                &W, &W0, &R, &ev, &st, &var) != 6 ||
-		    st < 1 || st > 4 || var < 1 || var > 3 || W0 > W || R < 1)
+		    st < 1 || st > 4 || var < 1 || var > 4 || W0 > W || R < 1)
 			return setError(kErrIo, std::string("'") + path + "': malformed entry: " + line);
 		read[TuneKey{W, W0, R, ev}] = std::make_pair(st, var);
 	}
@@ -1375,8 +1375,9 @@ int pwa_likelihood_set_plan(pwa_likelihood* L, int stages)
 int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events)
 {
 	PWA_TRY(checkFinished(L));
-	if (phase1Events < 0 || phase1Events > 3)
-		return setError(kErrArg, "FdF kernel variant must be 1 or 2 (events per lane), 3 (fused gradient) or 0 (keep)");
+	if (phase1Events < 0 || phase1Events > 4)
+		return setError(kErrArg,
+		                "FdF kernel variant must be 1, 2 or 4 (events per lane), 3 (fused gradient) or 0 (keep)");
 	const int ne = phase1Events ? phase1Events : L->plan.phase1Events;
 	std::vector<FdfPlan> cands;
 	PWA_TRY(planCandidates((int)L->nW[0], (int)L->W(), (int)L->rank, (int)L->storeB, L->nEvents, L->numSMs, L->maxSmem,

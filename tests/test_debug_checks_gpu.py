@@ -31,7 +31,7 @@ for n_neg, n_pos, rank, n in shapes:
     w = stress_workload(n_neg, n_pos, rank, n, flat=1.0)
     O, G = pair(w)
     stages = G.plan()[1]
-    for ne in (1, 2, 3):
+    for ne in (1, 2, 3, 4):
         try:
             G.setPlan(stages, ne)
         except R.PwaError:
@@ -40,7 +40,7 @@ for n_neg, n_pos, rank, n in shapes:
         G.DoEval(w["par"])
         runs += 1
 print("debug-checked runs", runs)
-assert runs >= 12
+assert runs >= 15
 '''
 
 

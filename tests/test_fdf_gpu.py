@@ -101,12 +101,13 @@ def test_shapes_against_oracle(n_neg, n_pos, rank, n_data):
     w = stress_workload(n_neg, n_pos, rank, n_data, flat=1.0)
     O, G = pair(w)
     stages = G.plan()[1]
-    # every kernel variant the shape supports: one or two events per lane in
-    # the coherent-sum phase, and the fused-gradient kernel (rank <= 2,
-    # 128-event tiles)
+    # every kernel variant the shape supports: one, two or four (rank <= 2,
+    # 128-event tiles) events per lane in the coherent-sum phase, and the
+    # fused-gradient kernel (rank <= 2, 128-event tiles)
     fused_ok = rank <= 2 and G.plan()[0] == 128 and n_neg <= 16 and 1 <= n_pos <= 104
-    for ne in (1, 2, 3):
-        if ne == 3 and not fused_ok:
+    four_ok = rank <= 2 and G.plan()[0] == 128
+    for ne in (1, 2, 3, 4):
+        if (ne == 3 and not fused_ok) or (ne == 4 and not four_ok):
             with pytest.raises(R.PwaError):
                 G.setPlan(stages, ne)
             continue
