@@ -486,6 +486,19 @@ class pwaLikelihood:
     def resetFuncCallInfo(self):
         N.call("pwa_likelihood_reset_func_call_info", self._h)
 
+    def printFuncInfo(self, out=None):
+        """printFuncInfo (pwaLikelihood.cc:1765-1779): calls and times per
+        evaluation type, one line each (to `out`, default stdout)."""
+        import sys
+        out = out or sys.stdout
+        for name, call in (("FdF", N.CALL_FDF), ("Gradient", N.CALL_GRADIENT), ("DoEval", N.CALL_DOEVAL),
+                           ("DoDerivative", N.CALL_DODERIVATIVE), ("Hessian", N.CALL_HESSIAN)):
+            i = self.funcCallInfo(call)
+            out.write("%-12s: %d calls, %.6f s total, %.6f s in the event kernels, %.6f s normalisation\n"
+                      % (name, i["nmbCalls"], i["totalTime"], i["funcTime"], i["normTime"]))
+
+    getIntegralMatrices = integralMatrices
+
     def setTiming(self, enable=True):
         """Record CUDA events around each evaluation's two kernels."""
         N.call("pwa_likelihood_set_timing", self._h, int(bool(enable)))

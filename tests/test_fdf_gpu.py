@@ -150,6 +150,11 @@ def test_doeval_gradient_doderivative_consistent():
     assert d == pytest.approx(O.Gradient(q)[7], rel=1e-5, abs=1e-6 * np.max(np.abs(g)))
     info = G.funcCallInfo(0)
     assert info["nmbCalls"] >= 2 and info["funcTime"] > 0
+    import io
+    buf = io.StringIO()
+    G.printFuncInfo(buf)
+    lines = buf.getvalue().splitlines()
+    assert len(lines) == 5 and lines[0].startswith("FdF") and " calls," in lines[0]
 
 
 def test_deterministic_and_batch():
