@@ -187,6 +187,10 @@ int pwa_likelihood_set_autotune(pwa_likelihood* L, int enable);
 int pwa_likelihood_plan(const pwa_likelihood* L, int* tileEvents, int* stages, int* blocks);
 /* selects the pipeline depth by hand after finishInit (2..4 as shared memory allows) */
 int pwa_likelihood_set_plan(pwa_likelihood* L, int stages);
+/* events per block of the amplitude store (and FdF tile): 64 or 128, 0 for
+ * the automatic choice (128 when two tiles fit in shared memory); before the
+ * first addAmplitude().  Batched fits need 128. */
+int pwa_likelihood_set_store_block(pwa_likelihood* L, uint32_t events);
 /* FdF kernel variant: 1, 2 or 4 events per lane in the coherent-sum phase
  * (adjacent events share each V load; 2 and 4 read them with 128-bit loads;
  * 4 needs rank <= 2 and 128-event tiles), 3 the fused-gradient kernel (each

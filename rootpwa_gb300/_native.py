@@ -122,6 +122,7 @@ SIGNATURES = {
     "pwa_likelihood_plan": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
     "pwa_likelihood_set_plan": (i, [vp, i]),
     "pwa_likelihood_set_plan_variant": (i, [vp, i, i]),
+    "pwa_likelihood_set_store_block": (i, [vp, u32]),
     "pwa_likelihood_plan_variant": (i, [vp, C.POINTER(C.c_int)]),
     "pwa_likelihood_init": (i, [vp, u32, C.POINTER(cc), C.POINTER(i32), pd, u32, C.c_double]),
     "pwa_likelihood_add_norm_integral": (i, [vp, vp]),

@@ -60,6 +60,7 @@ struct pwa_likelihood {
 
 	uint64_t nEvents = 0;
 	uint32_t storeB = 128;  // events per store block (storeIndex)
+	uint32_t storeBRequest = 0;  // pwa_likelihood_set_store_block (0: automatic)
 	// on-the-fly binning: indices of the selected events of the data file
 	bool otfSet = false;
 	uint64_t otfFileEvents = 0, otfSelected = 0;
@@ -670,6 +671,18 @@ int pwa_likelihood_set_stream(pwa_likelihood* L, void* s)
 	return kOk;
 }
 
+int pwa_likelihood_set_store_block(pwa_likelihood* L, uint32_t events)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (events != 0 && events != 64 && events != 128)
+		return setError(kErrArg, "store block must be 64 or 128 events (0: automatic)");
+	if (L->nEvents != 0)
+		return setError(kErrState, "the store block is fixed by the first addAmplitude()");
+	L->storeBRequest = events;
+	return kOk;
+}
+
 int pwa_likelihood_set_autotune(pwa_likelihood* L, int enable)
 {
 	if (!L)
@@ -900,7 +913,8 @@ int pwa_likelihood_add_amplitude(pwa_likelihood* L, const char* waveName, const 
 	}
 	if (L->nEvents == 0) {
 		L->nEvents = n;
-		L->storeB = (uint32_t)chooseStoreBlock((int)L->W(), (int)L->rank, L->maxSmem);
+		L->storeB = L->storeBRequest ? L->storeBRequest
+		                             : (uint32_t)chooseStoreBlock((int)L->W(), (int)L->rank, L->maxSmem);
 		const uint64_t nBlocks = (n + L->storeB - 1) / L->storeB;
 		PWA_TRY(L->amps.alloc((size_t)nBlocks * L->W() * L->storeB * sizeof(float2), "amplitude store"));
 		PWA_TRY(cudaCheck(cudaMemsetAsync(L->amps.p, 0, L->amps.bytes, s), "amplitude store memset"));

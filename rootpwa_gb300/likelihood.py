@@ -311,6 +311,11 @@ class pwaLikelihood:
         2 events per lane; 0 keeps the current one) by hand (after finishInit)."""
         N.call("pwa_likelihood_set_plan_variant", self._h, int(stages), int(phase1Events))
 
+    def setStoreBlock(self, events):
+        """Events per amplitude-store block / FdF tile (64 or 128; 0 automatic),
+        before the first addAmplitude."""
+        N.call("pwa_likelihood_set_store_block", self._h, int(events))
+
     def planVariant(self):
         """Events per lane of the FdF kernel's coherent-sum phase (1 or 2)."""
         v = C.c_int()

@@ -164,6 +164,9 @@ def test_setup_order_is_enforced():
         R.pwaLikelihood().init(["a", "a"], [1, 1])
     with pytest.raises(R.PwaError):
         R.pwaLikelihood().init(["a"], [0])
+    with pytest.raises(R.PwaError):
+        R.pwaLikelihood().setStoreBlock(100)  # 64 or 128 events only
+    R.pwaLikelihood().setStoreBlock(64)
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-GPU failure path")

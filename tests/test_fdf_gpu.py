@@ -323,3 +323,23 @@ def test_event_shards_sum_to_full_fdf(use_normalized, prior):
     f0, g0 = full.FdF(w["par"])
     assert helpers.rel(f, f0) < 1e-6
     assert helpers.normwise(g, g0) < 1e-5
+
+
+def test_store_block_64_matches_oracle():
+    """The 64-event store/tile layout (chosen automatically for wide wave
+    sets, or by setStoreBlock) gives the same FdF as the oracle."""
+    w = stress_workload(7, 80, 2, 30_001, flat=1.0)
+    norm, acc, gn, ga = helpers.integral_pairs(w)
+    O = helpers.build_oracle(w, norm, acc)
+    G = R.pwaLikelihood()
+    G.setStoreBlock(64)
+    G.init(w["names"], w["refl"], None, w["rank"], 0.0)
+    G.addNormIntegral(gn)
+    G.addAccIntegral(ga)
+    for k, n in enumerate(w["names"]):
+        G.addAmplitude(n, w["data"][k])
+    G.finishInit()
+    assert G.plan()[0] == 64
+    check_point(O, G, w["par"])
+    with pytest.raises(R.PwaError):
+        G.setStoreBlock(128)  # fixed by the first addAmplitude
