@@ -13,7 +13,10 @@
 //                       L = |S|^2 + V_flat^2, -ln L and c S (c = -2/L); phase 2
 //                       G_{s,w} += sum_e c S_{s,e} conj(A_{w,e});
 //                       per-thread FP32 (compensated for -ln L and c) over up
-//                       to 8 tiles, then FP64; FP64 partials per item;
+//                       to 8 tiles, then FP64; FP64 partials per item.
+//                       Groups of 32 starts use two tile stages and one block
+//                       per SM; groups of 8 (little work per tile) one stage
+//                       and three blocks per SM, which take turns;
 //   batchFinishKernel -- one warp per problem: sums the items' partials in item
 //                       order (deterministic), adds nEvt (Re V^H I^acc V +
 //                       V_flat^2 eta) and the half-Cauchy prior in FP64
@@ -41,12 +44,12 @@ struct BatchSmem {
 	size_t stages, vs, ts, flat, bars, total;
 };
 
-__host__ __device__ inline BatchSmem batchSmem(int W, int SG)
+__host__ __device__ inline BatchSmem batchSmem(int W, int SG, int NST)
 {
 	BatchSmem L{};
 	auto up = [](size_t x) { return (x + 127) & ~size_t(127); };
 	L.stages = 0;
-	L.vs = up((size_t)2 * W * kBE * 8);
+	L.vs = up((size_t)NST * W * kBE * 8);
 	L.ts = up(L.vs + (size_t)W * SG * 16);
 	L.flat = up(L.ts + (size_t)2 * kBE * SG * 8);
 	L.bars = up(L.flat + (size_t)SG * 4);
@@ -55,10 +58,14 @@ __host__ __device__ inline BatchSmem batchSmem(int W, int SG)
 }
 
 // SG starts per group; phase 1: SPT starts x EPT events per thread;
-// phase 2: SPT2 starts x WPT waves per thread (waves < 64).
-template <int SG, int SPT, int EPT, int SPT2, int WPT>
-__global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a)
+// phase 2: SPT2 starts x WPT waves per thread (waves < 64).  NST tile stages
+// per block: 2 (the next tile loads while this one is used) or 1 (several
+// blocks per SM, MINB, take turns instead; for small start groups, whose
+// blocks have little work per tile).
+template <int SG, int SPT, int EPT, int SPT2, int WPT, int NST, int MINB>
+__global__ void __launch_bounds__(kBThreads, MINB) fdfBatchKernel(const BatchArgs a)
 {
+	static_assert(NST == 1 || NST == 2, "one or two tile stages");
 	static_assert((SG / SPT) * (kBE / EPT) == kBThreads, "phase-1 mapping");
 	static_assert((SG / SPT2) * (64 / WPT) == kBThreads, "phase-2 mapping");
 	static_assert(EPT % 2 == 0 && SPT2 % 2 == 0 && SPT % 2 == 0, "paired loads");
@@ -66,8 +73,8 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 	constexpr int NQ = SG / SPT;  // start groups of SPT (phase-1 sq, phase-2 sp)
 	extern __shared__ __align__(128) unsigned char smem[];
 	const int W = a.W, P = a.P;
-	const BatchSmem lay = batchSmem(W, SG);
-	float2* stages = reinterpret_cast<float2*>(smem + lay.stages);  // [2][W][kBE]
+	const BatchSmem lay = batchSmem(W, SG, NST);
+	float2* stages = reinterpret_cast<float2*>(smem + lay.stages);  // [NST][W][kBE]
 	// V of start s = q * SPT + i at [w][i][q] (vx, vx, vy, vy): a quarter-warp
 	// (q = 0..7) reads 128 contiguous bytes
 	float4* Vs = reinterpret_cast<float4*>(smem + lay.vs);
@@ -124,7 +131,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 		const uint32_t ph0[2] = {phase[0], phase[1]};
 		if (tid == 0) {
 			fenceProxyAsync();
-			for (int k = 0; k < 2 && k < nt; ++k) {
+			for (int k = 0; k < NST && k < nt; ++k) {
 				mbarArriveExpectTx(&bars[k], tileBytes);
 				bulkCopyG2S(stages + (size_t)k * W * kBE, bin.amps + (size_t)(it.t0 + k) * W * kBE, tileBytes,
 				            &bars[k]);
@@ -152,7 +159,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 
 		int k = 0;
 		for (; k < nt; ++k) {
-			const int st = k & 1;
+			const int st = (NST == 2) ? (k & 1) : 0;
 			const bool ok = mbarWaitBounded(&bars[st], phase[st]);
 			phase[st] ^= 1u;
 			const float2* tile = stages + (size_t)st * W * kBE;
@@ -215,7 +222,7 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 				failed = true;
 				break;
 			}
-			if (tid == 0 && k >= 1 && k + 1 < nt) {
+			if (NST == 2 && tid == 0 && k >= 1 && k + 1 < nt) {
 				fenceProxyAsync();
 				const int ns2 = (k + 1) & 1;
 				mbarArriveExpectTx(&bars[ns2], tileBytes);
@@ -251,6 +258,15 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 					}
 				}
 			}
+			// one stage: the next tile loads once every thread is done with this one
+			if (NST == 1) {
+				__syncthreads();
+				if (tid == 0 && k + 1 < nt) {
+					fenceProxyAsync();
+					mbarArriveExpectTx(&bars[0], tileBytes);
+					bulkCopyG2S(stages, bin.amps + (size_t)(it.t0 + k + 1) * W * kBE, tileBytes, &bars[0]);
+				}
+			}
 			// fold the FP32 partials into FP64
 			if ((k + 1) % kBFold == 0 || k + 1 == nt) {
 #pragma unroll
@@ -273,9 +289,14 @@ __global__ void __launch_bounds__(kBThreads, 1) fdfBatchKernel(const BatchArgs a
 			if (tid == 0) {
 				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
 				// copies of this item still in flight land before the block
-				// exits: tiles k .. max(1, k) were issued and not consumed
-				for (int j = k; j <= max(1, k) && j < nt; ++j)
-					mbarWaitBounded(&bars[j & 1], ph0[j & 1] ^ (uint32_t)((j >> 1) & 1));
+				// exits: with two stages tiles k .. max(1, k) were issued and
+				// not consumed, with one stage tile k
+				if (NST == 2) {
+					for (int j = k; j <= max(1, k) && j < nt; ++j)
+						mbarWaitBounded(&bars[j & 1], ph0[j & 1] ^ (uint32_t)((j >> 1) & 1));
+				} else if (k < nt) {
+					mbarWaitBounded(&bars[0], ph0[0] ^ (uint32_t)(k & 1));
+				}
 			}
 			break;
 		}
@@ -609,49 +630,60 @@ __global__ void countActiveKernel(const int* status, int Q, int* active, unsigne
 	}
 }
 
-template <int SG, int SPT, int EPT, int SPT2, int WPT>
+template <int SG, int SPT, int EPT, int SPT2, int WPT, int NST, int MINB>
 int configureBatchT(int W)
 {
-	const BatchSmem lay = batchSmem(W, SG);
-	return cudaCheck(cudaFuncSetAttribute(fdfBatchKernel<SG, SPT, EPT, SPT2, WPT>,
+	const BatchSmem lay = batchSmem(W, SG, NST);
+	return cudaCheck(cudaFuncSetAttribute(fdfBatchKernel<SG, SPT, EPT, SPT2, WPT, NST, MINB>,
 	                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total),
 	                 "batch smem attribute");
 }
 
-template <int SG, int SPT, int EPT, int SPT2, int WPT>
-int launchBatchT(const BatchArgs& a, int grid, cudaStream_t s)
+// persistent grid: numSMs x the blocks of this variant that fit on an SM
+template <int SG, int SPT, int EPT, int SPT2, int WPT, int NST, int MINB>
+int launchBatchT(const BatchArgs& a, int numSMs, cudaStream_t s)
 {
-	const BatchSmem lay = batchSmem(a.W, SG);
-	fdfBatchKernel<SG, SPT, EPT, SPT2, WPT><<<grid, kBThreads, lay.total, s>>>(a);
+	auto kern = fdfBatchKernel<SG, SPT, EPT, SPT2, WPT, NST, MINB>;
+	const BatchSmem lay = batchSmem(a.W, SG, NST);
+	int perSM = 1;
+	if (NST == 1) {
+		const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, kBThreads, lay.total);
+		if (e != cudaSuccess)
+			return cudaCheck(e, "batch FdF occupancy");
+		perSM = std::max(1, std::min(perSM, MINB));
+	}
+	kern<<<numSMs * perSM, kBThreads, lay.total, s>>>(a);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "batch FdF launch");
 }
 
 }  // namespace
 
-size_t batchSmemBytes(int W, int SG) { return batchSmem(W, SG).total; }
+size_t batchSmemBytes(int W, int SG) { return batchSmem(W, SG, SG == 8 ? 1 : 2).total; }
 
+// start groups of 32: two stages, one block per SM; of 8: one stage, up to
+// three blocks per SM
 int configureBatchFdf(int W, int SG, size_t maxSmem)
 {
 	if (W < 1 || W > 64)
 		return setError(kErrUnsupported, "batched FdF supports 1..64 waves");
-	if (batchSmem(W, SG).total > maxSmem)
+	if (batchSmemBytes(W, SG) > maxSmem)
 		return setError(kErrUnsupported, "batched FdF: shared memory too small for this wave set");
 	if (SG == 32)
-		return configureBatchT<32, 4, 4, 4, 2>(W);
+		return configureBatchT<32, 4, 4, 4, 2, 2, 1>(W);
 	if (SG == 8)
-		return configureBatchT<8, 2, 2, 2, 1>(W);
+		return configureBatchT<8, 2, 2, 2, 1, 1, 3>(W);
 	return setError(kErrUnsupported, "batched FdF: start-group size must be 8 or 32");
 }
 
-int launchBatchFdf(const BatchArgs& a, int grid, cudaStream_t s)
+int launchBatchFdf(const BatchArgs& a, int numSMs, cudaStream_t s)
 {
 	if (a.W < 1 || a.W > 64)
 		return setError(kErrUnsupported, "batched FdF supports 1..64 waves");
 	if (a.SG == 32)
-		return launchBatchT<32, 4, 4, 4, 2>(a, grid, s);
+		return launchBatchT<32, 4, 4, 4, 2, 2, 1>(a, numSMs, s);
 	if (a.SG == 8)
-		return launchBatchT<8, 2, 2, 2, 1>(a, grid, s);
+		return launchBatchT<8, 2, 2, 2, 1, 1, 3>(a, numSMs, s);
 	return setError(kErrUnsupported, "batched FdF: start-group size must be 8 or 32");
 }
 

@@ -239,7 +239,7 @@ struct LbfgsArgs {
 size_t batchSmemBytes(int W, int SG);
 // sets the kernel's shared-memory limit (before any launch or stream capture)
 int configureBatchFdf(int W, int SG, size_t maxSmem);
-int launchBatchFdf(const BatchArgs& a, int grid, cudaStream_t s);
+int launchBatchFdf(const BatchArgs& a, int numSMs, cudaStream_t s);
 int launchBatchFinish(const FinishBatchArgs& a, cudaStream_t s);
 int launchLbfgs(const LbfgsArgs& a, cudaStream_t s);
 int launchCountActive(const int* status, int Q, int* active, unsigned* nActive, cudaStream_t s);
