@@ -204,6 +204,10 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 		kGc[q] = 0.f;
 	}
 	// P = sum a (.) t, Q = sum a (.) t_swapped  ->  G = (P.x + P.y, Q.x - Q.y)
+	// ranks 1-2: packed sums as above; ranks 3-4 keep (Gx, Gy) in Pp alone
+	// (half the accumulator registers, twice the FMA instructions), which
+	// keeps their larger accumulator sets out of local memory
+	constexpr bool kPacked = R <= 2;
 	float2 Pp[WPW][R], Qp[WPW][R];
 #pragma unroll
 	for (int wi = 0; wi < WPW; ++wi)
@@ -497,11 +501,19 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 						const float2 a0 = make_float2(av.x, av.y), a1 = make_float2(av.z, av.w);
 #pragma unroll
 						for (int r = 0; r < R; ++r) {
-							Pp[wi][r] = ffma2(a0, make_float2(t[r].x, t[r].y), Pp[wi][r]);
-							Pp[wi][r] = ffma2(a1, make_float2(t[r].z, t[r].w), Pp[wi][r]);
-							// the swapped (ty, tx) pairs come from registers
-							Qp[wi][r] = ffma2(a0, make_float2(t[r].y, t[r].x), Qp[wi][r]);
-							Qp[wi][r] = ffma2(a1, make_float2(t[r].w, t[r].z), Qp[wi][r]);
+							if constexpr (kPacked) {
+								Pp[wi][r] = ffma2(a0, make_float2(t[r].x, t[r].y), Pp[wi][r]);
+								Pp[wi][r] = ffma2(a1, make_float2(t[r].z, t[r].w), Pp[wi][r]);
+								// the swapped (ty, tx) pairs come from registers
+								Qp[wi][r] = ffma2(a0, make_float2(t[r].y, t[r].x), Qp[wi][r]);
+								Qp[wi][r] = ffma2(a1, make_float2(t[r].w, t[r].z), Qp[wi][r]);
+							} else {
+								// G += conj(a) t: (ax tx + ay ty, ax ty - ay tx)
+								Pp[wi][r].x = fmaf(a0.x, t[r].x, fmaf(a0.y, t[r].y, Pp[wi][r].x));
+								Pp[wi][r].y = fmaf(a0.x, t[r].y, fmaf(-a0.y, t[r].x, Pp[wi][r].y));
+								Pp[wi][r].x = fmaf(a1.x, t[r].z, fmaf(a1.y, t[r].w, Pp[wi][r].x));
+								Pp[wi][r].y = fmaf(a1.x, t[r].w, fmaf(-a1.y, t[r].z, Pp[wi][r].y));
+							}
 						}
 					}
 				}
@@ -546,8 +558,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				for (int wi = 0; wi < WPW; ++wi)
 #pragma unroll
 					for (int r = 0; r < R; ++r) {
-						part[(wi * R + r) * 2 + 0] = Pp[wi][r].x + Pp[wi][r].y;
-						part[(wi * R + r) * 2 + 1] = Qp[wi][r].x - Qp[wi][r].y;
+						part[(wi * R + r) * 2 + 0] = kPacked ? Pp[wi][r].x + Pp[wi][r].y : Pp[wi][r].x;
+						part[(wi * R + r) * 2 + 1] = kPacked ? Qp[wi][r].x - Qp[wi][r].y : Pp[wi][r].y;
 						Pp[wi][r] = make_float2(0.f, 0.f);
 						Qp[wi][r] = make_float2(0.f, 0.f);
 					}
