@@ -245,3 +245,41 @@ def test_oracle_matches_golden(name):
     assert np.array_equal(g, gold["grad"])
     if "hessian" in gold:
         assert np.array_equal(L.Hessian(w["par"]), gold["hessian"])
+
+
+@pytest.mark.parametrize("name,rank,seed", [("compass15", 1, 3), ("compass88", 2, 4), ("compass88", 3, 5)])
+def test_independent_numpy_restatement_of_the_value(name, rank, seed):
+    """A second, independent restatement of the extended likelihood in numpy
+    (pwaLikelihood.cc:209-276 with the normalisation of :1253-1260 and
+    :1311-1334, nEvt = 1) gives the oracle's value to 1e-12: the event term
+    -sum ln(sum_r sum_e |sum_{w in e} V_rw A_w / sqrt(N_ww)|^2 + V_flat^2) and
+    sum_r sum_e sum_ij Re(V_ri conj(V_rj) I_ij / sqrt(N_ii N_jj)) +
+    V_flat^2 eta over same-reflectivity blocks."""
+    w = synth.make_workload(name, seed=seed, n_data=600, n_mc=1200, rank=rank)
+    norm, acc = helpers.oracle_integrals(w)
+    n_gen = norm.nmb_events()
+    n_acc = acc.nmb_events()
+    N = norm.matrix()
+    I_acc = acc.raw() / float(n_gen)       # addAccIntegral sets the count to the generated events
+    eta = n_acc / float(n_gen)
+    L = helpers.build_oracle(w, norm, acc)
+    p = w["par"]
+    V = _prod_amps(w, p)                   # [rank][wave], reference layout
+    refl = np.array(w["refl"])
+    d = np.sqrt(np.real(np.diag(N)))
+    A = w["data"].astype(np.complex128) / d[:, None]
+    Ihat = I_acc / np.outer(d, d)
+    flat = p[-1]
+    intensity = np.full(A.shape[1], flat * flat)
+    norm_term = flat * flat * eta
+    for r in range(w["rank"]):
+        for e in (-1, 1):
+            m = refl == e
+            if not m.any():
+                continue
+            S = V[r, m] @ A[m]
+            intensity += np.abs(S) ** 2
+            Ie = Ihat[np.ix_(m, m)]
+            norm_term += np.real(V[r, m] @ Ie @ V[r, m].conj())
+    f_np = -np.sum(np.log(intensity)) + norm_term
+    assert L.DoEval(p) == pytest.approx(f_np, rel=1e-12)
