@@ -302,6 +302,14 @@ int pwa_likelihood_fdf_device(pwa_likelihood* L, const double* dPar, double* dOu
 int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* hessian);
 /* CovarianceMatrix(hessian) (pwaLikelihood.cc:929-981) */
 int pwa_likelihood_covariance_matrix(const pwa_likelihood* L, const double* hessian, double* covariance);
+/* HessianEigenVectors (pwaLikelihood.cc:864-912, called by pwaFit.cc:308,
+ * pwaNloptFit.cc:251 and pyInterface/module/_fit.py:197): eigenvalues and
+ * eigenvectors of the Hessian [P][P] restricted to the free parameters.
+ * eigenvalues [P]: the first *nFree entries, descending; eigenvectors [P][P]:
+ * row k is the eigenvector of eigenvalue k in the full parameter space (zero
+ * at fixed parameters; sign arbitrary).  Needs init() only. */
+int pwa_likelihood_hessian_eigenvectors(const pwa_likelihood* L, const double* hessian, double* eigenvalues,
+                                        double* eigenvectors, uint32_t* nFree);
 /* CorrectParamSigns (pwaLikelihood.cc:984-1010) */
 int pwa_likelihood_correct_param_signs(const pwa_likelihood* L, const double* par, double* out);
 /* getIntegralMatrices (pwaLikelihood.cc:1579-1622): norm and acc as

@@ -144,6 +144,7 @@ SIGNATURES = {
     "pwa_likelihood_fdf_device": (i, [vp, vp, vp, i, vp]),
     "pwa_likelihood_hessian": (i, [vp, pd, pd]),
     "pwa_likelihood_covariance_matrix": (i, [vp, pd, pd]),
+    "pwa_likelihood_hessian_eigenvectors": (i, [vp, pd, pd, pd, C.POINTER(u32)]),
     "pwa_likelihood_correct_param_signs": (i, [vp, pd, pd]),
     "pwa_likelihood_integral_matrices": (i, [vp, pd, pd, pd, i]),
     "pwa_likelihood_build_prod_amp_arrays": (i, [vp, pd, pd, C.POINTER(i32), C.POINTER(u32), i]),

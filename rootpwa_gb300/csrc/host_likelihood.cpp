@@ -1436,6 +1436,89 @@ int pwa_likelihood_covariance_matrix(const pwa_likelihood* L, const double* H, d
 	return kOk;
 }
 
+// HessianEigenVectors (pwaLikelihood.cc:864-912): eigen-decomposition of the
+// Hessian restricted to the free parameters, eigenvectors embedded in the
+// full parameter space with zeros at the fixed parameters.  Cyclic Jacobi
+// rotations in FP64 on the host (symmetric P x P, once per fit): each
+// rotation zeroes one off-diagonal pair; sweeps repeat until the
+// off-diagonal sum of squares is below 1e-30 of the total.  Eigenvalues in
+// descending order; the sign of each eigenvector is arbitrary.
+int pwa_likelihood_hessian_eigenvectors(const pwa_likelihood* L, const double* H, double* eigenvalues,
+                                        double* eigenvectors, uint32_t* nFree)
+{
+	if (!L || !H || !eigenvalues || !eigenvectors || !nFree)
+		return setError(kErrArg, "null argument");
+	if (!L->initialized)
+		return setError(kErrState, "likelihood not initialized");
+	const uint32_t P = L->nPars;
+	std::vector<uint32_t> fr;
+	for (uint32_t i = 0; i < P; ++i)
+		if (!L->pars[i].fixed)
+			fr.push_back(i);
+	const size_t n = fr.size();
+	std::vector<double> a(n * n), v(n * n, 0.);
+	double total = 0.;
+	for (size_t i = 0; i < n; ++i) {
+		for (size_t j = 0; j < n; ++j) {
+			// symmetrise: the Hessian is symmetric up to rounding
+			const double x = 0.5 * (H[(size_t)fr[i] * P + fr[j]] + H[(size_t)fr[j] * P + fr[i]]);
+			a[i * n + j] = x;
+			total += x * x;
+			if (!std::isfinite(x))
+				return setError(kErrNumerical, "Hessian has non-finite entries");
+		}
+		v[i * n + i] = 1.;
+	}
+	for (int sweep = 0; sweep < 100; ++sweep) {
+		double off = 0.;
+		for (size_t p = 0; p < n; ++p)
+			for (size_t q = p + 1; q < n; ++q)
+				off += a[p * n + q] * a[p * n + q];
+		if (off <= 1e-30 * total || off == 0.)
+			break;
+		for (size_t p = 0; p < n; ++p)
+			for (size_t q = p + 1; q < n; ++q) {
+				const double apq = a[p * n + q];
+				if (apq == 0.)
+					continue;
+				// rotation angle that zeroes a_pq: t = tan(phi) is the smaller
+				// root of t^2 + 2 theta t - 1 = 0, theta = (a_qq - a_pp) / (2 a_pq)
+				const double theta = (a[q * n + q] - a[p * n + p]) / (2. * apq);
+				const double t = (theta >= 0. ? 1. : -1.) / (std::fabs(theta) + std::sqrt(theta * theta + 1.));
+				const double c = 1. / std::sqrt(t * t + 1.), sn = t * c;
+				for (size_t k = 0; k < n; ++k) {  // columns p, q
+					const double akp = a[k * n + p], akq = a[k * n + q];
+					a[k * n + p] = c * akp - sn * akq;
+					a[k * n + q] = sn * akp + c * akq;
+				}
+				for (size_t k = 0; k < n; ++k) {  // rows p, q
+					const double apk = a[p * n + k], aqk = a[q * n + k];
+					a[p * n + k] = c * apk - sn * aqk;
+					a[q * n + k] = sn * apk + c * aqk;
+				}
+				for (size_t k = 0; k < n; ++k) {  // eigenvectors as columns of v
+					const double vkp = v[k * n + p], vkq = v[k * n + q];
+					v[k * n + p] = c * vkp - sn * vkq;
+					v[k * n + q] = sn * vkp + c * vkq;
+				}
+			}
+	}
+	std::vector<size_t> order(n);
+	for (size_t i = 0; i < n; ++i)
+		order[i] = i;
+	std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return a[x * n + x] > a[y * n + y]; });
+	std::fill(eigenvalues, eigenvalues + P, 0.);
+	std::fill(eigenvectors, eigenvectors + (size_t)P * P, 0.);
+	for (size_t k = 0; k < n; ++k) {
+		const size_t col = order[k];
+		eigenvalues[k] = a[col * n + col];
+		for (size_t i = 0; i < n; ++i)
+			eigenvectors[k * P + fr[i]] = v[i * n + col];
+	}
+	*nFree = (uint32_t)n;
+	return kOk;
+}
+
 int pwa_likelihood_correct_param_signs(const pwa_likelihood* L, const double* par, double* out)
 {
 	if (!L || !par || !out)

@@ -457,6 +457,18 @@ class pwaLikelihood:
         N.call("pwa_likelihood_covariance_matrix", self._h, _pd(H), _pd(Cm))
         return Cm
 
+    def HessianEigenVectors(self, hessian):
+        """HessianEigenVectors (pwaLikelihood.cc:864-912): [(eigenvector [P],
+        eigenvalue)] of the Hessian restricted to the free parameters,
+        eigenvalues descending, eigenvectors zero at fixed parameters."""
+        H = np.ascontiguousarray(hessian, dtype=np.float64)
+        n = self.nmbPars()
+        vals = np.zeros(n)
+        vecs = np.zeros((n, n))
+        k = C.c_uint32()
+        N.call("pwa_likelihood_hessian_eigenvectors", self._h, _pd(H), _pd(vals), _pd(vecs), C.byref(k))
+        return [(vecs[i].copy(), float(vals[i])) for i in range(k.value)]
+
     def CorrectParamSigns(self, par):
         p = self._par(par)
         out = np.zeros_like(p)

@@ -130,6 +130,49 @@ def test_threshold_fixing():
     assert any(fixed)
 
 
+@pytest.mark.parametrize("fix", [False, True])
+def test_hessian_eigenvectors(fix):
+    """HessianEigenVectors (pwaLikelihood.cc:864-912): the eigen-decomposition
+    of the free-parameter block of the Hessian, checked against LAPACK's
+    symmetric solver (numpy.linalg.eigh)."""
+    th = [0.0, 1.5, 2.0, 0.0, 1.0, 0.0, 0.0] if fix else None
+    L, O, names = _layout_pair(3, 4, 2, thresholds=th, mass=1.7)
+    P = L.nmbPars()
+    free = [k for k in range(P) if not L.parameter(k)["fixed"]]
+    assert len(free) == P - L.nmbParsFixed()
+    assert (L.nmbParsFixed() > 0) == fix
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((P, P))
+    H = X @ X.T + np.diag(np.linspace(0.1, 3.0, P))
+    H[0, 1] += 1e-13        # asymmetric at rounding level: symmetrised
+    pairs = L.HessianEigenVectors(H)
+    assert len(pairs) == len(free)
+    Hr = H[np.ix_(free, free)]
+    Hr = 0.5 * (Hr + Hr.T)
+    w, U = np.linalg.eigh(Hr)
+    w, U = w[::-1], U[:, ::-1]
+    vals = np.array([v for _, v in pairs])
+    assert np.all(np.diff(vals) <= 0)
+    np.testing.assert_allclose(vals, w, rtol=1e-12, atol=1e-12 * abs(w).max())
+    fixed = [k for k in range(P) if k not in free]
+    for k, (vec, val) in enumerate(pairs):
+        assert vec.shape == (P,)
+        assert np.all(vec[fixed] == 0.0)
+        assert abs(np.linalg.norm(vec) - 1.0) < 1e-12
+        assert abs(abs(vec[free] @ U[:, k]) - 1.0) < 1e-10
+        r = Hr @ vec[free] - val * vec[free]
+        assert np.linalg.norm(r) < 1e-11 * abs(w).max()
+    # degenerate eigenvalues: the identity has every vector as eigenvector
+    pairs = L.HessianEigenVectors(np.eye(P))
+    V = np.array([v[free] for v, _ in pairs])
+    np.testing.assert_allclose(V @ V.T, np.eye(len(free)), atol=1e-14)
+    assert all(v == 1.0 for _, v in pairs)
+    with pytest.raises(R.PwaError):
+        Hb = H.copy()
+        Hb[free[0], free[0]] = np.nan
+        L.HessianEigenVectors(Hb)
+
+
 def test_correct_param_signs_and_prod_amps_match_oracle():
     L, O, names = _layout_pair(3, 6, 2)
     rng = np.random.default_rng(1)
