@@ -429,6 +429,58 @@ int pwa_mlp_gradient(pwa_mlp* net, const float* X, const float* T, uint32_t B, d
 int pwa_mlp_train(pwa_mlp* net, const float* X, const float* T, uint64_t nSamples, uint32_t batch, uint32_t epochs,
                   float lr, uint64_t seed, double* lossHistory);
 
+/* ------------------------------------------------------------------------ */
+/* Decay amplitudes of three spinless final-state particles in the isobar    */
+/* model, helicity formalism (the step before the likelihood: replaces       */
+/* isobarHelicityAmplitude::amplitude, decayAmplitude/isobarAmplitude.h:80,  */
+/* isobarAmplitude.cc:98-262, isobarHelicityAmplitude.cc:64-195, for         */
+/* X -> isobar + bachelor, isobar -> a + b).  Spins, projections and orbital */
+/* angular momenta are integers in units of 1/2 (2J, 2M, 2L), as in the      */
+/* reference.  FP64 on the GPU, one thread per event.                        */
+/* ------------------------------------------------------------------------ */
+typedef struct pwa_isobar pwa_isobar;
+/* massDependence (decayAmplitude/massDependence.cc:169-320) */
+enum pwa_mass_dependence { PWA_MASSDEP_FLAT = 0, PWA_MASSDEP_RELATIVISTIC_BW = 1, PWA_MASSDEP_CONST_WIDTH_BW = 2 };
+/* one wave: the content of a key file of a three-body decay
+ * (decayAmplitude/waveDescription.cc:880-932) */
+typedef struct pwa_isobar_wave {
+	int32_t J, P, M, refl;            /* X: 2J, parity, 2M (>= 0 in the reflectivity basis), reflectivity */
+	int32_t L, S;                     /* X -> daughter 1 + daughter 2: 2L, 2S */
+	int32_t isobarJ, isobarL, isobarS; /* isobar 2J and its decay's 2L, 2S */
+	int32_t massDependence;           /* enum pwa_mass_dependence of the isobar */
+	double isobarMass, isobarWidth;   /* GeV/c^2 */
+	int32_t isobarDaughter1, isobarDaughter2, bachelor; /* final-state slots 0..2; isobar daughter 1 is the analyser */
+	int32_t bachelorFirst;            /* X-vertex daughter 1 (the analyser) is the bachelor rather than the isobar */
+} pwa_isobar_wave;
+int pwa_isobar_create(pwa_isobar** out);
+int pwa_isobar_destroy(pwa_isobar* A);
+/* three final-state particles: masses, species ids (equal ids are identical
+ * particles, Bose-symmetrised) and the beam mass (GeV/c^2); energies follow
+ * from the masses and momenta as in particle::setMomentum */
+int pwa_isobar_set_final_state(pwa_isobar* A, uint32_t nFsParticles, const double* masses, const int32_t* species,
+                               double beamMass);
+/* isobarAmplitude::enableReflectivityBasis / enableBoseSymmetrization /
+ * enableSpaceInversion / enableReflection (isobarAmplitude.h:68-75);
+ * defaults 1, 1, 0, 0 */
+int pwa_isobar_set_options(pwa_isobar* A, int reflectivityBasis, int boseSymmetrize, int spaceInversion,
+                           int reflection);
+int pwa_isobar_add_wave(pwa_isobar* A, const pwa_isobar_wave* wave);
+int pwa_isobar_nmb_waves(const pwa_isobar* A, uint32_t* n);
+/* number of symmetrisation terms of the current final state and options */
+int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t* n);
+/* amplitudes of every wave for nEvents events: beam momenta [3][nEvents]
+ * (px, py, pz rows), final-state momenta [3 particles][3][nEvents], lab frame,
+ * GeV/c; amps: complex128 [wave][nEvents].  memory: PWA_MEMORY_HOST or
+ * PWA_MEMORY_DEVICE for all three buffers. */
+int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, uint64_t nEvents, void* amps,
+                          int memory);
+/* host utilities: clebschGordanCoeff (utilities/spinUtils.hpp:241-330),
+ * dFunction (utilities/dFunction.hpp:52-170), barrierFactor with the
+ * 0.1973 GeV/c scale (utilities/physUtils.hpp:200-275); arguments doubled */
+int pwa_clebsch_gordan(int32_t j1, int32_t m1, int32_t j2, int32_t m2, int32_t J, int32_t M, double* out);
+int pwa_wigner_d(int32_t j, int32_t m, int32_t n, double theta, double* out);
+int pwa_barrier_factor(int32_t L, double q, double* out);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

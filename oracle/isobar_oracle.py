@@ -1,0 +1,397 @@
+"""FP64 restatement of the reference's isobar decay amplitudes for three
+spinless final-state particles (X -> isobar + bachelor, isobar -> a + b) in
+the helicity formalism.
+
+TEST INFRASTRUCTURE ONLY: this module is the checker of the GPU amplitude
+kernel (rootpwa_gb300/csrc/isobar.cu).  Only tests, the smoke check and the
+benchmark's CPU-baseline leg may import it; the product never calls it.
+
+It follows the reference step by step, vectorised over events with numpy:
+
+* Gottfried-Jackson frame: isobarAmplitude::gjTransform
+  (decayAmplitude/isobarAmplitude.cc:137-171) -- rotate so that beam x X is
+  the y axis, boost into the X rest frame, rotate about y so that the beam is
+  the z axis; the same sequence of ROOT-style active rotations and boosts.
+* helicity frame of the isobar: isobarHelicityAmplitude::hfTransform
+  (decayAmplitude/isobarHelicityAmplitude.cc:64-84), applied to the isobar's
+  daughters after the Gottfried-Jackson transformation
+  (transformDaughters, :87-126).
+* two-body amplitude: isobarHelicityAmplitude::twoBodyDecayAmplitude
+  (:130-195) = sqrt(L+1) * D*(phi, theta, 0) * (L 0 S lambda | J lambda)
+  * (s1 lambda1 s2 -lambda2 | S lambda) * F_L(q) * mass dependence, with the
+  reflectivity-basis D function at the X vertex (utilities/dFunction.hpp
+  DFunctionReflConj) and the sum over the isobar's helicities
+  (isobarAmplitude::twoBodyDecayAmplitudeSum, isobarAmplitude.cc:206-262).
+* Bose symmetrisation: sum over the permutations of identical final-state
+  particles with factor 1/sqrt(prod n_k!) (isobarDecayTopology.cc:638-670,
+  isobarAmplitude.cc:98-111); space inversion and reflection through the
+  production plane as in isobarAmplitude.cc:174-203.
+* mass dependences: flat, relativistic Breit-Wigner with the PWA2000 rule
+  q0 = sqrt|q0^2| (massDependence.cc:254-296, utilities/physUtils.hpp:283-300)
+  and constant-width Breit-Wigner (massDependence.cc:300-320).
+
+The building blocks are restated from the published formulas, not from the
+reference's arrangement of them: Clebsch-Gordan coefficients by Racah's
+formula, Wigner d functions by Wigner's formula, Blatt-Weisskopf barrier
+factors from spherical Hankel functions (scipy), normalised to 1 at q equal
+to the momentum scale 0.1973 GeV/c (utilities/physUtils.hpp:200-275).
+
+Parity unpinned against the reference itself: its decay-amplitude library
+needs ROOT and boost and does not build here, and its tests hold no
+amplitude values (test/decayAmplitude/testAmplitude.cc compares runs).  The
+building blocks are pinned against sympy and against the PDG closed forms,
+and the frames against rotation invariance and the reflectivity and parity
+eigenvalues, in tests/test_isobar_oracle.py.
+
+All spins, spin projections and orbital angular momenta are integers in
+units of 1/2 (2J, 2M, 2L), as in the reference.
+"""
+import math
+from itertools import permutations
+
+import numpy as np
+
+PR_DEFAULT = 0.1973        # GeV/c, 1 fm interaction radius
+MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW = 0, 1, 2
+
+
+# -- spin algebra ---------------------------------------------------------------
+
+def _f(n):
+    return math.factorial(n)
+
+
+def clebsch_gordan(j1, m1, j2, m2, J, M):
+    """(j1 m1 j2 m2 | J M), arguments doubled; Racah's formula
+    (clebschGordanCoeff, utilities/spinUtils.hpp:241-330)."""
+    def ok(j, m):
+        return j >= 0 and abs(m) <= j and (j - m) % 2 == 0
+    if not (ok(j1, m1) and ok(j2, m2) and ok(J, M)):
+        return 0.0
+    if not (abs(j1 - j2) <= J <= j1 + j2) or (j1 + j2 + J) % 2:
+        return 0.0
+    if m1 + m2 != M:
+        return 0.0
+    def h(x):                 # every combination below is even
+        return x // 2
+    pre = ((J + 1) * _f(h(J + j1 - j2)) * _f(h(J - j1 + j2)) * _f(h(j1 + j2 - J))
+           / _f(h(j1 + j2 + J) + 1))
+    pre *= _f(h(J + M)) * _f(h(J - M)) * _f(h(j1 - m1)) * _f(h(j1 + m1)) * _f(h(j2 - m2)) * _f(h(j2 + m2))
+    s = 0.0
+    for k in range(0, h(j1 + j2 + J) + 1):
+        den = [k, h(j1 + j2 - J) - k, h(j1 - m1) - k, h(j2 + m2) - k,
+               h(J - j2 + m1) + k, h(J - j1 - m2) + k]
+        if min(den) < 0:
+            continue
+        s += (-1) ** k / float(np.prod([_f(x) for x in den]))
+    return math.sqrt(pre) * s
+
+
+def wigner_d_terms(j, m, n):
+    """d^j_{m n}(theta) = sum of coef * cos(theta/2)^a * sin(theta/2)^b,
+    arguments doubled; Wigner's formula in the PDG sign convention
+    (dFunction, utilities/dFunction.hpp:52-170)."""
+    J, Mp, Mm = j, m, n
+    jpm, jmm, jpn, jmn = (J + Mp) // 2, (J - Mp) // 2, (J + Mm) // 2, (J - Mm) // 2
+    root = math.sqrt(_f(jpm) * _f(jmm) * _f(jpn) * _f(jmn))
+    d = (Mp - Mm) // 2            # m' - m in units of 1
+    out = []
+    for s in range(0, J + 1):
+        den = [jpn - s, s, d + s, jmm - s]
+        if min(den) < 0:
+            continue
+        coef = (-1) ** (d + s) * root / float(np.prod([_f(x) for x in den]))
+        out.append((coef, jpn + jmm - 2 * s, d + 2 * s))
+    return out
+
+
+def wigner_d(j, m, n, theta):
+    theta = np.asarray(theta, dtype=np.float64)
+    c, s = np.cos(theta / 2), np.sin(theta / 2)
+    return sum(coef * c ** a * s ** b for coef, a, b in wigner_d_terms(j, m, n)) + 0 * theta
+
+
+def D_conj(j, m, n, phi, theta):
+    """conj(D^j_{m n}(phi, theta, 0)) = exp(+i m phi / 2) d^j_{m n}(theta)."""
+    return np.exp(1j * (m / 2.0) * phi) * wigner_d(j, m, n, theta)
+
+
+def reflectivity_factor(J, P, M, refl):
+    """refl * P * (-1)^((J - M) / 2) (utilities/physUtils.hpp:172-196)."""
+    return refl * P * (-1) ** ((J - M) // 2)
+
+
+def D_refl_conj(J, M, n, P, refl, phi, theta):
+    """conj of the reflectivity-basis D function (utilities/dFunction.hpp
+    DFunctionRefl / DFunctionReflConj)."""
+    f = reflectivity_factor(J, P, M, refl)
+    if M == 0:
+        if f == +1:
+            return np.zeros_like(phi, dtype=np.complex128)
+        return D_conj(J, 0, n, phi, theta)
+    return (D_conj(J, M, n, phi, theta) - f * D_conj(J, -M, n, phi, theta)) / math.sqrt(2.0)
+
+
+# -- barrier factors and mass dependences -----------------------------------------
+
+def _hankel_abs2(l, x):
+    from scipy.special import spherical_jn, spherical_yn
+    return spherical_jn(l, x) ** 2 + spherical_yn(l, x) ** 2
+
+
+def barrier_factor(L, q, Pr=PR_DEFAULT):
+    """Blatt-Weisskopf factor F_L(q), L doubled: F_L^2 = |h_l(1)|^2 / (x^2 |h_l(x)|^2),
+    x = q / Pr (utilities/physUtils.hpp:200-275)."""
+    l = L // 2
+    q = np.asarray(q, dtype=np.float64)
+    if l == 0:
+        return np.ones_like(q)
+    x = q / Pr
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f2 = _hankel_abs2(l, 1.0) / (x * x * _hankel_abs2(l, x))
+    f2 = np.where(x == 0, 0.0, f2)
+    return np.sqrt(f2)
+
+
+def breakup_momentum_squared(M, m1, m2):
+    """(utilities/physUtils.hpp:75-96), sub-threshold values allowed."""
+    return (M - (m1 + m2)) * (M + (m1 + m2)) * (M - (m1 - m2)) * (M + (m1 - m2)) / (4 * M * M)
+
+
+def relativistic_bw(M, m1, m2, M0, G0, L):
+    """relativisticBreitWigner::amp (massDependence.cc:254-296) with
+    breitWigner (utilities/physUtils.hpp:283-300)."""
+    q = np.sqrt(np.maximum(breakup_momentum_squared(M, m1, m2), 0.0))
+    q0 = math.sqrt(abs(breakup_momentum_squared(M0, m1, m2)))
+    if q0 == 0:
+        return np.zeros_like(M, dtype=np.complex128)
+    G = G0 * (M0 / M) * (q / q0) * (barrier_factor(L, q) ** 2 / barrier_factor(L, q0) ** 2)
+    A, B, C = M0 * G0, M0 * M0 - M * M, M0 * G
+    return (A / (B * B + C * C)) * (B + 1j * C)
+
+
+def const_width_bw(M, M0, G0):
+    """constWidthBreitWigner::amp (massDependence.cc:300-320)."""
+    A, B = M0 * G0, M0 * M0 - M * M
+    return (A / (B * B + A * A)) * (B + 1j * A)
+
+
+# -- ROOT-style rotations and boosts (vectorised over events) ----------------------
+
+def _phi(v):
+    return np.where((v[..., 0] == 0) & (v[..., 1] == 0), 0.0, np.arctan2(v[..., 1], v[..., 0]))
+
+
+def _theta(v):
+    perp = np.hypot(v[..., 0], v[..., 1])
+    return np.where((perp == 0) & (v[..., 2] == 0), 0.0, np.arctan2(perp, v[..., 2]))
+
+
+def _rot(axis, a):
+    c, s = np.cos(a), np.sin(a)
+    o, z = np.ones_like(a), np.zeros_like(a)
+    if axis == "x":
+        m = [[o, z, z], [z, c, -s], [z, s, c]]
+    elif axis == "y":
+        m = [[c, z, s], [z, o, z], [-s, z, c]]
+    else:
+        m = [[c, -s, z], [s, c, z], [z, z, o]]
+    return np.moveaxis(np.array(m), (0, 1), (-2, -1))       # (N, 3, 3)
+
+
+def _apply_rot(R, lv):
+    out = lv.copy()
+    out[..., :3] = np.einsum("nij,nj->ni", R, lv[..., :3])
+    return out
+
+
+def _boost(lv, b):
+    """TLorentzVector::Boost(b)."""
+    b2 = np.sum(b * b, axis=-1)
+    g = 1.0 / np.sqrt(1.0 - b2)
+    bp = np.sum(b * lv[..., :3], axis=-1)
+    g2 = np.where(b2 > 0, (g - 1.0) / np.where(b2 > 0, b2, 1.0), 0.0)
+    out = np.empty_like(lv)
+    out[..., :3] = lv[..., :3] + (g2 * bp)[..., None] * b + (g * lv[..., 3])[..., None] * b
+    out[..., 3] = g * (lv[..., 3] + bp)
+    return out
+
+
+def _ytransform(yaxis):
+    """rotation taking yaxis to +y with the old z axis in the (x, z) plane:
+    RotateZ(pi/2 - phi_y) followed by RotateX(theta_y - pi/2)."""
+    return np.einsum("nij,njk->nik", _rot("x", _theta(yaxis) - math.pi / 2), _rot("z", math.pi / 2 - _phi(yaxis)))
+
+
+def gj_transform(beam, X, lvs):
+    """isobarAmplitude::gjTransform (isobarAmplitude.cc:137-171) applied to
+    the Lorentz vectors lvs [(N, 4), ...]."""
+    R1 = _ytransform(np.cross(beam[:, :3], X[:, :3]))
+    b1, X1 = _apply_rot(R1, beam), _apply_rot(R1, X)
+    bx = -X1[:, :3] / X1[:, 3:4]
+    b2 = _boost(b1, bx)
+    R2 = _rot("y", -np.sign(b2[:, 0]) * _theta(b2))
+    return [_apply_rot(R2, _boost(_apply_rot(R1, v), bx)) for v in lvs]
+
+
+def hf_transform(parent, lvs):
+    """isobarHelicityAmplitude::hfTransform (isobarHelicityAmplitude.cc:64-84)."""
+    z = np.zeros_like(parent[:, :3])
+    z[:, 2] = 1.0
+    R1 = _ytransform(np.cross(z, parent[:, :3]))
+    d1 = _apply_rot(R1, parent)
+    R2 = _rot("y", -np.sign(d1[:, 0]) * _theta(d1))
+    d2 = _apply_rot(R2, d1)
+    R = np.einsum("nij,njk->nik", R2, R1)
+    bx = -d2[:, :3] / d2[:, 3:4]
+    return [_boost(_apply_rot(R, v), bx) for v in lvs]
+
+
+def _lv(p, m):
+    return np.concatenate([p, np.sqrt(m * m + np.sum(p * p, axis=-1))[:, None]], axis=-1)
+
+
+def _mass(lv):
+    return np.sqrt(lv[:, 3] ** 2 - np.sum(lv[:, :3] ** 2, axis=-1))
+
+
+# -- amplitudes --------------------------------------------------------------------
+
+def bose_terms(species):
+    """all permutations that exchange identical final-state particles, with the
+    factor 1/sqrt(prod n_k!) (isobarDecayTopology.cc:638-670)."""
+    n = len(species)
+    perms = [p for p in permutations(range(n)) if all(species[p[i]] == species[i] for i in range(n))]
+    return perms, 1.0 / math.sqrt(len(perms))
+
+
+def _sym_term(w, beam, fs, masses, opts):
+    a, b, c = w["isobar_daughters"][0], w["isobar_daughters"][1], w["bachelor"]
+    X = fs[0] + fs[1] + fs[2]
+    gj = gj_transform(beam, X, fs)
+    if opts.get("space_inversion"):
+        gj = [np.concatenate([-v[:, :3], v[:, 3:]], axis=1) for v in gj]
+    if opts.get("reflection"):
+        gj = [v * np.array([1.0, -1.0, 1.0, 1.0]) for v in gj]
+    iso = gj[a] + gj[b]
+    bach = gj[c]
+    # X vertex: daughter 1 is the analyser
+    d1 = bach if w["bachelor_first"] else iso
+    phi, theta = _phi(d1[:, :3]), _theta(d1[:, :3])
+    qX = np.sqrt(np.sum(d1[:, :3] ** 2, axis=-1))
+    # isobar vertex: helicity frame of the isobar, analyser = isobar daughter 1
+    ha, = hf_transform(iso, [gj[a]])
+    phih, thetah = _phi(ha[:, :3]), _theta(ha[:, :3])
+    qI = np.sqrt(np.sum(ha[:, :3] ** 2, axis=-1))
+    mI = _mass(iso)
+    J, P, M, refl, L, S = w["J"], w["P"], w["M"], w["refl"], w["L"], w["S"]
+    j, l, s = w["isobar_J"], w["isobar_L"], w["isobar_S"]
+    md = w["mass_dep"]
+    if md == MASSDEP_REL_BW:
+        bw = relativistic_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"], l)
+    elif md == MASSDEP_CONST_BW:
+        bw = const_width_bw(mI, w["isobar_mass"], w["isobar_width"])
+    else:
+        bw = np.ones_like(mI, dtype=np.complex128)
+    fX = math.sqrt(L + 1) * barrier_factor(L, qX)
+    fI = math.sqrt(l + 1) * barrier_factor(l, qI) * bw
+    amp = np.zeros(len(phi), dtype=np.complex128)
+    for lam_iso in range(-j, j + 1, 2):
+        # X -> daughter1 + daughter2: helicities (lambda1, lambda2)
+        if w["bachelor_first"]:
+            s1, l1, s2, l2 = 0, 0, j, lam_iso
+        else:
+            s1, l1, s2, l2 = j, lam_iso, 0, 0
+        lam = l1 - l2
+        cg = clebsch_gordan(L, 0, S, lam, J, lam) * clebsch_gordan(s1, l1, s2, -l2, S, lam)
+        if cg == 0:
+            continue
+        if opts.get("reflectivity_basis", True):
+            DX = D_refl_conj(J, M, lam, P, refl, phi, theta)
+        else:
+            DX = D_conj(J, M, lam, phi, theta)
+        cgI = clebsch_gordan(l, 0, s, 0, j, 0) * clebsch_gordan(0, 0, 0, 0, s, 0)
+        if cgI == 0:
+            continue
+        DI = D_conj(j, lam_iso, 0, phih, thetah)
+        amp += (fX * cg * DX) * (fI * cgI * DI)
+    return amp
+
+
+def amplitudes(waves, beam_p, fs_p, masses, beam_mass, species, **opts):
+    """complex128 [W, N] amplitudes of the waves for events given by the beam
+    momentum (N, 3) and the final-state momenta (3, N, 3)."""
+    beam = _lv(np.asarray(beam_p, dtype=np.float64), beam_mass)
+    fs_p = np.asarray(fs_p, dtype=np.float64)
+    perms, factor = bose_terms(species) if opts.get("bose", True) else ([tuple(range(len(species)))], 1.0)
+    out = np.zeros((len(waves), beam.shape[0]), dtype=np.complex128)
+    for p in perms:
+        # particle i takes the momentum of particle p[i] (decayTopology::revertMomenta)
+        fs = [_lv(fs_p[p[i]], masses[i]) for i in range(len(masses))]
+        for k, w in enumerate(waves):
+            out[k] += factor * _sym_term(w, beam, fs, masses, opts)
+    return out
+
+
+def wave(J, P, M, refl, L, S, isobar_J, isobar_L, mass_dep, isobar_mass=0.0, isobar_width=0.0,
+         isobar_daughters=(0, 1), bachelor=2, bachelor_first=False, isobar_S=0):
+    """one wave's description (all spins doubled)."""
+    return dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobar_J=isobar_J, isobar_L=isobar_L, isobar_S=isobar_S,
+                mass_dep=mass_dep, isobar_mass=isobar_mass, isobar_width=isobar_width,
+                isobar_daughters=tuple(isobar_daughters), bachelor=bachelor, bachelor_first=bool(bachelor_first))
+
+
+def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2):
+    """seeded synthetic diffractive events pi- p -> (pi- pi+ pi-) p: the beam
+    along z with a small divergence, X of mass uniform in [m_lo, m_hi] with a
+    small transverse momentum, decaying by three-body phase space (uniform in
+    the two Dalitz variables, accepted inside the kinematic border).  Returns
+    beam (N, 3), final state (3, N, 3) momenta, masses (3,), beam mass."""
+    rng = np.random.default_rng(seed)
+    mpi = 0.13957039
+    masses = np.array([mpi, mpi, mpi])
+    beam = np.stack([rng.normal(0, 0.05, n), rng.normal(0, 0.05, n), np.full(n, beam_momentum)], axis=1)
+    MX = rng.uniform(m_lo, m_hi, n)
+    # X momentum: beam direction with a transverse kick
+    pX = beam.copy()
+    pX[:, 0] += rng.normal(0, 0.3, n)
+    pX[:, 1] += rng.normal(0, 0.3, n)
+    pX[:, 2] *= rng.uniform(0.95, 1.0, n)
+    EX = np.sqrt(MX ** 2 + np.sum(pX ** 2, axis=1))
+    # Dalitz variables m12^2, m23^2 by rejection inside the border
+    fs_rf = np.zeros((3, n, 4))
+    todo = np.arange(n)
+    while todo.size:
+        M = MX[todo]
+        s12 = rng.uniform((2 * mpi) ** 2, (M - mpi) ** 2)
+        s23 = rng.uniform((2 * mpi) ** 2, (M - mpi) ** 2)
+        # energies in the X rest frame
+        E3 = (M * M + mpi * mpi - s12) / (2 * M)
+        E1 = (M * M + mpi * mpi - s23) / (2 * M)
+        E2 = M - E1 - E3
+        p1, p2, p3 = [np.sqrt(np.maximum(E * E - mpi * mpi, 0)) for E in (E1, E2, E3)]
+        ok = (E1 > mpi) & (E2 > mpi) & (E3 > mpi)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            c13 = (p2 ** 2 - p1 ** 2 - p3 ** 2) / (2 * p1 * p3)
+        ok &= np.abs(c13) < 1
+        good = np.nonzero(ok)[0]
+        if good.size:
+            idx = todo[good]
+            c = c13[good]
+            sn = np.sqrt(1 - c * c)
+            v1 = np.stack([np.zeros(good.size), np.zeros(good.size), p1[good]], axis=1)
+            v3 = p3[good][:, None] * np.stack([sn, np.zeros(good.size), c], axis=1)
+            v2 = -(v1 + v3)
+            # random orientation
+            a, b, g = rng.uniform(0, 2 * np.pi, good.size), np.arccos(rng.uniform(-1, 1, good.size)), \
+                rng.uniform(0, 2 * np.pi, good.size)
+            R = np.einsum("nij,njk->nik", _rot("z", a), np.einsum("nij,njk->nik", _rot("y", b), _rot("z", g)))
+            for i, (v, E) in enumerate(((v1, E1), (v2, E2), (v3, E3))):
+                fs_rf[i, idx, :3] = np.einsum("nij,nj->ni", R, v)
+                fs_rf[i, idx, 3] = E[good]
+        todo = todo[~ok]
+    # boost to the lab
+    bX = pX / EX[:, None]
+    fs = np.stack([_boost(fs_rf[i], bX)[:, :3] for i in range(3)])
+    # particle order: pi- (0), pi+ (1), pi- (2)
+    return beam, fs, masses, mpi

@@ -46,6 +46,14 @@ cc = C.c_char_p
 i = C.c_int
 pvp = C.POINTER(C.c_void_p)
 
+class IsobarWave(C.Structure):
+    """struct pwa_isobar_wave of include/pwa_gb300.h."""
+    _fields_ = [(n, C.c_int32) for n in ("J", "P", "M", "refl", "L", "S", "isobarJ", "isobarL", "isobarS",
+                                          "massDependence")] + \
+        [("isobarMass", C.c_double), ("isobarWidth", C.c_double)] + \
+        [(n, C.c_int32) for n in ("isobarDaughter1", "isobarDaughter2", "bachelor", "bachelorFirst")]
+
+
 SIGNATURES = {
     "pwa_abi_version": (i, []),
     "pwa_last_error": (cc, []),
@@ -145,6 +153,17 @@ SIGNATURES = {
     "pwa_likelihood_hessian": (i, [vp, pd, pd]),
     "pwa_likelihood_covariance_matrix": (i, [vp, pd, pd]),
     "pwa_likelihood_hessian_eigenvectors": (i, [vp, pd, pd, pd, C.POINTER(u32)]),
+    "pwa_isobar_create": (i, [pvp]),
+    "pwa_isobar_destroy": (i, [vp]),
+    "pwa_isobar_set_final_state": (i, [vp, u32, pd, C.POINTER(i32), C.c_double]),
+    "pwa_isobar_set_options": (i, [vp, i, i, i, i]),
+    "pwa_isobar_add_wave": (i, [vp, C.POINTER(IsobarWave)]),
+    "pwa_isobar_nmb_waves": (i, [vp, C.POINTER(u32)]),
+    "pwa_isobar_nmb_sym_terms": (i, [vp, C.POINTER(u32)]),
+    "pwa_isobar_amplitudes": (i, [vp, vp, vp, u64, vp, i]),
+    "pwa_clebsch_gordan": (i, [i32, i32, i32, i32, i32, i32, pd]),
+    "pwa_wigner_d": (i, [i32, i32, i32, C.c_double, pd]),
+    "pwa_barrier_factor": (i, [i32, C.c_double, pd]),
     "pwa_likelihood_correct_param_signs": (i, [vp, pd, pd]),
     "pwa_likelihood_integral_matrices": (i, [vp, pd, pd, pd, i]),
     "pwa_likelihood_build_prod_amp_arrays": (i, [vp, pd, pd, C.POINTER(i32), C.POINTER(u32), i]),

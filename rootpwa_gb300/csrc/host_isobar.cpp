@@ -1,0 +1,247 @@
+// host_isobar.cpp -- C ABI of the three-body isobar decay amplitudes: the
+// wave set, the final state, the options of isobarAmplitude
+// (decayAmplitude/isobarAmplitude.h:68-75) and the evaluation on the GPU
+// (isobar.cu); the spin-algebra utilities the plan is built from.
+#include "host_common.h"
+#include "isobar_plan.h"
+
+struct pwa_isobar {
+	double masses[3] = {0.0, 0.0, 0.0};
+	int32_t species[3] = {0, 1, 2};
+	double beamMass = 0.0;
+	bool finalState = false;
+	bool reflBasis = true, bose = true, spaceInversion = false, reflection = false;
+	std::vector<pwa_isobar_wave> waves;
+	iso::Plan plan;
+	bool dirty = true;
+	DevBuf dPlan, dIn, dOut;
+	iso::PlanView devView{};
+	cudaStream_t stream = nullptr;
+	~pwa_isobar()
+	{
+		if (stream)
+			cudaStreamDestroy(stream);
+	}
+};
+
+namespace {
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// the plan's arrays in one device buffer; devView points into it
+int uploadPlan(pwa_isobar* A)
+{
+	iso::Plan& p = A->plan;
+	iso::buildPlan(A->waves, A->masses, A->species, A->beamMass, A->reflBasis, A->bose, A->spaceInversion,
+	               A->reflection, p);
+	const size_t oWaves = 0;
+	const size_t oOrder = align16(oWaves + p.waves.size() * sizeof(iso::WaveDev));
+	const size_t oLams = align16(oOrder + p.order.size() * sizeof(int32_t));
+	const size_t oTerms = align16(oLams + p.lams.size() * sizeof(iso::LamTerm));
+	const size_t oPoly = align16(oTerms + p.dterms.size() * sizeof(iso::DTerm));
+	const size_t oNorm = align16(oPoly + sizeof(p.bfPoly));
+	const size_t oPerms = align16(oNorm + sizeof(p.bfNorm));
+	const size_t total = align16(oPerms + p.perms.size() * sizeof(int32_t));
+	std::vector<unsigned char> h(total, 0);
+	auto put = [&](size_t off, const void* src, size_t bytes) {
+		if (bytes)
+			std::memcpy(h.data() + off, src, bytes);
+	};
+	put(oWaves, p.waves.data(), p.waves.size() * sizeof(iso::WaveDev));
+	put(oOrder, p.order.data(), p.order.size() * sizeof(int32_t));
+	put(oLams, p.lams.data(), p.lams.size() * sizeof(iso::LamTerm));
+	put(oTerms, p.dterms.data(), p.dterms.size() * sizeof(iso::DTerm));
+	put(oPoly, p.bfPoly, sizeof(p.bfPoly));
+	put(oNorm, p.bfNorm, sizeof(p.bfNorm));
+	put(oPerms, p.perms.data(), p.perms.size() * sizeof(int32_t));
+	PWA_TRY(A->dPlan.ensure(total, "isobar wave plan"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(A->dPlan.p, h.data(), total, cudaMemcpyHostToDevice, A->stream), "plan upload"));
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(A->stream), "plan upload"));
+	unsigned char* d = A->dPlan.as<unsigned char>();
+	iso::PlanView v = p.view();
+	v.waves = reinterpret_cast<const iso::WaveDev*>(d + oWaves);
+	v.order = reinterpret_cast<const int32_t*>(d + oOrder);
+	v.lams = reinterpret_cast<const iso::LamTerm*>(d + oLams);
+	v.dterms = reinterpret_cast<const iso::DTerm*>(d + oTerms);
+	v.bfPoly = reinterpret_cast<const double*>(d + oPoly);
+	v.bfNorm = reinterpret_cast<const double*>(d + oNorm);
+	v.perms = reinterpret_cast<const int32_t*>(d + oPerms);
+	A->devView = v;
+	A->dirty = false;
+	return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pwa_isobar_create(pwa_isobar** out)
+{
+	if (!out)
+		return setError(kErrArg, "null argument");
+	*out = new (std::nothrow) pwa_isobar();
+	return *out ? kOk : setError(kErrOom, "out of host memory");
+}
+
+int pwa_isobar_destroy(pwa_isobar* A)
+{
+	delete A;
+	return kOk;
+}
+
+int pwa_isobar_set_final_state(pwa_isobar* A, uint32_t nFs, const double* masses, const int32_t* species,
+                               double beamMass)
+{
+	if (!A || !masses || !species)
+		return setError(kErrArg, "null argument");
+	if (nFs != 3)
+		return setError(kErrUnsupported, "the isobar amplitudes cover three final-state particles");
+	for (int i = 0; i < 3; ++i)
+		if (!(masses[i] > 0.0) || !std::isfinite(masses[i]))
+			return setError(kErrArg, "final-state masses must be positive");
+	if (!(beamMass >= 0.0) || !std::isfinite(beamMass))
+		return setError(kErrArg, "the beam mass must be >= 0");
+	for (int i = 0; i < 3; ++i)
+		for (int j = 0; j < 3; ++j)
+			if (species[i] == species[j] && masses[i] != masses[j])
+				return setError(kErrArg, "identical particles must have equal masses");
+	for (int i = 0; i < 3; ++i) {
+		A->masses[i] = masses[i];
+		A->species[i] = species[i];
+	}
+	A->beamMass = beamMass;
+	A->finalState = true;
+	A->dirty = true;
+	return kOk;
+}
+
+int pwa_isobar_set_options(pwa_isobar* A, int reflectivityBasis, int boseSymmetrize, int spaceInversion, int reflection)
+{
+	if (!A)
+		return setError(kErrArg, "null argument");
+	if (reflectivityBasis)
+		for (const pwa_isobar_wave& w : A->waves)
+			if (w.M < 0)
+				return setError(kErrArg, "the reflectivity basis needs M >= 0 for every wave");
+	A->reflBasis = reflectivityBasis != 0;
+	A->bose = boseSymmetrize != 0;
+	A->spaceInversion = spaceInversion != 0;
+	A->reflection = reflection != 0;
+	A->dirty = true;
+	return kOk;
+}
+
+int pwa_isobar_add_wave(pwa_isobar* A, const pwa_isobar_wave* w)
+{
+	if (!A || !w)
+		return setError(kErrArg, "null argument");
+	const std::string why = iso::checkWave(*w, A->reflBasis);
+	if (!why.empty())
+		return setError(kErrArg, "pwa_isobar_add_wave: " + why);
+	A->waves.push_back(*w);
+	A->dirty = true;
+	return kOk;
+}
+
+int pwa_isobar_nmb_waves(const pwa_isobar* A, uint32_t* n)
+{
+	if (!A || !n)
+		return setError(kErrArg, "null argument");
+	*n = (uint32_t)A->waves.size();
+	return kOk;
+}
+
+int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t* n)
+{
+	if (!A || !n)
+		return setError(kErrArg, "null argument");
+	std::vector<int32_t> perms;
+	double f = 1.0;
+	iso::bosePermutations(A->species, A->bose, perms, f);
+	*n = (uint32_t)(perms.size() / 3);
+	return kOk;
+}
+
+int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, uint64_t n, void* amps, int memory)
+{
+	if (!A)
+		return setError(kErrArg, "null argument");
+	if (memory != PWA_MEMORY_HOST && memory != PWA_MEMORY_DEVICE)
+		return setError(kErrArg, "memory must be PWA_MEMORY_HOST or PWA_MEMORY_DEVICE");
+	if (!A->finalState)
+		return setError(kErrState, "set the final state first");
+	if (A->waves.empty())
+		return setError(kErrState, "no waves");
+	if (n == 0)
+		return kOk;
+	if (!beam || !fs || !amps)
+		return setError(kErrArg, "null buffer");
+	const uint64_t W = A->waves.size();
+	if (n > (uint64_t)1 << 40 || W * n > ((uint64_t)1 << 62) / 16)
+		return setError(kErrArg, "too many events");
+	if (!A->stream)
+		PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking), "stream create"));
+	if (A->dirty)
+		PWA_TRY(uploadPlan(A));
+	const double* dBeam = beam;
+	const double* dFs = fs;
+	double* dAmps = static_cast<double*>(amps);
+	if (memory == PWA_MEMORY_HOST) {
+		PWA_TRY(A->dIn.ensure(n * 12 * sizeof(double), "isobar event buffer"));
+		PWA_TRY(A->dOut.ensure(W * n * 16, "isobar amplitude buffer"));
+		double* in = A->dIn.as<double>();
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(in, beam, n * 3 * sizeof(double), cudaMemcpyHostToDevice, A->stream),
+		                  "beam upload"));
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(in + 3 * n, fs, n * 9 * sizeof(double), cudaMemcpyHostToDevice, A->stream),
+		                  "final-state upload"));
+		dBeam = in;
+		dFs = in + 3 * n;
+		dAmps = A->dOut.as<double>();
+	} else {
+		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device momenta"));
+	}
+	PWA_TRY(launchIsobarAmplitudes(A->devView, dBeam, dFs, n, dAmps, A->stream));
+	if (memory == PWA_MEMORY_HOST)
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(amps, dAmps, W * n * 16, cudaMemcpyDeviceToHost, A->stream),
+		                  "amplitude download"));
+	return cudaCheck(cudaStreamSynchronize(A->stream), "isobar amplitudes");
+}
+
+int pwa_clebsch_gordan(int32_t j1, int32_t m1, int32_t j2, int32_t m2, int32_t J, int32_t M, double* out)
+{
+	if (!out)
+		return setError(kErrArg, "null argument");
+	if (j1 > 2 * iso::kMaxSpin || j2 > 2 * iso::kMaxSpin || J > 4 * iso::kMaxSpin)
+		return setError(kErrArg, "spins out of range");
+	*out = iso::clebschGordan(j1, m1, j2, m2, J, M);
+	return kOk;
+}
+
+int pwa_wigner_d(int32_t j, int32_t m, int32_t n, double theta, double* out)
+{
+	if (!out)
+		return setError(kErrArg, "null argument");
+	if (j < 0 || j > 2 * iso::kMaxSpin || std::abs(m) > j || std::abs(n) > j || ((j - m) & 1) || ((j - n) & 1))
+		return setError(kErrArg, "illegal arguments of the Wigner d function");
+	*out = iso::wignerD(j, m, n, theta);
+	return kOk;
+}
+
+int pwa_barrier_factor(int32_t L, double q, double* out)
+{
+	if (!out)
+		return setError(kErrArg, "null argument");
+	if (L < 0 || L > iso::kMaxL || (L & 1))
+		return setError(kErrArg, "2L must be even and in 0 .. 14");
+	if (!(q >= 0.0))
+		return setError(kErrArg, "q must be >= 0");
+	double poly[8][8], norm[8];
+	iso::barrierPolynomials(poly, norm);
+	iso::PlanView v{};
+	v.bfPoly = &poly[0][0];
+	v.bfNorm = norm;
+	*out = std::sqrt(iso::barrierF2(v, L, q));
+	return kOk;
+}
+
+}  // extern "C"

@@ -1,0 +1,55 @@
+// isobar.cu -- GPU evaluation of the three-body isobar decay amplitudes
+// (isobarHelicityAmplitude::amplitude, decayAmplitude/isobarAmplitude.cc:98-262,
+// isobarHelicityAmplitude.cc:64-195).  One thread per event in a grid-stride
+// loop: the thread reads its event's beam and final-state momenta (SoA rows,
+// coalesced), builds the Gottfried-Jackson frame once, the kinematics of every
+// symmetrisation term once per topology class, and writes one complex128
+// amplitude per wave (row-major [wave][event], coalesced across the warp).
+// The wave plan (couplings, D-function terms, barrier polynomials) is a few
+// KB read by every thread through the read-only cache.  FP64 throughout: the
+// amplitudes are computed once per data set and then stored for the fit.
+#include "isobar_math.cuh"
+#include "pwa_internal.h"
+
+#include <algorithm>
+
+namespace pwa {
+
+namespace {
+
+constexpr int kIsoThreads = 128;
+
+__global__ void __launch_bounds__(kIsoThreads) isobarAmplitudeKernel(iso::PlanView P, const double* __restrict__ beam,
+                                                                     const double* __restrict__ fs, uint64_t n,
+                                                                     double* __restrict__ amps)
+{
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+		double bp[3], fp[3][3];
+		for (int k = 0; k < 3; ++k)
+			bp[k] = __ldg(beam + k * n + e);
+		for (int i = 0; i < 3; ++i)
+			for (int k = 0; k < 3; ++k)
+				fp[i][k] = __ldg(fs + (uint64_t)(3 * i + k) * n + e);
+		iso::eventAmplitudes(P, bp, fp, amps, n, e);
+	}
+}
+
+}  // namespace
+
+int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const double* fs, uint64_t n, double* amps,
+                           cudaStream_t s)
+{
+	if (n == 0 || v.nWaves == 0)
+		return kOk;
+	int dev = 0, sms = 0;
+	PWA_CHECK(cudaCheck(cudaGetDevice(&dev), "cudaGetDevice"));
+	PWA_CHECK(cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
+	const uint64_t need = (n + kIsoThreads - 1) / kIsoThreads;
+	const unsigned blocks = (unsigned)std::min<uint64_t>(need, (uint64_t)sms * 16);
+	isobarAmplitudeKernel<<<blocks, kIsoThreads, 0, s>>>(v, beam, fs, n, amps);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "isobar amplitude kernel");
+}
+
+}  // namespace pwa

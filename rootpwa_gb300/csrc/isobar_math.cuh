@@ -1,0 +1,320 @@
+// isobar_math.cuh -- per-event arithmetic of the three-body isobar decay
+// amplitudes in the helicity formalism, FP64, written once for the GPU
+// kernel (isobar.cu).  The functions are plain C++ on POD views of the wave
+// plan, so the same source also compiles as host code (the CPU tests compile
+// it with g++ to check the arithmetic against the FP64 oracle without a GPU).
+//
+// Reference: isobarHelicityAmplitude (decayAmplitude/isobarHelicityAmplitude.cc:
+// 64-195), isobarAmplitude (decayAmplitude/isobarAmplitude.cc:98-262),
+// mass dependences (decayAmplitude/massDependence.cc:169-320), barrier
+// factors and Breit-Wigner (utilities/physUtils.hpp:75-300).
+//
+// Frames.  The reference reaches the Gottfried-Jackson frame by a rotation
+// that puts beam x X on the y axis, a boost into the X rest frame and a
+// rotation about y that puts the beam on z (isobarAmplitude.cc:137-171).
+// The result is the orthonormal basis z = beam direction in the X rest
+// frame, y = unit(beam x X) in the lab (a boost along X keeps the components
+// perpendicular to X), x = y x z; here the final-state momenta are boosted
+// into the X rest frame once and projected on that basis.  The isobar's
+// helicity frame (isobarHelicityAmplitude.cc:64-84) is likewise the basis
+// z = isobar direction, y = unit(z_GJ x isobar), x = y x z followed by a boost
+// along z.  In the measure-zero case of an isobar along z_GJ (y undefined)
+// the kernel takes y = y_GJ.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define PWA_HD __host__ __device__ __forceinline__
+#else
+#define PWA_HD inline
+#endif
+
+namespace pwa {
+namespace iso {
+
+constexpr int kMaxSpin = 16;      // 2J: spins up to 8
+constexpr int kMaxL = 14;         // 2L: barrier factors up to L = 7
+constexpr int kMaxPerms = 6;      // Bose terms of three particles
+constexpr double kPr = 0.1973;    // GeV/c, 1 fm interaction radius
+
+enum { kMassFlat = 0, kMassRelBw = 1, kMassConstBw = 2 };
+
+// d^j_{m n}(theta) = sum over terms of coef * cos(theta/2)^a * sin(theta/2)^b
+struct DTerm {
+	double coef;
+	int32_t a, b;
+};
+
+// one helicity of the isobar in one wave: the X-vertex D function
+// cPlus e^{+i M phi/2} d^J_{M lam} + cMinus e^{-i M phi/2} d^J_{-M lam}
+// (couplings, norms and the reflectivity combination folded into cPlus,
+// cMinus) times the isobar vertex e^{+i lamIso phiH/2} d^j_{lamIso 0}
+struct LamTerm {
+	int32_t lamIso;                 // 2 lambda of the isobar
+	int32_t plus0, plus1;           // DTerm range of d^J_{M lam}
+	int32_t minus0, minus1;         // DTerm range of d^J_{-M lam} (empty if unused)
+	int32_t iso0, iso1;             // DTerm range of d^j_{lamIso 0}
+	double cPlus, cMinus;
+};
+
+struct WaveDev {
+	int32_t a, b, c;                // isobar daughters 1, 2 and the bachelor (final-state slots)
+	int32_t bachelorFirst;          // X-vertex daughter 1 (the analyser) is the bachelor
+	int32_t M;                      // 2M of X
+	int32_t LX, LI;                 // 2L of the X and isobar vertices (barrier factors)
+	int32_t massDep;
+	double m0, g0;                  // isobar mass and width
+	double q0, f2q0;                // breakup momentum at m0 and F_L^2(q0) (relativistic BW)
+	double ma, mb;                  // isobar daughter masses
+	int32_t lam0, lam1;             // LamTerm range
+	int32_t topo;                   // topology class (waves of one class share kinematics)
+	int32_t pad;
+};
+
+// read-only view of a wave plan (device or host pointers)
+struct PlanView {
+	const WaveDev* waves;
+	const int32_t* order;           // waves sorted by topology class
+	const LamTerm* lams;
+	const DTerm* dterms;
+	const double* bfPoly;           // [8][8]: P_l(z) coefficients of z^0..z^l
+	const double* bfNorm;           // [8]: P_l(1)
+	const int32_t* perms;           // [nPerms][3]: slot i takes particle perms[t][i]
+	uint32_t nWaves, nPerms;
+	double boseFactor;
+	double masses[3], beamMass;
+	int32_t spaceInversion, reflection;
+};
+
+struct C2 {
+	double re, im;
+};
+PWA_HD C2 cmul(C2 x, C2 y) { return C2{x.re * y.re - x.im * y.im, x.re * y.im + x.im * y.re}; }
+PWA_HD C2 cadd(C2 x, C2 y) { return C2{x.re + y.re, x.im + y.im}; }
+PWA_HD C2 cscale(C2 x, double s) { return C2{x.re * s, x.im * s}; }
+PWA_HD C2 cexpi(double x)
+{
+#if defined(__CUDA_ARCH__)
+	double s, c;
+	sincos(x, &s, &c);
+	return C2{c, s};
+#else
+	return C2{std::cos(x), std::sin(x)};
+#endif
+}
+
+struct V3 {
+	double x, y, z;
+};
+PWA_HD V3 vadd(V3 u, V3 v) { return V3{u.x + v.x, u.y + v.y, u.z + v.z}; }
+PWA_HD V3 vscale(V3 u, double s) { return V3{u.x * s, u.y * s, u.z * s}; }
+PWA_HD double vdot(V3 u, V3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; }
+PWA_HD V3 vcross(V3 u, V3 v) { return V3{u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x}; }
+PWA_HD V3 vunit(V3 u)
+{
+	const double n = sqrt(vdot(u, u));
+	return n > 0 ? vscale(u, 1.0 / n) : u;
+}
+
+struct LV {
+	V3 p;
+	double e;
+};
+
+// (e, p) in the rest frame of (eX, pX) of mass mX:
+// e' = (e eX - p.pX) / mX,  p' = p - pX (e + e') / (eX + mX)
+PWA_HD LV toRest(LV v, V3 pX, double eX, double mX)
+{
+	const double e1 = (v.e * eX - vdot(v.p, pX)) / mX;
+	return LV{vadd(v.p, vscale(pX, -(v.e + e1) / (eX + mX))), e1};
+}
+
+PWA_HD double ipow(double x, int n)
+{
+	double r = 1.0;
+	while (n > 0) {
+		if (n & 1)
+			r *= x;
+		x *= x;
+		n >>= 1;
+	}
+	return r;
+}
+
+PWA_HD double dEval(const DTerm* t, int t0, int t1, double c, double s)
+{
+	double d = 0.0;
+	for (int k = t0; k < t1; ++k)
+		d += t[k].coef * ipow(c, t[k].a) * ipow(s, t[k].b);
+	return d;
+}
+
+// Blatt-Weisskopf F_L(q)^2 = P_l(1) z^l / P_l(z), z = (q / 0.1973)^2, L = 2l
+PWA_HD double barrierF2(const PlanView& P, int L, double q)
+{
+	const int l = L / 2;
+	if (l == 0)
+		return 1.0;
+	const double z = (q * q) / (kPr * kPr);
+	const double* c = P.bfPoly + 8 * l;
+	double den = c[l];
+	for (int k = l - 1; k >= 0; --k)
+		den = den * z + c[k];
+	return P.bfNorm[l] * ipow(z, l) / den;
+}
+
+PWA_HD double breakup2(double M, double m1, double m2)
+{
+	const double s = m1 + m2, d = m1 - m2;
+	return (M - s) * (M + s) * (M - d) * (M + d) / (4.0 * M * M);
+}
+
+PWA_HD C2 massDependence(const PlanView& P, const WaveDev& w, double mI)
+{
+	if (w.massDep == kMassRelBw) {
+		if (w.q0 == 0.0)
+			return C2{0.0, 0.0};
+		const double q2 = breakup2(mI, w.ma, w.mb);
+		const double q = q2 > 0 ? sqrt(q2) : 0.0;
+		const double G = w.g0 * (w.m0 / mI) * (q / w.q0) * (barrierF2(P, w.LI, q) / w.f2q0);
+		const double A = w.m0 * w.g0, B = w.m0 * w.m0 - mI * mI, Cc = w.m0 * G;
+		const double f = A / (B * B + Cc * Cc);
+		return C2{f * B, f * Cc};
+	}
+	if (w.massDep == kMassConstBw) {
+		const double A = w.m0 * w.g0, B = w.m0 * w.m0 - mI * mI;
+		const double f = A / (B * B + A * A);
+		return C2{f * B, f * A};
+	}
+	return C2{1.0, 0.0};
+}
+
+// kinematics of one symmetrisation term for one topology class
+struct Kin {
+	double phi, cX, sX, qX;         // analyser of the X vertex in the GJ frame: phi, cos/sin(theta/2), |p|
+	double phiH, cI, sI, qI;        // isobar daughter 1 in the isobar helicity frame
+	double mI;                      // isobar mass
+};
+
+PWA_HD double phiOf(double x, double y) { return (x == 0.0 && y == 0.0) ? 0.0 : atan2(y, x); }
+
+PWA_HD void halfAngle(double perp, double z, double* c, double* s)
+{
+	const double th = (perp == 0.0 && z == 0.0) ? 0.0 : atan2(perp, z);
+#if defined(__CUDA_ARCH__)
+	sincos(0.5 * th, s, c);
+#else
+	*s = std::sin(0.5 * th);
+	*c = std::cos(0.5 * th);
+#endif
+}
+
+PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w)
+{
+	const LV A = g[perm[w.a]], B = g[perm[w.b]], Cb = g[perm[w.c]];
+	const LV I{vadd(A.p, B.p), A.e + B.e};
+	Kin k;
+	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
+	const double perp1 = sqrt(d1.x * d1.x + d1.y * d1.y);
+	k.phi = phiOf(d1.x, d1.y);
+	halfAngle(perp1, d1.z, &k.cX, &k.sX);
+	k.qX = sqrt(vdot(d1, d1));
+	const double pI = sqrt(vdot(I.p, I.p));
+	k.mI = sqrt((I.e - pI) * (I.e + pI));
+	// helicity frame of the isobar
+	const V3 zh = vunit(I.p);
+	const double perpI = sqrt(I.p.x * I.p.x + I.p.y * I.p.y);
+	const V3 yh = perpI > 0 ? V3{-I.p.y / perpI, I.p.x / perpI, 0.0} : V3{0.0, 1.0, 0.0};
+	const V3 xh = vcross(yh, zh);
+	const double ax = vdot(A.p, xh), ay = vdot(A.p, yh);
+	const double az = (I.e * vdot(A.p, zh) - pI * A.e) / k.mI;
+	const double perpA = sqrt(ax * ax + ay * ay);
+	k.phiH = phiOf(ax, ay);
+	halfAngle(perpA, az, &k.cI, &k.sI);
+	k.qI = sqrt(perpA * perpA + az * az);
+	return k;
+}
+
+// amplitude of wave w for one symmetrisation term
+PWA_HD C2 termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
+{
+	const C2 eM = cexpi(0.5 * w.M * k.phi);
+	const C2 eMc{eM.re, -eM.im};
+	// e^{i lam phiH / 2} stepped by e^{i phiH} from lam = lamIso of the first term
+	const C2 step = cexpi(k.phiH);
+	C2 eL{1.0, 0.0};
+	C2 sum{0.0, 0.0};
+	for (int t = w.lam0; t < w.lam1; ++t) {
+		const LamTerm& L = P.lams[t];
+		if (t == w.lam0)
+			eL = cexpi(0.5 * L.lamIso * k.phiH);
+		else
+			for (int s = P.lams[t - 1].lamIso; s < L.lamIso; s += 2)
+				eL = cmul(eL, step);
+		const double dP = dEval(P.dterms, L.plus0, L.plus1, k.cX, k.sX);
+		const double dM = dEval(P.dterms, L.minus0, L.minus1, k.cX, k.sX);
+		const double dI = dEval(P.dterms, L.iso0, L.iso1, k.cI, k.sI);
+		const C2 x = cadd(cscale(eM, L.cPlus * dP), cscale(eMc, L.cMinus * dM));
+		sum = cadd(sum, cmul(x, cscale(eL, dI)));
+	}
+	const double f = sqrt(barrierF2(P, w.LX, k.qX) * barrierF2(P, w.LI, k.qI));
+	return cscale(cmul(sum, massDependence(P, w, k.mI)), f);
+}
+
+// Gottfried-Jackson four-vectors of the three final-state particles of one
+// event: beam momentum bp, final-state momenta fp (lab)
+PWA_HD void gjFrame(const PlanView& P, const double bp[3], const double fp[3][3], LV g[3])
+{
+	LV f[3];
+	V3 pX{0.0, 0.0, 0.0};
+	double eX = 0.0;
+	for (int i = 0; i < 3; ++i) {
+		f[i].p = V3{fp[i][0], fp[i][1], fp[i][2]};
+		f[i].e = sqrt(P.masses[i] * P.masses[i] + vdot(f[i].p, f[i].p));
+		pX = vadd(pX, f[i].p);
+		eX += f[i].e;
+	}
+	const double pXa = sqrt(vdot(pX, pX));
+	const double mX = sqrt((eX - pXa) * (eX + pXa));
+	const V3 b{bp[0], bp[1], bp[2]};
+	const LV beam{b, sqrt(P.beamMass * P.beamMass + vdot(b, b))};
+	const V3 z = vunit(toRest(beam, pX, eX, mX).p);
+	const V3 y = vunit(vcross(b, pX));
+	const V3 x = vcross(y, z);
+	const double sgn = P.spaceInversion ? -1.0 : 1.0;
+	const double sgnY = P.reflection ? -sgn : sgn;
+	for (int i = 0; i < 3; ++i) {
+		const LV r = toRest(f[i], pX, eX, mX);
+		g[i] = LV{V3{sgn * vdot(r.p, x), sgnY * vdot(r.p, y), sgn * vdot(r.p, z)}, r.e};
+	}
+}
+
+// all waves of one event; out is complex128 [wave][ld] as interleaved doubles
+PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double fp[3][3], double* out, uint64_t ld,
+                            uint64_t e)
+{
+	LV g[3];
+	gjFrame(P, bp, fp, g);
+	Kin kin[kMaxPerms];
+	int topo = -1;
+	for (uint32_t o = 0; o < P.nWaves; ++o) {
+		const int wi = P.order[o];
+		const WaveDev w = P.waves[wi];
+		if (w.topo != topo) {
+			topo = w.topo;
+			for (uint32_t t = 0; t < P.nPerms; ++t)
+				kin[t] = kinematics(g, P.perms + 3 * t, w);
+		}
+		C2 a{0.0, 0.0};
+		for (uint32_t t = 0; t < P.nPerms; ++t)
+			a = cadd(a, termAmplitude(P, w, kin[t]));
+		a = cscale(a, P.boseFactor);
+		out[2 * ((uint64_t)wi * ld + e)] = a.re;
+		out[2 * ((uint64_t)wi * ld + e) + 1] = a.im;
+	}
+}
+
+}  // namespace iso
+}  // namespace pwa

@@ -1,0 +1,289 @@
+// isobar_plan.h -- host side of the three-body isobar amplitudes: spin
+// algebra and the wave plan that the per-event arithmetic (isobar_math.cuh)
+// reads.  Header-only so that the CPU tests can compile the plan builder and
+// the per-event arithmetic together without the CUDA runtime.
+//
+// Every spin, spin projection and orbital angular momentum is an integer in
+// units of 1/2 (2J, 2M, 2L), as in the reference (utilities/spinUtils.hpp).
+#pragma once
+
+#include "../../include/pwa_gb300.h"
+#include "isobar_math.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace pwa {
+namespace iso {
+
+inline double factorial(int n)
+{
+	double r = 1.0;
+	for (int i = 2; i <= n; ++i)
+		r *= i;
+	return r;
+}
+
+// (j1 m1 j2 m2 | J M) by Racah's formula, Condon-Shortley phase
+// (replaces clebschGordanCoeff, utilities/spinUtils.hpp:241-330)
+inline double clebschGordan(int j1, int m1, int j2, int m2, int J, int M)
+{
+	auto ok = [](int j, int m) { return j >= 0 && std::abs(m) <= j && ((j - m) & 1) == 0; };
+	if (!ok(j1, m1) || !ok(j2, m2) || !ok(J, M) || m1 + m2 != M)
+		return 0.0;
+	if (J < std::abs(j1 - j2) || J > j1 + j2 || ((j1 + j2 + J) & 1))
+		return 0.0;
+	const int a = (j1 + j2 - J) / 2, b = (j1 - m1) / 2, c = (j2 + m2) / 2;
+	const int d = (J - j2 + m1) / 2, e = (J - j1 - m2) / 2;
+	double sum = 0.0;
+	for (int k = std::max(0, std::max(-d, -e)); k <= std::min(a, std::min(b, c)); ++k)
+		sum += ((k & 1) ? -1.0 : 1.0) /
+		       (factorial(k) * factorial(a - k) * factorial(b - k) * factorial(c - k) * factorial(d + k) * factorial(e + k));
+	const double tri = (J + 1) * factorial((J + j1 - j2) / 2) * factorial((J - j1 + j2) / 2) * factorial(a) /
+	                   factorial((j1 + j2 + J) / 2 + 1);
+	const double proj = factorial((J + M) / 2) * factorial((J - M) / 2) * factorial(b) * factorial((j1 + m1) / 2) *
+	                    factorial((j2 - m2) / 2) * factorial(c);
+	return std::sqrt(tri * proj) * sum;
+}
+
+// Wigner's formula: d^j_{m n}(theta) as terms coef cos^a(theta/2) sin^b(theta/2)
+// (replaces dFunction, utilities/dFunction.hpp:52-170)
+inline void wignerTerms(int j, int m, int n, std::vector<DTerm>& out)
+{
+	const int jpm = (j + m) / 2, jmm = (j - m) / 2, jpn = (j + n) / 2, jmn = (j - n) / 2;
+	const int d = (m - n) / 2;
+	const double root = std::sqrt(factorial(jpm) * factorial(jmm) * factorial(jpn) * factorial(jmn));
+	for (int s = std::max(0, -d); s <= std::min(jpn, jmm); ++s) {
+		const double coef = (((d + s) & 1) ? -1.0 : 1.0) * root /
+		                    (factorial(jpn - s) * factorial(s) * factorial(d + s) * factorial(jmm - s));
+		out.push_back(DTerm{coef, jpn + jmm - 2 * s, d + 2 * s});
+	}
+}
+
+inline double wignerD(int j, int m, int n, double theta)
+{
+	std::vector<DTerm> t;
+	wignerTerms(j, m, n, t);
+	return dEval(t.data(), 0, (int)t.size(), std::cos(0.5 * theta), std::sin(0.5 * theta));
+}
+
+// Blatt-Weisskopf denominators.  x h_l(x) = (-i)^(l+1) e^{ix} sum_k a_k (i/2x)^k
+// with a_k = (l+k)! / (k! (l-k)!) (the reverse Bessel polynomial), so
+// |x h_l(x)|^2 z^l = P_l(z), z = x^2, with integer coefficients
+// [z^(l-m)] P_l = c_m / 4^m, c_m = sum_k (-1)^(m-k) a_{2m-k} a_k.  F_L^2 is
+// P_l(1) z^l / P_l(z): 1 at q = 0.1973 GeV/c, l = 0 .. 7 (replaces the table
+// in utilities/physUtils.hpp:200-262).
+inline void barrierPolynomials(double poly[8][8], double norm[8])
+{
+	for (int l = 0; l < 8; ++l) {
+		int64_t a[16] = {0};
+		for (int k = 0; k <= l; ++k) {
+			int64_t v = 1;  // (l+k)! / (k! (l-k)!)
+			for (int i = l - k + 1; i <= l + k; ++i)
+				v *= i;
+			for (int i = 2; i <= k; ++i)
+				v /= i;
+			a[k] = v;
+		}
+		for (int k = 0; k < 8; ++k)
+			poly[l][k] = 0.0;
+		for (int m = 0; m <= l; ++m) {
+			int64_t c = 0;
+			for (int k = 0; k <= 2 * m; ++k)
+				c += (((m - k) & 1) ? -1 : 1) * a[2 * m - k] * a[k];
+			poly[l][l - m] = (double)(c / ((int64_t)1 << (2 * m)));
+		}
+		double s = 0.0;
+		for (int k = 0; k <= l; ++k)
+			s += poly[l][k];
+		norm[l] = s;
+	}
+}
+
+// checks a wave; returns an empty string or the reason it is refused
+inline std::string checkWave(const pwa_isobar_wave& w, bool reflBasis)
+{
+	auto even = [](int x) { return (x & 1) == 0; };
+	if (w.J < 0 || w.J > kMaxSpin || w.isobarJ < 0 || w.isobarJ > kMaxSpin)
+		return "spins must be in 0 .. 16 (units of 1/2)";
+	if (!even(w.J) || !even(w.isobarJ) || !even(w.L) || !even(w.S) || !even(w.isobarL) || !even(w.isobarS) ||
+	    !even(w.M))
+		return "three spinless final-state particles: every spin and projection must be an integer (even in units of 1/2)";
+	if (std::abs(w.M) > w.J)
+		return "|M| > J";
+	if (reflBasis && w.M < 0)
+		return "the reflectivity basis needs M >= 0";
+	if ((w.P != 1 && w.P != -1) || (w.refl != 1 && w.refl != -1))
+		return "parity and reflectivity must be +1 or -1";
+	if (w.L < 0 || w.L > kMaxL || w.isobarL < 0 || w.isobarL > kMaxL)
+		return "orbital angular momenta must be in 0 .. 14 (units of 1/2)";
+	if (w.S < 0 || w.S > 2 * kMaxSpin || w.isobarS < 0 || w.isobarS > 2 * kMaxSpin)
+		return "coupled spins out of range";
+	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
+	if (a < 0 || b < 0 || c < 0 || a > 2 || b > 2 || c > 2 || a == b || a == c || b == c)
+		return "isobar daughters and bachelor must be three distinct final-state slots 0..2";
+	if (w.massDependence < kMassFlat || w.massDependence > kMassConstBw)
+		return "unknown mass dependence";
+	if (w.massDependence != kMassFlat && !(w.isobarMass > 0 && w.isobarWidth > 0))
+		return "a Breit-Wigner needs a positive mass and width";
+	return std::string();
+}
+
+struct Plan {
+	std::vector<WaveDev> waves;
+	std::vector<int32_t> order;
+	std::vector<LamTerm> lams;
+	std::vector<DTerm> dterms;
+	double bfPoly[8][8];
+	double bfNorm[8];
+	std::vector<int32_t> perms;
+	double boseFactor = 1.0;
+	double masses[3] = {0.0, 0.0, 0.0}, beamMass = 0.0;
+	int32_t spaceInversion = 0, reflection = 0;
+
+	PlanView view() const
+	{
+		PlanView v{};
+		v.waves = waves.data();
+		v.order = order.data();
+		v.lams = lams.data();
+		v.dterms = dterms.data();
+		v.bfPoly = &bfPoly[0][0];
+		v.bfNorm = bfNorm;
+		v.perms = perms.data();
+		v.nWaves = (uint32_t)waves.size();
+		v.nPerms = (uint32_t)(perms.size() / 3);
+		v.boseFactor = boseFactor;
+		for (int i = 0; i < 3; ++i)
+			v.masses[i] = masses[i];
+		v.beamMass = beamMass;
+		v.spaceInversion = spaceInversion;
+		v.reflection = reflection;
+		return v;
+	}
+};
+
+// permutations of the three final-state slots that only exchange particles
+// of equal species; factor 1/sqrt(number of terms) = 1/sqrt(prod n_k!)
+// (isobarDecayTopology::getBoseSymmetrization, isobarDecayTopology.cc:638-670)
+inline void bosePermutations(const int32_t species[3], bool bose, std::vector<int32_t>& perms, double& factor)
+{
+	perms.clear();
+	int p[3] = {0, 1, 2};
+	if (!bose) {
+		perms.assign(p, p + 3);
+		factor = 1.0;
+		return;
+	}
+	do {
+		if (species[p[0]] == species[0] && species[p[1]] == species[1] && species[p[2]] == species[2])
+			perms.insert(perms.end(), p, p + 3);
+	} while (std::next_permutation(p, p + 3));
+	factor = 1.0 / std::sqrt((double)(perms.size() / 3));
+}
+
+// wave plan of isobarHelicityAmplitude::twoBodyDecayAmplitude /
+// twoBodyDecayAmplitudeSum (isobarHelicityAmplitude.cc:130-195,
+// isobarAmplitude.cc:206-262) for every wave: the sum over the isobar's
+// helicities with the Clebsch-Gordan couplings, sqrt(2L+1) norms
+// (angMomNormFactor, physUtils.hpp:159-166) and the reflectivity-basis
+// combination (dFunction.hpp DFunctionReflConj) folded into coefficients.
+inline void buildPlan(const std::vector<pwa_isobar_wave>& specs, const double masses[3], const int32_t species[3],
+                      double beamMass, bool reflBasis, bool bose, bool spaceInversion, bool reflection, Plan& plan)
+{
+	for (int i = 0; i < 3; ++i)
+		plan.masses[i] = masses[i];
+	plan.beamMass = beamMass;
+	plan.spaceInversion = spaceInversion ? 1 : 0;
+	plan.reflection = reflection ? 1 : 0;
+	plan.waves.clear();
+	plan.lams.clear();
+	plan.dterms.clear();
+	barrierPolynomials(plan.bfPoly, plan.bfNorm);
+	bosePermutations(species, bose, plan.perms, plan.boseFactor);
+	std::vector<std::tuple<int, int, int, int>> topoKeys;
+	for (const pwa_isobar_wave& s : specs) {
+		WaveDev w{};
+		w.a = s.isobarDaughter1;
+		w.b = s.isobarDaughter2;
+		w.c = s.bachelor;
+		w.bachelorFirst = s.bachelorFirst ? 1 : 0;
+		w.M = s.M;
+		w.LX = s.L;
+		w.LI = s.isobarL;
+		w.massDep = s.massDependence;
+		w.m0 = s.isobarMass;
+		w.g0 = s.isobarWidth;
+		w.ma = masses[w.a];
+		w.mb = masses[w.b];
+		w.f2q0 = 1.0;
+		if (s.massDependence == kMassRelBw) {
+			// the PWA2000 rule q0 = sqrt|q0^2| (massDependence.cc:268-270)
+			w.q0 = std::sqrt(std::fabs(breakup2(s.isobarMass, w.ma, w.mb)));
+			const PlanView v = plan.view();
+			w.f2q0 = barrierF2(v, s.isobarL, w.q0);
+		}
+		const std::tuple<int, int, int, int> key(w.a, w.b, w.c, w.bachelorFirst);
+		auto it = std::find(topoKeys.begin(), topoKeys.end(), key);
+		w.topo = (int32_t)(it - topoKeys.begin());
+		if (it == topoKeys.end())
+			topoKeys.push_back(key);
+		// reflectivity combination of the X vertex
+		double wPlus = 1.0, wMinus = 0.0;
+		bool zero = false;
+		if (reflBasis) {
+			const int f = s.refl * s.P * ((((s.J - s.M) / 2) & 1) ? -1 : 1);
+			if (s.M == 0)
+				zero = (f == +1);
+			else {
+				wPlus = 1.0 / std::sqrt(2.0);
+				wMinus = -f / std::sqrt(2.0);
+			}
+		}
+		w.lam0 = (int32_t)plan.lams.size();
+		for (int lamIso = -s.isobarJ; lamIso <= s.isobarJ && !zero; lamIso += 2) {
+			// X -> daughter 1 + daughter 2 with helicities (l1, l2), spins (s1, s2)
+			const int s1 = s.bachelorFirst ? 0 : s.isobarJ, l1 = s.bachelorFirst ? 0 : lamIso;
+			const int s2 = s.bachelorFirst ? s.isobarJ : 0, l2 = s.bachelorFirst ? lamIso : 0;
+			const int lam = l1 - l2;
+			if (std::abs(lam) > s.J)
+				continue;
+			const double cgX = clebschGordan(s.L, 0, s.S, lam, s.J, lam) * clebschGordan(s1, l1, s2, -l2, s.S, lam);
+			const double cgI =
+			    clebschGordan(s.isobarL, 0, s.isobarS, 0, s.isobarJ, 0) * clebschGordan(0, 0, 0, 0, s.isobarS, 0);
+			if (cgX == 0.0 || cgI == 0.0)
+				continue;
+			const double c = std::sqrt(s.L + 1.0) * cgX * std::sqrt(s.isobarL + 1.0) * cgI;
+			LamTerm t{};
+			t.lamIso = lamIso;
+			t.plus0 = (int32_t)plan.dterms.size();
+			wignerTerms(s.J, s.M, lam, plan.dterms);
+			t.plus1 = (int32_t)plan.dterms.size();
+			t.minus0 = t.minus1 = t.plus1;
+			if (wMinus != 0.0) {
+				wignerTerms(s.J, -s.M, lam, plan.dterms);
+				t.minus1 = (int32_t)plan.dterms.size();
+			}
+			t.iso0 = (int32_t)plan.dterms.size();
+			wignerTerms(s.isobarJ, lamIso, 0, plan.dterms);
+			t.iso1 = (int32_t)plan.dterms.size();
+			t.cPlus = c * wPlus;
+			t.cMinus = c * wMinus;
+			plan.lams.push_back(t);
+		}
+		w.lam1 = (int32_t)plan.lams.size();
+		plan.waves.push_back(w);
+	}
+	plan.order.resize(plan.waves.size());
+	for (size_t i = 0; i < plan.order.size(); ++i)
+		plan.order[i] = (int32_t)i;
+	std::stable_sort(plan.order.begin(), plan.order.end(),
+	                 [&](int32_t x, int32_t y) { return plan.waves[x].topo < plan.waves[y].topo; });
+}
+
+}  // namespace iso
+}  // namespace pwa

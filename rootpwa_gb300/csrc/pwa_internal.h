@@ -311,4 +311,15 @@ int ampFileOpen(const char* path, AmpFile& f);
 // file bytes [offset, offset + bytes) -> device memory (synchronises s)
 int ampFileToDevice(const AmpFile& f, uint64_t offset, uint64_t bytes, void* dst, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Three-body isobar amplitudes (isobar.cu, plan in isobar_plan.h)
+// ---------------------------------------------------------------------------
+namespace iso {
+struct PlanView;
+}
+// amps complex128 [wave][n] from beam [3][n] and final state [3][3][n]
+// (device pointers; the view's arrays in device memory)
+int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const double* fs, uint64_t n, double* amps,
+                           cudaStream_t s);
+
 }  // namespace pwa

@@ -1,0 +1,190 @@
+"""Decay amplitudes of three spinless final-state particles in the isobar
+model (helicity formalism), evaluated on the GPU.
+
+Mirrors isobarHelicityAmplitude / isobarAmplitude
+(decayAmplitude/isobarAmplitude.h:53-120): the option switches
+enableReflectivityBasis, enableBoseSymmetrization, enableSpaceInversion and
+enableReflection, and the amplitude of every wave for every event.  A wave is
+what a three-body key file describes (waveDescription.cc:880-932): the X
+quantum numbers, X -> isobar + bachelor with (L, S), the isobar's spin, its
+decay's (L, S) and its mass dependence.  Spins, projections and orbital
+angular momenta are given in units of 1/2 (2J, 2M, 2L), as in the reference.
+
+    amp = isobarHelicityAmplitudes()
+    amp.setFinalState(["pi-", "pi+", "pi-"], [m_pi] * 3, beamMass=m_pi)
+    amp.addWave(J=2, P=+1, M=0, refl=+1, L=0, S=2, isobarJ=2, isobarL=2,
+                massDependence="relativisticBreitWigner", isobarMass=0.769,
+                isobarWidth=0.150, isobarDaughters=(1, 2), bachelor=0,
+                isobarName="rho(770)")
+    A = amp.amplitudes(beam, fs)       # complex128 [wave, event]
+
+beam is (N, 3) and fs (3, N, 3) lab momenta in GeV/c: numpy arrays (host)
+or CUDA tensors (device; the result is then a CUDA tensor).  Each row of the
+result goes straight into pwaLikelihood.addAmplitude.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2}
+
+
+def _qn(x):
+    """spinQn (utilities/conversionUtils.hpp:121-124) as printed: 0.5 * x."""
+    return ("%d" % (x // 2)) if x % 2 == 0 else ("%g" % (0.5 * x))
+
+
+def _par(x):
+    return "" if x == 0 else ("+" if x > 0 else "-")
+
+
+class isobarHelicityAmplitudes:
+    def __init__(self):
+        h = C.c_void_p()
+        N.call("pwa_isobar_create", C.byref(h))
+        self._h = h
+        self._names = None
+        self._waves = []
+        self._opts = [1, 1, 0, 0]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            try:
+                N.lib().pwa_isobar_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- final state and options ---------------------------------------------------
+    def setFinalState(self, names, masses, beamMass, species=None):
+        """names of the three final-state particles (equal names are identical
+        particles unless species says otherwise), their masses and the beam
+        mass in GeV/c^2."""
+        names = list(names)
+        if species is None:
+            ids = {}
+            species = [ids.setdefault(n, len(ids)) for n in names]
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        N.call("pwa_isobar_set_final_state", self._h, len(names), m.ctypes.data_as(N.pd),
+               sp.ctypes.data_as(C.POINTER(C.c_int32)), float(beamMass))
+        self._names = names
+
+    def _set_opts(self, k, flag):
+        o = list(self._opts)
+        o[k] = 1 if flag else 0
+        N.call("pwa_isobar_set_options", self._h, *o)
+        self._opts = o
+
+    def enableReflectivityBasis(self, flag=True):
+        self._set_opts(0, flag)
+
+    def enableBoseSymmetrization(self, flag=True):
+        self._set_opts(1, flag)
+
+    def enableSpaceInversion(self, flag=True):
+        self._set_opts(2, flag)
+
+    def enableReflection(self, flag=True):
+        self._set_opts(3, flag)
+
+    def reflectivityBasis(self):
+        return bool(self._opts[0])
+
+    def boseSymmetrization(self):
+        return bool(self._opts[1])
+
+    def doSpaceInversion(self):
+        return bool(self._opts[2])
+
+    def doReflection(self):
+        return bool(self._opts[3])
+
+    # -- waves ---------------------------------------------------------------------
+    def addWave(self, J, P, M, refl, L, S, isobarJ, isobarL, massDependence="flat", isobarMass=0.0,
+                isobarWidth=0.0, isobarDaughters=(0, 1), bachelor=2, bachelorFirst=False, isobarS=0,
+                isobarName="isobar", isospin=2, G=-1, C_=+1):
+        """adds one wave (all spins doubled); returns its index."""
+        md = MASS_DEPENDENCES[massDependence] if isinstance(massDependence, str) else int(massDependence)
+        w = N.IsobarWave(J=J, P=P, M=M, refl=refl, L=L, S=S, isobarJ=isobarJ, isobarL=isobarL, isobarS=isobarS,
+                         massDependence=md, isobarMass=isobarMass, isobarWidth=isobarWidth,
+                         isobarDaughter1=isobarDaughters[0], isobarDaughter2=isobarDaughters[1],
+                         bachelor=bachelor, bachelorFirst=1 if bachelorFirst else 0)
+        N.call("pwa_isobar_add_wave", self._h, C.byref(w))
+        self._waves.append(dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobarJ=isobarJ, isobarL=isobarL,
+                                isobarS=isobarS, isobarDaughters=tuple(isobarDaughters), bachelor=bachelor,
+                                bachelorFirst=bool(bachelorFirst), isobarName=isobarName, isospin=isospin, G=G,
+                                C=C_))
+        return len(self._waves) - 1
+
+    def nmbWaves(self):
+        n = C.c_uint32()
+        N.call("pwa_isobar_nmb_waves", self._h, C.byref(n))
+        return n.value
+
+    def nmbSymTerms(self):
+        n = C.c_uint32()
+        N.call("pwa_isobar_nmb_sym_terms", self._h, C.byref(n))
+        return n.value
+
+    def waveName(self, i):
+        """wave name in the layout of waveDescription::waveNameFromTopology
+        (waveDescription.cc:540-590): [I G,J P C,M refl]=[isobar=[a[L,S]b][L,S]bachelor]
+        with parentheses replaced by underscores."""
+        w = self._waves[i]
+        names = self._names or ["fs0", "fs1", "fs2"]
+        a, b = w["isobarDaughters"]
+        iso = "%s=[%s[%s,%s]%s]" % (w["isobarName"], names[a], _qn(w["isobarL"]), _qn(w["isobarS"]), names[b])
+        d1, d2 = (names[w["bachelor"]], iso) if w["bachelorFirst"] else (iso, names[w["bachelor"]])
+        s = "[%s%s,%s%s%s,%s%s]=[%s[%s,%s]%s]" % (_qn(w["isospin"]), _par(w["G"]), _qn(w["J"]), _par(w["P"]),
+                                                 _par(w["C"]), _qn(w["M"]), _par(w["refl"]), d1, _qn(w["L"]),
+                                                 _qn(w["S"]), d2)
+        return s.replace("(", "_").replace(")", "_")
+
+    # -- evaluation ----------------------------------------------------------------
+    def amplitudes(self, beam, fs):
+        """complex128 [wave, event] amplitudes for beam (N, 3) and final-state
+        (3, N, 3) lab momenta.  CUDA tensors in, CUDA tensor out."""
+        W = self.nmbWaves()
+        if hasattr(beam, "__cuda_array_interface__"):
+            import torch
+            b = beam.to(torch.float64).t().contiguous()                  # [3][N]
+            f = fs.to(torch.float64).permute(0, 2, 1).contiguous()       # [3][3][N]
+            n = b.shape[1]
+            out = torch.empty((W, n), dtype=torch.complex128, device=b.device)
+            N.call("pwa_isobar_amplitudes", self._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
+                   C.c_void_p(out.data_ptr()), N.MEMORY_DEVICE)
+            return out
+        b = np.ascontiguousarray(np.asarray(beam, dtype=np.float64).T)
+        f = np.ascontiguousarray(np.transpose(np.asarray(fs, dtype=np.float64), (0, 2, 1)))
+        if b.shape[0] != 3 or f.shape[:2] != (3, 3) or f.shape[2] != b.shape[1]:
+            raise ValueError("beam must be (N, 3) and fs (3, N, 3)")
+        n = b.shape[1]
+        out = np.empty((W, n), dtype=np.complex128)
+        N.call("pwa_isobar_amplitudes", self._h, b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), n,
+               out.ctypes.data_as(C.c_void_p), N.MEMORY_HOST)
+        return out
+
+
+def clebschGordanCoeff(j1, m1, j2, m2, J, M):
+    """(j1 m1 j2 m2 | J M), arguments doubled (utilities/spinUtils.hpp:241-330)."""
+    v = C.c_double()
+    N.call("pwa_clebsch_gordan", j1, m1, j2, m2, J, M, C.byref(v))
+    return v.value
+
+
+def dFunction(j, m, n, theta):
+    """Wigner d^j_{m n}(theta), arguments doubled (utilities/dFunction.hpp:52-170)."""
+    v = C.c_double()
+    N.call("pwa_wigner_d", j, m, n, float(theta), C.byref(v))
+    return v.value
+
+
+def barrierFactor(L, q):
+    """Blatt-Weisskopf barrier factor, 2L and breakup momentum q in GeV/c
+    (utilities/physUtils.hpp:265-278)."""
+    v = C.c_double()
+    N.call("pwa_barrier_factor", L, float(q), C.byref(v))
+    return v.value

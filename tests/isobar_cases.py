@@ -1,0 +1,58 @@
+"""Wave sets and events shared by the isobar-amplitude tests: seeded
+synthetic diffractive three-pion events (pi- pi+ pi-) and waves covering
+every mass dependence, both daughter orders at the X vertex, spins 0..4 of X
+and 0..3 of the isobar, M = 0..2 and both reflectivities.  Every wave
+conserves parity (P = (-1)^(L + l + 1) for three pseudoscalars)."""
+import numpy as np
+
+from oracle import isobar_oracle as O
+
+M_RHO, G_RHO = 0.7690, 0.1509
+M_F2, G_F2 = 1.2751, 0.1851
+M_RHO3, G_RHO3 = 1.6888, 0.161
+SPECIES = [0, 1, 0]              # pi-, pi+, pi-
+NAMES = ["pi-", "pi+", "pi-"]
+
+
+def waves():
+    """(oracle description, keyword arguments of isobarHelicityAmplitudes.addWave)."""
+    specs = [
+        # J  P  M refl L  S  j  l  massdep          mass    width  daughters bachelor first
+        (2, +1, 0, +1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 1++0+ rho S
+        (2, +1, 2, +1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 1++1+ rho S
+        (4, -1, 2, +1, 2, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 2-+1+ rho P
+        (4, +1, 2, -1, 4, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, True),    # 2++1- rho D, bachelor first
+        (0, -1, 0, +1, 0, 0, 0, 0, O.MASSDEP_FLAT, 0.0, 0.0, (1, 2), 0, False),          # 0-+0+ flat isobar
+        (4, -1, 0, +1, 4, 4, 4, 4, O.MASSDEP_CONST_BW, M_F2, G_F2, (1, 2), 0, False),   # 2-+0+ f2 S (const width)
+        (8, +1, 2, +1, 4, 6, 6, 6, O.MASSDEP_REL_BW, M_RHO3, G_RHO3, (2, 1), 0, False),  # 4++1+ rho3 D
+        (4, -1, 4, -1, 0, 4, 4, 4, O.MASSDEP_REL_BW, M_F2, G_F2, (0, 1), 2, False),     # 2-+2- f2 S, other pair
+        (2, +1, 0, -1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 1++0- (zero by reflectivity)
+    ]
+    out = []
+    md = {O.MASSDEP_FLAT: "flat", O.MASSDEP_REL_BW: "relativisticBreitWigner",
+          O.MASSDEP_CONST_BW: "constWidthBreitWigner"}
+    for J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first in specs:
+        ow = O.wave(J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first)
+        kw = dict(J=J, P=P, M=M, refl=r, L=L, S=S, isobarJ=j, isobarL=l, massDependence=md[m], isobarMass=mass,
+                  isobarWidth=width, isobarDaughters=dau, bachelor=bach, bachelorFirst=first)
+        out.append((ow, kw))
+    return out
+
+
+def events(n, seed=0):
+    return O.three_pion_events(n, seed=seed)
+
+
+def rel_err(A, B):
+    """max |A - B| per wave, relative to the wave's largest |A| (0 for a zero wave)."""
+    out = []
+    for a, b in zip(A, B):
+        s = np.abs(a).max()
+        out.append(np.abs(a - b).max() / s if s > 0 else np.abs(b).max())
+    return np.array(out)
+
+
+# FP64 tolerance: the lab momenta are ~190 GeV/c and the frames boost by
+# gamma ~ 100, so both FP64 restatements carry ~1e-10 relative rounding
+# (the oracle's own rotation invariance holds to ~6e-11)
+TOL = 1e-9

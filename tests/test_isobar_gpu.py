@@ -1,0 +1,130 @@
+"""GPU parity of the three-body isobar amplitude kernel (isobar.cu) against
+the FP64 oracle (oracle/isobar_oracle.py, which restates
+isobarHelicityAmplitude / isobarAmplitude, decayAmplitude/isobarAmplitude.cc:
+98-262, isobarHelicityAmplitude.cc:64-195), through the C ABI with host and
+device buffers; ragged and large event counts; and the chain events ->
+amplitudes -> integrals -> likelihood against the same chain in the oracle.
+
+Tolerance: max |A_gpu - A_oracle| per wave below 1e-9 of the wave's largest
+|A| (FP64 throughout; the frames boost ~190 GeV/c momenta by gamma ~ 100)."""
+import numpy as np
+import pytest
+
+import rootpwa_gb300 as R
+from oracle import isobar_oracle as O
+from rootpwa_gb300 import isobar as I
+import helpers
+from helpers import F_RTOL, G_NORMWISE, normwise, rel
+from isobar_cases import NAMES, SPECIES, TOL, events, rel_err, waves
+
+pytestmark = pytest.mark.gpu
+
+OPTIONS = [{}, {"bose": False}, {"space_inversion": True}, {"reflection": True},
+           {"space_inversion": True, "reflection": True}]
+SETTERS = {"bose": "enableBoseSymmetrization", "space_inversion": "enableSpaceInversion",
+           "reflection": "enableReflection", "reflectivity_basis": "enableReflectivityBasis"}
+
+
+def _amp(ws, masses, mb, opts=None):
+    A = I.isobarHelicityAmplitudes()
+    A.setFinalState(NAMES, masses, mb)
+    for k, v in (opts or {}).items():
+        getattr(A, SETTERS[k])(v)
+    for _, kw in ws:
+        A.addWave(**kw)
+    return A
+
+
+@pytest.mark.parametrize("opts", OPTIONS, ids=["default", "no-bose", "inversion", "reflection", "both"])
+def test_amplitudes_match_oracle_host_buffers(opts):
+    ws = waves()
+    beam, fs, masses, mb = events(2000, seed=11)
+    A = _amp(ws, masses, mb, opts)
+    got = A.amplitudes(beam, fs)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, **opts)
+    assert got.shape == ref.shape and got.dtype == np.complex128
+    err = rel_err(ref, got)
+    assert np.all(err < TOL), err
+    assert np.all(got[-1] == 0)                       # zero by reflectivity (M = 0, f = +1)
+
+
+def test_amplitudes_device_buffers_equal_host_buffers():
+    import torch
+    ws = waves()
+    beam, fs, masses, mb = events(3000, seed=12)
+    A = _amp(ws, masses, mb)
+    host = A.amplitudes(beam, fs)
+    dev = A.amplitudes(torch.from_numpy(beam).cuda(), torch.from_numpy(fs).cuda())
+    assert dev.is_cuda and dev.dtype == torch.complex128
+    assert np.array_equal(dev.cpu().numpy(), host)    # same kernel, same inputs: bitwise
+
+
+@pytest.mark.parametrize("n", [1, 31, 127, 129, 4099])
+def test_ragged_event_counts(n):
+    ws = waves()[:4]
+    beam, fs, masses, mb = events(n, seed=13)
+    got = _amp(ws, masses, mb).amplitudes(beam, fs)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES)
+    assert np.all(rel_err(ref, got) < TOL)
+
+
+def test_helicity_basis_negative_projection():
+    ws = [(dict(w, M=-w["M"]), dict(kw, M=-kw["M"])) for w, kw in waves()[:4]]
+    beam, fs, masses, mb = events(1000, seed=14)
+    got = _amp(ws, masses, mb, {"reflectivity_basis": False}).amplitudes(beam, fs)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, reflectivity_basis=False)
+    assert np.all(rel_err(ref, got) < TOL)
+
+
+def test_large_event_count_by_tiling():
+    """3,000,000 events (grid-stride loop well past one pass of the grid):
+    a 2,000-event block tiled 1,500 times gives 1,500 bitwise copies of the
+    block's amplitudes, and the block matches the oracle."""
+    import torch
+    ws = waves()
+    beam, fs, masses, mb = events(2000, seed=15)
+    A = _amp(ws, masses, mb)
+    small = A.amplitudes(torch.from_numpy(beam).cuda(), torch.from_numpy(fs).cuda())
+    reps = 1500
+    big = A.amplitudes(torch.from_numpy(beam).cuda().repeat(reps, 1), torch.from_numpy(fs).cuda().repeat(1, reps, 1))
+    assert big.shape == (len(ws), 2000 * reps)
+    assert torch.equal(big.view(len(ws), reps, 2000), small.unsqueeze(1).expand(-1, reps, -1))
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES)
+    assert np.all(rel_err(ref, small.cpu().numpy()) < TOL)
+
+
+def test_events_to_likelihood_chain():
+    """amplitudes of data and MC events on the GPU -> GPU integrals -> GPU
+    likelihood, against oracle amplitudes -> oracle integrals -> oracle
+    likelihood; FdF within the likelihood's tolerances."""
+    import torch
+    ws = waves()[:8]                                   # the non-zero waves
+    data = events(4000, seed=21)
+    mc = events(20000, seed=22)
+    masses, mb = data[2], data[3]
+    A = _amp(ws, masses, mb)
+    names = ["w%d_%s" % (k, A.waveName(k)) for k in range(len(ws))]
+    refl = [kw["refl"] for _, kw in ws]
+    accepted = np.random.default_rng(23).random(20000) < 0.7
+    Ow = [w for w, _ in ws]
+    w_or = dict(names=names, refl=refl, rank=1,
+                data=O.amplitudes(Ow, data[0], data[1], masses, mb, SPECIES),
+                mc=O.amplitudes(Ow, mc[0], mc[1], masses, mb, SPECIES), accepted=accepted)
+    Lo = helpers.build_oracle(w_or)
+    d_data = A.amplitudes(torch.from_numpy(data[0]).cuda(), torch.from_numpy(data[1]).cuda())
+    d_mc = A.amplitudes(torch.from_numpy(mc[0]).cuda(), torch.from_numpy(mc[1]).cuda())
+    w_gpu = dict(w_or, data=d_data, mc=d_mc)
+    norm, acc = helpers.gpu_integrals(w_gpu, precision="fp64")
+    Lg = helpers.build_gpu(w_gpu, norm, acc, amps=[d_data[k] for k in range(len(ws))])
+    p = np.random.default_rng(24).standard_normal(Lg.nmbPars())
+    f0, g0 = Lo.FdF(p)
+    f1, g1 = Lg.FdF(p)
+    assert rel(f1, f0) < F_RTOL
+    assert normwise(g1, g0) < G_NORMWISE
+
+
+def test_no_events():
+    ws = waves()[:2]
+    beam, fs, masses, mb = events(10, seed=1)
+    out = _amp(ws, masses, mb).amplitudes(np.zeros((0, 3)), np.zeros((3, 0, 3)))
+    assert out.shape == (2, 0)

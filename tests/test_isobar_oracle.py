@@ -1,0 +1,142 @@
+"""Pins of the isobar-amplitude oracle (oracle/isobar_oracle.py): its
+Clebsch-Gordan coefficients against sympy, its Wigner d functions against
+the PDG closed forms and the group properties, its barrier factors against
+the closed forms of F_1..F_3 (utilities/physUtils.hpp:200-262 quotes the same
+functions), and its amplitudes against the symmetries the frames must have:
+invariance under a rotation of the whole event, the reflectivity eigenvalue
+under reflection through the production plane (isobarAmplitude.cc:188-203),
+the parity eigenvalue under space inversion (:174-186) and Bose symmetry."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import isobar_oracle as O
+from isobar_cases import SPECIES, events, waves
+
+
+def test_clebsch_gordan_against_sympy():
+    cg = pytest.importorskip("sympy.physics.quantum.cg")
+    from sympy import Rational
+    n = 0
+    for j1 in range(0, 7):
+        for j2 in range(0, 5):
+            for J in range(abs(j1 - j2), j1 + j2 + 1, 2):
+                for m1 in range(-j1, j1 + 1, 2):
+                    for m2 in range(-j2, j2 + 1, 2):
+                        if abs(m1 + m2) > J:
+                            continue
+                        ref = float(cg.CG(Rational(j1, 2), Rational(m1, 2), Rational(j2, 2), Rational(m2, 2),
+                                          Rational(J, 2), Rational(m1 + m2, 2)).doit())
+                        assert abs(O.clebsch_gordan(j1, m1, j2, m2, J, m1 + m2) - ref) < 1e-13
+                        n += 1
+    assert n > 1000
+    # selection rules give exact zeros
+    assert O.clebsch_gordan(2, 0, 2, 0, 2, 0) == 0.0          # (1 0 1 0 | 1 0)
+    assert O.clebsch_gordan(2, 2, 2, 0, 2, 0) == 0.0          # M != m1 + m2
+
+
+@pytest.mark.parametrize("theta", [0.0, 0.3, 1.2, 2.5, math.pi])
+def test_wigner_d_closed_forms(theta):
+    c, s = math.cos(theta), math.sin(theta)
+    table = {  # PDG: Clebsch-Gordan coefficients, spherical harmonics and d functions
+        (1, 1, 1): math.cos(theta / 2), (1, 1, -1): -math.sin(theta / 2),
+        (2, 2, 2): (1 + c) / 2, (2, 2, 0): -s / math.sqrt(2), (2, 2, -2): (1 - c) / 2, (2, 0, 0): c,
+        (4, 4, 4): ((1 + c) / 2) ** 2, (4, 4, 2): -(1 + c) * s / 2, (4, 4, 0): math.sqrt(6) / 4 * s * s,
+        (4, 2, 2): (1 + c) * (2 * c - 1) / 2, (4, 2, 0): -math.sqrt(1.5) * s * c, (4, 0, 0): 1.5 * c * c - 0.5,
+        (3, 3, 3): math.cos(theta / 2) ** 3, (3, 3, 1): -math.sqrt(3) * (1 + c) / 2 * math.sin(theta / 2),
+        (6, 0, 0): (5 * c ** 3 - 3 * c) / 2,
+    }
+    for (j, m, n), v in table.items():
+        assert abs(O.wigner_d(j, m, n, theta) - v) < 1e-14, (j, m, n)
+
+
+@pytest.mark.parametrize("j", [1, 2, 3, 4, 6, 8])
+def test_wigner_d_group_properties(j):
+    ms = list(range(-j, j + 1, 2))
+    a, b = 0.7, 1.9
+
+    def mat(t):
+        return np.array([[O.wigner_d(j, m, n, t) for n in ms] for m in ms])
+    D = mat(a)
+    assert np.allclose(D @ D.T, np.eye(len(ms)), atol=1e-13)             # orthogonal
+    assert np.allclose(mat(a) @ mat(b), mat(a + b), atol=1e-13)          # d(a) d(b) = d(a + b)
+    for i, m in enumerate(ms):
+        for k, n in enumerate(ms):
+            assert abs(D[i, k] - (-1) ** ((m - n) // 2) * D[k, i]) < 1e-14   # d_mn = (-1)^(m-n) d_nm
+            assert abs(D[i, k] - D[len(ms) - 1 - k, len(ms) - 1 - i]) < 1e-14  # d_mn = d_{-n,-m}
+
+
+def test_barrier_factor_closed_forms():
+    for q in [0.01, 0.1, 0.1973, 0.35, 0.8, 2.0]:
+        z = (q / O.PR_DEFAULT) ** 2
+        forms = {2: 2 * z / (z + 1), 4: 13 * z * z / (z * (z + 3) + 9),
+                 6: 277 * z ** 3 / (z * (z * (z + 6) + 45) + 225)}
+        assert float(O.barrier_factor(0, q)) == 1.0
+        for L, f2 in forms.items():
+            assert abs(float(O.barrier_factor(L, q)) ** 2 - f2) < 1e-12 * max(1.0, f2)
+    for L in range(0, 16, 2):
+        assert abs(float(O.barrier_factor(L, O.PR_DEFAULT)) - 1.0) < 1e-13
+
+
+def test_breit_wigner_forms():
+    m = np.linspace(0.3, 1.5, 50)
+    bw = O.const_width_bw(m, 0.77, 0.15)
+    assert np.allclose(bw, 0.77 * 0.15 / (0.77 ** 2 - m ** 2 - 1j * 0.77 * 0.15))
+    rel = O.relativistic_bw(m, 0.1396, 0.1396, 0.77, 0.15, 2)
+    k = np.argmin(abs(m - 0.77))
+    assert abs(rel[k].imag) > abs(rel[k].real)                               # on the peak: ~ i
+    assert np.allclose(abs(O.relativistic_bw(np.array([0.77]), 0.1396, 0.1396, 0.77, 0.15, 2)), 1.0)
+
+
+@pytest.fixture(scope="module")
+def sample():
+    beam, fs, masses, mb = events(600, seed=3)
+    W = [w for w, _ in waves()]
+    return W, beam, fs, masses, mb, O.amplitudes(W, beam, fs, masses, mb, SPECIES)
+
+
+def test_rotation_invariance(sample):
+    W, beam, fs, masses, mb, A = sample
+    R = O._rot("z", np.full(1, 0.4))[0] @ O._rot("y", np.full(1, 1.1))[0] @ O._rot("x", np.full(1, -0.3))[0]
+    B = O.amplitudes(W, beam @ R.T, np.einsum("ij,knj->kni", R, fs), masses, mb, SPECIES)
+    assert np.abs(A - B).max() < 1e-9 * np.abs(A).max()
+
+
+def test_reflection_and_parity_eigenvalues(sample):
+    """reflection through the production plane multiplies a wave of
+    reflectivity refl by refl; space inversion by -P (P times the intrinsic
+    parity (-1)^3 of three pseudoscalars, which the amplitudes leave out)."""
+    W, beam, fs, masses, mb, A = sample
+    Ar = O.amplitudes(W, beam, fs, masses, mb, SPECIES, reflection=True)
+    Ap = O.amplitudes(W, beam, fs, masses, mb, SPECIES, space_inversion=True)
+    for k, w in enumerate(W):
+        s = np.abs(A[k]).max()
+        if s == 0:
+            continue
+        assert np.abs(Ar[k] - w["refl"] * A[k]).max() < 1e-10 * s
+        assert np.abs(Ap[k] + w["P"] * A[k]).max() < 1e-10 * s
+
+
+def test_bose_symmetry(sample):
+    W, beam, fs, masses, mb, A = sample
+    swapped = fs[[2, 1, 0]]
+    B = O.amplitudes(W, beam, swapped, masses, mb, SPECIES)
+    assert np.abs(A - B).max() < 1e-12 * np.abs(A).max()
+    # the symmetrised amplitude is the normalised sum of the two terms
+    A0 = O.amplitudes(W, beam, fs, masses, mb, SPECIES, bose=False)
+    A1 = O.amplitudes(W, beam, swapped, masses, mb, SPECIES, bose=False)
+    assert np.abs(A - (A0 + A1) / math.sqrt(2)).max() < 1e-12 * np.abs(A).max()
+
+
+def test_reflectivity_basis_combination(sample):
+    """DFunctionReflConj: A(M, refl) = (A(+M) - f A(-M)) / sqrt 2 with the
+    plain helicity basis, f = refl P (-1)^(J - M)."""
+    W, beam, fs, masses, mb, A = sample
+    for k, w in enumerate(W):
+        if w["M"] == 0:
+            continue
+        plus = O.amplitudes([w], beam, fs, masses, mb, SPECIES, reflectivity_basis=False)[0]
+        minus = O.amplitudes([dict(w, M=-w["M"])], beam, fs, masses, mb, SPECIES, reflectivity_basis=False)[0]
+        f = O.reflectivity_factor(w["J"], w["P"], w["M"], w["refl"])
+        assert np.abs(A[k] - (plus - f * minus) / math.sqrt(2)).max() < 1e-12 * np.abs(A[k]).max()
