@@ -59,9 +59,10 @@ def parse():
                     help="arithmetic of the normalisation / acceptance integrals (set-up, not timed)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
-    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision", "next"],
+    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision", "next", "isobar"],
                     help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
-                         "learned warm start; precision: error of each arithmetic variant against FP64")
+                         "learned warm start; precision: error of each arithmetic variant against FP64; "
+                         "isobar: decay amplitudes of the 88-wave 3pi set")
     ap.add_argument("--oracle-mc", type=int, default=200_000,
                     help="precision: MC events of the integrals compared with the CPU FP64 oracle")
     ap.add_argument("--bins", type=int, default=400, help="multibin: kinematic bins (100 mass x 4 t')")
@@ -846,12 +847,111 @@ def run_next(args):
     return 0
 
 
+def run_isobar(args):
+    """Decay amplitudes of the 88-wave pi- pi+ pi- isobar set (three spinless
+    final-state particles, helicity formalism) for --n-data events: events/s.
+    value: momenta resident in HBM, one call of pwa_isobar_amplitudes per step
+    on torch's stream, CUDA events around the timed steps; e2e: host momenta
+    in, host amplitudes out through the Python API (both copies inside); the
+    FP64 oracle on a bounded sample as the CPU baseline."""
+    import ctypes as C
+    import torch
+    from rootpwa_gb300 import _native as Nn
+    from rootpwa_gb300 import isobar as I
+    from rootpwa_gb300 import synth
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    kws = synth.three_pion_waves()
+    W, n = len(kws), args.n_data
+    beam, fs, masses, mb = synth.three_pion_events(n, seed=31 + rank)
+    A = I.isobarHelicityAmplitudes()
+    A.setFinalState(["pi-", "pi+", "pi-"], masses, mb)
+    for kw in kws:
+        A.addWave(**kw)
+    stream = torch.cuda.current_stream()
+    A.setStream(stream)
+    dev = torch.device("cuda", local)
+    b = torch.from_numpy(np.ascontiguousarray(beam.T)).to(dev)                        # [3][N]
+    f = torch.from_numpy(np.ascontiguousarray(np.transpose(fs, (0, 2, 1)))).to(dev)   # [3][3][N]
+    out = torch.empty((W, n), dtype=torch.complex128, device=dev)
+
+    def step():
+        Nn.call("pwa_isobar_amplitudes", A._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
+                C.c_void_p(out.data_ptr()), Nn.MEMORY_DEVICE)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 50))
+    launches0 = Nn.lib().pwa_kernel_launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / steps
+    launches = Nn.lib().pwa_kernel_launch_count() - launches0
+    # parity of the timed output on a sample against the FP64 oracle
+    from oracle import isobar_oracle as O
+    n_check = min(n, 1000)
+    ows = [O.wave(kw["J"], kw["P"], kw["M"], kw["refl"], kw["L"], kw["S"], kw["isobarJ"], kw["isobarL"],
+                  I.MASS_DEPENDENCES[kw["massDependence"]], kw["isobarMass"], kw["isobarWidth"],
+                  kw["isobarDaughters"], kw["bachelor"]) for kw in kws]
+    t0 = time.perf_counter()
+    ref = O.amplitudes(ows, beam[:n_check], fs[:, :n_check], masses, mb, [0, 1, 0])
+    t_cpu = time.perf_counter() - t0
+    got = out[:, :n_check].cpu().numpy()
+    err = max(float(np.abs(got[k] - ref[k]).max() / np.abs(ref[k]).max()) for k in range(W))
+    # end to end through the Python API with host buffers
+    B = I.isobarHelicityAmplitudes()
+    B.setFinalState(["pi-", "pi+", "pi-"], masses, mb)
+    for kw in kws:
+        B.addWave(**kw)
+    B.amplitudes(beam, fs)
+    e2e_steps = max(1, min(steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        B.amplitudes(beam, fs)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    hbm, peak_kind = measured_peaks()
+    algo_bytes = n * (12 * 8 + W * 16)
+    achieved = algo_bytes / (ms * 1e-3) / 1e9
+    line = {
+        "metric": "isobar amplitudes: events/s at 88 waves (pi- pi+ pi-, helicity formalism)",
+        "value": n / (ms * 1e-3), "unit": "events/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded diffractive 3pi events (phase space), 88-wave isobar set",
+        "config": {"workload": "isobar3pi88", "events": n, "waves": W, "sym_terms": A.nmbSymTerms(),
+                   "l2": "inputs and outputs (%.2f GB) larger than L2" % (algo_bytes / 1e9)},
+        "e2e": {"value": n / t_e2e, "unit": "events/s", "h2d_bytes_per_step": n * 12 * 8,
+                "d2h_bytes_per_step": n * W * 16},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_kind": peak_kind,
+                     "note": "algorithmic bytes (96 B in + 16 B per wave out per event); the kernel is bound by "
+                             "the FP64 arithmetic rate, not by HBM"},
+        "cpu_baseline": {"value": n_check / t_cpu, "unit": "events/s", "cores": 1, "kind": "port",
+                         "sample": "FP64 oracle (numpy) on %d events x %d waves" % (n_check, W)},
+        "max_rel_err_vs_oracle": err,
+        "clocks": clk,
+    }
+    emit(line, args)
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "precision":
         return run_precision(args)
     if args.workload == "next":
         return run_next(args)
+    if args.workload == "isobar":
+        return run_isobar(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "multibin":

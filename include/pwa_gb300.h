@@ -464,6 +464,10 @@ int pwa_isobar_set_final_state(pwa_isobar* A, uint32_t nFsParticles, const doubl
  * defaults 1, 1, 0, 0 */
 int pwa_isobar_set_options(pwa_isobar* A, int reflectivityBasis, int boseSymmetrize, int spaceInversion,
                            int reflection);
+/* no reference counterpart: run on the caller's CUDA stream (NULL = the
+ * default stream); calls with device buffers are then asynchronous in stream
+ * order, calls with host buffers still return with the results in place */
+int pwa_isobar_set_stream(pwa_isobar* A, void* cudaStream);
 int pwa_isobar_add_wave(pwa_isobar* A, const pwa_isobar_wave* wave);
 int pwa_isobar_nmb_waves(const pwa_isobar* A, uint32_t* n);
 /* number of symmetrisation terms of the current final state and options */

@@ -339,59 +339,3 @@ def wave(J, P, M, refl, L, S, isobar_J, isobar_L, mass_dep, isobar_mass=0.0, iso
     return dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobar_J=isobar_J, isobar_L=isobar_L, isobar_S=isobar_S,
                 mass_dep=mass_dep, isobar_mass=isobar_mass, isobar_width=isobar_width,
                 isobar_daughters=tuple(isobar_daughters), bachelor=bachelor, bachelor_first=bool(bachelor_first))
-
-
-def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2):
-    """seeded synthetic diffractive events pi- p -> (pi- pi+ pi-) p: the beam
-    along z with a small divergence, X of mass uniform in [m_lo, m_hi] with a
-    small transverse momentum, decaying by three-body phase space (uniform in
-    the two Dalitz variables, accepted inside the kinematic border).  Returns
-    beam (N, 3), final state (3, N, 3) momenta, masses (3,), beam mass."""
-    rng = np.random.default_rng(seed)
-    mpi = 0.13957039
-    masses = np.array([mpi, mpi, mpi])
-    beam = np.stack([rng.normal(0, 0.05, n), rng.normal(0, 0.05, n), np.full(n, beam_momentum)], axis=1)
-    MX = rng.uniform(m_lo, m_hi, n)
-    # X momentum: beam direction with a transverse kick
-    pX = beam.copy()
-    pX[:, 0] += rng.normal(0, 0.3, n)
-    pX[:, 1] += rng.normal(0, 0.3, n)
-    pX[:, 2] *= rng.uniform(0.95, 1.0, n)
-    EX = np.sqrt(MX ** 2 + np.sum(pX ** 2, axis=1))
-    # Dalitz variables m12^2, m23^2 by rejection inside the border
-    fs_rf = np.zeros((3, n, 4))
-    todo = np.arange(n)
-    while todo.size:
-        M = MX[todo]
-        s12 = rng.uniform((2 * mpi) ** 2, (M - mpi) ** 2)
-        s23 = rng.uniform((2 * mpi) ** 2, (M - mpi) ** 2)
-        # energies in the X rest frame
-        E3 = (M * M + mpi * mpi - s12) / (2 * M)
-        E1 = (M * M + mpi * mpi - s23) / (2 * M)
-        E2 = M - E1 - E3
-        p1, p2, p3 = [np.sqrt(np.maximum(E * E - mpi * mpi, 0)) for E in (E1, E2, E3)]
-        ok = (E1 > mpi) & (E2 > mpi) & (E3 > mpi)
-        with np.errstate(invalid="ignore", divide="ignore"):
-            c13 = (p2 ** 2 - p1 ** 2 - p3 ** 2) / (2 * p1 * p3)
-        ok &= np.abs(c13) < 1
-        good = np.nonzero(ok)[0]
-        if good.size:
-            idx = todo[good]
-            c = c13[good]
-            sn = np.sqrt(1 - c * c)
-            v1 = np.stack([np.zeros(good.size), np.zeros(good.size), p1[good]], axis=1)
-            v3 = p3[good][:, None] * np.stack([sn, np.zeros(good.size), c], axis=1)
-            v2 = -(v1 + v3)
-            # random orientation
-            a, b, g = rng.uniform(0, 2 * np.pi, good.size), np.arccos(rng.uniform(-1, 1, good.size)), \
-                rng.uniform(0, 2 * np.pi, good.size)
-            R = np.einsum("nij,njk->nik", _rot("z", a), np.einsum("nij,njk->nik", _rot("y", b), _rot("z", g)))
-            for i, (v, E) in enumerate(((v1, E1), (v2, E2), (v3, E3))):
-                fs_rf[i, idx, :3] = np.einsum("nij,nj->ni", R, v)
-                fs_rf[i, idx, 3] = E[good]
-        todo = todo[~ok]
-    # boost to the lab
-    bX = pX / EX[:, None]
-    fs = np.stack([_boost(fs_rf[i], bX)[:, :3] for i in range(3)])
-    # particle order: pi- (0), pi+ (1), pi- (2)
-    return beam, fs, masses, mpi

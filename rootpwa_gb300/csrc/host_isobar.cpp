@@ -17,9 +17,11 @@ struct pwa_isobar {
 	DevBuf dPlan, dIn, dOut;
 	iso::PlanView devView{};
 	cudaStream_t stream = nullptr;
+	bool ownStream = false;   // created here (destroyed here)
+	bool userStream = false;  // set by pwa_isobar_set_stream: device-buffer calls are asynchronous
 	~pwa_isobar()
 	{
-		if (stream)
+		if (ownStream && stream)
 			cudaStreamDestroy(stream);
 	}
 };
@@ -115,6 +117,20 @@ int pwa_isobar_set_final_state(pwa_isobar* A, uint32_t nFs, const double* masses
 	return kOk;
 }
 
+int pwa_isobar_set_stream(pwa_isobar* A, void* s)
+{
+	if (!A)
+		return setError(kErrArg, "null argument");
+	if (A->ownStream && A->stream) {
+		cudaStreamSynchronize(A->stream);
+		cudaStreamDestroy(A->stream);
+	}
+	A->ownStream = false;
+	A->userStream = true;
+	A->stream = static_cast<cudaStream_t>(s);  // NULL: the CUDA default stream
+	return kOk;
+}
+
 int pwa_isobar_set_options(pwa_isobar* A, int reflectivityBasis, int boseSymmetrize, int spaceInversion, int reflection)
 {
 	if (!A)
@@ -179,8 +195,10 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 	const uint64_t W = A->waves.size();
 	if (n > (uint64_t)1 << 40 || W * n > ((uint64_t)1 << 62) / 16)
 		return setError(kErrArg, "too many events");
-	if (!A->stream)
+	if (!A->stream && !A->userStream) {
 		PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking), "stream create"));
+		A->ownStream = true;
+	}
 	if (A->dirty)
 		PWA_TRY(uploadPlan(A));
 	const double* dBeam = beam;
@@ -197,13 +215,16 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 		dBeam = in;
 		dFs = in + 3 * n;
 		dAmps = A->dOut.as<double>();
-	} else {
+	} else if (!A->userStream) {
 		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device momenta"));
 	}
 	PWA_TRY(launchIsobarAmplitudes(A->devView, dBeam, dFs, n, dAmps, A->stream));
 	if (memory == PWA_MEMORY_HOST)
 		PWA_TRY(cudaCheck(cudaMemcpyAsync(amps, dAmps, W * n * 16, cudaMemcpyDeviceToHost, A->stream),
 		                  "amplitude download"));
+	// on the caller's stream, device-buffer calls stay asynchronous (stream order)
+	if (memory == PWA_MEMORY_DEVICE && A->userStream)
+		return kOk;
 	return cudaCheck(cudaStreamSynchronize(A->stream), "isobar amplitudes");
 }
 

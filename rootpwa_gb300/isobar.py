@@ -48,6 +48,8 @@ class isobarHelicityAmplitudes:
         self._names = None
         self._waves = []
         self._opts = [1, 1, 0, 0]
+        self._async = False
+        self._stream = 0
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -102,6 +104,14 @@ class isobarHelicityAmplitudes:
     def doReflection(self):
         return bool(self._opts[3])
 
+    def setStream(self, stream):
+        """run on this CUDA stream (a torch.cuda.Stream, a raw handle or None
+        for the default stream); device-buffer calls are then asynchronous."""
+        h = getattr(stream, "cuda_stream", stream)
+        N.call("pwa_isobar_set_stream", self._h, C.c_void_p(h or 0))
+        self._async = True
+        self._stream = h or 0
+
     # -- waves ---------------------------------------------------------------------
     def addWave(self, J, P, M, refl, L, S, isobarJ, isobarL, massDependence="flat", isobarMass=0.0,
                 isobarWidth=0.0, isobarDaughters=(0, 1), bachelor=2, bachelorFirst=False, isobarS=0,
@@ -154,6 +164,13 @@ class isobarHelicityAmplitudes:
             f = fs.to(torch.float64).permute(0, 2, 1).contiguous()       # [3][3][N]
             n = b.shape[1]
             out = torch.empty((W, n), dtype=torch.complex128, device=b.device)
+            if self._async and self._stream:
+                # the kernel runs on the caller's stream: order it after the
+                # layout copies above and keep their memory until it has run
+                es = torch.cuda.ExternalStream(self._stream, device=b.device)
+                es.wait_stream(torch.cuda.current_stream(b.device))
+                for t in (b, f, out):
+                    t.record_stream(es)
             N.call("pwa_isobar_amplitudes", self._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
                    C.c_void_p(out.data_ptr()), N.MEMORY_DEVICE)
             return out

@@ -18,6 +18,10 @@ synthetic decay amplitudes with the shapes of the standard workloads:
 Production amplitudes have re/im ~ N(0, 1) in the reference's parameter
 layout.  All draws are float32 (the device store is complex64); the FP64
 oracle receives the complex128 cast of the very same values.
+
+For the decay-amplitude step: ``three_pion_events`` draws diffractive
+pi- p -> (pi- pi+ pi-) p events (lab momenta) and ``three_pion_waves`` lists a
+COMPASS-like 3pi isobar wave set.
 """
 import numpy as np
 
@@ -154,3 +158,117 @@ def draw_bin_device(model, v_true, flat, n_events, seed, pool_factor=4, device="
     g.manual_seed(int(seed) + 7919)
     idx = torch.multinomial(inten, n_events, replacement=True, generator=g)
     return pool[:, idx].contiguous()
+
+
+# -- three-pion events and waves for the decay-amplitude step ---------------------
+
+M_PI = 0.13957039
+
+
+def _rotation(axis, a):
+    c, s = np.cos(a), np.sin(a)
+    o, z = np.ones_like(a), np.zeros_like(a)
+    m = {"y": [[c, z, s], [z, o, z], [-s, z, c]], "z": [[c, -s, z], [s, c, z], [z, z, o]]}[axis]
+    return np.moveaxis(np.array(m), (0, 1), (-2, -1))
+
+
+def _boost(p, E, b):
+    b2 = np.sum(b * b, axis=-1)
+    g = 1.0 / np.sqrt(1.0 - b2)
+    bp = np.sum(b * p, axis=-1)
+    g2 = np.where(b2 > 0, (g - 1.0) / np.where(b2 > 0, b2, 1.0), 0.0)
+    return p + (g2 * bp)[:, None] * b + (g * E)[:, None] * b
+
+
+def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2):
+    """Seeded diffractive events pi- p -> (pi- pi+ pi-) p: the beam along z
+    with a small divergence, X of mass uniform in [m_lo, m_hi] GeV/c^2 with a
+    small transverse momentum, decaying by three-body phase space (uniform in
+    the Dalitz plane).  Returns beam (N, 3), final state (3, N, 3) lab
+    momenta in GeV/c (particle order pi-, pi+, pi-), the three masses and the
+    beam mass."""
+    rng = np.random.default_rng(seed)
+    m = M_PI
+    beam = np.stack([rng.normal(0, 0.05, n), rng.normal(0, 0.05, n), np.full(n, beam_momentum)], axis=1)
+    MX = rng.uniform(m_lo, m_hi, n)
+    pX = beam.copy()
+    pX[:, 0] += rng.normal(0, 0.3, n)
+    pX[:, 1] += rng.normal(0, 0.3, n)
+    pX[:, 2] *= rng.uniform(0.95, 1.0, n)
+    EX = np.sqrt(MX ** 2 + np.sum(pX ** 2, axis=1))
+    rest = np.zeros((3, n, 4))
+    todo = np.arange(n)
+    while todo.size:
+        M = MX[todo]
+        s12 = rng.uniform((2 * m) ** 2, (M - m) ** 2)
+        s23 = rng.uniform((2 * m) ** 2, (M - m) ** 2)
+        E3 = (M * M + m * m - s12) / (2 * M)
+        E1 = (M * M + m * m - s23) / (2 * M)
+        E2 = M - E1 - E3
+        p1, p2, p3 = [np.sqrt(np.maximum(E * E - m * m, 0)) for E in (E1, E2, E3)]
+        ok = (E1 > m) & (E2 > m) & (E3 > m)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            c13 = (p2 ** 2 - p1 ** 2 - p3 ** 2) / (2 * p1 * p3)
+        ok &= np.abs(c13) < 1
+        good = np.nonzero(ok)[0]
+        if good.size:
+            idx = todo[good]
+            c = c13[good]
+            z0 = np.zeros(good.size)
+            v1 = np.stack([z0, z0, p1[good]], axis=1)
+            v3 = p3[good][:, None] * np.stack([np.sqrt(1 - c * c), z0, c], axis=1)
+            v2 = -(v1 + v3)
+            a, b, g = (rng.uniform(0, 2 * np.pi, good.size), np.arccos(rng.uniform(-1, 1, good.size)),
+                       rng.uniform(0, 2 * np.pi, good.size))
+            R = np.einsum("nij,njk->nik", _rotation("z", a),
+                          np.einsum("nij,njk->nik", _rotation("y", b), _rotation("z", g)))
+            for i, (v, E) in enumerate(((v1, E1), (v2, E2), (v3, E3))):
+                rest[i, idx, :3] = np.einsum("nij,nj->ni", R, v)
+                rest[i, idx, 3] = E[good]
+        todo = todo[~ok]
+    bX = pX / EX[:, None]
+    fs = np.stack([_boost(rest[i, :, :3], rest[i, :, 3], bX) for i in range(3)])
+    return beam, fs, np.array([m, m, m]), m
+
+
+# isobars of the 3pi wave sets: (name, 2J, mass, width, mass dependence)
+PIPI_ISOBARS = [
+    ("sigma", 0, 0.60, 0.60, "constWidthBreitWigner"),
+    ("rho(770)", 2, 0.7690, 0.1509, "relativisticBreitWigner"),
+    ("f0(980)", 0, 0.980, 0.070, "relativisticBreitWigner"),
+    ("f2(1270)", 4, 1.2751, 0.1851, "relativisticBreitWigner"),
+    ("f0(1500)", 0, 1.505, 0.109, "relativisticBreitWigner"),
+    ("rho3(1690)", 6, 1.6888, 0.161, "relativisticBreitWigner"),
+]
+
+
+def three_pion_waves(n_waves=88, n_neg=8, max_J=6, max_L=8):
+    """A COMPASS-like pi- pi+ pi- wave set: X -> isobar(pi+ pi-) + pi- with
+    every isobar above, J = 0..3, M = 0..2, parity-conserving L
+    (P = (-1)^(L + l + 1) for three pseudoscalars), L <= 4, ordered by J,
+    isobar and L: the first n_waves - n_neg waves of reflectivity +1 and the
+    first n_neg of reflectivity -1.  Returns keyword arguments of
+    isobarHelicityAmplitudes.addWave (spins doubled)."""
+    out = []
+    for refl, n in ((+1, n_waves - n_neg), (-1, n_neg)):
+        out += _waves_of_reflectivity(refl, max_J, max_L)[:n]
+    return out
+
+
+def _waves_of_reflectivity(refl, max_J, max_L):
+    waves = []
+    for J in range(0, max_J + 1, 2):
+        for P in (-1, +1):
+            for M in range(0, min(J, 4) + 1, 2):
+                # reflectivity basis: M = 0 exists only for refl * P * (-1)^J = -1
+                if M == 0 and refl * P * (-1) ** (J // 2) == +1:
+                    continue
+                for name, j, mass, width, md in PIPI_ISOBARS:
+                    for L in range(0, max_L + 1, 2):
+                        # parity of three pseudoscalars; J from L x S with S = isobar spin
+                        if (-1) ** (L // 2 + j // 2 + 1) != P or not (abs(L - j) <= J <= L + j):
+                            continue
+                        waves.append(dict(J=J, P=P, M=M, refl=refl, L=L, S=j, isobarJ=j, isobarL=j,
+                                          massDependence=md, isobarMass=mass, isobarWidth=width,
+                                          isobarDaughters=(1, 2), bachelor=0, isobarName=name))
+    return waves

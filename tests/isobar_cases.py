@@ -6,6 +6,7 @@ conserves parity (P = (-1)^(L + l + 1) for three pseudoscalars)."""
 import numpy as np
 
 from oracle import isobar_oracle as O
+from rootpwa_gb300 import synth
 
 M_RHO, G_RHO = 0.7690, 0.1509
 M_F2, G_F2 = 1.2751, 0.1851
@@ -40,7 +41,7 @@ def waves():
 
 
 def events(n, seed=0):
-    return O.three_pion_events(n, seed=seed)
+    return synth.three_pion_events(n, seed=seed)
 
 
 def rel_err(A, B):

@@ -128,3 +128,20 @@ def test_no_events():
     beam, fs, masses, mb = events(10, seed=1)
     out = _amp(ws, masses, mb).amplitudes(np.zeros((0, 3)), np.zeros((3, 0, 3)))
     assert out.shape == (2, 0)
+
+
+def test_caller_stream():
+    """pwa_isobar_set_stream: device-buffer calls run asynchronously on the
+    caller's stream; results equal the synchronous host-buffer call's."""
+    import torch
+    ws = waves()[:4]
+    beam, fs, masses, mb = events(5000, seed=16)
+    A = _amp(ws, masses, mb)
+    host = A.amplitudes(beam, fs)
+    s = torch.cuda.Stream()
+    A.setStream(s)
+    with torch.cuda.stream(s):
+        dev = A.amplitudes(torch.from_numpy(beam).cuda(), torch.from_numpy(fs).cuda())
+    s.synchronize()
+    assert np.array_equal(dev.cpu().numpy(), host)
+    assert np.array_equal(A.amplitudes(beam, fs), host)       # host buffers: synchronous on that stream

@@ -39,7 +39,7 @@ def _c_waves(ws):
                               massDependence=I.MASS_DEPENDENCES[kw["massDependence"]],
                               isobarMass=kw["isobarMass"], isobarWidth=kw["isobarWidth"],
                               isobarDaughter1=kw["isobarDaughters"][0], isobarDaughter2=kw["isobarDaughters"][1],
-                              bachelor=kw["bachelor"], bachelorFirst=int(kw["bachelorFirst"]))
+                              bachelor=kw["bachelor"], bachelorFirst=int(kw.get("bachelorFirst", False)))
     return arr
 
 
@@ -140,6 +140,8 @@ def test_wave_checks_and_state():
     with pytest.raises(N.PwaError):
         A.enableReflectivityBasis(True)
     assert not A.reflectivityBasis()
+    with pytest.raises(N.PwaError):
+        N.call("pwa_isobar_set_stream", None, None)
 
 
 def _has_gpu():
@@ -162,3 +164,28 @@ def test_evaluation_fails_loudly_without_gpu():
     # no events: nothing to do, no device needed
     out = A.amplitudes(np.zeros((0, 3)), np.zeros((3, 0, 3)))
     assert out.shape == (1, 0)
+
+
+def test_three_pion_wave_set(shim):
+    """the 88-wave benchmark set (rootpwa_gb300.synth.three_pion_waves):
+    accepted by the library, parity-conserving, and the kernel arithmetic
+    matches the oracle on every wave."""
+    from rootpwa_gb300 import synth
+    kws = synth.three_pion_waves()
+    A = I.isobarHelicityAmplitudes()
+    A.setFinalState(NAMES, [synth.M_PI] * 3, synth.M_PI)
+    for kw in kws:
+        A.addWave(**kw)
+    assert A.nmbWaves() == 88
+    assert len({A.waveName(k) for k in range(88)}) == 88
+    ws = [(O.wave(kw["J"], kw["P"], kw["M"], kw["refl"], kw["L"], kw["S"], kw["isobarJ"], kw["isobarL"],
+                  I.MASS_DEPENDENCES[kw["massDependence"]], kw["isobarMass"], kw["isobarWidth"],
+                  kw["isobarDaughters"], kw["bachelor"]), kw) for kw in kws]
+    beam, fs, masses, mb = events(300, seed=8)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES)
+    got = _shim_amps(shim, ws, beam, fs, masses, mb, {})
+    assert np.all(rel_err(ref, got) < TOL)
+    assert np.all(np.abs(ref).max(axis=1) > 0)          # no wave vanishes identically
+    par = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, space_inversion=True)
+    for k, (w, _) in enumerate(ws):
+        assert np.abs(par[k] + w["P"] * ref[k]).max() < 1e-10 * np.abs(ref[k]).max()
