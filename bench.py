@@ -873,29 +873,36 @@ def run_isobar(args):
     dev = torch.device("cuda", local)
     b = torch.from_numpy(np.ascontiguousarray(beam.T)).to(dev)                        # [3][N]
     f = torch.from_numpy(np.ascontiguousarray(np.transpose(fs, (0, 2, 1)))).to(dev)   # [3][3][N]
-    out = torch.empty((W, n), dtype=torch.complex128, device=dev)
-
-    def step():
-        Nn.call("pwa_isobar_amplitudes", A._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
-                C.c_void_p(out.data_ptr()), Nn.MEMORY_DEVICE)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+    outs = {"complex64": torch.empty((W, n), dtype=torch.complex64, device=dev),
+            "complex128": torch.empty((W, n), dtype=torch.complex128, device=dev)}
     steps = max(1, min(args.steps, 50))
-    launches0 = Nn.lib().pwa_kernel_launch_count()
-    clocks = ClockSampler(local)
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / steps
-    launches = Nn.lib().pwa_kernel_launch_count() - launches0
+
+    def timed(dtype, clocked=False):
+        out = outs[dtype]
+        t = Nn.COMPLEX64 if dtype == "complex64" else Nn.COMPLEX128
+
+        def step():
+            Nn.call("pwa_isobar_amplitudes", A._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
+                    C.c_void_p(out.data_ptr()), t, Nn.MEMORY_DEVICE)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        launches0 = Nn.lib().pwa_kernel_launch_count()
+        clocks = ClockSampler(local) if clocked else None
+        if clocks:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop() if clocks else None
+        return e0.elapsed_time(e1) / steps, Nn.lib().pwa_kernel_launch_count() - launches0, clk
+
+    ms, launches, clk = timed("complex64", clocked=True)
+    ms64, _, _ = timed("complex128")
     # parity of the timed output on a sample against the FP64 oracle
     from oracle import isobar_oracle as O
     n_check = min(n, 1000)
@@ -905,39 +912,44 @@ def run_isobar(args):
     t0 = time.perf_counter()
     ref = O.amplitudes(ows, beam[:n_check], fs[:, :n_check], masses, mb, [0, 1, 0])
     t_cpu = time.perf_counter() - t0
-    got = out[:, :n_check].cpu().numpy()
-    err = max(float(np.abs(got[k] - ref[k]).max() / np.abs(ref[k]).max()) for k in range(W))
+    err = {}
+    for dtype, o in outs.items():
+        got = o[:, :n_check].cpu().numpy().astype(np.complex128)
+        err[dtype] = max(float(np.abs(got[k] - ref[k]).max() / np.abs(ref[k]).max()) for k in range(W))
     # end to end through the Python API with host buffers
     B = I.isobarHelicityAmplitudes()
     B.setFinalState(["pi-", "pi+", "pi-"], masses, mb)
     for kw in kws:
         B.addWave(**kw)
-    B.amplitudes(beam, fs)
+    B.amplitudes(beam, fs, dtype="complex64")
     e2e_steps = max(1, min(steps, 5))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        B.amplitudes(beam, fs)
+        B.amplitudes(beam, fs, dtype="complex64")
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     hbm, peak_kind = measured_peaks()
-    algo_bytes = n * (12 * 8 + W * 16)
+    algo_bytes = n * (12 * 8 + W * 8)
     achieved = algo_bytes / (ms * 1e-3) / 1e9
     line = {
         "metric": "isobar amplitudes: events/s at 88 waves (pi- pi+ pi-, helicity formalism)",
         "value": n / (ms * 1e-3), "unit": "events/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 frames, f32 per-wave arithmetic, complex64 out",
+        "fp64_mode": {"ms_per_step": ms64, "value": n / (ms64 * 1e-3), "unit": "events/s",
+                      "dtype": "f64 throughout, complex128 out"},
         "data": "synthetic: seeded diffractive 3pi events (phase space), 88-wave isobar set",
         "config": {"workload": "isobar3pi88", "events": n, "waves": W, "sym_terms": A.nmbSymTerms(),
                    "l2": "inputs and outputs (%.2f GB) larger than L2" % (algo_bytes / 1e9)},
         "e2e": {"value": n / t_e2e, "unit": "events/s", "h2d_bytes_per_step": n * 12 * 8,
-                "d2h_bytes_per_step": n * W * 16},
+                "d2h_bytes_per_step": n * W * 8},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None, "peak_kind": peak_kind,
-                     "note": "algorithmic bytes (96 B in + 16 B per wave out per event); the kernel is bound by "
-                             "the FP64 arithmetic rate, not by HBM"},
+                     "note": "algorithmic bytes (96 B in + 8 B per wave out per event, complex64 mode)"},
         "cpu_baseline": {"value": n_check / t_cpu, "unit": "events/s", "cores": 1, "kind": "port",
                          "sample": "FP64 oracle (numpy) on %d events x %d waves" % (n_check, W)},
         "max_rel_err_vs_oracle": err,
+        "timing": "CUDA events on torch's stream (pwa_isobar_set_stream), device-resident momenta",
         "clocks": clk,
     }
     emit(line, args)

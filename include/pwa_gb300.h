@@ -474,10 +474,13 @@ int pwa_isobar_nmb_waves(const pwa_isobar* A, uint32_t* n);
 int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t* n);
 /* amplitudes of every wave for nEvents events: beam momenta [3][nEvents]
  * (px, py, pz rows), final-state momenta [3 particles][3][nEvents], lab frame,
- * GeV/c; amps: complex128 [wave][nEvents].  memory: PWA_MEMORY_HOST or
- * PWA_MEMORY_DEVICE for all three buffers. */
+ * GeV/c; amps [wave][nEvents] of ampType: PWA_COMPLEX128 (FP64 arithmetic
+ * throughout, like the reference) or PWA_COMPLEX64 (frames and kinematics in
+ * FP64, the per-wave D functions, barrier factors and mass dependences in
+ * FP32; the likelihood's amplitude store is complex64).  memory:
+ * PWA_MEMORY_HOST or PWA_MEMORY_DEVICE for all three buffers. */
 int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, uint64_t nEvents, void* amps,
-                          int memory);
+                          int ampType, int memory);
 /* host utilities: clebschGordanCoeff (utilities/spinUtils.hpp:241-330),
  * dFunction (utilities/dFunction.hpp:52-170), barrierFactor with the
  * 0.1973 GeV/c scale (utilities/physUtils.hpp:200-275); arguments doubled */

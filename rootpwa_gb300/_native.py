@@ -161,7 +161,7 @@ SIGNATURES = {
     "pwa_isobar_add_wave": (i, [vp, C.POINTER(IsobarWave)]),
     "pwa_isobar_nmb_waves": (i, [vp, C.POINTER(u32)]),
     "pwa_isobar_nmb_sym_terms": (i, [vp, C.POINTER(u32)]),
-    "pwa_isobar_amplitudes": (i, [vp, vp, vp, u64, vp, i]),
+    "pwa_isobar_amplitudes": (i, [vp, vp, vp, u64, vp, i, i]),
     "pwa_clebsch_gordan": (i, [i32, i32, i32, i32, i32, i32, pd]),
     "pwa_wigner_d": (i, [i32, i32, i32, C.c_double, pd]),
     "pwa_barrier_factor": (i, [i32, C.c_double, pd]),

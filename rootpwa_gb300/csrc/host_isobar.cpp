@@ -178,10 +178,15 @@ int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t* n)
 	return kOk;
 }
 
-int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, uint64_t n, void* amps, int memory)
+int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, uint64_t n, void* amps, int ampType,
+                          int memory)
 {
 	if (!A)
 		return setError(kErrArg, "null argument");
+	if (ampType != PWA_COMPLEX64 && ampType != PWA_COMPLEX128)
+		return setError(kErrArg, "ampType must be PWA_COMPLEX64 or PWA_COMPLEX128");
+	const bool fp32 = ampType == PWA_COMPLEX64;
+	const uint64_t ampBytes = fp32 ? 8 : 16;
 	if (memory != PWA_MEMORY_HOST && memory != PWA_MEMORY_DEVICE)
 		return setError(kErrArg, "memory must be PWA_MEMORY_HOST or PWA_MEMORY_DEVICE");
 	if (!A->finalState)
@@ -193,7 +198,7 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 	if (!beam || !fs || !amps)
 		return setError(kErrArg, "null buffer");
 	const uint64_t W = A->waves.size();
-	if (n > (uint64_t)1 << 40 || W * n > ((uint64_t)1 << 62) / 16)
+	if (n > (uint64_t)1 << 40 || W * n > ((uint64_t)1 << 62) / ampBytes)
 		return setError(kErrArg, "too many events");
 	if (!A->stream && !A->userStream) {
 		PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking), "stream create"));
@@ -203,10 +208,10 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 		PWA_TRY(uploadPlan(A));
 	const double* dBeam = beam;
 	const double* dFs = fs;
-	double* dAmps = static_cast<double*>(amps);
+	void* dAmps = amps;
 	if (memory == PWA_MEMORY_HOST) {
 		PWA_TRY(A->dIn.ensure(n * 12 * sizeof(double), "isobar event buffer"));
-		PWA_TRY(A->dOut.ensure(W * n * 16, "isobar amplitude buffer"));
+		PWA_TRY(A->dOut.ensure(W * n * ampBytes, "isobar amplitude buffer"));
 		double* in = A->dIn.as<double>();
 		PWA_TRY(cudaCheck(cudaMemcpyAsync(in, beam, n * 3 * sizeof(double), cudaMemcpyHostToDevice, A->stream),
 		                  "beam upload"));
@@ -214,13 +219,13 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 		                  "final-state upload"));
 		dBeam = in;
 		dFs = in + 3 * n;
-		dAmps = A->dOut.as<double>();
+		dAmps = A->dOut.p;
 	} else if (!A->userStream) {
 		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device momenta"));
 	}
-	PWA_TRY(launchIsobarAmplitudes(A->devView, dBeam, dFs, n, dAmps, A->stream));
+	PWA_TRY(launchIsobarAmplitudes(A->devView, dBeam, dFs, n, dAmps, fp32, A->stream));
 	if (memory == PWA_MEMORY_HOST)
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(amps, dAmps, W * n * 16, cudaMemcpyDeviceToHost, A->stream),
+		PWA_TRY(cudaCheck(cudaMemcpyAsync(amps, dAmps, W * n * ampBytes, cudaMemcpyDeviceToHost, A->stream),
 		                  "amplitude download"));
 	// on the caller's stream, device-buffer calls stay asynchronous (stream order)
 	if (memory == PWA_MEMORY_DEVICE && A->userStream)

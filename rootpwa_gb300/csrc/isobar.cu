@@ -4,10 +4,12 @@
 // loop: the thread reads its event's beam and final-state momenta (SoA rows,
 // coalesced), builds the Gottfried-Jackson frame once, the kinematics of every
 // symmetrisation term once per topology class, and writes one complex128
-// amplitude per wave (row-major [wave][event], coalesced across the warp).
+// amplitude per wave (row-major [wave][event], coalesced across the warp):
+// complex128 with FP64 arithmetic throughout, or complex64 with the frames
+// and kinematics in FP64 and the per-wave arithmetic in FP32 (GB300 runs FP32
+// at many times its FP64 rate; the likelihood's amplitude store is complex64).
 // The wave plan (couplings, D-function terms, barrier polynomials) is a few
-// KB read by every thread through the read-only cache.  FP64 throughout: the
-// amplitudes are computed once per data set and then stored for the fit.
+// KB read by every thread through the read-only cache.
 #include "isobar_math.cuh"
 #include "pwa_internal.h"
 
@@ -19,9 +21,10 @@ namespace {
 
 constexpr int kIsoThreads = 128;
 
+template <typename T>
 __global__ void __launch_bounds__(kIsoThreads) isobarAmplitudeKernel(iso::PlanView P, const double* __restrict__ beam,
                                                                      const double* __restrict__ fs, uint64_t n,
-                                                                     double* __restrict__ amps)
+                                                                     T* __restrict__ amps)
 {
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
@@ -31,14 +34,14 @@ __global__ void __launch_bounds__(kIsoThreads) isobarAmplitudeKernel(iso::PlanVi
 		for (int i = 0; i < 3; ++i)
 			for (int k = 0; k < 3; ++k)
 				fp[i][k] = __ldg(fs + (uint64_t)(3 * i + k) * n + e);
-		iso::eventAmplitudes(P, bp, fp, amps, n, e);
+		iso::eventAmplitudes<T>(P, bp, fp, amps, n, e);
 	}
 }
 
 }  // namespace
 
-int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const double* fs, uint64_t n, double* amps,
-                           cudaStream_t s)
+int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const double* fs, uint64_t n, void* amps,
+                           bool fp32, cudaStream_t s)
 {
 	if (n == 0 || v.nWaves == 0)
 		return kOk;
@@ -47,7 +50,10 @@ int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const dou
 	PWA_CHECK(cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
 	const uint64_t need = (n + kIsoThreads - 1) / kIsoThreads;
 	const unsigned blocks = (unsigned)std::min<uint64_t>(need, (uint64_t)sms * 16);
-	isobarAmplitudeKernel<<<blocks, kIsoThreads, 0, s>>>(v, beam, fs, n, amps);
+	if (fp32)
+		isobarAmplitudeKernel<float><<<blocks, kIsoThreads, 0, s>>>(v, beam, fs, n, static_cast<float*>(amps));
+	else
+		isobarAmplitudeKernel<double><<<blocks, kIsoThreads, 0, s>>>(v, beam, fs, n, static_cast<double*>(amps));
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "isobar amplitude kernel");
 }

@@ -88,20 +88,44 @@ struct PlanView {
 	int32_t spaceInversion, reflection;
 };
 
-struct C2 {
-	double re, im;
+template <typename T>
+struct C2T {
+	T re, im;
 };
-PWA_HD C2 cmul(C2 x, C2 y) { return C2{x.re * y.re - x.im * y.im, x.re * y.im + x.im * y.re}; }
-PWA_HD C2 cadd(C2 x, C2 y) { return C2{x.re + y.re, x.im + y.im}; }
-PWA_HD C2 cscale(C2 x, double s) { return C2{x.re * s, x.im * s}; }
-PWA_HD C2 cexpi(double x)
+typedef C2T<double> C2;
+template <typename T>
+PWA_HD C2T<T> cmul(C2T<T> x, C2T<T> y)
+{
+	return C2T<T>{x.re * y.re - x.im * y.im, x.re * y.im + x.im * y.re};
+}
+template <typename T>
+PWA_HD C2T<T> cadd(C2T<T> x, C2T<T> y)
+{
+	return C2T<T>{x.re + y.re, x.im + y.im};
+}
+template <typename T>
+PWA_HD C2T<T> cscale(C2T<T> x, T s)
+{
+	return C2T<T>{x.re * s, x.im * s};
+}
+PWA_HD C2T<double> cexpi(double x)
 {
 #if defined(__CUDA_ARCH__)
 	double s, c;
 	sincos(x, &s, &c);
-	return C2{c, s};
+	return C2T<double>{c, s};
 #else
-	return C2{std::cos(x), std::sin(x)};
+	return C2T<double>{std::cos(x), std::sin(x)};
+#endif
+}
+PWA_HD C2T<float> cexpi(float x)
+{
+#if defined(__CUDA_ARCH__)
+	float s, c;
+	sincosf(x, &s, &c);
+	return C2T<float>{c, s};
+#else
+	return C2T<float>{std::cos(x), std::sin(x)};
 #endif
 }
 
@@ -131,9 +155,10 @@ PWA_HD LV toRest(LV v, V3 pX, double eX, double mX)
 	return LV{vadd(v.p, vscale(pX, -(v.e + e1) / (eX + mX))), e1};
 }
 
-PWA_HD double ipow(double x, int n)
+template <typename T>
+PWA_HD T ipow(T x, int n)
 {
-	double r = 1.0;
+	T r = T(1);
 	while (n > 0) {
 		if (n & 1)
 			r *= x;
@@ -143,52 +168,57 @@ PWA_HD double ipow(double x, int n)
 	return r;
 }
 
-PWA_HD double dEval(const DTerm* t, int t0, int t1, double c, double s)
+template <typename T>
+PWA_HD T dEval(const DTerm* t, int t0, int t1, T c, T s)
 {
-	double d = 0.0;
+	T d = T(0);
 	for (int k = t0; k < t1; ++k)
-		d += t[k].coef * ipow(c, t[k].a) * ipow(s, t[k].b);
+		d += T(t[k].coef) * ipow(c, t[k].a) * ipow(s, t[k].b);
 	return d;
 }
 
 // Blatt-Weisskopf F_L(q)^2 = P_l(1) z^l / P_l(z), z = (q / 0.1973)^2, L = 2l
-PWA_HD double barrierF2(const PlanView& P, int L, double q)
+template <typename T>
+PWA_HD T barrierF2(const PlanView& P, int L, T q)
 {
 	const int l = L / 2;
 	if (l == 0)
-		return 1.0;
-	const double z = (q * q) / (kPr * kPr);
+		return T(1);
+	const T z = (q * q) / T(kPr * kPr);
 	const double* c = P.bfPoly + 8 * l;
-	double den = c[l];
+	T den = T(c[l]);
 	for (int k = l - 1; k >= 0; --k)
-		den = den * z + c[k];
-	return P.bfNorm[l] * ipow(z, l) / den;
+		den = den * z + T(c[k]);
+	return T(P.bfNorm[l]) * ipow(z, l) / den;
 }
 
-PWA_HD double breakup2(double M, double m1, double m2)
+template <typename T>
+PWA_HD T breakup2(T M, T m1, T m2)
 {
-	const double s = m1 + m2, d = m1 - m2;
-	return (M - s) * (M + s) * (M - d) * (M + d) / (4.0 * M * M);
+	const T s = m1 + m2, d = m1 - m2;
+	return (M - s) * (M + s) * (M - d) * (M + d) / (T(4) * M * M);
 }
 
-PWA_HD C2 massDependence(const PlanView& P, const WaveDev& w, double mI)
+template <typename T>
+PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI)
 {
+	const T m0 = T(w.m0), g0 = T(w.g0);
 	if (w.massDep == kMassRelBw) {
 		if (w.q0 == 0.0)
-			return C2{0.0, 0.0};
-		const double q2 = breakup2(mI, w.ma, w.mb);
-		const double q = q2 > 0 ? sqrt(q2) : 0.0;
-		const double G = w.g0 * (w.m0 / mI) * (q / w.q0) * (barrierF2(P, w.LI, q) / w.f2q0);
-		const double A = w.m0 * w.g0, B = w.m0 * w.m0 - mI * mI, Cc = w.m0 * G;
-		const double f = A / (B * B + Cc * Cc);
-		return C2{f * B, f * Cc};
+			return C2T<T>{T(0), T(0)};
+		const T q2 = breakup2<T>(mI, T(w.ma), T(w.mb));
+		const T q = q2 > T(0) ? sqrt(q2) : T(0);
+		const T G = g0 * (m0 / mI) * (q / T(w.q0)) * (barrierF2<T>(P, w.LI, q) / T(w.f2q0));
+		const T A = m0 * g0, B = m0 * m0 - mI * mI, Cc = m0 * G;
+		const T f = A / (B * B + Cc * Cc);
+		return C2T<T>{f * B, f * Cc};
 	}
 	if (w.massDep == kMassConstBw) {
-		const double A = w.m0 * w.g0, B = w.m0 * w.m0 - mI * mI;
-		const double f = A / (B * B + A * A);
-		return C2{f * B, f * A};
+		const T A = m0 * g0, B = m0 * m0 - mI * mI;
+		const T f = A / (B * B + A * A);
+		return C2T<T>{f * B, f * A};
 	}
-	return C2{1.0, 0.0};
+	return C2T<T>{T(1), T(0)};
 }
 
 // kinematics of one symmetrisation term for one topology class
@@ -237,30 +267,33 @@ PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w)
 	return k;
 }
 
-// amplitude of wave w for one symmetrisation term
-PWA_HD C2 termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
+// amplitude of wave w for one symmetrisation term; T is the arithmetic of
+// the per-wave part (the kinematics come in FP64)
+template <typename T>
+PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
 {
-	const C2 eM = cexpi(0.5 * w.M * k.phi);
-	const C2 eMc{eM.re, -eM.im};
+	const T cX = T(k.cX), sX = T(k.sX), cI = T(k.cI), sI = T(k.sI), phiH = T(k.phiH);
+	const C2T<T> eM = cexpi(T(0.5 * w.M * k.phi));
+	const C2T<T> eMc{eM.re, -eM.im};
 	// e^{i lam phiH / 2} stepped by e^{i phiH} from lam = lamIso of the first term
-	const C2 step = cexpi(k.phiH);
-	C2 eL{1.0, 0.0};
-	C2 sum{0.0, 0.0};
+	const C2T<T> step = cexpi(phiH);
+	C2T<T> eL{T(1), T(0)};
+	C2T<T> sum{T(0), T(0)};
 	for (int t = w.lam0; t < w.lam1; ++t) {
 		const LamTerm& L = P.lams[t];
 		if (t == w.lam0)
-			eL = cexpi(0.5 * L.lamIso * k.phiH);
+			eL = cexpi(T(0.5) * T(L.lamIso) * phiH);
 		else
 			for (int s = P.lams[t - 1].lamIso; s < L.lamIso; s += 2)
 				eL = cmul(eL, step);
-		const double dP = dEval(P.dterms, L.plus0, L.plus1, k.cX, k.sX);
-		const double dM = dEval(P.dterms, L.minus0, L.minus1, k.cX, k.sX);
-		const double dI = dEval(P.dterms, L.iso0, L.iso1, k.cI, k.sI);
-		const C2 x = cadd(cscale(eM, L.cPlus * dP), cscale(eMc, L.cMinus * dM));
+		const T dP = dEval<T>(P.dterms, L.plus0, L.plus1, cX, sX);
+		const T dM = dEval<T>(P.dterms, L.minus0, L.minus1, cX, sX);
+		const T dI = dEval<T>(P.dterms, L.iso0, L.iso1, cI, sI);
+		const C2T<T> x = cadd(cscale(eM, T(L.cPlus) * dP), cscale(eMc, T(L.cMinus) * dM));
 		sum = cadd(sum, cmul(x, cscale(eL, dI)));
 	}
-	const double f = sqrt(barrierF2(P, w.LX, k.qX) * barrierF2(P, w.LI, k.qI));
-	return cscale(cmul(sum, massDependence(P, w, k.mI)), f);
+	const T f = sqrt(barrierF2<T>(P, w.LX, T(k.qX)) * barrierF2<T>(P, w.LI, T(k.qI)));
+	return cscale(cmul(sum, massDependence<T>(P, w, T(k.mI))), f);
 }
 
 // Gottfried-Jackson four-vectors of the three final-state particles of one
@@ -291,8 +324,11 @@ PWA_HD void gjFrame(const PlanView& P, const double bp[3], const double fp[3][3]
 	}
 }
 
-// all waves of one event; out is complex128 [wave][ld] as interleaved doubles
-PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double fp[3][3], double* out, uint64_t ld,
+// all waves of one event; out is complex [wave][ld] as interleaved T
+// (complex128 for T = double, complex64 for T = float: FP64 frames and
+// kinematics, per-wave arithmetic in T)
+template <typename T>
+PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double fp[3][3], T* out, uint64_t ld,
                             uint64_t e)
 {
 	LV g[3];
@@ -307,10 +343,10 @@ PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double 
 			for (uint32_t t = 0; t < P.nPerms; ++t)
 				kin[t] = kinematics(g, P.perms + 3 * t, w);
 		}
-		C2 a{0.0, 0.0};
+		C2T<T> a{T(0), T(0)};
 		for (uint32_t t = 0; t < P.nPerms; ++t)
-			a = cadd(a, termAmplitude(P, w, kin[t]));
-		a = cscale(a, P.boseFactor);
+			a = cadd(a, termAmplitude<T>(P, w, kin[t]));
+		a = cscale(a, T(P.boseFactor));
 		out[2 * ((uint64_t)wi * ld + e)] = a.re;
 		out[2 * ((uint64_t)wi * ld + e) + 1] = a.im;
 	}

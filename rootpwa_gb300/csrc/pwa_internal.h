@@ -317,9 +317,10 @@ int ampFileToDevice(const AmpFile& f, uint64_t offset, uint64_t bytes, void* dst
 namespace iso {
 struct PlanView;
 }
-// amps complex128 [wave][n] from beam [3][n] and final state [3][3][n]
-// (device pointers; the view's arrays in device memory)
-int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const double* fs, uint64_t n, double* amps,
-                           cudaStream_t s);
+// amps complex128 (fp32 false) or complex64 (fp32 true: per-wave arithmetic
+// in FP32) [wave][n] from beam [3][n] and final state [3][3][n] (device
+// pointers; the view's arrays in device memory)
+int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const double* fs, uint64_t n, void* amps,
+                           bool fp32, cudaStream_t s);
 
 }  // namespace pwa

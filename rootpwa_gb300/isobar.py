@@ -154,16 +154,20 @@ class isobarHelicityAmplitudes:
         return s.replace("(", "_").replace(")", "_")
 
     # -- evaluation ----------------------------------------------------------------
-    def amplitudes(self, beam, fs):
-        """complex128 [wave, event] amplitudes for beam (N, 3) and final-state
-        (3, N, 3) lab momenta.  CUDA tensors in, CUDA tensor out."""
+    def amplitudes(self, beam, fs, dtype="complex128"):
+        """[wave, event] amplitudes for beam (N, 3) and final-state (3, N, 3)
+        lab momenta.  CUDA tensors in, CUDA tensor out.  dtype complex128:
+        FP64 throughout; complex64: FP64 frames, FP32 per-wave arithmetic."""
         W = self.nmbWaves()
+        if dtype not in ("complex128", "complex64"):
+            raise ValueError("dtype must be complex128 or complex64")
+        t = N.COMPLEX64 if dtype == "complex64" else N.COMPLEX128
         if hasattr(beam, "__cuda_array_interface__"):
             import torch
             b = beam.to(torch.float64).t().contiguous()                  # [3][N]
             f = fs.to(torch.float64).permute(0, 2, 1).contiguous()       # [3][3][N]
             n = b.shape[1]
-            out = torch.empty((W, n), dtype=torch.complex128, device=b.device)
+            out = torch.empty((W, n), dtype=getattr(torch, dtype), device=b.device)
             if self._async and self._stream:
                 # the kernel runs on the caller's stream: order it after the
                 # layout copies above and keep their memory until it has run
@@ -172,16 +176,16 @@ class isobarHelicityAmplitudes:
                 for t in (b, f, out):
                     t.record_stream(es)
             N.call("pwa_isobar_amplitudes", self._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
-                   C.c_void_p(out.data_ptr()), N.MEMORY_DEVICE)
+                   C.c_void_p(out.data_ptr()), t, N.MEMORY_DEVICE)
             return out
         b = np.ascontiguousarray(np.asarray(beam, dtype=np.float64).T)
         f = np.ascontiguousarray(np.transpose(np.asarray(fs, dtype=np.float64), (0, 2, 1)))
         if b.shape[0] != 3 or f.shape[:2] != (3, 3) or f.shape[2] != b.shape[1]:
             raise ValueError("beam must be (N, 3) and fs (3, N, 3)")
         n = b.shape[1]
-        out = np.empty((W, n), dtype=np.complex128)
+        out = np.empty((W, n), dtype=np.dtype(dtype))
         N.call("pwa_isobar_amplitudes", self._h, b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), n,
-               out.ctypes.data_as(C.c_void_p), N.MEMORY_HOST)
+               out.ctypes.data_as(C.c_void_p), t, N.MEMORY_HOST)
         return out
 
 

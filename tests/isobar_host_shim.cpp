@@ -5,9 +5,10 @@
 // temporary directory; never part of the library.
 #include "../rootpwa_gb300/csrc/isobar_plan.h"
 
+// out: complex128 [wave][n] (fp32 = 0) or complex64 (fp32 = 1), as the kernel writes them
 extern "C" int shim_amplitudes(const pwa_isobar_wave* waves, int nWaves, const double* masses, const int32_t* species,
                                double beamMass, int reflBasis, int bose, int spaceInversion, int reflection,
-                               const double* beam, const double* fs, uint64_t n, double* out)
+                               const double* beam, const double* fs, uint64_t n, void* out, int fp32)
 {
 	std::vector<pwa_isobar_wave> ws(waves, waves + nWaves);
 	for (const pwa_isobar_wave& w : ws)
@@ -24,7 +25,10 @@ extern "C" int shim_amplitudes(const pwa_isobar_wave* waves, int nWaves, const d
 		for (int i = 0; i < 3; ++i)
 			for (int k = 0; k < 3; ++k)
 				fp[i][k] = fs[(3 * i + k) * n + e];
-		pwa::iso::eventAmplitudes(v, bp, fp, out, n, e);
+		if (fp32)
+			pwa::iso::eventAmplitudes<float>(v, bp, fp, static_cast<float*>(out), n, e);
+		else
+			pwa::iso::eventAmplitudes<double>(v, bp, fp, static_cast<double*>(out), n, e);
 	}
 	return 0;
 }

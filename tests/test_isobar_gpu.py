@@ -6,7 +6,8 @@ device buffers; ragged and large event counts; and the chain events ->
 amplitudes -> integrals -> likelihood against the same chain in the oracle.
 
 Tolerance: max |A_gpu - A_oracle| per wave below 1e-9 of the wave's largest
-|A| (FP64 throughout; the frames boost ~190 GeV/c momenta by gamma ~ 100)."""
+|A| (FP64 throughout; the frames boost ~190 GeV/c momenta by gamma ~ 100);
+5e-6 in the complex64 mode (FP32 per-wave arithmetic)."""
 import numpy as np
 import pytest
 
@@ -15,7 +16,7 @@ from oracle import isobar_oracle as O
 from rootpwa_gb300 import isobar as I
 import helpers
 from helpers import F_RTOL, G_NORMWISE, normwise, rel
-from isobar_cases import NAMES, SPECIES, TOL, events, rel_err, waves
+from isobar_cases import NAMES, SPECIES, TOL, TOL32, events, rel_err, waves
 
 pytestmark = pytest.mark.gpu
 
@@ -46,6 +47,22 @@ def test_amplitudes_match_oracle_host_buffers(opts):
     err = rel_err(ref, got)
     assert np.all(err < TOL), err
     assert np.all(got[-1] == 0)                       # zero by reflectivity (M = 0, f = +1)
+
+
+@pytest.mark.parametrize("opts", OPTIONS[:2], ids=["default", "no-bose"])
+def test_complex64_mode_matches_oracle(opts):
+    import torch
+    ws = waves()
+    beam, fs, masses, mb = events(3000, seed=17)
+    A = _amp(ws, masses, mb, opts)
+    got = A.amplitudes(beam, fs, dtype="complex64")
+    assert got.dtype == np.complex64
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, **opts)
+    err = rel_err(ref, got.astype(np.complex128))
+    assert np.all(err < TOL32), err
+    dev = A.amplitudes(torch.from_numpy(beam).cuda(), torch.from_numpy(fs).cuda(), dtype="complex64")
+    assert dev.dtype == torch.complex64
+    assert np.array_equal(dev.cpu().numpy(), got)
 
 
 def test_amplitudes_device_buffers_equal_host_buffers():
@@ -93,10 +110,13 @@ def test_large_event_count_by_tiling():
     assert np.all(rel_err(ref, small.cpu().numpy()) < TOL)
 
 
-def test_events_to_likelihood_chain():
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_events_to_likelihood_chain(dtype):
     """amplitudes of data and MC events on the GPU -> GPU integrals -> GPU
     likelihood, against oracle amplitudes -> oracle integrals -> oracle
-    likelihood; FdF within the likelihood's tolerances."""
+    likelihood; FdF within the likelihood's tolerances.  In the complex64
+    mode the oracle chain starts from the GPU's complex64 amplitudes (cast to
+    complex128), whose own error the tests above bound."""
     import torch
     ws = waves()[:8]                                   # the non-zero waves
     data = events(4000, seed=21)
@@ -111,8 +131,12 @@ def test_events_to_likelihood_chain():
                 data=O.amplitudes(Ow, data[0], data[1], masses, mb, SPECIES),
                 mc=O.amplitudes(Ow, mc[0], mc[1], masses, mb, SPECIES), accepted=accepted)
     Lo = helpers.build_oracle(w_or)
-    d_data = A.amplitudes(torch.from_numpy(data[0]).cuda(), torch.from_numpy(data[1]).cuda())
-    d_mc = A.amplitudes(torch.from_numpy(mc[0]).cuda(), torch.from_numpy(mc[1]).cuda())
+    d_data = A.amplitudes(torch.from_numpy(data[0]).cuda(), torch.from_numpy(data[1]).cuda(), dtype=dtype)
+    d_mc = A.amplitudes(torch.from_numpy(mc[0]).cuda(), torch.from_numpy(mc[1]).cuda(), dtype=dtype)
+    if dtype == "complex64":
+        w_or = dict(w_or, data=d_data.cpu().numpy().astype(np.complex128),
+                    mc=d_mc.cpu().numpy().astype(np.complex128))
+        Lo = helpers.build_oracle(w_or)
     w_gpu = dict(w_or, data=d_data, mc=d_mc)
     norm, acc = helpers.gpu_integrals(w_gpu, precision="fp64")
     Lg = helpers.build_gpu(w_gpu, norm, acc, amps=[d_data[k] for k in range(len(ws))])

@@ -15,7 +15,7 @@ import pytest
 from oracle import isobar_oracle as O
 from rootpwa_gb300 import _native as N
 from rootpwa_gb300 import isobar as I
-from isobar_cases import NAMES, SPECIES, TOL, events, rel_err, waves
+from isobar_cases import NAMES, SPECIES, TOL, TOL32, events, rel_err, waves
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -43,18 +43,18 @@ def _c_waves(ws):
     return arr
 
 
-def _shim_amps(lib, ws, beam, fs, masses, mb, opts):
+def _shim_amps(lib, ws, beam, fs, masses, mb, opts, dtype=np.complex128):
     n = beam.shape[0]
     b = np.ascontiguousarray(beam.T)
     f = np.ascontiguousarray(np.transpose(fs, (0, 2, 1)))
-    out = np.zeros((len(ws), n), dtype=np.complex128)
+    out = np.zeros((len(ws), n), dtype=dtype)
     m = np.ascontiguousarray(masses, dtype=np.float64)
     sp = np.ascontiguousarray(SPECIES, dtype=np.int32)
     rc = lib.shim_amplitudes(_c_waves(ws), len(ws), m.ctypes.data_as(C.c_void_p), sp.ctypes.data_as(C.c_void_p),
                              C.c_double(mb), int(opts.get("reflectivity_basis", True)), int(opts.get("bose", True)),
                              int(opts.get("space_inversion", False)), int(opts.get("reflection", False)),
                              b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), C.c_uint64(n),
-                             out.ctypes.data_as(C.c_void_p))
+                             out.ctypes.data_as(C.c_void_p), int(dtype == np.complex64))
     assert rc == 0
     return out
 
@@ -73,6 +73,18 @@ def test_kernel_arithmetic_matches_oracle(shim, opts):
     assert np.all(err < TOL), err
     # the parity-forbidden combination of the last wave is exactly zero in both
     assert np.all(ref[-1] == 0) and np.all(got[-1] == 0)
+
+
+@pytest.mark.parametrize("opts", OPTIONS[:2], ids=["default", "no-bose"])
+def test_kernel_arithmetic_complex64_mode(shim, opts):
+    """FP64 frames and kinematics, FP32 per-wave arithmetic, complex64 out."""
+    ws = waves()
+    beam, fs, masses, mb = events(1500, seed=7)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, **opts)
+    got = _shim_amps(shim, ws, beam, fs, masses, mb, opts, np.complex64)
+    err = rel_err(ref, got.astype(np.complex128))
+    assert np.all(err < TOL32), err
+    assert np.all(got[-1] == 0)
 
 
 def test_kernel_arithmetic_helicity_basis(shim):
