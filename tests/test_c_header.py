@@ -36,7 +36,25 @@ int main(void)
     int st = pwa_likelihood_fdf(L, par, &f, g);
     printf("fdf status %d: %s\n", st, pwa_last_error());
     pwa_likelihood_destroy(L);
-    return st == PWA_ERROR_INVALID_STATE ? 0 : 5;
+    if (st != PWA_ERROR_INVALID_STATE) return 5;
+    /* decay amplitudes: a wave given as a plain C struct (spins doubled) */
+    pwa_isobar* A = 0;
+    pwa_isobar_wave w = {2, 1, 0, 1, 0, 2, 2, 2, 0, PWA_MASSDEP_RELATIVISTIC_BW, 0.769, 0.150, 1, 2, 0, 0};
+    const double m[3] = {0.13957, 0.13957, 0.13957};
+    const int32_t sp[3] = {0, 1, 0};
+    double cg = 0;
+    uint32_t terms = 0;
+    if (pwa_isobar_create(&A) != PWA_SUCCESS) return 6;
+    if (pwa_isobar_set_final_state(A, 3, m, sp, 0.13957) != PWA_SUCCESS) return 7;
+    if (pwa_isobar_add_wave(A, &w) != PWA_SUCCESS) return 8;
+    if (pwa_isobar_nmb_sym_terms(A, &terms) != PWA_SUCCESS || terms != 2) return 9;
+    w.M = 4; /* |M| > J */
+    if (pwa_isobar_add_wave(A, &w) != PWA_ERROR_INVALID_ARGUMENT) return 10;
+    printf("wave refused: %s\n", pwa_last_error());
+    if (pwa_clebsch_gordan(2, 2, 2, -2, 0, 0, &cg) != PWA_SUCCESS) return 11;
+    printf("cg %.6f\n", cg);  /* (1 1 1 -1 | 0 0) = 1/sqrt(3) */
+    pwa_isobar_destroy(A);
+    return (cg > 0.577 && cg < 0.578) ? 0 : 12;
 }
 """
 
