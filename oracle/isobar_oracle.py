@@ -27,8 +27,10 @@ It follows the reference step by step, vectorised over events with numpy:
   isobarAmplitude.cc:98-111); space inversion and reflection through the
   production plane as in isobarAmplitude.cc:174-203.
 * mass dependences: flat, relativistic Breit-Wigner with the PWA2000 rule
-  q0 = sqrt|q0^2| (massDependence.cc:254-296, utilities/physUtils.hpp:283-300)
-  and constant-width Breit-Wigner (massDependence.cc:300-320).
+  q0 = sqrt|q0^2| (massDependence.cc:254-296, utilities/physUtils.hpp:283-300),
+  constant-width Breit-Wigner (massDependence.cc:300-320), the rho and
+  f0(980) Breit-Wigners (:324-390) and the f0(980) Flatte form with the BES II
+  parameters (:395-445).
 
 The building blocks are restated from the published formulas, not from the
 reference's arrangement of them: Clebsch-Gordan coefficients by Racah's
@@ -52,7 +54,8 @@ from itertools import permutations
 import numpy as np
 
 PR_DEFAULT = 0.1973        # GeV/c, 1 fm interaction radius
-MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW = 0, 1, 2
+MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW, MASSDEP_RHO_BW, MASSDEP_F0980_BW, MASSDEP_F0980_FLATTE = range(6)
+M_PI_CHARGED, M_K_CHARGED = 0.13957039, 0.493677   # GeV/c^2 (the particle table's pi+ and K+)
 
 
 # -- spin algebra ---------------------------------------------------------------
@@ -168,6 +171,41 @@ def relativistic_bw(M, m1, m2, M0, G0, L):
     G = G0 * (M0 / M) * (q / q0) * (barrier_factor(L, q) ** 2 / barrier_factor(L, q0) ** 2)
     A, B, C = M0 * G0, M0 * M0 - M * M, M0 * G
     return (A / (B * B + C * C)) * (B + 1j * C)
+
+
+def rho_bw(M, m1, m2, M0, G0):
+    """rhoBreitWigner::amp (massDependence.cc:324-359): F = 2 q^2 / (q0^2 + q^2)."""
+    q2 = np.maximum(breakup_momentum_squared(M, m1, m2), 0.0)
+    q02 = breakup_momentum_squared(M0, m1, m2)
+    q, q0 = np.sqrt(q2), math.sqrt(q02)
+    F = 2 * q2 / (q02 + q2)
+    G = G0 * (M0 / M) * (q / q0) * F
+    A, B, C = M0 * G0 * np.sqrt(F), M0 * M0 - M * M, M0 * G
+    return (A / (B * B + C * C)) * (B + 1j * C)
+
+
+def f0980_bw(M, m1, m2, M0, G0):
+    """f0980BreitWigner::amp (massDependence.cc:363-390): Gamma = Gamma0 q / q0,
+    numerator M0 Gamma M / q."""
+    q = np.sqrt(np.maximum(breakup_momentum_squared(M, m1, m2), 0.0))
+    q0 = math.sqrt(max(breakup_momentum_squared(M0, m1, m2), 0.0))
+    G = G0 * (q / q0)
+    C = M0 * G
+    A, B = C * M / q, M0 * M0 - M * M
+    return (A / (B * B + C * C)) * (B + 1j * C)
+
+
+def f0980_flatte(M):
+    """f0980FlatteBesII::amp (massDependence.cc:395-445): the BES II Flatte
+    parameters M0 = 0.965, g1 = 0.165, g2/g1 = 4.21; complex breakup momenta
+    of pi+ pi- and K+ K- (imaginary below threshold, physUtils.hpp:108-120)."""
+    def kc(m):
+        q2 = breakup_momentum_squared(M, m, m)
+        q = np.sqrt(np.abs(q2))
+        return np.where(q2 < 0, 1j * q, q + 0j)
+    rho_pi, rho_k = 2 * kc(M_PI_CHARGED) / M, 2 * kc(M_K_CHARGED) / M
+    denom = (0.965 ** 2 - M * M) + 0j - 1j * 0.165 * (rho_pi + 4.21 * rho_k)
+    return 1.0 / denom
 
 
 def const_width_bw(M, M0, G0):
@@ -291,6 +329,12 @@ def _sym_term(w, beam, fs, masses, opts):
         bw = relativistic_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"], l)
     elif md == MASSDEP_CONST_BW:
         bw = const_width_bw(mI, w["isobar_mass"], w["isobar_width"])
+    elif md == MASSDEP_RHO_BW:
+        bw = rho_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"])
+    elif md == MASSDEP_F0980_BW:
+        bw = f0980_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"])
+    elif md == MASSDEP_F0980_FLATTE:
+        bw = f0980_flatte(mI)
     else:
         bw = np.ones_like(mI, dtype=np.complex128)
     fX = math.sqrt(L + 1) * barrier_factor(L, qX)

@@ -34,8 +34,10 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 int uploadPlan(pwa_isobar* A)
 {
 	iso::Plan& p = A->plan;
-	iso::buildPlan(A->waves, A->masses, A->species, A->beamMass, A->reflBasis, A->bose, A->spaceInversion,
-	               A->reflection, p);
+	const std::string why = iso::buildPlan(A->waves, A->masses, A->species, A->beamMass, A->reflBasis, A->bose,
+	                                       A->spaceInversion, A->reflection, p);
+	if (!why.empty())
+		return setError(kErrArg, why);
 	const size_t oWaves = 0;
 	const size_t oOrder = align16(oWaves + p.waves.size() * sizeof(iso::WaveDev));
 	const size_t oLams = align16(oOrder + p.order.size() * sizeof(int32_t));

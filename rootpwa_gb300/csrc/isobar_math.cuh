@@ -39,7 +39,12 @@ constexpr int kMaxL = 14;         // 2L: barrier factors up to L = 7
 constexpr int kMaxPerms = 6;      // Bose terms of three particles
 constexpr double kPr = 0.1973;    // GeV/c, 1 fm interaction radius
 
-enum { kMassFlat = 0, kMassRelBw = 1, kMassConstBw = 2 };
+enum { kMassFlat = 0, kMassRelBw = 1, kMassConstBw = 2, kMassRhoBw = 3, kMassF0980Bw = 4, kMassF0980Flatte = 5 };
+
+// f0(980) Flatte form with the BES II parameters (massDependence.cc:395-445)
+// and the charged pion and kaon masses of the particle table
+constexpr double kFlatteM0 = 0.965, kFlatteG1 = 0.165, kFlatteG2G1 = 4.21;
+constexpr double kMassPiCharged = 0.13957039, kMassKCharged = 0.493677;
 
 // d^j_{m n}(theta) = sum over terms of coef * cos(theta/2)^a * sin(theta/2)^b
 struct DTerm {
@@ -68,6 +73,7 @@ struct WaveDev {
 	double m0, g0;                  // isobar mass and width
 	double q0, f2q0;                // breakup momentum at m0 and F_L^2(q0) (relativistic BW)
 	double ma, mb;                  // isobar daughter masses
+	double q02;                     // breakup momentum squared at m0 (rho BW)
 	int32_t lam0, lam1;             // LamTerm range
 	int32_t topo;                   // topology class (waves of one class share kinematics)
 	int32_t pad;
@@ -199,8 +205,11 @@ PWA_HD T breakup2(T M, T m1, T m2)
 	return (M - s) * (M + s) * (M - d) * (M + d) / (T(4) * M * M);
 }
 
+// dm2 = m0^2 - mI^2 is formed in FP64 (it cancels near the peak, where FP32
+// would lose a narrow width's resolution); mId is the FP64 isobar mass for
+// the breakup momenta of the Flatte form, which cancel at the K K threshold
 template <typename T>
-PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI)
+PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, double mId)
 {
 	const T m0 = T(w.m0), g0 = T(w.g0);
 	if (w.massDep == kMassRelBw) {
@@ -209,14 +218,49 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI)
 		const T q2 = breakup2<T>(mI, T(w.ma), T(w.mb));
 		const T q = q2 > T(0) ? sqrt(q2) : T(0);
 		const T G = g0 * (m0 / mI) * (q / T(w.q0)) * (barrierF2<T>(P, w.LI, q) / T(w.f2q0));
-		const T A = m0 * g0, B = m0 * m0 - mI * mI, Cc = m0 * G;
+		const T A = m0 * g0, B = dm2, Cc = m0 * G;
 		const T f = A / (B * B + Cc * Cc);
 		return C2T<T>{f * B, f * Cc};
 	}
 	if (w.massDep == kMassConstBw) {
-		const T A = m0 * g0, B = m0 * m0 - mI * mI;
+		const T A = m0 * g0, B = dm2;
 		const T f = A / (B * B + A * A);
 		return C2T<T>{f * B, f * A};
+	}
+	if (w.massDep == kMassRhoBw) {
+		// rhoBreitWigner (massDependence.cc:324-359): F = 2 q^2 / (q0^2 + q^2)
+		const T q2r = breakup2<T>(mI, T(w.ma), T(w.mb));
+		const T q2 = q2r > T(0) ? q2r : T(0);
+		const T q02 = T(w.q02);
+		const T F = T(2) * q2 / (q02 + q2);
+		const T G = g0 * (m0 / mI) * (sqrt(q2) / T(w.q0)) * F;
+		const T A = m0 * g0 * sqrt(F), B = dm2, Cc = m0 * G;
+		const T f = A / (B * B + Cc * Cc);
+		return C2T<T>{f * B, f * Cc};
+	}
+	if (w.massDep == kMassF0980Bw) {
+		// f0980BreitWigner (massDependence.cc:363-390): Gamma = Gamma0 q / q0
+		const T q2 = breakup2<T>(mI, T(w.ma), T(w.mb));
+		const T q = q2 > T(0) ? sqrt(q2) : T(0);
+		const T Cc = m0 * g0 * (q / T(w.q0));
+		const T A = Cc * mI / q, B = dm2;
+		const T f = A / (B * B + Cc * Cc);
+		return C2T<T>{f * B, f * Cc};
+	}
+	if (w.massDep == kMassF0980Flatte) {
+		// 1 / (M0^2 - m^2 - i g1 (rho_pipi + g2/g1 rho_KK)), rho = 2 k / m with
+		// the complex breakup momenta k (imaginary below threshold)
+		const T kPi2 = T(breakup2<double>(mId, kMassPiCharged, kMassPiCharged));
+		const T kK2 = T(breakup2<double>(mId, kMassKCharged, kMassKCharged));
+		const T rPi = T(2) * sqrt(kPi2 < T(0) ? -kPi2 : kPi2) / mI;
+		const T rK = T(2) * sqrt(kK2 < T(0) ? -kK2 : kK2) / mI;
+		const T reRho = (kPi2 < T(0) ? T(0) : rPi) + T(kFlatteG2G1) * (kK2 < T(0) ? T(0) : rK);
+		const T imRho = (kPi2 < T(0) ? rPi : T(0)) + T(kFlatteG2G1) * (kK2 < T(0) ? rK : T(0));
+		// denominator d = (M0^2 - m^2 + g1 Im rho) - i g1 Re rho; 1/d = conj(d) / |d|^2
+		const T dRe = dm2 + T(kFlatteG1) * imRho;
+		const T dIm = -T(kFlatteG1) * reRho;
+		const T n2 = dRe * dRe + dIm * dIm;
+		return C2T<T>{dRe / n2, -dIm / n2};
 	}
 	return C2T<T>{T(1), T(0)};
 }
@@ -293,7 +337,8 @@ PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
 		sum = cadd(sum, cmul(x, cscale(eL, dI)));
 	}
 	const T f = sqrt(barrierF2<T>(P, w.LX, T(k.qX)) * barrierF2<T>(P, w.LI, T(k.qI)));
-	return cscale(cmul(sum, massDependence<T>(P, w, T(k.mI))), f);
+	const double m0 = w.massDep == kMassF0980Flatte ? kFlatteM0 : w.m0;
+	return cscale(cmul(sum, massDependence<T>(P, w, T(k.mI), T((m0 - k.mI) * (m0 + k.mI)), k.mI)), f);
 }
 
 // Gottfried-Jackson four-vectors of the three final-state particles of one

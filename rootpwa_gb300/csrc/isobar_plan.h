@@ -126,9 +126,10 @@ inline std::string checkWave(const pwa_isobar_wave& w, bool reflBasis)
 	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
 	if (a < 0 || b < 0 || c < 0 || a > 2 || b > 2 || c > 2 || a == b || a == c || b == c)
 		return "isobar daughters and bachelor must be three distinct final-state slots 0..2";
-	if (w.massDependence < kMassFlat || w.massDependence > kMassConstBw)
+	if (w.massDependence < kMassFlat || w.massDependence > kMassF0980Flatte)
 		return "unknown mass dependence";
-	if (w.massDependence != kMassFlat && !(w.isobarMass > 0 && w.isobarWidth > 0))
+	if (w.massDependence != kMassFlat && w.massDependence != kMassF0980Flatte &&
+	    !(w.isobarMass > 0 && w.isobarWidth > 0))
 		return "a Breit-Wigner needs a positive mass and width";
 	return std::string();
 }
@@ -192,8 +193,11 @@ inline void bosePermutations(const int32_t species[3], bool bose, std::vector<in
 // helicities with the Clebsch-Gordan couplings, sqrt(2L+1) norms
 // (angMomNormFactor, physUtils.hpp:159-166) and the reflectivity-basis
 // combination (dFunction.hpp DFunctionReflConj) folded into coefficients.
-inline void buildPlan(const std::vector<pwa_isobar_wave>& specs, const double masses[3], const int32_t species[3],
-                      double beamMass, bool reflBasis, bool bose, bool spaceInversion, bool reflection, Plan& plan)
+// returns an empty string, or why a wave cannot be evaluated with these
+// final-state masses
+inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const double masses[3],
+                             const int32_t species[3], double beamMass, bool reflBasis, bool bose,
+                             bool spaceInversion, bool reflection, Plan& plan)
 {
 	for (int i = 0; i < 3; ++i)
 		plan.masses[i] = masses[i];
@@ -221,11 +225,18 @@ inline void buildPlan(const std::vector<pwa_isobar_wave>& specs, const double ma
 		w.ma = masses[w.a];
 		w.mb = masses[w.b];
 		w.f2q0 = 1.0;
+		w.q02 = breakup2(s.isobarMass, w.ma, w.mb);
 		if (s.massDependence == kMassRelBw) {
 			// the PWA2000 rule q0 = sqrt|q0^2| (massDependence.cc:268-270)
-			w.q0 = std::sqrt(std::fabs(breakup2(s.isobarMass, w.ma, w.mb)));
+			w.q0 = std::sqrt(std::fabs(w.q02));
 			const PlanView v = plan.view();
 			w.f2q0 = barrierF2(v, s.isobarL, w.q0);
+		} else if (s.massDependence == kMassRhoBw || s.massDependence == kMassF0980Bw) {
+			// the reference refuses a resonance mass below the daughters' threshold
+			if (!(w.q02 > 0.0))
+				return "wave " + std::to_string(plan.waves.size()) +
+				       ": the isobar mass is below the threshold of its daughters";
+			w.q0 = std::sqrt(w.q02);
 		}
 		const std::tuple<int, int, int, int> key(w.a, w.b, w.c, w.bachelorFirst);
 		auto it = std::find(topoKeys.begin(), topoKeys.end(), key);
@@ -283,6 +294,7 @@ inline void buildPlan(const std::vector<pwa_isobar_wave>& specs, const double ma
 		plan.order[i] = (int32_t)i;
 	std::stable_sort(plan.order.begin(), plan.order.end(),
 	                 [&](int32_t x, int32_t y) { return plan.waves[x].topo < plan.waves[y].topo; });
+	return std::string();
 }
 
 }  // namespace iso

@@ -28,7 +28,8 @@ import numpy as np
 
 from . import _native as N
 
-MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2}
+MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2, "rhoBreitWigner": 3,
+                    "f0980BreitWigner": 4, "f0980FlatteBesII": 5}
 
 
 def _qn(x):

@@ -27,11 +27,15 @@ def waves():
         (4, -1, 0, +1, 4, 4, 4, 4, O.MASSDEP_CONST_BW, M_F2, G_F2, (1, 2), 0, False),   # 2-+0+ f2 S (const width)
         (8, +1, 2, +1, 4, 6, 6, 6, O.MASSDEP_REL_BW, M_RHO3, G_RHO3, (2, 1), 0, False),  # 4++1+ rho3 D
         (4, -1, 4, -1, 0, 4, 4, 4, O.MASSDEP_REL_BW, M_F2, G_F2, (0, 1), 2, False),     # 2-+2- f2 S, other pair
+        (2, +1, 2, +1, 0, 2, 2, 2, O.MASSDEP_RHO_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 1++1+ rho S (rho BW)
+        (0, -1, 0, +1, 0, 0, 0, 0, O.MASSDEP_F0980_BW, 0.980, 0.070, (1, 2), 0, False),  # 0-+0+ f0(980) S
+        (2, +1, 2, +1, 2, 0, 0, 0, O.MASSDEP_F0980_FLATTE, 0.0, 0.0, (1, 2), 0, True),   # 1++1+ f0(980) P (Flatte)
         (2, +1, 0, -1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 1++0- (zero by reflectivity)
     ]
     out = []
     md = {O.MASSDEP_FLAT: "flat", O.MASSDEP_REL_BW: "relativisticBreitWigner",
-          O.MASSDEP_CONST_BW: "constWidthBreitWigner"}
+          O.MASSDEP_CONST_BW: "constWidthBreitWigner", O.MASSDEP_RHO_BW: "rhoBreitWigner",
+          O.MASSDEP_F0980_BW: "f0980BreitWigner", O.MASSDEP_F0980_FLATTE: "f0980FlatteBesII"}
     for J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first in specs:
         ow = O.wave(J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first)
         kw = dict(J=J, P=P, M=M, refl=r, L=L, S=S, isobarJ=j, isobarL=l, massDependence=md[m], isobarMass=mass,
@@ -57,5 +61,13 @@ def rel_err(A, B):
 # gamma ~ 100, so both FP64 restatements carry ~1e-10 relative rounding
 # (the oracle's own rotation invariance holds to ~6e-11)
 TOL = 1e-9
-# complex64 mode (FP64 frames, FP32 per-wave arithmetic): measured <= 1.3e-6
+# complex64 mode (FP64 frames, FP32 per-wave arithmetic): measured <= 5e-7
 TOL32 = 5e-6
+
+
+def tolerances(ws, base):
+    """per-wave tolerance: base, ten times base for the f0(980) Flatte form,
+    whose K K threshold cusp (d amp / dm ~ 1/sqrt(m - 2 m_K)) turns the
+    ~1e-11 differences between the two restatements' isobar masses into up
+    to ~3e-9 of the amplitude for events next to the threshold."""
+    return np.array([base * (10 if w["mass_dep"] == O.MASSDEP_F0980_FLATTE else 1) for w, _ in ws])

@@ -15,8 +15,10 @@ extern "C" int shim_amplitudes(const pwa_isobar_wave* waves, int nWaves, const d
 		if (!pwa::iso::checkWave(w, reflBasis != 0).empty())
 			return 1;
 	pwa::iso::Plan plan;
-	pwa::iso::buildPlan(ws, masses, species, beamMass, reflBasis != 0, bose != 0, spaceInversion != 0,
-	                    reflection != 0, plan);
+	if (!pwa::iso::buildPlan(ws, masses, species, beamMass, reflBasis != 0, bose != 0, spaceInversion != 0,
+	                         reflection != 0, plan)
+	         .empty())
+		return 2;
 	const pwa::iso::PlanView v = plan.view();
 	for (uint64_t e = 0; e < n; ++e) {
 		double bp[3], fp[3][3];
