@@ -431,10 +431,11 @@ int pwa_mlp_train(pwa_mlp* net, const float* X, const float* T, uint64_t nSample
 
 /* ------------------------------------------------------------------------ */
 /* Decay amplitudes of three spinless final-state particles in the isobar    */
-/* model, helicity formalism (the step before the likelihood: replaces       */
-/* isobarHelicityAmplitude::amplitude, decayAmplitude/isobarAmplitude.h:80,  */
-/* isobarAmplitude.cc:98-262, isobarHelicityAmplitude.cc:64-195, for         */
-/* X -> isobar + bachelor, isobar -> a + b).  Spins, projections and orbital */
+/* model, helicity or canonical formalism (the step before the likelihood:   */
+/* replaces isobarAmplitude::amplitude, decayAmplitude/isobarAmplitude.h:80, */
+/* isobarAmplitude.cc:98-262, isobarHelicityAmplitude.cc:64-195,             */
+/* isobarCanonicalAmplitude.cc:64-190, for X -> isobar + bachelor,           */
+/* isobar -> a + b).  Spins, projections and orbital                         */
 /* angular momenta are integers in units of 1/2 (2J, 2M, 2L), as in the      */
 /* reference.  FP64 on the GPU, one thread per event.                        */
 /* ------------------------------------------------------------------------ */
@@ -462,6 +463,9 @@ typedef struct pwa_isobar_wave {
 	int32_t isobarDaughter1, isobarDaughter2, bachelor; /* final-state slots 0..2; isobar daughter 1 is the analyser */
 	int32_t bachelorFirst;            /* X-vertex daughter 1 (the analyser) is the bachelor rather than the isobar */
 } pwa_isobar_wave;
+/* isobarHelicityAmplitude (decayAmplitude/isobarHelicityAmplitude.cc:64-195)
+ * or isobarCanonicalAmplitude (decayAmplitude/isobarCanonicalAmplitude.cc:64-190) */
+enum pwa_formalism { PWA_FORMALISM_HELICITY = 0, PWA_FORMALISM_CANONICAL = 1 };
 int pwa_isobar_create(pwa_isobar** out);
 int pwa_isobar_destroy(pwa_isobar* A);
 /* three final-state particles: masses, species ids (equal ids are identical
@@ -474,6 +478,8 @@ int pwa_isobar_set_final_state(pwa_isobar* A, uint32_t nFsParticles, const doubl
  * defaults 1, 1, 0, 0 */
 int pwa_isobar_set_options(pwa_isobar* A, int reflectivityBasis, int boseSymmetrize, int spaceInversion,
                            int reflection);
+/* helicity (the default) or canonical formalism */
+int pwa_isobar_set_formalism(pwa_isobar* A, int formalism);
 /* no reference counterpart: run on the caller's CUDA stream (NULL = the
  * default stream); calls with device buffers are then asynchronous in stream
  * order, calls with host buffers still return with the results in place */

@@ -1,6 +1,6 @@
 """FP64 restatement of the reference's isobar decay amplitudes for three
 spinless final-state particles (X -> isobar + bachelor, isobar -> a + b) in
-the helicity formalism.
+the helicity and the canonical formalism.
 
 TEST INFRASTRUCTURE ONLY: this module is the checker of the GPU amplitude
 kernel (rootpwa_gb300/csrc/isobar.cu).  Only tests, the smoke check and the
@@ -22,6 +22,10 @@ It follows the reference step by step, vectorised over events with numpy:
   reflectivity-basis D function at the X vertex (utilities/dFunction.hpp
   DFunctionReflConj) and the sum over the isobar's helicities
   (isobarAmplitude::twoBodyDecayAmplitudeSum, isobarAmplitude.cc:206-262).
+* canonical formalism (formalism="canonical"): isobarCanonicalAmplitude
+  (decayAmplitude/isobarCanonicalAmplitude.cc:64-190): the isobar's rest
+  frame by a boost alone, sqrt(4 pi) (s1 m1 s2 m2 | S mS) F_L(q) * sum over
+  mL of the (reflectivity-combined) (L mL S mS | J M) Y_L^mL(theta, phi).
 * Bose symmetrisation: sum over the permutations of identical final-state
   particles with factor 1/sqrt(prod n_k!) (isobarDecayTopology.cc:638-670,
   isobarAmplitude.cc:98-111); space inversion and reflection through the
@@ -303,6 +307,35 @@ def bose_terms(species):
     return perms, 1.0 / math.sqrt(len(perms))
 
 
+def Y(l, m, theta, phi):
+    """spherical harmonic Y_l^m, arguments doubled (sphericalHarmonic,
+    utilities/dFunction.hpp:176-192): sqrt((2l+1)/4pi) e^{i m phi} d^l_{m 0}."""
+    return math.sqrt((l + 1) / (4 * math.pi)) * np.exp(1j * (m / 2.0) * phi) * wigner_d(l, m, 0, theta)
+
+
+def _canonical_two_body(J, M, P, refl, L, S, s1, m1, s2, m2, theta, phi, q, bw, top, refl_basis):
+    """isobarCanonicalAmplitude::twoBodyDecayAmplitude (isobarCanonicalAmplitude.cc:
+    118-190): sqrt(4 pi) (s1 m1 s2 m2 | S mS) F_L(q) bw sum_mL C_LS(mL) Y_L^mL."""
+    mS = m1 + m2
+    ss = clebsch_gordan(s1, m1, s2, m2, S, mS)
+    if ss == 0:
+        return np.zeros_like(theta, dtype=np.complex128)
+    amp = np.zeros_like(theta, dtype=np.complex128)
+    for mL in range(-L, L + 1, 2):
+        if refl_basis and top:
+            f = reflectivity_factor(J, P, M, refl)
+            if M == 0:
+                c = 0.0 if f == +1 else clebsch_gordan(L, mL, S, mS, J, 0)
+            else:
+                c = (clebsch_gordan(L, mL, S, mS, J, M) - f * clebsch_gordan(L, mL, S, mS, J, -M)) / math.sqrt(2)
+        else:
+            c = clebsch_gordan(L, mL, S, mS, J, M)
+        if c == 0:
+            continue
+        amp = amp + c * Y(L, mL, theta, phi)
+    return amp * (math.sqrt(4 * math.pi) * ss * barrier_factor(L, q) * bw)
+
+
 def _sym_term(w, beam, fs, masses, opts):
     a, b, c = w["isobar_daughters"][0], w["isobar_daughters"][1], w["bachelor"]
     X = fs[0] + fs[1] + fs[2]
@@ -317,8 +350,10 @@ def _sym_term(w, beam, fs, masses, opts):
     d1 = bach if w["bachelor_first"] else iso
     phi, theta = _phi(d1[:, :3]), _theta(d1[:, :3])
     qX = np.sqrt(np.sum(d1[:, :3] ** 2, axis=-1))
-    # isobar vertex: helicity frame of the isobar, analyser = isobar daughter 1
-    ha, = hf_transform(iso, [gj[a]])
+    canonical = opts.get("formalism", "helicity") == "canonical"
+    # isobar vertex: helicity frame of the isobar (canonical: its rest frame
+    # by a boost alone, isobarCanonicalAmplitude.cc:94-108), analyser = isobar daughter 1
+    ha, = ([_boost(gj[a], -iso[:, :3] / iso[:, 3:4])] if canonical else hf_transform(iso, [gj[a]]))
     phih, thetah = _phi(ha[:, :3]), _theta(ha[:, :3])
     qI = np.sqrt(np.sum(ha[:, :3] ** 2, axis=-1))
     mI = _mass(iso)
@@ -337,9 +372,20 @@ def _sym_term(w, beam, fs, masses, opts):
         bw = f0980_flatte(mI)
     else:
         bw = np.ones_like(mI, dtype=np.complex128)
+    amp = np.zeros(len(phi), dtype=np.complex128)
+    if canonical:
+        rb = opts.get("reflectivity_basis", True)
+        for m in range(-j, j + 1, 2):
+            if w["bachelor_first"]:
+                s1, m1, s2, m2 = 0, 0, j, m
+            else:
+                s1, m1, s2, m2 = j, m, 0, 0
+            top = _canonical_two_body(J, M, P, refl, L, S, s1, m1, s2, m2, theta, phi, qX, 1.0, True, rb)
+            iso_amp = _canonical_two_body(j, m, 0, 0, l, s, 0, 0, 0, 0, thetah, phih, qI, bw, False, rb)
+            amp += top * iso_amp
+        return amp
     fX = math.sqrt(L + 1) * barrier_factor(L, qX)
     fI = math.sqrt(l + 1) * barrier_factor(l, qI) * bw
-    amp = np.zeros(len(phi), dtype=np.complex128)
     for lam_iso in range(-j, j + 1, 2):
         # X -> daughter1 + daughter2: helicities (lambda1, lambda2)
         if w["bachelor_first"]:

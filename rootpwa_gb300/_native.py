@@ -158,6 +158,7 @@ SIGNATURES = {
     "pwa_isobar_set_final_state": (i, [vp, u32, pd, C.POINTER(i32), C.c_double]),
     "pwa_isobar_set_options": (i, [vp, i, i, i, i]),
     "pwa_isobar_set_stream": (i, [vp, vp]),
+    "pwa_isobar_set_formalism": (i, [vp, i]),
     "pwa_isobar_add_wave": (i, [vp, C.POINTER(IsobarWave)]),
     "pwa_isobar_nmb_waves": (i, [vp, C.POINTER(u32)]),
     "pwa_isobar_nmb_sym_terms": (i, [vp, C.POINTER(u32)]),

@@ -10,7 +10,7 @@ struct pwa_isobar {
 	int32_t species[3] = {0, 1, 2};
 	double beamMass = 0.0;
 	bool finalState = false;
-	bool reflBasis = true, bose = true, spaceInversion = false, reflection = false;
+	bool reflBasis = true, bose = true, spaceInversion = false, reflection = false, canonical = false;
 	std::vector<pwa_isobar_wave> waves;
 	iso::Plan plan;
 	bool dirty = true;
@@ -35,7 +35,7 @@ int uploadPlan(pwa_isobar* A)
 {
 	iso::Plan& p = A->plan;
 	const std::string why = iso::buildPlan(A->waves, A->masses, A->species, A->beamMass, A->reflBasis, A->bose,
-	                                       A->spaceInversion, A->reflection, p);
+	                                       A->spaceInversion, A->reflection, A->canonical, p);
 	if (!why.empty())
 		return setError(kErrArg, why);
 	const size_t oWaves = 0;
@@ -130,6 +130,17 @@ int pwa_isobar_set_stream(pwa_isobar* A, void* s)
 	A->ownStream = false;
 	A->userStream = true;
 	A->stream = static_cast<cudaStream_t>(s);  // NULL: the CUDA default stream
+	return kOk;
+}
+
+int pwa_isobar_set_formalism(pwa_isobar* A, int formalism)
+{
+	if (!A)
+		return setError(kErrArg, "null argument");
+	if (formalism != PWA_FORMALISM_HELICITY && formalism != PWA_FORMALISM_CANONICAL)
+		return setError(kErrArg, "formalism must be PWA_FORMALISM_HELICITY or PWA_FORMALISM_CANONICAL");
+	A->canonical = formalism == PWA_FORMALISM_CANONICAL;
+	A->dirty = true;
 	return kOk;
 }
 

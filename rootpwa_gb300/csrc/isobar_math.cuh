@@ -19,7 +19,9 @@
 // helicity frame (isobarHelicityAmplitude.cc:64-84) is likewise the basis
 // z = isobar direction, y = unit(z_GJ x isobar), x = y x z followed by a boost
 // along z.  In the measure-zero case of an isobar along z_GJ (y undefined)
-// the kernel takes y = y_GJ.
+// the kernel takes y = y_GJ.  The canonical formalism
+// (decayAmplitude/isobarCanonicalAmplitude.cc:64-190) reaches the isobar's
+// rest frame by the boost alone, keeping the Gottfried-Jackson axes.
 #pragma once
 
 #include <cmath>
@@ -52,15 +54,19 @@ struct DTerm {
 	int32_t a, b;
 };
 
-// one helicity of the isobar in one wave: the X-vertex D function
-// cPlus e^{+i M phi/2} d^J_{M lam} + cMinus e^{-i M phi/2} d^J_{-M lam}
+// one spin projection of the isobar in one wave: the X-vertex angular part
+// cPlus e^{i mPlus phi/2} dPlus(theta) + cMinus e^{i mMinus phi/2} dMinus(theta)
 // (couplings, norms and the reflectivity combination folded into cPlus,
-// cMinus) times the isobar vertex e^{+i lamIso phiH/2} d^j_{lamIso 0}
+// cMinus) times the isobar vertex e^{i lamIso phiH/2} dIso(thetaH).
+// Helicity formalism: mPlus/mMinus = +-M, dPlus/dMinus = d^J_{+-M lam},
+// dIso = d^j_{lam 0}.  Canonical formalism: mPlus/mMinus = +-M - m,
+// dPlus/dMinus = d^L_{+-M-m, 0} (spherical harmonics Y_L), dIso = d^l_{m 0}.
 struct LamTerm {
-	int32_t lamIso;                 // 2 lambda of the isobar
-	int32_t plus0, plus1;           // DTerm range of d^J_{M lam}
-	int32_t minus0, minus1;         // DTerm range of d^J_{-M lam} (empty if unused)
-	int32_t iso0, iso1;             // DTerm range of d^j_{lamIso 0}
+	int32_t lamIso;                 // 2 lambda (helicity) or 2 m (canonical) of the isobar
+	int32_t plus0, plus1;           // DTerm range of dPlus
+	int32_t minus0, minus1;         // DTerm range of dMinus (empty if unused)
+	int32_t iso0, iso1;             // DTerm range of dIso
+	int32_t mPlus, mMinus;          // phase multipliers (units of 1/2)
 	double cPlus, cMinus;
 };
 
@@ -92,6 +98,8 @@ struct PlanView {
 	double boseFactor;
 	double masses[3], beamMass;
 	int32_t spaceInversion, reflection;
+	int32_t canonical;              // isobar rest frame by a boost alone (canonical formalism)
+	int32_t pad;
 };
 
 template <typename T>
@@ -285,7 +293,7 @@ PWA_HD void halfAngle(double perp, double z, double* c, double* s)
 #endif
 }
 
-PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w)
+PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w, bool canonical)
 {
 	const LV A = g[perm[w.a]], B = g[perm[w.b]], Cb = g[perm[w.c]];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
@@ -297,13 +305,24 @@ PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w)
 	k.qX = sqrt(vdot(d1, d1));
 	const double pI = sqrt(vdot(I.p, I.p));
 	k.mI = sqrt((I.e - pI) * (I.e + pI));
-	// helicity frame of the isobar
-	const V3 zh = vunit(I.p);
-	const double perpI = sqrt(I.p.x * I.p.x + I.p.y * I.p.y);
-	const V3 yh = perpI > 0 ? V3{-I.p.y / perpI, I.p.x / perpI, 0.0} : V3{0.0, 1.0, 0.0};
-	const V3 xh = vcross(yh, zh);
-	const double ax = vdot(A.p, xh), ay = vdot(A.p, yh);
-	const double az = (I.e * vdot(A.p, zh) - pI * A.e) / k.mI;
+	double ax, ay, az;
+	if (canonical) {
+		// rest frame of the isobar with the Gottfried-Jackson axes
+		// (isobarCanonicalAmplitude.cc:94-108)
+		const LV r = toRest(A, I.p, I.e, k.mI);
+		ax = r.p.x;
+		ay = r.p.y;
+		az = r.p.z;
+	} else {
+		// helicity frame of the isobar
+		const V3 zh = vunit(I.p);
+		const double perpI = sqrt(I.p.x * I.p.x + I.p.y * I.p.y);
+		const V3 yh = perpI > 0 ? V3{-I.p.y / perpI, I.p.x / perpI, 0.0} : V3{0.0, 1.0, 0.0};
+		const V3 xh = vcross(yh, zh);
+		ax = vdot(A.p, xh);
+		ay = vdot(A.p, yh);
+		az = (I.e * vdot(A.p, zh) - pI * A.e) / k.mI;
+	}
 	const double perpA = sqrt(ax * ax + ay * ay);
 	k.phiH = phiOf(ax, ay);
 	halfAngle(perpA, az, &k.cI, &k.sI);
@@ -316,9 +335,7 @@ PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w)
 template <typename T>
 PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
 {
-	const T cX = T(k.cX), sX = T(k.sX), cI = T(k.cI), sI = T(k.sI), phiH = T(k.phiH);
-	const C2T<T> eM = cexpi(T(0.5 * w.M * k.phi));
-	const C2T<T> eMc{eM.re, -eM.im};
+	const T cX = T(k.cX), sX = T(k.sX), cI = T(k.cI), sI = T(k.sI), phiH = T(k.phiH), phi = T(k.phi);
 	// e^{i lam phiH / 2} stepped by e^{i phiH} from lam = lamIso of the first term
 	const C2T<T> step = cexpi(phiH);
 	C2T<T> eL{T(1), T(0)};
@@ -333,7 +350,8 @@ PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
 		const T dP = dEval<T>(P.dterms, L.plus0, L.plus1, cX, sX);
 		const T dM = dEval<T>(P.dterms, L.minus0, L.minus1, cX, sX);
 		const T dI = dEval<T>(P.dterms, L.iso0, L.iso1, cI, sI);
-		const C2T<T> x = cadd(cscale(eM, T(L.cPlus) * dP), cscale(eMc, T(L.cMinus) * dM));
+		const C2T<T> x = cadd(cscale(cexpi(T(0.5) * T(L.mPlus) * phi), T(L.cPlus) * dP),
+		                      cscale(cexpi(T(0.5) * T(L.mMinus) * phi), T(L.cMinus) * dM));
 		sum = cadd(sum, cmul(x, cscale(eL, dI)));
 	}
 	const T f = sqrt(barrierF2<T>(P, w.LX, T(k.qX)) * barrierF2<T>(P, w.LI, T(k.qI)));
@@ -386,7 +404,7 @@ PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double 
 		if (w.topo != topo) {
 			topo = w.topo;
 			for (uint32_t t = 0; t < P.nPerms; ++t)
-				kin[t] = kinematics(g, P.perms + 3 * t, w);
+				kin[t] = kinematics(g, P.perms + 3 * t, w, P.canonical != 0);
 		}
 		C2T<T> a{T(0), T(0)};
 		for (uint32_t t = 0; t < P.nPerms; ++t)

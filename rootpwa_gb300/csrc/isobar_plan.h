@@ -144,7 +144,7 @@ struct Plan {
 	std::vector<int32_t> perms;
 	double boseFactor = 1.0;
 	double masses[3] = {0.0, 0.0, 0.0}, beamMass = 0.0;
-	int32_t spaceInversion = 0, reflection = 0;
+	int32_t spaceInversion = 0, reflection = 0, canonical = 0;
 
 	PlanView view() const
 	{
@@ -164,6 +164,7 @@ struct Plan {
 		v.beamMass = beamMass;
 		v.spaceInversion = spaceInversion;
 		v.reflection = reflection;
+		v.canonical = canonical;
 		return v;
 	}
 };
@@ -187,6 +188,64 @@ inline void bosePermutations(const int32_t species[3], bool bose, std::vector<in
 	factor = 1.0 / std::sqrt((double)(perms.size() / 3));
 }
 
+// canonical formalism (isobarCanonicalAmplitude::twoBodyDecayAmplitude,
+// isobarCanonicalAmplitude.cc:118-190): for each spin projection m of the
+// isobar, X vertex sqrt(4 pi) (s1 m1 s2 m2 | S m) F_L sum_mL C(mL) Y_L^mL and
+// isobar vertex sqrt(4 pi) (0 0 0 0 | S' 0) F_l (l m S' 0 | j m) Y_l^m.  The
+// (L mL S m | J +-M) couplings vanish unless mL = +-M - m, so the sum over mL
+// keeps two terms; sqrt(4 pi) Y_L^mu = sqrt(2L+1) e^{i mu phi} d^L_{mu 0}.
+inline void addCanonicalTerms(const pwa_isobar_wave& s, bool reflBasis, Plan& plan)
+{
+	const int J = s.J, M = s.M, L = s.L, S = s.S, j = s.isobarJ, l = s.isobarL, Si = s.isobarS;
+	for (int m = -j; m <= j; m += 2) {
+		const int s1 = s.bachelorFirst ? 0 : j, m1 = s.bachelorFirst ? 0 : m;
+		const int s2 = s.bachelorFirst ? j : 0, m2 = s.bachelorFirst ? m : 0;
+		const double ss = clebschGordan(s1, m1, s2, m2, S, m);
+		const double iso = std::sqrt(l + 1.0) * clebschGordan(0, 0, 0, 0, Si, 0) * clebschGordan(l, m, Si, 0, j, m);
+		if (ss == 0.0 || iso == 0.0 || std::abs(m) > l)
+			continue;
+		double cP = 0.0, cM = 0.0;
+		const int mP = M - m, mM = -M - m;
+		if (reflBasis) {
+			const int f = s.refl * s.P * ((((J - M) / 2) & 1) ? -1 : 1);
+			if (M == 0) {
+				if (f != +1)
+					cP = clebschGordan(L, mP, S, m, J, 0);
+			} else {
+				cP = clebschGordan(L, mP, S, m, J, M) / std::sqrt(2.0);
+				cM = -f * clebschGordan(L, mM, S, m, J, -M) / std::sqrt(2.0);
+			}
+		} else {
+			cP = clebschGordan(L, mP, S, m, J, M);
+		}
+		if (std::abs(mP) > L)
+			cP = 0.0;
+		if (std::abs(mM) > L)
+			cM = 0.0;
+		if (cP == 0.0 && cM == 0.0)
+			continue;
+		const double c = std::sqrt(L + 1.0) * ss * iso;
+		LamTerm t{};
+		t.lamIso = m;
+		t.plus0 = (int32_t)plan.dterms.size();
+		if (cP != 0.0)
+			wignerTerms(L, mP, 0, plan.dterms);
+		t.plus1 = (int32_t)plan.dterms.size();
+		t.minus0 = t.plus1;
+		if (cM != 0.0)
+			wignerTerms(L, mM, 0, plan.dterms);
+		t.minus1 = (int32_t)plan.dterms.size();
+		t.iso0 = t.minus1;
+		wignerTerms(l, m, 0, plan.dterms);
+		t.iso1 = (int32_t)plan.dterms.size();
+		t.mPlus = mP;
+		t.mMinus = mM;
+		t.cPlus = c * cP;
+		t.cMinus = c * cM;
+		plan.lams.push_back(t);
+	}
+}
+
 // wave plan of isobarHelicityAmplitude::twoBodyDecayAmplitude /
 // twoBodyDecayAmplitudeSum (isobarHelicityAmplitude.cc:130-195,
 // isobarAmplitude.cc:206-262) for every wave: the sum over the isobar's
@@ -197,8 +256,9 @@ inline void bosePermutations(const int32_t species[3], bool bose, std::vector<in
 // final-state masses
 inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const double masses[3],
                              const int32_t species[3], double beamMass, bool reflBasis, bool bose,
-                             bool spaceInversion, bool reflection, Plan& plan)
+                             bool spaceInversion, bool reflection, bool canonical, Plan& plan)
 {
+	plan.canonical = canonical ? 1 : 0;
 	for (int i = 0; i < 3; ++i)
 		plan.masses[i] = masses[i];
 	plan.beamMass = beamMass;
@@ -256,6 +316,12 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 			}
 		}
 		w.lam0 = (int32_t)plan.lams.size();
+		if (canonical) {
+			addCanonicalTerms(s, reflBasis, plan);
+			w.lam1 = (int32_t)plan.lams.size();
+			plan.waves.push_back(w);
+			continue;
+		}
 		for (int lamIso = -s.isobarJ; lamIso <= s.isobarJ && !zero; lamIso += 2) {
 			// X -> daughter 1 + daughter 2 with helicities (l1, l2), spins (s1, s2)
 			const int s1 = s.bachelorFirst ? 0 : s.isobarJ, l1 = s.bachelorFirst ? 0 : lamIso;
@@ -284,6 +350,8 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 			t.iso1 = (int32_t)plan.dterms.size();
 			t.cPlus = c * wPlus;
 			t.cMinus = c * wMinus;
+			t.mPlus = s.M;
+			t.mMinus = -s.M;
 			plan.lams.push_back(t);
 		}
 		w.lam1 = (int32_t)plan.lams.size();

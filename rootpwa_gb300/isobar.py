@@ -190,6 +190,15 @@ class isobarHelicityAmplitudes:
         return out
 
 
+class isobarCanonicalAmplitudes(isobarHelicityAmplitudes):
+    """The same wave set in the canonical formalism (isobarCanonicalAmplitude,
+    decayAmplitude/isobarCanonicalAmplitude.cc:64-190)."""
+
+    def __init__(self):
+        super().__init__()
+        N.call("pwa_isobar_set_formalism", self._h, 1)
+
+
 def clebschGordanCoeff(j1, m1, j2, m2, J, M):
     """(j1 m1 j2 m2 | J M), arguments doubled (utilities/spinUtils.hpp:241-330)."""
     v = C.c_double()

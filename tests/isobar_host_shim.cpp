@@ -8,7 +8,8 @@
 // out: complex128 [wave][n] (fp32 = 0) or complex64 (fp32 = 1), as the kernel writes them
 extern "C" int shim_amplitudes(const pwa_isobar_wave* waves, int nWaves, const double* masses, const int32_t* species,
                                double beamMass, int reflBasis, int bose, int spaceInversion, int reflection,
-                               const double* beam, const double* fs, uint64_t n, void* out, int fp32)
+                               const double* beam, const double* fs, uint64_t n, void* out, int fp32,
+                               int canonical)
 {
 	std::vector<pwa_isobar_wave> ws(waves, waves + nWaves);
 	for (const pwa_isobar_wave& w : ws)
@@ -16,7 +17,7 @@ extern "C" int shim_amplitudes(const pwa_isobar_wave* waves, int nWaves, const d
 			return 1;
 	pwa::iso::Plan plan;
 	if (!pwa::iso::buildPlan(ws, masses, species, beamMass, reflBasis != 0, bose != 0, spaceInversion != 0,
-	                         reflection != 0, plan)
+	                         reflection != 0, canonical != 0, plan)
 	         .empty())
 		return 2;
 	const pwa::iso::PlanView v = plan.view();

@@ -21,22 +21,26 @@ from isobar_cases import NAMES, SPECIES, TOL, TOL32, events, rel_err, tolerances
 pytestmark = pytest.mark.gpu
 
 OPTIONS = [{}, {"bose": False}, {"space_inversion": True}, {"reflection": True},
-           {"space_inversion": True, "reflection": True}]
+           {"space_inversion": True, "reflection": True}, {"formalism": "canonical"},
+           {"formalism": "canonical", "bose": False, "reflection": True}]
+OPTION_IDS = ["default", "no-bose", "inversion", "reflection", "both", "canonical", "canonical-no-bose-reflection"]
 SETTERS = {"bose": "enableBoseSymmetrization", "space_inversion": "enableSpaceInversion",
            "reflection": "enableReflection", "reflectivity_basis": "enableReflectivityBasis"}
 
 
 def _amp(ws, masses, mb, opts=None):
-    A = I.isobarHelicityAmplitudes()
+    opts = dict(opts or {})
+    canonical = opts.pop("formalism", "helicity") == "canonical"
+    A = I.isobarCanonicalAmplitudes() if canonical else I.isobarHelicityAmplitudes()
     A.setFinalState(NAMES, masses, mb)
-    for k, v in (opts or {}).items():
+    for k, v in opts.items():
         getattr(A, SETTERS[k])(v)
     for _, kw in ws:
         A.addWave(**kw)
     return A
 
 
-@pytest.mark.parametrize("opts", OPTIONS, ids=["default", "no-bose", "inversion", "reflection", "both"])
+@pytest.mark.parametrize("opts", OPTIONS, ids=OPTION_IDS)
 def test_amplitudes_match_oracle_host_buffers(opts):
     ws = waves()
     beam, fs, masses, mb = events(2000, seed=11)
@@ -49,7 +53,7 @@ def test_amplitudes_match_oracle_host_buffers(opts):
     assert np.all(got[-1] == 0)                       # zero by reflectivity (M = 0, f = +1)
 
 
-@pytest.mark.parametrize("opts", OPTIONS[:2], ids=["default", "no-bose"])
+@pytest.mark.parametrize("opts", [OPTIONS[0], OPTIONS[1], OPTIONS[5]], ids=["default", "no-bose", "canonical"])
 def test_complex64_mode_matches_oracle(opts):
     import torch
     ws = waves()

@@ -54,16 +54,19 @@ def _shim_amps(lib, ws, beam, fs, masses, mb, opts, dtype=np.complex128):
                              C.c_double(mb), int(opts.get("reflectivity_basis", True)), int(opts.get("bose", True)),
                              int(opts.get("space_inversion", False)), int(opts.get("reflection", False)),
                              b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), C.c_uint64(n),
-                             out.ctypes.data_as(C.c_void_p), int(dtype == np.complex64))
+                             out.ctypes.data_as(C.c_void_p), int(dtype == np.complex64),
+                             int(opts.get("formalism", "helicity") == "canonical"))
     assert rc == 0
     return out
 
 
 OPTIONS = [{}, {"bose": False}, {"space_inversion": True}, {"reflection": True},
-           {"space_inversion": True, "reflection": True}]
+           {"space_inversion": True, "reflection": True}, {"formalism": "canonical"},
+           {"formalism": "canonical", "bose": False, "reflection": True}]
+OPTION_IDS = ["default", "no-bose", "inversion", "reflection", "both", "canonical", "canonical-no-bose-reflection"]
 
 
-@pytest.mark.parametrize("opts", OPTIONS, ids=["default", "no-bose", "inversion", "reflection", "both"])
+@pytest.mark.parametrize("opts", OPTIONS, ids=OPTION_IDS)
 def test_kernel_arithmetic_matches_oracle(shim, opts):
     ws = waves()
     beam, fs, masses, mb = events(1500, seed=5)
@@ -75,7 +78,7 @@ def test_kernel_arithmetic_matches_oracle(shim, opts):
     assert np.all(ref[-1] == 0) and np.all(got[-1] == 0)
 
 
-@pytest.mark.parametrize("opts", OPTIONS[:2], ids=["default", "no-bose"])
+@pytest.mark.parametrize("opts", [OPTIONS[0], OPTIONS[1], OPTIONS[5]], ids=["default", "no-bose", "canonical"])
 def test_kernel_arithmetic_complex64_mode(shim, opts):
     """FP64 frames and kinematics, FP32 per-wave arithmetic, complex64 out."""
     ws = waves()
@@ -87,12 +90,14 @@ def test_kernel_arithmetic_complex64_mode(shim, opts):
     assert np.all(got[-1] == 0)
 
 
-def test_kernel_arithmetic_helicity_basis(shim):
+@pytest.mark.parametrize("formalism", ["helicity", "canonical"])
+def test_kernel_arithmetic_without_reflectivity_basis(shim, formalism):
     """without the reflectivity basis M may be negative (DFunctionConj)."""
     ws = [(dict(w, M=-w["M"]), dict(kw, M=-kw["M"])) for w, kw in waves()[:4]]
     beam, fs, masses, mb = events(500, seed=6)
-    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, reflectivity_basis=False)
-    got = _shim_amps(shim, ws, beam, fs, masses, mb, {"reflectivity_basis": False})
+    opts = {"reflectivity_basis": False, "formalism": formalism}
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, **opts)
+    got = _shim_amps(shim, ws, beam, fs, masses, mb, opts)
     assert np.all(rel_err(ref, got) < tolerances(ws, TOL))
 
 

@@ -140,3 +140,37 @@ def test_reflectivity_basis_combination(sample):
         minus = O.amplitudes([dict(w, M=-w["M"])], beam, fs, masses, mb, SPECIES, reflectivity_basis=False)[0]
         f = O.reflectivity_factor(w["J"], w["P"], w["M"], w["refl"])
         assert np.abs(A[k] - (plus - f * minus) / math.sqrt(2)).max() < 1e-12 * np.abs(A[k]).max()
+
+
+def test_canonical_equals_helicity_up_to_a_sign(sample):
+    """for spinless final-state particles the canonical amplitudes
+    (isobarCanonicalAmplitude: boost-only isobar frame, sum over mL of
+    couplings times Y_L^mL) equal the helicity ones (rotated helicity frame,
+    D functions): two independent routes through the frames and the spin
+    algebra.  With the bachelor as the X vertex's daughter 1 the two
+    conventions differ by a sign that is constant per wave (the order of the
+    spins in the S coupling); with the isobar first they are equal."""
+    W, beam, fs, masses, mb, A = sample
+    Cn = O.amplitudes(W, beam, fs, masses, mb, SPECIES, formalism="canonical")
+    for k, w in enumerate(W):
+        s = np.abs(A[k]).max()
+        if s == 0:
+            assert np.all(Cn[k] == 0)
+            continue
+        sign = -1.0 if np.abs(Cn[k] + A[k]).max() < np.abs(Cn[k] - A[k]).max() else 1.0
+        assert np.abs(Cn[k] - sign * A[k]).max() < 1e-9 * s    # the frames' FP64 rounding
+        if not w["bachelor_first"]:
+            assert sign == 1.0
+
+
+def test_canonical_eigenvalues(sample):
+    W, beam, fs, masses, mb, A = sample
+    Cn = O.amplitudes(W, beam, fs, masses, mb, SPECIES, formalism="canonical")
+    Cr = O.amplitudes(W, beam, fs, masses, mb, SPECIES, formalism="canonical", reflection=True)
+    Cp = O.amplitudes(W, beam, fs, masses, mb, SPECIES, formalism="canonical", space_inversion=True)
+    for k, w in enumerate(W):
+        s = np.abs(Cn[k]).max()
+        if s == 0:
+            continue
+        assert np.abs(Cr[k] - w["refl"] * Cn[k]).max() < 1e-10 * s
+        assert np.abs(Cp[k] + w["P"] * Cn[k]).max() < 1e-10 * s
