@@ -247,7 +247,8 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 		return C2T<T>{f * B, f * Cc};
 	}
 	if (w.massDep == kMassF0980Bw) {
-		// f0980BreitWigner (massDependence.cc:363-390): Gamma = Gamma0 q / q0
+		// f0980BreitWigner (massDependence.cc:363-390): Gamma = Gamma0 q / q0;
+		// at q = 0 (an isobar exactly at its threshold) 0/0 as in the reference
 		const T q2 = breakup2<T>(mI, T(w.ma), T(w.mb));
 		const T q = q2 > T(0) ? sqrt(q2) : T(0);
 		const T Cc = m0 * g0 * (q / T(w.q0));
@@ -276,7 +277,7 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 // kinematics of one symmetrisation term for one topology class
 struct Kin {
 	double phi, cX, sX, qX;         // analyser of the X vertex in the GJ frame: phi, cos/sin(theta/2), |p|
-	double phiH, cI, sI, qI;        // isobar daughter 1 in the isobar helicity frame
+	double phiH, cI, sI, qI;        // isobar daughter 1 in the isobar's helicity (canonical: rest) frame
 	double mI;                      // isobar mass
 };
 

@@ -199,6 +199,32 @@ class isobarCanonicalAmplitudes(isobarHelicityAmplitudes):
         N.call("pwa_isobar_set_formalism", self._h, 1)
 
 
+def finalStateMass(ev):
+    """invariant mass of the final state of every event of an .evt file
+    (readEvtFile), the usual on-the-fly binning variable ("mass")."""
+    p = np.sum(ev["fs"], axis=0)
+    E = np.sum(np.sqrt(ev["fs_masses"][:, None] ** 2 + np.sum(ev["fs"] ** 2, axis=2)), axis=0)
+    return np.sqrt(np.maximum(E * E - np.sum(p * p, axis=1), 0.0))
+
+
+def calcAmplitudes(amp, evtPath, ampPath, dtype="complex64", binVars=None):
+    """The calcAmplitudes step (pyInterface/scripts/calcAmplitudes.py): the
+    amplitudes of every wave of `amp` (a wave set whose final state is set)
+    for the events of an .evt file, written as one raw amplitude file with the
+    final-state mass (and any further binVars {name: [N]}) as binning
+    variables, ready for pwaLikelihood.loadAmplitudeFiles.  Returns the wave
+    names written."""
+    from . import evtfile
+    from .ampfile import writeAmplitudeFile
+    ev = evtfile.readEvtFile(evtPath)
+    A = amp.amplitudes(ev["beam"], ev["fs"], dtype=dtype)
+    names = [amp.waveName(k) for k in range(amp.nmbWaves())]
+    bv = {"mass": finalStateMass(ev)}
+    bv.update(binVars or {})
+    writeAmplitudeFile(ampPath, names, A, bv)
+    return names
+
+
 def clebschGordanCoeff(j1, m1, j2, m2, J, M):
     """(j1 m1 j2 m2 | J M), arguments doubled (utilities/spinUtils.hpp:241-330)."""
     v = C.c_double()

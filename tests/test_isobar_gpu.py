@@ -173,3 +173,50 @@ def test_caller_stream():
     s.synchronize()
     assert np.array_equal(dev.cpu().numpy(), host)
     assert np.array_equal(A.amplitudes(beam, fs), host)       # host buffers: synchronous on that stream
+
+
+def test_evt_file_to_amplitude_file_to_likelihood(tmp_path):
+    """events in an .evt file -> calcAmplitudes (GPU, complex64) -> raw
+    amplitude file with the 3pi mass -> likelihood with on-the-fly binning
+    on that mass, against the same likelihood fed the selected events'
+    amplitudes directly."""
+    from rootpwa_gb300 import evtfile, synth
+    ws = waves()[:8]
+    beam, fs, masses, mb = events(6000, seed=41)
+    evt = tmp_path / "ev.evt"
+    evtfile.writeEvtFile(evt, 9, beam, [9, 8, 9], fs)
+    A = _amp(ws, masses, mb)
+    names = I.calcAmplitudes(A, evt, tmp_path / "ev.amp")
+    assert len(names) == len(ws) and len(set(names)) == len(ws)
+    amps = A.amplitudes(beam, fs, dtype="complex64")
+    m3 = I.finalStateMass(evtfile.readEvtFile(evt))
+    keep = (m3 >= 1.2) & (m3 < 1.6)
+    refl = [kw["refl"] for _, kw in ws]
+    mc = A.amplitudes(*events(20000, seed=42)[:2], dtype="complex64")
+    norm = R.ampIntegralMatrix()
+    norm.integrate(names, mc, precision="fp64")
+    p = np.random.default_rng(43)
+
+    def lik(load):
+        L = R.pwaLikelihood()
+        L.init(names, refl, None, 1, 0.0)
+        n2 = R.ampIntegralMatrix()
+        n2.setWaveNames(names)
+        n2.setMatrix(norm.matrix())
+        n2.setNmbEvents(norm.nmbEvents())
+        a2 = R.ampIntegralMatrix()
+        a2.setWaveNames(names)
+        a2.setMatrix(norm.matrix())
+        a2.setNmbEvents(norm.nmbEvents())
+        L.addNormIntegral(n2)
+        L.addAccIntegral(a2)
+        load(L)
+        L.finishInit()
+        return L
+    Lf = lik(lambda L: L.loadAmplitudeFiles([tmp_path / "ev.amp"], {"mass": (1.2, 1.6)}))
+    Ld = lik(lambda L: [L.addAmplitude(n, np.ascontiguousarray(amps[k][keep])) for k, n in enumerate(names)])
+    assert Lf.nmbEvents() == Ld.nmbEvents() == int(keep.sum())
+    x = p.standard_normal(Lf.nmbPars())
+    f1, g1 = Lf.FdF(x)
+    f2, g2 = Ld.FdF(x)
+    assert f1 == f2 and np.array_equal(g1, g2)
