@@ -938,7 +938,7 @@ def run_isobar(args):
         "fp64_mode": {"ms_per_step": ms64, "value": n / (ms64 * 1e-3), "unit": "events/s",
                       "dtype": "f64 throughout, complex128 out"},
         "data": "synthetic: seeded diffractive 3pi events (phase space), 88-wave isobar set",
-        "config": {"workload": "isobar3pi88", "events": n, "waves": W, "sym_terms": A.nmbSymTerms(),
+        "config": {"workload": "isobar3pi88", "events": n, "waves": W, "sym_terms": A.nmbSymTerms(0),
                    "l2": "inputs and outputs (%.2f GB) larger than L2" % (algo_bytes / 1e9)},
         "e2e": {"value": n / t_e2e, "unit": "events/s", "h2d_bytes_per_step": n * 12 * 8,
                 "d2h_bytes_per_step": n * W * 8},

@@ -462,6 +462,7 @@ typedef struct pwa_isobar_wave {
 	double isobarMass, isobarWidth;   /* GeV/c^2 */
 	int32_t isobarDaughter1, isobarDaughter2, bachelor; /* final-state slots 0..2; isobar daughter 1 is the analyser */
 	int32_t bachelorFirst;            /* X-vertex daughter 1 (the analyser) is the bachelor rather than the isobar */
+	int32_t isospin, isobarIsospin;   /* 2I of X and of the isobar (isospin symmetrisation only) */
 } pwa_isobar_wave;
 /* isobarHelicityAmplitude (decayAmplitude/isobarHelicityAmplitude.cc:64-195)
  * or isobarCanonicalAmplitude (decayAmplitude/isobarCanonicalAmplitude.cc:64-190) */
@@ -484,10 +485,19 @@ int pwa_isobar_set_formalism(pwa_isobar* A, int formalism);
  * default stream); calls with device buffers are then asynchronous in stream
  * order, calls with host buffers still return with the results in place */
 int pwa_isobar_set_stream(pwa_isobar* A, void* cudaStream);
+/* isospin symmetrisation (isobarDecayTopology::getIsospinSymmetrization,
+ * isobarDecayTopology.cc:505-630; isobarAmplitude::enableIsospinSymmetrization):
+ * the final-state particles' 2I, 2I_3 and intrinsic parities; enabling it
+ * needs them (it is off by default here, on in the reference, which takes the
+ * isospins from its particle table) */
+int pwa_isobar_set_isospins(pwa_isobar* A, const int32_t* isospin, const int32_t* isospinProj,
+                            const int32_t* parity);
+int pwa_isobar_enable_isospin_symmetrization(pwa_isobar* A, int flag);
 int pwa_isobar_add_wave(pwa_isobar* A, const pwa_isobar_wave* wave);
 int pwa_isobar_nmb_waves(const pwa_isobar* A, uint32_t* n);
-/* number of symmetrisation terms of the current final state and options */
-int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t* n);
+/* number of symmetrisation terms (Bose times isospin) of one wave with the
+ * current final state and options */
+int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t wave, uint32_t* n);
 /* amplitudes of every wave for nEvents events: beam momenta [3][nEvents]
  * (px, py, pz rows), final-state momenta [3 particles][3][nEvents], lab frame,
  * GeV/c; amps [wave][nEvents] of ampType: PWA_COMPLEX128 (FP64 arithmetic

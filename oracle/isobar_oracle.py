@@ -28,7 +28,10 @@ It follows the reference step by step, vectorised over events with numpy:
   mL of the (reflectivity-combined) (L mL S mS | J M) Y_L^mL(theta, phi).
 * Bose symmetrisation: sum over the permutations of identical final-state
   particles with factor 1/sqrt(prod n_k!) (isobarDecayTopology.cc:638-670,
-  isobarAmplitude.cc:98-111); space inversion and reflection through the
+  isobarAmplitude.cc:98-111); isospin symmetrisation over permutations of
+  isospin partners with isospin Clebsch-Gordan factors
+  (isobarDecayTopology.cc:505-630), combined with the Bose terms as in
+  isobarAmplitude.cc:265-330; space inversion and reflection through the
   production plane as in isobarAmplitude.cc:174-203.
 * mass dependences: flat, relativistic Breit-Wigner with the PWA2000 rule
   q0 = sqrt|q0^2| (massDependence.cc:254-296, utilities/physUtils.hpp:283-300),
@@ -299,6 +302,87 @@ def _mass(lv):
 
 # -- amplitudes --------------------------------------------------------------------
 
+def _can_couple(j1, m1, j2, m2, J, M):
+    """spinStatesCanCouple(j1, m1, j2, m2, J, M) (utilities/spinUtils.hpp:167):
+    valid projections, triangle rule, M = m1 + m2 (arguments doubled)."""
+    def ok(j, m):
+        return j >= 0 and abs(m) <= j and (j - m) % 2 == 0
+    return (ok(j1, m1) and ok(j2, m2) and ok(J, M) and abs(j1 - j2) <= J <= j1 + j2
+            and (j1 + j2 - J) % 2 == 0 and M == m1 + m2)
+
+
+def isospin_terms(w, species, isospins, isospin_projs, parities):
+    """isobarDecayTopology::getIsospinSymmetrization (isobarDecayTopology.cc:
+    505-630) for X -> isobar(a, b) + bachelor c: permutations within groups of
+    final-state particles of equal isospin and parity (all spin 0), in the
+    order of getAllGroupPermutations (:889-923); a permutation is dropped if,
+    against an accepted one, it exchanges particles of equal species or two
+    particles of one vertex, or if the permuted isospin projections cannot
+    couple at a vertex; the factor is the product of the isospin
+    Clebsch-Gordan coefficients of both vertices, divided by sqrt(number of
+    terms), or 1 when only one term survives.  Returns [(perm, factor)],
+    slot i taking particle perm[i]."""
+    n = len(species)
+    keys = []
+    for i in range(n):
+        k = (isospins[i], parities[i])
+        if k not in keys:
+            keys.append(k)
+    groups = [[i for i in range(n) if (isospins[i], parities[i]) == k] for k in keys]
+
+    def group_perms(gs):
+        cur = sorted(gs[-1])
+        curs = list(permutations(cur))            # lexicographic, like next_permutation
+        if len(gs) == 1:
+            return [[list(c)] for c in curs]
+        sub = group_perms(gs[:-1])
+        return [sp + [list(c)] for c in curs for sp in sub]
+    a, b, c = w["isobar_daughters"][0], w["isobar_daughters"][1], w["bachelor"]
+    vertex = {a: 1, b: 1, c: 0}                   # the vertex each final-state slot comes from
+    I_iso, I_X = w["isobar_isospin"], w["isospin"]
+    accepted = []
+    for gp in group_perms(groups):
+        perm = [0] * n
+        for g, pg in zip(groups, gp):
+            for slot, part in zip(g, pg):
+                perm[slot] = part
+        discard = False
+        for q, _ in accepted:
+            for i in range(n):
+                if q[i] == perm[i]:
+                    continue
+                if species[q[i]] == species[perm[i]]:
+                    discard = True
+                    break
+                for j in range(i + 1, n):
+                    if q[j] == perm[j]:
+                        continue
+                    if vertex[q[i]] == vertex[q[j]] == vertex[perm[i]] == vertex[perm[j]]:
+                        discard = True
+                        break
+                if discard:
+                    break
+            if discard:
+                break
+        if discard:
+            continue
+        I3 = [isospin_projs[perm[i]] for i in range(n)]
+        I3_iso = I3[a] + I3[b]
+        I3_X = sum(isospin_projs)
+        d = [(I_iso, I3_iso), (isospins[c], I3[c])]
+        if w["bachelor_first"]:
+            d = d[::-1]
+        if not (_can_couple(isospins[a], I3[a], isospins[b], I3[b], I_iso, I3_iso)
+                and _can_couple(d[0][0], d[0][1], d[1][0], d[1][1], I_X, I3_X)):
+            continue
+        f = (clebsch_gordan(d[0][0], d[0][1], d[1][0], d[1][1], I_X, I3_X)
+             * clebsch_gordan(isospins[a], I3[a], isospins[b], I3[b], I_iso, I3_iso))
+        accepted.append((perm, f))
+    if len(accepted) == 1:
+        return [(accepted[0][0], 1.0)]            # a single term keeps factor 1 (isobarAmplitude.cc:276-279)
+    return [(p, f / math.sqrt(len(accepted))) for p, f in accepted]
+
+
 def bose_terms(species):
     """all permutations that exchange identical final-state particles, with the
     factor 1/sqrt(prod n_k!) (isobarDecayTopology.cc:638-670)."""
@@ -408,24 +492,47 @@ def _sym_term(w, beam, fs, masses, opts):
     return amp
 
 
+def sym_terms(w, species, opts):
+    """isobarAmplitude::initSymTermMaps (isobarAmplitude.cc:265-330): every
+    isospin term combined with every Bose term, map[i] = bose[iso[i]],
+    factor iso * bose."""
+    n = len(species)
+    if opts.get("isospin"):
+        iso = isospin_terms(w, species, *opts["isospin"])
+    else:
+        iso = [(list(range(n)), 1.0)]
+    if opts.get("bose", True):
+        perms, fb = bose_terms(species)
+        bose = [(list(p), fb) for p in perms]
+    else:
+        bose = [(list(range(n)), 1.0)]
+    return [([pb[pi[i]] for i in range(n)], fi * fb) for pi, fi in iso for pb, fb in bose]
+
+
 def amplitudes(waves, beam_p, fs_p, masses, beam_mass, species, **opts):
     """complex128 [W, N] amplitudes of the waves for events given by the beam
-    momentum (N, 3) and the final-state momenta (3, N, 3)."""
+    momentum (N, 3) and the final-state momenta (3, N, 3).  opts: bose,
+    reflectivity_basis, space_inversion, reflection, formalism ("helicity" or
+    "canonical"), isospin = (isospins, isospin projections, parities) of the
+    final-state particles (doubled) to isospin-symmetrise (the waves then
+    carry "isospin" and "isobar_isospin")."""
     beam = _lv(np.asarray(beam_p, dtype=np.float64), beam_mass)
     fs_p = np.asarray(fs_p, dtype=np.float64)
-    perms, factor = bose_terms(species) if opts.get("bose", True) else ([tuple(range(len(species)))], 1.0)
     out = np.zeros((len(waves), beam.shape[0]), dtype=np.complex128)
-    for p in perms:
-        # particle i takes the momentum of particle p[i] (decayTopology::revertMomenta)
-        fs = [_lv(fs_p[p[i]], masses[i]) for i in range(len(masses))]
-        for k, w in enumerate(waves):
+    for k, w in enumerate(waves):
+        for p, factor in sym_terms(w, species, opts):
+            if factor == 0:
+                continue
+            # slot i takes the momentum of particle p[i] (decayTopology::revertMomenta)
+            fs = [_lv(fs_p[p[i]], masses[i]) for i in range(len(masses))]
             out[k] += factor * _sym_term(w, beam, fs, masses, opts)
     return out
 
 
 def wave(J, P, M, refl, L, S, isobar_J, isobar_L, mass_dep, isobar_mass=0.0, isobar_width=0.0,
-         isobar_daughters=(0, 1), bachelor=2, bachelor_first=False, isobar_S=0):
-    """one wave's description (all spins doubled)."""
+         isobar_daughters=(0, 1), bachelor=2, bachelor_first=False, isobar_S=0, isospin=2, isobar_isospin=0):
+    """one wave's description (all spins and isospins doubled)."""
     return dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobar_J=isobar_J, isobar_L=isobar_L, isobar_S=isobar_S,
                 mass_dep=mass_dep, isobar_mass=isobar_mass, isobar_width=isobar_width,
-                isobar_daughters=tuple(isobar_daughters), bachelor=bachelor, bachelor_first=bool(bachelor_first))
+                isobar_daughters=tuple(isobar_daughters), bachelor=bachelor, bachelor_first=bool(bachelor_first),
+                isospin=isospin, isobar_isospin=isobar_isospin)

@@ -51,7 +51,8 @@ class IsobarWave(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("J", "P", "M", "refl", "L", "S", "isobarJ", "isobarL", "isobarS",
                                           "massDependence")] + \
         [("isobarMass", C.c_double), ("isobarWidth", C.c_double)] + \
-        [(n, C.c_int32) for n in ("isobarDaughter1", "isobarDaughter2", "bachelor", "bachelorFirst")]
+        [(n, C.c_int32) for n in ("isobarDaughter1", "isobarDaughter2", "bachelor", "bachelorFirst", "isospin",
+                                  "isobarIsospin")]
 
 
 SIGNATURES = {
@@ -161,7 +162,9 @@ SIGNATURES = {
     "pwa_isobar_set_formalism": (i, [vp, i]),
     "pwa_isobar_add_wave": (i, [vp, C.POINTER(IsobarWave)]),
     "pwa_isobar_nmb_waves": (i, [vp, C.POINTER(u32)]),
-    "pwa_isobar_nmb_sym_terms": (i, [vp, C.POINTER(u32)]),
+    "pwa_isobar_nmb_sym_terms": (i, [vp, u32, C.POINTER(u32)]),
+    "pwa_isobar_set_isospins": (i, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "pwa_isobar_enable_isospin_symmetrization": (i, [vp, i]),
     "pwa_isobar_amplitudes": (i, [vp, vp, vp, u64, vp, i, i]),
     "pwa_clebsch_gordan": (i, [i32, i32, i32, i32, i32, i32, pd]),
     "pwa_wigner_d": (i, [i32, i32, i32, C.c_double, pd]),

@@ -11,6 +11,8 @@ struct pwa_isobar {
 	double beamMass = 0.0;
 	bool finalState = false;
 	bool reflBasis = true, bose = true, spaceInversion = false, reflection = false, canonical = false;
+	bool isospinSet = false, isospinSym = false;
+	iso::FsIsospin isospin{};
 	std::vector<pwa_isobar_wave> waves;
 	iso::Plan plan;
 	bool dirty = true;
@@ -34,8 +36,9 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 int uploadPlan(pwa_isobar* A)
 {
 	iso::Plan& p = A->plan;
-	const std::string why = iso::buildPlan(A->waves, A->masses, A->species, A->beamMass, A->reflBasis, A->bose,
-	                                       A->spaceInversion, A->reflection, A->canonical, p);
+	const std::string why =
+	    iso::buildPlan(A->waves, A->masses, A->species, A->beamMass, A->reflBasis, A->bose, A->spaceInversion,
+	                   A->reflection, A->canonical, A->isospinSym ? &A->isospin : nullptr, p);
 	if (!why.empty())
 		return setError(kErrArg, why);
 	const size_t oWaves = 0;
@@ -45,7 +48,8 @@ int uploadPlan(pwa_isobar* A)
 	const size_t oPoly = align16(oTerms + p.dterms.size() * sizeof(iso::DTerm));
 	const size_t oNorm = align16(oPoly + sizeof(p.bfPoly));
 	const size_t oPerms = align16(oNorm + sizeof(p.bfNorm));
-	const size_t total = align16(oPerms + p.perms.size() * sizeof(int32_t));
+	const size_t oTermsS = align16(oPerms + p.perms.size() * sizeof(int32_t));
+	const size_t total = align16(oTermsS + p.terms.size() * sizeof(iso::SymTerm));
 	std::vector<unsigned char> h(total, 0);
 	auto put = [&](size_t off, const void* src, size_t bytes) {
 		if (bytes)
@@ -58,6 +62,7 @@ int uploadPlan(pwa_isobar* A)
 	put(oPoly, p.bfPoly, sizeof(p.bfPoly));
 	put(oNorm, p.bfNorm, sizeof(p.bfNorm));
 	put(oPerms, p.perms.data(), p.perms.size() * sizeof(int32_t));
+	put(oTermsS, p.terms.data(), p.terms.size() * sizeof(iso::SymTerm));
 	PWA_TRY(A->dPlan.ensure(total, "isobar wave plan"));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(A->dPlan.p, h.data(), total, cudaMemcpyHostToDevice, A->stream), "plan upload"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(A->stream), "plan upload"));
@@ -70,6 +75,7 @@ int uploadPlan(pwa_isobar* A)
 	v.bfPoly = reinterpret_cast<const double*>(d + oPoly);
 	v.bfNorm = reinterpret_cast<const double*>(d + oNorm);
 	v.perms = reinterpret_cast<const int32_t*>(d + oPerms);
+	v.terms = reinterpret_cast<const iso::SymTerm*>(d + oTermsS);
 	A->devView = v;
 	A->dirty = false;
 	return kOk;
@@ -180,14 +186,43 @@ int pwa_isobar_nmb_waves(const pwa_isobar* A, uint32_t* n)
 	return kOk;
 }
 
-int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t* n)
+int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t wave, uint32_t* n)
 {
 	if (!A || !n)
 		return setError(kErrArg, "null argument");
-	std::vector<int32_t> perms;
-	double f = 1.0;
-	iso::bosePermutations(A->species, A->bose, perms, f);
-	*n = (uint32_t)(perms.size() / 3);
+	if (wave >= A->waves.size())
+		return setError(kErrArg, "wave index out of range");
+	if (A->isospinSym && !A->isospinSet)
+		return setError(kErrState, "isospin symmetrisation needs the final-state isospins");
+	*n = (uint32_t)iso::symTerms(A->waves[wave], A->species, A->bose, A->isospinSym ? &A->isospin : nullptr).size();
+	return kOk;
+}
+
+int pwa_isobar_set_isospins(pwa_isobar* A, const int32_t* I, const int32_t* I3, const int32_t* P)
+{
+	if (!A || !I || !I3 || !P)
+		return setError(kErrArg, "null argument");
+	for (int i = 0; i < 3; ++i)
+		if (I[i] < 0 || std::abs(I3[i]) > I[i] || ((I[i] - I3[i]) & 1) || (P[i] != 1 && P[i] != -1))
+			return setError(kErrArg, "isospins need 0 <= |2I_3| <= 2I of equal parity and parities +-1");
+	for (int i = 0; i < 3; ++i) {
+		A->isospin.I[i] = I[i];
+		A->isospin.I3[i] = I3[i];
+		A->isospin.P[i] = P[i];
+	}
+	A->isospinSet = true;
+	A->dirty = true;
+	return kOk;
+}
+
+int pwa_isobar_enable_isospin_symmetrization(pwa_isobar* A, int flag)
+{
+	if (!A)
+		return setError(kErrArg, "null argument");
+	if (flag && !A->isospinSet)
+		return setError(kErrState, "set the final-state isospins first");
+	A->isospinSym = flag != 0;
+	A->dirty = true;
 	return kOk;
 }
 

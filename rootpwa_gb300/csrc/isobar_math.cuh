@@ -81,8 +81,17 @@ struct WaveDev {
 	double ma, mb;                  // isobar daughter masses
 	double q02;                     // breakup momentum squared at m0 (rho BW)
 	int32_t lam0, lam1;             // LamTerm range
+	int32_t term0, term1;           // SymTerm range (symmetrisation terms)
 	int32_t topo;                   // topology class (waves of one class share kinematics)
 	int32_t pad;
+};
+
+// one symmetrisation term of a wave: final-state permutation (index into the
+// six permutations of three slots) and its factor (Bose times isospin)
+struct SymTerm {
+	int32_t perm;
+	int32_t pad;
+	double factor;
 };
 
 // read-only view of a wave plan (device or host pointers)
@@ -93,9 +102,9 @@ struct PlanView {
 	const DTerm* dterms;
 	const double* bfPoly;           // [8][8]: P_l(z) coefficients of z^0..z^l
 	const double* bfNorm;           // [8]: P_l(1)
-	const int32_t* perms;           // [nPerms][3]: slot i takes particle perms[t][i]
-	uint32_t nWaves, nPerms;
-	double boseFactor;
+	const int32_t* perms;           // [6][3]: the permutations of three slots; slot i takes particle perms[p][i]
+	const SymTerm* terms;
+	uint32_t nWaves, pad0;
 	double masses[3], beamMass;
 	int32_t spaceInversion, reflection;
 	int32_t canonical;              // isobar rest frame by a boost alone (canonical formalism)
@@ -294,9 +303,11 @@ PWA_HD void halfAngle(double perp, double z, double* c, double* s)
 #endif
 }
 
-PWA_HD Kin kinematics(const LV g[3], const int32_t* perm, const WaveDev& w, bool canonical)
+// g: the Gottfried-Jackson four-vectors of the final-state slots of one
+// symmetrisation term
+PWA_HD Kin kinematics(const LV g[3], const WaveDev& w, bool canonical)
 {
-	const LV A = g[perm[w.a]], B = g[perm[w.b]], Cb = g[perm[w.c]];
+	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
 	Kin k;
 	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
@@ -360,15 +371,20 @@ PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
 	return cscale(cmul(sum, massDependence<T>(P, w, T(k.mI), T((m0 - k.mI) * (m0 + k.mI)), k.mI)), f);
 }
 
-// Gottfried-Jackson four-vectors of the three final-state particles of one
-// event: beam momentum bp, final-state momenta fp (lab)
-PWA_HD void gjFrame(const PlanView& P, const double bp[3], const double fp[3][3], LV g[3])
+// Gottfried-Jackson four-vectors of the three final-state slots of one
+// event and symmetrisation term: beam momentum bp, final-state momenta fp
+// (lab); slot i takes the momentum of particle perm[i] and keeps its own
+// mass (decayTopology::revertMomenta with particle::setMomentum), so X and
+// the frame follow the permutation when it exchanges particles of different
+// mass (isospin partners)
+PWA_HD void gjFrame(const PlanView& P, const double bp[3], const double fp[3][3], const int32_t* perm, LV g[3])
 {
 	LV f[3];
 	V3 pX{0.0, 0.0, 0.0};
 	double eX = 0.0;
 	for (int i = 0; i < 3; ++i) {
-		f[i].p = V3{fp[i][0], fp[i][1], fp[i][2]};
+		const int k = perm[i];
+		f[i].p = V3{fp[k][0], fp[k][1], fp[k][2]};
 		f[i].e = sqrt(P.masses[i] * P.masses[i] + vdot(f[i].p, f[i].p));
 		pX = vadd(pX, f[i].p);
 		eX += f[i].e;
@@ -395,22 +411,39 @@ template <typename T>
 PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double fp[3][3], T* out, uint64_t ld,
                             uint64_t e)
 {
-	LV g[3];
-	gjFrame(P, bp, fp, g);
+	// the frame of the unpermuted event; a permutation that only exchanges
+	// particles of equal mass (Bose terms) permutes its four-vectors
+	LV g0[3];
+	gjFrame(P, bp, fp, P.perms, g0);
+	// kinematics per permutation, computed once per topology class on first use
 	Kin kin[kMaxPerms];
+	uint32_t valid = 0;
 	int topo = -1;
 	for (uint32_t o = 0; o < P.nWaves; ++o) {
 		const int wi = P.order[o];
 		const WaveDev w = P.waves[wi];
 		if (w.topo != topo) {
 			topo = w.topo;
-			for (uint32_t t = 0; t < P.nPerms; ++t)
-				kin[t] = kinematics(g, P.perms + 3 * t, w, P.canonical != 0);
+			valid = 0;
 		}
 		C2T<T> a{T(0), T(0)};
-		for (uint32_t t = 0; t < P.nPerms; ++t)
-			a = cadd(a, termAmplitude<T>(P, w, kin[t]));
-		a = cscale(a, T(P.boseFactor));
+		for (int t = w.term0; t < w.term1; ++t) {
+			const SymTerm st = P.terms[t];
+			if (!((valid >> st.perm) & 1u)) {
+				const int32_t* perm = P.perms + 3 * st.perm;
+				LV g[3];
+				if (P.masses[perm[0]] == P.masses[0] && P.masses[perm[1]] == P.masses[1] &&
+				    P.masses[perm[2]] == P.masses[2]) {
+					for (int i = 0; i < 3; ++i)
+						g[i] = g0[perm[i]];
+				} else {
+					gjFrame(P, bp, fp, perm, g);
+				}
+				kin[st.perm] = kinematics(g, w, P.canonical != 0);
+				valid |= 1u << st.perm;
+			}
+			a = cadd(a, cscale(termAmplitude<T>(P, w, kin[st.perm]), T(st.factor)));
+		}
 		out[2 * ((uint64_t)wi * ld + e)] = a.re;
 		out[2 * ((uint64_t)wi * ld + e) + 1] = a.im;
 	}

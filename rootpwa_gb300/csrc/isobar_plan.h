@@ -141,8 +141,8 @@ struct Plan {
 	std::vector<DTerm> dterms;
 	double bfPoly[8][8];
 	double bfNorm[8];
-	std::vector<int32_t> perms;
-	double boseFactor = 1.0;
+	std::vector<int32_t> perms;     // the six permutations of three slots
+	std::vector<SymTerm> terms;
 	double masses[3] = {0.0, 0.0, 0.0}, beamMass = 0.0;
 	int32_t spaceInversion = 0, reflection = 0, canonical = 0;
 
@@ -156,9 +156,8 @@ struct Plan {
 		v.bfPoly = &bfPoly[0][0];
 		v.bfNorm = bfNorm;
 		v.perms = perms.data();
+		v.terms = terms.data();
 		v.nWaves = (uint32_t)waves.size();
-		v.nPerms = (uint32_t)(perms.size() / 3);
-		v.boseFactor = boseFactor;
 		for (int i = 0; i < 3; ++i)
 			v.masses[i] = masses[i];
 		v.beamMass = beamMass;
@@ -169,23 +168,174 @@ struct Plan {
 	}
 };
 
-// permutations of the three final-state slots that only exchange particles
-// of equal species; factor 1/sqrt(number of terms) = 1/sqrt(prod n_k!)
-// (isobarDecayTopology::getBoseSymmetrization, isobarDecayTopology.cc:638-670)
-inline void bosePermutations(const int32_t species[3], bool bose, std::vector<int32_t>& perms, double& factor)
+// a permutation of the three final-state slots: slot i takes particle p[i]
+typedef std::vector<int> Perm;
+struct Term {
+	Perm perm;
+	double factor;
+};
+
+// index of a permutation in the lexicographic list of the six (the kernel's table)
+inline int permIndex(const Perm& p)
 {
-	perms.clear();
+	int q[3] = {0, 1, 2}, k = 0;
+	do {
+		if (q[0] == p[0] && q[1] == p[1] && q[2] == p[2])
+			return k;
+		++k;
+	} while (std::next_permutation(q, q + 3));
+	return -1;
+}
+
+// permutations that only exchange particles of equal species, factor
+// 1/sqrt(number of terms) = 1/sqrt(prod n_k!)
+// (isobarDecayTopology::getBoseSymmetrization, isobarDecayTopology.cc:638-670)
+inline std::vector<Term> boseTerms(const int32_t species[3], bool bose)
+{
+	std::vector<Term> out;
 	int p[3] = {0, 1, 2};
-	if (!bose) {
-		perms.assign(p, p + 3);
-		factor = 1.0;
-		return;
-	}
+	if (!bose)
+		return {Term{Perm(p, p + 3), 1.0}};
 	do {
 		if (species[p[0]] == species[0] && species[p[1]] == species[1] && species[p[2]] == species[2])
-			perms.insert(perms.end(), p, p + 3);
+			out.push_back(Term{Perm(p, p + 3), 1.0});
 	} while (std::next_permutation(p, p + 3));
-	factor = 1.0 / std::sqrt((double)(perms.size() / 3));
+	for (Term& t : out)
+		t.factor = 1.0 / std::sqrt((double)out.size());
+	return out;
+}
+
+// spinStatesCanCouple(j1, m1, j2, m2, J, M) (utilities/spinUtils.hpp:167):
+// valid projections, triangle rule, M = m1 + m2
+inline bool canCouple(int j1, int m1, int j2, int m2, int J, int M)
+{
+	auto ok = [](int j, int m) { return j >= 0 && std::abs(m) <= j && ((j - m) & 1) == 0; };
+	return ok(j1, m1) && ok(j2, m2) && ok(J, M) && J >= std::abs(j1 - j2) && J <= j1 + j2 &&
+	       ((j1 + j2 - J) & 1) == 0 && M == m1 + m2;
+}
+
+// final-state isospins for isospin symmetrisation (all doubled)
+struct FsIsospin {
+	int32_t I[3], I3[3], P[3];
+};
+
+// isobarDecayTopology::getIsospinSymmetrization (isobarDecayTopology.cc:505-630)
+// for X -> isobar(a, b) + bachelor c: all permutations within groups of
+// final-state particles of equal isospin and parity (spins are 0), ordered
+// like getAllGroupPermutations (:889-923: the last group's permutation
+// outermost); against every accepted permutation, one that exchanges
+// particles of equal species or two particles of one vertex is dropped; the
+// permuted isospin projections must couple at both vertices; the factor is
+// the product of both vertices' isospin Clebsch-Gordan coefficients over
+// sqrt(number of terms), or 1 for a single term (isobarAmplitude.cc:276-279).
+inline std::vector<Term> isospinTerms(const pwa_isobar_wave& w, const int32_t species[3], const FsIsospin& fs)
+{
+	// groups of equal (I, P), in order of first appearance
+	std::vector<std::vector<int>> groups;
+	std::vector<std::pair<int, int>> keys;
+	for (int i = 0; i < 3; ++i) {
+		const std::pair<int, int> k(fs.I[i], fs.P[i]);
+		auto it = std::find(keys.begin(), keys.end(), k);
+		if (it == keys.end()) {
+			keys.push_back(k);
+			groups.push_back({i});
+		} else {
+			groups[it - keys.begin()].push_back(i);
+		}
+	}
+	// all products of within-group permutations, the last group outermost
+	std::vector<std::vector<std::vector<int>>> combos{{}};
+	for (const std::vector<int>& g : groups) {
+		std::vector<int> cur = g;
+		std::sort(cur.begin(), cur.end());
+		std::vector<std::vector<int>> gp;
+		do
+			gp.push_back(cur);
+		while (std::next_permutation(cur.begin(), cur.end()));
+		std::vector<std::vector<std::vector<int>>> next;
+		for (const std::vector<int>& c : gp)
+			for (const std::vector<std::vector<int>>& sub : combos) {
+				std::vector<std::vector<int>> e = sub;
+				e.push_back(c);
+				next.push_back(e);
+			}
+		combos.swap(next);
+	}
+	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
+	int vertexOf[3];
+	vertexOf[a] = vertexOf[b] = 1;
+	vertexOf[c] = 0;
+	int I3X = 0;
+	for (int i = 0; i < 3; ++i)
+		I3X += fs.I3[i];
+	std::vector<Term> acc;
+	for (const std::vector<std::vector<int>>& combo : combos) {
+		Perm p(3);
+		for (size_t gi = 0; gi < groups.size(); ++gi)
+			for (size_t k = 0; k < groups[gi].size(); ++k)
+				p[groups[gi][k]] = combo[gi][k];
+		bool drop = false;
+		for (const Term& q : acc) {
+			for (int i = 0; i < 3 && !drop; ++i) {
+				if (q.perm[i] == p[i])
+					continue;
+				if (species[q.perm[i]] == species[p[i]]) {
+					drop = true;
+					break;
+				}
+				for (int j = i + 1; j < 3; ++j)
+					if (q.perm[j] != p[j] && vertexOf[q.perm[i]] == vertexOf[q.perm[j]] &&
+					    vertexOf[q.perm[i]] == vertexOf[p[i]] && vertexOf[p[i]] == vertexOf[p[j]]) {
+						drop = true;
+						break;
+					}
+			}
+			if (drop)
+				break;
+		}
+		if (drop)
+			continue;
+		int I3[3];
+		for (int i = 0; i < 3; ++i)
+			I3[i] = fs.I3[p[i]];
+		const int I3iso = I3[a] + I3[b];
+		int d1 = w.isobarIsospin, d1p = I3iso, d2 = fs.I[c], d2p = I3[c];
+		if (w.bachelorFirst) {
+			std::swap(d1, d2);
+			std::swap(d1p, d2p);
+		}
+		if (!canCouple(fs.I[a], I3[a], fs.I[b], I3[b], w.isobarIsospin, I3iso) ||
+		    !canCouple(d1, d1p, d2, d2p, w.isospin, I3X))
+			continue;
+		const double f = clebschGordan(d1, d1p, d2, d2p, w.isospin, I3X) *
+		                 clebschGordan(fs.I[a], I3[a], fs.I[b], I3[b], w.isobarIsospin, I3iso);
+		acc.push_back(Term{p, f});
+	}
+	if (acc.size() == 1)
+		acc[0].factor = 1.0;
+	else
+		for (Term& t : acc)
+			t.factor /= std::sqrt((double)acc.size());
+	return acc;
+}
+
+// isobarAmplitude::initSymTermMaps (isobarAmplitude.cc:265-330): every
+// isospin term combined with every Bose term, map[i] = bose[iso[i]], factor
+// iso * bose
+inline std::vector<Term> symTerms(const pwa_isobar_wave& w, const int32_t species[3], bool bose,
+                                  const FsIsospin* isospin)
+{
+	const std::vector<Term> iso = isospin ? isospinTerms(w, species, *isospin) : std::vector<Term>{Term{{0, 1, 2}, 1.0}};
+	const std::vector<Term> bt = boseTerms(species, bose);
+	std::vector<Term> out;
+	for (const Term& ti : iso)
+		for (const Term& tb : bt) {
+			Perm m(3);
+			for (int i = 0; i < 3; ++i)
+				m[i] = tb.perm[ti.perm[i]];
+			out.push_back(Term{m, ti.factor * tb.factor});
+		}
+	return out;
 }
 
 // canonical formalism (isobarCanonicalAmplitude::twoBodyDecayAmplitude,
@@ -256,7 +406,8 @@ inline void addCanonicalTerms(const pwa_isobar_wave& s, bool reflBasis, Plan& pl
 // final-state masses
 inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const double masses[3],
                              const int32_t species[3], double beamMass, bool reflBasis, bool bose,
-                             bool spaceInversion, bool reflection, bool canonical, Plan& plan)
+                             bool spaceInversion, bool reflection, bool canonical, const FsIsospin* isospin,
+                             Plan& plan)
 {
 	plan.canonical = canonical ? 1 : 0;
 	for (int i = 0; i < 3; ++i)
@@ -267,8 +418,15 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 	plan.waves.clear();
 	plan.lams.clear();
 	plan.dterms.clear();
+	plan.terms.clear();
 	barrierPolynomials(plan.bfPoly, plan.bfNorm);
-	bosePermutations(species, bose, plan.perms, plan.boseFactor);
+	plan.perms.clear();
+	{
+		int q[3] = {0, 1, 2};
+		do
+			plan.perms.insert(plan.perms.end(), q, q + 3);
+		while (std::next_permutation(q, q + 3));
+	}
 	std::vector<std::tuple<int, int, int, int>> topoKeys;
 	for (const pwa_isobar_wave& s : specs) {
 		WaveDev w{};
@@ -298,6 +456,11 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 				       ": the isobar mass is below the threshold of its daughters";
 			w.q0 = std::sqrt(w.q02);
 		}
+		w.term0 = (int32_t)plan.terms.size();
+		for (const Term& t : symTerms(s, species, bose, isospin))
+			if (t.factor != 0.0)  // zero terms (a vanishing isospin coupling) only enter the normalisation
+				plan.terms.push_back(SymTerm{permIndex(t.perm), 0, t.factor});
+		w.term1 = (int32_t)plan.terms.size();
 		const std::tuple<int, int, int, int> key(w.a, w.b, w.c, w.bachelorFirst);
 		auto it = std::find(topoKeys.begin(), topoKeys.end(), key);
 		w.topo = (int32_t)(it - topoKeys.begin());

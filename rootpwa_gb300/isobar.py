@@ -28,6 +28,8 @@ import numpy as np
 
 from . import _native as N
 
+# (2I, 2I_3, intrinsic parity) of the pions
+PION_ISOSPINS = {"pi-": (2, -2, -1), "pi0": (2, 0, -1), "pi+": (2, 2, -1)}
 MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2, "rhoBreitWigner": 3,
                     "f0980BreitWigner": 4, "f0980FlatteBesII": 5}
 
@@ -51,6 +53,7 @@ class isobarHelicityAmplitudes:
         self._opts = [1, 1, 0, 0]
         self._async = False
         self._stream = 0
+        self._isospin = False
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -61,10 +64,11 @@ class isobarHelicityAmplitudes:
             self._h = None
 
     # -- final state and options ---------------------------------------------------
-    def setFinalState(self, names, masses, beamMass, species=None):
+    def setFinalState(self, names, masses, beamMass, species=None, isospins=None):
         """names of the three final-state particles (equal names are identical
         particles unless species says otherwise), their masses and the beam
-        mass in GeV/c^2."""
+        mass in GeV/c^2; isospins [(2I, 2I_3, intrinsic parity)] for isospin
+        symmetrisation (filled in for pions when not given)."""
         names = list(names)
         if species is None:
             ids = {}
@@ -74,6 +78,20 @@ class isobarHelicityAmplitudes:
         N.call("pwa_isobar_set_final_state", self._h, len(names), m.ctypes.data_as(N.pd),
                sp.ctypes.data_as(C.POINTER(C.c_int32)), float(beamMass))
         self._names = names
+        if isospins is None and all(n in PION_ISOSPINS for n in names):
+            isospins = [PION_ISOSPINS[n] for n in names]
+        if isospins is not None:
+            I, I3, P = (np.ascontiguousarray([x[k] for x in isospins], dtype=np.int32) for k in range(3))
+            N.call("pwa_isobar_set_isospins", self._h, *(a.ctypes.data_as(C.POINTER(C.c_int32)) for a in (I, I3, P)))
+
+    def enableIsospinSymmetrization(self, flag=True):
+        """isobarAmplitude::enableIsospinSymmetrization (isobarAmplitude.h:70);
+        off by default here (it needs the final-state isospins)."""
+        N.call("pwa_isobar_enable_isospin_symmetrization", self._h, 1 if flag else 0)
+        self._isospin = bool(flag)
+
+    def isospinSymmetrization(self):
+        return self._isospin
 
     def _set_opts(self, k, flag):
         o = list(self._opts)
@@ -116,13 +134,16 @@ class isobarHelicityAmplitudes:
     # -- waves ---------------------------------------------------------------------
     def addWave(self, J, P, M, refl, L, S, isobarJ, isobarL, massDependence="flat", isobarMass=0.0,
                 isobarWidth=0.0, isobarDaughters=(0, 1), bachelor=2, bachelorFirst=False, isobarS=0,
-                isobarName="isobar", isospin=2, G=-1, C_=+1):
-        """adds one wave (all spins doubled); returns its index."""
+                isobarName="isobar", isospin=2, G=-1, C_=+1, isobarIsospin=0):
+        """adds one wave (all spins and isospins doubled); returns its index.
+        isospin and isobarIsospin (2I of X and of the isobar) enter isospin
+        symmetrisation and the wave name."""
         md = MASS_DEPENDENCES[massDependence] if isinstance(massDependence, str) else int(massDependence)
         w = N.IsobarWave(J=J, P=P, M=M, refl=refl, L=L, S=S, isobarJ=isobarJ, isobarL=isobarL, isobarS=isobarS,
                          massDependence=md, isobarMass=isobarMass, isobarWidth=isobarWidth,
                          isobarDaughter1=isobarDaughters[0], isobarDaughter2=isobarDaughters[1],
-                         bachelor=bachelor, bachelorFirst=1 if bachelorFirst else 0)
+                         bachelor=bachelor, bachelorFirst=1 if bachelorFirst else 0, isospin=isospin,
+                         isobarIsospin=isobarIsospin)
         N.call("pwa_isobar_add_wave", self._h, C.byref(w))
         self._waves.append(dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobarJ=isobarJ, isobarL=isobarL,
                                 isobarS=isobarS, isobarDaughters=tuple(isobarDaughters), bachelor=bachelor,
@@ -135,9 +156,10 @@ class isobarHelicityAmplitudes:
         N.call("pwa_isobar_nmb_waves", self._h, C.byref(n))
         return n.value
 
-    def nmbSymTerms(self):
+    def nmbSymTerms(self, wave=0):
+        """symmetrisation terms (Bose times isospin) of one wave."""
         n = C.c_uint32()
-        N.call("pwa_isobar_nmb_sym_terms", self._h, C.byref(n))
+        N.call("pwa_isobar_nmb_sym_terms", self._h, int(wave), C.byref(n))
         return n.value
 
     def waveName(self, i):

@@ -180,15 +180,15 @@ def _boost(p, E, b):
     return p + (g2 * bp)[:, None] * b + (g * E)[:, None] * b
 
 
-def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2):
+def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2, masses=None):
     """Seeded diffractive events pi- p -> (pi- pi+ pi-) p: the beam along z
     with a small divergence, X of mass uniform in [m_lo, m_hi] GeV/c^2 with a
     small transverse momentum, decaying by three-body phase space (uniform in
     the Dalitz plane).  Returns beam (N, 3), final state (3, N, 3) lab
     momenta in GeV/c (particle order pi-, pi+, pi-), the three masses and the
-    beam mass."""
+    beam mass.  masses: other final-state masses (e.g. pi- pi0 pi0)."""
     rng = np.random.default_rng(seed)
-    m = M_PI
+    m1, m2, m3 = (M_PI, M_PI, M_PI) if masses is None else masses
     beam = np.stack([rng.normal(0, 0.05, n), rng.normal(0, 0.05, n), np.full(n, beam_momentum)], axis=1)
     MX = rng.uniform(m_lo, m_hi, n)
     pX = beam.copy()
@@ -200,13 +200,13 @@ def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2):
     todo = np.arange(n)
     while todo.size:
         M = MX[todo]
-        s12 = rng.uniform((2 * m) ** 2, (M - m) ** 2)
-        s23 = rng.uniform((2 * m) ** 2, (M - m) ** 2)
-        E3 = (M * M + m * m - s12) / (2 * M)
-        E1 = (M * M + m * m - s23) / (2 * M)
+        s12 = rng.uniform((m1 + m2) ** 2, (M - m3) ** 2)
+        s23 = rng.uniform((m2 + m3) ** 2, (M - m1) ** 2)
+        E3 = (M * M + m3 * m3 - s12) / (2 * M)
+        E1 = (M * M + m1 * m1 - s23) / (2 * M)
         E2 = M - E1 - E3
-        p1, p2, p3 = [np.sqrt(np.maximum(E * E - m * m, 0)) for E in (E1, E2, E3)]
-        ok = (E1 > m) & (E2 > m) & (E3 > m)
+        p1, p2, p3 = [np.sqrt(np.maximum(E * E - mm * mm, 0)) for E, mm in ((E1, m1), (E2, m2), (E3, m3))]
+        ok = (E1 > m1) & (E2 > m2) & (E3 > m3)
         with np.errstate(invalid="ignore", divide="ignore"):
             c13 = (p2 ** 2 - p1 ** 2 - p3 ** 2) / (2 * p1 * p3)
         ok &= np.abs(c13) < 1
@@ -228,7 +228,7 @@ def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2):
         todo = todo[~ok]
     bX = pX / EX[:, None]
     fs = np.stack([_boost(rest[i, :, :3], rest[i, :, 3], bX) for i in range(3)])
-    return beam, fs, np.array([m, m, m]), m
+    return beam, fs, np.array([m1, m2, m3]), M_PI
 
 
 # isobars of the 3pi wave sets: (name, 2J, mass, width, mass dependence)

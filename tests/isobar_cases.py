@@ -71,3 +71,37 @@ def tolerances(ws, base):
     ~1e-11 differences between the two restatements' isobar masses into up
     to ~3e-9 of the amplitude for events next to the threshold."""
     return np.array([base * (10 if w["mass_dep"] == O.MASSDEP_F0980_FLATTE else 1) for w, _ in ws])
+
+
+# pi- pi0 pi0: slot 0 pi-, slots 1 and 2 pi0 (identical)
+NEUTRAL_SPECIES = [0, 1, 1]
+NEUTRAL_NAMES = ["pi-", "pi0", "pi0"]
+NEUTRAL_MASSES = (0.13957039, 0.1349768, 0.1349768)
+NEUTRAL_ISOSPIN = ([2, 2, 2], [-2, 0, 0], [-1, -1, -1])     # 2I, 2I_3, intrinsic parity
+
+
+def neutral_waves():
+    """pi- pi0 pi0 waves with X isospin 1: rho- pi0 (the isobar from the pi-
+    and one pi0), f2 and f0(980) to pi0 pi0, and a wave keyed as rho0 pi- that
+    isospin symmetrisation turns into rho- pi0 terms."""
+    specs = [
+        # J  P  M refl L  S  j  l  massdep             mass   width  daughters bachelor first  I_isobar
+        (2, +1, 0, +1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (0, 1), 2, False, 2),   # 1++0+ rho- pi0 S
+        (4, +1, 2, +1, 4, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (0, 1), 2, True, 2),    # 2++1+ rho- pi0 D
+        (4, -1, 0, +1, 0, 4, 4, 4, O.MASSDEP_REL_BW, M_F2, G_F2, (1, 2), 0, False, 0),     # 2-+0+ f2 pi- S
+        (0, -1, 0, +1, 0, 0, 0, 0, O.MASSDEP_F0980_BW, 0.980, 0.070, (1, 2), 0, False, 0),  # 0-+0+ f0 pi- S
+        (2, +1, 0, +1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False, 2),   # 1++0+ "rho0" pi- S
+    ]
+    md = {O.MASSDEP_REL_BW: "relativisticBreitWigner", O.MASSDEP_F0980_BW: "f0980BreitWigner"}
+    out = []
+    for J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first, Ii in specs:
+        ow = O.wave(J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first, isospin=2, isobar_isospin=Ii)
+        kw = dict(J=J, P=P, M=M, refl=r, L=L, S=S, isobarJ=j, isobarL=l, massDependence=md[m], isobarMass=mass,
+                  isobarWidth=width, isobarDaughters=dau, bachelor=bach, bachelorFirst=first, isospin=2,
+                  isobarIsospin=Ii)
+        out.append((ow, kw))
+    return out
+
+
+def neutral_events(n, seed=0):
+    return synth.three_pion_events(n, seed=seed, masses=NEUTRAL_MASSES)

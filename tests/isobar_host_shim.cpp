@@ -9,15 +9,22 @@
 extern "C" int shim_amplitudes(const pwa_isobar_wave* waves, int nWaves, const double* masses, const int32_t* species,
                                double beamMass, int reflBasis, int bose, int spaceInversion, int reflection,
                                const double* beam, const double* fs, uint64_t n, void* out, int fp32,
-                               int canonical)
+                               int canonical, const int32_t* isospins /* [3][3]: 2I, 2I_3, P, or NULL */)
 {
+	pwa::iso::FsIsospin iso{};
+	if (isospins)
+		for (int i = 0; i < 3; ++i) {
+			iso.I[i] = isospins[3 * i];
+			iso.I3[i] = isospins[3 * i + 1];
+			iso.P[i] = isospins[3 * i + 2];
+		}
 	std::vector<pwa_isobar_wave> ws(waves, waves + nWaves);
 	for (const pwa_isobar_wave& w : ws)
 		if (!pwa::iso::checkWave(w, reflBasis != 0).empty())
 			return 1;
 	pwa::iso::Plan plan;
 	if (!pwa::iso::buildPlan(ws, masses, species, beamMass, reflBasis != 0, bose != 0, spaceInversion != 0,
-	                         reflection != 0, canonical != 0, plan)
+	                         reflection != 0, canonical != 0, isospins ? &iso : nullptr, plan)
 	         .empty())
 		return 2;
 	const pwa::iso::PlanView v = plan.view();

@@ -47,7 +47,7 @@ int main(void)
     if (pwa_isobar_create(&A) != PWA_SUCCESS) return 6;
     if (pwa_isobar_set_final_state(A, 3, m, sp, 0.13957) != PWA_SUCCESS) return 7;
     if (pwa_isobar_add_wave(A, &w) != PWA_SUCCESS) return 8;
-    if (pwa_isobar_nmb_sym_terms(A, &terms) != PWA_SUCCESS || terms != 2) return 9;
+    if (pwa_isobar_nmb_sym_terms(A, 0, &terms) != PWA_SUCCESS || terms != 2) return 9;
     w.M = 4; /* |M| > J */
     if (pwa_isobar_add_wave(A, &w) != PWA_ERROR_INVALID_ARGUMENT) return 10;
     printf("wave refused: %s\n", pwa_last_error());

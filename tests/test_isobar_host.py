@@ -39,7 +39,8 @@ def _c_waves(ws):
                               massDependence=I.MASS_DEPENDENCES[kw["massDependence"]],
                               isobarMass=kw["isobarMass"], isobarWidth=kw["isobarWidth"],
                               isobarDaughter1=kw["isobarDaughters"][0], isobarDaughter2=kw["isobarDaughters"][1],
-                              bachelor=kw["bachelor"], bachelorFirst=int(kw.get("bachelorFirst", False)))
+                              bachelor=kw["bachelor"], bachelorFirst=int(kw.get("bachelorFirst", False)),
+                              isospin=kw.get("isospin", 2), isobarIsospin=kw.get("isobarIsospin", 0))
     return arr
 
 
@@ -49,13 +50,18 @@ def _shim_amps(lib, ws, beam, fs, masses, mb, opts, dtype=np.complex128):
     f = np.ascontiguousarray(np.transpose(fs, (0, 2, 1)))
     out = np.zeros((len(ws), n), dtype=dtype)
     m = np.ascontiguousarray(masses, dtype=np.float64)
-    sp = np.ascontiguousarray(SPECIES, dtype=np.int32)
+    sp = np.ascontiguousarray(opts.get("species", SPECIES), dtype=np.int32)
+    iso = None
+    if opts.get("isospin"):
+        I, I3, P = opts["isospin"]
+        iso = np.ascontiguousarray(np.array([I, I3, P]).T, dtype=np.int32)
     rc = lib.shim_amplitudes(_c_waves(ws), len(ws), m.ctypes.data_as(C.c_void_p), sp.ctypes.data_as(C.c_void_p),
                              C.c_double(mb), int(opts.get("reflectivity_basis", True)), int(opts.get("bose", True)),
                              int(opts.get("space_inversion", False)), int(opts.get("reflection", False)),
                              b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), C.c_uint64(n),
                              out.ctypes.data_as(C.c_void_p), int(dtype == np.complex64),
-                             int(opts.get("formalism", "helicity") == "canonical"))
+                             int(opts.get("formalism", "helicity") == "canonical"),
+                             iso.ctypes.data_as(C.c_void_p) if iso is not None else None)
     assert rc == 0
     return out
 
@@ -132,10 +138,8 @@ def test_wave_checks_and_state():
         A.amplitudes(np.zeros((1, 3)), np.zeros((3, 1, 3)))
     assert e.value.status == 2                      # no final state, no waves
     A.setFinalState(NAMES, [0.1396] * 3, 0.1396)
-    assert A.nmbSymTerms() == 2                     # the two pi- exchange
-    A.enableBoseSymmetrization(False)
-    assert A.nmbSymTerms() == 1
-    A.enableBoseSymmetrization(True)
+    with pytest.raises(N.PwaError):
+        A.nmbSymTerms(0)                            # no wave yet
     bad = [dict(kw, J=3), dict(kw, M=-2), dict(kw, P=0), dict(kw, L=16), dict(kw, bachelor=1),
            dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=7), dict(kw, isobarWidth=0.0),
            dict(kw, M=6)]
@@ -146,6 +150,10 @@ def test_wave_checks_and_state():
     assert A.nmbWaves() == 0
     A.addWave(**kw)
     assert A.nmbWaves() == 1
+    assert A.nmbSymTerms(0) == 2                    # the two pi- exchange
+    A.enableBoseSymmetrization(False)
+    assert A.nmbSymTerms(0) == 1
+    A.enableBoseSymmetrization(True)
     assert A.waveName(0) == "[1-,1++,0+]=[isobar=[pi+[1,0]pi-][0,1]pi-]"
     with pytest.raises(N.PwaError):
         A.setFinalState(["pi-", "pi+", "pi-"], [0.1396, 0.1396, 0.14], 0.1396)   # identical, unequal masses
@@ -206,3 +214,37 @@ def test_three_pion_wave_set(shim):
     par = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, SPECIES, space_inversion=True)
     for k, (w, _) in enumerate(ws):
         assert np.abs(par[k] + w["P"] * ref[k]).max() < 1e-10 * np.abs(ref[k]).max()
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+@pytest.mark.parametrize("formalism", ["helicity", "canonical"])
+def test_kernel_arithmetic_isospin_symmetrisation(shim, dtype, formalism):
+    """pi- pi0 pi0 with isospin symmetrisation (isobarDecayTopology.cc:505-630)
+    combined with the Bose terms of the two pi0."""
+    from isobar_cases import NEUTRAL_ISOSPIN, NEUTRAL_SPECIES, neutral_events, neutral_waves
+    ws = neutral_waves()
+    beam, fs, masses, mb = neutral_events(1000, seed=10)
+    opts = {"isospin": NEUTRAL_ISOSPIN, "formalism": formalism}
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, NEUTRAL_SPECIES, **opts)
+    got = _shim_amps(shim, ws, beam, fs, masses, mb, dict(opts, species=NEUTRAL_SPECIES), dtype)
+    tol = TOL if dtype == np.complex128 else TOL32
+    assert np.all(rel_err(ref, got.astype(np.complex128)) < tolerances(ws, tol))
+
+
+def test_isospin_api():
+    from isobar_cases import NEUTRAL_NAMES, NEUTRAL_MASSES, neutral_waves
+    A = I.isobarHelicityAmplitudes()
+    A.setFinalState(NEUTRAL_NAMES, NEUTRAL_MASSES, 0.1396)        # pion isospins filled in
+    for _, kw in neutral_waves():
+        A.addWave(**kw)
+    assert not A.isospinSymmetrization()
+    assert [A.nmbSymTerms(k) for k in range(5)] == [2] * 5          # Bose: the two pi0
+    A.enableIsospinSymmetrization(True)
+    assert [A.nmbSymTerms(k) for k in range(5)] == [4, 4, 2, 2, 4]  # isospin x Bose terms
+    B = I.isobarHelicityAmplitudes()
+    B.setFinalState(["a", "b", "c"], [0.1, 0.2, 0.3], 0.1)           # no isospins known
+    with pytest.raises(N.PwaError) as e:
+        B.enableIsospinSymmetrization(True)
+    assert e.value.status == 2
+    with pytest.raises(N.PwaError):
+        B.setFinalState(["a", "b", "c"], [0.1, 0.2, 0.3], 0.1, isospins=[(1, 3, 1)] * 3)   # |2I_3| > 2I

@@ -174,3 +174,44 @@ def test_canonical_eigenvalues(sample):
             continue
         assert np.abs(Cr[k] - w["refl"] * Cn[k]).max() < 1e-10 * s
         assert np.abs(Cp[k] + w["P"] * Cn[k]).max() < 1e-10 * s
+
+
+def test_isospin_terms_hand_derived():
+    """isobarDecayTopology::getIsospinSymmetrization on two cases worked out by
+    hand: pi- pi+ pi- through rho0 pi- keeps one term (factor 1); pi- pi0 pi0
+    through rho- pi0 keeps the identity with (1 -1 1 0 | 1 -1)^2 / sqrt 2 =
+    1 / (2 sqrt 2) and the rho0 -> pi0 pi0 partner with factor 0."""
+    from isobar_cases import NEUTRAL_ISOSPIN, NEUTRAL_SPECIES, neutral_waves
+    w = O.wave(2, 1, 0, 1, 0, 2, 2, 2, 1, 0.77, 0.15, (1, 2), 0, isospin=2, isobar_isospin=2)
+    assert O.isospin_terms(w, [0, 1, 0], [2, 2, 2], [-2, 2, -2], [-1, -1, -1]) == [([0, 1, 2], 1.0)]
+    rho_minus = neutral_waves()[0][0]
+    t = O.isospin_terms(rho_minus, NEUTRAL_SPECIES, *NEUTRAL_ISOSPIN)
+    assert [p for p, _ in t] == [[0, 1, 2], [2, 1, 0]]
+    assert abs(t[0][1] - 0.5 / math.sqrt(2)) < 1e-15 and t[1][1] == 0.0
+    # the wave keyed rho0 pi-: the rho0 -> pi0 pi0 term vanishes, a rho- pi0 term appears
+    t = O.isospin_terms(neutral_waves()[4][0], NEUTRAL_SPECIES, *NEUTRAL_ISOSPIN)
+    assert t[0] == ([0, 1, 2], 0.0) and t[1][0] == [1, 0, 2] and abs(t[1][1] - 0.5 / math.sqrt(2)) < 1e-15
+
+
+def test_isospin_symmetrised_amplitudes():
+    """for rho- pi0 the isospin-symmetrised amplitude is the Bose-symmetrised
+    one times +-1 / (2 sqrt 2) (the sign of the X vertex's isospin coupling
+    follows the daughters' order); the f0 and f2 waves (isospin 0 to
+    pi0 pi0) keep one isospin term; the amplitudes stay reflectivity and
+    parity eigenstates."""
+    from isobar_cases import NEUTRAL_ISOSPIN, NEUTRAL_SPECIES, neutral_events, neutral_waves
+    W = [w for w, _ in neutral_waves()]
+    beam, fs, masses, mb = neutral_events(400, seed=9)
+    A0 = O.amplitudes(W, beam, fs, masses, mb, NEUTRAL_SPECIES)
+    A1 = O.amplitudes(W, beam, fs, masses, mb, NEUTRAL_SPECIES, isospin=NEUTRAL_ISOSPIN)
+    for k, sign in ((0, +1), (1, -1)):
+        assert np.abs(A1[k] - sign * A0[k] / (2 * math.sqrt(2))).max() < 1e-13 * np.abs(A0[k]).max()
+    for k in (2, 3):
+        assert np.abs(A1[k] - A0[k]).max() < 1e-13 * np.abs(A0[k]).max()
+    Ar = O.amplitudes(W, beam, fs, masses, mb, NEUTRAL_SPECIES, isospin=NEUTRAL_ISOSPIN, reflection=True)
+    Ap = O.amplitudes(W, beam, fs, masses, mb, NEUTRAL_SPECIES, isospin=NEUTRAL_ISOSPIN, space_inversion=True)
+    for k, w in enumerate(W):
+        s = np.abs(A1[k]).max()
+        assert s > 0
+        assert np.abs(Ar[k] - w["refl"] * A1[k]).max() < 1e-10 * s
+        assert np.abs(Ap[k] + w["P"] * A1[k]).max() < 1e-10 * s
