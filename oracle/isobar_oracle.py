@@ -26,6 +26,9 @@ It follows the reference step by step, vectorised over events with numpy:
   (decayAmplitude/isobarCanonicalAmplitude.cc:64-190): the isobar's rest
   frame by a boost alone, sqrt(4 pi) (s1 m1 s2 m2 | S mS) F_L(q) * sum over
   mL of the (reflectivity-combined) (L mL S mS | J M) Y_L^mL(theta, phi).
+* symmetrisation terms: slot i takes the momentum of particle p[i] with slot
+  i's own mass (decayTopology::revertMomenta, particle::setMomentum), and the
+  frames are built per term.
 * Bose symmetrisation: sum over the permutations of identical final-state
   particles with factor 1/sqrt(prod n_k!) (isobarDecayTopology.cc:638-670,
   isobarAmplitude.cc:98-111); isospin symmetrisation over permutations of
