@@ -167,6 +167,16 @@ int pwa_likelihood_use_normalized_amps(pwa_likelihood* L, int flag);
 /* setPriorType / setCauchyWidth (pwaLikelihood.h:212-215) */
 int pwa_likelihood_set_prior_type(pwa_likelihood* L, int priorType);
 int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double width);
+/* normalizedAmpsUsed, priorType, cauchyWidth (pwaLikelihood.h:216-224); any
+ * output may be NULL */
+int pwa_likelihood_options(const pwa_likelihood* L, int* useNormalizedAmps, int* priorType, double* cauchyWidth);
+/* dLcache (pwaLikelihood.h:200): grad [P] of the last FdF / Gradient call
+ * (PWA_ERROR_INVALID_STATE before one) */
+int pwa_likelihood_deriv_cache(const pwa_likelihood* L, double* grad);
+/* clear (pwaLikelihood.cc:1670-1674): releases the device amplitude store;
+ * evaluation is refused until the amplitudes are added and finishInit is
+ * called again */
+int pwa_likelihood_clear(pwa_likelihood* L);
 /* No reference counterpart: event-sharded evaluation across processes (one
  * likelihood per process over a contiguous share of the data events).  Only
  * the root shard adds the normalisation term (with nEvt = totalEvents when

@@ -154,6 +154,9 @@ SIGNATURES = {
     "pwa_likelihood_hessian": (i, [vp, pd, pd]),
     "pwa_likelihood_covariance_matrix": (i, [vp, pd, pd]),
     "pwa_likelihood_hessian_eigenvectors": (i, [vp, pd, pd, pd, C.POINTER(u32)]),
+    "pwa_likelihood_options": (i, [vp, C.POINTER(i), C.POINTER(i), pd]),
+    "pwa_likelihood_deriv_cache": (i, [vp, pd]),
+    "pwa_likelihood_clear": (i, [vp]),
     "pwa_isobar_create": (i, [pvp]),
     "pwa_isobar_destroy": (i, [vp]),
     "pwa_isobar_set_final_state": (i, [vp, u32, pd, C.POINTER(i32), C.c_double]),

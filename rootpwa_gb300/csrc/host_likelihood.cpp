@@ -409,6 +409,47 @@ int pwa_likelihood_set_cauchy_width(pwa_likelihood* L, double w)
 	return kOk;
 }
 
+int pwa_likelihood_options(const pwa_likelihood* L, int* useNormalizedAmps, int* priorType, double* cauchyWidth)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (useNormalizedAmps)
+		*useNormalizedAmps = L->useNormalizedAmps ? 1 : 0;
+	if (priorType)
+		*priorType = L->priorType;
+	if (cauchyWidth)
+		*cauchyWidth = L->cauchyWidth;
+	return kOk;
+}
+
+int pwa_likelihood_deriv_cache(const pwa_likelihood* L, double* grad)
+{
+	if (!L || !grad)
+		return setError(kErrArg, "null argument");
+	if (!L->cacheValid)
+		return setError(kErrState, "no gradient evaluated since the last change");
+	std::copy(L->derivCache.begin(), L->derivCache.end(), grad);
+	return kOk;
+}
+
+// clear (pwaLikelihood.cc:1670-1674) releases the decay amplitudes; here the
+// device amplitude store.  Evaluation is refused until the amplitudes are
+// added and finishInit is called again.
+int pwa_likelihood_clear(pwa_likelihood* L)
+{
+	if (!L)
+		return setError(kErrArg, "null likelihood");
+	if (L->stream)
+		cudaStreamSynchronize(L->stream);
+	L->amps.release();
+	L->ampTmp.release();
+	for (int e = 0; e < 2; ++e)
+		std::fill(L->added[e].begin(), L->added[e].end(), 0);
+	L->finished = false;
+	L->cacheValid = false;
+	return kOk;
+}
+
 int pwa_likelihood_set_otf_binning(pwa_likelihood* L, uint32_t nVars, const double* lower, const double* upper,
                                    const double* const* binVars, uint64_t nFileEvents, int memory)
 {

@@ -282,6 +282,45 @@ class pwaLikelihood:
     def setCauchyWidth(self, width):
         N.call("pwa_likelihood_set_cauchy_width", self._h, float(width))
 
+    def _options(self):
+        u, p, w = C.c_int(), C.c_int(), C.c_double()
+        N.call("pwa_likelihood_options", self._h, C.byref(u), C.byref(p), C.byref(w))
+        return bool(u.value), p.value, w.value
+
+    def normalizedAmpsUsed(self):
+        return self._options()[0]
+
+    def priorType(self):
+        return self._options()[1]
+
+    def cauchyWidth(self):
+        return self._options()[2]
+
+    def enableCuda(self, flag=True):
+        """enableCuda (pwaLikelihood.h:212): every evaluation runs on the GPU;
+        there is no CPU path to switch to."""
+        if not flag:
+            raise N.PwaError(7, "the GB300 engine has no CPU evaluation path")
+
+    def cudaEnabled(self):
+        return True
+
+    def dLcache(self, i):
+        """dLcache (pwaLikelihood.h:200): component i of the gradient of the
+        last FdF / Gradient call."""
+        g = np.zeros(self.nmbPars())
+        N.call("pwa_likelihood_deriv_cache", self._h, _pd(g))
+        return float(g[i])
+
+    def clear(self):
+        """clear (pwaLikelihood.cc:1670-1674): releases the amplitude store."""
+        N.call("pwa_likelihood_clear", self._h)
+
+    def Clone(self):
+        """Clone (pwaLikelihood.h:160): the handle owns device memory; build a
+        second likelihood instead."""
+        raise N.PwaError(7, "pwaLikelihood handles cannot be cloned; create a new one")
+
     @staticmethod
     def setQuiet(flag=True):
         """The engine prints nothing; kept for call compatibility."""
@@ -499,6 +538,18 @@ class pwaLikelihood:
         t, fn, nm = C.c_double(), C.c_double(), C.c_double()
         N.call("pwa_likelihood_func_call_info", self._h, int(call), C.byref(n), C.byref(t), C.byref(fn), C.byref(nm))
         return {"nmbCalls": n.value, "totalTime": t.value, "funcTime": fn.value, "normTime": nm.value}
+
+    def ncalls(self, func=N.CALL_FDF):
+        """ncalls (pwaLikelihood.h:199)."""
+        return self.funcCallInfo(func)["nmbCalls"]
+
+    def Ltime(self, func=N.CALL_FDF):
+        """Ltime (pwaLikelihood.h:201): seconds in the event kernels."""
+        return self.funcCallInfo(func)["funcTime"]
+
+    def Ntime(self, func=N.CALL_FDF):
+        """Ntime (pwaLikelihood.h:203): seconds in the normalisation term."""
+        return self.funcCallInfo(func)["normTime"]
 
     def resetFuncCallInfo(self):
         N.call("pwa_likelihood_reset_func_call_info", self._h)

@@ -229,3 +229,26 @@ def test_device_work_fails_loudly_without_gpu():
     J = R.ampIntegralMatrix()
     with pytest.raises(R.PwaError):
         J.integrate(w["names"], w["mc"])
+
+
+def test_reference_accessors_without_gpu():
+    """normalizedAmpsUsed / priorType / cauchyWidth, enableCuda / cudaEnabled,
+    dLcache before any evaluation, clear and Clone (pwaLikelihood.h:160-224,
+    pwaLikelihood.cc:1670-1674)."""
+    L, O, names = _layout_pair(2, 3, 1)
+    assert L.normalizedAmpsUsed() and L.priorType() == 0 and L.cauchyWidth() == 0.5
+    L.useNormalizedAmps(False)
+    L.setPriorType(1)
+    L.setCauchyWidth(0.25)
+    assert (L.normalizedAmpsUsed(), L.priorType(), L.cauchyWidth()) == (False, 1, 0.25)
+    assert L.cudaEnabled()
+    L.enableCuda(True)
+    with pytest.raises(R.PwaError):
+        L.enableCuda(False)
+    with pytest.raises(R.PwaError) as e:
+        L.dLcache(0)
+    assert e.value.status == 2
+    assert L.ncalls() == 0 and L.Ltime() == 0.0 and L.Ntime() == 0.0
+    L.clear()
+    with pytest.raises(R.PwaError):
+        L.Clone()

@@ -343,3 +343,18 @@ def test_store_block_64_matches_oracle():
     check_point(O, G, w["par"])
     with pytest.raises(R.PwaError):
         G.setStoreBlock(128)  # fixed by the first addAmplitude
+
+
+def test_dlcache_and_clear():
+    """dLcache (pwaLikelihood.h:200) holds the last gradient; clear
+    (pwaLikelihood.cc:1670-1674) releases the amplitude store and evaluation
+    is refused afterwards."""
+    w = synth.make_workload("compass15", seed=3, n_data=5000, n_mc=20000)
+    O, G = pair(w)
+    f, g = G.FdF(w["par"])
+    assert [G.dLcache(i) for i in range(G.nmbPars())] == list(g)
+    assert G.ncalls() >= 1
+    G.clear()
+    with pytest.raises(R.PwaError) as e:
+        G.FdF(w["par"])
+    assert e.value.status == 2
