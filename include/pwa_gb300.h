@@ -123,6 +123,14 @@ int pwa_integral_set_nmb_events(pwa_integral* I, uint64_t n);
 /* waveIndex / waveName (ampIntegralMatrix.cc:195-216) */
 int pwa_integral_wave_name(const pwa_integral* I, uint32_t i, char* buf, uint32_t bufLen);
 int pwa_integral_wave_index(const pwa_integral* I, const char* name, uint32_t* index);
+/* containsWave (ampIntegralMatrix.cc:188-191) */
+int pwa_integral_contains_wave(const pwa_integral* I, const char* name, int* contains);
+/* hasIdenticalWaveSet (ampIntegralMatrix.cc:633-646) and operator ==
+ * (ampIntegralMatrix.h:179-195: same waves, same event count, equal raw sums
+ * matched by wave name); either output may be NULL */
+int pwa_integral_compare(const pwa_integral* I, const pwa_integral* other, int* identicalWaveSet, int* equal);
+/* clear (ampIntegralMatrix.cc:93-103) */
+int pwa_integral_clear(pwa_integral* I);
 /* operator+= / -= / *= / /= (ampIntegralMatrix.cc:126-185) */
 int pwa_integral_add(pwa_integral* I, const pwa_integral* other);
 int pwa_integral_subtract(pwa_integral* I, const pwa_integral* other);

@@ -157,6 +157,9 @@ SIGNATURES = {
     "pwa_likelihood_options": (i, [vp, C.POINTER(i), C.POINTER(i), pd]),
     "pwa_likelihood_deriv_cache": (i, [vp, pd]),
     "pwa_likelihood_clear": (i, [vp]),
+    "pwa_integral_contains_wave": (i, [vp, cc, C.POINTER(i)]),
+    "pwa_integral_compare": (i, [vp, vp, C.POINTER(i), C.POINTER(i)]),
+    "pwa_integral_clear": (i, [vp]),
     "pwa_isobar_create": (i, [pvp]),
     "pwa_isobar_destroy": (i, [vp]),
     "pwa_isobar_set_final_state": (i, [vp, u32, pd, C.POINTER(i32), C.c_double]),

@@ -359,6 +359,48 @@ int pwa_integral_wave_index(const pwa_integral* I, const char* name, uint32_t* i
 	return kOk;
 }
 
+// containsWave (ampIntegralMatrix.cc:188-191)
+int pwa_integral_contains_wave(const pwa_integral* I, const char* name, int* contains)
+{
+	if (!I || !name || !contains)
+		return setError(kErrArg, "null argument");
+	*contains = I->index(name) >= 0 ? 1 : 0;
+	return kOk;
+}
+
+// hasIdenticalWaveSet (ampIntegralMatrix.cc:633-646) and operator ==
+// (ampIntegralMatrix.h:179-195): same wave set, same event count and equal
+// raw sums element by element, matched by wave name
+int pwa_integral_compare(const pwa_integral* I, const pwa_integral* o, int* identicalWaveSet, int* equal)
+{
+	if (!I || !o)
+		return setError(kErrArg, "null argument");
+	const bool same = I->sameWaveSet(*o) && o->sameWaveSet(*I);
+	bool eq = same && I->nEvents == o->nEvents;
+	for (uint32_t i = 0; eq && i < I->nWaves; ++i) {
+		const int oi = o->index(I->names[i]);
+		for (uint32_t j = 0; eq && j < I->nWaves; ++j)
+			eq = I->sums[(size_t)i * I->nWaves + j] == o->sums[(size_t)oi * o->nWaves + o->index(I->names[j])];
+	}
+	if (identicalWaveSet)
+		*identicalWaveSet = same ? 1 : 0;
+	if (equal)
+		*equal = eq ? 1 : 0;
+	return kOk;
+}
+
+// clear (ampIntegralMatrix.cc:93-103): no waves, no events
+int pwa_integral_clear(pwa_integral* I)
+{
+	if (!I)
+		return setError(kErrArg, "null argument");
+	I->nWaves = 0;
+	I->nEvents = 0;
+	I->names.clear();
+	I->sums.clear();
+	return kOk;
+}
+
 static int integralCombine(pwa_integral* I, const pwa_integral* o, double sign)
 {
 	if (!I || !o)

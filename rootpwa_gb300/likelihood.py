@@ -139,6 +139,36 @@ class ampIntegralMatrix:
     def waveNames(self):
         return [self.waveName(i) for i in range(self.nmbWaves())]
 
+    def containsWave(self, name):
+        """containsWave (ampIntegralMatrix.cc:188-191)."""
+        c = C.c_int()
+        N.call("pwa_integral_contains_wave", self._h, name.encode(), C.byref(c))
+        return bool(c.value)
+
+    def hasIdenticalWaveSet(self, other):
+        """hasIdenticalWaveSet (ampIntegralMatrix.cc:633-646)."""
+        same = C.c_int()
+        N.call("pwa_integral_compare", self._h, other._h, C.byref(same), None)
+        return bool(same.value)
+
+    def __eq__(self, other):
+        """operator == (ampIntegralMatrix.h:179-195)."""
+        if not isinstance(other, ampIntegralMatrix):
+            return NotImplemented
+        eq = C.c_int()
+        N.call("pwa_integral_compare", self._h, other._h, None, C.byref(eq))
+        return bool(eq.value)
+
+    def __ne__(self, other):
+        r = self.__eq__(other)
+        return r if r is NotImplemented else not r
+
+    __hash__ = None
+
+    def clear(self):
+        """clear (ampIntegralMatrix.cc:93-103)."""
+        N.call("pwa_integral_clear", self._h)
+
     def waveIndex(self, name):
         k = C.c_uint32()
         N.call("pwa_integral_wave_index", self._h, name.encode(), C.byref(k))

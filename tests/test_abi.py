@@ -252,3 +252,27 @@ def test_reference_accessors_without_gpu():
     L.clear()
     with pytest.raises(R.PwaError):
         L.Clone()
+
+
+def test_integral_comparison_and_clear():
+    """containsWave, hasIdenticalWaveSet, operator == and clear
+    (ampIntegralMatrix.cc:93-103, :188-191, :633-646; .h:179-195)."""
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((3, 20)) + 1j * rng.standard_normal((3, 20))
+
+    def build(names, amps):
+        I = R.ampIntegralMatrix()
+        I.setWaveNames(names)
+        for e in range(amps.shape[1]):
+            I.addEvent(amps[:, e])
+        return I
+    I1 = build(["a", "b", "c"], A)
+    I2 = build(["c", "a", "b"], A[[2, 0, 1]])          # same sums, other wave order
+    assert I1.containsWave("b") and not I1.containsWave("d")
+    assert I1.hasIdenticalWaveSet(I2) and I1 == I2 and not (I1 != I2)
+    I3 = build(["a", "b", "c"], A[:, :19])
+    assert I1.hasIdenticalWaveSet(I3) and I1 != I3
+    I4 = build(["a", "b", "x"], A)
+    assert not I1.hasIdenticalWaveSet(I4) and I1 != I4
+    I1.clear()
+    assert I1.nmbWaves() == 0 and I1.nmbEvents() == 0 and not I1.containsWave("a")
