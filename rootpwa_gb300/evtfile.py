@@ -14,6 +14,8 @@ common order first, convertEvtToTree.py:39-55).
     amp.setFinalState(ev["fs_names"], ev["fs_masses"], ev["beam_mass"])
     A = amp.amplitudes(ev["beam"], ev["fs"])
 """
+import re
+
 import numpy as np
 
 # GEANT3 particle codes: name, charge, mass (GeV/c^2, PDG)
@@ -27,6 +29,10 @@ GEANT_PARTICLES = {
 }
 
 
+# anything but numbers and whitespace: let the slow path raise a clear error
+_BAD = re.compile(r"[^0-9eE+\-.\s]")
+
+
 def _particle(gid):
     if gid not in GEANT_PARTICLES:
         raise ValueError("unknown GEANT particle code %d" % gid)
@@ -38,16 +44,20 @@ def readEvtFile(path):
     momenta, the GEANT codes, names, charges and masses of the beam and the
     final-state particles."""
     with open(path) as f:
-        tokens = f.read().split()
-    if not tokens:
+        text = f.read()
+    # numbers straight into one float array (a token list would cost ~60
+    # bytes per number: gigabytes for millions of events)
+    values = np.array(text.split(), dtype=np.float64) if _BAD.search(text) else \
+        np.fromstring(text, dtype=np.float64, sep=" ")
+    if values.size == 0:
         raise ValueError("%s: no events" % path)
-    n = int(tokens[0])
-    if n < 2:
+    n = int(values[0])
+    if n < 2 or n != values[0]:
         raise ValueError("%s: an event needs a beam and at least one final-state particle" % path)
     width = 1 + 6 * n
-    if len(tokens) % width:
+    if values.size % width:
         raise ValueError("%s: truncated file or events with different particle counts" % path)
-    rows = np.array(tokens, dtype=np.float64).reshape(-1, width)
+    rows = values.reshape(-1, width)
     if np.any(rows[:, 0] != n):
         raise ValueError("%s: events with different particle counts" % path)
     parts = rows[:, 1:].reshape(rows.shape[0], n, 6)

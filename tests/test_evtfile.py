@@ -41,3 +41,21 @@ def test_malformed_files_are_refused(tmp_path, text, why):
     p.write_text(text)
     with pytest.raises(ValueError, match=why):
         evtfile.readEvtFile(p)
+
+
+def test_large_file_is_read_quickly(tmp_path):
+    import time
+    beam, fs, masses, mb = synth.three_pion_events(100_000, seed=5)
+    p = tmp_path / "big.evt"
+    evtfile.writeEvtFile(p, 9, beam, [9, 8, 9], fs)
+    t = time.perf_counter()
+    ev = evtfile.readEvtFile(p)
+    assert time.perf_counter() - t < 10.0
+    assert np.array_equal(ev["fs"], fs)
+
+
+def test_non_numeric_content_is_refused(tmp_path):
+    p = tmp_path / "text.evt"
+    p.write_text("4\n9 -1 0.1 0 190 190\nfoo\n")
+    with pytest.raises(ValueError):
+        evtfile.readEvtFile(p)
