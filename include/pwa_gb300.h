@@ -458,17 +458,21 @@ int pwa_mlp_train(pwa_mlp* net, const float* X, const float* T, uint64_t nSample
 /* reference.  FP64 on the GPU, one thread per event.                        */
 /* ------------------------------------------------------------------------ */
 typedef struct pwa_isobar pwa_isobar;
-/* massDependence (decayAmplitude/massDependence.cc:169-445): flatMassDependence,
+/* massDependence (decayAmplitude/massDependence.cc:169-625): flatMassDependence,
  * relativisticBreitWigner, constWidthBreitWigner, rhoBreitWigner,
- * f0980BreitWigner, f0980FlatteBesII (fixed BES II parameters; mass and width
- * unused) */
+ * f0980BreitWigner, f0980FlatteBesII (fixed BES II parameters),
+ * piPiSWaveAuMorganPenningtonM / Ves / Kachaev (fixed AMP parameters; for the
+ * fixed-parameter forms mass and width are unused) */
 enum pwa_mass_dependence {
 	PWA_MASSDEP_FLAT = 0,
 	PWA_MASSDEP_RELATIVISTIC_BW = 1,
 	PWA_MASSDEP_CONST_WIDTH_BW = 2,
 	PWA_MASSDEP_RHO_BW = 3,
 	PWA_MASSDEP_F0980_BW = 4,
-	PWA_MASSDEP_F0980_FLATTE = 5
+	PWA_MASSDEP_F0980_FLATTE = 5,
+	PWA_MASSDEP_PIPI_S_AMP_M = 6,
+	PWA_MASSDEP_PIPI_S_AMP_VES = 7,
+	PWA_MASSDEP_PIPI_S_AMP_KACHAEV = 8
 };
 /* one wave: the content of a key file of a three-body decay
  * (decayAmplitude/waveDescription.cc:880-932) */

@@ -39,8 +39,9 @@ It follows the reference step by step, vectorised over events with numpy:
 * mass dependences: flat, relativistic Breit-Wigner with the PWA2000 rule
   q0 = sqrt|q0^2| (massDependence.cc:254-296, utilities/physUtils.hpp:283-300),
   constant-width Breit-Wigner (massDependence.cc:300-320), the rho and
-  f0(980) Breit-Wigners (:324-390) and the f0(980) Flatte form with the BES II
-  parameters (:395-445).
+  f0(980) Breit-Wigners (:324-390), the f0(980) Flatte form with the BES II
+  parameters (:395-445) and the pi pi S-wave of Au, Morgan and Pennington
+  (M, VES and Kachaev variants, :449-625).
 
 The building blocks are restated from the published formulas, not from the
 reference's arrangement of them: Clebsch-Gordan coefficients by Racah's
@@ -64,8 +65,20 @@ from itertools import permutations
 import numpy as np
 
 PR_DEFAULT = 0.1973        # GeV/c, 1 fm interaction radius
-MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW, MASSDEP_RHO_BW, MASSDEP_F0980_BW, MASSDEP_F0980_FLATTE = range(6)
+(MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW, MASSDEP_RHO_BW, MASSDEP_F0980_BW, MASSDEP_F0980_FLATTE,
+ MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV) = range(9)
 M_PI_CHARGED, M_K_CHARGED = 0.13957039, 0.493677   # GeV/c^2 (the particle table's pi+ and K+)
+M_PI_NEUTRAL, M_K_NEUTRAL = 0.1349768, 0.497611
+
+# Au, Morgan, Pennington, Phys. Rev. D 35 (1987) 1633, Table 1, M solution, as
+# used by piPiSWaveAuMorganPenningtonImpl (massDependence.cc:449-500): pole
+# residues a_i (2 x 2), pole positions s_i, background polynomial c_n (2 x 2)
+AMP_F = np.array([0.1968, -0.0154])
+AMP_A = [np.array([[0.1131, 0.0150], [0.0150, -0.3216]]), np.outer(AMP_F, AMP_F)]
+AMP_C = [np.array([[0.0337, -0.2826], [-0.2826, 0.3010]]), np.array([[-0.3185, 0.0918], [0.0918, -0.5140]]),
+         np.array([[-0.0942, 0.1669], [0.1669, 0.1176]]), np.array([[-0.5927, -0.2082], [-0.2082, 0.5204]]),
+         np.array([[0.1957, -0.1386], [-0.1386, -0.3977]])]
+AMP_SP = [-0.0074, 0.9828]
 
 
 # -- spin algebra ---------------------------------------------------------------
@@ -216,6 +229,58 @@ def f0980_flatte(M):
     rho_pi, rho_k = 2 * kc(M_PI_CHARGED) / M, 2 * kc(M_K_CHARGED) / M
     denom = (0.965 ** 2 - M * M) + 0j - 1j * 0.165 * (rho_pi + 4.21 * rho_k)
     return 1.0 / denom
+
+
+def _q_complex(M, m):
+    """breakupMomentumComplex (utilities/physUtils.hpp:108-120) for equal masses."""
+    q2 = breakup_momentum_squared(M, m, m)
+    q = np.sqrt(np.abs(q2))
+    return np.where(q2 < 0, 1j * q, q + 0j)
+
+
+def pipi_s_wave(M, variant):
+    """piPiSWaveAuMorganPennington{M,Ves,Kachaev}::amp (massDependence.cc:
+    505-625): M(s) = sum_i a_i / (s - s_i) + sum_n c_n (s / 4 m_K^2 - 1)^n with
+    the off-diagonal elements set to zero, T = (M - i rho)^-1, amp = T_00;
+    rho from the charged and neutral pi pi (K K) breakup momenta, or the
+    charged ones only on the VES sheet, which also subtracts an f0(980)
+    Breit-Wigner; the Kachaev variant drops c_4 (diagonal), the off-diagonal
+    a_0 and a_1."""
+    a = [x.copy() for x in AMP_A]
+    c = [x.copy() for x in AMP_C]
+    if variant == "kachaev":
+        c[4][0, 0] = c[4][1, 1] = 0.0
+        a[0][0, 1] = a[0][1, 0] = 0.0
+        a[1][:] = 0.0
+    M = np.asarray(M, dtype=np.float64)
+    out = np.zeros(M.shape, dtype=np.complex128)
+    mk = (M_K_CHARGED + M_K_NEUTRAL) / 2
+    for e, m in np.ndenumerate(M):
+        s = m * m
+        if abs(s - AMP_SP[1]) < 1e-6:
+            m += 1e-6
+            s = m * m
+        rho = np.zeros((2, 2), dtype=np.complex128)
+        if variant == "ves":
+            rho[0, 0] = 2 * _q_complex(m, M_PI_CHARGED) / m
+            rho[1, 1] = 2 * _q_complex(m, mk) / m
+        else:
+            rho[0, 0] = (2 * _q_complex(m, M_PI_CHARGED) / m + 2 * _q_complex(m, M_PI_NEUTRAL) / m) / 2
+            rho[1, 1] = (2 * _q_complex(m, M_K_CHARGED) / m + 2 * _q_complex(m, M_K_NEUTRAL) / m) / 2
+        scale = s / (4 * mk * mk) - 1
+        Mm = sum(a[i] / (s - AMP_SP[i]) for i in range(2)) + sum(c[n] * scale ** n for n in range(5))
+        Mm = Mm.astype(np.complex128)
+        Mm[0, 1] = Mm[1, 0] = 0
+        amp = np.linalg.inv(Mm - 1j * rho)[0, 0]
+        if variant == "ves" and m > 2 * M_PI_CHARGED:
+            f0m, f0w, coupling = 0.9837, 0.0376, -0.3743 + 0.3197j
+            q = math.sqrt(breakup_momentum_squared(m, M_PI_CHARGED, M_PI_CHARGED))
+            q0 = math.sqrt(breakup_momentum_squared(f0m, M_PI_CHARGED, M_PI_CHARGED))
+            C = f0m * f0w * q / q0
+            A, B = C * m / q, f0m * f0m - m * m
+            amp = amp - coupling * (A / (B * B + C * C)) * (B + 1j * C)
+        out[e] = amp
+    return out
 
 
 def const_width_bw(M, M0, G0):
@@ -457,6 +522,8 @@ def _sym_term(w, beam, fs, masses, opts):
         bw = f0980_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"])
     elif md == MASSDEP_F0980_FLATTE:
         bw = f0980_flatte(mI)
+    elif md in (MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV):
+        bw = pipi_s_wave(mI, {MASSDEP_PIPIS_M: "m", MASSDEP_PIPIS_VES: "ves", MASSDEP_PIPIS_KACHAEV: "kachaev"}[md])
     else:
         bw = np.ones_like(mI, dtype=np.complex128)
     amp = np.zeros(len(phi), dtype=np.complex128)

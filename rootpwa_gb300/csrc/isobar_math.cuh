@@ -41,12 +41,34 @@ constexpr int kMaxL = 14;         // 2L: barrier factors up to L = 7
 constexpr int kMaxPerms = 6;      // Bose terms of three particles
 constexpr double kPr = 0.1973;    // GeV/c, 1 fm interaction radius
 
-enum { kMassFlat = 0, kMassRelBw = 1, kMassConstBw = 2, kMassRhoBw = 3, kMassF0980Bw = 4, kMassF0980Flatte = 5 };
+enum {
+	kMassFlat = 0,
+	kMassRelBw = 1,
+	kMassConstBw = 2,
+	kMassRhoBw = 3,
+	kMassF0980Bw = 4,
+	kMassF0980Flatte = 5,
+	kMassPiPiSM = 6,        // pi pi S-wave, Au-Morgan-Pennington M solution
+	kMassPiPiSVes = 7,      // ... VES sheet with the f0(980) subtracted
+	kMassPiPiSKachaev = 8   // ... Kachaev's reduced parameter set
+};
 
 // f0(980) Flatte form with the BES II parameters (massDependence.cc:395-445)
 // and the charged pion and kaon masses of the particle table
 constexpr double kFlatteM0 = 0.965, kFlatteG1 = 0.165, kFlatteG2G1 = 4.21;
 constexpr double kMassPiCharged = 0.13957039, kMassKCharged = 0.493677;
+constexpr double kMassPiNeutral = 0.1349768, kMassKNeutral = 0.497611;
+
+// Au, Morgan, Pennington, Phys. Rev. D 35 (1987) 1633, Table 1, M solution
+// (the parameters of massDependence.cc:449-500).  The amplitude is T_00 of
+// (M - i rho)^-1 with M's off-diagonal elements set to zero, so only the
+// (0, 0) elements enter: residues of the poles at s_0, s_1 and the
+// background polynomial in (s / 4 m_K^2 - 1).
+constexpr double kAmpA0 = 0.1131, kAmpF1 = 0.1968;
+constexpr double kAmpS0 = -0.0074, kAmpS1 = 0.9828;
+constexpr double kAmpC0 = 0.0337, kAmpC1 = -0.3185, kAmpC2 = -0.0942, kAmpC3 = -0.5927, kAmpC4 = 0.1957;
+// VES: f0(980) Breit-Wigner subtracted with this coupling (massDependence.cc:578-604)
+constexpr double kVesF0Mass = 0.9837, kVesF0Width = 0.0376, kVesCouplingRe = -0.3743, kVesCouplingIm = 0.3197;
 
 // d^j_{m n}(theta) = sum over terms of coef * cos(theta/2)^a * sin(theta/2)^b
 struct DTerm {
@@ -222,6 +244,53 @@ PWA_HD T breakup2(T M, T m1, T m2)
 	return (M - s) * (M + s) * (M - d) * (M + d) / (T(4) * M * M);
 }
 
+// 2 k / m with the complex breakup momentum k of two particles of mass m1
+// (imaginary below threshold, physUtils.hpp:108-120)
+PWA_HD C2T<double> rhoOf(double m, double m1)
+{
+	const double q2 = breakup2<double>(m, m1, m1);
+	const double r = 2.0 * sqrt(q2 < 0 ? -q2 : q2) / m;
+	return q2 < 0 ? C2T<double>{0.0, r} : C2T<double>{r, 0.0};
+}
+
+// piPiSWaveAuMorganPennington{M,Ves,Kachaev}::amp (massDependence.cc:505-625),
+// FP64 (the poles cancel near s_1)
+PWA_HD C2T<double> piPiSWave(double m, int variant)
+{
+	double s = m * m;
+	if (fabs(s - kAmpS1) < 1e-6) {
+		m += 1e-6;
+		s = m * m;
+	}
+	C2T<double> rho;
+	if (variant == kMassPiPiSVes) {
+		rho = rhoOf(m, kMassPiCharged);
+	} else {
+		const C2T<double> rc = rhoOf(m, kMassPiCharged), rn = rhoOf(m, kMassPiNeutral);
+		rho = C2T<double>{0.5 * (rc.re + rn.re), 0.5 * (rc.im + rn.im)};
+	}
+	const double mk = 0.5 * (kMassKCharged + kMassKNeutral);
+	const double scale = s / (4.0 * mk * mk) - 1.0;
+	const bool kachaev = variant == kMassPiPiSKachaev;
+	double M = kAmpA0 / (s - kAmpS0) + (kachaev ? 0.0 : kAmpF1 * kAmpF1 / (s - kAmpS1));
+	const double x = scale, x2 = x * x;
+	M += kAmpC0 + kAmpC1 * x + kAmpC2 * x2 + kAmpC3 * x2 * x + (kachaev ? 0.0 : kAmpC4 * x2 * x2);
+	// 1 / (M - i rho) = 1 / ((M + Im rho) - i Re rho)
+	const double dRe = M + rho.im, dIm = -rho.re, n2 = dRe * dRe + dIm * dIm;
+	C2T<double> amp{dRe / n2, -dIm / n2};
+	if (variant == kMassPiPiSVes && m > 2.0 * kMassPiCharged) {
+		const double q = sqrt(breakup2<double>(m, kMassPiCharged, kMassPiCharged));
+		const double q0 = sqrt(breakup2<double>(kVesF0Mass, kMassPiCharged, kMassPiCharged));
+		const double C = kVesF0Mass * kVesF0Width * (q / q0);
+		const double A = C * (m / q), B = kVesF0Mass * kVesF0Mass - m * m;
+		const double f = A / (B * B + C * C);
+		const C2T<double> bw{f * B, f * C};
+		amp.re -= kVesCouplingRe * bw.re - kVesCouplingIm * bw.im;
+		amp.im -= kVesCouplingRe * bw.im + kVesCouplingIm * bw.re;
+	}
+	return amp;
+}
+
 // dm2 = m0^2 - mI^2 is formed in FP64 (it cancels near the peak, where FP32
 // would lose a narrow width's resolution); mId is the FP64 isobar mass for
 // the breakup momenta of the Flatte form, which cancel at the K K threshold
@@ -279,6 +348,10 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 		const T dIm = -T(kFlatteG1) * reRho;
 		const T n2 = dRe * dRe + dIm * dIm;
 		return C2T<T>{dRe / n2, -dIm / n2};
+	}
+	if (w.massDep >= kMassPiPiSM && w.massDep <= kMassPiPiSKachaev) {
+		const C2T<double> a = piPiSWave(mId, w.massDep);
+		return C2T<T>{T(a.re), T(a.im)};
 	}
 	return C2T<T>{T(1), T(0)};
 }

@@ -126,10 +126,9 @@ inline std::string checkWave(const pwa_isobar_wave& w, bool reflBasis)
 	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
 	if (a < 0 || b < 0 || c < 0 || a > 2 || b > 2 || c > 2 || a == b || a == c || b == c)
 		return "isobar daughters and bachelor must be three distinct final-state slots 0..2";
-	if (w.massDependence < kMassFlat || w.massDependence > kMassF0980Flatte)
+	if (w.massDependence < kMassFlat || w.massDependence > kMassPiPiSKachaev)
 		return "unknown mass dependence";
-	if (w.massDependence != kMassFlat && w.massDependence != kMassF0980Flatte &&
-	    !(w.isobarMass > 0 && w.isobarWidth > 0))
+	if (w.massDependence >= kMassRelBw && w.massDependence <= kMassF0980Bw && !(w.isobarMass > 0 && w.isobarWidth > 0))
 		return "a Breit-Wigner needs a positive mass and width";
 	return std::string();
 }

@@ -31,7 +31,8 @@ from . import _native as N
 # (2I, 2I_3, intrinsic parity) of the pions
 PION_ISOSPINS = {"pi-": (2, -2, -1), "pi0": (2, 0, -1), "pi+": (2, 2, -1)}
 MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2, "rhoBreitWigner": 3,
-                    "f0980BreitWigner": 4, "f0980FlatteBesII": 5}
+                    "f0980BreitWigner": 4, "f0980FlatteBesII": 5, "piPiSWaveAuMorganPenningtonM": 6,
+                    "piPiSWaveAuMorganPenningtonVes": 7, "piPiSWaveAuMorganPenningtonKachaev": 8}
 
 
 def _qn(x):

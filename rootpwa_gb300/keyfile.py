@@ -26,6 +26,9 @@ KEY_MASS_DEPENDENCES = {
     "constWidthBreitWigner": "constWidthBreitWigner", "rhoBreitWigner": "rhoBreitWigner",
     "f0980BreitWigner": "f0980BreitWigner", "f_0(980)": "f0980BreitWigner",
     "f0980FlatteBesII": "f0980FlatteBesII", "f_0(980)Flatte": "f0980FlatteBesII",
+    "piPiSWaveAuMorganPenningtonM": "piPiSWaveAuMorganPenningtonM",
+    "piPiSWaveAuMorganPenningtonVes": "piPiSWaveAuMorganPenningtonVes",
+    "piPiSWaveAuMorganPenningtonKachaev": "piPiSWaveAuMorganPenningtonKachaev",
 }
 
 

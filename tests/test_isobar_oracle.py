@@ -215,3 +215,19 @@ def test_isospin_symmetrised_amplitudes():
         assert s > 0
         assert np.abs(Ar[k] - w["refl"] * A1[k]).max() < 1e-10 * s
         assert np.abs(Ap[k] + w["P"] * A1[k]).max() < 1e-10 * s
+
+
+def test_pipi_s_wave_unitarity_and_f0_dip():
+    """the AMP pi pi S-wave (massDependence.cc:505-625): below the K K
+    threshold T_00 = 1 / (M_00 - i rho_00) with real M_00, so elastic
+    unitarity Im(1 / T) = -rho_00 holds exactly (rho the mean of the charged
+    and neutral pi pi phase-space factors); the M solution has the f0(980)
+    dip just below the K K threshold."""
+    m = np.linspace(0.3, 0.98, 40)
+    for variant in ("m", "kachaev"):
+        T = O.pipi_s_wave(m, variant)
+        rho = ((2 * O._q_complex(m, O.M_PI_CHARGED) / m + 2 * O._q_complex(m, O.M_PI_NEUTRAL) / m) / 2).real
+        assert np.allclose((1 / T).imag, -rho, rtol=1e-12, atol=1e-14)
+    grid = np.linspace(0.9, 1.05, 301)
+    a = np.abs(O.pipi_s_wave(grid, "m"))
+    assert 0.97 < grid[np.argmin(a)] < 1.0 and a.min() < 0.2 * a.max()

@@ -122,8 +122,8 @@ def test_refusals(files, tmp_path):
     with pytest.raises(NotImplementedError):
         keyfile.waveFromKeyFile(tmp_path / "four.key", t, ["pi-", "pi+", "pi-"])
     (tmp_path / "md.key").write_text(KEY_RHO.replace("L = 2; S = 0;", 'L = 2; S = 0; massDep : { name = '
-                                                     '"piPiSWaveAuMorganPenningtonKachaev"; };'))
-    with pytest.raises(NotImplementedError, match="piPiSWave"):
+                                                     '"KPiSGLASS"; };'))
+    with pytest.raises(NotImplementedError, match="KPiSGLASS"):
         keyfile.waveFromKeyFile(tmp_path / "md.key", t, ["pi-", "pi+", "pi-"])
     (tmp_path / "iso.key").write_text(KEY_RHO.replace('name = "rho(770)"', 'name = "rho(1450)"'))
     with pytest.raises(ValueError, match="particle table"):
