@@ -231,9 +231,10 @@ def three_pion_events(n, seed=0, beam_momentum=190.0, m_lo=0.9, m_hi=2.2, masses
     return beam, fs, np.array([m1, m2, m3]), M_PI
 
 
-# isobars of the 3pi wave sets: (name, 2J, mass, width, mass dependence)
+# isobars of the 3pi wave sets: (name, 2J, mass, width, mass dependence;
+# mass and width unused by the fixed-parameter pi pi S-wave)
 PIPI_ISOBARS = [
-    ("sigma", 0, 0.60, 0.60, "constWidthBreitWigner"),
+    ("sigma", 0, 0.0, 0.0, "piPiSWaveAuMorganPenningtonKachaev"),      # the (pi pi)_S isobar
     ("rho(770)", 2, 0.7690, 0.1509, "relativisticBreitWigner"),
     ("f0(980)", 0, 0.980, 0.070, "relativisticBreitWigner"),
     ("f2(1270)", 4, 1.2751, 0.1851, "relativisticBreitWigner"),
