@@ -458,7 +458,7 @@ int pwa_mlp_train(pwa_mlp* net, const float* X, const float* T, uint64_t nSample
 /* reference.  FP64 on the GPU, one thread per event.                        */
 /* ------------------------------------------------------------------------ */
 typedef struct pwa_isobar pwa_isobar;
-/* massDependence (decayAmplitude/massDependence.cc:169-625): flatMassDependence,
+/* massDependence (decayAmplitude/massDependence.cc:169-625): flatMassDependence, binnedMassDependence,
  * relativisticBreitWigner, constWidthBreitWigner, rhoBreitWigner,
  * f0980BreitWigner, f0980FlatteBesII (fixed BES II parameters),
  * piPiSWaveAuMorganPenningtonM / Ves / Kachaev (fixed AMP parameters; for the
@@ -472,7 +472,8 @@ enum pwa_mass_dependence {
 	PWA_MASSDEP_F0980_FLATTE = 5,
 	PWA_MASSDEP_PIPI_S_AMP_M = 6,
 	PWA_MASSDEP_PIPI_S_AMP_VES = 7,
-	PWA_MASSDEP_PIPI_S_AMP_KACHAEV = 8
+	PWA_MASSDEP_PIPI_S_AMP_KACHAEV = 8,
+	PWA_MASSDEP_BINNED = 9            /* binnedMassDependence: 1 inside [binLower, binUpper), else 0 */
 };
 /* one wave: the content of a key file of a three-body decay
  * (decayAmplitude/waveDescription.cc:880-932) */
@@ -485,6 +486,7 @@ typedef struct pwa_isobar_wave {
 	int32_t isobarDaughter1, isobarDaughter2, bachelor; /* final-state slots 0..2; isobar daughter 1 is the analyser */
 	int32_t bachelorFirst;            /* X-vertex daughter 1 (the analyser) is the bachelor rather than the isobar */
 	int32_t isospin, isobarIsospin;   /* 2I of X and of the isobar (isospin symmetrisation only) */
+	double binLower, binUpper;        /* PWA_MASSDEP_BINNED: the isobar mass bin [lower, upper) */
 } pwa_isobar_wave;
 /* isobarHelicityAmplitude (decayAmplitude/isobarHelicityAmplitude.cc:64-195)
  * or isobarCanonicalAmplitude (decayAmplitude/isobarCanonicalAmplitude.cc:64-190) */

@@ -66,7 +66,7 @@ import numpy as np
 
 PR_DEFAULT = 0.1973        # GeV/c, 1 fm interaction radius
 (MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW, MASSDEP_RHO_BW, MASSDEP_F0980_BW, MASSDEP_F0980_FLATTE,
- MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV) = range(9)
+ MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV, MASSDEP_BINNED) = range(10)
 M_PI_CHARGED, M_K_CHARGED = 0.13957039, 0.493677   # GeV/c^2 (the particle table's pi+ and K+)
 M_PI_NEUTRAL, M_K_NEUTRAL = 0.1349768, 0.497611
 
@@ -522,6 +522,10 @@ def _sym_term(w, beam, fs, masses, opts):
         bw = f0980_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"])
     elif md == MASSDEP_F0980_FLATTE:
         bw = f0980_flatte(mI)
+    elif md == MASSDEP_BINNED:
+        # binnedMassDependence::amp (massDependence.cc:212-230)
+        lo, hi = w["bounds"]
+        bw = np.where((mI >= lo) & (mI < hi), 1.0 + 0j, 0j)
     elif md in (MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV):
         bw = pipi_s_wave(mI, {MASSDEP_PIPIS_M: "m", MASSDEP_PIPIS_VES: "ves", MASSDEP_PIPIS_KACHAEV: "kachaev"}[md])
     else:
@@ -600,9 +604,11 @@ def amplitudes(waves, beam_p, fs_p, masses, beam_mass, species, **opts):
 
 
 def wave(J, P, M, refl, L, S, isobar_J, isobar_L, mass_dep, isobar_mass=0.0, isobar_width=0.0,
-         isobar_daughters=(0, 1), bachelor=2, bachelor_first=False, isobar_S=0, isospin=2, isobar_isospin=0):
-    """one wave's description (all spins and isospins doubled)."""
+         isobar_daughters=(0, 1), bachelor=2, bachelor_first=False, isobar_S=0, isospin=2, isobar_isospin=0,
+         bounds=(0.0, 0.0)):
+    """one wave's description (all spins and isospins doubled; bounds: the
+    isobar mass bin of the binned mass dependence)."""
     return dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobar_J=isobar_J, isobar_L=isobar_L, isobar_S=isobar_S,
                 mass_dep=mass_dep, isobar_mass=isobar_mass, isobar_width=isobar_width,
                 isobar_daughters=tuple(isobar_daughters), bachelor=bachelor, bachelor_first=bool(bachelor_first),
-                isospin=isospin, isobar_isospin=isobar_isospin)
+                isospin=isospin, isobar_isospin=isobar_isospin, bounds=tuple(bounds))

@@ -52,7 +52,8 @@ class IsobarWave(C.Structure):
                                           "massDependence")] + \
         [("isobarMass", C.c_double), ("isobarWidth", C.c_double)] + \
         [(n, C.c_int32) for n in ("isobarDaughter1", "isobarDaughter2", "bachelor", "bachelorFirst", "isospin",
-                                  "isobarIsospin")]
+                                  "isobarIsospin")] + \
+        [("binLower", C.c_double), ("binUpper", C.c_double)]
 
 
 SIGNATURES = {

@@ -50,7 +50,8 @@ enum {
 	kMassF0980Flatte = 5,
 	kMassPiPiSM = 6,        // pi pi S-wave, Au-Morgan-Pennington M solution
 	kMassPiPiSVes = 7,      // ... VES sheet with the f0(980) subtracted
-	kMassPiPiSKachaev = 8   // ... Kachaev's reduced parameter set
+	kMassPiPiSKachaev = 8,  // ... Kachaev's reduced parameter set
+	kMassBinned = 9         // 1 inside a mass bin [m0, g0), else 0
 };
 
 // f0(980) Flatte form with the BES II parameters (massDependence.cc:395-445)
@@ -98,7 +99,7 @@ struct WaveDev {
 	int32_t M;                      // 2M of X
 	int32_t LX, LI;                 // 2L of the X and isobar vertices (barrier factors)
 	int32_t massDep;
-	double m0, g0;                  // isobar mass and width
+	double m0, g0;                  // isobar mass and width (binned: the bin's lower and upper edge)
 	double q0, f2q0;                // breakup momentum at m0 and F_L^2(q0) (relativistic BW)
 	double ma, mb;                  // isobar daughter masses
 	double q02;                     // breakup momentum squared at m0 (rho BW)
@@ -349,6 +350,8 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 		const T n2 = dRe * dRe + dIm * dIm;
 		return C2T<T>{dRe / n2, -dIm / n2};
 	}
+	if (w.massDep == kMassBinned)  // binnedMassDependence (massDependence.cc:212-230), FP64 mass
+		return C2T<T>{(mId >= w.m0 && mId < w.g0) ? T(1) : T(0), T(0)};
 	if (w.massDep >= kMassPiPiSM && w.massDep <= kMassPiPiSKachaev) {
 		const C2T<double> a = piPiSWave(mId, w.massDep);
 		return C2T<T>{T(a.re), T(a.im)};

@@ -126,8 +126,10 @@ inline std::string checkWave(const pwa_isobar_wave& w, bool reflBasis)
 	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
 	if (a < 0 || b < 0 || c < 0 || a > 2 || b > 2 || c > 2 || a == b || a == c || b == c)
 		return "isobar daughters and bachelor must be three distinct final-state slots 0..2";
-	if (w.massDependence < kMassFlat || w.massDependence > kMassPiPiSKachaev)
+	if (w.massDependence < kMassFlat || w.massDependence > kMassBinned)
 		return "unknown mass dependence";
+	if (w.massDependence == kMassBinned && !(w.binLower <= w.binUpper))
+		return "a mass bin needs lower <= upper";
 	if (w.massDependence >= kMassRelBw && w.massDependence <= kMassF0980Bw && !(w.isobarMass > 0 && w.isobarWidth > 0))
 		return "a Breit-Wigner needs a positive mass and width";
 	return std::string();
@@ -437,8 +439,8 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 		w.LX = s.L;
 		w.LI = s.isobarL;
 		w.massDep = s.massDependence;
-		w.m0 = s.isobarMass;
-		w.g0 = s.isobarWidth;
+		w.m0 = s.massDependence == kMassBinned ? s.binLower : s.isobarMass;
+		w.g0 = s.massDependence == kMassBinned ? s.binUpper : s.isobarWidth;
 		w.ma = masses[w.a];
 		w.mb = masses[w.b];
 		w.f2q0 = 1.0;

@@ -28,7 +28,7 @@ KEY_MASS_DEPENDENCES = {
     "f0980FlatteBesII": "f0980FlatteBesII", "f_0(980)Flatte": "f0980FlatteBesII",
     "piPiSWaveAuMorganPenningtonM": "piPiSWaveAuMorganPenningtonM",
     "piPiSWaveAuMorganPenningtonVes": "piPiSWaveAuMorganPenningtonVes",
-    "piPiSWaveAuMorganPenningtonKachaev": "piPiSWaveAuMorganPenningtonKachaev",
+    "piPiSWaveAuMorganPenningtonKachaev": "piPiSWaveAuMorganPenningtonKachaev", "binned": "binned",
 }
 
 
@@ -259,6 +259,11 @@ def waveFromKeyFile(path, table, fsNames):
               bachelorFirst=xd.index("fsParticles") < xd.index("isobars"),
               isobarName=iname.replace("(", "_").replace(")", "_"), isospin=int(xq.get("isospin", 0)),
               G=int(xq.get("G", 0)), C_=int(xq.get("C", 0)), isobarIsospin=ip["isospin"])
+    if mdname == "binned":
+        b = md.get("bounds")
+        if not isinstance(b, list) or len(b) != 2 or not b[0] <= b[1]:
+            raise ValueError("%s: a binned mass dependence needs bounds = [lower, upper]" % path)
+        kw["bounds"] = (float(b[0]), float(b[1]))
     amp = key.get("amplitude") or _Group()
     opts = dict(formalism=amp.get("formalism", "helicity"), boseSymmetrize=bool(amp.get("boseSymmetrize", True)),
                 isospinSymmetrize=bool(amp.get("isospinSymmetrize", True)),

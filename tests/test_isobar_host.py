@@ -40,7 +40,8 @@ def _c_waves(ws):
                               isobarMass=kw["isobarMass"], isobarWidth=kw["isobarWidth"],
                               isobarDaughter1=kw["isobarDaughters"][0], isobarDaughter2=kw["isobarDaughters"][1],
                               bachelor=kw["bachelor"], bachelorFirst=int(kw.get("bachelorFirst", False)),
-                              isospin=kw.get("isospin", 2), isobarIsospin=kw.get("isobarIsospin", 0))
+                              isospin=kw.get("isospin", 2), isobarIsospin=kw.get("isobarIsospin", 0),
+                              binLower=kw.get("bounds", (0.0, 0.0))[0], binUpper=kw.get("bounds", (0.0, 0.0))[1])
     return arr
 
 
@@ -141,7 +142,7 @@ def test_wave_checks_and_state():
     with pytest.raises(N.PwaError):
         A.nmbSymTerms(0)                            # no wave yet
     bad = [dict(kw, J=3), dict(kw, M=-2), dict(kw, P=0), dict(kw, L=16), dict(kw, bachelor=1),
-           dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=9), dict(kw, isobarWidth=0.0),
+           dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=10), dict(kw, isobarWidth=0.0),
            dict(kw, M=6)]
     for b in bad:
         with pytest.raises(N.PwaError) as e:

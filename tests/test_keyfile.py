@@ -130,3 +130,20 @@ def test_refusals(files, tmp_path):
         keyfile.waveFromKeyFile(tmp_path / "iso.key", t, ["pi-", "pi+", "pi-"])
     with pytest.raises(ValueError, match="not in"):
         keyfile.waveFromKeyFile(files / "rho.key", t, ["pi-", "pi+", "pi0"])
+
+
+def test_binned_mass_dependence_key(files, tmp_path):
+    """a freed isobar: massDep { name = "binned"; bounds = [lower, upper]; }
+    (massDependence.cc:187-210)."""
+    t = keyfile.readParticleTable(files / "table.txt")
+    key = KEY_RHO.replace('name = "rho(770)"', 'name = "f0(980)"').replace(
+        "L = 2; S = 0;", 'L = 0; S = 0; massDep : { name = "binned"; bounds = [0.6, 0.9]; };').replace(
+        "XQuantumNumbers : { isospin = 2; G = -1; J = 2; P = +1; C = +1; M = 0; refl = +1; };",
+        "XQuantumNumbers : { isospin = 2; G = -1; J = 0; P = -1; C = +1; M = 0; refl = +1; };").replace(
+        "S = 2;", "S = 0;")
+    (tmp_path / "bin.key").write_text(key)
+    kw, _ = keyfile.waveFromKeyFile(tmp_path / "bin.key", t, ["pi-", "pi+", "pi-"])
+    assert kw["massDependence"] == "binned" and kw["bounds"] == (0.6, 0.9)
+    (tmp_path / "bad.key").write_text(key.replace("[0.6, 0.9]", "[0.9, 0.6]"))
+    with pytest.raises(ValueError, match="bounds"):
+        keyfile.waveFromKeyFile(tmp_path / "bad.key", t, ["pi-", "pi+", "pi-"])
