@@ -241,3 +241,25 @@ def test_isospin_symmetrisation_matches_oracle(formalism, dtype):
                        formalism=formalism)
     tol = TOL if dtype == "complex128" else TOL32
     assert np.all(rel_err(ref, got) < tolerances(ws, tol))
+
+
+def test_golden_fixture():
+    """the kernel against the committed oracle amplitudes
+    (tests/golden/oracle_isobar3pi.npz): pi- pi+ pi- in both formalisms and
+    pi- pi0 pi0 with isospin symmetrisation."""
+    import os
+    from isobar_cases import NEUTRAL_NAMES, neutral_waves
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_isobar3pi.npz"))
+    ws = waves()
+    for formalism in ("helicity", "canonical"):
+        A = _amp(ws, gold["masses"], float(gold["beam_mass"]), {"formalism": formalism})
+        got = A.amplitudes(gold["beam"], gold["fs"])
+        assert np.all(rel_err(gold[formalism], got) < tolerances(ws, TOL)), formalism
+    nws = neutral_waves()
+    B = I.isobarHelicityAmplitudes()
+    B.setFinalState(NEUTRAL_NAMES, gold["neutral_masses"], float(gold["neutral_beam_mass"]))
+    for _, kw in nws:
+        B.addWave(**kw)
+    B.enableIsospinSymmetrization(True)
+    got = B.amplitudes(gold["neutral_beam"], gold["neutral_fs"])
+    assert np.all(rel_err(gold["neutral_isospin"], got) < tolerances(nws, TOL))

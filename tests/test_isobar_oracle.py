@@ -231,3 +231,20 @@ def test_pipi_s_wave_unitarity_and_f0_dip():
     grid = np.linspace(0.9, 1.05, 301)
     a = np.abs(O.pipi_s_wave(grid, "m"))
     assert 0.97 < grid[np.argmin(a)] < 1.0 and a.min() < 0.2 * a.max()
+
+
+def test_golden_fixture():
+    """tests/golden/oracle_isobar3pi.npz (make_isobar_golden.py): the oracle
+    and the seeded event generator reproduce the committed amplitudes."""
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    import make_isobar_golden as G
+    gold = np.load(os.path.join(here, "golden", "oracle_isobar3pi.npz"))
+    now = G.compute()
+    for k in ("beam", "fs", "neutral_beam", "neutral_fs"):
+        assert np.array_equal(now[k], gold[k]), k
+    for k in ("helicity", "canonical", "neutral_isospin"):
+        scale = np.abs(gold[k]).max(axis=1, keepdims=True) + 1e-300
+        assert np.all(np.abs(now[k] - gold[k]) <= 1e-12 * scale), k
