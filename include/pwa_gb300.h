@@ -458,7 +458,7 @@ int pwa_mlp_train(pwa_mlp* net, const float* X, const float* T, uint64_t nSample
 /* reference.  FP64 on the GPU, one thread per event.                        */
 /* ------------------------------------------------------------------------ */
 typedef struct pwa_isobar pwa_isobar;
-/* massDependence (decayAmplitude/massDependence.cc:169-625): flatMassDependence, binnedMassDependence,
+/* massDependence (decayAmplitude/massDependence.cc:169-862): flatMassDependence, binnedMassDependence,
  * relativisticBreitWigner, constWidthBreitWigner, rhoBreitWigner,
  * f0980BreitWigner, f0980FlatteBesII (fixed BES II parameters),
  * piPiSWaveAuMorganPenningtonM / Ves / Kachaev (fixed AMP parameters; for the
@@ -473,7 +473,8 @@ enum pwa_mass_dependence {
 	PWA_MASSDEP_PIPI_S_AMP_M = 6,
 	PWA_MASSDEP_PIPI_S_AMP_VES = 7,
 	PWA_MASSDEP_PIPI_S_AMP_KACHAEV = 8,
-	PWA_MASSDEP_BINNED = 9            /* binnedMassDependence: 1 inside [binLower, binUpper), else 0 */
+	PWA_MASSDEP_BINNED = 9,           /* binnedMassDependence: 1 inside [binLower, binUpper), else 0 */
+	PWA_MASSDEP_RHO_PRIME = 10        /* rhoPrimeMassDep: fixed rho(1450) / rho(1700) mixture */
 };
 /* one wave: the content of a key file of a three-body decay
  * (decayAmplitude/waveDescription.cc:880-932) */

@@ -66,7 +66,7 @@ import numpy as np
 
 PR_DEFAULT = 0.1973        # GeV/c, 1 fm interaction radius
 (MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW, MASSDEP_RHO_BW, MASSDEP_F0980_BW, MASSDEP_F0980_FLATTE,
- MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV, MASSDEP_BINNED) = range(10)
+ MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV, MASSDEP_BINNED, MASSDEP_RHO_PRIME) = range(11)
 M_PI_CHARGED, M_K_CHARGED = 0.13957039, 0.493677   # GeV/c^2 (the particle table's pi+ and K+)
 M_PI_NEUTRAL, M_K_NEUTRAL = 0.1349768, 0.497611
 
@@ -522,6 +522,9 @@ def _sym_term(w, beam, fs, masses, opts):
         bw = f0980_bw(mI, masses[a], masses[b], w["isobar_mass"], w["isobar_width"])
     elif md == MASSDEP_F0980_FLATTE:
         bw = f0980_flatte(mI)
+    elif md == MASSDEP_RHO_PRIME:
+        # rhoPrimeMassDep::amp (massDependence.cc:830-862)
+        bw = (4 * const_width_bw(mI, 1.465, 0.235) - 3 * const_width_bw(mI, 1.700, 0.220)) / 7
     elif md == MASSDEP_BINNED:
         # binnedMassDependence::amp (massDependence.cc:212-230)
         lo, hi = w["bounds"]

@@ -51,7 +51,8 @@ enum {
 	kMassPiPiSM = 6,        // pi pi S-wave, Au-Morgan-Pennington M solution
 	kMassPiPiSVes = 7,      // ... VES sheet with the f0(980) subtracted
 	kMassPiPiSKachaev = 8,  // ... Kachaev's reduced parameter set
-	kMassBinned = 9         // 1 inside a mass bin [m0, g0), else 0
+	kMassBinned = 9,        // 1 inside a mass bin [m0, g0), else 0
+	kMassRhoPrime = 10      // (4 BW(rho(1450)) - 3 BW(rho(1700))) / 7
 };
 
 // f0(980) Flatte form with the BES II parameters (massDependence.cc:395-445)
@@ -349,6 +350,14 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 		const T dIm = -T(kFlatteG1) * reRho;
 		const T n2 = dRe * dRe + dIm * dIm;
 		return C2T<T>{dRe / n2, -dIm / n2};
+	}
+	if (w.massDep == kMassRhoPrime) {
+		// rhoPrimeMassDep (massDependence.cc:830-862): constant-width Breit-Wigners
+		// of rho(1450) (1.465, 0.235) and rho(1700) (1.700, 0.220) mixed 4 : -3
+		const double m2 = mId * mId;
+		const double A1 = 1.465 * 0.235, B1 = 1.465 * 1.465 - m2, f1 = A1 / (B1 * B1 + A1 * A1);
+		const double A2 = 1.700 * 0.220, B2 = 1.700 * 1.700 - m2, f2 = A2 / (B2 * B2 + A2 * A2);
+		return C2T<T>{T((4.0 * f1 * B1 - 3.0 * f2 * B2) / 7.0), T((4.0 * f1 * A1 - 3.0 * f2 * A2) / 7.0)};
 	}
 	if (w.massDep == kMassBinned)  // binnedMassDependence (massDependence.cc:212-230), FP64 mass
 		return C2T<T>{(mId >= w.m0 && mId < w.g0) ? T(1) : T(0), T(0)};

@@ -126,7 +126,7 @@ inline std::string checkWave(const pwa_isobar_wave& w, bool reflBasis)
 	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
 	if (a < 0 || b < 0 || c < 0 || a > 2 || b > 2 || c > 2 || a == b || a == c || b == c)
 		return "isobar daughters and bachelor must be three distinct final-state slots 0..2";
-	if (w.massDependence < kMassFlat || w.massDependence > kMassBinned)
+	if (w.massDependence < kMassFlat || w.massDependence > kMassRhoPrime)
 		return "unknown mass dependence";
 	if (w.massDependence == kMassBinned && !(w.binLower <= w.binUpper))
 		return "a mass bin needs lower <= upper";

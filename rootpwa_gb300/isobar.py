@@ -32,7 +32,8 @@ from . import _native as N
 PION_ISOSPINS = {"pi-": (2, -2, -1), "pi0": (2, 0, -1), "pi+": (2, 2, -1)}
 MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2, "rhoBreitWigner": 3,
                     "f0980BreitWigner": 4, "f0980FlatteBesII": 5, "piPiSWaveAuMorganPenningtonM": 6,
-                    "piPiSWaveAuMorganPenningtonVes": 7, "piPiSWaveAuMorganPenningtonKachaev": 8, "binned": 9}
+                    "piPiSWaveAuMorganPenningtonVes": 7, "piPiSWaveAuMorganPenningtonKachaev": 8, "binned": 9,
+                    "rhoPrime": 10}
 
 
 def _qn(x):

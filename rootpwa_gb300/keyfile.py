@@ -29,6 +29,7 @@ KEY_MASS_DEPENDENCES = {
     "piPiSWaveAuMorganPenningtonM": "piPiSWaveAuMorganPenningtonM",
     "piPiSWaveAuMorganPenningtonVes": "piPiSWaveAuMorganPenningtonVes",
     "piPiSWaveAuMorganPenningtonKachaev": "piPiSWaveAuMorganPenningtonKachaev", "binned": "binned",
+    "rhoPrime": "rhoPrime",
 }
 
 

@@ -1,4 +1,4 @@
-"""Generates tests/golden/oracle_isobar3pi.npz: FP64 oracle amplitudes
+"""Generates tests/golden/isobar3pi_oracle.npz: FP64 oracle amplitudes
 (oracle/isobar_oracle.py) of the test wave sets of tests/isobar_cases.py on
 seeded synthetic events -- pi- pi+ pi- with the default options and in the
 canonical formalism, pi- pi0 pi0 with isospin symmetrisation -- together with
@@ -39,5 +39,5 @@ def compute():
 
 
 if __name__ == "__main__":
-    np.savez_compressed(os.path.join(HERE, "oracle_isobar3pi.npz"), **compute())
-    print("wrote oracle_isobar3pi.npz")
+    np.savez_compressed(os.path.join(HERE, "isobar3pi_oracle.npz"), **compute())
+    print("wrote isobar3pi_oracle.npz")

@@ -34,6 +34,7 @@ def waves():
         (4, -1, 0, +1, 4, 0, 0, 0, O.MASSDEP_PIPIS_VES, 0.0, 0.0, (2, 1), 0, False),    # 2-+0+ (pi pi)_S D, VES
         (2, +1, 2, +1, 2, 0, 0, 0, O.MASSDEP_PIPIS_KACHAEV, 0.0, 0.0, (1, 2), 0, True),  # 1++1+ (pi pi)_S P, Kachaev
         (0, -1, 0, +1, 0, 0, 0, 0, O.MASSDEP_BINNED, 0.6, 0.9, (1, 2), 0, False),       # 0-+0+ freed (pi pi)_S bin
+        (2, -1, 2, +1, 2, 2, 2, 2, O.MASSDEP_RHO_PRIME, 0.0, 0.0, (1, 2), 0, False),    # 1-+1+ rho' P (exotic)
         (2, +1, 0, -1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, False),   # 1++0- (zero by reflectivity)
     ]
     out = []
@@ -41,7 +42,8 @@ def waves():
           O.MASSDEP_CONST_BW: "constWidthBreitWigner", O.MASSDEP_RHO_BW: "rhoBreitWigner",
           O.MASSDEP_F0980_BW: "f0980BreitWigner", O.MASSDEP_F0980_FLATTE: "f0980FlatteBesII",
           O.MASSDEP_PIPIS_M: "piPiSWaveAuMorganPenningtonM", O.MASSDEP_PIPIS_VES: "piPiSWaveAuMorganPenningtonVes",
-          O.MASSDEP_PIPIS_KACHAEV: "piPiSWaveAuMorganPenningtonKachaev", O.MASSDEP_BINNED: "binned"}
+          O.MASSDEP_PIPIS_KACHAEV: "piPiSWaveAuMorganPenningtonKachaev", O.MASSDEP_BINNED: "binned",
+          O.MASSDEP_RHO_PRIME: "rhoPrime"}
     for J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first in specs:
         bounds = (mass, width) if m == O.MASSDEP_BINNED else (0.0, 0.0)
         ow = O.wave(J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first, bounds=bounds)

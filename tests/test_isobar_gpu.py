@@ -245,11 +245,11 @@ def test_isospin_symmetrisation_matches_oracle(formalism, dtype):
 
 def test_golden_fixture():
     """the kernel against the committed oracle amplitudes
-    (tests/golden/oracle_isobar3pi.npz): pi- pi+ pi- in both formalisms and
+    (tests/golden/isobar3pi_oracle.npz): pi- pi+ pi- in both formalisms and
     pi- pi0 pi0 with isospin symmetrisation."""
     import os
     from isobar_cases import NEUTRAL_NAMES, neutral_waves
-    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_isobar3pi.npz"))
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "isobar3pi_oracle.npz"))
     ws = waves()
     for formalism in ("helicity", "canonical"):
         A = _amp(ws, gold["masses"], float(gold["beam_mass"]), {"formalism": formalism})

@@ -142,7 +142,7 @@ def test_wave_checks_and_state():
     with pytest.raises(N.PwaError):
         A.nmbSymTerms(0)                            # no wave yet
     bad = [dict(kw, J=3), dict(kw, M=-2), dict(kw, P=0), dict(kw, L=16), dict(kw, bachelor=1),
-           dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=10), dict(kw, isobarWidth=0.0),
+           dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=11), dict(kw, isobarWidth=0.0),
            dict(kw, M=6)]
     for b in bad:
         with pytest.raises(N.PwaError) as e:

@@ -234,14 +234,14 @@ def test_pipi_s_wave_unitarity_and_f0_dip():
 
 
 def test_golden_fixture():
-    """tests/golden/oracle_isobar3pi.npz (make_isobar_golden.py): the oracle
+    """tests/golden/isobar3pi_oracle.npz (make_isobar_golden.py): the oracle
     and the seeded event generator reproduce the committed amplitudes."""
     import os
     import sys
     here = os.path.dirname(os.path.abspath(__file__))
     sys.path.insert(0, os.path.join(here, "golden"))
     import make_isobar_golden as G
-    gold = np.load(os.path.join(here, "golden", "oracle_isobar3pi.npz"))
+    gold = np.load(os.path.join(here, "golden", "isobar3pi_oracle.npz"))
     now = G.compute()
     for k in ("beam", "fs", "neutral_beam", "neutral_fs"):
         assert np.array_equal(now[k], gold[k]), k
