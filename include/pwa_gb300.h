@@ -474,7 +474,9 @@ enum pwa_mass_dependence {
 	PWA_MASSDEP_PIPI_S_AMP_VES = 7,
 	PWA_MASSDEP_PIPI_S_AMP_KACHAEV = 8,
 	PWA_MASSDEP_BINNED = 9,           /* binnedMassDependence: 1 inside [binLower, binUpper), else 0 */
-	PWA_MASSDEP_RHO_PRIME = 10        /* rhoPrimeMassDep: fixed rho(1450) / rho(1700) mixture */
+	PWA_MASSDEP_RHO_PRIME = 10,       /* rhoPrimeMassDep: fixed rho(1450) / rho(1700) mixture */
+	PWA_MASSDEP_KPI_S_GLASS = 11,     /* KPiSGLASS: K pi S-wave, LASS form with massDepParams */
+	PWA_MASSDEP_KPI_S_PALANO_PENNINGTON = 12 /* KPiSPalanoPennington: K pi / K eta K-matrix */
 };
 /* one wave: the content of a key file of a three-body decay
  * (decayAmplitude/waveDescription.cc:880-932) */
@@ -488,6 +490,8 @@ typedef struct pwa_isobar_wave {
 	int32_t bachelorFirst;            /* X-vertex daughter 1 (the analyser) is the bachelor rather than the isobar */
 	int32_t isospin, isobarIsospin;   /* 2I of X and of the isobar (isospin symmetrisation only) */
 	double binLower, binUpper;        /* PWA_MASSDEP_BINNED: the isobar mass bin [lower, upper) */
+	double massDepParams[10];         /* PWA_MASSDEP_KPI_S_GLASS: a, r, M0, G0, phiF, phiR, phiRsin, F, R, MMax;
+	                                     PWA_MASSDEP_KPI_S_PALANO_PENNINGTON: MMax (0: 2.4 GeV/c^2) */
 } pwa_isobar_wave;
 /* isobarHelicityAmplitude (decayAmplitude/isobarHelicityAmplitude.cc:64-195)
  * or isobarCanonicalAmplitude (decayAmplitude/isobarCanonicalAmplitude.cc:64-190) */

@@ -40,8 +40,10 @@ It follows the reference step by step, vectorised over events with numpy:
   q0 = sqrt|q0^2| (massDependence.cc:254-296, utilities/physUtils.hpp:283-300),
   constant-width Breit-Wigner (massDependence.cc:300-320), the rho and
   f0(980) Breit-Wigners (:324-390), the f0(980) Flatte form with the BES II
-  parameters (:395-445) and the pi pi S-wave of Au, Morgan and Pennington
-  (M, VES and Kachaev variants, :449-625).
+  parameters (:395-445), the pi pi S-wave of Au, Morgan and Pennington
+  (M, VES and Kachaev variants, :449-625), the K pi S-wave forms (LASS and
+  Palano-Pennington, :700-828), rho' (:830-862) and the binned mass
+  dependence (:187-230).
 
 The building blocks are restated from the published formulas, not from the
 reference's arrangement of them: Clebsch-Gordan coefficients by Racah's
@@ -66,7 +68,9 @@ import numpy as np
 
 PR_DEFAULT = 0.1973        # GeV/c, 1 fm interaction radius
 (MASSDEP_FLAT, MASSDEP_REL_BW, MASSDEP_CONST_BW, MASSDEP_RHO_BW, MASSDEP_F0980_BW, MASSDEP_F0980_FLATTE,
- MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV, MASSDEP_BINNED, MASSDEP_RHO_PRIME) = range(11)
+ MASSDEP_PIPIS_M, MASSDEP_PIPIS_VES, MASSDEP_PIPIS_KACHAEV, MASSDEP_BINNED, MASSDEP_RHO_PRIME, MASSDEP_KPIS_GLASS,
+ MASSDEP_KPIS_PALANO) = range(13)
+M_ETA = 0.547862
 M_PI_CHARGED, M_K_CHARGED = 0.13957039, 0.493677   # GeV/c^2 (the particle table's pi+ and K+)
 M_PI_NEUTRAL, M_K_NEUTRAL = 0.1349768, 0.497611
 
@@ -280,6 +284,59 @@ def pipi_s_wave(M, variant):
             A, B = C * m / q, f0m * f0m - m * m
             amp = amp - coupling * (A / (B * B + C * C)) * (B + 1j * C)
         out[e] = amp
+    return out
+
+
+def kpi_s_glass(M, p):
+    """KPiSGLASS::amp (massDependence.cc:700-722); p = a, r, M0, G0, phiF,
+    phiR, phiRsin, F, R, MMax."""
+    a, r, M0, G0, phiF, phiR, phiRsin, F, R, MMax = p
+    out = np.zeros(np.shape(M), dtype=np.complex128)
+    for e, m in np.ndenumerate(np.asarray(M, dtype=np.float64)):
+        if not (M_K_CHARGED + M_PI_CHARGED < m < MMax):
+            continue
+        q = math.sqrt(breakup_momentum_squared(m, M_K_CHARGED, M_PI_CHARGED))
+        q0 = math.sqrt(breakup_momentum_squared(M0, M_K_CHARGED, M_PI_CHARGED))
+        G = G0 * M0 / m * q / q0
+        dR = math.atan(M0 * G / (M0 * M0 - m * m))
+        dF = math.atan(2.0 * a * q / (2.0 + a * r * q * q))
+        amp = (F * math.sin(dF + phiF) * np.exp(1j * (dF + phiF))
+               + R * math.sin(dR + phiRsin) * np.exp(1j * (dR + phiR)) * np.exp(2j * (dF + phiF)))
+        out[e] = amp * 0.5 * m / q
+    return out
+
+
+def _q_complex2(M, m1, m2):
+    q2 = breakup_momentum_squared(M, m1, m2)
+    q = np.sqrt(np.abs(q2))
+    return np.where(q2 < 0, 1j * q, q + 0j)
+
+
+def kpi_s_palano(M, MMax=2.4):
+    """KPiSPalanoPennington::amp (massDependence.cc:770-828): T_11 of the
+    (K pi, K eta) K-matrix with an Adler zero."""
+    sTop, sBot, sa, sb = 5.832, 0.36, 1.7991, 8.3627
+    ga, gb = (0.3139, -0.00775), (1.1804, -0.22335)
+    C = (((-0.1553, 0.0909, 0.8618, 0.0629), (0.0738, 0.3866, 1.2195, 0.8390)),
+         ((0.0738, 0.3866, 1.2195, 0.8390), (-0.0036, 0.2590, 1.6950, 2.2300)))
+    sKpi = M_K_CHARGED ** 2 + M_PI_CHARGED ** 2
+    sA = 0.87753 * sKpi
+    out = np.zeros(np.shape(M), dtype=np.complex128)
+    for e, m in np.ndenumerate(np.asarray(M, dtype=np.float64)):
+        if not (M_K_CHARGED + M_PI_CHARGED < m < MMax):
+            continue
+        s = m * m
+        rho1 = 2 * _q_complex2(m, M_K_CHARGED, M_PI_CHARGED) / m
+        rho2 = 2 * _q_complex2(m, M_K_CHARGED, M_ETA) / m
+        x = (2 * s - (sTop + sBot)) / (sTop - sBot)
+
+        def K(i, j):
+            return (s - sA) / sKpi * (ga[i] * ga[j] / (sa - s) + gb[i] * gb[j] / (sb - s)
+                                      + sum(C[i][j][n] * x ** n for n in range(4)))
+        K11, K12, K22 = K(0, 0), K(0, 1), K(1, 1)
+        detK = K11 * K22 - K12 * K12
+        delta = 1.0 - 1j * rho1 * K11 - 1j * rho2 * K22 - rho1 * rho2 * detK
+        out[e] = (K11 - 1j * rho2 * detK) / delta
     return out
 
 
@@ -525,6 +582,11 @@ def _sym_term(w, beam, fs, masses, opts):
     elif md == MASSDEP_RHO_PRIME:
         # rhoPrimeMassDep::amp (massDependence.cc:830-862)
         bw = (4 * const_width_bw(mI, 1.465, 0.235) - 3 * const_width_bw(mI, 1.700, 0.220)) / 7
+    elif md == MASSDEP_KPIS_GLASS:
+        bw = kpi_s_glass(mI, w["mass_dep_params"])
+    elif md == MASSDEP_KPIS_PALANO:
+        p = w.get("mass_dep_params") or (2.4,)
+        bw = kpi_s_palano(mI, p[0] if p[0] > 0 else 2.4)
     elif md == MASSDEP_BINNED:
         # binnedMassDependence::amp (massDependence.cc:212-230)
         lo, hi = w["bounds"]
@@ -608,10 +670,12 @@ def amplitudes(waves, beam_p, fs_p, masses, beam_mass, species, **opts):
 
 def wave(J, P, M, refl, L, S, isobar_J, isobar_L, mass_dep, isobar_mass=0.0, isobar_width=0.0,
          isobar_daughters=(0, 1), bachelor=2, bachelor_first=False, isobar_S=0, isospin=2, isobar_isospin=0,
-         bounds=(0.0, 0.0)):
+         bounds=(0.0, 0.0), mass_dep_params=()):
     """one wave's description (all spins and isospins doubled; bounds: the
-    isobar mass bin of the binned mass dependence)."""
+    isobar mass bin of the binned mass dependence; mass_dep_params: those of
+    the K pi S-wave forms)."""
     return dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobar_J=isobar_J, isobar_L=isobar_L, isobar_S=isobar_S,
                 mass_dep=mass_dep, isobar_mass=isobar_mass, isobar_width=isobar_width,
                 isobar_daughters=tuple(isobar_daughters), bachelor=bachelor, bachelor_first=bool(bachelor_first),
-                isospin=isospin, isobar_isospin=isobar_isospin, bounds=tuple(bounds))
+                isospin=isospin, isobar_isospin=isobar_isospin, bounds=tuple(bounds),
+                mass_dep_params=tuple(mass_dep_params))

@@ -53,7 +53,7 @@ class IsobarWave(C.Structure):
         [("isobarMass", C.c_double), ("isobarWidth", C.c_double)] + \
         [(n, C.c_int32) for n in ("isobarDaughter1", "isobarDaughter2", "bachelor", "bachelorFirst", "isospin",
                                   "isobarIsospin")] + \
-        [("binLower", C.c_double), ("binUpper", C.c_double)]
+        [("binLower", C.c_double), ("binUpper", C.c_double), ("massDepParams", C.c_double * 10)]
 
 
 SIGNATURES = {

@@ -52,8 +52,11 @@ enum {
 	kMassPiPiSVes = 7,      // ... VES sheet with the f0(980) subtracted
 	kMassPiPiSKachaev = 8,  // ... Kachaev's reduced parameter set
 	kMassBinned = 9,        // 1 inside a mass bin [m0, g0), else 0
-	kMassRhoPrime = 10      // (4 BW(rho(1450)) - 3 BW(rho(1700))) / 7
+	kMassRhoPrime = 10,     // (4 BW(rho(1450)) - 3 BW(rho(1700))) / 7
+	kMassKPiSGlass = 11,    // K pi S-wave, LASS form (parameters per wave)
+	kMassKPiSPalano = 12    // K pi S-wave, Palano-Pennington K-matrix
 };
+constexpr double kMassEta = 0.547862;
 
 // f0(980) Flatte form with the BES II parameters (massDependence.cc:395-445)
 // and the charged pion and kaon masses of the particle table
@@ -104,6 +107,7 @@ struct WaveDev {
 	double q0, f2q0;                // breakup momentum at m0 and F_L^2(q0) (relativistic BW)
 	double ma, mb;                  // isobar daughter masses
 	double q02;                     // breakup momentum squared at m0 (rho BW)
+	double mdp[10];                 // parameters of the K pi S-wave forms
 	int32_t lam0, lam1;             // LamTerm range
 	int32_t term0, term1;           // SymTerm range (symmetrisation terms)
 	int32_t topo;                   // topology class (waves of one class share kinematics)
@@ -255,6 +259,59 @@ PWA_HD C2T<double> rhoOf(double m, double m1)
 	return q2 < 0 ? C2T<double>{0.0, r} : C2T<double>{r, 0.0};
 }
 
+// KPiSGLASS::amp (massDependence.cc:700-722): LASS-type K pi S-wave,
+// p = a, r, M0, G0, phiF, phiR, phiRsin, F, R, MMax; atan as in the reference
+PWA_HD C2T<double> kPiSGlass(double M, const double* p)
+{
+	const double mk = kMassKCharged, mpi = kMassPiCharged;
+	if (!(M > mk + mpi && M < p[9]))
+		return C2T<double>{0.0, 0.0};
+	const double q = sqrt(breakup2<double>(M, mk, mpi));
+	const double q0 = sqrt(fabs(breakup2<double>(p[2], mk, mpi)));
+	const double G = p[3] * p[2] / M * q / q0;
+	const double dR = atan(p[2] * G / (p[2] * p[2] - M * M));
+	const double dF = atan(2.0 * p[0] * q / (2.0 + p[0] * p[1] * q * q));
+	const double aF = dF + p[4];
+	const double sF = p[7] * sin(aF), sR = p[8] * sin(dR + p[6]);
+	// F sin(aF) e^{i aF} + R sin(dR + phiRsin) e^{i (dR + phiR + 2 aF)}
+	const double ph = dR + p[5] + 2.0 * aF;
+	const double scale = 0.5 * M / q;
+	return C2T<double>{scale * (sF * cos(aF) + sR * cos(ph)), scale * (sF * sin(aF) + sR * sin(ph))};
+}
+
+// KPiSPalanoPennington::amp (massDependence.cc:770-828): two-channel (K pi,
+// K eta) K-matrix with an Adler zero, published parameters; T_11
+PWA_HD C2T<double> kPiSPalano(double M, double MMax)
+{
+	const double mk = kMassKCharged, mpi = kMassPiCharged;
+	if (!(M > mk + mpi && M < MMax))
+		return C2T<double>{0.0, 0.0};
+	const double sTop = 5.832, sBot = 0.36, sa = 1.7991, sb = 8.3627;
+	const double ga0 = 0.3139, ga1 = -0.00775, gb0 = 1.1804, gb1 = -0.22335;
+	const double sKpi = mk * mk + mpi * mpi, sA = 0.87753 * sKpi;
+	const double s = M * M, x = (2.0 * s - (sTop + sBot)) / (sTop - sBot);
+	const double pre = (s - sA) / sKpi;
+	auto poly = [x](double c0, double c1, double c2, double c3) { return c0 + x * (c1 + x * (c2 + x * c3)); };
+	const double K11 = pre * (ga0 * ga0 / (sa - s) + gb0 * gb0 / (sb - s) + poly(-0.1553, 0.0909, 0.8618, 0.0629));
+	const double K12 = pre * (ga0 * ga1 / (sa - s) + gb0 * gb1 / (sb - s) + poly(0.0738, 0.3866, 1.2195, 0.8390));
+	const double K22 = pre * (ga1 * ga1 / (sa - s) + gb1 * gb1 / (sb - s) + poly(-0.0036, 0.2590, 1.6950, 2.2300));
+	// rho = 2 q / M with complex breakup momenta (imaginary below threshold)
+	auto rho = [M](double m1, double m2) {
+		const double q2 = breakup2<double>(M, m1, m2);
+		const double r = 2.0 * sqrt(q2 < 0 ? -q2 : q2) / M;
+		return q2 < 0 ? C2T<double>{0.0, r} : C2T<double>{r, 0.0};
+	};
+	const C2T<double> r1 = rho(mk, mpi), r2 = rho(mk, kMassEta);
+	const double detK = K11 * K22 - K12 * K12;
+	// delta = 1 - i r1 K11 - i r2 K22 - r1 r2 detK;  T11 = (K11 - i r2 detK) / delta
+	const C2T<double> r1r2 = cmul(r1, r2);
+	const C2T<double> delta{1.0 + r1.im * K11 + r2.im * K22 - r1r2.re * detK,
+	                        -r1.re * K11 - r2.re * K22 - r1r2.im * detK};
+	const C2T<double> num{K11 + r2.im * detK, -r2.re * detK};
+	const double n2 = delta.re * delta.re + delta.im * delta.im;
+	return C2T<double>{(num.re * delta.re + num.im * delta.im) / n2, (num.im * delta.re - num.re * delta.im) / n2};
+}
+
 // piPiSWaveAuMorganPennington{M,Ves,Kachaev}::amp (massDependence.cc:505-625),
 // FP64 (the poles cancel near s_1)
 PWA_HD C2T<double> piPiSWave(double m, int variant)
@@ -358,6 +415,11 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 		const double A1 = 1.465 * 0.235, B1 = 1.465 * 1.465 - m2, f1 = A1 / (B1 * B1 + A1 * A1);
 		const double A2 = 1.700 * 0.220, B2 = 1.700 * 1.700 - m2, f2 = A2 / (B2 * B2 + A2 * A2);
 		return C2T<T>{T((4.0 * f1 * B1 - 3.0 * f2 * B2) / 7.0), T((4.0 * f1 * A1 - 3.0 * f2 * A2) / 7.0)};
+	}
+	if (w.massDep == kMassKPiSGlass || w.massDep == kMassKPiSPalano) {
+		const C2T<double> a = w.massDep == kMassKPiSGlass ? kPiSGlass(mId, w.mdp)
+		                                                  : kPiSPalano(mId, w.mdp[0] > 0 ? w.mdp[0] : 2.4);
+		return C2T<T>{T(a.re), T(a.im)};
 	}
 	if (w.massDep == kMassBinned)  // binnedMassDependence (massDependence.cc:212-230), FP64 mass
 		return C2T<T>{(mId >= w.m0 && mId < w.g0) ? T(1) : T(0), T(0)};

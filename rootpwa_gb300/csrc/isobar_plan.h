@@ -126,7 +126,7 @@ inline std::string checkWave(const pwa_isobar_wave& w, bool reflBasis)
 	const int a = w.isobarDaughter1, b = w.isobarDaughter2, c = w.bachelor;
 	if (a < 0 || b < 0 || c < 0 || a > 2 || b > 2 || c > 2 || a == b || a == c || b == c)
 		return "isobar daughters and bachelor must be three distinct final-state slots 0..2";
-	if (w.massDependence < kMassFlat || w.massDependence > kMassRhoPrime)
+	if (w.massDependence < kMassFlat || w.massDependence > kMassKPiSPalano)
 		return "unknown mass dependence";
 	if (w.massDependence == kMassBinned && !(w.binLower <= w.binUpper))
 		return "a mass bin needs lower <= upper";
@@ -444,6 +444,8 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 		w.ma = masses[w.a];
 		w.mb = masses[w.b];
 		w.f2q0 = 1.0;
+		for (int k = 0; k < 10; ++k)
+			w.mdp[k] = s.massDepParams[k];
 		w.q02 = breakup2(s.isobarMass, w.ma, w.mb);
 		if (s.massDependence == kMassRelBw) {
 			// the PWA2000 rule q0 = sqrt|q0^2| (massDependence.cc:268-270)

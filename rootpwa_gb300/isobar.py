@@ -33,7 +33,7 @@ PION_ISOSPINS = {"pi-": (2, -2, -1), "pi0": (2, 0, -1), "pi+": (2, 2, -1)}
 MASS_DEPENDENCES = {"flat": 0, "relativisticBreitWigner": 1, "constWidthBreitWigner": 2, "rhoBreitWigner": 3,
                     "f0980BreitWigner": 4, "f0980FlatteBesII": 5, "piPiSWaveAuMorganPenningtonM": 6,
                     "piPiSWaveAuMorganPenningtonVes": 7, "piPiSWaveAuMorganPenningtonKachaev": 8, "binned": 9,
-                    "rhoPrime": 10}
+                    "rhoPrime": 10, "KPiSGLASS": 11, "KPiSPalanoPennington": 12}
 
 
 def _qn(x):
@@ -136,17 +136,24 @@ class isobarHelicityAmplitudes:
     # -- waves ---------------------------------------------------------------------
     def addWave(self, J, P, M, refl, L, S, isobarJ, isobarL, massDependence="flat", isobarMass=0.0,
                 isobarWidth=0.0, isobarDaughters=(0, 1), bachelor=2, bachelorFirst=False, isobarS=0,
-                isobarName="isobar", isospin=2, G=-1, C_=+1, isobarIsospin=0, bounds=(0.0, 0.0)):
+                isobarName="isobar", isospin=2, G=-1, C_=+1, isobarIsospin=0, bounds=(0.0, 0.0),
+                massDepParams=()):
         """adds one wave (all spins and isospins doubled); returns its index.
         isospin and isobarIsospin (2I of X and of the isobar) enter isospin
         symmetrisation and the wave name; bounds is the isobar mass bin of
-        the binned mass dependence."""
+        the binned mass dependence, massDepParams the parameters of the K pi
+        S-wave forms (KPiSGLASS: a, r, M0, G0, phiF, phiR, phiRsin, F, R,
+        MMax; KPiSPalanoPennington: MMax)."""
         md = MASS_DEPENDENCES[massDependence] if isinstance(massDependence, str) else int(massDependence)
         w = N.IsobarWave(J=J, P=P, M=M, refl=refl, L=L, S=S, isobarJ=isobarJ, isobarL=isobarL, isobarS=isobarS,
                          massDependence=md, isobarMass=isobarMass, isobarWidth=isobarWidth,
                          isobarDaughter1=isobarDaughters[0], isobarDaughter2=isobarDaughters[1],
                          bachelor=bachelor, bachelorFirst=1 if bachelorFirst else 0, isospin=isospin,
                          isobarIsospin=isobarIsospin, binLower=float(bounds[0]), binUpper=float(bounds[1]))
+        if len(massDepParams) > 10:
+            raise ValueError("at most 10 mass-dependence parameters")
+        for k, v in enumerate(massDepParams):
+            w.massDepParams[k] = float(v)
         N.call("pwa_isobar_add_wave", self._h, C.byref(w))
         self._waves.append(dict(J=J, P=P, M=M, refl=refl, L=L, S=S, isobarJ=isobarJ, isobarL=isobarL,
                                 isobarS=isobarS, isobarDaughters=tuple(isobarDaughters), bachelor=bachelor,

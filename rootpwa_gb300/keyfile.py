@@ -29,8 +29,10 @@ KEY_MASS_DEPENDENCES = {
     "piPiSWaveAuMorganPenningtonM": "piPiSWaveAuMorganPenningtonM",
     "piPiSWaveAuMorganPenningtonVes": "piPiSWaveAuMorganPenningtonVes",
     "piPiSWaveAuMorganPenningtonKachaev": "piPiSWaveAuMorganPenningtonKachaev", "binned": "binned",
-    "rhoPrime": "rhoPrime",
+    "rhoPrime": "rhoPrime", "KPiSGLASS": "KPiSGLASS", "KPiSPalanoPennington": "KPiSPalanoPennington",
 }
+# KPiSGLASS::Create (massDependence.cc:660-686) reads these from the massDep group
+GLASS_PARAMETERS = ("a", "r", "M0", "G0", "phiF", "phiR", "phiRsin", "F", "R", "MMax")
 
 
 # -- libconfig subset ----------------------------------------------------------------
@@ -260,6 +262,13 @@ def waveFromKeyFile(path, table, fsNames):
               bachelorFirst=xd.index("fsParticles") < xd.index("isobars"),
               isobarName=iname.replace("(", "_").replace(")", "_"), isospin=int(xq.get("isospin", 0)),
               G=int(xq.get("G", 0)), C_=int(xq.get("C", 0)), isobarIsospin=ip["isospin"])
+    if mdname == "KPiSGLASS":
+        missing = [k for k in GLASS_PARAMETERS if md.get(k) is None]
+        if missing:
+            raise ValueError("%s: KPiSGLASS needs %s" % (path, ", ".join(missing)))
+        kw["massDepParams"] = tuple(float(md.get(k)) for k in GLASS_PARAMETERS)
+    elif mdname == "KPiSPalanoPennington":
+        kw["massDepParams"] = (float(md.get("MMax", 2.4)),)     # massDependence.cc:750-759
     if mdname == "binned":
         b = md.get("bounds")
         if not isinstance(b, list) or len(b) != 2 or not b[0] <= b[1]:

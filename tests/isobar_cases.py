@@ -114,3 +114,35 @@ def neutral_waves():
 
 def neutral_events(n, seed=0):
     return synth.three_pion_events(n, seed=seed, masses=NEUTRAL_MASSES)
+
+
+# K- pi+ pi-: slot 0 K-, slot 1 pi+, slot 2 pi- (no identical particles)
+KPIPI_SPECIES = [0, 1, 2]
+KPIPI_NAMES = ["K-", "pi+", "pi-"]
+KPIPI_MASSES = (0.493677, 0.13957039, 0.13957039)
+# LASS-type K pi S-wave parameters: a, r, M0, G0, phiF, phiR, phiRsin, F, R, MMax
+GLASS = (1.95, 1.76, 1.435, 0.279, 0.0, 0.0, 0.0, 1.0, 1.0, 1.9)
+
+
+def kpipi_waves():
+    """K- pi+ pi- waves: K*(892) pi S, the K pi S-wave (LASS and
+    Palano-Pennington forms) pi S, and rho(770) K S."""
+    specs = [
+        (2, +1, 0, +1, 0, 2, 2, 2, O.MASSDEP_REL_BW, 0.8955, 0.0473, (0, 1), 2, False, ()),
+        (0, -1, 0, +1, 0, 0, 0, 0, O.MASSDEP_KPIS_GLASS, 0.0, 0.0, (0, 1), 2, False, GLASS),
+        (0, -1, 0, +1, 0, 0, 0, 0, O.MASSDEP_KPIS_PALANO, 0.0, 0.0, (1, 0), 2, False, ()),
+        (2, +1, 2, +1, 0, 2, 2, 2, O.MASSDEP_REL_BW, M_RHO, G_RHO, (1, 2), 0, True, ()),
+    ]
+    md = {O.MASSDEP_REL_BW: "relativisticBreitWigner", O.MASSDEP_KPIS_GLASS: "KPiSGLASS",
+          O.MASSDEP_KPIS_PALANO: "KPiSPalanoPennington"}
+    out = []
+    for J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first, par in specs:
+        ow = O.wave(J, P, M, r, L, S, j, l, m, mass, width, dau, bach, first, mass_dep_params=par)
+        kw = dict(J=J, P=P, M=M, refl=r, L=L, S=S, isobarJ=j, isobarL=l, massDependence=md[m], isobarMass=mass,
+                  isobarWidth=width, isobarDaughters=dau, bachelor=bach, bachelorFirst=first, massDepParams=par)
+        out.append((ow, kw))
+    return out
+
+
+def kpipi_events(n, seed=0):
+    return synth.three_pion_events(n, seed=seed, masses=KPIPI_MASSES, m_lo=1.0, m_hi=2.4)

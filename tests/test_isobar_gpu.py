@@ -263,3 +263,18 @@ def test_golden_fixture():
     B.enableIsospinSymmetrization(True)
     got = B.amplitudes(gold["neutral_beam"], gold["neutral_fs"])
     assert np.all(rel_err(gold["neutral_isospin"], got) < tolerances(nws, TOL))
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_kpipi_matches_oracle(dtype):
+    """K- pi+ pi- with the K pi S-wave forms (massDependence.cc:700-828)."""
+    from isobar_cases import KPIPI_NAMES, KPIPI_SPECIES, kpipi_events, kpipi_waves
+    ws = kpipi_waves()
+    beam, fs, masses, mb = kpipi_events(2000, seed=19)
+    A = I.isobarHelicityAmplitudes()
+    A.setFinalState(KPIPI_NAMES, masses, mb)
+    for _, kw in ws:
+        A.addWave(**kw)
+    got = A.amplitudes(beam, fs, dtype=dtype).astype(np.complex128)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, KPIPI_SPECIES)
+    assert np.all(rel_err(ref, got) < tolerances(ws, TOL if dtype == "complex128" else TOL32))

@@ -42,6 +42,8 @@ def _c_waves(ws):
                               bachelor=kw["bachelor"], bachelorFirst=int(kw.get("bachelorFirst", False)),
                               isospin=kw.get("isospin", 2), isobarIsospin=kw.get("isobarIsospin", 0),
                               binLower=kw.get("bounds", (0.0, 0.0))[0], binUpper=kw.get("bounds", (0.0, 0.0))[1])
+        for j, v in enumerate(kw.get("massDepParams", ())):
+            arr[k].massDepParams[j] = v
     return arr
 
 
@@ -142,7 +144,7 @@ def test_wave_checks_and_state():
     with pytest.raises(N.PwaError):
         A.nmbSymTerms(0)                            # no wave yet
     bad = [dict(kw, J=3), dict(kw, M=-2), dict(kw, P=0), dict(kw, L=16), dict(kw, bachelor=1),
-           dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=11), dict(kw, isobarWidth=0.0),
+           dict(kw, isobarDaughters=(0, 3)), dict(kw, massDependence=13), dict(kw, isobarWidth=0.0),
            dict(kw, M=6)]
     for b in bad:
         with pytest.raises(N.PwaError) as e:
@@ -249,3 +251,16 @@ def test_isospin_api():
     assert e.value.status == 2
     with pytest.raises(N.PwaError):
         B.setFinalState(["a", "b", "c"], [0.1, 0.2, 0.3], 0.1, isospins=[(1, 3, 1)] * 3)   # |2I_3| > 2I
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_kernel_arithmetic_kpipi(shim, dtype):
+    """K- pi+ pi- with the K pi S-wave forms (massDependence.cc:700-828)."""
+    from isobar_cases import KPIPI_SPECIES, kpipi_events, kpipi_waves
+    ws = kpipi_waves()
+    beam, fs, masses, mb = kpipi_events(1500, seed=12)
+    ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, KPIPI_SPECIES)
+    got = _shim_amps(shim, ws, beam, fs, masses, mb, {"species": KPIPI_SPECIES}, dtype)
+    tol = TOL if dtype == np.complex128 else TOL32
+    assert np.all(np.abs(ref).max(axis=1) > 0)
+    assert np.all(rel_err(ref, got.astype(np.complex128)) < tolerances(ws, tol))

@@ -248,3 +248,19 @@ def test_golden_fixture():
     for k in ("helicity", "canonical", "neutral_isospin"):
         scale = np.abs(gold[k]).max(axis=1, keepdims=True) + 1e-300
         assert np.all(np.abs(now[k] - gold[k]) <= 1e-12 * scale), k
+
+
+def test_kpi_s_wave_unitarity():
+    """the K pi S-wave forms (massDependence.cc:700-828): LASS with F = R = 1
+    and no phases is elastic, |1 + 2 i t| = 1 for t = amp 2q / M; the
+    Palano-Pennington T_11 obeys Im(1 / T_11) = -rho_Kpi below the K eta
+    threshold (the K eta channel then only renormalises K_11)."""
+    from isobar_cases import GLASS
+    m = np.linspace(0.7, 1.85, 60)
+    q = np.sqrt(O.breakup_momentum_squared(m, O.M_K_CHARGED, O.M_PI_CHARGED))
+    t = O.kpi_s_glass(m, GLASS) * 2 * q / m
+    assert np.allclose(np.abs(1 + 2j * t), 1.0, atol=1e-12)
+    m = np.linspace(0.65, 1.03, 40)
+    T = O.kpi_s_palano(m)
+    rho = (2 * O._q_complex2(m, O.M_K_CHARGED, O.M_PI_CHARGED) / m).real
+    assert np.allclose((1 / T).imag, -rho, rtol=1e-10, atol=1e-13)

@@ -122,8 +122,8 @@ def test_refusals(files, tmp_path):
     with pytest.raises(NotImplementedError):
         keyfile.waveFromKeyFile(tmp_path / "four.key", t, ["pi-", "pi+", "pi-"])
     (tmp_path / "md.key").write_text(KEY_RHO.replace("L = 2; S = 0;", 'L = 2; S = 0; massDep : { name = '
-                                                     '"KPiSGLASS"; };'))
-    with pytest.raises(NotImplementedError, match="KPiSGLASS"):
+                                                     '"someOtherMassDependence"; };'))
+    with pytest.raises(NotImplementedError, match="someOtherMassDependence"):
         keyfile.waveFromKeyFile(tmp_path / "md.key", t, ["pi-", "pi+", "pi-"])
     (tmp_path / "iso.key").write_text(KEY_RHO.replace('name = "rho(770)"', 'name = "rho(1450)"'))
     with pytest.raises(ValueError, match="particle table"):
@@ -146,4 +146,24 @@ def test_binned_mass_dependence_key(files, tmp_path):
     assert kw["massDependence"] == "binned" and kw["bounds"] == (0.6, 0.9)
     (tmp_path / "bad.key").write_text(key.replace("[0.6, 0.9]", "[0.9, 0.6]"))
     with pytest.raises(ValueError, match="bounds"):
+        keyfile.waveFromKeyFile(tmp_path / "bad.key", t, ["pi-", "pi+", "pi-"])
+
+
+def test_kpi_s_wave_keys(files, tmp_path):
+    """KPiSGLASS takes its ten parameters from the massDep group
+    (massDependence.cc:660-686); KPiSPalanoPennington its MMax (default 2.4)."""
+    t = keyfile.readParticleTable(files / "table.txt")
+    glass = ('massDep : { name = "KPiSGLASS"; a = 1.95; r = 1.76; M0 = 1.435; G0 = 0.279; phiF = 0.0; '
+             'phiR = 0.0; phiRsin = 0.0; F = 1.0; R = 1.0; MMax = 1.9; tag = "lass"; };')
+    (tmp_path / "g.key").write_text(KEY_RHO.replace("L = 2; S = 0;", "L = 2; S = 0; " + glass))
+    kw, _ = keyfile.waveFromKeyFile(tmp_path / "g.key", t, ["pi-", "pi+", "pi-"])
+    assert kw["massDependence"] == "KPiSGLASS" and kw["massDepParams"] == (1.95, 1.76, 1.435, 0.279, 0.0, 0.0,
+                                                                         0.0, 1.0, 1.0, 1.9)
+    (tmp_path / "p.key").write_text(KEY_RHO.replace("L = 2; S = 0;", 'L = 2; S = 0; massDep : { name = '
+                                                    '"KPiSPalanoPennington"; };'))
+    kw, _ = keyfile.waveFromKeyFile(tmp_path / "p.key", t, ["pi-", "pi+", "pi-"])
+    assert kw["massDepParams"] == (2.4,)
+    (tmp_path / "bad.key").write_text(KEY_RHO.replace("L = 2; S = 0;", 'L = 2; S = 0; massDep : { name = '
+                                                      '"KPiSGLASS"; a = 1.0; };'))
+    with pytest.raises(ValueError, match="KPiSGLASS needs"):
         keyfile.waveFromKeyFile(tmp_path / "bad.key", t, ["pi-", "pi+", "pi-"])
