@@ -1,13 +1,16 @@
 // isobar_math.cuh -- per-event arithmetic of the three-body isobar decay
-// amplitudes in the helicity formalism, FP64, written once for the GPU
-// kernel (isobar.cu).  The functions are plain C++ on POD views of the wave
-// plan, so the same source also compiles as host code (the CPU tests compile
-// it with g++ to check the arithmetic against the FP64 oracle without a GPU).
+// amplitudes in the helicity or canonical formalism, written once for the
+// GPU kernel (isobar.cu): frames and kinematics in FP64, the per-wave part in
+// FP64 or FP32 (template parameter).  The functions are plain C++ on POD
+// views of the wave plan, so the same source also compiles as host code (the
+// CPU tests compile it with g++ to check the arithmetic against the FP64
+// oracle without a GPU).
 //
 // Reference: isobarHelicityAmplitude (decayAmplitude/isobarHelicityAmplitude.cc:
-// 64-195), isobarAmplitude (decayAmplitude/isobarAmplitude.cc:98-262),
-// mass dependences (decayAmplitude/massDependence.cc:169-320), barrier
-// factors and Breit-Wigner (utilities/physUtils.hpp:75-300).
+// 64-195), isobarCanonicalAmplitude (decayAmplitude/isobarCanonicalAmplitude.cc:
+// 64-190), isobarAmplitude (decayAmplitude/isobarAmplitude.cc:98-330), mass
+// dependences (decayAmplitude/massDependence.cc:169-862), barrier factors and
+// Breit-Wigner (utilities/physUtils.hpp:75-300).
 //
 // Frames.  The reference reaches the Gottfried-Jackson frame by a rotation
 // that puts beam x X on the y axis, a boost into the X rest frame and a
@@ -15,7 +18,9 @@
 // The result is the orthonormal basis z = beam direction in the X rest
 // frame, y = unit(beam x X) in the lab (a boost along X keeps the components
 // perpendicular to X), x = y x z; here the final-state momenta are boosted
-// into the X rest frame once and projected on that basis.  The isobar's
+// into the X rest frame and projected on that basis, once per event and
+// once more per symmetrisation term that exchanges particles of different
+// mass (the term keeps each slot's mass, so X changes).  The isobar's
 // helicity frame (isobarHelicityAmplitude.cc:64-84) is likewise the basis
 // z = isobar direction, y = unit(z_GJ x isobar), x = y x z followed by a boost
 // along z.  In the measure-zero case of an isobar along z_GJ (y undefined)
