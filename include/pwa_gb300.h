@@ -514,6 +514,9 @@ int pwa_isobar_set_formalism(pwa_isobar* A, int formalism);
  * default stream); calls with device buffers are then asynchronous in stream
  * order, calls with host buffers still return with the results in place */
 int pwa_isobar_set_stream(pwa_isobar* A, void* cudaStream);
+/* no reference counterpart: host-buffer calls process at most this many
+ * events per device pass (0, the default: 1 GiB of device buffers) */
+int pwa_isobar_set_chunk_events(pwa_isobar* A, uint64_t events);
 /* isospin symmetrisation (isobarDecayTopology::getIsospinSymmetrization,
  * isobarDecayTopology.cc:505-630; isobarAmplitude::enableIsospinSymmetrization):
  * the final-state particles' 2I, 2I_3 and intrinsic parities; enabling it

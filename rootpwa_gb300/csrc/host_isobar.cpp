@@ -12,6 +12,7 @@ struct pwa_isobar {
 	bool finalState = false;
 	bool reflBasis = true, bose = true, spaceInversion = false, reflection = false, canonical = false;
 	bool isospinSet = false, isospinSym = false;
+	uint64_t chunkEvents = 0;  // host-buffer calls: events per device pass (0: 1 GiB of buffers)
 	iso::FsIsospin isospin{};
 	std::vector<pwa_isobar_wave> waves;
 	iso::Plan plan;
@@ -150,6 +151,14 @@ int pwa_isobar_set_formalism(pwa_isobar* A, int formalism)
 	return kOk;
 }
 
+int pwa_isobar_set_chunk_events(pwa_isobar* A, uint64_t events)
+{
+	if (!A)
+		return setError(kErrArg, "null argument");
+	A->chunkEvents = events;
+	return kOk;
+}
+
 int pwa_isobar_set_options(pwa_isobar* A, int reflectivityBasis, int boseSymmetrize, int spaceInversion, int reflection)
 {
 	if (!A)
@@ -254,29 +263,39 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 	}
 	if (A->dirty)
 		PWA_TRY(uploadPlan(A));
-	const double* dBeam = beam;
-	const double* dFs = fs;
-	void* dAmps = amps;
 	if (memory == PWA_MEMORY_HOST) {
-		PWA_TRY(A->dIn.ensure(n * 12 * sizeof(double), "isobar event buffer"));
-		PWA_TRY(A->dOut.ensure(W * n * ampBytes, "isobar amplitude buffer"));
+		// slabs of events: rows [3][slab] and [9][slab] taken from the host's
+		// [3][n] and [9][n], amplitude rows [W][slab] put back into [W][n], so
+		// the device buffers stay bounded
+		const uint64_t perEvent = 12 * sizeof(double) + W * ampBytes;
+		const uint64_t slab = std::min<uint64_t>(n, A->chunkEvents ? A->chunkEvents
+		                                                              : std::max<uint64_t>(1, (1ull << 30) / perEvent));
+		PWA_TRY(A->dIn.ensure(slab * 12 * sizeof(double), "isobar event buffer"));
+		PWA_TRY(A->dOut.ensure(W * slab * ampBytes, "isobar amplitude buffer"));
 		double* in = A->dIn.as<double>();
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(in, beam, n * 3 * sizeof(double), cudaMemcpyHostToDevice, A->stream),
-		                  "beam upload"));
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(in + 3 * n, fs, n * 9 * sizeof(double), cudaMemcpyHostToDevice, A->stream),
-		                  "final-state upload"));
-		dBeam = in;
-		dFs = in + 3 * n;
-		dAmps = A->dOut.p;
-	} else if (!A->userStream) {
-		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device momenta"));
+		// one copy per row (no pitch limit for long rows)
+		for (uint64_t e0 = 0; e0 < n; e0 += slab) {
+			const uint64_t m = std::min(slab, n - e0);
+			for (uint64_t r = 0; r < 12; ++r) {
+				const double* src = (r < 3 ? beam + r * n : fs + (r - 3) * n) + e0;
+				PWA_TRY(cudaCheck(cudaMemcpyAsync(in + r * m, src, m * sizeof(double), cudaMemcpyHostToDevice,
+				                                  A->stream),
+				                  "momentum upload"));
+			}
+			PWA_TRY(launchIsobarAmplitudes(A->devView, in, in + 3 * m, m, A->dOut.p, fp32, A->stream));
+			for (uint64_t w = 0; w < W; ++w)
+				PWA_TRY(cudaCheck(cudaMemcpyAsync(static_cast<unsigned char*>(amps) + (w * n + e0) * ampBytes,
+				                                  static_cast<const unsigned char*>(A->dOut.p) + w * m * ampBytes,
+				                                  m * ampBytes, cudaMemcpyDeviceToHost, A->stream),
+				                  "amplitude download"));
+		}
+		return cudaCheck(cudaStreamSynchronize(A->stream), "isobar amplitudes");
 	}
-	PWA_TRY(launchIsobarAmplitudes(A->devView, dBeam, dFs, n, dAmps, fp32, A->stream));
-	if (memory == PWA_MEMORY_HOST)
-		PWA_TRY(cudaCheck(cudaMemcpyAsync(amps, dAmps, W * n * ampBytes, cudaMemcpyDeviceToHost, A->stream),
-		                  "amplitude download"));
+	if (!A->userStream)
+		PWA_TRY(cudaCheck(cudaDeviceSynchronize(), "synchronise before reading device momenta"));
+	PWA_TRY(launchIsobarAmplitudes(A->devView, beam, fs, n, amps, fp32, A->stream));
 	// on the caller's stream, device-buffer calls stay asynchronous (stream order)
-	if (memory == PWA_MEMORY_DEVICE && A->userStream)
+	if (A->userStream)
 		return kOk;
 	return cudaCheck(cudaStreamSynchronize(A->stream), "isobar amplitudes");
 }

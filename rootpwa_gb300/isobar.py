@@ -133,6 +133,11 @@ class isobarHelicityAmplitudes:
         self._async = True
         self._stream = h or 0
 
+    def setChunkEvents(self, events):
+        """host-buffer calls process at most this many events per device pass
+        (0: 1 GiB of device buffers)."""
+        N.call("pwa_isobar_set_chunk_events", self._h, int(events))
+
     # -- waves ---------------------------------------------------------------------
     def addWave(self, J, P, M, refl, L, S, isobarJ, isobarL, massDependence="flat", isobarMass=0.0,
                 isobarWidth=0.0, isobarDaughters=(0, 1), bachelor=2, bachelorFirst=False, isobarS=0,

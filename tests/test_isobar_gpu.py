@@ -278,3 +278,17 @@ def test_kpipi_matches_oracle(dtype):
     got = A.amplitudes(beam, fs, dtype=dtype).astype(np.complex128)
     ref = O.amplitudes([w for w, _ in ws], beam, fs, masses, mb, KPIPI_SPECIES)
     assert np.all(rel_err(ref, got) < tolerances(ws, TOL if dtype == "complex128" else TOL32))
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_host_buffers_in_slabs(dtype):
+    """host-buffer calls split into device passes of at most chunk events
+    (pwa_isobar_set_chunk_events) give the single-pass result bit for bit."""
+    ws = waves()
+    beam, fs, masses, mb = events(4099, seed=20)
+    A = _amp(ws, masses, mb)
+    whole = A.amplitudes(beam, fs, dtype=dtype)
+    A.setChunkEvents(1000)
+    assert np.array_equal(A.amplitudes(beam, fs, dtype=dtype), whole)
+    A.setChunkEvents(1)
+    assert np.array_equal(A.amplitudes(beam[:7], fs[:, :7], dtype=dtype), whole[:, :7])
