@@ -202,6 +202,12 @@ class isobarHelicityAmplitudes:
         t = N.COMPLEX64 if dtype == "complex64" else N.COMPLEX128
         if hasattr(beam, "__cuda_array_interface__"):
             import torch
+            if not hasattr(fs, "__cuda_array_interface__"):
+                raise ValueError("beam and fs must both be CUDA tensors or both host arrays")
+            # the kernel reads N events from every row: the shapes must agree
+            # (device buffer sizes cannot be checked behind the C ABI)
+            if beam.dim() != 2 or beam.shape[1] != 3 or tuple(fs.shape) != (3, beam.shape[0], 3):
+                raise ValueError("beam must be (N, 3) and fs (3, N, 3)")
             b = beam.to(torch.float64).t().contiguous()                  # [3][N]
             f = fs.to(torch.float64).permute(0, 2, 1).contiguous()       # [3][3][N]
             n = b.shape[1]
@@ -216,10 +222,12 @@ class isobarHelicityAmplitudes:
             N.call("pwa_isobar_amplitudes", self._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
                    C.c_void_p(out.data_ptr()), t, N.MEMORY_DEVICE)
             return out
-        b = np.ascontiguousarray(np.asarray(beam, dtype=np.float64).T)
-        f = np.ascontiguousarray(np.transpose(np.asarray(fs, dtype=np.float64), (0, 2, 1)))
-        if b.shape[0] != 3 or f.shape[:2] != (3, 3) or f.shape[2] != b.shape[1]:
+        beam = np.asarray(beam, dtype=np.float64)
+        fs = np.asarray(fs, dtype=np.float64)
+        if beam.ndim != 2 or beam.shape[1] != 3 or fs.shape != (3, beam.shape[0], 3):
             raise ValueError("beam must be (N, 3) and fs (3, N, 3)")
+        b = np.ascontiguousarray(beam.T)
+        f = np.ascontiguousarray(np.transpose(fs, (0, 2, 1)))
         n = b.shape[1]
         out = np.empty((W, n), dtype=np.dtype(dtype))
         N.call("pwa_isobar_amplitudes", self._h, b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), n,

@@ -264,3 +264,16 @@ def test_kernel_arithmetic_kpipi(shim, dtype):
     tol = TOL if dtype == np.complex128 else TOL32
     assert np.all(np.abs(ref).max(axis=1) > 0)
     assert np.all(rel_err(ref, got.astype(np.complex128)) < tolerances(ws, tol))
+
+
+def test_shape_checks():
+    """mismatched event counts are refused before any buffer is read."""
+    A = I.isobarHelicityAmplitudes()
+    A.setFinalState(NAMES, [0.1396] * 3, 0.1396)
+    A.addWave(**waves()[0][1])
+    with pytest.raises(ValueError):
+        A.amplitudes(np.zeros((5, 3)), np.zeros((3, 4, 3)))
+    with pytest.raises(ValueError):
+        A.amplitudes(np.zeros((5, 2)), np.zeros((3, 5, 3)))
+    with pytest.raises(ValueError):
+        A.amplitudes(np.zeros((5, 3)), np.zeros((2, 5, 3)))
