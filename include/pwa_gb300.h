@@ -539,6 +539,14 @@ int pwa_isobar_nmb_sym_terms(const pwa_isobar* A, uint32_t wave, uint32_t* n);
  * PWA_MEMORY_HOST or PWA_MEMORY_DEVICE for all three buffers. */
 int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, uint64_t nEvents, void* amps,
                           int ampType, int memory);
+/* calcAmplitudes (pyInterface/scripts/calcAmplitudes.py): the amplitudes of
+ * every wave for host momenta (layout as above), computed on the GPU in slabs
+ * and written as one raw amplitude file (pwa_ampfile_*): complex64 rows named
+ * waveNames[W], binning variables "mass" (the final-state mass) and the
+ * caller's nVars rows vars [nVars][nEvents] */
+int pwa_isobar_write_amp_file(pwa_isobar* A, const char* path, const char* const* waveNames, const double* beam,
+                              const double* fs, uint64_t nEvents, uint32_t nVars, const char* const* varNames,
+                              const double* vars);
 /* host utilities: clebschGordanCoeff (utilities/spinUtils.hpp:241-330),
  * dFunction (utilities/dFunction.hpp:52-170), barrierFactor with the
  * 0.1973 GeV/c scale (utilities/physUtils.hpp:200-275); arguments doubled */

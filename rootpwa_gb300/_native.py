@@ -168,6 +168,7 @@ SIGNATURES = {
     "pwa_isobar_set_stream": (i, [vp, vp]),
     "pwa_isobar_set_formalism": (i, [vp, i]),
     "pwa_isobar_set_chunk_events": (i, [vp, u64]),
+    "pwa_isobar_write_amp_file": (i, [vp, cc, C.POINTER(cc), vp, vp, u64, u32, C.POINTER(cc), vp]),
     "pwa_isobar_add_wave": (i, [vp, C.POINTER(IsobarWave)]),
     "pwa_isobar_nmb_waves": (i, [vp, C.POINTER(u32)]),
     "pwa_isobar_nmb_sym_terms": (i, [vp, u32, C.POINTER(u32)]),

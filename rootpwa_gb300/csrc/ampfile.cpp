@@ -212,14 +212,14 @@ int ampFileToDevice(const AmpFile& f, uint64_t offset, uint64_t bytes, void* dst
 
 using namespace pwa;
 
-extern "C" int pwa_ampfile_write(const char* path, uint32_t nWaves, const char* const* waveNames, uint64_t nEvents,
-                                 const void* amps, uint32_t nVars, const char* const* varNames, const double* vars)
+namespace pwa {
+
+// header of an amplitude file up to its data block (padded to the 4096-byte
+// boundary); names[0 .. nWaves) are the waves, the rest the binning variables
+int ampFileHeader(uint32_t nWaves, uint32_t nVars, const char* const* names, uint64_t nEvents,
+                  std::vector<unsigned char>& h)
 {
-	if (!path || (nWaves && (!waveNames || !amps)) || (nVars && (!varNames || !vars)))
-		return setError(kErrArg, "pwa_ampfile_write: null argument");
-	if (nWaves == 0)
-		return setError(kErrArg, "pwa_ampfile_write: no waves");
-	std::vector<unsigned char> h(kMagic, kMagic + 8);
+	h.assign(kMagic, kMagic + 8);
 	put<uint32_t>(h, kVersion);
 	put<uint32_t>(h, nWaves);
 	put<uint32_t>(h, nVars);
@@ -227,18 +227,52 @@ extern "C" int pwa_ampfile_write(const char* path, uint32_t nWaves, const char* 
 	put<uint64_t>(h, nEvents);
 	put<uint64_t>(h, 0);  // data offset, filled below
 	for (uint32_t i = 0; i < nWaves + nVars; ++i) {
-		const char* name = i < nWaves ? waveNames[i] : varNames[i - nWaves];
+		const char* name = names[i];
 		if (!name)
-			return setError(kErrArg, "pwa_ampfile_write: null name");
+			return setError(kErrArg, "amplitude file: null name");
 		const size_t len = std::strlen(name);
 		if (len == 0 || len > 65535)
-			return setError(kErrArg, "pwa_ampfile_write: names must have 1..65535 bytes");
+			return setError(kErrArg, "amplitude file: names must have 1..65535 bytes");
 		put<uint16_t>(h, (uint16_t)len);
 		h.insert(h.end(), name, name + len);
 	}
 	const uint64_t dataOffset = (h.size() + kAlign - 1) / kAlign * kAlign;
 	std::memcpy(h.data() + 32, &dataOffset, 8);
 	h.resize(dataOffset, 0);
+	return kOk;
+}
+
+// bytes to file offset (pwrite, restarted on EINTR and short writes)
+int ampFilePwrite(int fd, const void* p, size_t bytes, uint64_t offset, const char* path)
+{
+	const unsigned char* c = static_cast<const unsigned char*>(p);
+	while (bytes > 0) {
+		const ssize_t w = ::pwrite(fd, c, bytes, (off_t)offset);
+		if (w < 0) {
+			if (errno == EINTR)
+				continue;
+			return setError(kErrIo, std::string("write failed for '") + path + "': " + std::strerror(errno));
+		}
+		c += w;
+		bytes -= (size_t)w;
+		offset += (uint64_t)w;
+	}
+	return kOk;
+}
+
+}  // namespace pwa
+
+extern "C" int pwa_ampfile_write(const char* path, uint32_t nWaves, const char* const* waveNames, uint64_t nEvents,
+                                 const void* amps, uint32_t nVars, const char* const* varNames, const double* vars)
+{
+	if (!path || (nWaves && (!waveNames || !amps)) || (nVars && (!varNames || !vars)))
+		return setError(kErrArg, "pwa_ampfile_write: null argument");
+	if (nWaves == 0)
+		return setError(kErrArg, "pwa_ampfile_write: no waves");
+	std::vector<const char*> names(waveNames, waveNames + nWaves);
+	names.insert(names.end(), varNames, varNames + nVars);
+	std::vector<unsigned char> h;
+	PWA_CHECK(ampFileHeader(nWaves, nVars, names.data(), nEvents, h));
 	const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
 	if (fd < 0)
 		return setError(kErrIo, std::string("cannot create '") + path + "': " + std::strerror(errno));

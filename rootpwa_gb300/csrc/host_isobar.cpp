@@ -5,6 +5,9 @@
 #include "host_common.h"
 #include "isobar_plan.h"
 
+#include <fcntl.h>
+#include <unistd.h>
+
 struct pwa_isobar {
 	double masses[3] = {0.0, 0.0, 0.0};
 	int32_t species[3] = {0, 1, 2};
@@ -298,6 +301,68 @@ int pwa_isobar_amplitudes(pwa_isobar* A, const double* beam, const double* fs, u
 	if (A->userStream)
 		return kOk;
 	return cudaCheck(cudaStreamSynchronize(A->stream), "isobar amplitudes");
+}
+
+// calcAmplitudes (pyInterface/scripts/calcAmplitudes.py, which writes one
+// amplitude tree per wave): the amplitudes of every wave for host momenta,
+// computed in slabs and written as complex64 rows of one raw amplitude file,
+// with the final-state mass ("mass") and the caller's variables as binning
+// variables
+int pwa_isobar_write_amp_file(pwa_isobar* A, const char* path, const char* const* waveNames, const double* beam,
+                              const double* fs, uint64_t n, uint32_t nVars, const char* const* varNames,
+                              const double* vars)
+{
+	if (!A || !path || !waveNames || (n && (!beam || !fs)) || (nVars && (!varNames || !vars)))
+		return setError(kErrArg, "null argument");
+	if (!A->finalState)
+		return setError(kErrState, "set the final state first");
+	const uint32_t W = (uint32_t)A->waves.size();
+	if (W == 0)
+		return setError(kErrState, "no waves");
+	std::vector<const char*> names(waveNames, waveNames + W);
+	names.push_back("mass");
+	for (uint32_t v = 0; v < nVars; ++v)
+		names.push_back(varNames[v]);
+	std::vector<unsigned char> header;
+	PWA_TRY(ampFileHeader(W, nVars + 1, names.data(), n, header));
+	const uint64_t data = header.size();
+	const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+	if (fd < 0)
+		return setError(kErrIo, std::string("cannot create '") + path + "': " + std::strerror(errno));
+	struct Closer {
+		int fd;
+		~Closer() { ::close(fd); }
+	} closer{fd};
+	PWA_TRY(ampFilePwrite(fd, header.data(), header.size(), 0, path));
+	const uint64_t slab = std::min<uint64_t>(std::max<uint64_t>(n, 1), A->chunkEvents ? A->chunkEvents : 1u << 20);
+	std::vector<double> b(3 * slab), f(9 * slab), mass(slab);
+	std::vector<float> amps(2 * (size_t)W * slab);
+	for (uint64_t e0 = 0; e0 < n; e0 += slab) {
+		const uint64_t m = std::min(slab, n - e0);
+		for (int r = 0; r < 3; ++r)
+			std::copy(beam + r * n + e0, beam + r * n + e0 + m, b.begin() + r * m);
+		for (int r = 0; r < 9; ++r)
+			std::copy(fs + r * n + e0, fs + r * n + e0 + m, f.begin() + r * m);
+		PWA_TRY(pwa_isobar_amplitudes(A, b.data(), f.data(), m, amps.data(), PWA_COMPLEX64, PWA_MEMORY_HOST));
+		for (uint32_t w = 0; w < W; ++w)
+			PWA_TRY(ampFilePwrite(fd, amps.data() + 2 * (size_t)w * m, m * 8, data + ((uint64_t)w * n + e0) * 8, path));
+		// final-state mass from the momenta and the particle masses
+		for (uint64_t e = 0; e < m; ++e) {
+			double E = 0, px = 0, py = 0, pz = 0;
+			for (int i = 0; i < 3; ++i) {
+				const double x = f[(3 * i) * m + e], y = f[(3 * i + 1) * m + e], z = f[(3 * i + 2) * m + e];
+				E += std::sqrt(A->masses[i] * A->masses[i] + x * x + y * y + z * z);
+				px += x;
+				py += y;
+				pz += z;
+			}
+			mass[e] = std::sqrt(std::max(0.0, E * E - px * px - py * py - pz * pz));
+		}
+		PWA_TRY(ampFilePwrite(fd, mass.data(), m * 8, data + (uint64_t)W * n * 8 + e0 * 8, path));
+	}
+	for (uint32_t v = 0; v < nVars; ++v)
+		PWA_TRY(ampFilePwrite(fd, vars + (uint64_t)v * n, n * 8, data + ((uint64_t)W + 1 + v) * n * 8, path));
+	return kOk;
 }
 
 int pwa_clebsch_gordan(int32_t j1, int32_t m1, int32_t j2, int32_t m2, int32_t J, int32_t M, double* out)

@@ -310,6 +310,11 @@ struct AmpFile {
 int ampFileOpen(const char* path, AmpFile& f);
 // file bytes [offset, offset + bytes) -> device memory (synchronises s)
 int ampFileToDevice(const AmpFile& f, uint64_t offset, uint64_t bytes, void* dst, cudaStream_t s);
+// header bytes of an amplitude file up to its data block (names: the waves,
+// then the binning variables) and positioned writes into an open file
+int ampFileHeader(uint32_t nWaves, uint32_t nVars, const char* const* names, uint64_t nEvents,
+                  std::vector<unsigned char>& header);
+int ampFilePwrite(int fd, const void* p, size_t bytes, uint64_t offset, const char* path);
 
 // ---------------------------------------------------------------------------
 // Three-body isobar amplitudes (isobar.cu, plan in isobar_plan.h)

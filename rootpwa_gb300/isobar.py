@@ -244,6 +244,32 @@ class isobarCanonicalAmplitudes(isobarHelicityAmplitudes):
         N.call("pwa_isobar_set_formalism", self._h, 1)
 
 
+def _cstrs(names):
+    return (C.c_char_p * len(names))(*[n.encode() for n in names])
+
+
+def writeAmplitudeFileNative(amp, path, beam, fs, waveNames=None, binVars=None):
+    """pwa_isobar_write_amp_file: the calcAmplitudes step in native code --
+    amplitudes of host momenta beam (N, 3), fs (3, N, 3) computed in slabs and
+    streamed into one raw amplitude file with the final-state mass and
+    binVars {name: [N]} as binning variables.  Returns the wave names."""
+    beam = np.asarray(beam, dtype=np.float64)
+    fs = np.asarray(fs, dtype=np.float64)
+    if beam.ndim != 2 or beam.shape[1] != 3 or fs.shape != (3, beam.shape[0], 3):
+        raise ValueError("beam must be (N, 3) and fs (3, N, 3)")
+    n = beam.shape[0]
+    names = waveNames or [amp.waveName(k) for k in range(amp.nmbWaves())]
+    b = np.ascontiguousarray(beam.T)
+    f = np.ascontiguousarray(np.transpose(fs, (0, 2, 1)))
+    binVars = binVars or {}
+    vn = list(binVars)
+    v = np.ascontiguousarray(np.stack([np.asarray(binVars[k], dtype=np.float64) for k in vn])) if vn else None
+    N.call("pwa_isobar_write_amp_file", amp._h, str(path).encode(), _cstrs(names), b.ctypes.data_as(C.c_void_p),
+           f.ctypes.data_as(C.c_void_p), n, len(vn), _cstrs(vn) if vn else None,
+           v.ctypes.data_as(C.c_void_p) if v is not None else None)
+    return names
+
+
 def finalStateMass(ev):
     """invariant mass of the final state of every event of an .evt file
     (readEvtFile), the usual on-the-fly binning variable ("mass")."""

@@ -292,3 +292,20 @@ def test_host_buffers_in_slabs(dtype):
     assert np.array_equal(A.amplitudes(beam, fs, dtype=dtype), whole)
     A.setChunkEvents(1)
     assert np.array_equal(A.amplitudes(beam[:7], fs[:, :7], dtype=dtype), whole[:, :7])
+
+
+def test_native_amplitude_file_equals_python_path(tmp_path):
+    """pwa_isobar_write_amp_file (slabs of 1,000 events) writes the same file,
+    byte for byte, as calcAmplitudes (one pass) for the same events."""
+    from rootpwa_gb300 import evtfile
+    ws = waves()[:6]
+    beam, fs, masses, mb = events(3500, seed=44)
+    evt = tmp_path / "ev.evt"
+    evtfile.writeEvtFile(evt, 9, beam, [9, 8, 9], fs)
+    ev = evtfile.readEvtFile(evt)
+    A = _amp(ws, ev["fs_masses"], ev["beam_mass"])
+    tp = np.random.default_rng(45).random(3500)
+    names = I.calcAmplitudes(A, evt, tmp_path / "py.amp", binVars={"tPrime": tp})
+    A.setChunkEvents(1000)
+    I.writeAmplitudeFileNative(A, tmp_path / "native.amp", ev["beam"], ev["fs"], names, {"tPrime": tp})
+    assert (tmp_path / "py.amp").read_bytes() == (tmp_path / "native.amp").read_bytes()

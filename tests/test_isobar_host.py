@@ -277,3 +277,20 @@ def test_shape_checks():
         A.amplitudes(np.zeros((5, 2)), np.zeros((3, 5, 3)))
     with pytest.raises(ValueError):
         A.amplitudes(np.zeros((5, 3)), np.zeros((2, 5, 3)))
+
+
+def test_native_amplitude_file_header_without_events(tmp_path):
+    """pwa_isobar_write_amp_file with no events writes a valid file (header,
+    the "mass" variable and the caller's variables) without touching the
+    GPU; argument and state errors are refused."""
+    from rootpwa_gb300 import ampFileInfo
+    A = I.isobarHelicityAmplitudes()
+    with pytest.raises(N.PwaError):
+        I.writeAmplitudeFileNative(A, tmp_path / "x.amp", np.zeros((0, 3)), np.zeros((3, 0, 3)), ["w"])
+    A.setFinalState(NAMES, [0.1396] * 3, 0.1396)
+    for _, kw in waves()[:3]:
+        A.addWave(**kw)
+    names = I.writeAmplitudeFileNative(A, tmp_path / "e.amp", np.zeros((0, 3)), np.zeros((3, 0, 3)),
+                                       binVars={"tPrime": np.zeros(0)})
+    waves_, n, vars_ = ampFileInfo(tmp_path / "e.amp")
+    assert waves_ == names and n == 0 and vars_ == ["mass", "tPrime"]
