@@ -351,12 +351,12 @@ int pwa_isobar_write_amp_file(pwa_isobar* A, const char* path, const char* const
 			double E = 0, px = 0, py = 0, pz = 0;
 			for (int i = 0; i < 3; ++i) {
 				const double x = f[(3 * i) * m + e], y = f[(3 * i + 1) * m + e], z = f[(3 * i + 2) * m + e];
-				E += std::sqrt(A->masses[i] * A->masses[i] + x * x + y * y + z * z);
+				E += std::sqrt(A->masses[i] * A->masses[i] + (x * x + y * y + z * z));
 				px += x;
 				py += y;
 				pz += z;
 			}
-			mass[e] = std::sqrt(std::max(0.0, E * E - px * px - py * py - pz * pz));
+			mass[e] = std::sqrt(std::max(0.0, E * E - (px * px + py * py + pz * pz)));
 		}
 		PWA_TRY(ampFilePwrite(fd, mass.data(), m * 8, data + (uint64_t)W * n * 8 + e0 * 8, path));
 	}
