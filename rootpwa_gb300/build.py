@@ -17,7 +17,9 @@ LIB = os.path.join(HERE, "libpwa_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+# host code: no FMA contraction, so that it rounds the same on x86-64 and
+# aarch64 hosts (gcc contracts a*b+c by default on aarch64)
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def _nvcc():

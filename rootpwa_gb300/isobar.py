@@ -199,7 +199,7 @@ class isobarHelicityAmplitudes:
         W = self.nmbWaves()
         if dtype not in ("complex128", "complex64"):
             raise ValueError("dtype must be complex128 or complex64")
-        t = N.COMPLEX64 if dtype == "complex64" else N.COMPLEX128
+        ampType = N.COMPLEX64 if dtype == "complex64" else N.COMPLEX128
         if hasattr(beam, "__cuda_array_interface__"):
             import torch
             if not hasattr(fs, "__cuda_array_interface__"):
@@ -217,10 +217,10 @@ class isobarHelicityAmplitudes:
                 # layout copies above and keep their memory until it has run
                 es = torch.cuda.ExternalStream(self._stream, device=b.device)
                 es.wait_stream(torch.cuda.current_stream(b.device))
-                for t in (b, f, out):
-                    t.record_stream(es)
+                for buf in (b, f, out):
+                    buf.record_stream(es)
             N.call("pwa_isobar_amplitudes", self._h, C.c_void_p(b.data_ptr()), C.c_void_p(f.data_ptr()), n,
-                   C.c_void_p(out.data_ptr()), t, N.MEMORY_DEVICE)
+                   C.c_void_p(out.data_ptr()), ampType, N.MEMORY_DEVICE)
             return out
         beam = np.asarray(beam, dtype=np.float64)
         fs = np.asarray(fs, dtype=np.float64)
@@ -231,7 +231,7 @@ class isobarHelicityAmplitudes:
         n = b.shape[1]
         out = np.empty((W, n), dtype=np.dtype(dtype))
         N.call("pwa_isobar_amplitudes", self._h, b.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p), n,
-               out.ctypes.data_as(C.c_void_p), t, N.MEMORY_HOST)
+               out.ctypes.data_as(C.c_void_p), ampType, N.MEMORY_HOST)
         return out
 
 
