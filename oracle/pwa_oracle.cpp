@@ -4,12 +4,14 @@
 // checker for the CUDA product (tests, the smoke check and the CPU-baseline leg
 // of bench.py).  Nothing in the product links, loads or calls this file.
 //
-// Parity status: the reference cannot be built here (ROOT, Boost.MultiArray,
-// Boost.Accumulators, libconfig are absent) and its own tests pin no likelihood,
-// gradient or integral numbers, so this restatement is "parity unpinned" at the
-// reference-test level.  It is pinned instead by the reference's ASCII integral
-// fixture (test/decayAmplitude/testIntegral.int, read and re-written bit-exactly),
-// by central finite differences, and by the analytic identities of
+// Parity status: pinned against the reference's own code.  `make ref` in this
+// directory compiles the reference's pwaLikelihood.cc and ampIntegralMatrix.cc
+// from their sources against local stand-ins for ROOT and Boost (ref_shim/),
+// and tests/test_ref_pinned.py finds this restatement bit for bit equal to them
+// (integrals, FdF / DoEval / Gradient, Hessian, parameter layout, on-the-fly
+// binning).  Also pinned by the reference's ASCII integral fixture
+// (test/decayAmplitude/testIntegral.int, read and re-written bit-exactly), by
+// central finite differences and by the analytic identities of
 // doc/tex/likelihood.tex.
 //
 // The summation semantics follow the reference exactly: event-major loops,

@@ -8,8 +8,9 @@
    Hessian) on seeded synthetic workloads, with a checksum of the generated
    inputs so that a change of the random streams is detected.
 
-Run from the repository root:  python tests/golden/make_golden.py
-(needs the reference checkout at /root/reference for step 1).
+Run from the repository root:
+    python tests/golden/make_golden.py [path to the reference checkout]
+(step 1 needs the reference checkout: the argument, else PWA_REFERENCE_DIR).
 """
 import os
 import shutil
@@ -25,7 +26,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 from rootpwa_gb300 import synth  # noqa: E402
 import helpers  # noqa: E402
 
-REF_FIXTURE = "/root/reference/test/decayAmplitude/testIntegral.int"
+REF_FIXTURE = os.path.join("test", "decayAmplitude", "testIntegral.int")
 
 GOLDEN_WORKLOADS = {
     "compass15_seed0": dict(name="compass15", seed=0),
@@ -57,8 +58,9 @@ def make(name, spec):
 
 
 def main():
-    if os.path.exists(REF_FIXTURE):
-        shutil.copyfile(REF_FIXTURE, os.path.join(HERE, "testIntegral.int"))
+    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PWA_REFERENCE_DIR")
+    if refdir and os.path.exists(os.path.join(refdir, REF_FIXTURE)):
+        shutil.copyfile(os.path.join(refdir, REF_FIXTURE), os.path.join(HERE, "testIntegral.int"))
     for name, spec in GOLDEN_WORKLOADS.items():
         make(name, spec)
 

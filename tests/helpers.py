@@ -11,21 +11,22 @@ F_RTOL = 1e-6          # relative error of the function value
 G_NORMWISE = 1e-6      # max |g - g_ref| / max |g_ref|
 
 
-def oracle_integrals(w):
-    """Normalisation (all MC events) and acceptance (accepted events) integrals."""
+def oracle_integrals(w, Integral=OracleIntegral):
+    """Normalisation (all MC events) and acceptance (accepted events) integrals
+    (Integral: the oracle's class, or the reference's own, oracle.ref.RefIntegral)."""
     mc = w["mc"].astype(np.complex128)
-    norm = OracleIntegral()
+    norm = Integral()
     assert norm.integrate(w["names"], mc)
-    acc = OracleIntegral()
+    acc = Integral()
     assert acc.integrate(w["names"], mc, in_bin=w["accepted"])
     return norm, acc
 
 
 def build_oracle(w, norm=None, acc=None, use_normalized=True, prior=0, cauchy_width=0.5, thresholds=None,
-                 mass_bin_center=0.0, acc_override=0):
+                 mass_bin_center=0.0, acc_override=0, Likelihood=OracleLikelihood):
     if norm is None:
         norm, acc = oracle_integrals(w)
-    L = OracleLikelihood(use_normalized, prior, cauchy_width)
+    L = Likelihood(use_normalized, prior, cauchy_width)
     assert L.init(w["names"], w["refl"], thresholds, w["rank"], mass_bin_center)
     assert L.addNormIntegral(norm)
     assert L.addAccIntegral(acc, acc_override)

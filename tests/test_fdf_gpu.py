@@ -34,10 +34,9 @@ def check_point(O, G, p, frtol=F_RTOL, gtol=G_NORMWISE):
     return f0, g0, f1, g1
 
 
-def test_golden_compass15():
-    from golden.make_golden import GOLDEN_WORKLOADS
-    gold = np.load(os.path.join(GOLDEN, "oracle_compass15_seed0.npz"))
-    w = synth.make_workload(**GOLDEN_WORKLOADS["compass15_seed0"])
+def _golden_gpu(fixture, spec):
+    gold = np.load(os.path.join(GOLDEN, fixture))
+    w = synth.make_workload(**spec)
     gn = R.ampIntegralMatrix()
     gn.setWaveNames(w["names"])
     gn.setMatrix(gold["norm_raw"])
@@ -46,27 +45,37 @@ def test_golden_compass15():
     ga.setWaveNames(w["names"])
     ga.setMatrix(gold["acc_raw"])
     ga.setNmbEvents(int(gold["acc_n"]))
-    G = helpers.build_gpu(w, gn, ga)
+    return gold, w, helpers.build_gpu(w, gn, ga)
+
+
+@pytest.mark.parametrize("source", ["ref", "oracle"])
+def test_golden_compass15(source):
+    """The single-bin config at full size (20,000 events, 15 waves) against
+    fixtures written by the reference's own code (ref_*, make_ref_golden.py)
+    and by the oracle (oracle_*): value, DoEval, gradient, Hessian, and the
+    GPU integrals of the same MC events against the fixture's raw sums."""
+    from golden.make_ref_golden import GOLDEN_WORKLOADS
+    gold, w, G = _golden_gpu("%s_compass15_seed0.npz" % source, GOLDEN_WORKLOADS["compass15_seed0"])
     f, g = G.FdF(w["par"])
     assert rel(f, float(gold["f"])) < F_RTOL
     assert normwise(g, gold["grad"]) < G_NORMWISE
     assert rel(G.DoEval(w["par"]), float(gold["doeval"])) < F_RTOL
-    assert G.totAcc() == pytest.approx(float(gold["tot_acc"]), rel=1e-15)
+    if "tot_acc" in gold:
+        assert G.totAcc() == pytest.approx(float(gold["tot_acc"]), rel=1e-15)
+    H = G.Hessian(w["par"])
+    assert np.max(np.abs(H - gold["hessian"])) < 1e-5 * np.max(np.abs(gold["hessian"]))
+    gn, ga = helpers.gpu_integrals(w, precision="fp64")
+    assert gn.nmbEvents() == int(gold["norm_n"]) and ga.nmbEvents() == int(gold["acc_n"])
+    for m, key in ((gn, "norm_raw"), (ga, "acc_raw")):
+        assert np.max(np.abs(m.matrix() - gold[key])) < 1e-12 * np.max(np.abs(gold[key]))
 
 
-def test_golden_compass88_small():
-    from golden.make_golden import GOLDEN_WORKLOADS
-    gold = np.load(os.path.join(GOLDEN, "oracle_compass88_small_seed1.npz"))
-    w = synth.make_workload(**GOLDEN_WORKLOADS["compass88_small_seed1"])
-    gn = R.ampIntegralMatrix()
-    gn.setWaveNames(w["names"])
-    gn.setMatrix(gold["norm_raw"])
-    gn.setNmbEvents(int(gold["norm_n"]))
-    ga = R.ampIntegralMatrix()
-    ga.setWaveNames(w["names"])
-    ga.setMatrix(gold["acc_raw"])
-    ga.setNmbEvents(int(gold["acc_n"]))
-    G = helpers.build_gpu(w, gn, ga)
+@pytest.mark.parametrize("source", ["ref", "oracle"])
+def test_golden_compass88_small(source):
+    """The production shape (7 + 80 waves, rank 2, 341 parameters) against the
+    reference-made and the oracle-made fixtures."""
+    from golden.make_ref_golden import GOLDEN_WORKLOADS
+    gold, w, G = _golden_gpu("%s_compass88_small_seed1.npz" % source, GOLDEN_WORKLOADS["compass88_small_seed1"])
     f, g = G.FdF(w["par"])
     assert rel(f, float(gold["f"])) < F_RTOL
     assert normwise(g, gold["grad"]) < G_NORMWISE
