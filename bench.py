@@ -179,6 +179,34 @@ def oracle_likelihood(names, refl, data_c64, mc_c64, accepted, rank):
     return L
 
 
+def integral_snapshot(I):
+    """(wave names, raw sums, event count) of a product integral"""
+    return I.waveNames(), I.matrix(), I.nmbEvents()
+
+
+def oracle_with_integrals(names, refl, data_c64, norm, acc, rank):
+    """FP64 oracle on the given data amplitudes with exactly the raw sums and
+    event counts of the product's normalisation and acceptance integrals
+    (integral_snapshot, taken before addAccIntegral changes the acceptance
+    integral's event count), so that a comparison of the two likelihoods
+    measures the event term alone."""
+    from oracle.oracle import OracleIntegral, OracleLikelihood
+    ints = []
+    for wn, raw, n in (norm, acc):
+        o = OracleIntegral()
+        assert o.set_wave_names(wn)
+        o.set_raw(raw)
+        o.set_nmb_events(n)
+        ints.append(o)
+    L = OracleLikelihood()
+    assert L.init(names, refl, None, rank, 0.0)
+    assert L.addNormIntegral(ints[0]) and L.addAccIntegral(ints[1])
+    for k, n in enumerate(names):
+        assert L.addAmplitude(n, data_c64[k].astype(np.complex128))
+    assert L.finishInit()
+    return L
+
+
 def time_oracle(L, par, threads, min_seconds, max_reps):
     """Median seconds of one oracle FdF."""
     ts = []
@@ -266,6 +294,7 @@ def run_gb300(args):
     integral_s = time.perf_counter() - t0
     acc = R.ampIntegralMatrix()
     acc.integrate(names, mc, inBin=accepted, precision=args.integral_precision)
+    int_snap = (integral_snapshot(norm), integral_snapshot(acc))
     del mc
     torch.cuda.empty_cache()
     L = R.pwaLikelihood()
@@ -386,24 +415,31 @@ def run_gb300(args):
                 "frac_isolated_launch": alg_bytes / isolated_s / 1e9 / peak,
                 "frac_of_8TBs_spec": achieved / 8000.0}
 
-    # ---- CPU baseline: the FP64 oracle on this machine's host cores ----
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    # ---- parity and CPU baseline: the FP64 oracle on this machine's host cores,
+    # over the same events, with the product's own integral sums ----
+    cpu = parity = None
+    if rank == 0:
         n_cpu = args.n_data
         host = data[:, :n_cpu].cpu().numpy()
-        rng2 = np.random.Generator(np.random.PCG64(5))
-        mc_s = model.draw(rng2, 20_000)
-        acc_s = rng2.random(20_000) < 0.6
-        Lo = oracle_likelihood(names, refl, host, mc_s, acc_s, RANK)
+        Lo = oracle_with_integrals(names, refl, host, int_snap[0], int_snap[1], RANK)
         del host
         threads = cpu_threads()
-        t_all, reps_all = time_oracle(Lo, pts[0], threads, 8.0, 10)
-        t_one, reps_one = time_oracle(Lo, pts[0], 1, 0.0, 1)
-        cpu = {"value": 1.0 / t_all, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": ("FP64 oracle FdF over all %d events (%d reps, median) on %d host threads; "
-                          "single-thread (the reference is single-threaded): %.4f FdF/s" %
-                          (n_cpu, reps_all, threads, 1.0 / t_one)),
-               "single_thread_value": 1.0 / t_one}
+        f_o, g_o = Lo.FdF(pts[0], threads=threads)
+        ll_rel = abs(f_host - f_o) / abs(f_o)
+        parity = {"ll_rel": ll_rel, "grad_normwise": float(np.max(np.abs(g_host - g_o)) / np.max(np.abs(g_o))),
+                  "events": n_cpu, "point": "pts[0]", "tolerance_ll_rel": 1e-6,
+                  "against": "FP64 oracle (bit-for-bit restatement of pwaLikelihood::FdF) with the same "
+                             "normalisation and acceptance sums"}
+        if not ll_rel <= 1e-6:
+            raise SystemExit("parity failure at full size: ll_rel %.3g > 1e-6" % ll_rel)
+        if not args.no_cpu_baseline:
+            t_all, reps_all = time_oracle(Lo, pts[0], threads, 8.0, 10)
+            t_one, reps_one = time_oracle(Lo, pts[0], 1, 0.0, 1)
+            cpu = {"value": 1.0 / t_all, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": ("FP64 oracle FdF over all %d events (%d reps, median) on %d host threads; "
+                              "single-thread (the reference is single-threaded): %.4f FdF/s" %
+                              (n_cpu, reps_all, threads, 1.0 / t_one)),
+                   "single_thread_value": 1.0 / t_one}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -422,7 +458,7 @@ def run_gb300(args):
                         "entry": "pwa_likelihood_fdf (host buffers, staged through mapped pinned memory that "
                                  "the kernel reads and writes directly)"},
                 "gpu_launches": int(launches), "launches_per_step": launches / args.steps,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clocks,
                 "extra": {"integral_norm_s": integral_s, "integral_precision": args.integral_precision,
                           "mc_events": args.n_mc}}
         emit(line, args)

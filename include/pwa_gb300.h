@@ -284,6 +284,13 @@ int pwa_autotune_cache_size(uint32_t* n);
  * without calling the CUDA allocator; n < 0 switches it off.  Exercises the
  * error paths of setup without exhausting a GPU. */
 int pwa_debug_fail_alloc_after(int64_t n);
+/* Test hook (no reference counterpart): runs one warp that waits, with the
+ * kernels' own bounded-wait helper and a limit of limitMicroseconds
+ * (1 .. 1,000,000), on an mbarrier armed for a transfer that is never
+ * issued.  The wait expires without any fault and the call returns
+ * PWA_ERROR_DEVICE_TIMEOUT, the status every streaming kernel reports when a
+ * wait runs out; the context stays usable. */
+int pwa_debug_stalled_wait(uint32_t limitMicroseconds);
 /* finishInit (pwaLikelihood.cc:1291-1388) */
 int pwa_likelihood_finish_init(pwa_likelihood* L);
 

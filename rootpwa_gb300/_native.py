@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_HERE, "libpwa_gb300_debug.so" if os.environ.get("PWA_GB
 HEADER = os.path.join(os.path.dirname(_HERE), "include", "pwa_gb300.h")
 
 SUCCESS = 0
+ERROR_INVALID_ARGUMENT, ERROR_DEVICE_TIMEOUT = 1, 5
 STATUS_NAMES = {
     0: "PWA_SUCCESS", 1: "PWA_ERROR_INVALID_ARGUMENT", 2: "PWA_ERROR_INVALID_STATE", 3: "PWA_ERROR_CUDA",
     4: "PWA_ERROR_OUT_OF_MEMORY", 5: "PWA_ERROR_DEVICE_TIMEOUT", 6: "PWA_ERROR_IO", 7: "PWA_ERROR_UNSUPPORTED",
@@ -118,6 +119,7 @@ SIGNATURES = {
     "pwa_likelihood_set_otf_binning": (i, [vp, u32, pd, pd, C.POINTER(vp), u64, i]),
     "pwa_likelihood_otf_selected": (i, [vp, C.POINTER(u64)]),
     "pwa_debug_fail_alloc_after": (i, [i64]),
+    "pwa_debug_stalled_wait": (i, [u32]),
     "pwa_autotune_cache_save": (i, [C.c_char_p]),
     "pwa_autotune_cache_load": (i, [C.c_char_p]),
     "pwa_autotune_cache_clear": (i, []),

@@ -62,8 +62,9 @@ __device__ __forceinline__ unsigned long long globalTimer()
 	return t;
 }
 
-// Bounded wait for the phase with the given parity to complete.
-static __device__ bool mbarWaitBounded(uint64_t* bar, uint32_t parity)
+// Bounded wait for the phase with the given parity to complete (false after
+// limitNs of %globaltimer).
+static __device__ bool mbarWaitBounded(uint64_t* bar, uint32_t parity, unsigned long long limitNs = kWaitLimitNs)
 {
 	if (mbarTryWait(bar, parity))
 		return true;
@@ -71,7 +72,7 @@ static __device__ bool mbarWaitBounded(uint64_t* bar, uint32_t parity)
 	while (true) {
 		if (mbarTryWait(bar, parity))
 			return true;
-		if (globalTimer() - t0 > kWaitLimitNs)
+		if (globalTimer() - t0 > limitNs)
 			return false;
 	}
 }

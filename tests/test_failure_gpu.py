@@ -76,3 +76,27 @@ def test_non_finite_parameters():
         assert not np.all(np.isfinite(g))
     f, g = G.FdF(w["par"])
     assert f == f0 and np.array_equal(g, g0)
+
+
+def test_bounded_device_wait_expires_and_context_stays_usable():
+    """The device-side failure path without a fault: a warp waits with the
+    kernels' bounded-wait helper on an mbarrier armed for a transfer that is
+    never issued (pwa_debug_stalled_wait).  The wait gives up after its limit,
+    the call returns PWA_ERROR_DEVICE_TIMEOUT, and afterwards the same
+    context evaluates a likelihood that agrees with the oracle."""
+    import time
+    lib = N.lib()
+    assert lib.pwa_debug_stalled_wait(0) == N.ERROR_INVALID_ARGUMENT
+    for limit_us in (2_000, 50_000):
+        t0 = time.perf_counter()
+        assert lib.pwa_debug_stalled_wait(limit_us) == N.ERROR_DEVICE_TIMEOUT
+        dt = time.perf_counter() - t0
+        assert dt >= limit_us * 1e-6
+        assert b"expired" in N.lib().pwa_last_error()
+    w = synth.make_workload("compass15", seed=6, n_data=3001, n_mc=2000)
+    norm, acc = helpers.oracle_integrals(w)
+    G = _build(w, norm, acc)
+    O = helpers.build_oracle(w, norm, acc)
+    f, g = G.FdF(w["par"])
+    f0, g0 = O.FdF(w["par"])
+    assert helpers.rel(f, f0) < helpers.F_RTOL and helpers.normwise(g, g0) < helpers.G_NORMWISE

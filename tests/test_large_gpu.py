@@ -62,3 +62,30 @@ def test_twenty_million_events_equal_two_shards():
     fb, gb = B.FdF(par)
     assert abs((fa + fb) - f) <= 1e-10 * abs(f), (fa + fb, f)
     assert np.max(np.abs((ga + gb) - g)) <= 1e-10 * np.max(np.abs(g))
+
+
+def test_production_shape_full_size_against_oracle():
+    """The production configuration at its full size -- 7 negative + 80
+    positive waves + flat, rank 2, 341 parameters, 1,000,000 data events --
+    against the FP64 oracle (the bit-for-bit restatement of
+    pwaLikelihood::FdF, partialWaveFit/pwaLikelihood.cc:170-315) on the same
+    events with the same integral sums, at two parameter points: value to
+    1e-6 relative and gradient to 1e-6 normwise (FP32 contraction, FP64
+    cross-tile and exact cross-block sums; measured errors are ~1e-9 / ~1e-8)."""
+    import os
+    names, refl = synth.wave_names(7, 80)
+    rng = np.random.Generator(np.random.PCG64(21))
+    model = synth.AmplitudeModel(len(names), 8, rng)
+    data = model.draw(rng, 1_000_000)
+    mc = model.draw(rng, 20_000)
+    w = dict(names=names, refl=refl, rank=2, data=data, mc=mc, accepted=rng.random(20_000) < 0.6)
+    on, oa = helpers.oracle_integrals(w)
+    G = helpers.build_gpu(w, helpers.copy_oracle_integral_to_gpu(on), helpers.copy_oracle_integral_to_gpu(oa))
+    O = helpers.build_oracle(w, on, oa)
+    assert G.nmbPars() == O.nmbPars() == 341
+    threads = len(os.sched_getaffinity(0))
+    for par in (rng.standard_normal(341), 0.3 * rng.standard_normal(341)):
+        f0, g0 = O.FdF(par, threads=threads)
+        f1, g1 = G.FdF(par)
+        assert helpers.rel(f1, f0) < 1e-6
+        assert helpers.normwise(g1, g0) < 1e-6
