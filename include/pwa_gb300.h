@@ -150,14 +150,16 @@ int pwa_integral_write_ascii(const pwa_integral* I, const char* path);
  * row-major on the device, full Hermitian matrix of raw sums (divide by the
  * event count for element()).  precision: PWA_PRECISION_FP64 or
  * PWA_PRECISION_FP32 (SIMT kernels).  Asynchronous on `stream`.
- * Partial sums go to a fixed 8 MiB device array (no cudaMalloc, no cudaFree,
+ * Partial sums go to a fixed 32 MiB device array (no cudaMalloc, no cudaFree,
  * no host synchronisation), for callers that must not allocate, e.g. one
  * integral per kinematic bin issued back to back on several streams, where a
  * cudaFree would synchronise the whole device.  Limits: nWaves <= 256
  * (PWA_GRAM_NOALLOC_MAX_WAVES); larger sets return PWA_ERROR_INVALID_ARGUMENT.  The first
  * call on a device (that device current) resolves the array's address and
- * has to precede any stream capture.  Calls that overlap in time share the
- * array and race: order them on one stream.
+ * has to precede any stream capture; the address it caches stays valid for
+ * the life of the device's primary context (not across cudaDeviceReset).
+ * Calls that overlap in time share the array and race: order them on one
+ * stream.
  */
 #define PWA_GRAM_NOALLOC_MAX_WAVES 256
 int pwa_gram_device_noalloc(const void* amps, uint64_t nK, uint64_t ldK, uint32_t nWaves, const double* weights,

@@ -11,7 +11,9 @@
 //
 // Setup: the first call on a device (that device current) resolves the
 // array's address with cudaGetSymbolAddress; that first call has to happen
-// before any stream capture on the device.  The partial sums need no
+// before any stream capture on the device.  The cached address is valid for
+// the life of the device's primary context (a cudaDeviceReset invalidates
+// it).  The partial sums need no
 // initial value (every entry the reduction reads is written by the Gram
 // kernel of the same call).  All calls on one device share the array, so
 // calls that overlap in time (different streams or host threads without
@@ -33,8 +35,9 @@ namespace {
 			return _st;         \
 	} while (0)
 
-// 2^20 doubles = 8 MiB of chunk partials: chunks x W x W x 2 doubles
-constexpr size_t kScratchDoubles = size_t(1) << 20;
+// 2^22 doubles = 32 MiB of chunk partials (chunks x W x W x 2 doubles):
+// 32 chunks at the largest wave set, 270 at 88 waves
+constexpr size_t kScratchDoubles = size_t(1) << 22;
 constexpr uint32_t kMaxWaves = PWA_GRAM_NOALLOC_MAX_WAVES;
 constexpr int kMaxDevices = 64;
 
@@ -83,26 +86,35 @@ extern "C" int pwa_gram_device_noalloc(const void* amps, uint64_t nK, uint64_t l
 	double* scratch = nullptr;
 	NOALLOC_TRY(scratchFor(dev, &scratch));
 
-	// chunks of K per output tile: enough CTAs to fill the GPU, bounded by the
-	// events and by the fixed scratch (at least one chunk fits for W <= 256)
+	// integrate()'s chunking: chunks of K per output tile so that the grid
+	// fills the GPU, each a run of chunkLen events summed in the kernel's
+	// accumulator type
 	const size_t perChunk = (size_t)nWaves * nWaves * 2;
 	const int tps = ((int)nWaves + 63) / 64;
 	const int nTiles = tps * (tps + 1) / 2;
 	uint64_t chunks = (uint64_t)std::max(1, (4 * sms + nTiles - 1) / nTiles);
 	chunks = std::min<uint64_t>(chunks, std::max<uint64_t>(1, nK / 64));
-	chunks = std::min<uint64_t>(chunks, kScratchDoubles / perChunk);
-
-	GramArgs g{};
-	g.amps = static_cast<const float2*>(amps);
-	g.amps64 = nullptr;
-	g.K = nK;
-	g.ldK = ldK;
-	g.W = (int)nWaves;
-	g.weightK = weights;
-	g.partials = scratch;
-	g.chunks = (int)chunks;
-	g.devErr = nullptr;
+	const uint64_t chunkLen = (nK + chunks - 1) / chunks;
+	// the fixed array holds maxChunks chunk partials; a longer input is taken
+	// in segments of maxChunks chunks of the same length, each reduced into
+	// out in FP64 (the first segment overwrites out, the others add to it)
+	const uint64_t maxChunks = kScratchDoubles / perChunk;
+	const uint64_t segLen = maxChunks * chunkLen;
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
-	NOALLOC_TRY(launchGramSimt(g, precision == PWA_PRECISION_FP64 ? 0 : 1, s));
-	return launchGramReduce(scratch, (int)chunks, (int)nWaves, out, 0, s);
+	for (uint64_t k0 = 0, seg = 0; k0 < nK; k0 += segLen, ++seg) {
+		const uint64_t kSeg = std::min(segLen, nK - k0);
+		GramArgs g{};
+		g.amps = static_cast<const float2*>(amps) + k0;
+		g.amps64 = nullptr;
+		g.K = kSeg;
+		g.ldK = ldK;
+		g.W = (int)nWaves;
+		g.weightK = weights ? weights + k0 : nullptr;
+		g.partials = scratch;
+		g.chunks = (int)((kSeg + chunkLen - 1) / chunkLen);
+		g.devErr = nullptr;
+		NOALLOC_TRY(launchGramSimt(g, precision == PWA_PRECISION_FP64 ? 0 : 1, s));
+		NOALLOC_TRY(launchGramReduce(scratch, g.chunks, (int)nWaves, out, seg > 0 ? 1 : 0, s));
+	}
+	return kOk;
 }

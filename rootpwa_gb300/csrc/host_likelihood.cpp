@@ -1482,7 +1482,8 @@ int pwa_likelihood_covariance_matrix(const pwa_likelihood* L, const double* H, d
 // full parameter space with zeros at the fixed parameters.  Cyclic Jacobi
 // rotations in FP64 on the host (symmetric P x P, once per fit): each
 // rotation zeroes one off-diagonal pair; sweeps repeat until the
-// off-diagonal sum of squares is below 1e-30 of the total.  Eigenvalues in
+// off-diagonal sum of squares is below 1e-30 of the total
+// (PWA_ERROR_NUMERICAL if 100 sweeps do not get there).  Eigenvalues in
 // descending order; the sign of each eigenvector is arbitrary.
 int pwa_likelihood_hessian_eigenvectors(const pwa_likelihood* L, const double* H, double* eigenvalues,
                                         double* eigenvectors, uint32_t* nFree)
@@ -1510,12 +1511,18 @@ int pwa_likelihood_hessian_eigenvectors(const pwa_likelihood* L, const double* H
 		}
 		v[i * n + i] = 1.;
 	}
-	for (int sweep = 0; sweep < 100; ++sweep) {
+	const int kMaxSweeps = 100;
+	bool converged = false;
+	for (int sweep = 0; sweep <= kMaxSweeps; ++sweep) {
 		double off = 0.;
 		for (size_t p = 0; p < n; ++p)
 			for (size_t q = p + 1; q < n; ++q)
 				off += a[p * n + q] * a[p * n + q];
-		if (off <= 1e-30 * total || off == 0.)
+		if (off <= 1e-30 * total || off == 0.) {
+			converged = true;
+			break;
+		}
+		if (sweep == kMaxSweeps)
 			break;
 		for (size_t p = 0; p < n; ++p)
 			for (size_t q = p + 1; q < n; ++q) {
@@ -1542,8 +1549,15 @@ int pwa_likelihood_hessian_eigenvectors(const pwa_likelihood* L, const double* H
 					v[k * n + p] = c * vkp - sn * vkq;
 					v[k * n + q] = sn * vkp + c * vkq;
 				}
+				// the rotation zeroes a_pq; set it exactly instead of keeping
+				// its rounding residue, so that the off-diagonal norm can fall
+				// below the threshold
+				a[p * n + q] = a[q * n + p] = 0.;
 			}
 	}
+	if (!converged)
+		return setError(kErrNumerical, "HessianEigenVectors: Jacobi rotations did not converge in " +
+		                                   std::to_string(kMaxSweeps) + " sweeps");
 	std::vector<size_t> order(n);
 	for (size_t i = 0; i < n; ++i)
 		order[i] = i;

@@ -83,3 +83,37 @@ def test_noalloc_gram_rejects_oversized_wave_set():
     with pytest.raises(N.PwaError) as e:
         _noalloc(dA, 64, 64, 257, None, 1, out, s)
     assert e.value.status == 1 and "256" in str(e.value)
+
+
+def test_noalloc_gram_largest_wave_set_million_events():
+    """256 waves (the limit) over 1,000,000 events: more chunk partials than
+    the fixed array holds, so the call runs in segments with integrate()'s
+    chunk length.  Unweighted FP32 and FP64 sums agree with integrate() in
+    FP64, weighted FP32 sums with the weighted FP64 sums, each on two calls in
+    a row, and the calls take no device memory."""
+    names, _ = synth.wave_names(0, 256)
+    model = synth.AmplitudeModel(256, 8, np.random.Generator(np.random.PCG64(9)))
+    mc = synth.draw_device(model, 1_000_000, seed=19)
+    W, K = mc.shape
+    I = R.ampIntegralMatrix()
+    I.integrate(names, mc, precision="fp64")
+    ref = I.matrix()
+    dW = torch.rand(K, dtype=torch.float64, device="cuda") + 0.5
+    out = torch.empty((W, W), dtype=torch.complex128, device="cuda")
+    s = torch.cuda.Stream()
+
+    def run(weights, precision):
+        out.fill_(float("nan"))
+        torch.cuda.synchronize()
+        _noalloc(mc, K, K, W, weights, precision, out, s)
+        s.synchronize()
+        return out.cpu().numpy()
+
+    ref_w = run(dW, 0)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        for weights, precision, expect, tol in ((None, 1, ref, TOL), (None, 0, ref, 1e-12), (dW, 1, ref_w, TOL)):
+            got = run(weights, precision)
+            assert np.abs(got - expect).max() <= tol * np.abs(expect).max()
+    assert torch.cuda.mem_get_info()[0] == free0
