@@ -33,6 +33,7 @@
 
 #include <cerrno>
 #include <cstring>
+#include <set>
 
 namespace pwa {
 
@@ -226,6 +227,7 @@ int ampFileHeader(uint32_t nWaves, uint32_t nVars, const char* const* names, uin
 	put<uint32_t>(h, 0);
 	put<uint64_t>(h, nEvents);
 	put<uint64_t>(h, 0);  // data offset, filled below
+	std::set<std::string> waveSet, varSet;
 	for (uint32_t i = 0; i < nWaves + nVars; ++i) {
 		const char* name = names[i];
 		if (!name)
@@ -233,6 +235,10 @@ int ampFileHeader(uint32_t nWaves, uint32_t nVars, const char* const* names, uin
 		const size_t len = std::strlen(name);
 		if (len == 0 || len > 65535)
 			return setError(kErrArg, "amplitude file: names must have 1..65535 bytes");
+		// readers look waves and binning variables up by name
+		if (!(i < nWaves ? waveSet : varSet).insert(name).second)
+			return setError(kErrArg, std::string("amplitude file: duplicate ") + (i < nWaves ? "wave" : "variable") +
+			                             " name '" + name + "'");
 		put<uint16_t>(h, (uint16_t)len);
 		h.insert(h.end(), name, name + len);
 	}
@@ -260,6 +266,40 @@ int ampFilePwrite(int fd, const void* p, size_t bytes, uint64_t offset, const ch
 	return kOk;
 }
 
+AmpFileWriter::~AmpFileWriter()
+{
+	if (fd >= 0) {
+		::close(fd);
+		::unlink(tmp.c_str());
+	}
+}
+
+int AmpFileWriter::create(const char* finalPath)
+{
+	path = finalPath;
+	tmp = path + ".tmp";
+	fd = ::open(tmp.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+	if (fd < 0)
+		return setError(kErrIo, "cannot create '" + tmp + "': " + std::strerror(errno));
+	return kOk;
+}
+
+int AmpFileWriter::commit()
+{
+	const int f = fd;
+	fd = -1;
+	if (::close(f) != 0) {
+		::unlink(tmp.c_str());
+		return setError(kErrIo, "close failed for '" + tmp + "'");
+	}
+	if (::rename(tmp.c_str(), path.c_str()) != 0) {
+		const int e = errno;
+		::unlink(tmp.c_str());
+		return setError(kErrIo, "cannot rename '" + tmp + "' to '" + path + "': " + std::strerror(e));
+	}
+	return kOk;
+}
+
 }  // namespace pwa
 
 extern "C" int pwa_ampfile_write(const char* path, uint32_t nWaves, const char* const* waveNames, uint64_t nEvents,
@@ -273,17 +313,13 @@ extern "C" int pwa_ampfile_write(const char* path, uint32_t nWaves, const char* 
 	names.insert(names.end(), varNames, varNames + nVars);
 	std::vector<unsigned char> h;
 	PWA_CHECK(ampFileHeader(nWaves, nVars, names.data(), nEvents, h));
-	const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
-	if (fd < 0)
-		return setError(kErrIo, std::string("cannot create '") + path + "': " + std::strerror(errno));
-	int st = writeAll(fd, h.data(), h.size(), path);
-	if (st == kOk)
-		st = writeAll(fd, amps, (size_t)(nEvents * 8ull * nWaves), path);
-	if (st == kOk && nVars)
-		st = writeAll(fd, vars, (size_t)(nEvents * 8ull * nVars), path);
-	if (::close(fd) != 0 && st == kOk)
-		st = setError(kErrIo, std::string("close failed for '") + path + "'");
-	return st;
+	AmpFileWriter out;
+	PWA_CHECK(out.create(path));
+	PWA_CHECK(writeAll(out.fd, h.data(), h.size(), path));
+	PWA_CHECK(writeAll(out.fd, amps, (size_t)(nEvents * 8ull * nWaves), path));
+	if (nVars)
+		PWA_CHECK(writeAll(out.fd, vars, (size_t)(nEvents * 8ull * nVars), path));
+	return out.commit();
 }
 
 extern "C" int pwa_ampfile_info(const char* path, uint32_t* nWaves, uint64_t* nEvents, uint32_t* nVars)

@@ -321,18 +321,19 @@ int pwa_isobar_write_amp_file(pwa_isobar* A, const char* path, const char* const
 		return setError(kErrState, "no waves");
 	std::vector<const char*> names(waveNames, waveNames + W);
 	names.push_back("mass");
-	for (uint32_t v = 0; v < nVars; ++v)
+	for (uint32_t v = 0; v < nVars; ++v) {
+		if (varNames[v] && std::strcmp(varNames[v], "mass") == 0)
+			return setError(kErrArg, "binning variable 'mass' is written by the call itself (the final-state mass)");
 		names.push_back(varNames[v]);
+	}
 	std::vector<unsigned char> header;
 	PWA_TRY(ampFileHeader(W, nVars + 1, names.data(), n, header));
 	const uint64_t data = header.size();
-	const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
-	if (fd < 0)
-		return setError(kErrIo, std::string("cannot create '") + path + "': " + std::strerror(errno));
-	struct Closer {
-		int fd;
-		~Closer() { ::close(fd); }
-	} closer{fd};
+	// written to <path>.tmp and renamed at the end: an error part-way leaves
+	// no file behind
+	AmpFileWriter out;
+	PWA_TRY(out.create(path));
+	const int fd = out.fd;
 	PWA_TRY(ampFilePwrite(fd, header.data(), header.size(), 0, path));
 	const uint64_t slab = std::min<uint64_t>(std::max<uint64_t>(n, 1), A->chunkEvents ? A->chunkEvents : 1u << 20);
 	std::vector<double> b(3 * slab), f(9 * slab), mass(slab);
@@ -362,7 +363,7 @@ int pwa_isobar_write_amp_file(pwa_isobar* A, const char* path, const char* const
 	}
 	for (uint32_t v = 0; v < nVars; ++v)
 		PWA_TRY(ampFilePwrite(fd, vars + (uint64_t)v * n, n * 8, data + ((uint64_t)W + 1 + v) * n * 8, path));
-	return kOk;
+	return out.commit();
 }
 
 int pwa_clebsch_gordan(int32_t j1, int32_t m1, int32_t j2, int32_t m2, int32_t J, int32_t M, double* out)

@@ -315,6 +315,19 @@ int ampFileToDevice(const AmpFile& f, uint64_t offset, uint64_t bytes, void* dst
 int ampFileHeader(uint32_t nWaves, uint32_t nVars, const char* const* names, uint64_t nEvents,
                   std::vector<unsigned char>& header);
 int ampFilePwrite(int fd, const void* p, size_t bytes, uint64_t offset, const char* path);
+// a file written as <path>.tmp and renamed to <path> by commit(), so that a
+// failed write never leaves a truncated file with a valid header at <path>;
+// without commit() the destructor closes and removes the temporary file
+struct AmpFileWriter {
+	int fd = -1;
+	std::string path, tmp;
+	AmpFileWriter() = default;
+	AmpFileWriter(const AmpFileWriter&) = delete;
+	AmpFileWriter& operator=(const AmpFileWriter&) = delete;
+	~AmpFileWriter();
+	int create(const char* finalPath);
+	int commit();
+};
 
 // ---------------------------------------------------------------------------
 // Three-body isobar amplitudes (isobar.cu, plan in isobar_plan.h)

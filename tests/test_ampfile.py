@@ -60,3 +60,49 @@ def test_rejects_bad_files(tmp_path):
         R.ampFileInfo(tmp_path / "missing.amp")
     with pytest.raises(ValueError):
         R.writeAmplitudeFile(p, names[:1], amps, bv)
+
+
+def test_duplicate_names_rejected_and_nothing_written(tmp_path):
+    """Waves and binning variables are looked up by name: a repeated wave or
+    variable name is refused before anything is written."""
+    names, amps, bv = sample(n=50, w=3)
+    p = tmp_path / "d.amp"
+    with pytest.raises(R.PwaError) as e:
+        R.writeAmplitudeFile(p, [names[0], names[1], names[0]], amps, bv)
+    assert e.value.status == 1 and "duplicate" in str(e.value)
+    assert not p.exists() and not (tmp_path / "d.amp.tmp").exists()
+    # one name may be a wave and a variable at once (separate tables)
+    R.writeAmplitudeFile(p, ["mass", names[1], names[2]], amps, bv)
+    assert R.ampFileInfo(p)[0][0] == "mass"
+
+
+def test_failed_write_leaves_no_file(tmp_path):
+    """A write that fails part-way (here: the process's file-size limit) leaves
+    neither the file nor its temporary behind; an existing file of that name
+    is kept until a write succeeds."""
+    import subprocess
+    import sys
+    import textwrap
+    p = tmp_path / "big.amp"
+    code = textwrap.dedent("""
+        import resource, signal, sys
+        import numpy as np
+        sys.path.insert(0, %r)
+        import rootpwa_gb300 as R
+        signal.signal(signal.SIGXFSZ, signal.SIG_IGN)
+        resource.setrlimit(resource.RLIMIT_FSIZE, (65536, 65536))
+        amps = np.ones((4, 100000), np.complex64)
+        try:
+            R.writeAmplitudeFile(%r, ["a", "b", "c", "d"], amps)
+        except R.PwaError as e:
+            print("status", e.status)
+    """) % (str(__import__("pathlib").Path(__file__).resolve().parents[1]), str(p))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert "status 6" in r.stdout, r.stdout + r.stderr
+    assert not p.exists() and not (tmp_path / "big.amp.tmp").exists()
+    names, amps, bv = sample(n=20, w=2)
+    R.writeAmplitudeFile(p, names, amps, bv)
+    before = p.read_bytes()
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert "status 6" in r.stdout, r.stdout + r.stderr
+    assert p.read_bytes() == before and not (tmp_path / "big.amp.tmp").exists()
