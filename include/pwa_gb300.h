@@ -60,9 +60,14 @@ enum pwa_prior { PWA_PRIOR_FLAT = 0, PWA_PRIOR_HALF_CAUCHY = 1 };
 enum pwa_amp_type { PWA_COMPLEX64 = 0, PWA_COMPLEX128 = 1 };
 enum pwa_memory   { PWA_MEMORY_HOST = 0, PWA_MEMORY_DEVICE = 1 };
 
-/* cross-event reduction of the FdF kernel: FP32 per 128-event tile, then
- * FP64 (default) or compensated FP32 across tiles; FP64 across blocks always. */
-enum pwa_reduction { PWA_REDUCE_FP64 = 0, PWA_REDUCE_KAHAN_FP32 = 1 };
+/* cross-event reduction of the FdF kernel (exact fixed point across blocks
+ * in every mode).  Within a block each lane sums its events of a tile in
+ * FP32; across tiles:
+ *   PWA_REDUCE_FP64        FP32 partials of 32 tiles folded into FP64 (default)
+ *   PWA_REDUCE_KAHAN_FP32  every tile's partial added to compensated FP32 sums
+ *   PWA_REDUCE_FP32        plain FP32 sums over all of a lane's tiles
+ * The two FP32 modes run the main kernel variant (not the fused-gradient one). */
+enum pwa_reduction { PWA_REDUCE_FP64 = 0, PWA_REDUCE_KAHAN_FP32 = 1, PWA_REDUCE_FP32 = 2 };
 
 /* arithmetic of the integral-matrix Gram kernel */
 enum pwa_precision {

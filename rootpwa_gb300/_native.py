@@ -25,7 +25,7 @@ STATUS_NAMES = {
 COMPLEX64, COMPLEX128 = 0, 1
 MEMORY_HOST, MEMORY_DEVICE = 0, 1
 PRIOR_FLAT, PRIOR_HALF_CAUCHY = 0, 1
-REDUCE_FP64, REDUCE_KAHAN_FP32 = 0, 1
+REDUCE_FP64, REDUCE_KAHAN_FP32, REDUCE_FP32 = 0, 1, 2
 PRECISION = {"fp64": 0, "fp32": 1, "tf32": 2, "tf32x3": 3, "bf16x3": 4}
 CALL_FDF, CALL_GRADIENT, CALL_DOEVAL, CALL_DODERIVATIVE, CALL_HESSIAN = range(5)
 

@@ -97,10 +97,12 @@ __host__ __device__ inline int waveSplit(int W0, int W, int* nNeg, int* wn, int*
 }
 
 // Tiles whose gradient partials are summed in FP32 before the warp
-// reduce-scatter folds them into the FP64 (or compensated) accumulators
-// (a lane's FP32 partial then covers 128 events of one wave; the LL and
-// gradient errors against FP64 at 1 M events are the same as with 8).
+// reduce-scatter folds them into the FP64 accumulators (a lane's FP32
+// partial then covers 128 events of one wave; the LL and gradient errors
+// against FP64 at 1 M events are the same as with 8).  The compensated mode
+// folds every tile; the plain FP32 mode only after the last one.
 constexpr int kFold = 32;
+__device__ __forceinline__ int foldTiles(int reduction) { return reduction == 0 ? kFold : reduction == 1 ? 1 : 1 << 30; }
 
 
 template <int R, int E, int WPW, int NE>
@@ -219,6 +221,7 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 
 	bool failed = false;
 	uint64_t k = 0;
+	int foldLeft = foldTiles(a.reduction);
 	// stage, phase parity and first event of tile k, advanced incrementally
 	// (no division by the runtime stage count inside the loop)
 	int s = 0;
@@ -538,8 +541,9 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 			}
 		}
 
-		// fold the FP32 tile partials every kFold tiles and after the last tile
-		if ((k + 1) % kFold == 0 || k + 1 == myTiles) {
+		// fold the FP32 tile partials every foldTiles(reduction) tiles and after the last tile
+		if (--foldLeft == 0 || k + 1 == myTiles) {
+			foldLeft = foldTiles(a.reduction);
 			const float ll = warpSum(llPart), cs = warpSum(cPart);
 			llPart = 0.f;
 			cPart = 0.f;
@@ -547,9 +551,12 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 				if (a.reduction == 0) {
 					accLL += (double)ll;
 					accC += (double)cs;
-				} else {
+				} else if (a.reduction == 1) {
 					kahanAdd(kLL, kLLc, ll);
 					kahanAdd(kC, kCc, cs);
+				} else {
+					kLL += ll;
+					kC += cs;
 				}
 			}
 			if (a.withGrad) {
@@ -571,8 +578,10 @@ __global__ void __launch_bounds__(kThreads, 1) fdfMainKernel(const FdfArgs a, co
 					const float v = reduceScatter32(&part[q * 32], lane);
 					if (a.reduction == 0)
 						accG[q] += (double)v;
-					else
+					else if (a.reduction == 1)
 						kahanAdd(kG[q], kGc[q], v);
+					else
+						kG[q] += v;
 				}
 			}
 		}
@@ -800,8 +809,23 @@ size_t fdfAccumulatorWords(int nPartial) { return (size_t)kReplicas * kLimbs * (
 
 int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {
-	if (p.phase1Events == 3)
-		return launchFdfFused(p, a, s);
+	if (p.phase1Events == 3) {
+		if (a.reduction == 0)
+			return launchFdfFused(p, a, s);
+		// the FP32 reduction modes are those of the main kernel (two events
+		// per lane, the fused variant's pipeline depth)
+		FdfPlan q = p;
+		q.phase1Events = 2;
+		q.smemBytes = smemLayout(a.W, a.R, q.E, q.stages).total;
+		int nNeg, wn, wp;
+		const int wpwa = waveSplit(a.W0, a.W, &nNeg, &wn, &wp);
+		q.wpw = wpwa <= 2 ? 2 : wpwa <= 4 ? 4 : wpwa <= 6 ? 6 : wpwa <= 8 ? 8 : 14;
+		switch (a.R) {
+		case 1: return launchR<1>(q, a, s);
+		case 2: return launchR<2>(q, a, s);
+		default: return setError(kErrUnsupported, "fused FdF plan beyond rank 2");
+		}
+	}
 	switch (a.R) {
 	case 1: return launchR<1>(p, a, s);
 	case 2: return launchR<2>(p, a, s);

@@ -779,7 +779,7 @@ int pwa_likelihood_set_reduction(pwa_likelihood* L, int r)
 {
 	if (!L)
 		return setError(kErrArg, "null likelihood");
-	if (r != PWA_REDUCE_FP64 && r != PWA_REDUCE_KAHAN_FP32)
+	if (r != PWA_REDUCE_FP64 && r != PWA_REDUCE_KAHAN_FP32 && r != PWA_REDUCE_FP32)
 		return setError(kErrArg, "unknown reduction mode");
 	L->reduction = r;
 	return kOk;

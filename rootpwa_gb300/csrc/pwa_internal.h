@@ -90,7 +90,7 @@ struct FdfArgs {
 	int prior;               // 0 flat, 1 half-Cauchy
 	double cauchyWidth;
 	int withGrad;
-	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32
+	int reduction;           // 0 = FP64 across tiles, 1 = compensated FP32, 2 = plain FP32
 	int nPartial;            // 2 + 2*R*W summed values (LL, sum c, gradient re/im per slot)
 	unsigned long long* fixAcc;  // device, fdfAccumulatorWords(nPartial) 128-bit fixed-point totals, zero between launches
 	double* nfAcc;           // device, [nPartial] totals of values outside the fixed-point range, zero between launches

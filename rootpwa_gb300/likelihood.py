@@ -361,8 +361,11 @@ class pwaLikelihood:
         N.call("pwa_likelihood_set_stream", self._h, C.c_void_p(int(stream_handle)))
 
     def setReduction(self, mode):
-        """'fp64' (default) or 'kahan_fp32' cross-tile reduction."""
-        m = {"fp64": N.REDUCE_FP64, "kahan_fp32": N.REDUCE_KAHAN_FP32}[mode] if isinstance(mode, str) else int(mode)
+        """cross-tile reduction: 'fp64' (default: FP32 partials of 32 tiles
+        folded into FP64), 'kahan_fp32' (every tile into compensated FP32) or
+        'fp32' (plain FP32 over all tiles)."""
+        m = {"fp64": N.REDUCE_FP64, "kahan_fp32": N.REDUCE_KAHAN_FP32,
+             "fp32": N.REDUCE_FP32}[mode] if isinstance(mode, str) else int(mode)
         N.call("pwa_likelihood_set_reduction", self._h, m)
 
     def setAutotune(self, enable=True):

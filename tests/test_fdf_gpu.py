@@ -180,12 +180,22 @@ def test_deterministic_and_batch():
         assert fb[k] == fk and np.array_equal(gb[k], gk)
 
 
-@pytest.mark.parametrize("mode", ["fp64", "kahan_fp32"])
+@pytest.mark.parametrize("mode", ["fp64", "kahan_fp32", "fp32"])
 def test_reduction_modes(mode):
+    """The three cross-tile reduction modes at 50,000 events: each within the
+    engine's tolerances of the FP64 oracle; the modes give different sums
+    (the FP32 ones fold at other points), each bitwise reproducible."""
     w = synth.make_workload("compass88", seed=5, n_data=50000, n_mc=4000)
     O, G = pair(w)
     G.setReduction(mode)
     check_point(O, G, w["par"])
+    f1, g1 = G.FdF(w["par"])
+    f2, g2 = G.FdF(w["par"])
+    assert f1 == f2 and np.array_equal(g1, g2)
+    if mode != "fp64":
+        G.setReduction("fp64")
+        f0, g0 = G.FdF(w["par"])
+        assert f0 != f1 or not np.array_equal(g0, g1)
 
 
 def test_options_prior_unnormalised_thresholds_override():
