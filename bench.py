@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--integral-precision", default="tf32x3", choices=["fp64", "fp32", "tf32", "tf32x3", "bf16x3"],
                     help="arithmetic of the normalisation / acceptance integrals (set-up, not timed)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sharded", action="store_true",
+                    help="fdf: the event-sharded design (one all-reduce of P + 1 doubles per FdF) even on one "
+                         "process (always on for more than one process)")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
     ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision", "next", "isobar"],
                     help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
@@ -184,7 +187,7 @@ def integral_snapshot(I):
     return I.waveNames(), I.matrix(), I.nmbEvents()
 
 
-def oracle_with_integrals(names, refl, data_c64, norm, acc, rank):
+def oracle_with_integrals(names, refl, data_c64, norm, acc, rank, shard=None):
     """FP64 oracle on the given data amplitudes with exactly the raw sums and
     event counts of the product's normalisation and acceptance integrals
     (integral_snapshot, taken before addAccIntegral changes the acceptance
@@ -199,6 +202,8 @@ def oracle_with_integrals(names, refl, data_c64, norm, acc, rank):
         o.set_nmb_events(n)
         ints.append(o)
     L = OracleLikelihood()
+    if shard is not None:
+        L.set_shard(*shard)
     assert L.init(names, refl, None, rank, 0.0)
     assert L.addNormIntegral(ints[0]) and L.addAccIntegral(ints[1])
     for k, n in enumerate(names):
@@ -266,10 +271,11 @@ def run_reference(args):
 def run_gb300(args):
     import torch
     rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    sharded = args.sharded or world > 1
     torch.cuda.set_device(local)
+    if sharded:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import rootpwa_gb300 as R
     from rootpwa_gb300 import synth
     from rootpwa_gb300 import _native as N
@@ -294,10 +300,24 @@ def run_gb300(args):
     integral_s = time.perf_counter() - t0
     acc = R.ampIntegralMatrix()
     acc.integrate(names, mc, inBin=accepted, precision=args.integral_precision)
+    if sharded:
+        # every rank integrated its own MC events: one all-reduce of the raw
+        # sums and event counts gives every rank the integrals of all of them
+        for I in (norm, acc):
+            raw = torch.from_numpy(np.ascontiguousarray(I.matrix()).view(np.float64).copy()).cuda()
+            cnt = torch.tensor([float(I.nmbEvents())], dtype=torch.float64, device="cuda")
+            dist.all_reduce(raw)
+            dist.all_reduce(cnt)
+            I.setMatrix(raw.cpu().numpy().view(np.complex128).reshape(W, W))
+            I.setNmbEvents(int(round(cnt.item())))
     int_snap = (integral_snapshot(norm), integral_snapshot(acc))
     del mc
     torch.cuda.empty_cache()
     L = R.pwaLikelihood()
+    if sharded:
+        # this rank's share of a data set of world x n_data events: only the
+        # root shard adds the normalisation and prior terms
+        L.setShard(world * args.n_data, rank == 0)
     L.init(names, refl, None, RANK, 0.0)
     L.addNormIntegral(norm)
     L.addAccIntegral(acc)
@@ -324,6 +344,10 @@ def run_gb300(args):
         st = fdf_dev(h, C.c_void_p(par_ptr[i % n_pts]), C.c_void_p(out_ptr[i % n_pts]), 1, sptr)
         if st:
             N.check(st)
+        if sharded:
+            # f and the gradient of all shards, on the kernel's stream
+            with torch.cuda.stream(stream):
+                dist.all_reduce(d_out[i % n_pts, :P + 1])
 
     for i in range(max(3, args.warmup)):
         step(i)
@@ -342,7 +366,7 @@ def run_gb300(args):
             stream.synchronize()
     stream.synchronize()
     launches0 = lib.pwa_kernel_launch_count()
-    if world > 1:
+    if sharded:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -366,7 +390,7 @@ def run_gb300(args):
     out = d_out.cpu().numpy()
     assert np.all(out[:, P + 1] == 0.0), "device error flag set"
     assert np.all(np.isfinite(out[:, :P + 1]))
-    if world > 1:
+    if sharded:
         t = torch.tensor([ms], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
@@ -374,11 +398,18 @@ def run_gb300(args):
     value = world * args.steps / (ms / 1e3)
 
     # cross-check the device-resident result against the host entry point
-    f_host, g_host = L.FdF(pts[0])
+    # (in the sharded design: the host-API ShardedFdF over all ranks)
+    if sharded:
+        from rootpwa_gb300.sharded import ShardedFdF
+        whole = ShardedFdF(L, device="cuda")
+        f_host, g_host = whole.FdF(pts[0])
+    else:
+        f_host, g_host = L.FdF(pts[0])
     f_dev = out[0, 0]
     assert abs(f_dev - f_host) <= 1e-12 * abs(f_host), (f_dev, f_host)
 
-    # ---- e2e: the C-ABI call with host buffers ----
+    # ---- e2e: the C-ABI call with host buffers (sharded: the ShardedFdF
+    # host API, whose all-reduce buffer goes host -> device -> host) ----
     n_e2e = args.e2e_steps or min(args.steps, 2000)
     host_pts = [np.ascontiguousarray(p) for p in pts]
     fbuf = C.c_double()
@@ -386,17 +417,24 @@ def run_gb300(args):
     gptr = gbuf.ctypes.data_as(C.POINTER(C.c_double))
     pptrs = [p.ctypes.data_as(C.POINTER(C.c_double)) for p in host_pts]
     fdf_host = lib.pwa_likelihood_fdf
-    for i in range(3):
-        N.check(fdf_host(h, pptrs[i % n_pts], C.byref(fbuf), gptr))
-    if world > 1:
-        torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for i in range(n_e2e):
+
+    def e2e_step(i):
+        if sharded:
+            whole.FdF(host_pts[i % n_pts])
+            return
         st = fdf_host(h, pptrs[i % n_pts], C.byref(fbuf), gptr)
         if st:
             N.check(st)
+
+    for i in range(3):
+        e2e_step(i)
+    if sharded:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for i in range(n_e2e):
+        e2e_step(i)
     e2e_s = time.perf_counter() - t0
-    if world > 1:
+    if sharded:
         t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
@@ -416,18 +454,26 @@ def run_gb300(args):
                 "frac_of_8TBs_spec": achieved / 8000.0}
 
     # ---- parity and CPU baseline: the FP64 oracle on this machine's host cores,
-    # over the same events, with the product's own integral sums ----
+    # over the same events, with the product's own integral sums (sharded:
+    # every rank's oracle over its shard, summed like the product's) ----
     cpu = parity = None
-    if rank == 0:
+    if rank == 0 or sharded:
         n_cpu = args.n_data
         host = data[:, :n_cpu].cpu().numpy()
-        Lo = oracle_with_integrals(names, refl, host, int_snap[0], int_snap[1], RANK)
+        Lo = oracle_with_integrals(names, refl, host, int_snap[0], int_snap[1], RANK,
+                                   shard=(world * args.n_data, rank == 0) if sharded else None)
         del host
         threads = cpu_threads()
         f_o, g_o = Lo.FdF(pts[0], threads=threads)
+        if sharded:
+            buf = torch.from_numpy(np.concatenate([[f_o], g_o])).cuda()
+            torch.distributed.all_reduce(buf)
+            buf = buf.cpu().numpy()
+            f_o, g_o = float(buf[0]), buf[1:]
+    if rank == 0:
         ll_rel = abs(f_host - f_o) / abs(f_o)
         parity = {"ll_rel": ll_rel, "grad_normwise": float(np.max(np.abs(g_host - g_o)) / np.max(np.abs(g_o))),
-                  "events": n_cpu, "point": "pts[0]", "tolerance_ll_rel": 1e-6,
+                  "events": world * n_cpu if sharded else n_cpu, "point": "pts[0]", "tolerance_ll_rel": 1e-6,
                   "against": "FP64 oracle (bit-for-bit restatement of pwaLikelihood::FdF) with the same "
                              "normalisation and acceptance sums"}
         if not ll_rel <= 1e-6:
@@ -451,18 +497,27 @@ def run_gb300(args):
                            "mc_events": args.n_mc, "reduction": args.reduction,
                            "l2": "inputs (%.0f MB) larger than L2 (129 MB); no flush" % (alg_bytes / 1e6),
                            "entry": "pwa_likelihood_fdf_device (parameters and results in HBM)",
+                           "design": ("event-sharded: rank r holds events [r n, (r+1) n) of one data set of "
+                                      "%d x %d events; per FdF one NCCL all-reduce of P + 1 doubles on the "
+                                      "kernel's stream; value counts %d-event FdF equivalents"
+                                      % (world, args.n_data, args.n_data)) if sharded else
+                                     "one process, one likelihood",
                            "plan": dict(zip(("tile_events", "stages", "blocks"), L.plan()),
                                         phase1_events_per_lane=L.planVariant())},
-                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": P * 8,
-                        "d2h_bytes_per_step": (P + 2) * 8,
-                        "entry": "pwa_likelihood_fdf (host buffers, staged through mapped pinned memory that "
-                                 "the kernel reads and writes directly)"},
+                "e2e": {"value": e2e_value, "unit": UNIT,
+                        "h2d_bytes_per_step": P * 8 + ((P + 1) * 8 if sharded else 0),
+                        "d2h_bytes_per_step": (P + 2) * 8 + ((P + 1) * 8 if sharded else 0),
+                        "entry": ("rootpwa_gb300.sharded.ShardedFdF.FdF (host parameters; per rank "
+                                  "pwa_likelihood_fdf of its shard, then one NCCL all-reduce of P + 1 doubles)"
+                                  if sharded else
+                                  "pwa_likelihood_fdf (host buffers, staged through mapped pinned memory that "
+                                  "the kernel reads and writes directly)")},
                 "gpu_launches": int(launches), "launches_per_step": launches / args.steps,
                 "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clocks,
                 "extra": {"integral_norm_s": integral_s, "integral_precision": args.integral_precision,
                           "mc_events": args.n_mc}}
         emit(line, args)
-    if world > 1:
+    if sharded:
         torch.distributed.destroy_process_group()
     return 0
 
