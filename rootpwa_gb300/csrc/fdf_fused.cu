@@ -84,6 +84,14 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 	const uint64_t myTiles = (first < nTiles) ? (nTiles - 1 - first) / stride + 1 : 0;
 	const uint32_t stageBytes = (uint32_t)W * E * 8u;
 
+	// batched fits: the launch of a problem that no longer iterates does
+	// nothing (the flag is written by the preceding grid; uniform over the grid)
+	if (a.active) {
+		gridDependencyWait();
+		if (*(const volatile int*)a.active == 0)
+			return;
+	}
+
 	if (tid == 0) {
 		for (int s = 0; s < stages; ++s) {
 			mbarInit(&bars[s], 1);

@@ -202,6 +202,7 @@ int launchEval(pwa_likelihood* L, const double* dPar, double* dOut, int withGrad
 	a.counter = L->dCounter.as<unsigned>();
 	a.devErr = L->dErr.as<unsigned>();
 	a.out = dOut;
+	a.active = nullptr;
 	cudaEvent_t* te = nullptr;
 	if (L->timing && 2 * (L->nTimed + 1) <= L->timingEvents.size()) {
 		te = &L->timingEvents[2 * L->nTimed];
@@ -1747,6 +1748,42 @@ int pwa_likelihood_reset_func_call_info(pwa_likelihood* L)
 // ===========================================================================
 namespace pwa {
 
+int launchLikelihoodEval(pwa_likelihood* L, const double* dPar, double* dOut, const int* dActive, cudaStream_t s)
+{
+	PWA_TRY(checkFinished(L));
+	FdfArgs a{};
+	a.amps = L->amps.as<float2>();
+	a.nEvents = L->nEvents;
+	a.W0 = (int)L->nW[0];
+	a.W = (int)L->W();
+	a.R = (int)L->rank;
+	a.P = (int)L->nPars;
+	a.par = dPar;
+	a.slotRe = L->dSlotRe.as<int>();
+	a.slotIm = L->dSlotIm.as<int>();
+	a.accI = L->dAccI.as<double>();
+	a.nEvt = normFactor(L);
+	a.totAcc = L->totAcc;
+	a.prior = priorOf(L);
+	a.cauchyWidth = L->cauchyWidth;
+	a.withGrad = 1;
+	a.reduction = L->reduction;
+	a.nPartial = 2 + 2 * a.R * a.W;
+	a.fixAcc = L->dFixAcc.as<unsigned long long>();
+	a.nfAcc = L->dNfAcc.as<double>();
+	a.counter = L->dCounter.as<unsigned>();
+	a.devErr = L->dErr.as<unsigned>();
+	a.out = dOut;
+	a.active = dActive;
+	return launchFdf(L->plan, a, s);
+}
+
+int clearLikelihoodError(pwa_likelihood* L, cudaStream_t s)
+{
+	PWA_TRY(checkFinished(L));
+	return cudaCheck(cudaMemsetAsync(L->dErr.p, 0, sizeof(unsigned), s), "clear device error flag");
+}
+
 int likelihoodView(const pwa_likelihood* L, LikelihoodView* v)
 {
 	PWA_TRY(checkFinished(L));
@@ -1765,6 +1802,9 @@ int likelihoodView(const pwa_likelihood* L, LikelihoodView* v)
 	v->prior = priorOf(L);
 	v->cauchyWidth = L->cauchyWidth;
 	v->device = L->device;
+	v->fixed.assign(L->nPars, 0);
+	for (uint32_t i = 0; i < L->nPars; ++i)
+		v->fixed[i] = L->pars[i].fixed ? 1 : 0;
 	return kOk;
 }
 

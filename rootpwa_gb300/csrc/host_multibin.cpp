@@ -1,7 +1,14 @@
 // host_multibin.cpp -- batched multibin x multistart fits: work items over
 // the bins' amplitude stores, graph-captured sweeps of the batched FdF and
 // L-BFGS kernels, the chunk autotuner and checkpoint / resume of the fit
-// state.
+// state.  Bins of rank 1 with one reflectivity and at most 64 waves run the
+// start-packed batch kernels; every other layout of the reference (any rank,
+// both reflectivities, up to the FdF kernel's wave limit) evaluates each
+// (bin, start) problem with its bin's own FdF kernel inside the same
+// captured sweep.  Parameters the layout holds fixed (threshold-fixed and
+// all-zero waves) start at 0 and keep a zero gradient, as the reference's
+// minimiser drivers keep them at 0 (pwaFit.cc:249-266,
+// pwaNloptFit.cc:383-401).
 
 #include "host_common.h"
 
@@ -19,6 +26,8 @@ struct pwa_multibin {
 		uint32_t nStarts;
 	};
 	std::vector<Bin> bins;
+	// general layout: one FdF launch of the bin's own kernel per problem
+	bool general = false;
 	int W = 0, P = 0;
 	std::vector<int> slotRe, slotIm;
 	int prior = PWA_PRIOR_FLAT;
@@ -36,6 +45,8 @@ struct pwa_multibin {
 	DevBuf dBins, dItems, dProblems, dSlotRe, dSlotIm, dPartials, dErr;
 	DevBuf dX, dXt, dG, dGt, dD, dF, dFt, dGnorm, dStep, dGamma, dGBest, dS, dY, dRho, dAlpha;
 	DevBuf dStatus, dIter, dNBack, dHist, dHead, dItBest, dActive, dNActive;
+	DevBuf dFixed;   // [bins][P] fixed-parameter masks
+	DevBuf dOut;     // general layout: [Q][P + 2] FdF outputs
 	PinnedBuf hCount;
 	// per check of the last fit: elapsed seconds and every problem's current f
 	std::vector<double> traceT, traceF;
@@ -77,6 +88,12 @@ int buildBatch(pwa_multibin* M)
 		d.q0 = q0;
 		d.nStarts = (int)B.nStarts;
 		bins.push_back(d);
+		if (M->general) {
+			for (uint32_t s = 0; s < B.nStarts; ++s)
+				problems.push_back(ProblemDesc{(int)b, (int)s, 0, 0});
+			q0 += (int)B.nStarts;
+			continue;
+		}
 		const uint64_t tiles = (B.v.nEvents + 127) / 128;
 		const uint32_t chunk = std::max<uint32_t>(1, M->chunkTiles[sizeClass(tiles)]);
 		const int groups = ((int)B.nStarts + M->SG - 1) / M->SG;
@@ -92,14 +109,23 @@ int buildBatch(pwa_multibin* M)
 	}
 	M->Q = q0;
 	M->nItems = (int)items.size();
-	PWA_TRY(configureBatchFdf(M->W, M->SG, M->maxSmem));
 	const size_t Q = (size_t)M->Q, P = (size_t)M->P;
+	std::vector<unsigned char> fixed;
+	for (const auto& B : M->bins)
+		fixed.insert(fixed.end(), B.v.fixed.begin(), B.v.fixed.end());
+	PWA_TRY(M->dFixed.alloc(fixed.size(), "multibin fixed masks"));
 	PWA_TRY(M->dBins.alloc(bins.size() * sizeof(BinDesc), "multibin bins"));
-	PWA_TRY(M->dItems.alloc(items.size() * sizeof(BatchItem), "multibin items"));
 	PWA_TRY(M->dProblems.alloc(problems.size() * sizeof(ProblemDesc), "multibin problems"));
-	PWA_TRY(M->dSlotRe.alloc(M->W * sizeof(int), "slot map"));
-	PWA_TRY(M->dSlotIm.alloc(M->W * sizeof(int), "slot map"));
-	PWA_TRY(M->dPartials.alloc((size_t)M->nItems * M->SG * (2 + 2 * M->W) * sizeof(double), "multibin partials"));
+	if (M->general) {
+		PWA_TRY(M->dOut.alloc(Q * (P + 2) * sizeof(double), "multibin FdF outputs"));
+	} else {
+		PWA_TRY(configureBatchFdf(M->W, M->SG, M->maxSmem));
+		PWA_TRY(M->dItems.alloc(items.size() * sizeof(BatchItem), "multibin items"));
+		PWA_TRY(M->dSlotRe.alloc(M->W * sizeof(int), "slot map"));
+		PWA_TRY(M->dSlotIm.alloc(M->W * sizeof(int), "slot map"));
+		PWA_TRY(M->dPartials.alloc((size_t)M->nItems * M->SG * (2 + 2 * M->W) * sizeof(double),
+		                           "multibin partials"));
+	}
 	PWA_TRY(M->dErr.alloc(sizeof(unsigned), "flag"));
 	for (DevBuf* b : {&M->dX, &M->dXt, &M->dG, &M->dGt, &M->dD})
 		PWA_TRY(b->alloc(Q * P * sizeof(double), "multibin vectors"));
@@ -116,16 +142,19 @@ int buildBatch(pwa_multibin* M)
 	cudaStream_t s = M->stream;
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dBins.p, bins.data(), bins.size() * sizeof(BinDesc), cudaMemcpyHostToDevice, s),
 	                  "upload"));
-	PWA_TRY(cudaCheck(
-	    cudaMemcpyAsync(M->dItems.p, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, s),
-	    "upload"));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dProblems.p, problems.data(), problems.size() * sizeof(ProblemDesc),
 	                                  cudaMemcpyHostToDevice, s),
 	                  "upload"));
-	PWA_TRY(cudaCheck(
-	    cudaMemcpyAsync(M->dSlotRe.p, M->slotRe.data(), M->W * sizeof(int), cudaMemcpyHostToDevice, s), "upload"));
-	PWA_TRY(cudaCheck(
-	    cudaMemcpyAsync(M->dSlotIm.p, M->slotIm.data(), M->W * sizeof(int), cudaMemcpyHostToDevice, s), "upload"));
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dFixed.p, fixed.data(), fixed.size(), cudaMemcpyHostToDevice, s), "upload"));
+	if (!M->general) {
+		PWA_TRY(cudaCheck(
+		    cudaMemcpyAsync(M->dItems.p, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, s),
+		    "upload"));
+		PWA_TRY(cudaCheck(
+		    cudaMemcpyAsync(M->dSlotRe.p, M->slotRe.data(), M->W * sizeof(int), cudaMemcpyHostToDevice, s), "upload"));
+		PWA_TRY(cudaCheck(
+		    cudaMemcpyAsync(M->dSlotIm.p, M->slotIm.data(), M->W * sizeof(int), cudaMemcpyHostToDevice, s), "upload"));
+	}
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "multibin build"));
 	M->built = true;
 	return kOk;
@@ -134,6 +163,25 @@ int buildBatch(pwa_multibin* M)
 // one evaluation sweep at the trial points dXt of the active problems
 int batchSweep(pwa_multibin* M)
 {
+	if (M->general) {
+		const size_t P = (size_t)M->P;
+		int q = 0;
+		for (const auto& B : M->bins)
+			for (uint32_t s = 0; s < B.nStarts; ++s, ++q)
+				PWA_TRY(launchLikelihoodEval(B.L, M->dXt.as<double>() + q * P, M->dOut.as<double>() + q * (P + 2),
+				                             M->dActive.as<int>() + q, M->stream));
+		GatherEvalArgs g{};
+		g.Q = M->Q;
+		g.P = M->P;
+		g.out = M->dOut.as<double>();
+		g.active = M->dActive.as<int>();
+		g.problems = M->dProblems.as<ProblemDesc>();
+		g.fixed = M->dFixed.as<unsigned char>();
+		g.f = M->dFt.as<double>();
+		g.g = M->dGt.as<double>();
+		g.devErr = M->dErr.as<unsigned>();
+		return launchGatherEval(g, M->stream);
+	}
 	BatchArgs a{};
 	a.bins = M->dBins.as<BinDesc>();
 	a.items = M->dItems.as<BatchItem>();
@@ -162,6 +210,7 @@ int batchSweep(pwa_multibin* M)
 	f.partials = a.partials;
 	f.prior = M->prior;
 	f.cauchyWidth = M->cauchyWidth;
+	f.fixed = M->dFixed.as<unsigned char>();
 	f.f = M->dFt.as<double>();
 	f.g = M->dGt.as<double>();
 	return launchBatchFinish(f, M->stream);
@@ -231,6 +280,9 @@ int startSweep(pwa_multibin* M, const double* x)
 	std::vector<int> ones(Q, 1);
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dActive.p, ones.data(), Q * sizeof(int), cudaMemcpyHostToDevice, s), "upload"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(M->dErr.p, 0, sizeof(unsigned), s), "memset"));
+	if (M->general)
+		for (const auto& B : M->bins)
+			PWA_TRY(clearLikelihoodError(B.L, s));
 	return cudaCheck(cudaStreamSynchronize(s), "upload sync");
 }
 
@@ -468,11 +520,12 @@ int pwa_multibin_add_bin(pwa_multibin* M, pwa_likelihood* L, uint32_t nStarts)
 		return setError(kErrArg, "multibin: a bin needs at least one start point");
 	LikelihoodView v;
 	PWA_TRY(likelihoodView(L, &v));
-	if (v.R != 1 || v.W0 != 0)
-		return setError(kErrUnsupported, "multibin batches support rank 1 with one reflectivity");
-	if (v.storeB != 128 || v.W > 64)
-		return setError(kErrUnsupported, "multibin batches support up to 64 waves");
+	// the start-packed kernels: rank 1, one reflectivity, <= 64 waves,
+	// 128-event store blocks; anything else is batched with the bins' own
+	// FdF kernels
+	const bool general = !(v.R == 1 && v.W0 == 0 && v.storeB == 128 && v.W <= 64);
 	if (M->bins.empty()) {
+		M->general = general;
 		M->W = v.W;
 		M->P = v.P;
 		M->slotRe = v.slotRe;
@@ -481,8 +534,8 @@ int pwa_multibin_add_bin(pwa_multibin* M, pwa_likelihood* L, uint32_t nStarts)
 		M->cauchyWidth = v.cauchyWidth;
 		PWA_TRY(deviceInfo(&M->device, &M->numSMs, &M->maxSmem));
 		PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking), "stream"));
-	} else if (v.W != M->W || v.P != M->P || v.slotRe != M->slotRe || v.slotIm != M->slotIm ||
-	           v.prior != M->prior || v.cauchyWidth != M->cauchyWidth) {
+	} else if (general != M->general || v.W != M->W || v.P != M->P || v.slotRe != M->slotRe ||
+	           v.slotIm != M->slotIm || v.prior != M->prior || v.cauchyWidth != M->cauchyWidth) {
 		return setError(kErrArg, "multibin: every bin needs the same wave set, parameter layout and prior");
 	}
 	M->bins.push_back(pwa_multibin::Bin{L, v, nStarts});
@@ -608,6 +661,8 @@ int pwa_multibin_autotune(pwa_multibin* M, const double* x)
 		return setError(kErrArg, "null argument");
 	static const uint32_t cand[] = {4, 8, 16, 32, 64};
 	PWA_TRY(ensureBuilt(M));
+	if (M->general)
+		return kOk;  // each bin's FdF plan was tuned by its likelihood
 	for (int c = 0; c < 3; ++c) {
 		uint32_t best = M->chunkTiles[c];
 		float bestMs = 1e30f;
@@ -640,10 +695,19 @@ int pwa_multibin_fit(pwa_multibin* M, const double* x0, int useGraph, uint32_t s
 	const size_t Q = (size_t)M->Q, P = (size_t)M->P;
 	cudaStream_t s = M->stream;
 	M->stateValid = false;
-	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dX.p, x0, Q * P * sizeof(double), cudaMemcpyHostToDevice, s), "upload"));
+	// parameters held fixed start (and stay) at 0
+	std::vector<double> start(x0, x0 + Q * P);
+	size_t q = 0;
+	for (const auto& B : M->bins)
+		for (uint32_t k = 0; k < B.nStarts; ++k, ++q)
+			for (size_t i = 0; i < P; ++i)
+				if (B.v.fixed[i])
+					start[q * P + i] = 0.;
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(M->dX.p, start.data(), Q * P * sizeof(double), cudaMemcpyHostToDevice, s),
+	                  "upload"));
 	for (DevBuf* b : {&M->dStatus, &M->dIter, &M->dNBack, &M->dHist, &M->dHead, &M->dItBest})
 		PWA_TRY(cudaCheck(cudaMemsetAsync(b->p, 0, Q * sizeof(int), s), "memset"));
-	PWA_TRY(startSweep(M, x0));
+	PWA_TRY(startSweep(M, start.data()));
 	M->sweepsDone = 0;
 	M->stateValid = true;
 	return runFit(M, useGraph, sweepsPerGraph, maxSweeps, x, f, gnorm, status, iterations, sweeps);

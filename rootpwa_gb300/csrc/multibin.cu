@@ -4,8 +4,12 @@
 //
 // A "problem" is one (bin, start point) pair with its own parameter vector in
 // the pwaLikelihood layout (partialWaveFit/pwaLikelihood.cc:1487-1556).  All
-// bins share the wave set (rank 1, one reflectivity).  One sweep evaluates
-// every active problem at its trial point:
+// bins share the wave set.  For rank 1 with one reflectivity and at most 64
+// waves one sweep evaluates every active problem at its trial point with the
+// start-packed kernels below; other layouts (any rank, both reflectivities)
+// evaluate each problem with its bin's own FdF kernel (fdf_kernels.cu,
+// returning at once for converged problems) and gatherEvalKernel.  Packed
+// layouts:
 //   fdfBatchKernel   -- persistent blocks walk a list of work items
 //                       (bin, group of SG starts, range of 128-event tiles);
 //                       each tile is loaded once by a bulk copy and used for all
@@ -421,6 +425,36 @@ __global__ void batchFinishKernel(const FinishBatchArgs a)
 		a.f[q] = fLL + nEvt * (norm + flat * flat * bin.totAcc) + prior;
 		g[P - 1] = flat * fC + twice * flat * bin.totAcc;
 	}
+	// parameters the layout holds fixed do not move: their gradient
+	// components are 0 to the minimiser (the reference strips them,
+	// highLevelInterface/pwaNloptFit.cc:383-401)
+	__syncwarp();
+	const unsigned char* fx = a.fixed + (size_t)pd.bin * P;
+	for (int i = lane; i < P; i += 32)
+		if (fx[i])
+			g[i] = 0.;
+}
+
+// General-layout batches: problem q's FdF launch wrote [f, gradient, device
+// status] to out[q]; copy f and the gradient (fixed components 0) into the
+// L-BFGS buffers.  One warp per problem.
+__global__ void gatherEvalKernel(const GatherEvalArgs a)
+{
+	const int q = (int)((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5);
+	const int lane = threadIdx.x & 31;
+	if (q >= a.Q || !a.active[q])
+		return;
+	const int P = a.P;
+	const double* o = a.out + (size_t)q * (P + 2);
+	const unsigned char* fx = a.fixed + (size_t)a.problems[q].bin * P;
+	double* g = a.g + (size_t)q * P;
+	for (int i = lane; i < P; i += 32)
+		g[i] = fx[i] ? 0. : o[1 + i];
+	if (lane == 0) {
+		a.f[q] = o[0];
+		if (o[P + 1] != 0.)
+			atomicOr(a.devErr, (unsigned)o[P + 1]);
+	}
 }
 
 // ---------------------------------------------------------------------------
@@ -694,6 +728,15 @@ int launchBatchFinish(const FinishBatchArgs& a, cudaStream_t s)
 	batchFinishKernel<<<std::max(blocks, 1), threads, 0, s>>>(a);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "batch finish launch");
+}
+
+int launchGatherEval(const GatherEvalArgs& a, cudaStream_t s)
+{
+	const int threads = 256;
+	const int blocks = (int)((a.Q * 32ull + threads - 1) / threads);
+	gatherEvalKernel<<<std::max(blocks, 1), threads, 0, s>>>(a);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "gather launch");
 }
 
 int launchLbfgs(const LbfgsArgs& a, cudaStream_t s)

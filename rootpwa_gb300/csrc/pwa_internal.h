@@ -97,6 +97,7 @@ struct FdfArgs {
 	unsigned* counter;       // device, arrival counter, zero between launches
 	unsigned* devErr;        // device error flags
 	double* out;             // device, [P + 2]: f, gradient, device error status
+	const int* active;       // device flag or null: when it is 0 the launch does nothing (batched fits)
 };
 
 // Store block size for a wave set: 128 when two 128-event tiles fit in shared
@@ -174,8 +175,16 @@ struct LikelihoodView {
 	int prior;
 	double cauchyWidth;
 	int device;
+	std::vector<unsigned char> fixed;  // [P] 1 for parameters the layout holds fixed
 };
 int likelihoodView(const pwa_likelihood* L, LikelihoodView* v);
+// One launch of the likelihood's own FdF kernel (its plan, any rank and
+// reflectivities) at device parameters dPar into dOut [P + 2] on stream s;
+// with dActive non-null the launch returns at once when *dActive == 0.
+// Stream-ordered, no synchronisation or allocation (capturable).
+int launchLikelihoodEval(pwa_likelihood* L, const double* dPar, double* dOut, const int* dActive, cudaStream_t s);
+// clears the likelihood's device error flag (stream-ordered)
+int clearLikelihoodError(pwa_likelihood* L, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Batched multibin x multistart FdF and L-BFGS (multibin.cu)
@@ -219,9 +228,24 @@ struct FinishBatchArgs {
 	const double* partials;
 	int prior;
 	double cauchyWidth;
+	const unsigned char* fixed;  // [bins][P] parameters held fixed (gradient components set to 0)
 	double* f;           // [Q]
 	double* g;           // [Q][P]
 };
+// general-layout batches: f and the gradient of every active problem from
+// its FdF launch's output [Q][P + 2] into the L-BFGS buffers, fixed
+// parameters' gradient components set to 0, device error flags collected
+struct GatherEvalArgs {
+	int Q, P;
+	const double* out;           // [Q][P + 2]
+	const int* active;           // [Q]
+	const ProblemDesc* problems; // [Q]
+	const unsigned char* fixed;  // [bins][P]
+	double* f;                   // [Q]
+	double* g;                   // [Q][P]
+	unsigned* devErr;
+};
+int launchGatherEval(const GatherEvalArgs& a, cudaStream_t s);
 enum { kLbfgsInit = 0, kLbfgsSearch = 1, kLbfgsConverged = 2, kLbfgsMaxIter = 3, kLbfgsStalled = 4, kLbfgsFailed = 5,
        kLbfgsFloor = 6 };
 struct LbfgsArgs {
