@@ -220,8 +220,9 @@ int pwa_likelihood_set_store_block(pwa_likelihood* L, uint32_t events);
  * (adjacent events share each V load; 2 and 4 read them with 128-bit loads;
  * 4 needs rank <= 2 and 128-event tiles), 3 the fused-gradient kernel (each
  * warp contracts its own events' gradient from registers; rank <= 2,
- * 128-event tiles); 0 keeps the current one.  The autotuner times all that
- * fit. */
+ * 128-event tiles), 5 the narrow kernel for small wave sets (one event per
+ * thread, rank x waves <= 16: rank 1 up to 16 waves, rank 2 up to 8); 0
+ * keeps the current one.  The autotuner times all that fit. */
 int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events);
 int pwa_likelihood_plan_variant(const pwa_likelihood* L, int* phase1Events);
 /*

@@ -77,7 +77,7 @@ def build(force=False, ptxas_verbose=False, verbose=False):
 LIB_DEBUG = os.path.join(HERE, "libpwa_gb300_debug.so")
 BUILD_DEBUG = os.path.join(HERE, "_build_debug")
 # translation units rebuilt with the shared-memory bounds checks compiled in
-DEBUG_SOURCES = ("fdf_kernels.cu", "fdf_fused.cu")
+DEBUG_SOURCES = ("fdf_kernels.cu", "fdf_fused.cu", "fdf_narrow.cu")
 
 
 def build_debug():

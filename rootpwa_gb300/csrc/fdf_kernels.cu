@@ -810,6 +810,21 @@ int planCandidates(int W0, int W, int R, int B, uint64_t nEvents, int numSMs, si
 			p.smemBytes = need;
 			out->push_back(p);
 		}
+	// the narrow variant for small wave sets, two to four stages where they fit
+	if (B == 128)
+		for (int st = 2; st <= 4; ++st) {
+			const size_t need = narrowFdfSmem(W, R, st);
+			if (need == 0 || need + 1024 > maxSmem)
+				break;
+			FdfPlan p;
+			p.E = B;
+			p.stages = st;
+			p.wpw = wpw;
+			p.phase1Events = 5;
+			p.blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)numSMs, narrowFdfTiles(nEvents)));
+			p.smemBytes = need;
+			out->push_back(p);
+		}
 	return kOk;
 }
 
@@ -817,6 +832,8 @@ size_t fdfAccumulatorWords(int nPartial) { return (size_t)kReplicas * kLimbs * (
 
 int launchFdf(const FdfPlan& p, const FdfArgs& a, cudaStream_t s)
 {
+	if (p.phase1Events == 5)
+		return launchFdfNarrow(p, a, s);
 	if (p.phase1Events == 3) {
 		if (a.reduction == 0)
 			return launchFdfFused(p, a, s);

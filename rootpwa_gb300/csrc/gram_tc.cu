@@ -26,12 +26,18 @@
 // The tensor cores add into FP32 accumulators with truncation, so a long
 // chain of accumulations drifts towards zero by a fraction of an ulp per
 // instruction.  The accumulators therefore start from zero every `period`
-// tiles, and four drain warps (10..13) add them into a second pair of FP32
-// accumulators in tensor memory with round-to-nearest additions; cross
+// tiles, and eight drain warps (10..17, two per tensor-memory lane quarter,
+// each taking every other 16-column chunk) add them into a second pair of
+// FP32 accumulators in tensor memory with round-to-nearest additions; cross
 // products come first in each tile so that their truncation acts on small
-// partial sums.  At the end the drain warps store the CTA's FP32 partials; a
-// second kernel sums the partials of all CTAs in FP64 in a fixed order and
-// assembles the Hermitian matrix.
+// partial sums.  The Re and D accumulators are drained separately: the MMA
+// warp issues a tile's Re products, then its D products, and signals each
+// group's end on its own barrier, so the drain of Re runs while the D
+// products execute and the drain of D while the next tile's Re products
+// execute; the MMA warp waits only for the drain of the accumulator it is
+// about to restart.  At the end the drain warps store the CTA's FP32
+// partials; a second kernel sums the partials of all CTAs in FP64 in a fixed
+// order and assembles the Hermitian matrix.
 //
 // Every wait on an mbarrier is bounded (1 s of globaltimer): on expiry the
 // CTA records kDevErrTimeout, stops issuing work, waits (bounded) for its own
@@ -60,8 +66,9 @@ constexpr int kKTB = 64;                  // events per tile of the BF16 variant
 constexpr int kConvWarps = 8;             // converter warps 0..7
 constexpr int kTmaWarp = kConvWarps;      // warp 8
 constexpr int kMmaWarp = kConvWarps + 1;  // warp 9
-constexpr int kDrainWarp0 = kConvWarps + 2;  // warps 10..13 (one warpgroup)
-constexpr int kThreadsTc = (kConvWarps + 6) * 32;
+constexpr int kDrainWarp0 = kConvWarps + 2;  // warps 10..17 (two warpgroups)
+constexpr int kDrainWarps = 8;
+constexpr int kThreadsTc = (kConvWarps + 2 + kDrainWarps) * 32;
 constexpr int kOpBufs = 2;
 constexpr int kTmemCols = 512;
 constexpr uint32_t kPlaneBytes = 256u * 128u;  // Ar rows 0..127, Ai rows 128..255
@@ -254,9 +261,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 	uint64_t* rawEmpty = bars + a.stages;
 	uint64_t* opFull = bars + 2 * a.stages;
 	uint64_t* opEmpty = opFull + kOpBufs;
-	uint64_t* drainReady = opEmpty + kOpBufs;
-	uint64_t* drainDone = drainReady + 1;
-	uint64_t* mmaFinal = drainDone + 1;
+	uint64_t* drainReady = opEmpty + kOpBufs;  // [2]: Re, D accumulators complete for a drain
+	uint64_t* drainDone = drainReady + 2;      // [2]: Re, D accumulators read by the drain
+	uint64_t* mmaFinal = drainDone + 2;
 	uint32_t* tmemHolder = reinterpret_cast<uint32_t*>(mmaFinal + 1);
 	__shared__ unsigned sFail;
 
@@ -275,8 +282,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 			barInit(&opFull[b], kConvWarps);
 			barInit(&opEmpty[b], 1);
 		}
-		barInit(drainReady, 1);
-		barInit(drainDone, 4);
+		for (int x = 0; x < 2; ++x) {
+			barInit(&drainReady[x], 1);
+			barInit(&drainDone[x], kDrainWarps);
+		}
 		barInit(mmaFinal, 1);
 		sFail = 0u;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -346,18 +355,25 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 					fresh = false;
 				}
 			};
-			for (int t = 0; t < nT; ++t) {
-				const int b = t % kOpBufs;
+			// waits (bounded) for the drain of accumulator x before a period restarts it
+			auto drained = [&](int x, int t) {
 				if (t > 0 && t % a.period == 0) {
-					// the drain of the previous period has read the working accumulators
-					if (!barWait(drainDone, (uint32_t)(((t / a.period) - 1) & 1))) {
+					if (!barWait(&drainDone[x], (uint32_t)(((t / a.period) - 1) & 1))) {
 						atomicOr(a.devErr, (unsigned)kDevErrTimeout);
 						sFail = 1u;
-						break;
+						return false;
 					}
 					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-					freshRe = freshD = true;
+					if (x == 0)
+						freshRe = true;
+					else
+						freshD = true;
 				}
+				return true;
+			};
+			for (int t = 0; t < nT; ++t) {
+				const int b = t % kOpBufs;
+				const bool last = (t + 1) % a.period == 0 || t + 1 == nT;
 				if (!barWait(&opFull[b], (uint32_t)((t / kOpBufs) & 1))) {
 					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
 					sFail = 1u;
@@ -366,21 +382,31 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 				const uint32_t hi = opBase + (uint32_t)b * a.planes * kPlaneBytes;
 				const uint32_t arH = hi, aiH = hi + 16384u;
+				const uint32_t arL = hi + kPlaneBytes, aiL = arL + 16384u;
+				// Re = Ar Ar^T + Ai Ai^T: cross products first
+				if (!drained(0, t))
+					break;
 				if (a.planes == 2) {
-					const uint32_t arL = hi + kPlaneBytes, aiL = arL + 16384u;
 					product(accRe, freshRe, arH, arL);
 					product(accRe, freshRe, arL, arH);
 					product(accRe, freshRe, aiH, aiL);
 					product(accRe, freshRe, aiL, aiH);
-					product(accD, freshD, aiH, arL);
-					product(accD, freshD, aiL, arH);
 				}
 				product(accRe, freshRe, arH, arH);
 				product(accRe, freshRe, aiH, aiH);
+				if (last)
+					mmaCommit(&drainReady[0]);
+				// D = Ai Ar^T
+				if (!drained(1, t))
+					break;
+				if (a.planes == 2) {
+					product(accD, freshD, aiH, arL);
+					product(accD, freshD, aiL, arH);
+				}
 				product(accD, freshD, aiH, arH);
 				mmaCommit(&opEmpty[b]);
-				if ((t + 1) % a.period == 0 || t + 1 == nT)
-					mmaCommit(drainReady);
+				if (last)
+					mmaCommit(&drainReady[1]);
 			}
 			// all MMAs of this CTA complete before tensor memory is freed
 			mmaCommit(mmaFinal);
@@ -389,43 +415,63 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 		}
 	} else if (warp >= kDrainWarp0) {
 		// ---- drain: sums += working accumulators (round to nearest) ----
-		const int q = warp & 3;  // lane quarter of tensor memory
+		// warp w reaches tensor-memory lanes 32 (w % 4) ..; the two drain
+		// warps of a lane quarter take alternate 16-column chunks
+		const int q = warp & 3;
+		const int half = (warp - kDrainWarp0) >> 2;
 		const uint32_t rowBase = tmem + ((uint32_t)(q * 32) << 16);
+		const int nChunks = N / 16;  // per accumulator
 		bool ok = true;
-		for (int d = 0; d < nDrains; ++d) {
-			if (!barWait(drainReady, (uint32_t)(d & 1))) {
-				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
-				ok = false;
-				break;
-			}
-			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-			for (int c = 0; c < 2 * N; c += 16) {
-				uint32_t w[16], s[16];
-				tmemLd16(rowBase + (uint32_t)c, w);
-				if (d > 0)
-					tmemLd16(rowBase + (uint32_t)(2 * N + c), s);
-				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-				if (d > 0)
+		for (int d = 0; d < nDrains && ok; ++d) {
+			for (int x = 0; x < 2; ++x) {  // Re [0, N) -> [2N, 3N), D [N, 2N) -> [3N, 4N)
+				if (!barWait(&drainReady[x], (uint32_t)(d & 1))) {
+					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+					ok = false;
+					break;
+				}
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				const uint32_t work = rowBase + (uint32_t)(x * N), sums = rowBase + (uint32_t)((2 + x) * N);
+				// two chunks per round trip: their loads are in flight together
+				for (int c0 = half; c0 < nChunks; c0 += 4) {
+					const int c1 = c0 + 2;
+					const bool two = c1 < nChunks;
+					uint32_t w0[16], w1[16], s0[16], s1[16];
+					tmemLd16(work + (uint32_t)(16 * c0), w0);
+					if (two)
+						tmemLd16(work + (uint32_t)(16 * c1), w1);
+					if (d > 0) {
+						tmemLd16(sums + (uint32_t)(16 * c0), s0);
+						if (two)
+							tmemLd16(sums + (uint32_t)(16 * c1), s1);
+					}
+					asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+					if (d > 0) {
 #pragma unroll
-					for (int i = 0; i < 16; ++i)
-						w[i] = __float_as_uint(__uint_as_float(w[i]) + __uint_as_float(s[i]));
-				tmemSt16(rowBase + (uint32_t)(2 * N + c), w);
+						for (int i = 0; i < 16; ++i) {
+							w0[i] = __float_as_uint(__uint_as_float(w0[i]) + __uint_as_float(s0[i]));
+							w1[i] = __float_as_uint(__uint_as_float(w1[i]) + __uint_as_float(s1[i]));
+						}
+					}
+					tmemSt16(sums + (uint32_t)(16 * c0), w0);
+					if (two)
+						tmemSt16(sums + (uint32_t)(16 * c1), w1);
+				}
+				asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+				asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+				__syncwarp();
+				if (lane == 0)
+					barArrive(&drainDone[x]);
 			}
-			asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-			__syncwarp();
-			if (lane == 0)
-				barArrive(drainDone);
 		}
 		if (ok) {
-			// partials of this CTA: [2][128][N], rows < W
+			// partials of this CTA: [2][128][N], rows < W; this warp's chunks
 			const int row = q * 32 + lane;
-			for (int c = 0; c < 2 * N; c += 16) {
+			for (int c = half; c < 2 * nChunks; c += 2) {
 				uint32_t r[16];
-				tmemLd16(rowBase + (uint32_t)(2 * N + c), r);
+				tmemLd16(rowBase + (uint32_t)(2 * N + 16 * c), r);
 				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 				if (row < W) {
-					const int part = c / N, col = c - part * N;
+					const int part = c / nChunks, col = 16 * c - part * N;
 					float4* d4 = reinterpret_cast<float4*>(
 					    a.partials + (((size_t)blockIdx.x * 2 + part) * 128 + row) * N + col);
 #pragma unroll

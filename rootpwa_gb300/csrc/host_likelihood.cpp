@@ -753,9 +753,9 @@ int pwa_likelihood_set_plan(pwa_likelihood* L, int stages)
 int pwa_likelihood_set_plan_variant(pwa_likelihood* L, int stages, int phase1Events)
 {
 	PWA_TRY(checkFinished(L));
-	if (phase1Events < 0 || phase1Events > 4)
-		return setError(kErrArg,
-		                "FdF kernel variant must be 1, 2 or 4 (events per lane), 3 (fused gradient) or 0 (keep)");
+	if (phase1Events < 0 || phase1Events > 5)
+		return setError(kErrArg, "FdF kernel variant must be 1, 2 or 4 (events per lane), 3 (fused gradient), "
+		                         "5 (narrow, one event per thread) or 0 (keep)");
 	const int ne = phase1Events ? phase1Events : L->plan.phase1Events;
 	std::vector<FdfPlan> cands;
 	PWA_TRY(planCandidates((int)L->nW[0], (int)L->W(), (int)L->rank, (int)L->storeB, L->nEvents, L->numSMs, L->maxSmem,

@@ -73,7 +73,7 @@ struct FdfPlan {
 	int E = 128;        // events per tile (= store block)
 	int stages = 2;     // shared-memory pipeline depth
 	int wpw = 2;        // wave bucket per warp (template)
-	int phase1Events = 2;  // events per lane in the coherent-sum phase (1 or 2; 3: fused-gradient variant)
+	int phase1Events = 2;  // events per lane in the coherent-sum phase (1, 2 or 4; 3: fused-gradient variant; 5: narrow variant)
 	int blocks = 0;     // grid size (persistent, <= #SMs)
 	size_t smemBytes = 0;
 };
@@ -114,6 +114,12 @@ size_t fdfAccumulatorWords(int nPartial);
 // Dynamic shared memory it needs for `stages` stages, 0 when unsupported.
 size_t fusedFdfSmem(int W0, int W, int R, int stages);
 int launchFdfFused(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
+// Narrow FdF variant for small wave sets (fdf_narrow.cu, plan phase1Events
+// == 5): one event per thread, 512-event tiles, rank x waves <= 16.
+int narrowMaxWaves(int R);
+size_t narrowFdfSmem(int W, int R, int stages);
+uint64_t narrowFdfTiles(uint64_t nEvents);
+int launchFdfNarrow(const FdfPlan& plan, const FdfArgs& args, cudaStream_t s);
 
 // Converts one wave w of amplitudes (complex64 or complex128, device memory)
 // into the tiled complex64 store, divided by `divisor` in FP64; sets *nonzero

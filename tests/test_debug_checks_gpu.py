@@ -25,13 +25,14 @@ import rootpwa_gb300 as R
 from rootpwa_gb300 import _native as N
 assert N.LIB_PATH.endswith("libpwa_gb300_debug.so")
 from test_fdf_gpu import stress_workload, pair, check_point
-shapes = [(0, 15, 1, 20000), (7, 80, 2, 30001), (3, 5, 1, 127), (2, 9, 3, 129), (20, 120, 1, 4099), (10, 54, 4, 3000)]
+shapes = [(0, 15, 1, 20000), (7, 80, 2, 30001), (3, 5, 1, 127), (2, 9, 3, 129), (20, 120, 1, 4099), (10, 54, 4, 3000),
+          (5, 0, 2, 1000)]
 runs = 0
 for n_neg, n_pos, rank, n in shapes:
     w = stress_workload(n_neg, n_pos, rank, n, flat=1.0)
     O, G = pair(w)
     stages = G.plan()[1]
-    for ne in (1, 2, 3, 4):
+    for ne in (1, 2, 3, 4, 5):
         try:
             G.setPlan(stages, ne)
         except R.PwaError:

@@ -111,12 +111,14 @@ def test_shapes_against_oracle(n_neg, n_pos, rank, n_data):
     O, G = pair(w)
     stages = G.plan()[1]
     # every kernel variant the shape supports: one, two or four (rank <= 2,
-    # 128-event tiles) events per lane in the coherent-sum phase, and the
-    # fused-gradient kernel (rank <= 2, 128-event tiles)
+    # 128-event tiles) events per lane in the coherent-sum phase, the
+    # fused-gradient kernel (rank <= 2, 128-event tiles) and the narrow
+    # kernel (one event per thread; rank 1 up to 16 waves, rank 2 up to 8)
     fused_ok = rank <= 2 and G.plan()[0] == 128 and n_neg <= 16 and 1 <= n_pos <= 104
     four_ok = rank <= 2 and G.plan()[0] == 128
-    for ne in (1, 2, 3, 4):
-        if (ne == 3 and not fused_ok) or (ne == 4 and not four_ok):
+    narrow_ok = G.plan()[0] == 128 and n_neg + n_pos <= {1: 16, 2: 8}.get(rank, 0)
+    for ne in (1, 2, 3, 4, 5):
+        if (ne == 3 and not fused_ok) or (ne == 4 and not four_ok) or (ne == 5 and not narrow_ok):
             with pytest.raises(R.PwaError):
                 G.setPlan(stages, ne)
             continue

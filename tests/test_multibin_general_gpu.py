@@ -39,7 +39,7 @@ def test_general_layout_batched_fdf_equals_each_bins_likelihood():
     # threshold-fixed waves
     wa = workload(7, 20, 2, 3001, seed=41)
     wb = workload(7, 20, 2, 12011, seed=42)
-    th = thresholds(27, [2, 9, 15], 2.0)
+    th = thresholds(27, [2, 9, 15], 3.0)     # at or above the bin centre 2.5: fixed
     La = helpers.build_gpu(wa, *helpers.gpu_integrals(wa))
     Lb = helpers.build_gpu(wb, *helpers.gpu_integrals(wb), thresholds=th, mass_bin_center=2.5)
     assert La.nmbParsFixed() == 0 and Lb.nmbParsFixed() > 0
@@ -70,7 +70,7 @@ def test_production_shape_multistart_fit_with_fixed_waves():
     every fitted point are exactly 0."""
     scipy_opt = pytest.importorskip("scipy.optimize")
     w = workload(7, 80, 2, 8000, seed=43, n_mc=6000)
-    th = thresholds(87, [1, 30, 60], 3.0)
+    th = thresholds(87, [1, 30, 60], 3.5)    # at or above the bin centre 3.2: fixed
     kw = dict(thresholds=th, mass_bin_center=3.2)
     on, oa, gn, ga = helpers.integral_pairs(w)
     O = helpers.build_oracle(w, on, oa, **kw)
