@@ -26,18 +26,22 @@
 // The tensor cores add into FP32 accumulators with truncation, so a long
 // chain of accumulations drifts towards zero by a fraction of an ulp per
 // instruction.  The accumulators therefore start from zero every `period`
-// tiles, and eight drain warps (10..17, two per tensor-memory lane quarter,
-// each taking every other 16-column chunk) add them into a second pair of
-// FP32 accumulators in tensor memory with round-to-nearest additions; cross
-// products come first in each tile so that their truncation acts on small
-// partial sums.  The Re and D accumulators are drained separately: the MMA
-// warp issues a tile's Re products, then its D products, and signals each
-// group's end on its own barrier, so the drain of Re runs while the D
-// products execute and the drain of D while the next tile's Re products
-// execute; the MMA warp waits only for the drain of the accumulator it is
-// about to restart.  At the end the drain warps store the CTA's FP32
-// partials; a second kernel sums the partials of all CTAs in FP64 in a fixed
-// order and assembles the Hermitian matrix.
+// tiles and are drained into round-to-nearest FP32 sums; cross products come
+// first in each tile so that their truncation acts on small partial sums.
+// Two drain schemes:
+//   * up to 96 waves (N <= 96, the double-buffered kernel): two working
+//     pairs (Re, D) in tensor memory, 4N <= 384 columns; the MMAs of period
+//     p go to pair p % 2 while sixteen drain warps (10..25, four per
+//     tensor-memory lane quarter) add pair (p - 1) % 2 into sums they keep in
+//     registers (at most 48 per thread), so the tensor pipe does not wait
+//     for a drain unless a drain takes longer than a period's MMAs;
+//   * wider sets (the single-buffered kernel): one working pair, sums in
+//     tensor memory (4N <= 512 columns), four drain warps (10..13); the MMA
+//     warp waits for each drain before the next period.
+// The additions are the same in both, in the same order.  At the end the
+// drain warps store the CTA's FP32 partials; a second kernel sums the
+// partials of all CTAs in FP64 in a fixed order and assembles the Hermitian
+// matrix.
 //
 // Every wait on an mbarrier is bounded (1 s of globaltimer): on expiry the
 // CTA records kDevErrTimeout, stops issuing work, waits (bounded) for its own
@@ -66,9 +70,14 @@ constexpr int kKTB = 64;                  // events per tile of the BF16 variant
 constexpr int kConvWarps = 8;             // converter warps 0..7
 constexpr int kTmaWarp = kConvWarps;      // warp 8
 constexpr int kMmaWarp = kConvWarps + 1;  // warp 9
-constexpr int kDrainWarp0 = kConvWarps + 2;  // warps 10..17 (two warpgroups)
-constexpr int kDrainWarps = 8;
-constexpr int kThreadsTc = (kConvWarps + 2 + kDrainWarps) * 32;
+constexpr int kDrainWarp0 = kConvWarps + 2;  // first drain warp (10..13, or 10..25 double-buffered)
+constexpr int kThreadsTc = (kConvWarps + 6) * 32;
+// double-buffered kernel: sixteen drain warps (10..25, four per lane
+// quarter), sums in registers
+constexpr int kDrainWarpsDB = 16;
+constexpr int kThreadsDB = (kConvWarps + 2 + kDrainWarpsDB) * 32;
+constexpr int kMaxNDB = 96;          // 2N / 8 = 24 chunks of 8 columns, 6 per drain warp
+constexpr int kChunksPerWarpDB = 6;
 constexpr int kOpBufs = 2;
 constexpr int kTmemCols = 512;
 constexpr uint32_t kPlaneBytes = 256u * 128u;  // Ar rows 0..127, Ai rows 128..255
@@ -246,7 +255,16 @@ __device__ __forceinline__ void tmemSt16(uint32_t taddr, const uint32_t (&r)[16]
 	    : "memory");
 }
 
-__global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_constant__ CUtensorMap map, const TcArgs a)
+__device__ __forceinline__ void tmemLd8(uint32_t taddr, uint32_t (&r)[8])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+	             : "r"(taddr));
+}
+
+template <bool DB>
+__global__ void __launch_bounds__(DB ? kThreadsDB : kThreadsTc, 1)
+    gramTcKernel(const __grid_constant__ CUtensorMap map, const TcArgs a)
 {
 	extern __shared__ __align__(1024) unsigned char smemRaw[];
 	unsigned char* smem =
@@ -261,8 +279,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 	uint64_t* rawEmpty = bars + a.stages;
 	uint64_t* opFull = bars + 2 * a.stages;
 	uint64_t* opEmpty = opFull + kOpBufs;
-	uint64_t* drainReady = opEmpty + kOpBufs;  // [2]: Re, D accumulators complete for a drain
-	uint64_t* drainDone = drainReady + 2;      // [2]: Re, D accumulators read by the drain
+	uint64_t* drainReady = opEmpty + kOpBufs;  // [2]: a working pair complete for a drain
+	uint64_t* drainDone = drainReady + 2;      // [2]: a working pair read by the drain
 	uint64_t* mmaFinal = drainDone + 2;
 	uint32_t* tmemHolder = reinterpret_cast<uint32_t*>(mmaFinal + 1);
 	__shared__ unsigned sFail;
@@ -284,7 +302,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 		}
 		for (int x = 0; x < 2; ++x) {
 			barInit(&drainReady[x], 1);
-			barInit(&drainDone[x], kDrainWarps);
+			barInit(&drainDone[x], DB ? kDrainWarpsDB : 4);
 		}
 		barInit(mmaFinal, 1);
 		sFail = 0u;
@@ -340,7 +358,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 		if (lane == 0) {
 			const uint32_t idesc = a.bf16 ? idescBf16(128, N) : idescTf32(128, N);
 			const uint32_t opBase = sAddr(ops);
-			const uint32_t accRe = tmem, accD = tmem + (uint32_t)N;
 			bool freshRe = true, freshD = true;
 			// one product over the tile: acc += A B^T, 4 instructions of 32
 			// bytes of K (8 TF32 or 16 BF16 elements)
@@ -355,25 +372,23 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 					fresh = false;
 				}
 			};
-			// waits (bounded) for the drain of accumulator x before a period restarts it
-			auto drained = [&](int x, int t) {
-				if (t > 0 && t % a.period == 0) {
-					if (!barWait(&drainDone[x], (uint32_t)(((t / a.period) - 1) & 1))) {
-						atomicOr(a.devErr, (unsigned)kDevErrTimeout);
-						sFail = 1u;
-						return false;
-					}
-					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-					if (x == 0)
-						freshRe = true;
-					else
-						freshD = true;
-				}
-				return true;
-			};
 			for (int t = 0; t < nT; ++t) {
 				const int b = t % kOpBufs;
-				const bool last = (t + 1) % a.period == 0 || t + 1 == nT;
+				// working pair of this period (double-buffered: period p uses pair p % 2)
+				const int p = t / a.period, x = DB ? (p & 1) : 0;
+				const uint32_t accRe = tmem + (uint32_t)(x * 2 * N), accD = accRe + (uint32_t)N;
+				if (t % a.period == 0 && p >= (DB ? 2 : 1)) {
+					// the drain of the last period that used this pair has read it
+					const uint32_t k = DB ? (uint32_t)(p / 2 - 1) : (uint32_t)(p - 1);
+					if (!barWait(&drainDone[x], k & 1u)) {
+						atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+						sFail = 1u;
+						break;
+					}
+					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				}
+				if (t % a.period == 0)
+					freshRe = freshD = true;
 				if (!barWait(&opFull[b], (uint32_t)((t / kOpBufs) & 1))) {
 					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
 					sFail = 1u;
@@ -382,96 +397,123 @@ __global__ void __launch_bounds__(kThreadsTc, 1) gramTcKernel(const __grid_const
 				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 				const uint32_t hi = opBase + (uint32_t)b * a.planes * kPlaneBytes;
 				const uint32_t arH = hi, aiH = hi + 16384u;
-				const uint32_t arL = hi + kPlaneBytes, aiL = arL + 16384u;
-				// Re = Ar Ar^T + Ai Ai^T: cross products first
-				if (!drained(0, t))
-					break;
 				if (a.planes == 2) {
+					const uint32_t arL = hi + kPlaneBytes, aiL = arL + 16384u;
 					product(accRe, freshRe, arH, arL);
 					product(accRe, freshRe, arL, arH);
 					product(accRe, freshRe, aiH, aiL);
 					product(accRe, freshRe, aiL, aiH);
-				}
-				product(accRe, freshRe, arH, arH);
-				product(accRe, freshRe, aiH, aiH);
-				if (last)
-					mmaCommit(&drainReady[0]);
-				// D = Ai Ar^T
-				if (!drained(1, t))
-					break;
-				if (a.planes == 2) {
 					product(accD, freshD, aiH, arL);
 					product(accD, freshD, aiL, arH);
 				}
+				product(accRe, freshRe, arH, arH);
+				product(accRe, freshRe, aiH, aiH);
 				product(accD, freshD, aiH, arH);
 				mmaCommit(&opEmpty[b]);
-				if (last)
-					mmaCommit(&drainReady[1]);
+				if ((t + 1) % a.period == 0 || t + 1 == nT)
+					mmaCommit(&drainReady[x]);
 			}
 			// all MMAs of this CTA complete before tensor memory is freed
 			mmaCommit(mmaFinal);
 			if (!barWait(mmaFinal, 0u))
 				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
 		}
-	} else if (warp >= kDrainWarp0) {
-		// ---- drain: sums += working accumulators (round to nearest) ----
-		// warp w reaches tensor-memory lanes 32 (w % 4) ..; the two drain
-		// warps of a lane quarter take alternate 16-column chunks
-		const int q = warp & 3;
-		const int half = (warp - kDrainWarp0) >> 2;
+	} else if (DB && warp >= kDrainWarp0) {
+		// ---- drain, double-buffered: register sums += working pair d % 2 ----
+		// warp w reaches tensor-memory lanes 32 (w % 4) ..; the four drain
+		// warps of a lane quarter take every fourth 8-column chunk of the pair
+		const int q = warp & 3, sub = (warp - kDrainWarp0) >> 2;
 		const uint32_t rowBase = tmem + ((uint32_t)(q * 32) << 16);
-		const int nChunks = N / 16;  // per accumulator
-		bool ok = true;
-		for (int d = 0; d < nDrains && ok; ++d) {
-			for (int x = 0; x < 2; ++x) {  // Re [0, N) -> [2N, 3N), D [N, 2N) -> [3N, 4N)
-				if (!barWait(&drainReady[x], (uint32_t)(d & 1))) {
-					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
-					ok = false;
-					break;
-				}
-				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-				const uint32_t work = rowBase + (uint32_t)(x * N), sums = rowBase + (uint32_t)((2 + x) * N);
-				// two chunks per round trip: their loads are in flight together
-				for (int c0 = half; c0 < nChunks; c0 += 4) {
-					const int c1 = c0 + 2;
-					const bool two = c1 < nChunks;
-					uint32_t w0[16], w1[16], s0[16], s1[16];
-					tmemLd16(work + (uint32_t)(16 * c0), w0);
-					if (two)
-						tmemLd16(work + (uint32_t)(16 * c1), w1);
-					if (d > 0) {
-						tmemLd16(sums + (uint32_t)(16 * c0), s0);
-						if (two)
-							tmemLd16(sums + (uint32_t)(16 * c1), s1);
-					}
-					asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-					if (d > 0) {
+		const int nch = 2 * N / 8;  // chunks of a working pair (Re then D)
+		float acc[kChunksPerWarpDB][8];
 #pragma unroll
-						for (int i = 0; i < 16; ++i) {
-							w0[i] = __float_as_uint(__uint_as_float(w0[i]) + __uint_as_float(s0[i]));
-							w1[i] = __float_as_uint(__uint_as_float(w1[i]) + __uint_as_float(s1[i]));
-						}
-					}
-					tmemSt16(sums + (uint32_t)(16 * c0), w0);
-					if (two)
-						tmemSt16(sums + (uint32_t)(16 * c1), w1);
-				}
-				asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-				asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-				__syncwarp();
-				if (lane == 0)
-					barArrive(&drainDone[x]);
+		for (int j = 0; j < kChunksPerWarpDB; ++j)
+#pragma unroll
+			for (int i = 0; i < 8; ++i)
+				acc[j][i] = 0.f;
+		bool ok = true;
+		for (int d = 0; d < nDrains; ++d) {
+			const int x = d & 1;
+			if (!barWait(&drainReady[x], (uint32_t)((d >> 1) & 1))) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				ok = false;
+				break;
 			}
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			const uint32_t pair = rowBase + (uint32_t)(x * 2 * N);
+#pragma unroll
+			for (int j = 0; j < kChunksPerWarpDB; ++j) {
+				const int c = sub + 4 * j;
+				if (c < nch) {
+					uint32_t w[8];
+					tmemLd8(pair + (uint32_t)(8 * c), w);
+					asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+					for (int i = 0; i < 8; ++i)
+						acc[j][i] += __uint_as_float(w[i]);
+				}
+			}
+			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+			__syncwarp();
+			if (lane == 0)
+				barArrive(&drainDone[x]);
 		}
 		if (ok) {
-			// partials of this CTA: [2][128][N], rows < W; this warp's chunks
+			// partials of this CTA: [2][128][N], rows < W
 			const int row = q * 32 + lane;
-			for (int c = half; c < 2 * nChunks; c += 2) {
+			if (row < W) {
+#pragma unroll
+				for (int j = 0; j < kChunksPerWarpDB; ++j) {
+					const int c = sub + 4 * j;
+					if (c < nch) {
+						const int part = (8 * c) / N, col = 8 * c - part * N;
+						float4* d4 = reinterpret_cast<float4*>(
+						    a.partials + (((size_t)blockIdx.x * 2 + part) * 128 + row) * N + col);
+						d4[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+						d4[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+					}
+				}
+			}
+		}
+	} else if (!DB && warp >= kDrainWarp0) {
+		// ---- drain, single-buffered: sums += working accumulators (round to nearest) ----
+		const int q = warp & 3;  // lane quarter of tensor memory
+		const uint32_t rowBase = tmem + ((uint32_t)(q * 32) << 16);
+		bool ok = true;
+		for (int d = 0; d < nDrains; ++d) {
+			if (!barWait(&drainReady[0], (uint32_t)(d & 1))) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				ok = false;
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+			for (int c = 0; c < 2 * N; c += 16) {
+				uint32_t w[16], s[16];
+				tmemLd16(rowBase + (uint32_t)c, w);
+				if (d > 0)
+					tmemLd16(rowBase + (uint32_t)(2 * N + c), s);
+				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+				if (d > 0)
+#pragma unroll
+					for (int i = 0; i < 16; ++i)
+						w[i] = __float_as_uint(__uint_as_float(w[i]) + __uint_as_float(s[i]));
+				tmemSt16(rowBase + (uint32_t)(2 * N + c), w);
+			}
+			asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+			asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+			__syncwarp();
+			if (lane == 0)
+				barArrive(&drainDone[0]);
+		}
+		if (ok) {
+			// partials of this CTA: [2][128][N], rows < W
+			const int row = q * 32 + lane;
+			for (int c = 0; c < 2 * N; c += 16) {
 				uint32_t r[16];
-				tmemLd16(rowBase + (uint32_t)(2 * N + 16 * c), r);
+				tmemLd16(rowBase + (uint32_t)(2 * N + c), r);
 				asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 				if (row < W) {
-					const int part = c / nChunks, col = 16 * c - part * N;
+					const int part = c / N, col = c - part * N;
 					float4* d4 = reinterpret_cast<float4*>(
 					    a.partials + (((size_t)blockIdx.x * 2 + part) * 128 + row) * N + col);
 #pragma unroll
@@ -680,10 +722,17 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	if (cr != CUDA_SUCCESS)
 		return setError(kErrCuda, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
 
-	PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                                             (int)smemBytes),
-	                        "gram TC smem attribute"));
-	gramTcKernel<<<grid, kThreadsTc, smemBytes, s>>>(map, a);
+	if (a.N <= kMaxNDB) {
+		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                             (int)smemBytes),
+		                        "gram TC smem attribute"));
+		gramTcKernel<true><<<grid, kThreadsDB, smemBytes, s>>>(map, a);
+	} else {
+		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                             (int)smemBytes),
+		                        "gram TC smem attribute"));
+		gramTcKernel<false><<<grid, kThreadsTc, smemBytes, s>>>(map, a);
+	}
 	countLaunches(1);
 	PWA_CHECK_RET(cudaCheck(cudaGetLastError(), "gram TC launch"));
 	const int n = g.W * g.W;
