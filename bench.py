@@ -73,6 +73,12 @@ def parse():
     ap.add_argument("--train-bins", type=int, default=20_000, help="multibin: synthetic training bins")
     ap.add_argument("--augment", type=int, default=3, help="multibin: phase-rotated copies per training bin")
     ap.add_argument("--epochs", type=int, default=30, help="multibin: training epochs")
+    ap.add_argument("--repeats", type=int, default=3, help="multibin: timed repeats of both fits (median reported)")
+    ap.add_argument("--chunks", default="16,16,16",
+                    help="multibin: tiles per work item for bins of < 64, < 512, >= 512 tiles (fixed, so that "
+                         "repeats and runs take the same sweeps); 'auto' runs the chunk autotuner")
+    ap.add_argument("--cpu-fits", type=int, default=4,
+                    help="multibin: (bin, start) fits of the CPU baseline (scipy L-BFGS-B on the FP64 oracle)")
     ap.add_argument("--metrics-log", default=None,
                     help="also append the JSON line (with a UTC time stamp) to this JSON-lines file")
     ap.add_argument("--gtol-rel", type=float, default=1e-10,
@@ -555,6 +561,7 @@ def run_multibin(args):
         acc.integrate(names, mc, inBin=accepted, precision="tf32x3")
         del mc
         diag = np.real(np.diag(norm.matrix())) / norm.nmbEvents()
+        ints = (integral_snapshot(norm), integral_snapshot(acc))
         L = R.pwaLikelihood()
         L.init(names, [1] * W, None, 1, 0.0)
         L.addNormIntegral(norm)
@@ -562,7 +569,7 @@ def run_multibin(args):
         for k, nm in enumerate(names):
             L.addAmplitude(nm, data[k])
         L.finishInit()
-        bins.append(dict(L=L, n=n, data=data, diag=diag))
+        bins.append(dict(L=L, n=n, data=data, diag=diag, ints=ints))
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
     P = bins[0]["L"].nmbPars()
@@ -598,13 +605,24 @@ def run_multibin(args):
     for bn in bins:
         Mp.addBin(bn["L"], S)
     x0 = np.random.default_rng(21).standard_normal((len(bins) * S, P))
-    Mp.autotune(x0)
+    fixed_chunks = None if args.chunks == "auto" else [int(c) for c in args.chunks.split(",")]
+
+    def set_chunks(M, x):
+        if fixed_chunks is None:
+            return M.autotune(x)
+        M.setChunks(fixed_chunks)
+        return fixed_chunks
+
+    chunks_plain = set_chunks(Mp, x0)
     sweep_ms = Mp.sweepMs(x0)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rp = Mp.fit(x0, sweepsPerGraph=10)
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
+    plain_runs = []
+    for _ in range(max(1, args.repeats)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rp = Mp.fit(x0, sweepsPerGraph=10)
+        torch.cuda.synchronize()
+        plain_runs.append((time.perf_counter() - t0, rp["sweeps"], Mp.trace()))
+    plain_s = float(np.median([r[0] for r in plain_runs]))
 
     # ---- learned warm start: features + inference + 1 warm + 4 random starts ----
     Sw = 5
@@ -613,40 +631,48 @@ def run_multibin(args):
     for bn in bins:
         Mw.addBin(bn["L"], Sw)
     xr = np.random.default_rng(22).standard_normal((len(bins) * Sw, P))
-    Mw.autotune(xr)
+    chunks_learned = set_chunks(Mw, xr)
     # one-time kernel loading of the feature and inference paths, outside the timed region
     WS.moment_features_batch([bins[0]["data"]], [bins[0]["diag"]])
     net.forward(np.zeros((1, net.shape[0]), dtype=np.float32))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    Fe = WS.moment_features_batch([bn["data"] for bn in bins], [bn["diag"] for bn in bins])
-    t_feat = time.perf_counter()
-    Yp = net.forward(net.standardise(Fe))
-    xw = xr.copy()
-    for b, bn in enumerate(bins):
-        xw[b * Sw] = WS.params_from_targets(bn["L"], Yp[b], bn["n"])
-    t_inf = time.perf_counter()
-    rw = Mw.fit(xw, sweepsPerGraph=10)
-    torch.cuda.synchronize()
-    learned_s = time.perf_counter() - t0
-    breakdown = {"features_s": t_feat - t0, "inference_s": t_inf - t_feat, "fit_s": time.perf_counter() - t_inf}
+    learned_runs = []
+    for _ in range(max(1, args.repeats)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Fe = WS.moment_features_batch([bn["data"] for bn in bins], [bn["diag"] for bn in bins])
+        t_feat = time.perf_counter()
+        Yp = net.forward(net.standardise(Fe))
+        xw = xr.copy()
+        for b, bn in enumerate(bins):
+            xw[b * Sw] = WS.params_from_targets(bn["L"], Yp[b], bn["n"])
+        t_inf = time.perf_counter()
+        rw = Mw.fit(xw, sweepsPerGraph=10)
+        torch.cuda.synchronize()
+        t_end = time.perf_counter()
+        learned_runs.append((t_end - t0, rw["sweeps"], Mw.trace(),
+                             {"features_s": t_feat - t0, "inference_s": t_inf - t_feat, "fit_s": t_end - t_inf}))
+    k_med = int(np.argsort([r[0] for r in learned_runs])[len(learned_runs) // 2])
+    learned_s = learned_runs[k_med][0]
+    breakdown = learned_runs[k_med][3]
 
     fp = rp["f"].reshape(len(bins), S)
     fw = rw["f"].reshape(len(bins), Sw)
     fstar = np.minimum(fp.min(axis=1), fw.min(axis=1))
     tol = 1e-6 * np.abs(fstar)
 
-    def time_to_global(Mx, starts, offset):
+    def time_to_global(trace, starts, offset):
         # first check at which every bin has a start within 1e-6 of its global minimum
-        t, f = Mx.trace()
+        t, f = trace
         for k in range(len(t)):
             best = np.nanmin(f[k].reshape(len(bins), starts), axis=1)
             if np.all(best <= fstar + tol):
                 return offset + float(t[k])
         return None
 
-    ttg_plain = time_to_global(Mp, S, 0.0)
-    ttg_learned = time_to_global(Mw, Sw, breakdown["features_s"] + breakdown["inference_s"])
+    ttg_p = [time_to_global(r[2], S, 0.0) for r in plain_runs]
+    ttg_w = [time_to_global(r[2], Sw, r[3]["features_s"] + r[3]["inference_s"]) for r in learned_runs]
+    ttg_plain = float(np.median(ttg_p)) if all(v is not None for v in ttg_p) else None
+    ttg_learned = float(np.median(ttg_w)) if all(v is not None for v in ttg_w) else None
     reach_p = float(np.mean(fp.min(axis=1) <= fstar + tol))
     reach_w = float(np.mean(fw.min(axis=1) <= fstar + tol))
     warm_alone = float(np.mean(fw[:, 0] <= fstar + tol))
@@ -661,13 +687,68 @@ def run_multibin(args):
         cov = L.CovarianceMatrix(xa)
         sig = np.sqrt(np.maximum(np.diag(cov), 1e-300))
         verr.append(float(np.max(np.abs(xa - xb) / sig)))
+    # ---- roofline of one full sweep of the plain fit (all problems active):
+    # each tile is read once per group of `group` starts; 16 flop per
+    # (event, start, wave) (value and gradient contractions, complex FMA) ----
+    group = 32 if S > 8 else 8
+    n_tot = int(counts.sum())
+    sweep_bytes = n_tot * W * 8 * ((S + group - 1) // group)
+    sweep_flop = 16.0 * n_tot * S * W
+    hbm_peak, peak_kind = measured_peaks()
+    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12  # SIMT FP32 FMA lanes x 2 flop x max SM clock
+    sweep_roofline = {"bound": "fp32 simt", "achieved": sweep_flop / (sweep_ms / 1e3) / 1e12,
+                      "peak": fp32_nominal, "unit": "TFLOP/s",
+                      "frac": sweep_flop / (sweep_ms / 1e3) / 1e12 / fp32_nominal,
+                      "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 flop x 2.07 GHz); not measured",
+                      "hbm_achieved_gbs": sweep_bytes / (sweep_ms / 1e3) / 1e9, "hbm_peak_gbs": hbm_peak,
+                      "hbm_frac": sweep_bytes / (sweep_ms / 1e3) / 1e9 / hbm_peak,
+                      "algorithmic_bytes_per_sweep": sweep_bytes, "algorithmic_flop_per_sweep": sweep_flop,
+                      "sweep_ms": sweep_ms}
+
+    # ---- CPU baseline: scipy L-BFGS-B on the FP64 oracle (the reference's
+    # likelihood arithmetic) for a sample of (bin, start) fits, extrapolated
+    # to every bin and start in proportion to the bin's events ----
+    cpu = None
+    if args.cpu_fits > 0:
+        import scipy.optimize as so
+        threads = cpu_threads()
+        # bins spread over the event-count distribution (quantiles)
+        order = np.argsort(counts)
+        pick = [int(order[(2 * i + 1) * len(order) // (2 * args.cpu_fits)]) for i in range(args.cpu_fits)]
+        fit_s, fit_ev, nfev = [], [], []
+        for b in pick:
+            bn = bins[b]
+            Lo = oracle_with_integrals(names, [1] * W, bn["data"].cpu().numpy(), bn["ints"][0], bn["ints"][1], 1)
+            xs = x0[b * S]
+            t_c = time.perf_counter()
+            r = so.minimize(lambda p: Lo.FdF(p, threads=threads), xs, jac=True, method="L-BFGS-B",
+                            options=dict(maxiter=5000, gtol=1e-6, ftol=1e-15))
+            fit_s.append(time.perf_counter() - t_c)
+            fit_ev.append(bn["n"])
+            nfev.append(int(r.nfev))
+        per_event_fit = float(np.sum(fit_s) / np.sum(fit_ev))
+        total = per_event_fit * n_tot * S
+        cpu = {"value": total, "unit": "s", "cores": threads, "kind": "port",
+               "sample": ("%d (bin, start) fits (bins of %s events; %s FdF evaluations) with scipy L-BFGS-B "
+                          "(gtol 1e-6) on the FP64 oracle on %d host threads took %.1f s; extrapolated to %d bins "
+                          "x %d starts in proportion to events (%.3g s per event and start)"
+                          % (len(pick), [int(e) for e in fit_ev], nfev, threads, float(np.sum(fit_s)), len(bins), S,
+                             per_event_fit)),
+               "compares_to": "full_fit_s.plain"}
+
     line = {"metric": "multibin fit: GPU wall time to reach every bin's global-minimum LL (1e-6 relative), "
                       "learned warm start", "value": ttg_learned, "unit": "s", "higher_is_better": False,
             "n_gpus": 1, "impl": "gb300",
             "plain_time_to_global_s": ttg_plain,
             "speedup_time_to_global": (ttg_plain / ttg_learned) if (ttg_plain and ttg_learned) else None,
-            "full_fit_s": {"learned": learned_s, "plain": plain_s, "speedup": plain_s / learned_s},
+            "full_fit_s": {"learned": learned_s, "plain": plain_s, "speedup": plain_s / learned_s,
+                           "statistic": "median of %d repeats" % len(plain_runs),
+                           "plain_runs": [r[0] for r in plain_runs], "learned_runs": [r[0] for r in learned_runs]},
+            "time_to_global_runs_s": {"plain": ttg_p, "learned": ttg_w},
             "learned_breakdown": breakdown,
+            "roofline_sweep": sweep_roofline, "cpu_baseline": cpu,
+            "chunks": {"plain": list(chunks_plain), "learned": list(chunks_learned),
+                       "mode": "autotuned" if fixed_chunks is None else "fixed"},
             "data": "synthetic",
             "config": {"workload": "%d bins x 50 waves + flat, rank 1, %d data events (log-normal per bin), "
                                    "MC 5x per bin" % (len(bins), int(counts.sum())),
@@ -676,7 +757,7 @@ def run_multibin(args):
                                   (args.train_bins, args.augment + 1, args.epochs)},
             "reached_global_min": {"plain": reach_p, "learned": reach_w, "warm_start_alone": warm_alone},
             "v_error_sigma_max": max(verr) if verr else None, "v_error_bins": len(verr),
-            "sweeps": {"plain": rp["sweeps"], "learned": rw["sweeps"]},
+            "sweeps": {"plain": [r[1] for r in plain_runs], "learned": [r[1] for r in learned_runs]},
             "full_sweep_ms_plain": sweep_ms,
             "status_counts": {"plain": np.bincount(rp["status"], minlength=7).tolist(),
                               "learned": np.bincount(rw["status"], minlength=7).tolist(),
