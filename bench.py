@@ -62,7 +62,7 @@ def parse():
                     help="fdf: the event-sharded design (one all-reduce of P + 1 doubles per FdF) even on one "
                          "process (always on for more than one process)")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the host-buffer loop (default: min(steps, 2000))")
-    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision", "next", "isobar"],
+    ap.add_argument("--workload", default="fdf", choices=["fdf", "multibin", "precision", "next", "isobar", "config0"],
                     help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
                          "learned warm start; precision: error of each arithmetic variant against FP64; "
                          "isobar: decay amplitudes of the 88-wave 3pi set")
@@ -901,6 +901,114 @@ def run_precision(args):
     return 0
 
 
+def run_config0(args):
+    """The single-bin configuration of the reference's own CPU-runnable case:
+    15 positive-reflectivity waves + flat, rank 1, 20,000 data events,
+    100,000 MC events with Bernoulli(0.6) acceptance, seed 0 (complex128
+    amplitudes as drawn; the GPU stores them as complex64).  Timed on the GPU
+    and, beside it, with the FP64 oracle on one host core (the reference's own
+    threading): the normalisation + acceptance integral pair, one FdF, and one
+    full fit from the same start point -- the GPU's L-BFGS to a gradient
+    norm of 1e-6, scipy's L-BFGS-B on the oracle with the same tolerance
+    (the reference's NLopt fit stops at xtol_rel 1e-4 / ftol_abs 1e-6,
+    highLevelInterface/pwaNloptFit.cc:105-107, a looser criterion)."""
+    import torch
+    import scipy.optimize as so
+    import rootpwa_gb300 as R
+    from rootpwa_gb300 import synth
+    from oracle.oracle import OracleIntegral, OracleLikelihood
+    w = synth.make_workload("compass15", seed=0)
+    names, refl = w["names"], w["refl"]
+    mc128, data128 = w["mc"].astype(np.complex128), w["data"].astype(np.complex128)
+    reps = max(3, min(args.steps, 20))
+
+    def best(fn, n=reps):
+        ts = []
+        for _ in range(n):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts), statistics.median(ts)
+
+    # ---- GPU: integral pair from host amplitudes, FdF, full fit ----
+    def gpu_integrals():
+        gn, ga = R.ampIntegralMatrix(), R.ampIntegralMatrix()
+        gn.integrate(names, w["mc"], precision="tf32x3")
+        ga.integrate(names, w["mc"], inBin=w["accepted"], precision="tf32x3")
+        return gn, ga
+    gpu_integrals()
+    int_gpu, _ = best(gpu_integrals)
+    gn, ga = gpu_integrals()
+    snap = (integral_snapshot(gn), integral_snapshot(ga))
+    L = R.pwaLikelihood()
+    L.init(names, refl, None, 1, 0.0)
+    L.addNormIntegral(gn)
+    L.addAccIntegral(ga)
+    for k, n in enumerate(names):
+        L.addAmplitude(n, w["data"][k])
+    L.finishInit()
+    par = w["par"]
+    for _ in range(5):
+        L.FdF(par)
+    fdf_gpu, fdf_gpu_med = best(lambda: L.FdF(par), n=200)
+    M = R.pwaMultibin()
+    M.setOptions(startGroup=8, gtolAbs=1e-6, gtolRel=0.0, maxIter=20000)
+    M.addBin(L, 1)
+    M.fit(par[None, :], sweepsPerGraph=20)
+    torch.cuda.synchronize()
+    fit_gpu_runs = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        res = M.fit(par[None, :], sweepsPerGraph=20)
+        fit_gpu_runs.append(time.perf_counter() - t0)
+    fit_gpu = statistics.median(fit_gpu_runs)
+
+    # ---- CPU: the FP64 oracle, one thread ----
+    def cpu_integrals():
+        on, oa = OracleIntegral(), OracleIntegral()
+        assert on.integrate(names, mc128) and oa.integrate(names, mc128, in_bin=w["accepted"])
+        return on, oa
+    int_cpu, _ = best(cpu_integrals, n=3)
+    on, oa = cpu_integrals()
+    O = OracleLikelihood()
+    assert O.init(names, refl, None, 1, 0.0)
+    assert O.addNormIntegral(on) and O.addAccIntegral(oa)
+    for k, n in enumerate(names):
+        assert O.addAmplitude(n, data128[k])
+    assert O.finishInit()
+    fdf_cpu, _ = best(lambda: O.FdF(par, threads=1), n=5)
+    t0 = time.perf_counter()
+    r = so.minimize(lambda p: O.FdF(p, threads=1), par, jac=True, method="L-BFGS-B",
+                    options=dict(maxiter=20000, maxcor=8, gtol=1e-6, ftol=1e-15))
+    fit_cpu = time.perf_counter() - t0
+    # the GPU fit's minimum evaluated by the oracle with the GPU's own integrals
+    Og = oracle_with_integrals(names, refl, w["data"], snap[0], snap[1], 1)
+    f_gpu_at_min = Og.FdF(res["x"][0])[0]
+    x_cpu = O.CorrectParamSigns(r.x)
+    x_gpu = O.CorrectParamSigns(res["x"][0])
+    cov = O.CovarianceMatrix(O.Hessian(x_cpu))
+    sig = np.sqrt(np.maximum(np.diag(cov), 1e-300))
+    line = {"metric": "single-bin configuration: one full fit, GPU wall time", "value": fit_gpu, "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "impl": "gb300", "data": "synthetic",
+            "config": {"workload": "compass15: 15 waves (+) + flat, rank 1, 20000 data / 100000 MC events, seed 0",
+                       "parameters": len(par), "gtol": "gradient norm 1e-6 (both)"},
+            "fit": {"gpu_s_median": fit_gpu, "gpu_runs_s": fit_gpu_runs, "gpu_iterations": int(res["iterations"][0]),
+                    "gpu_status": int(res["status"][0]), "cpu_s": fit_cpu, "cpu_iterations": int(r.nit),
+                    "cpu_fdf_evaluations": int(r.nfev), "speedup": fit_cpu / fit_gpu,
+                    "ll_gpu": float(res["f"][0]), "ll_cpu": float(r.fun),
+                    "ll_rel_diff": abs(float(res["f"][0]) - float(r.fun)) / abs(float(r.fun)),
+                    "ll_gpu_point_by_oracle": float(f_gpu_at_min),
+                    "v_diff_sigma_max": float(np.max(np.abs(x_gpu - x_cpu) / sig))},
+            "fdf": {"gpu_host_call_us": fdf_gpu * 1e6, "gpu_host_call_median_us": fdf_gpu_med * 1e6,
+                    "cpu_us": fdf_cpu * 1e6, "speedup": fdf_cpu / fdf_gpu},
+            "integral_pair": {"gpu_s": int_gpu, "gpu_precision": "tf32x3, host complex64 amplitudes uploaded",
+                              "cpu_s": int_cpu, "speedup": int_cpu / int_gpu},
+            "cpu_baseline": {"value": fit_cpu, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "the whole fit, scipy L-BFGS-B on the FP64 oracle FdF (one thread)"}}
+    emit(line, args)
+    return 0
+
+
 def run_next(args):
     """Measurements of the rows after the FdF path: the GPU Hessian at the
     88-wave shapes (against the FP64 oracle's on a sample), loading a raw
@@ -1148,6 +1256,8 @@ def main():
         return run_next(args)
     if args.workload == "isobar":
         return run_isobar(args)
+    if args.workload == "config0":
+        return run_config0(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "multibin":
