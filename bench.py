@@ -42,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_NEG, N_POS, RANK = 7, 80, 2
+RANK_DEFAULT = RANK
 METRIC = "FdF evals/s at 88 waves x 1M events"
 UNIT = "FdF/s"
 
@@ -53,6 +54,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-data", type=int, default=1_000_000)
+    ap.add_argument("--shape", default="%d,%d,%d" % (N_NEG, N_POS, RANK),
+                    help="fdf: negative waves, positive waves, rank (default: the production wave set)")
     ap.add_argument("--n-mc", type=int, default=5_000_000)
     ap.add_argument("--reduction", default="fp64", choices=["fp64", "kahan_fp32", "fp32"])
     ap.add_argument("--integral-precision", default="tf32x3", choices=["fp64", "fp32", "tf32", "tf32x3", "bf16x3"],
@@ -286,11 +289,14 @@ def run_gb300(args):
     from rootpwa_gb300 import synth
     from rootpwa_gb300 import _native as N
 
-    names, refl = synth.wave_names(N_NEG, N_POS)
+    n_neg, n_pos, RANK = (int(v) for v in args.shape.split(","))
+    names, refl = synth.wave_names(n_neg, n_pos)
     W = len(names)
     rng = np.random.Generator(np.random.PCG64(1))
     model = synth.AmplitudeModel(W, 8, rng)
-    P = synth.n_pars(N_NEG, N_POS, RANK)
+    P = synth.n_pars(n_neg, n_pos, RANK)
+    default_shape = (n_neg, n_pos, RANK) == (N_NEG, N_POS, RANK_DEFAULT)
+    metric = METRIC if default_shape else "FdF evals/s at %d waves x %d events" % (W + 1, args.n_data)
     par0 = rng.standard_normal(P)
 
     # ---- set-up (not timed): amplitudes on the device, integrals on the GPU ----
@@ -494,12 +500,14 @@ def run_gb300(args):
                    "single_thread_value": 1.0 / t_one}
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32 (complex64 store, FP64 cross-tile reductions)",
                 "data": "synthetic",
-                "config": {"workload": "compass88: 7-/80+ waves + flat, rank 2, %d events per GPU" % args.n_data,
-                           "waves": 88, "rank": RANK, "events": args.n_data, "parameters": P,
+                "config": {"workload": ("compass88: 7-/80+ waves + flat, rank 2, %d events per GPU" % args.n_data
+                                        if default_shape else "%d-/%d+ waves + flat, rank %d, %d events per GPU"
+                                        % (n_neg, n_pos, RANK, args.n_data)),
+                           "waves": W + 1, "rank": RANK, "events": args.n_data, "parameters": P,
                            "mc_events": args.n_mc, "reduction": args.reduction,
                            "l2": "inputs (%.0f MB) larger than L2 (129 MB); no flush" % (alg_bytes / 1e6),
                            "entry": "pwa_likelihood_fdf_device (parameters and results in HBM)",
