@@ -17,6 +17,10 @@ struct pwa_mlp {
 	// training set on the device
 	DevBuf trainX, trainT;
 	long step = 0;
+	// split-K partials of the GEMMs with few output tiles
+	int numSMs = 1;
+	DevBuf work;
+	size_t workFloats = 0;
 
 	~pwa_mlp()
 	{
@@ -49,6 +53,22 @@ int mlpEnsureBatch(pwa_mlp* N, int B)
 	return kOk;
 }
 
+// one product, split over K when its output has few tiles; the workspace
+// grows to the largest split product on first use (a batch size's first step)
+int mlpGemm(pwa_mlp* N, MlpGemm g, cudaStream_t s)
+{
+	g.splitK = mlpGemmSplit(g, N->numSMs);
+	if (g.splitK > 1) {
+		const size_t need = (size_t)g.splitK * g.M * g.N;
+		if (need > N->workFloats) {
+			PWA_TRY(N->work.alloc(need * sizeof(float), "MLP split-K workspace"));
+			N->workFloats = need;
+		}
+		g.work = N->work.as<float>();
+	}
+	return launchMlpGemm(g, s);
+}
+
 MlpGemm gemmXWt(int M, int N, int K, const uint16_t* X, const uint16_t* W)
 {
 	// C[m][n] = sum_k X[m][k] W[n][k]
@@ -76,16 +96,16 @@ int mlpForward(pwa_mlp* N, int B)
 	g.bias = P + N->ob1;
 	g.relu = 1;
 	g.C16 = N->h1b.as<uint16_t>();
-	PWA_TRY(launchMlpGemm(g, N->stream));
+	PWA_TRY(mlpGemm(N, g, N->stream));
 	g = gemmXWt(B, N->h2, N->h1, N->h1b.as<uint16_t>(), W + N->oW2);
 	g.bias = P + N->ob2;
 	g.relu = 1;
 	g.C16 = N->h2b.as<uint16_t>();
-	PWA_TRY(launchMlpGemm(g, N->stream));
+	PWA_TRY(mlpGemm(N, g, N->stream));
 	g = gemmXWt(B, N->nOut, N->h2, N->h2b.as<uint16_t>(), W + N->oW3);
 	g.bias = P + N->ob3;
 	g.C32 = N->y32.as<float>();
-	return launchMlpGemm(g, N->stream);
+	return mlpGemm(N, g, N->stream);
 }
 
 // gradient of the mean squared error of the batch (targets in t32) into grads
@@ -110,7 +130,7 @@ int mlpBackward(pwa_mlp* N, int B)
 	g.ldb_k = (size_t)N->h2;
 	g.ldb_n = 1;
 	g.C32 = G + N->oW3;
-	PWA_TRY(launchMlpGemm(g, s));
+	PWA_TRY(mlpGemm(N, g, s));
 	PWA_TRY(launchColSum(N->dy32.as<float>(), B, N->nOut, G + N->ob3, s));
 	// dh2 = (dY W3) masked by h2 > 0
 	g = MlpGemm{};
@@ -127,7 +147,7 @@ int mlpBackward(pwa_mlp* N, int B)
 	g.mask = N->h2b.as<uint16_t>();
 	g.C16 = N->dh16.as<uint16_t>();
 	g.C32 = N->dh32.as<float>();
-	PWA_TRY(launchMlpGemm(g, s));
+	PWA_TRY(mlpGemm(N, g, s));
 	PWA_TRY(launchColSum(N->dh32.as<float>(), B, N->h2, G + N->ob2, s));
 	// dW2[n][k] = sum_b dh2[b][n] h1[b][k]
 	g = MlpGemm{};
@@ -141,7 +161,7 @@ int mlpBackward(pwa_mlp* N, int B)
 	g.ldb_k = (size_t)N->h1;
 	g.ldb_n = 1;
 	g.C32 = G + N->oW2;
-	PWA_TRY(launchMlpGemm(g, s));
+	PWA_TRY(mlpGemm(N, g, s));
 	// dh1 = (dh2 W2) masked by h1 > 0 (dh32 is reused after its last read)
 	g = MlpGemm{};
 	g.M = B;
@@ -157,7 +177,7 @@ int mlpBackward(pwa_mlp* N, int B)
 	g.mask = N->h1b.as<uint16_t>();
 	g.C16 = N->dh1.as<uint16_t>();
 	g.C32 = N->dh32.as<float>();
-	PWA_TRY(launchMlpGemm(g, s));
+	PWA_TRY(mlpGemm(N, g, s));
 	PWA_TRY(launchColSum(N->dh32.as<float>(), B, N->h1, G + N->ob1, s));
 	// dW1[n][k] = sum_b dh1[b][n] x[b][k]
 	g = MlpGemm{};
@@ -171,7 +191,7 @@ int mlpBackward(pwa_mlp* N, int B)
 	g.ldb_k = (size_t)N->nIn;
 	g.ldb_n = 1;
 	g.C32 = G + N->oW1;
-	return launchMlpGemm(g, s);
+	return mlpGemm(N, g, s);
 }
 
 int mlpAdam(pwa_mlp* N, float lr)
@@ -217,6 +237,9 @@ int pwa_mlp_create(pwa_mlp** out, uint32_t nIn, uint32_t nHidden1, uint32_t nHid
 	N->ob3 = N->oW3 + (size_t)nOut * nHidden2;
 	N->nPar = N->ob3 + nOut;
 	PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking), "stream"));
+	int dev = 0;
+	PWA_TRY(cudaCheck(cudaGetDevice(&dev), "cudaGetDevice"));
+	PWA_TRY(cudaCheck(cudaDeviceGetAttribute(&N->numSMs, cudaDevAttrMultiProcessorCount, dev), "SM count"));
 	for (DevBuf* b : {&N->params, &N->grads, &N->adamM, &N->adamV})
 		PWA_TRY(b->alloc(N->nPar * 4, "MLP parameters"));
 	PWA_TRY(N->w16.alloc(N->nPar * 2, "MLP BF16 weights"));

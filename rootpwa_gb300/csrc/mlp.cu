@@ -8,6 +8,10 @@
 // same kernel), BF16 operands widened to FP32 in shared memory, 64 x 64 output
 // tiles, 16 x 16 threads with 4 x 4 FP32 accumulators each, and an epilogue
 // that adds a bias, applies relu or a relu mask and writes FP32 and/or BF16.
+// A product of few output tiles (the batch has 256 rows, the layers 102 to
+// 512 columns) and a long K is split into K slices, one block per (tile,
+// slice), so that the grid covers the GPU; a second kernel sums the slices'
+// FP32 partials in slice order (deterministic) and applies the epilogue.
 
 #include "pwa_internal.h"
 
@@ -20,6 +24,23 @@ namespace {
 
 constexpr int kT = 64;   // output tile
 constexpr int kKt = 16;  // k per shared-memory stage
+
+// bias, relu, relu mask and the FP32 / BF16 stores of one output element
+__device__ __forceinline__ void mlpEpilogue(const MlpGemm& g, int m, int n, float v)
+{
+	const size_t o = (size_t)m * g.N + n;
+	if (g.bias)
+		v += g.bias[n];
+	if (g.relu)
+		v = fmaxf(v, 0.f);
+	const __nv_bfloat16* mask = reinterpret_cast<const __nv_bfloat16*>(g.mask);
+	if (mask && !(__bfloat162float(mask[o]) > 0.f))
+		v = 0.f;
+	if (g.C32)
+		g.C32[o] = v;
+	if (g.C16)
+		reinterpret_cast<__nv_bfloat16*>(g.C16)[o] = __float2bfloat16_rn(v);
+}
 
 __global__ void __launch_bounds__(256) mlpGemmKernel(const MlpGemm g)
 {
@@ -35,7 +56,11 @@ __global__ void __launch_bounds__(256) mlpGemmKernel(const MlpGemm g)
 			acc[i][j] = 0.f;
 	const __nv_bfloat16* A = reinterpret_cast<const __nv_bfloat16*>(g.A);
 	const __nv_bfloat16* B = reinterpret_cast<const __nv_bfloat16*>(g.B);
-	for (int k0 = 0; k0 < g.K; k0 += kKt) {
+	// this block's K slice
+	const int split = g.splitK > 1 ? g.splitK : 1;
+	const int kc = ((g.K + split - 1) / split + kKt - 1) / kKt * kKt;
+	const int kBeg = (int)blockIdx.z * kc, kEnd = min(g.K, kBeg + kc);
+	for (int k0 = kBeg; k0 < kEnd; k0 += kKt) {
 		// 64 x 16 of A and 16 x 64 of B; the element order follows the
 		// operand's contiguous dimension so that neighbouring threads read
 		// neighbouring addresses
@@ -49,7 +74,7 @@ __global__ void __launch_bounds__(256) mlpGemmKernel(const MlpGemm g)
 				r = e - k * kT;
 			}
 			const int gm = m0 + r, gk = k0 + k;
-			sa[k][r] = (gm < g.M && gk < g.K) ? __bfloat162float(A[(size_t)gm * g.lda_m + (size_t)gk * g.lda_k]) : 0.f;
+			sa[k][r] = (gm < g.M && gk < kEnd) ? __bfloat162float(A[(size_t)gm * g.lda_m + (size_t)gk * g.lda_k]) : 0.f;
 		}
 		for (int e = threadIdx.x; e < kT * kKt; e += 256) {
 			int c, k;
@@ -61,7 +86,7 @@ __global__ void __launch_bounds__(256) mlpGemmKernel(const MlpGemm g)
 				c = e - k * kT;
 			}
 			const int gn = n0 + c, gk = k0 + k;
-			sb[k][c] = (gn < g.N && gk < g.K) ? __bfloat162float(B[(size_t)gk * g.ldb_k + (size_t)gn * g.ldb_n]) : 0.f;
+			sb[k][c] = (gn < g.N && gk < kEnd) ? __bfloat162float(B[(size_t)gk * g.ldb_k + (size_t)gn * g.ldb_n]) : 0.f;
 		}
 		__syncthreads();
 #pragma unroll
@@ -80,8 +105,6 @@ __global__ void __launch_bounds__(256) mlpGemmKernel(const MlpGemm g)
 		}
 		__syncthreads();
 	}
-	const __nv_bfloat16* mask = reinterpret_cast<const __nv_bfloat16*>(g.mask);
-	__nv_bfloat16* C16 = reinterpret_cast<__nv_bfloat16*>(g.C16);
 #pragma unroll
 	for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -89,19 +112,23 @@ __global__ void __launch_bounds__(256) mlpGemmKernel(const MlpGemm g)
 			const int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
 			if (m >= g.M || n >= g.N)
 				continue;
-			const size_t o = (size_t)m * g.N + n;
-			float v = acc[i][j];
-			if (g.bias)
-				v += g.bias[n];
-			if (g.relu)
-				v = fmaxf(v, 0.f);
-			if (mask && !(__bfloat162float(mask[o]) > 0.f))
-				v = 0.f;
-			if (g.C32)
-				g.C32[o] = v;
-			if (C16)
-				C16[o] = __float2bfloat16_rn(v);
+			if (split > 1)
+				g.work[((size_t)blockIdx.z * g.M + m) * g.N + n] = acc[i][j];
+			else
+				mlpEpilogue(g, m, n, acc[i][j]);
 		}
+}
+
+// sum of the K slices' partials in slice order, then the epilogue
+__global__ void mlpSplitReduceKernel(const MlpGemm g)
+{
+	const size_t total = (size_t)g.M * g.N;
+	for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < total; o += (size_t)gridDim.x * blockDim.x) {
+		float v = 0.f;
+		for (int z = 0; z < g.splitK; ++z)
+			v += g.work[(size_t)z * total + o];
+		mlpEpilogue(g, (int)(o / g.N), (int)(o % g.N), v);
+	}
 }
 
 // column sums of an FP32 [M][N] matrix (bias gradients)
@@ -174,14 +201,32 @@ __global__ void gatherRowsKernel(const unsigned char* src, const uint32_t* idx, 
 
 }  // namespace
 
+int mlpGemmSplit(const MlpGemm& g, int numSMs)
+{
+	const int tiles = ((g.N + kT - 1) / kT) * ((g.M + kT - 1) / kT);
+	if (tiles >= numSMs || g.K < 8 * kKt)
+		return 1;
+	return std::max(1, std::min({16, (2 * numSMs + tiles - 1) / tiles, g.K / (4 * kKt)}));
+}
+
 int launchMlpGemm(const MlpGemm& g, cudaStream_t s)
 {
 	if (g.M <= 0 || g.N <= 0 || g.K <= 0)
 		return setError(kErrArg, "MLP GEMM: empty shape");
-	dim3 grid((g.N + kT - 1) / kT, (g.M + kT - 1) / kT);
+	const int split = g.splitK > 1 ? g.splitK : 1;
+	if (split > 1 && !g.work)
+		return setError(kErrArg, "MLP GEMM: split K without a workspace");
+	dim3 grid((g.N + kT - 1) / kT, (g.M + kT - 1) / kT, split);
 	mlpGemmKernel<<<grid, 256, 0, s>>>(g);
 	countLaunches(1);
-	return cudaCheck(cudaGetLastError(), "MLP GEMM launch");
+	PWA_CHECK(cudaCheck(cudaGetLastError(), "MLP GEMM launch"));
+	if (split == 1)
+		return kOk;
+	const size_t total = (size_t)g.M * g.N;
+	const int blocks = (int)std::min<size_t>(4096, (total + 255) / 256);
+	mlpSplitReduceKernel<<<blocks, 256, 0, s>>>(g);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "MLP split-K reduce launch");
 }
 
 int launchColSum(const float* X, int M, int N, float* out, cudaStream_t s)
