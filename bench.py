@@ -459,7 +459,8 @@ def run_gb300(args):
     achieved = alg_bytes / avg_main_s / 1e9
     peak, peak_kind = measured_peaks()
     roofline = {"bound": "hbm", "kernel": "fdfMainKernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": profile_traffic(),
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": profile_traffic() if default_shape else None,
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": avg_main_s * 1e6,
                 "isolated_launch_us": isolated_s * 1e6,
                 "frac_isolated_launch": alg_bytes / isolated_s / 1e9 / peak,
