@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-data", type=int, default=1_000_000)
+    ap.add_argument("--store-block", type=int, default=0,
+                    help="fdf: events per amplitude-store block and FdF tile (64 or 128; 0: automatic)")
     ap.add_argument("--shape", default="%d,%d,%d" % (N_NEG, N_POS, RANK),
                     help="fdf: negative waves, positive waves, rank (default: the production wave set)")
     ap.add_argument("--n-mc", type=int, default=5_000_000)
@@ -306,12 +308,14 @@ def run_gb300(args):
     g.manual_seed(2011 + rank)
     accepted = (torch.rand(args.n_mc, generator=g, device="cuda") < 0.6).to(torch.uint8).cpu().numpy()
     torch.cuda.synchronize()
+    # the tensor-core Gram covers up to 128 waves; wider sets use the SIMT FP32 kernel
+    int_prec = args.integral_precision if W <= 128 or args.integral_precision in ("fp32", "fp64") else "fp32"
     t0 = time.perf_counter()
     norm = R.ampIntegralMatrix()
-    norm.integrate(names, mc, precision=args.integral_precision)
+    norm.integrate(names, mc, precision=int_prec)
     integral_s = time.perf_counter() - t0
     acc = R.ampIntegralMatrix()
-    acc.integrate(names, mc, inBin=accepted, precision=args.integral_precision)
+    acc.integrate(names, mc, inBin=accepted, precision=int_prec)
     if sharded:
         # every rank integrated its own MC events: one all-reduce of the raw
         # sums and event counts gives every rank the integrals of all of them
@@ -326,6 +330,8 @@ def run_gb300(args):
     del mc
     torch.cuda.empty_cache()
     L = R.pwaLikelihood()
+    if args.store_block:
+        L.setStoreBlock(args.store_block)
     if sharded:
         # this rank's share of a data set of world x n_data events: only the
         # root shard adds the normalisation and prior terms
@@ -529,7 +535,7 @@ def run_gb300(args):
                                   "the kernel reads and writes directly)")},
                 "gpu_launches": int(launches), "launches_per_step": launches / args.steps,
                 "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clocks,
-                "extra": {"integral_norm_s": integral_s, "integral_precision": args.integral_precision,
+                "extra": {"integral_norm_s": integral_s, "integral_precision": int_prec,
                           "mc_events": args.n_mc}}
         emit(line, args)
     if sharded:
