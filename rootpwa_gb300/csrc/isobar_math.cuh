@@ -455,9 +455,82 @@ PWA_HD void halfAngle(double perp, double z, double* c, double* s)
 #endif
 }
 
+// angles from FP64 components, evaluated in FP32 (the complex64 mode: the
+// per-wave arithmetic that consumes them is FP32)
+PWA_HD double phiOfF(double x, double y)
+{
+	const float xf = (float)x, yf = (float)y;
+	return (xf == 0.f && yf == 0.f) ? 0.0 : (double)atan2f(yf, xf);
+}
+
+PWA_HD void halfAngleF(double x, double y, double z, double* c, double* s, double* q)
+{
+	const float xf = (float)x, yf = (float)y, zf = (float)z;
+	const float perp = sqrtf(xf * xf + yf * yf);
+	const float th = (perp == 0.f && zf == 0.f) ? 0.f : atan2f(perp, zf);
+	float sf, cf;
+#if defined(__CUDA_ARCH__)
+	sincosf(0.5f * th, &sf, &cf);
+#else
+	sf = std::sin(0.5f * th);
+	cf = std::cos(0.5f * th);
+#endif
+	*s = sf;
+	*c = cf;
+	*q = sqrtf(perp * perp + zf * zf);
+}
+
 // g: the Gottfried-Jackson four-vectors of the final-state slots of one
-// symmetrisation term
-PWA_HD Kin kinematics(const LV g[3], const WaveDev& w, bool canonical)
+// symmetrisation term.  T = double: FP64 throughout.  T = float (complex64
+// amplitudes): the boosts, the isobar mass and momentum and the helicity
+// frame's boost along z stay in FP64 (they cancel); the angles and
+// magnitudes the per-wave FP32 arithmetic consumes are computed in FP32
+// from the FP64 components, which keeps GB300's narrow FP64 pipe off the
+// transcendental functions.
+template <typename T>
+PWA_HD Kin kinematics(const LV g[3], const WaveDev& w, bool canonical);
+
+template <>
+PWA_HD Kin kinematics<float>(const LV g[3], const WaveDev& w, bool canonical)
+{
+	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
+	const LV I{vadd(A.p, B.p), A.e + B.e};
+	Kin k;
+	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
+	k.phi = phiOfF(d1.x, d1.y);
+	halfAngleF(d1.x, d1.y, d1.z, &k.cX, &k.sX, &k.qX);
+	const double pI = sqrt(vdot(I.p, I.p));
+	k.mI = sqrt((I.e - pI) * (I.e + pI));
+	double ax, ay, az;
+	if (canonical) {
+		const LV r = toRest(A, I.p, I.e, k.mI);
+		ax = r.p.x;
+		ay = r.p.y;
+		az = r.p.z;
+	} else {
+		// helicity frame: transverse axes in FP32, the boost along z in FP64
+		const float ix = (float)I.p.x, iy = (float)I.p.y, iz = (float)I.p.z;
+		const float perpI = sqrtf(ix * ix + iy * iy), pIf = (float)pI;
+		float yx = 0.f, yy = 1.f;
+		if (perpI > 0.f) {
+			yx = -iy / perpI;
+			yy = ix / perpI;
+		}
+		// x = y cross z with z = I / |I|
+		const float zx = ix / pIf, zy = iy / pIf, zz = iz / pIf;
+		const float xx = yy * zz, xy = -yx * zz, xz = yx * zy - yy * zx;
+		const float axf = (float)A.p.x, ayf = (float)A.p.y, azf = (float)A.p.z;
+		ax = axf * xx + ayf * xy + azf * xz;
+		ay = axf * yx + ayf * yy;
+		az = (I.e * (vdot(A.p, I.p) / pI) - pI * A.e) / k.mI;
+	}
+	k.phiH = phiOfF(ax, ay);
+	halfAngleF(ax, ay, az, &k.cI, &k.sI, &k.qI);
+	return k;
+}
+
+template <>
+PWA_HD Kin kinematics<double>(const LV g[3], const WaveDev& w, bool canonical)
 {
 	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
@@ -591,7 +664,7 @@ PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double 
 				} else {
 					gjFrame(P, bp, fp, perm, g);
 				}
-				kin[st.perm] = kinematics(g, w, P.canonical != 0);
+				kin[st.perm] = kinematics<T>(g, w, P.canonical != 0);
 				valid |= 1u << st.perm;
 			}
 			a = cadd(a, cscale(termAmplitude<T>(P, w, kin[st.perm]), T(st.factor)));
