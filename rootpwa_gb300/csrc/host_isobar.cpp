@@ -51,7 +51,9 @@ int uploadPlan(pwa_isobar* A)
 	const size_t oTerms = align16(oLams + p.lams.size() * sizeof(iso::LamTerm));
 	const size_t oPoly = align16(oTerms + p.dterms.size() * sizeof(iso::DTerm));
 	const size_t oNorm = align16(oPoly + sizeof(p.bfPoly));
-	const size_t oPerms = align16(oNorm + sizeof(p.bfNorm));
+	const size_t oPolyF = align16(oNorm + sizeof(p.bfNorm));
+	const size_t oNormF = align16(oPolyF + sizeof(p.bfPolyF));
+	const size_t oPerms = align16(oNormF + sizeof(p.bfNormF));
 	const size_t oTermsS = align16(oPerms + p.perms.size() * sizeof(int32_t));
 	const size_t total = align16(oTermsS + p.terms.size() * sizeof(iso::SymTerm));
 	std::vector<unsigned char> h(total, 0);
@@ -65,6 +67,8 @@ int uploadPlan(pwa_isobar* A)
 	put(oTerms, p.dterms.data(), p.dterms.size() * sizeof(iso::DTerm));
 	put(oPoly, p.bfPoly, sizeof(p.bfPoly));
 	put(oNorm, p.bfNorm, sizeof(p.bfNorm));
+	put(oPolyF, p.bfPolyF, sizeof(p.bfPolyF));
+	put(oNormF, p.bfNormF, sizeof(p.bfNormF));
 	put(oPerms, p.perms.data(), p.perms.size() * sizeof(int32_t));
 	put(oTermsS, p.terms.data(), p.terms.size() * sizeof(iso::SymTerm));
 	PWA_TRY(A->dPlan.ensure(total, "isobar wave plan"));
@@ -78,6 +82,8 @@ int uploadPlan(pwa_isobar* A)
 	v.dterms = reinterpret_cast<const iso::DTerm*>(d + oTerms);
 	v.bfPoly = reinterpret_cast<const double*>(d + oPoly);
 	v.bfNorm = reinterpret_cast<const double*>(d + oNorm);
+	v.bfPolyF = reinterpret_cast<const float*>(d + oPolyF);
+	v.bfNormF = reinterpret_cast<const float*>(d + oNormF);
 	v.perms = reinterpret_cast<const int32_t*>(d + oPerms);
 	v.terms = reinterpret_cast<const iso::SymTerm*>(d + oTermsS);
 	A->devView = v;

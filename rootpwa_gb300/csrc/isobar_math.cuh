@@ -84,6 +84,8 @@ constexpr double kVesF0Mass = 0.9837, kVesF0Width = 0.0376, kVesCouplingRe = -0.
 struct DTerm {
 	double coef;
 	int32_t a, b;
+	float coefF;                    // coef in FP32 (complex64 mode)
+	int32_t pad;
 };
 
 // one spin projection of the isobar in one wave: the X-vertex angular part
@@ -100,6 +102,7 @@ struct LamTerm {
 	int32_t iso0, iso1;             // DTerm range of dIso
 	int32_t mPlus, mMinus;          // phase multipliers (units of 1/2)
 	double cPlus, cMinus;
+	float cPlusF, cMinusF;          // FP32 copies (complex64 mode)
 };
 
 struct WaveDev {
@@ -116,6 +119,11 @@ struct WaveDev {
 	int32_t lam0, lam1;             // LamTerm range
 	int32_t term0, term1;           // SymTerm range (symmetrisation terms)
 	int32_t topo;                   // topology class (waves of one class share kinematics)
+	int32_t q0Zero;                 // q0 == 0 (the relativistic Breit-Wigner is then 0)
+	// FP32 copies for the complex64 mode, whose per-wave arithmetic must not
+	// convert FP64 constants (a conversion runs on the FP64 pipe)
+	float m0F, g0F, q0F, f2q0F, maF, mbF, q02F;
+	float dmHi, dmLo;               // the mass M that M^2 - m^2 is formed with (m0; Flatte: its M0), hi + lo
 	int32_t pad;
 };
 
@@ -123,7 +131,7 @@ struct WaveDev {
 // six permutations of three slots) and its factor (Bose times isospin)
 struct SymTerm {
 	int32_t perm;
-	int32_t pad;
+	float factorF;                  // factor in FP32 (complex64 mode)
 	double factor;
 };
 
@@ -135,6 +143,8 @@ struct PlanView {
 	const DTerm* dterms;
 	const double* bfPoly;           // [8][8]: P_l(z) coefficients of z^0..z^l
 	const double* bfNorm;           // [8]: P_l(1)
+	const float* bfPolyF;           // FP32 copies (complex64 mode)
+	const float* bfNormF;
 	const int32_t* perms;           // [6][3]: the permutations of three slots; slot i takes particle perms[p][i]
 	const SymTerm* terms;
 	uint32_t nWaves, pad0;
@@ -185,6 +195,14 @@ PWA_HD C2T<float> cexpi(float x)
 #endif
 }
 
+// a plan constant in the arithmetic type T: the FP64 value or its FP32 copy
+template <typename T>
+PWA_HD T pick(double d, float f);
+template <>
+PWA_HD double pick<double>(double d, float) { return d; }
+template <>
+PWA_HD float pick<float>(double, float f) { return f; }
+
 struct V3 {
 	double x, y, z;
 };
@@ -229,9 +247,24 @@ PWA_HD T dEval(const DTerm* t, int t0, int t1, T c, T s)
 {
 	T d = T(0);
 	for (int k = t0; k < t1; ++k)
-		d += T(t[k].coef) * ipow(c, t[k].a) * ipow(s, t[k].b);
+		d += pick<T>(t[k].coef, t[k].coefF) * ipow(c, t[k].a) * ipow(s, t[k].b);
 	return d;
 }
+
+// the barrier polynomials' coefficients in T (the FP32 copies exist only in
+// plans built for the kernel; the FP64 path reads only the FP64 arrays)
+template <typename T>
+PWA_HD T bfPolyAt(const PlanView& P, int i);
+template <>
+PWA_HD double bfPolyAt<double>(const PlanView& P, int i) { return P.bfPoly[i]; }
+template <>
+PWA_HD float bfPolyAt<float>(const PlanView& P, int i) { return P.bfPolyF[i]; }
+template <typename T>
+PWA_HD T bfNormAt(const PlanView& P, int l);
+template <>
+PWA_HD double bfNormAt<double>(const PlanView& P, int l) { return P.bfNorm[l]; }
+template <>
+PWA_HD float bfNormAt<float>(const PlanView& P, int l) { return P.bfNormF[l]; }
 
 // Blatt-Weisskopf F_L(q)^2 = P_l(1) z^l / P_l(z), z = (q / 0.1973)^2, L = 2l
 template <typename T>
@@ -241,11 +274,10 @@ PWA_HD T barrierF2(const PlanView& P, int L, T q)
 	if (l == 0)
 		return T(1);
 	const T z = (q * q) / T(kPr * kPr);
-	const double* c = P.bfPoly + 8 * l;
-	T den = T(c[l]);
+	T den = bfPolyAt<T>(P, 8 * l + l);
 	for (int k = l - 1; k >= 0; --k)
-		den = den * z + T(c[k]);
-	return T(P.bfNorm[l]) * ipow(z, l) / den;
+		den = den * z + bfPolyAt<T>(P, 8 * l + k);
+	return bfNormAt<T>(P, l) * ipow(z, l) / den;
 }
 
 template <typename T>
@@ -361,13 +393,14 @@ PWA_HD C2T<double> piPiSWave(double m, int variant)
 template <typename T>
 PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, double mId)
 {
-	const T m0 = T(w.m0), g0 = T(w.g0);
+	const T m0 = pick<T>(w.m0, w.m0F), g0 = pick<T>(w.g0, w.g0F);
+	const T ma = pick<T>(w.ma, w.maF), mb = pick<T>(w.mb, w.mbF), q0 = pick<T>(w.q0, w.q0F);
 	if (w.massDep == kMassRelBw) {
-		if (w.q0 == 0.0)
+		if (w.q0Zero)
 			return C2T<T>{T(0), T(0)};
-		const T q2 = breakup2<T>(mI, T(w.ma), T(w.mb));
+		const T q2 = breakup2<T>(mI, ma, mb);
 		const T q = q2 > T(0) ? sqrt(q2) : T(0);
-		const T G = g0 * (m0 / mI) * (q / T(w.q0)) * (barrierF2<T>(P, w.LI, q) / T(w.f2q0));
+		const T G = g0 * (m0 / mI) * (q / q0) * (barrierF2<T>(P, w.LI, q) / pick<T>(w.f2q0, w.f2q0F));
 		const T A = m0 * g0, B = dm2, Cc = m0 * G;
 		const T f = A / (B * B + Cc * Cc);
 		return C2T<T>{f * B, f * Cc};
@@ -379,11 +412,11 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 	}
 	if (w.massDep == kMassRhoBw) {
 		// rhoBreitWigner (massDependence.cc:324-359): F = 2 q^2 / (q0^2 + q^2)
-		const T q2r = breakup2<T>(mI, T(w.ma), T(w.mb));
+		const T q2r = breakup2<T>(mI, ma, mb);
 		const T q2 = q2r > T(0) ? q2r : T(0);
-		const T q02 = T(w.q02);
+		const T q02 = pick<T>(w.q02, w.q02F);
 		const T F = T(2) * q2 / (q02 + q2);
-		const T G = g0 * (m0 / mI) * (sqrt(q2) / T(w.q0)) * F;
+		const T G = g0 * (m0 / mI) * (sqrt(q2) / q0) * F;
 		const T A = m0 * g0 * sqrt(F), B = dm2, Cc = m0 * G;
 		const T f = A / (B * B + Cc * Cc);
 		return C2T<T>{f * B, f * Cc};
@@ -391,9 +424,9 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 	if (w.massDep == kMassF0980Bw) {
 		// f0980BreitWigner (massDependence.cc:363-390): Gamma = Gamma0 q / q0;
 		// at q = 0 (an isobar exactly at its threshold) 0/0 as in the reference
-		const T q2 = breakup2<T>(mI, T(w.ma), T(w.mb));
+		const T q2 = breakup2<T>(mI, ma, mb);
 		const T q = q2 > T(0) ? sqrt(q2) : T(0);
-		const T Cc = m0 * g0 * (q / T(w.q0));
+		const T Cc = m0 * g0 * (q / q0);
 		const T A = Cc * mI / q, B = dm2;
 		const T f = A / (B * B + Cc * Cc);
 		return C2T<T>{f * B, f * Cc};
@@ -435,12 +468,24 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 	return C2T<T>{T(1), T(0)};
 }
 
-// kinematics of one symmetrisation term for one topology class
+// kinematics of one symmetrisation term for one topology class, in the
+// arithmetic type T of the per-wave part
+template <typename T>
 struct Kin {
-	double phi, cX, sX, qX;         // analyser of the X vertex in the GJ frame: phi, cos/sin(theta/2), |p|
-	double phiH, cI, sI, qI;        // isobar daughter 1 in the isobar's helicity (canonical: rest) frame
-	double mI;                      // isobar mass
+	T phi, cX, sX, qX;              // analyser of the X vertex in the GJ frame: phi, cos/sin(theta/2), |p|
+	T phiH, cI, sI, qI;             // isobar daughter 1 in the isobar's helicity (canonical: rest) frame
+	T mI, mIlo;                     // isobar mass in T; FP32: mI + mIlo is the FP64 mass to ~2^-48
+	double mId;                     // isobar mass in FP64
+	int32_t mdKind;                 // mass dependence cached in md (-1: none)
+	C2T<T> md;
 };
+
+// mass dependences that depend on the isobar mass alone (no per-wave
+// parameters): evaluated once per topology class and symmetrisation term
+PWA_HD bool massDepOfMassAlone(int k)
+{
+	return k == kMassF0980Flatte || k == kMassRhoPrime || (k >= kMassPiPiSM && k <= kMassPiPiSKachaev);
+}
 
 PWA_HD double phiOf(double x, double y) { return (x == 0.0 && y == 0.0) ? 0.0 : atan2(y, x); }
 
@@ -457,13 +502,13 @@ PWA_HD void halfAngle(double perp, double z, double* c, double* s)
 
 // angles from FP64 components, evaluated in FP32 (the complex64 mode: the
 // per-wave arithmetic that consumes them is FP32)
-PWA_HD double phiOfF(double x, double y)
+PWA_HD float phiOfF(double x, double y)
 {
 	const float xf = (float)x, yf = (float)y;
-	return (xf == 0.f && yf == 0.f) ? 0.0 : (double)atan2f(yf, xf);
+	return (xf == 0.f && yf == 0.f) ? 0.f : atan2f(yf, xf);
 }
 
-PWA_HD void halfAngleF(double x, double y, double z, double* c, double* s, double* q)
+PWA_HD void halfAngleF(double x, double y, double z, float* c, float* s, float* q)
 {
 	const float xf = (float)x, yf = (float)y, zf = (float)z;
 	const float perp = sqrtf(xf * xf + yf * yf);
@@ -488,22 +533,25 @@ PWA_HD void halfAngleF(double x, double y, double z, double* c, double* s, doubl
 // from the FP64 components, which keeps GB300's narrow FP64 pipe off the
 // transcendental functions.
 template <typename T>
-PWA_HD Kin kinematics(const LV g[3], const WaveDev& w, bool canonical);
+PWA_HD Kin<T> kinematics(const LV g[3], const WaveDev& w, bool canonical);
 
 template <>
-PWA_HD Kin kinematics<float>(const LV g[3], const WaveDev& w, bool canonical)
+PWA_HD Kin<float> kinematics<float>(const LV g[3], const WaveDev& w, bool canonical)
 {
 	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
-	Kin k;
+	Kin<float> k;
+	k.mdKind = -1;
 	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
 	k.phi = phiOfF(d1.x, d1.y);
 	halfAngleF(d1.x, d1.y, d1.z, &k.cX, &k.sX, &k.qX);
 	const double pI = sqrt(vdot(I.p, I.p));
-	k.mI = sqrt((I.e - pI) * (I.e + pI));
+	k.mId = sqrt((I.e - pI) * (I.e + pI));
+	k.mI = (float)k.mId;
+	k.mIlo = (float)(k.mId - (double)k.mI);
 	double ax, ay, az;
 	if (canonical) {
-		const LV r = toRest(A, I.p, I.e, k.mI);
+		const LV r = toRest(A, I.p, I.e, k.mId);
 		ax = r.p.x;
 		ay = r.p.y;
 		az = r.p.z;
@@ -522,7 +570,7 @@ PWA_HD Kin kinematics<float>(const LV g[3], const WaveDev& w, bool canonical)
 		const float axf = (float)A.p.x, ayf = (float)A.p.y, azf = (float)A.p.z;
 		ax = axf * xx + ayf * xy + azf * xz;
 		ay = axf * yx + ayf * yy;
-		az = (I.e * (vdot(A.p, I.p) / pI) - pI * A.e) / k.mI;
+		az = (I.e * (vdot(A.p, I.p) / pI) - pI * A.e) / k.mId;
 	}
 	k.phiH = phiOfF(ax, ay);
 	halfAngleF(ax, ay, az, &k.cI, &k.sI, &k.qI);
@@ -530,18 +578,20 @@ PWA_HD Kin kinematics<float>(const LV g[3], const WaveDev& w, bool canonical)
 }
 
 template <>
-PWA_HD Kin kinematics<double>(const LV g[3], const WaveDev& w, bool canonical)
+PWA_HD Kin<double> kinematics<double>(const LV g[3], const WaveDev& w, bool canonical)
 {
 	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
-	Kin k;
+	Kin<double> k;
+	k.mdKind = -1;
 	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
 	const double perp1 = sqrt(d1.x * d1.x + d1.y * d1.y);
 	k.phi = phiOf(d1.x, d1.y);
 	halfAngle(perp1, d1.z, &k.cX, &k.sX);
 	k.qX = sqrt(vdot(d1, d1));
 	const double pI = sqrt(vdot(I.p, I.p));
-	k.mI = sqrt((I.e - pI) * (I.e + pI));
+	k.mId = k.mI = sqrt((I.e - pI) * (I.e + pI));
+	k.mIlo = 0.0;
 	double ax, ay, az;
 	if (canonical) {
 		// rest frame of the isobar with the Gottfried-Jackson axes
@@ -567,12 +617,28 @@ PWA_HD Kin kinematics<double>(const LV g[3], const WaveDev& w, bool canonical)
 	return k;
 }
 
-// amplitude of wave w for one symmetrisation term; T is the arithmetic of
-// the per-wave part (the kinematics come in FP64)
-template <typename T>
-PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
+// M^2 - mI^2 of a wave's Breit-Wigner denominator (M = m0; Flatte: its M0).
+// It cancels near the peak, where a narrow width needs the resolution of
+// the FP64 masses: FP64 for T = double; for T = float from the hi + lo FP32
+// pairs of M and mI, whose difference of the hi parts is exact near the
+// peak (Sterbenz), so the result carries FP32 relative accuracy.
+PWA_HD double deltaM2(const WaveDev& w, const Kin<double>& k)
 {
-	const T cX = T(k.cX), sX = T(k.sX), cI = T(k.cI), sI = T(k.sI), phiH = T(k.phiH), phi = T(k.phi);
+	const double m0 = w.massDep == kMassF0980Flatte ? kFlatteM0 : w.m0;
+	return (m0 - k.mId) * (m0 + k.mId);
+}
+PWA_HD float deltaM2(const WaveDev& w, const Kin<float>& k)
+{
+	return ((w.dmHi - k.mI) + (w.dmLo - k.mIlo)) * (w.dmHi + k.mI);
+}
+
+// amplitude of wave w for one symmetrisation term; T is the arithmetic of
+// the per-wave part.  k is the term's kinematics; mass dependences of the
+// isobar mass alone are cached in it.
+template <typename T>
+PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, Kin<T>& k)
+{
+	const T cX = k.cX, sX = k.sX, cI = k.cI, sI = k.sI, phiH = k.phiH, phi = k.phi;
 	// e^{i lam phiH / 2} stepped by e^{i phiH} from lam = lamIso of the first term
 	const C2T<T> step = cexpi(phiH);
 	C2T<T> eL{T(1), T(0)};
@@ -587,13 +653,22 @@ PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, const Kin& k)
 		const T dP = dEval<T>(P.dterms, L.plus0, L.plus1, cX, sX);
 		const T dM = dEval<T>(P.dterms, L.minus0, L.minus1, cX, sX);
 		const T dI = dEval<T>(P.dterms, L.iso0, L.iso1, cI, sI);
-		const C2T<T> x = cadd(cscale(cexpi(T(0.5) * T(L.mPlus) * phi), T(L.cPlus) * dP),
-		                      cscale(cexpi(T(0.5) * T(L.mMinus) * phi), T(L.cMinus) * dM));
+		const C2T<T> x = cadd(cscale(cexpi(T(0.5) * T(L.mPlus) * phi), pick<T>(L.cPlus, L.cPlusF) * dP),
+		                      cscale(cexpi(T(0.5) * T(L.mMinus) * phi), pick<T>(L.cMinus, L.cMinusF) * dM));
 		sum = cadd(sum, cmul(x, cscale(eL, dI)));
 	}
-	const T f = sqrt(barrierF2<T>(P, w.LX, T(k.qX)) * barrierF2<T>(P, w.LI, T(k.qI)));
-	const double m0 = w.massDep == kMassF0980Flatte ? kFlatteM0 : w.m0;
-	return cscale(cmul(sum, massDependence<T>(P, w, T(k.mI), T((m0 - k.mI) * (m0 + k.mI)), k.mI)), f);
+	const T f = sqrt(barrierF2<T>(P, w.LX, k.qX) * barrierF2<T>(P, w.LI, k.qI));
+	C2T<T> md;
+	if (massDepOfMassAlone(w.massDep)) {
+		if (k.mdKind != w.massDep) {
+			k.md = massDependence<T>(P, w, k.mI, deltaM2(w, k), k.mId);
+			k.mdKind = w.massDep;
+		}
+		md = k.md;
+	} else {
+		md = massDependence<T>(P, w, k.mI, deltaM2(w, k), k.mId);
+	}
+	return cscale(cmul(sum, md), f);
 }
 
 // Gottfried-Jackson four-vectors of the three final-state slots of one
@@ -641,7 +716,7 @@ PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double 
 	LV g0[3];
 	gjFrame(P, bp, fp, P.perms, g0);
 	// kinematics per permutation, computed once per topology class on first use
-	Kin kin[kMaxPerms];
+	Kin<T> kin[kMaxPerms];
 	uint32_t valid = 0;
 	int topo = -1;
 	for (uint32_t o = 0; o < P.nWaves; ++o) {
@@ -667,7 +742,7 @@ PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double 
 				kin[st.perm] = kinematics<T>(g, w, P.canonical != 0);
 				valid |= 1u << st.perm;
 			}
-			a = cadd(a, cscale(termAmplitude<T>(P, w, kin[st.perm]), T(st.factor)));
+			a = cadd(a, cscale(termAmplitude<T>(P, w, kin[st.perm]), pick<T>(st.factor, st.factorF)));
 		}
 		out[2 * ((uint64_t)wi * ld + e)] = a.re;
 		out[2 * ((uint64_t)wi * ld + e) + 1] = a.im;

@@ -142,6 +142,8 @@ struct Plan {
 	std::vector<DTerm> dterms;
 	double bfPoly[8][8];
 	double bfNorm[8];
+	float bfPolyF[8][8];            // FP32 copies (complex64 mode)
+	float bfNormF[8];
 	std::vector<int32_t> perms;     // the six permutations of three slots
 	std::vector<SymTerm> terms;
 	double masses[3] = {0.0, 0.0, 0.0}, beamMass = 0.0;
@@ -156,6 +158,8 @@ struct Plan {
 		v.dterms = dterms.data();
 		v.bfPoly = &bfPoly[0][0];
 		v.bfNorm = bfNorm;
+		v.bfPolyF = &bfPolyF[0][0];
+		v.bfNormF = bfNormF;
 		v.perms = perms.data();
 		v.terms = terms.data();
 		v.nWaves = (uint32_t)waves.size();
@@ -168,6 +172,40 @@ struct Plan {
 		return v;
 	}
 };
+
+// FP32 copies of the plan's constants for the complex64 kernel, whose
+// per-wave arithmetic is FP32 (converting FP64 constants there would put
+// each conversion on the FP64 pipe); M^2 - m^2 of the Breit-Wigner
+// denominators takes M as an FP32 hi + lo pair
+inline void fillFp32Copies(Plan& plan)
+{
+	for (DTerm& t : plan.dterms)
+		t.coefF = (float)t.coef;
+	for (LamTerm& t : plan.lams) {
+		t.cPlusF = (float)t.cPlus;
+		t.cMinusF = (float)t.cMinus;
+	}
+	for (SymTerm& t : plan.terms)
+		t.factorF = (float)t.factor;
+	for (int i = 0; i < 8; ++i) {
+		for (int k = 0; k < 8; ++k)
+			plan.bfPolyF[i][k] = (float)plan.bfPoly[i][k];
+		plan.bfNormF[i] = (float)plan.bfNorm[i];
+	}
+	for (WaveDev& w : plan.waves) {
+		w.q0Zero = w.q0 == 0.0 ? 1 : 0;
+		w.m0F = (float)w.m0;
+		w.g0F = (float)w.g0;
+		w.q0F = (float)w.q0;
+		w.f2q0F = (float)w.f2q0;
+		w.maF = (float)w.ma;
+		w.mbF = (float)w.mb;
+		w.q02F = (float)w.q02;
+		const double M = w.massDep == kMassF0980Flatte ? kFlatteM0 : w.m0;
+		w.dmHi = (float)M;
+		w.dmLo = (float)(M - (double)w.dmHi);
+	}
+}
 
 // a permutation of the three final-state slots: slot i takes particle p[i]
 typedef std::vector<int> Perm;
@@ -462,7 +500,7 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 		w.term0 = (int32_t)plan.terms.size();
 		for (const Term& t : symTerms(s, species, bose, isospin))
 			if (t.factor != 0.0)  // zero terms (a vanishing isospin coupling) only enter the normalisation
-				plan.terms.push_back(SymTerm{permIndex(t.perm), 0, t.factor});
+				plan.terms.push_back(SymTerm{permIndex(t.perm), 0.f, t.factor});
 		w.term1 = (int32_t)plan.terms.size();
 		const std::tuple<int, int, int, int> key(w.a, w.b, w.c, w.bachelorFirst);
 		auto it = std::find(topoKeys.begin(), topoKeys.end(), key);
@@ -526,8 +564,13 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 	plan.order.resize(plan.waves.size());
 	for (size_t i = 0; i < plan.order.size(); ++i)
 		plan.order[i] = (int32_t)i;
-	std::stable_sort(plan.order.begin(), plan.order.end(),
-	                 [&](int32_t x, int32_t y) { return plan.waves[x].topo < plan.waves[y].topo; });
+	// waves of one topology class together (they share the kinematics), and
+	// within a class those of one mass dependence (they share its cached value)
+	std::stable_sort(plan.order.begin(), plan.order.end(), [&](int32_t x, int32_t y) {
+		const WaveDev &a = plan.waves[x], &b = plan.waves[y];
+		return a.topo != b.topo ? a.topo < b.topo : a.massDep < b.massDep;
+	});
+	fillFp32Copies(plan);
 	return std::string();
 }
 
