@@ -610,9 +610,359 @@ __global__ void __launch_bounds__(DB ? kThreadsDB : kThreadsTc, 1)
 	}
 }
 
+// ---- hi/lo kernel (TF32x3, BF16x3; N <= 96): wide products ----
+// A tcgen05.mma of M = 128 costs about the same time for every N up to 96,
+// so the products are made as wide as the operand layout allows.  The four
+// planes of a tile sit one after another in one operand buffer, NB = N rows
+// each: Ar_hi at row 0, Ar_lo at NB, Ai_lo at 2NB, Ai_hi at 3NB (plus 32
+// rows of slack, so that an A operand of 128 rows starting at Ai_hi stays
+// inside; the rows of A beyond NB produce accumulator lanes >= W that are
+// never read).  Per K step four instructions:
+//   [Hr | C]     += Ar_hi [Ar_hi; Ar_lo]^T      (N = 2NB)
+//   [C | Hi]     += Ai_hi [Ai_lo; Ai_hi]^T      (N = 2NB)
+//   [Dh | E]     += Ai_hi [Ar_hi; Ar_lo]^T      (N = 2NB)
+//   E            += Ai_lo Ar_hi^T               (N = NB)
+// in the tensor-memory blocks Hr, C, Hi (columns [0, 3NB)) and Dh, E
+// ([3NB, 5NB)).  The three-product sums follow from symmetry: Re = Hr + Hi
+// + C + C^T = (S + S^T) / 2 with S = Hr + Hi + 2C, and Im = D - D^T with
+// D = Dh + E.  The drain warps keep S and D in registers (2N sums per row),
+// the reduction kernel symmetrises.  The blocks collect `period` tiles
+// between drains; the tensor cores add into them with truncation, so each
+// block of large values (Hr, Hi, Dh) gets only four additions per tile.  At
+// the first tile of a period the second instruction is issued as two of
+// N = NB, so that Hi starts from zero while C keeps the first one's
+// products.  The first three blocks (X) are drained while the MMAs of the
+// last two (Y) run, and Y while the next tile's MMAs of X run.
+constexpr int kDrainWarpsHL = 16;
+constexpr int kThreadsHL = (kConvWarps + 2 + kDrainWarpsHL) * 32;
+constexpr int kChunksPerWarpHL = 3;  // NB / 8 <= 12 chunks of a block, every fourth per drain warp
+
+__host__ __device__ constexpr uint32_t hlOpBytes(int NB) { return (uint32_t)(3 * NB + 128) * 128u; }
+
+// one MMA of the operand type of the kernel (descriptors precomputed)
+template <bool BF16>
+__device__ __forceinline__ void mmaOp(uint32_t d, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, uint32_t acc)
+{
+	if (BF16)
+		mmaBf16(d, aDesc, bDesc, idesc, acc);
+	else
+		mmaTf32(d, aDesc, bDesc, idesc, acc);
+}
+
+template <bool BF16>
+__global__ void __launch_bounds__(kThreadsHL, 1) gramTcHiLoKernel(const __grid_constant__ CUtensorMap map, const TcArgs a)
+{
+	extern __shared__ __align__(1024) unsigned char smemRaw[];
+	unsigned char* smem =
+	    reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
+	const int W = a.W, NB = a.N;
+	const uint32_t rawBytes = (uint32_t)W * (uint32_t)a.kt * 8u;
+	const uint32_t rawStride = (rawBytes + 1023u) & ~1023u;
+	const uint32_t opBytes = hlOpBytes(NB);
+	unsigned char* ops = smem;                                   // [kOpBufs][3NB + 128 rows x 128 B]
+	unsigned char* raw = ops + (size_t)kOpBufs * opBytes;        // [stages][W][kt complex]
+	uint64_t* bars = reinterpret_cast<uint64_t*>(raw + (size_t)a.stages * rawStride);
+	uint64_t* rawFull = bars;
+	uint64_t* rawEmpty = bars + a.stages;
+	uint64_t* opFull = bars + 2 * a.stages;
+	uint64_t* opEmpty = opFull + kOpBufs;
+	uint64_t* drainReady = opEmpty + kOpBufs;  // [2]: X, Y complete for a drain
+	uint64_t* drainDone = drainReady + 2;      // [2]: X, Y read by the drain
+	uint64_t* mmaFinal = drainDone + 2;
+	uint32_t* tmemHolder = reinterpret_cast<uint32_t*>(mmaFinal + 1);
+	__shared__ unsigned sFail;
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const uint64_t t0 = (uint64_t)blockIdx.x * a.tilesTotal / gridDim.x;
+	const uint64_t t1 = (uint64_t)(blockIdx.x + 1) * a.tilesTotal / gridDim.x;
+	const int nT = (int)(t1 - t0);
+	const int nDrains = (nT + a.period - 1) / a.period;
+
+	if (tid == 0) {
+		for (int s = 0; s < a.stages; ++s) {
+			barInit(&rawFull[s], 1);
+			barInit(&rawEmpty[s], kConvWarps);
+		}
+		for (int b = 0; b < kOpBufs; ++b) {
+			barInit(&opFull[b], kConvWarps);
+			barInit(&opEmpty[b], 1);
+		}
+		for (int x = 0; x < 2; ++x) {
+			barInit(&drainReady[x], 1);
+			barInit(&drainDone[x], kDrainWarpsHL);
+		}
+		barInit(mmaFinal, 1);
+		sFail = 0u;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	if (warp == kMmaWarp) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sAddr(tmemHolder)),
+		             "r"(kTmemCols)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	// the operand buffers start at zero: rows W..NB-1 of every plane and the
+	// slack rows are never written
+	if (warp < kConvWarps) {
+		uint4* p = reinterpret_cast<uint4*>(ops);
+		const int n16 = (int)(kOpBufs * opBytes / 16u);
+		for (int i = tid; i < n16; i += kConvWarps * 32)
+			p[i] = make_uint4(0u, 0u, 0u, 0u);
+		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	const uint32_t tmem = *tmemHolder;
+
+	if (warp == kTmaWarp) {
+		// ---- producer: one TMA load per tile ----
+		if (lane == 0) {
+			asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map)) : "memory");
+			int issued = 0;
+			for (int t = 0; t < nT; ++t) {
+				const int s = t % a.stages;
+				if (t >= a.stages && !barWait(&rawEmpty[s], (uint32_t)(((t / a.stages) - 1) & 1))) {
+					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+					sFail = 1u;
+					break;
+				}
+				if (*(volatile unsigned*)&sFail)
+					break;
+				barExpectTx(&rawFull[s], rawBytes);
+				tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, &rawFull[s]);
+				++issued;
+			}
+			for (int t = (issued > a.stages ? issued - a.stages : 0); t < issued; ++t)
+				barWait(&rawFull[t % a.stages], (uint32_t)((t / a.stages) & 1));
+		}
+	} else if (warp == kMmaWarp) {
+		// ---- MMA issuer ----
+		if (lane == 0) {
+			const uint32_t id2 = BF16 ? idescBf16(128, 2 * NB) : idescTf32(128, 2 * NB);
+			const uint32_t id1 = BF16 ? idescBf16(128, NB) : idescTf32(128, NB);
+			const uint32_t tX = tmem, tY = tmem + (uint32_t)(3 * NB);
+			// descriptors of the planes of buffer 0; a plane is NB x 128 B (NB * 8
+			// in the descriptor's 16-byte address units), a buffer opBytes, a K
+			// step of 32 bytes 2 units
+			const uint64_t desc0 = smemDesc(sAddr(ops));
+			const uint64_t planeD = (uint64_t)NB * 8u, bufD = (uint64_t)(opBytes >> 4);
+			for (int t = 0; t < nT; ++t) {
+				const int b = t % kOpBufs;
+				const int p = t / a.period;
+				const bool first = (t % a.period) == 0;
+				const bool last = (t + 1) % a.period == 0 || t + 1 == nT;
+				if (!barWait(&opFull[b], (uint32_t)((t / kOpBufs) & 1))) {
+					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+					sFail = 1u;
+					break;
+				}
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				const uint64_t rh = desc0 + (uint64_t)b * bufD, il = rh + 2 * planeD, ih = rh + 3 * planeD;
+				// X: the drain of the last period has read it
+				if (first && p >= 1) {
+					if (!barWait(&drainDone[0], (uint32_t)((p - 1) & 1))) {
+						atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+						sFail = 1u;
+						break;
+					}
+					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				}
+#pragma unroll
+				for (uint32_t kk = 0; kk < 4; ++kk)
+					mmaOp<BF16>(tX, rh + 2 * kk, rh + 2 * kk, id2, (first && kk == 0) ? 0u : 1u);
+				if (first) {
+#pragma unroll
+					for (uint32_t kk = 0; kk < 4; ++kk) {
+						mmaOp<BF16>(tX + (uint32_t)NB, ih + 2 * kk, il + 2 * kk, id1, 1u);
+						mmaOp<BF16>(tX + (uint32_t)(2 * NB), ih + 2 * kk, ih + 2 * kk, id1, kk == 0 ? 0u : 1u);
+					}
+				} else {
+#pragma unroll
+					for (uint32_t kk = 0; kk < 4; ++kk)
+						mmaOp<BF16>(tX + (uint32_t)NB, ih + 2 * kk, il + 2 * kk, id2, 1u);
+				}
+				if (last)
+					mmaCommit(&drainReady[0]);
+				if (first && p >= 1) {
+					if (!barWait(&drainDone[1], (uint32_t)((p - 1) & 1))) {
+						atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+						sFail = 1u;
+						break;
+					}
+					asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+				}
+#pragma unroll
+				for (uint32_t kk = 0; kk < 4; ++kk)
+					mmaOp<BF16>(tY, ih + 2 * kk, rh + 2 * kk, id2, (first && kk == 0) ? 0u : 1u);
+#pragma unroll
+				for (uint32_t kk = 0; kk < 4; ++kk)
+					mmaOp<BF16>(tY + (uint32_t)NB, il + 2 * kk, rh + 2 * kk, id1, 1u);
+				mmaCommit(&opEmpty[b]);
+				if (last)
+					mmaCommit(&drainReady[1]);
+			}
+			mmaCommit(mmaFinal);
+			if (!barWait(mmaFinal, 0u))
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+		}
+	} else if (warp >= kDrainWarp0) {
+		// ---- drain: S += Hr + Hi + 2 C, D += Dh + E ----
+		const int q = warp & 3, sub = (warp - kDrainWarp0) >> 2;
+		const uint32_t rowBase = tmem + ((uint32_t)(q * 32) << 16);
+		const int nc = NB / 8;
+		float S[kChunksPerWarpHL][8], D[kChunksPerWarpHL][8];
+#pragma unroll
+		for (int j = 0; j < kChunksPerWarpHL; ++j)
+#pragma unroll
+			for (int i = 0; i < 8; ++i)
+				S[j][i] = D[j][i] = 0.f;
+		bool ok = true;
+		for (int d = 0; d < nDrains && ok; ++d) {
+#pragma unroll
+			for (int x = 0; x < 2; ++x) {
+				if (!barWait(&drainReady[x], (uint32_t)(d & 1))) {
+					atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+					ok = false;
+					break;
+				}
+				asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+				for (int j = 0; j < kChunksPerWarpHL; ++j) {
+					const int c = sub + 4 * j;
+					if (c < nc) {
+						uint32_t u[8], v[8];
+						if (x == 0) {
+							// Hr and Hi, then C
+							tmemLd8(rowBase + (uint32_t)(8 * c), u);
+							tmemLd8(rowBase + (uint32_t)(2 * NB + 8 * c), v);
+							asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+							for (int i = 0; i < 8; ++i)
+								S[j][i] += __uint_as_float(u[i]) + __uint_as_float(v[i]);
+							tmemLd8(rowBase + (uint32_t)(NB + 8 * c), u);
+							asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+							for (int i = 0; i < 8; ++i)
+								S[j][i] += 2.f * __uint_as_float(u[i]);
+						} else {
+							tmemLd8(rowBase + (uint32_t)(3 * NB + 8 * c), u);
+							tmemLd8(rowBase + (uint32_t)(4 * NB + 8 * c), v);
+							asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+							for (int i = 0; i < 8; ++i)
+								D[j][i] += __uint_as_float(u[i]) + __uint_as_float(v[i]);
+						}
+					}
+				}
+				asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+				__syncwarp();
+				if (lane == 0)
+					barArrive(&drainDone[x]);
+			}
+		}
+		if (ok) {
+			// partials of this CTA: [2 (S, D)][128][N], rows < W
+			const int row = q * 32 + lane;
+			if (row < W) {
+#pragma unroll
+				for (int j = 0; j < kChunksPerWarpHL; ++j) {
+					const int c = sub + 4 * j;
+					if (c < nc) {
+						float4* s4 = reinterpret_cast<float4*>(a.partials + (((size_t)blockIdx.x * 2) * 128 + row) * NB + 8 * c);
+						float4* d4 = reinterpret_cast<float4*>(a.partials + (((size_t)blockIdx.x * 2 + 1) * 128 + row) * NB + 8 * c);
+						s4[0] = make_float4(S[j][0], S[j][1], S[j][2], S[j][3]);
+						s4[1] = make_float4(S[j][4], S[j][5], S[j][6], S[j][7]);
+						d4[0] = make_float4(D[j][0], D[j][1], D[j][2], D[j][3]);
+						d4[1] = make_float4(D[j][4], D[j][5], D[j][6], D[j][7]);
+					}
+				}
+			}
+		}
+	} else {
+		// ---- converters: raw interleaved rows -> four planes of the operand buffer ----
+		const int sub = lane >> 4, p = lane & 15;
+		const uint32_t plane = (uint32_t)NB * 128u;
+		for (int t = 0; t < nT; ++t) {
+			const int s = t % a.stages, b = t % kOpBufs;
+			if (!barWait(&rawFull[s], (uint32_t)((t / a.stages) & 1)) ||
+			    (t >= kOpBufs && !barWait(&opEmpty[b], (uint32_t)(((t / kOpBufs) - 1) & 1)))) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				sFail = 1u;
+				break;
+			}
+			const float* rs = reinterpret_cast<const float*>(raw + (size_t)s * rawStride);
+			unsigned char* op = ops + (size_t)b * opBytes;
+			if (BF16) {
+				const uint64_t kb = (t0 + t) * (uint64_t)kKTB + 4u * p;
+				float wq[4] = {1.f, 1.f, 1.f, 1.f};
+				if (a.weightK)
+#pragma unroll
+					for (int q = 0; q < 4; ++q)
+						wq[q] = (kb + q < a.K) ? sqrtf((float)a.weightK[kb + q]) : 0.f;
+				for (int w = 2 * warp + sub; w < W; w += 2 * kConvWarps) {
+					const float4 v0 = *reinterpret_cast<const float4*>(rs + w * 128 + 8 * p);
+					const float4 v1 = *reinterpret_cast<const float4*>(rs + w * 128 + 8 * p + 4);
+					const float re[4] = {v0.x * wq[0], v0.z * wq[1], v1.x * wq[2], v1.z * wq[3]};
+					const float im[4] = {v0.y * wq[0], v0.w * wq[1], v1.y * wq[2], v1.w * wq[3]};
+					uint32_t hr[4], hm[4], lr[4], lm[4];
+#pragma unroll
+					for (int q = 0; q < 4; ++q) {
+						float br, bm, dummy;
+						hr[q] = bf16Bits(re[q], &br);
+						hm[q] = bf16Bits(im[q], &bm);
+						lr[q] = bf16Bits(re[q] - br, &dummy);
+						lm[q] = bf16Bits(im[q] - bm, &dummy);
+					}
+					// planes NB rows apart (NB a multiple of 8: the same swizzle phase)
+					unsigned char* o = op + swzOffset16(w, 4 * p);
+					*reinterpret_cast<uint2*>(o) = make_uint2(hr[0] | (hr[1] << 16), hr[2] | (hr[3] << 16));
+					*reinterpret_cast<uint2*>(o + plane) = make_uint2(lr[0] | (lr[1] << 16), lr[2] | (lr[3] << 16));
+					*reinterpret_cast<uint2*>(o + 2 * plane) =
+					    make_uint2(lm[0] | (lm[1] << 16), lm[2] | (lm[3] << 16));
+					*reinterpret_cast<uint2*>(o + 3 * plane) =
+					    make_uint2(hm[0] | (hm[1] << 16), hm[2] | (hm[3] << 16));
+				}
+			} else {
+				const uint64_t k0 = (t0 + t) * (uint64_t)kKT + 2u * p;
+				float w0 = 1.f, w1 = 1.f;
+				if (a.weightK) {
+					w0 = (k0 < a.K) ? sqrtf((float)a.weightK[k0]) : 0.f;
+					w1 = (k0 + 1 < a.K) ? sqrtf((float)a.weightK[k0 + 1]) : 0.f;
+				}
+				for (int w = 2 * warp + sub; w < W; w += 2 * kConvWarps) {
+					const float4 v = *reinterpret_cast<const float4*>(rs + w * 64 + 4 * p);
+					const float re0 = v.x * w0, im0 = v.y * w0, re1 = v.z * w1, im1 = v.w * w1;
+					const float2 hre = make_float2(tf32Round(re0), tf32Round(re1));
+					const float2 him = make_float2(tf32Round(im0), tf32Round(im1));
+					unsigned char* o = op + swzOffset(w, 2 * p);
+					*reinterpret_cast<float2*>(o) = hre;
+					*reinterpret_cast<float2*>(o + plane) = make_float2(tf32Round(re0 - hre.x), tf32Round(re1 - hre.y));
+					*reinterpret_cast<float2*>(o + 2 * plane) =
+					    make_float2(tf32Round(im0 - him.x), tf32Round(im1 - him.y));
+					*reinterpret_cast<float2*>(o + 3 * plane) = him;
+				}
+			}
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+			__syncwarp();
+			if (lane == 0) {
+				barArrive(&rawEmpty[s]);
+				barArrive(&opFull[b]);
+			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	if (warp == kMmaWarp) {
+		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+	}
+}
+
 // FP64 sum of the CTAs' partials in CTA order; assembles the Hermitian matrix
-// (upper triangle from Re and D, lower mirrored, real diagonal).
-__global__ void gramTcReduceKernel(const float* partials, int grid, int W, int N, double* out)
+// (upper triangle from Re and D, lower mirrored, real diagonal).  sym: the
+// first partial is S with Re = (S + S^T) / 2 (the hi/lo kernel).
+__global__ void gramTcReduceKernel(const float* partials, int grid, int W, int N, int sym, double* out)
 {
 	const int n = W * W;
 	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
@@ -623,7 +973,8 @@ __global__ void gramTcReduceKernel(const float* partials, int grid, int W, int N
 		for (int c = 0; c < grid; ++c) {
 			const float* Re = partials + (size_t)c * 2 * 128 * N;
 			const float* D = Re + (size_t)128 * N;
-			re += (double)Re[(size_t)i * N + j];
+			re += sym ? 0.5 * ((double)Re[(size_t)i * N + j] + (double)Re[(size_t)j * N + i])
+			          : (double)Re[(size_t)i * N + j];
 			im += (double)D[(size_t)i * N + j] - (double)D[(size_t)j * N + i];
 		}
 		if (i == j)
@@ -687,14 +1038,19 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	a.W = g.W;
 	a.N = ((g.W + 15) / 16) * 16;
 	a.planes = (precision == 2) ? 1 : 2;
-	a.period = (precision == 2) ? 8 : 1;
+	// hi/lo precisions up to 96 waves: the wide-product kernel, drained every
+	// third tile (each accumulator element then collects as many tensor-core
+	// additions between drains as the per-tile drain of the narrow kernel)
+	const bool hiLo = a.planes == 2 && ((g.W + 15) / 16) * 16 <= kMaxNDB;
+	a.period = (precision == 2) ? 8 : (hiLo ? 3 : 1);
 	a.bf16 = (precision == 4) ? 1 : 0;
 	a.kt = a.bf16 ? kKTB : kKT;
 	a.tilesTotal = (g.K + a.kt - 1) / a.kt;
 	a.weightK = g.weightK;
 	a.devErr = g.devErr;
 	const size_t rawStride = ((size_t)g.W * a.kt * 8 + 1023) & ~size_t(1023);
-	const size_t fixed = 1024 /* alignment */ + (size_t)kOpBufs * a.planes * kPlaneBytes + 256 /* barriers */;
+	const size_t opBytes = hiLo ? (size_t)hlOpBytes(((g.W + 15) / 16) * 16) : (size_t)a.planes * kPlaneBytes;
+	const size_t fixed = 1024 /* alignment */ + (size_t)kOpBufs * opBytes + 256 /* barriers */;
 	a.stages = 4;
 	while (a.stages > 1 && fixed + a.stages * rawStride > (size_t)maxSmem)
 		--a.stages;
@@ -722,7 +1078,12 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	if (cr != CUDA_SUCCESS)
 		return setError(kErrCuda, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
 
-	if (a.N <= kMaxNDB) {
+	if (hiLo) {
+		auto* k = a.bf16 ? gramTcHiLoKernel<true> : gramTcHiLoKernel<false>;
+		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes),
+		                        "gram TC smem attribute"));
+		k<<<grid, kThreadsHL, smemBytes, s>>>(map, a);
+	} else if (a.N <= kMaxNDB) {
 		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                                             (int)smemBytes),
 		                        "gram TC smem attribute"));
@@ -737,7 +1098,7 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	PWA_CHECK_RET(cudaCheck(cudaGetLastError(), "gram TC launch"));
 	const int n = g.W * g.W;
 	const int blocks = std::max(1, std::min(1024, (n + 255) / 256));
-	gramTcReduceKernel<<<blocks, 256, 0, s>>>(a.partials, grid, g.W, a.N, out);
+	gramTcReduceKernel<<<blocks, 256, 0, s>>>(a.partials, grid, g.W, a.N, hiLo ? 1 : 0, out);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "gram TC reduce launch");
 }
