@@ -9,39 +9,36 @@
 // Weights enter as sqrt(w_k) on both sides (the host passes w_k >= 0).
 //
 // One persistent CTA per SM owns a contiguous range of events.  Per tile of
-// 32 events:
+// 32 events (64 for BF16):
 //   - one TMA load brings the complex64 rows [W][32] (interleaved re, im)
 //     into a raw shared-memory stage (warp 8);
-//   - eight converter warps split re / im into the planar operand in the
-//     canonical K-major 128-byte-swizzled layout, Ar in rows 0..127 and Ai in
-//     rows 128..255 (TF32: one plane rounded to TF32; TF32x3: hi = tf32(x),
-//     lo = tf32(x - hi)), weighted;
-//   - one thread of warp 9 issues tcgen05.mma kind::tf32 (M = 128, N = W
-//     rounded up to 16, K = 8 per instruction) into two FP32 accumulators
-//     (Re, D) in tensor memory; TF32x3 adds the cross products hi lo^T and
-//     lo hi^T before hi hi^T.
-// BF16x3 uses tiles of 64 events (one 128-byte swizzle row of BF16), hi =
-// bf16(x), lo = bf16(x - hi), and tcgen05.mma kind::f16 with BF16 operands
-// (K = 16 per instruction) for the same three products.
+//   - eight converter warps split re / im into planar operands in the
+//     canonical K-major 128-byte-swizzled layout (TF32: one plane rounded to
+//     TF32; TF32x3: hi = tf32(x), lo = tf32(x - hi); BF16x3: the same with
+//     bf16), weighted;
+//   - one thread of warp 9 issues tcgen05.mma (M = 128, K = 32 bytes per
+//     instruction) into FP32 accumulators in tensor memory;
+//   - drain warps move the accumulators into round-to-nearest FP32 sums.
 // The tensor cores add into FP32 accumulators with truncation, so a long
 // chain of accumulations drifts towards zero by a fraction of an ulp per
-// instruction.  The accumulators therefore start from zero every `period`
-// tiles and are drained into round-to-nearest FP32 sums; cross products come
-// first in each tile so that their truncation acts on small partial sums.
-// Two drain schemes:
-//   * up to 96 waves (N <= 96, the double-buffered kernel): two working
-//     pairs (Re, D) in tensor memory, 4N <= 384 columns; the MMAs of period
-//     p go to pair p % 2 while sixteen drain warps (10..25, four per
-//     tensor-memory lane quarter) add pair (p - 1) % 2 into sums they keep in
-//     registers (at most 48 per thread), so the tensor pipe does not wait
-//     for a drain unless a drain takes longer than a period's MMAs;
-//   * wider sets (the single-buffered kernel): one working pair, sums in
-//     tensor memory (4N <= 512 columns), four drain warps (10..13); the MMA
-//     warp waits for each drain before the next period.
-// The additions are the same in both, in the same order.  At the end the
-// drain warps store the CTA's FP32 partials; a second kernel sums the
-// partials of all CTAs in FP64 in a fixed order and assembles the Hermitian
-// matrix.
+// instruction; the accumulators therefore start from zero every `period`
+// tiles and are drained.  A tcgen05.mma of M = 128 takes about the same time
+// for any N up to 96, so the instruction count sets the speed.  Three kernels:
+//   * hi/lo precisions up to 96 waves (gramTcHiLoKernel, described at the
+//     kernel): the planes side by side so that one instruction multiplies a
+//     plane by two (N = 2W), 16 instructions per tile instead of 36, the
+//     symmetric products assembled from one orientation;
+//   * TF32 up to 96 waves (gramTcKernel<true>): Ar Ar^T + Ai Ai^T and
+//     Ai Ar^T into two working pairs (Re, D) in tensor memory, 4N <= 384
+//     columns; the MMAs of period p go to pair p % 2 while sixteen drain
+//     warps (10..25, four per lane quarter) add pair (p - 1) % 2 into sums
+//     they keep in registers;
+//   * wider sets (gramTcKernel<false>): one working pair, sums in tensor
+//     memory (4N <= 512 columns), four drain warps (10..13); the MMA warp
+//     waits for each drain before the next period.
+// At the end the drain warps store the CTA's FP32 partials; a second kernel
+// sums the partials of all CTAs in FP64 in a fixed order and assembles the
+// Hermitian matrix.
 //
 // Every wait on an mbarrier is bounded (1 s of globaltimer): on expiry the
 // CTA records kDevErrTimeout, stops issuing work, waits (bounded) for its own
