@@ -139,11 +139,41 @@ using namespace pwa;
 // ===========================================================================
 // ampIntegralMatrix: raw sums and the wave list
 // ===========================================================================
+// device buffers and stream of integrate(), kept by an integral between
+// calls on one device (the output matrix, the error flag and the Gram
+// partials: no allocation per call once they have their size)
+struct GramScratch {
+	int dev = -1;
+	cudaStream_t stream = nullptr;
+	DevBuf out, err, part;
+	GramScratch() = default;
+	GramScratch(const GramScratch&) = delete;
+	GramScratch& operator=(const GramScratch&) = delete;
+	~GramScratch() { reset(); }
+	void reset()
+	{
+		out.release();
+		err.release();
+		part.release();
+		if (stream)
+			cudaStreamDestroy(stream);
+		stream = nullptr;
+		dev = -1;
+	}
+};
+
 struct pwa_integral {
 	uint32_t nWaves = 0;
 	uint64_t nEvents = 0;
 	std::vector<std::string> names;
 	std::vector<cplx> sums;  // raw sums [i][j]
+	// not part of the value: a copy starts without device buffers
+	struct ScratchHolder {
+		std::unique_ptr<GramScratch> p;
+		ScratchHolder() = default;
+		ScratchHolder(const ScratchHolder&) {}
+		ScratchHolder& operator=(const ScratchHolder&) { return *this; }
+	} scratch;
 
 	int index(const std::string& n) const
 	{

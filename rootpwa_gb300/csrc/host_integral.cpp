@@ -12,18 +12,18 @@
 namespace {
 
 // Sums the GPU Gram kernel for integrate().
-int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, int ampType, int memory,
-                 const std::vector<double>& weightK, uint64_t K, int precision, std::vector<cplx>& out)
+int gramOnDevice(GramScratch& sc, uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, int ampType,
+                 int memory, const std::vector<double>& weightK, uint64_t K, int precision, std::vector<cplx>& out)
 {
 	int dev, sms;
 	size_t smem;
 	PWA_TRY(deviceInfo(&dev, &sms, &smem));
-	cudaStream_t s = nullptr;
-	PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream"));
-	struct StreamGuard {
-		cudaStream_t s;
-		~StreamGuard() { cudaStreamDestroy(s); }
-	} guard{s};
+	if (sc.dev != dev) {
+		sc.reset();
+		PWA_TRY(cudaCheck(cudaStreamCreateWithFlags(&sc.stream, cudaStreamNonBlocking), "stream"));
+		sc.dev = dev;
+	}
+	cudaStream_t s = sc.stream;
 
 	// device inputs may still be written by the caller's streams
 	if (memory == PWA_MEMORY_DEVICE)
@@ -35,7 +35,8 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 	// the tensor-core kernel reads rows with TMA: even row stride (16-byte
 	// multiple) and a 16-byte aligned base
 	const uint64_t ldPad = tensorCore ? (K + (K & 1ull)) : K;
-	DevBuf dIn, dConv, dW, dPart, dOut, dErr;
+	DevBuf dIn, dConv, dW;
+	DevBuf &dPart = sc.part, &dOut = sc.out, &dErr = sc.err;
 	const float2* a32 = nullptr;
 	const double2* a64 = nullptr;
 	uint64_t ldK = ldIn;
@@ -54,7 +55,6 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 			a64 = static_cast<const double2*>(amps);
 		} else {
 			PWA_TRY(dConv.alloc((size_t)W * ldPad * sizeof(float2), "integral conversion buffer"));
-			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
 			for (uint32_t w = 0; w < W; ++w)
 				PWA_TRY(launchConvertPlain(static_cast<const double2*>(amps) + (size_t)w * ldIn,
 				                           dConv.as<float2>() + (size_t)w * ldPad, K, s));
@@ -74,7 +74,6 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 			a64 = dIn.as<double2>();
 		} else {
 			PWA_TRY(dConv.alloc((size_t)W * ldPad * sizeof(float2), "integral conversion buffer"));
-			PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
 			PWA_TRY(launchConvertPlain(dIn.as<double2>(), dConv.as<float2>(), (uint64_t)W * ldPad, s));
 			a32 = dConv.as<float2>();
 		}
@@ -90,9 +89,8 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		                                  cudaMemcpyHostToDevice, s),
 		                  "weight upload"));
 	}
-	PWA_TRY(dOut.alloc((size_t)W * W * 2 * sizeof(double), "integral output"));
-	if (!dErr.p)
-		PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
+	PWA_TRY(dOut.ensure((size_t)W * W * 2 * sizeof(double), "integral output"));
+	PWA_TRY(dErr.ensure(sizeof(unsigned), "flag"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(dErr.p, 0, sizeof(unsigned), s), "memset"));
 
 	GramArgs g{};
@@ -106,7 +104,7 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 	int st = kErrUnsupported;
 	if (tensorCore) {
 		const size_t scratch = gramTcScratchFloats((int)W, sms) / 2 + 1;  // doubles holding the FP32 partials
-		PWA_TRY(dPart.alloc(scratch * sizeof(double), "gram partials"));
+		PWA_TRY(dPart.ensure(scratch * sizeof(double), "gram partials"));
 		st = launchGramTc(g, precision, sms, s, dOut.as<double>(), dPart.as<double>(), scratch);
 		if (st != kOk)
 			return st;
@@ -117,8 +115,8 @@ int gramOnDevice(uint32_t W, const void* amps, uint64_t nEvents, uint32_t nSub, 
 		const uint64_t maxChunks = std::max<uint64_t>(1, K / 64);
 		chunks = (int)std::min<uint64_t>((uint64_t)chunks, maxChunks);
 		g.chunks = chunks;
-		PWA_TRY(dPart.alloc((size_t)chunks * W * W * 2 * sizeof(double), "gram partials"));
-		PWA_TRY(cudaCheck(cudaMemsetAsync(dPart.p, 0, dPart.bytes, s), "memset"));
+		PWA_TRY(dPart.ensure((size_t)chunks * W * W * 2 * sizeof(double), "gram partials"));
+		PWA_TRY(cudaCheck(cudaMemsetAsync(dPart.p, 0, (size_t)chunks * W * W * 2 * sizeof(double), s), "memset"));
 		g.partials = dPart.as<double>();
 		PWA_TRY(launchGramSimt(g, precision, s));
 		PWA_TRY(launchGramReduce(g.partials, chunks, (int)W, dOut.as<double>(), 0, s));
@@ -252,10 +250,16 @@ int pwa_integral_integrate(pwa_integral* I, uint32_t nWaves, const char* const* 
 	}
 	const uint64_t K = nProc * nSubAmps;
 	std::vector<cplx> result;
-	if (lastK > 0 && counter > 0)
-		PWA_TRY(gramOnDevice(nWaves, amps, nEvents, nSubAmps, ampType, memory, weightK, K, precision, result));
-	else
+	if (lastK > 0 && counter > 0) {
+		if (!I->scratch.p)
+			I->scratch.p.reset(new (std::nothrow) GramScratch());
+		if (!I->scratch.p)
+			return setError(kErrOom, "out of host memory");
+		PWA_TRY(gramOnDevice(*I->scratch.p, nWaves, amps, nEvents, nSubAmps, ampType, memory, weightK, K, precision,
+		                     result));
+	} else {
 		result.assign((size_t)nWaves * nWaves, cplx(0, 0));
+	}
 	I->nEvents = counter;
 	I->sums = result;
 	if (useWeight && counter > 0) {
