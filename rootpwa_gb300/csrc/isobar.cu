@@ -20,9 +20,15 @@ namespace pwa {
 namespace {
 
 constexpr int kIsoThreads = 128;
+// eight blocks (32 warps) per SM: the per-event arithmetic is a long chain
+// of dependent operations, and the kernel is latency-bound at the 12 warps
+// its unconstrained register count allows (measured on 10^6 events x 88
+// waves: 20.4 ms at 160 registers, 16.8 ms at 128, 10.9 ms at 64 with a
+// few hundred bytes of spills to L1, 11.3 ms at 40, 12.5 ms at 32)
+constexpr int kIsoBlocksPerSM = 8;
 
 template <typename T>
-__global__ void __launch_bounds__(kIsoThreads) isobarAmplitudeKernel(iso::PlanView P, const double* __restrict__ beam,
+__global__ void __launch_bounds__(kIsoThreads, kIsoBlocksPerSM) isobarAmplitudeKernel(iso::PlanView P, const double* __restrict__ beam,
                                                                      const double* __restrict__ fs, uint64_t n,
                                                                      T* __restrict__ amps)
 {
@@ -49,7 +55,7 @@ int launchIsobarAmplitudes(const iso::PlanView& v, const double* beam, const dou
 	PWA_CHECK(cudaCheck(cudaGetDevice(&dev), "cudaGetDevice"));
 	PWA_CHECK(cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
 	const uint64_t need = (n + kIsoThreads - 1) / kIsoThreads;
-	const unsigned blocks = (unsigned)std::min<uint64_t>(need, (uint64_t)sms * 16);
+	const unsigned blocks = (unsigned)std::min<uint64_t>(need, (uint64_t)sms * kIsoBlocksPerSM * 2);
 	if (fp32)
 		isobarAmplitudeKernel<float><<<blocks, kIsoThreads, 0, s>>>(v, beam, fs, n, static_cast<float*>(amps));
 	else

@@ -119,12 +119,12 @@ struct WaveDev {
 	int32_t lam0, lam1;             // LamTerm range
 	int32_t term0, term1;           // SymTerm range (symmetrisation terms)
 	int32_t topo;                   // topology class (waves of one class share kinematics)
+	int32_t iso;                    // isobar class: waves of equal mass dependence and isobar L
 	int32_t q0Zero;                 // q0 == 0 (the relativistic Breit-Wigner is then 0)
 	// FP32 copies for the complex64 mode, whose per-wave arithmetic must not
 	// convert FP64 constants (a conversion runs on the FP64 pipe)
 	float m0F, g0F, q0F, f2q0F, maF, mbF, q02F;
 	float dmHi, dmLo;               // the mass M that M^2 - m^2 is formed with (m0; Flatte: its M0), hi + lo
-	int32_t pad;
 };
 
 // one symmetrisation term of a wave: final-state permutation (index into the
@@ -472,12 +472,25 @@ PWA_HD C2T<T> massDependence(const PlanView& P, const WaveDev& w, T mI, T dm2, d
 // arithmetic type T of the per-wave part
 template <typename T>
 struct Kin {
-	T phi, cX, sX, qX;              // analyser of the X vertex in the GJ frame: phi, cos/sin(theta/2), |p|
-	T phiH, cI, sI, qI;             // isobar daughter 1 in the isobar's helicity (canonical: rest) frame
+	// analyser of the X vertex in the GJ frame: e^{i phi/2}, cos/sin(theta/2)
+	// and their squares, |p|
+	C2T<T> u;
+	T cX, sX, c2X, s2X, qX;
+	// isobar daughter 1 in the isobar's helicity (canonical: rest) frame
+	C2T<T> uH;
+	T cI, sI, c2I, s2I, qI;
 	T mI, mIlo;                     // isobar mass in T; FP32: mI + mIlo is the FP64 mass to ~2^-48
 	double mId;                     // isobar mass in FP64
-	int32_t mdKind;                 // mass dependence cached in md (-1: none)
-	C2T<T> md;
+	// values shared by the waves of this kinematics, cached on first use:
+	// the mass dependence of the isobar mass alone (by mass-dependence kind),
+	// mass dependence x sqrt(F_LI(qI)) (by isobar class), sqrt(F_LX(qX)) (by LX)
+	int32_t mdKind, isoKey, lxKey;
+	C2T<T> md, isoVal;
+	T lxVal;
+	PWA_HD void clearCaches()
+	{
+		mdKind = isoKey = lxKey = -1;
+	}
 };
 
 // mass dependences that depend on the isobar mass alone (no per-wave
@@ -541,10 +554,12 @@ PWA_HD Kin<float> kinematics<float>(const LV g[3], const WaveDev& w, bool canoni
 	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
 	Kin<float> k;
-	k.mdKind = -1;
+	k.clearCaches();
 	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
-	k.phi = phiOfF(d1.x, d1.y);
+	k.u = cexpi(0.5f * phiOfF(d1.x, d1.y));
 	halfAngleF(d1.x, d1.y, d1.z, &k.cX, &k.sX, &k.qX);
+	k.c2X = k.cX * k.cX;
+	k.s2X = k.sX * k.sX;
 	const double pI = sqrt(vdot(I.p, I.p));
 	k.mId = sqrt((I.e - pI) * (I.e + pI));
 	k.mI = (float)k.mId;
@@ -572,8 +587,10 @@ PWA_HD Kin<float> kinematics<float>(const LV g[3], const WaveDev& w, bool canoni
 		ay = axf * yx + ayf * yy;
 		az = (I.e * (vdot(A.p, I.p) / pI) - pI * A.e) / k.mId;
 	}
-	k.phiH = phiOfF(ax, ay);
+	k.uH = cexpi(0.5f * phiOfF(ax, ay));
 	halfAngleF(ax, ay, az, &k.cI, &k.sI, &k.qI);
+	k.c2I = k.cI * k.cI;
+	k.s2I = k.sI * k.sI;
 	return k;
 }
 
@@ -583,11 +600,13 @@ PWA_HD Kin<double> kinematics<double>(const LV g[3], const WaveDev& w, bool cano
 	const LV A = g[w.a], B = g[w.b], Cb = g[w.c];
 	const LV I{vadd(A.p, B.p), A.e + B.e};
 	Kin<double> k;
-	k.mdKind = -1;
+	k.clearCaches();
 	const V3 d1 = w.bachelorFirst ? Cb.p : I.p;
 	const double perp1 = sqrt(d1.x * d1.x + d1.y * d1.y);
-	k.phi = phiOf(d1.x, d1.y);
+	k.u = cexpi(0.5 * phiOf(d1.x, d1.y));
 	halfAngle(perp1, d1.z, &k.cX, &k.sX);
+	k.c2X = k.cX * k.cX;
+	k.s2X = k.sX * k.sX;
 	k.qX = sqrt(vdot(d1, d1));
 	const double pI = sqrt(vdot(I.p, I.p));
 	k.mId = k.mI = sqrt((I.e - pI) * (I.e + pI));
@@ -611,8 +630,10 @@ PWA_HD Kin<double> kinematics<double>(const LV g[3], const WaveDev& w, bool cano
 		az = (I.e * vdot(A.p, zh) - pI * A.e) / k.mI;
 	}
 	const double perpA = sqrt(ax * ax + ay * ay);
-	k.phiH = phiOf(ax, ay);
+	k.uH = cexpi(0.5 * phiOf(ax, ay));
 	halfAngle(perpA, az, &k.cI, &k.sI);
+	k.c2I = k.cI * k.cI;
+	k.s2I = k.sI * k.sI;
 	k.qI = sqrt(perpA * perpA + az * az);
 	return k;
 }
@@ -632,43 +653,103 @@ PWA_HD float deltaM2(const WaveDev& w, const Kin<float>& k)
 	return ((w.dmHi - k.mI) + (w.dmLo - k.mIlo)) * (w.dmHi + k.mI);
 }
 
+// u^m for a unit complex u and an integer m of either sign (u^-1 = conj u),
+// by repeated squaring
+template <typename T>
+PWA_HD C2T<T> cpowi(C2T<T> u, int m)
+{
+	if (m < 0) {
+		u.im = -u.im;
+		m = -m;
+	}
+	C2T<T> r{T(1), T(0)};
+	while (m > 0) {
+		if (m & 1)
+			r = cmul(r, u);
+		u = cmul(u, u);
+		m >>= 1;
+	}
+	return r;
+}
+
+// d^j_{m n}(theta) from its Wigner terms t0..t1-1 (dEval's arguments): the
+// power of cos(theta/2) falls and that of sin(theta/2) rises by 2 from one
+// term to the next (wignerTerms), so the sum is c^a_last s^b_first times a
+// homogeneous polynomial in c^2 and s^2, evaluated Horner-like
+template <typename T>
+PWA_HD T dHorner(const DTerm* t, int t0, int t1, T c, T s, T c2, T s2)
+{
+	if (t0 >= t1)
+		return T(0);
+	T r = pick<T>(t[t0].coef, t[t0].coefF), sk = T(1);
+	for (int k = t0 + 1; k < t1; ++k) {
+		sk *= s2;
+		r = r * c2 + pick<T>(t[k].coef, t[k].coefF) * sk;
+	}
+	return r * ipow(c, t[t1 - 1].a) * ipow(s, t[t0].b);
+}
+
 // amplitude of wave w for one symmetrisation term; T is the arithmetic of
-// the per-wave part.  k is the term's kinematics; mass dependences of the
-// isobar mass alone are cached in it.
+// the per-wave part.  k is the term's kinematics; the values that several
+// waves share (mass dependence and isobar barrier factor of one isobar class,
+// the X-vertex barrier factor of one L) are cached in it.
 template <typename T>
 PWA_HD C2T<T> termAmplitude(const PlanView& P, const WaveDev& w, Kin<T>& k)
 {
-	const T cX = k.cX, sX = k.sX, cI = k.cI, sI = k.sI, phiH = k.phiH, phi = k.phi;
-	// e^{i lam phiH / 2} stepped by e^{i phiH} from lam = lamIso of the first term
-	const C2T<T> step = cexpi(phiH);
+	// e^{i lamIso phiH / 2} as a power of e^{i phiH / 2}, stepped by e^{i phiH}
+	const C2T<T> stepH = cmul(k.uH, k.uH);
 	C2T<T> eL{T(1), T(0)};
 	C2T<T> sum{T(0), T(0)};
+	// e^{i m phi / 2} of the X vertex, recomputed only when m changes
+	// (helicity formalism: m = +-M for every isobar helicity of the wave)
+	constexpr int kNone = 1 << 30;
+	int mP = kNone, mM = kNone;
+	C2T<T> eP{T(1), T(0)}, eM{T(1), T(0)};
 	for (int t = w.lam0; t < w.lam1; ++t) {
 		const LamTerm& L = P.lams[t];
 		if (t == w.lam0)
-			eL = cexpi(T(0.5) * T(L.lamIso) * phiH);
+			eL = cpowi(k.uH, L.lamIso);
 		else
 			for (int s = P.lams[t - 1].lamIso; s < L.lamIso; s += 2)
-				eL = cmul(eL, step);
-		const T dP = dEval<T>(P.dterms, L.plus0, L.plus1, cX, sX);
-		const T dM = dEval<T>(P.dterms, L.minus0, L.minus1, cX, sX);
-		const T dI = dEval<T>(P.dterms, L.iso0, L.iso1, cI, sI);
-		const C2T<T> x = cadd(cscale(cexpi(T(0.5) * T(L.mPlus) * phi), pick<T>(L.cPlus, L.cPlusF) * dP),
-		                      cscale(cexpi(T(0.5) * T(L.mMinus) * phi), pick<T>(L.cMinus, L.cMinusF) * dM));
+				eL = cmul(eL, stepH);
+		C2T<T> x{T(0), T(0)};
+		if (L.plus1 > L.plus0) {
+			if (L.mPlus != mP) {
+				mP = L.mPlus;
+				eP = cpowi(k.u, mP);
+			}
+			x = cscale(eP, pick<T>(L.cPlus, L.cPlusF) * dHorner<T>(P.dterms, L.plus0, L.plus1, k.cX, k.sX, k.c2X, k.s2X));
+		}
+		if (L.minus1 > L.minus0) {
+			if (L.mMinus != mM) {
+				mM = L.mMinus;
+				eM = (mP != kNone && mM == -mP) ? C2T<T>{eP.re, -eP.im} : cpowi(k.u, mM);
+			}
+			x = cadd(x, cscale(eM, pick<T>(L.cMinus, L.cMinusF) *
+			                           dHorner<T>(P.dterms, L.minus0, L.minus1, k.cX, k.sX, k.c2X, k.s2X)));
+		}
+		const T dI = dHorner<T>(P.dterms, L.iso0, L.iso1, k.cI, k.sI, k.c2I, k.s2I);
 		sum = cadd(sum, cmul(x, cscale(eL, dI)));
 	}
-	const T f = sqrt(barrierF2<T>(P, w.LX, k.qX) * barrierF2<T>(P, w.LI, k.qI));
-	C2T<T> md;
-	if (massDepOfMassAlone(w.massDep)) {
-		if (k.mdKind != w.massDep) {
-			k.md = massDependence<T>(P, w, k.mI, deltaM2(w, k), k.mId);
-			k.mdKind = w.massDep;
+	if (k.isoKey != w.iso) {
+		C2T<T> md;
+		if (massDepOfMassAlone(w.massDep)) {
+			if (k.mdKind != w.massDep) {
+				k.md = massDependence<T>(P, w, k.mI, deltaM2(w, k), k.mId);
+				k.mdKind = w.massDep;
+			}
+			md = k.md;
+		} else {
+			md = massDependence<T>(P, w, k.mI, deltaM2(w, k), k.mId);
 		}
-		md = k.md;
-	} else {
-		md = massDependence<T>(P, w, k.mI, deltaM2(w, k), k.mId);
+		k.isoVal = cscale(md, static_cast<T>(sqrt(barrierF2<T>(P, w.LI, k.qI))));
+		k.isoKey = w.iso;
 	}
-	return cscale(cmul(sum, md), f);
+	if (k.lxKey != w.LX) {
+		k.lxVal = static_cast<T>(sqrt(barrierF2<T>(P, w.LX, k.qX)));
+		k.lxKey = w.LX;
+	}
+	return cscale(cmul(sum, k.isoVal), k.lxVal);
 }
 
 // Gottfried-Jackson four-vectors of the three final-state slots of one

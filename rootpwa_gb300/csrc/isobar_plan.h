@@ -561,14 +561,41 @@ inline std::string buildPlan(const std::vector<pwa_isobar_wave>& specs, const do
 		w.lam1 = (int32_t)plan.lams.size();
 		plan.waves.push_back(w);
 	}
+	// isobar classes: waves whose mass dependence (kind and parameters) and
+	// isobar barrier factor agree share their product per event and term
+	auto sameIsobar = [](const WaveDev& x, const WaveDev& y) {
+		if (x.massDep != y.massDep || x.LI != y.LI || x.a != y.a || x.b != y.b || x.m0 != y.m0 || x.g0 != y.g0 ||
+		    x.q0 != y.q0 || x.f2q0 != y.f2q0 || x.ma != y.ma || x.mb != y.mb || x.q02 != y.q02)
+			return false;
+		for (int k = 0; k < 10; ++k)
+			if (x.mdp[k] != y.mdp[k])
+				return false;
+		return true;
+	};
+	for (size_t i = 0; i < plan.waves.size(); ++i) {
+		WaveDev& w = plan.waves[i];
+		w.iso = (int32_t)i;
+		for (size_t j = 0; j < i; ++j)
+			if (sameIsobar(plan.waves[j], w)) {
+				w.iso = plan.waves[j].iso;
+				break;
+			}
+	}
 	plan.order.resize(plan.waves.size());
 	for (size_t i = 0; i < plan.order.size(); ++i)
 		plan.order[i] = (int32_t)i;
-	// waves of one topology class together (they share the kinematics), and
-	// within a class those of one mass dependence (they share its cached value)
+	// waves of one topology class together (they share the kinematics), within
+	// a class those of one mass dependence and isobar class, then of one X-vertex
+	// L (they share the cached values)
 	std::stable_sort(plan.order.begin(), plan.order.end(), [&](int32_t x, int32_t y) {
 		const WaveDev &a = plan.waves[x], &b = plan.waves[y];
-		return a.topo != b.topo ? a.topo < b.topo : a.massDep < b.massDep;
+		if (a.topo != b.topo)
+			return a.topo < b.topo;
+		if (a.massDep != b.massDep)
+			return a.massDep < b.massDep;
+		if (a.iso != b.iso)
+			return a.iso < b.iso;
+		return a.LX < b.LX;
 	});
 	fillFp32Copies(plan);
 	return std::string();
