@@ -802,7 +802,7 @@ PWA_HD void eventAmplitudes(const PlanView& P, const double bp[3], const double 
 	int topo = -1;
 	for (uint32_t o = 0; o < P.nWaves; ++o) {
 		const int wi = P.order[o];
-		const WaveDev w = P.waves[wi];
+		const WaveDev& w = P.waves[wi];
 		if (w.topo != topo) {
 			topo = w.topo;
 			valid = 0;
