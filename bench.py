@@ -1251,8 +1251,9 @@ def run_isobar(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None, "peak_kind": peak_kind,
                      "note": ("algorithmic bytes (96 B in + 8 B per wave out per event, complex64 mode); the "
-                              "kernel is not HBM-bound: ncu shows the FP64 pipe 76 % active (per-event FP64 "
-                              "frames), FP32 8 %, DRAM 0.4 % (profiles/isobar_amplitude_kernel_3pi88.md)")},
+                              "kernel is not HBM-bound: it is latency-bound on the per-wave FP32 arithmetic "
+                              "and its plan loads (ncu: issue active 49 %, DRAM < 1 %; "
+                              "profiles/isobar_amplitude_kernel_3pi88.md)")},
         "cpu_baseline": {"value": n_check / t_cpu, "unit": "events/s", "cores": 1, "kind": "port",
                          "sample": "FP64 oracle (numpy) on %d events x %d waves" % (n_check, W)},
         "max_rel_err_vs_oracle": err,
