@@ -89,6 +89,7 @@ struct TcArgs {
 	int kt;             // events per tile: kKT or kKTB
 	int stages;         // raw TMA stages
 	int period;         // tiles between drains of the accumulators
+	int groups;         // 1, or 2 row groups of W / 2 rows loaded by one 3-D TMA copy
 	uint64_t tilesTotal;
 	const double* weightK;  // per event, or null
 	float* partials;        // [grid][2 (Re, D)][128][N]
@@ -150,6 +151,16 @@ __device__ __forceinline__ void tmaLoad2d(void* dst, const CUtensorMap* map, int
 	    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
 	        sAddr(dst)),
 	    "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(sAddr(bar))
+	    : "memory");
+}
+
+// the same for a map of two row groups (x, row, group)
+__device__ __forceinline__ void tmaLoad3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+	asm volatile(
+	    "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+	        sAddr(dst)),
+	    "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(sAddr(bar))
 	    : "memory");
 }
 
@@ -343,7 +354,10 @@ __global__ void __launch_bounds__(DB ? kThreadsDB : kThreadsTc, 1)
 				if (*(volatile unsigned*)&sFail)
 					break;
 				barExpectTx(&rawFull[s], rawBytes);
-				tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, &rawFull[s]);
+				if (a.groups == 2)
+					tmaLoad3d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, 0, &rawFull[s]);
+				else
+					tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, &rawFull[s]);
 				++issued;
 			}
 			// the copies of this CTA land before it exits
@@ -727,7 +741,10 @@ __global__ void __launch_bounds__(kThreadsHL, 1) gramTcHiLoKernel(const __grid_c
 				if (*(volatile unsigned*)&sFail)
 					break;
 				barExpectTx(&rawFull[s], rawBytes);
-				tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, &rawFull[s]);
+				if (a.groups == 2)
+					tmaLoad3d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, 0, &rawFull[s]);
+				else
+					tmaLoad2d(raw + (size_t)s * rawStride, &map, (int)(2 * (t0 + t) * (uint64_t)a.kt), 0, &rawFull[s]);
 				++issued;
 			}
 			for (int t = (issued > a.stages ? issued - a.stages : 0); t < issued; ++t)
@@ -1025,6 +1042,8 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 		return setError(kErrUnsupported, "tensor-core Gram needs an even row stride and a 16-byte aligned base");
 	if (g.K == 0)
 		return setError(kErrArg, "tensor-core Gram: no events");
+	if (g.groupStride && ((g.W & 1) || (g.groupStride & 1ull)))
+		return setError(kErrUnsupported, "tensor-core Gram: two row groups need an even wave count and group offset");
 	int dev = 0;
 	PWA_CHECK_RET(cudaCheck(cudaGetDevice(&dev), "cudaGetDevice"));
 	int maxSmem = 0;
@@ -1043,6 +1062,7 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	a.bf16 = (precision == 4) ? 1 : 0;
 	a.kt = a.bf16 ? kKTB : kKT;
 	a.tilesTotal = (g.K + a.kt - 1) / a.kt;
+	a.groups = g.groupStride ? 2 : 1;
 	a.weightK = g.weightK;
 	a.devErr = g.devErr;
 	const size_t rawStride = ((size_t)g.W * a.kt * 8 + 1023) & ~size_t(1023);
@@ -1065,12 +1085,15 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	EncodeTiledFn enc = nullptr;
 	PWA_CHECK_RET(encodeTiled(&enc));
 	CUtensorMap map;
-	const cuuint64_t dims[2] = {(cuuint64_t)(2 * g.K), (cuuint64_t)g.W};
-	const cuuint64_t strides[1] = {(cuuint64_t)(g.ldK * 8)};
-	const cuuint32_t box[2] = {(cuuint32_t)(2 * a.kt), (cuuint32_t)g.W};
-	const cuuint32_t estr[2] = {1u, 1u};
-	const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(g.amps), dims, strides, box,
-	                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+	// one group: (float x, row); two groups: (float x, row, group), the box
+	// [2][W/2][64 floats] landing in shared memory as [W][64]
+	const int G = a.groups == 2 ? g.W / 2 : g.W;
+	const cuuint64_t dims[3] = {(cuuint64_t)(2 * g.K), (cuuint64_t)G, 2};
+	const cuuint64_t strides[2] = {(cuuint64_t)(g.ldK * 8), (cuuint64_t)(g.groupStride * 8)};
+	const cuuint32_t box[3] = {(cuuint32_t)(2 * a.kt), (cuuint32_t)G, 2};
+	const cuuint32_t estr[3] = {1u, 1u, 1u};
+	const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, a.groups == 2 ? 3 : 2, const_cast<float2*>(g.amps),
+	                        dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
 	                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	if (cr != CUDA_SUCCESS)
 		return setError(kErrCuda, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");

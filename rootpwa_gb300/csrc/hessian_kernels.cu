@@ -6,12 +6,13 @@
 // weighted by f^2 (f = 2/L) plus a same-(rank, reflectivity) block of
 // f A_i conj(A_j).  This kernel writes, for one slab of events, the complex
 // columns [d; conj(d); 1] and [A; 1] with weights f^2 and f, so that two
-// weighted complex Gram products (integral_kernels.cu) yield
+// weighted complex Gram products (the tensor-core Gram of gram_tc.cu, TF32x3,
+// in pairs of 48-row groups for the wide first set) yield
 //   sum f^2 d_i conj(d_j), sum f^2 d_i d_j, sum f^2 d_i, sum f^2,
 //   sum f A_i conj(A_j), sum f
 // from which the host assembles the three real blocks the reference keeps
-// per slot pair.  Coherent sums are FP32, Gram sums FP32 per chunk and FP64
-// across chunks.
+// per slot pair.  Coherent sums are FP32; the Gram sums FP32 in tensor
+// memory per few tiles and FP64 across CTAs and slabs.
 
 #include "pwa_internal.h"
 

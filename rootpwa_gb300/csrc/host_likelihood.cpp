@@ -1289,52 +1289,94 @@ int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* H)
 	const uint32_t P = L->nPars, W = L->W(), R = L->rank;
 	const uint32_t nS = R * W, nY1 = 2 * nS + 1, nY2 = W + 1;
 	cudaStream_t s = L->stream;
-	// event slabs sized so that the [d; conj d; 1] columns stay below ~1 GB
+	// The weighted Grams run on the tensor cores (TF32x3, the hi/lo kernel of
+	// gram_tc.cu, up to 96 columns): a set of at most 96 columns in one Gram;
+	// a wider set is split into groups of 48 rows, and the Gram of each pair
+	// of groups (one 3-D TMA copy brings both) supplies their cross block and
+	// the groups' diagonal blocks.  The operand rows are padded with zero rows
+	// to whole groups.
+	auto groupsOf = [](uint32_t n, uint32_t* G, uint32_t* ng) {
+		*G = n <= 96 ? n : 48;
+		*ng = (n + *G - 1) / *G;
+	};
+	uint32_t gs1, ng1, gs2, ng2;
+	groupsOf(nY1, &gs1, &ng1);
+	groupsOf(nY2, &gs2, &ng2);
+	const uint64_t rows1 = (uint64_t)gs1 * ng1, rows2 = (uint64_t)gs2 * ng2;
+	// event slabs sized so that the [d; conj d; 1] columns stay below ~1 GB;
+	// a multiple of 64 events (the tensor maps want an even row stride)
 	uint64_t slab = (uint64_t)1 << 30;
-	slab /= (uint64_t)nY1 * sizeof(float2);
-	slab = std::max<uint64_t>(1024, std::min<uint64_t>(slab, (L->nEvents + 63) / 64 * 64));
-	const int tps = ((int)nY1 + 63) / 64;
-	const int nTiles = tps * (tps + 1) / 2;
-	int chunks = std::max(1, (4 * L->numSMs + nTiles - 1) / nTiles);
-	chunks = (int)std::min<uint64_t>((uint64_t)chunks, std::max<uint64_t>(1, slab / 64));
-	DevBuf dY1, dY2, dW1, dW2, dPart, dG1, dG2, dHP;
-	PWA_TRY(dY1.alloc((size_t)nY1 * slab * sizeof(float2), "hessian operand"));
-	PWA_TRY(dY2.alloc((size_t)nY2 * slab * sizeof(float2), "hessian operand"));
+	slab /= rows1 * sizeof(float2);
+	slab = std::max<uint64_t>(1024, std::min<uint64_t>(slab, (L->nEvents + 63) / 64 * 64)) / 64 * 64;
+	const uint32_t maxGram = std::max(ng1 > 1 ? 2 * gs1 : gs1, ng2 > 1 ? 2 * gs2 : gs2);
+	const size_t scratch = gramTcScratchFloats((int)maxGram, L->numSMs) / 2 + 1;
+	DevBuf dY1, dY2, dW1, dW2, dPart, dBlk, dErrG, dG1, dG2, dHP;
+	PWA_TRY(dY1.alloc((size_t)rows1 * slab * sizeof(float2), "hessian operand"));
+	PWA_TRY(dY2.alloc((size_t)rows2 * slab * sizeof(float2), "hessian operand"));
 	PWA_TRY(dW1.alloc(slab * sizeof(double), "hessian weights"));
 	PWA_TRY(dW2.alloc(slab * sizeof(double), "hessian weights"));
-	PWA_TRY(dPart.alloc((size_t)chunks * nY1 * nY1 * 2 * sizeof(double), "hessian partials"));
+	PWA_TRY(dPart.alloc(scratch * sizeof(double), "hessian gram partials"));
+	PWA_TRY(dBlk.alloc((size_t)maxGram * maxGram * 2 * sizeof(double), "hessian gram block"));
+	PWA_TRY(dErrG.alloc(sizeof(unsigned), "flag"));
 	PWA_TRY(dG1.alloc((size_t)nY1 * nY1 * 2 * sizeof(double), "hessian gram"));
 	PWA_TRY(dG2.alloc((size_t)nY2 * nY2 * 2 * sizeof(double), "hessian gram"));
 	PWA_TRY(dHP.alloc(P * sizeof(double), "hessian parameters"));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(dHP.p, par, P * sizeof(double), cudaMemcpyHostToDevice, s), "H2D par"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(dG1.p, 0, dG1.bytes, s), "memset"));
 	PWA_TRY(cudaCheck(cudaMemsetAsync(dG2.p, 0, dG2.bytes, s), "memset"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(dErrG.p, 0, sizeof(unsigned), s), "memset"));
+	if (rows1 > nY1)
+		PWA_TRY(cudaCheck(cudaMemsetAsync(dY1.as<float2>() + (size_t)nY1 * slab, 0,
+		                                  (size_t)(rows1 - nY1) * slab * sizeof(float2), s),
+		                  "memset"));
+	if (rows2 > nY2)
+		PWA_TRY(cudaCheck(cudaMemsetAsync(dY2.as<float2>() + (size_t)nY2 * slab, 0,
+		                                  (size_t)(rows2 - nY2) * slab * sizeof(float2), s),
+		                  "memset"));
+	// dG (n x n) += the weighted Gram of the n rows of Y over K events
+	auto gramAdd = [&](const float2* Y, uint32_t n, uint32_t G, uint32_t ng, const double* w, uint64_t K,
+	                   double* dG) -> int {
+		GramArgs g{};
+		g.K = K;
+		g.ldK = slab;
+		g.weightK = w;
+		g.devErr = dErrG.as<unsigned>();
+		if (ng == 1) {
+			g.amps = Y;
+			g.W = (int)n;
+			PWA_TRY(launchGramTc(g, PWA_PRECISION_TF32X3, L->numSMs, s, dBlk.as<double>(), dPart.as<double>(), scratch));
+			return launchGramBlockAdd(dBlk.as<double>(), (int)n, (int)n, 0, 0, (int)n, 1, 1, dG, s);
+		}
+		for (uint32_t ga = 0; ga < ng; ++ga)
+			for (uint32_t gb = ga + 1; gb < ng; ++gb) {
+				g.amps = Y + (size_t)ga * G * slab;
+				g.W = (int)(2 * G);
+				g.groupStride = (uint64_t)(gb - ga) * G * slab;
+				PWA_TRY(launchGramTc(g, PWA_PRECISION_TF32X3, L->numSMs, s, dBlk.as<double>(), dPart.as<double>(),
+				                     scratch));
+				// group ga's diagonal block from its pair with ga + 1, the last
+				// group's from the last pair
+				PWA_TRY(launchGramBlockAdd(dBlk.as<double>(), (int)(2 * G), (int)G, (int)ga, (int)gb, (int)n,
+				                           gb == ga + 1 ? 1 : 0, (ga + 2 == ng && gb + 1 == ng) ? 1 : 0, dG, s));
+			}
+		return kOk;
+	};
 	for (uint64_t e0 = 0; e0 < L->nEvents; e0 += slab) {
 		const uint64_t K = std::min<uint64_t>(slab, L->nEvents - e0);
 		PWA_TRY(launchHessPrep(L->amps.as<float2>(), L->nEvents, L->storeB, e0, slab, (int)L->nW[0], (int)W, (int)R,
 		                       (int)P, dHP.as<double>(), L->dSlotRe.as<int>(), L->dSlotIm.as<int>(), dY1.as<float2>(),
 		                       dY2.as<float2>(), dW1.as<double>(), dW2.as<double>(), s));
-		const int ck = (int)std::min<uint64_t>((uint64_t)chunks, std::max<uint64_t>(1, K / 64));
-		GramArgs g{};
-		g.K = K;
-		g.ldK = slab;
-		g.partials = dPart.as<double>();
-		g.chunks = ck;
-		g.amps = dY1.as<float2>();
-		g.W = (int)nY1;
-		g.weightK = dW1.as<double>();
-		PWA_TRY(launchGramSimt(g, PWA_PRECISION_FP32, s));
-		PWA_TRY(launchGramReduce(g.partials, ck, (int)nY1, dG1.as<double>(), 1, s));
-		g.amps = dY2.as<float2>();
-		g.W = (int)nY2;
-		g.weightK = dW2.as<double>();
-		PWA_TRY(launchGramSimt(g, PWA_PRECISION_FP32, s));
-		PWA_TRY(launchGramReduce(g.partials, ck, (int)nY2, dG2.as<double>(), 1, s));
+		PWA_TRY(gramAdd(dY1.as<float2>(), nY1, gs1, ng1, dW1.as<double>(), K, dG1.as<double>()));
+		PWA_TRY(gramAdd(dY2.as<float2>(), nY2, gs2, ng2, dW2.as<double>(), K, dG2.as<double>()));
 	}
+	unsigned gramErr = 0;
+	PWA_TRY(cudaCheck(cudaMemcpyAsync(&gramErr, dErrG.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "D2H flag"));
 	std::vector<double> G1((size_t)nY1 * nY1 * 2), G2((size_t)nY2 * nY2 * 2);
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(G1.data(), dG1.p, G1.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H"));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(G2.data(), dG2.p, G2.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H"));
 	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "hessian sync"));
+	if (gramErr)
+		return setError(kErrTimeout, "Hessian Gram kernel: a bounded device-side wait expired");
 	auto g1 = [&](uint32_t a, uint32_t b) { return cplx(G1[((size_t)a * nY1 + b) * 2], G1[((size_t)a * nY1 + b) * 2 + 1]); };
 	auto g2 = [&](uint32_t a, uint32_t b) { return cplx(G2[((size_t)a * nY2 + b) * 2], G2[((size_t)a * nY2 + b) * 2 + 1]); };
 

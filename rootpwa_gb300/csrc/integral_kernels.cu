@@ -172,6 +172,38 @@ int launchGramSimt(const GramArgs& a, int precision, cudaStream_t s)
 	return cudaCheck(cudaGetLastError(), "gram SIMT launch");
 }
 
+// out += the blocks of a Gram of two row groups: rows and columns i < G of
+// blk belong to group a (global index a G + i), the others to group b
+// (b G + i - G); the cross blocks are always added, the diagonal blocks of
+// group a / b only when addAA / addBB (another pair may supply them);
+// indices >= nOut are padding and skipped.  One group (G = n2) adds all.
+__global__ void gramBlockAddKernel(const double* blk, int n2, int G, int a, int b, int nOut, int addAA, int addBB,
+                                   double* out)
+{
+	const int n = n2 * n2;
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+		const int i = e / n2, j = e - i * n2;
+		const bool ia = i < G, ja = j < G;
+		if ((ia && ja && !addAA) || (!ia && !ja && !addBB))
+			continue;
+		const int gi = ia ? a * G + i : b * G + (i - G), gj = ja ? a * G + j : b * G + (j - G);
+		if (gi >= nOut || gj >= nOut)
+			continue;
+		out[((size_t)gi * nOut + gj) * 2] += blk[(size_t)e * 2];
+		out[((size_t)gi * nOut + gj) * 2 + 1] += blk[(size_t)e * 2 + 1];
+	}
+}
+
+int launchGramBlockAdd(const double* blk, int n2, int G, int a, int b, int nOut, int addAA, int addBB, double* out,
+                       cudaStream_t s)
+{
+	const int n = n2 * n2;
+	const int blocks = std::max(1, std::min(1024, (n + 255) / 256));
+	gramBlockAddKernel<<<blocks, 256, 0, s>>>(blk, n2, G, a, b, nOut, addAA, addBB, out);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "gram block add launch");
+}
+
 int launchGramReduce(const double* partials, int chunks, int W, double* out, int accumulate, cudaStream_t s)
 {
 	const int n = W * W;

@@ -157,10 +157,17 @@ struct GramArgs {
 	double* partials;       // [chunks][W*W*2]
 	int chunks;
 	unsigned* devErr;
+	// tensor-core Gram only: 0, or the element offset between two groups of
+	// W / 2 rows each (the Gram of rows 0..W/2-1 and groupStride.. + W/2-1)
+	uint64_t groupStride;
 };
 int launchGramSimt(const GramArgs& a, int precision, cudaStream_t s);
 // out = (accumulate ? out : 0) + sum of chunk partials, mirrored to the lower triangle
 int launchGramReduce(const double* partials, int chunks, int W, double* out, int accumulate, cudaStream_t s);
+// out (nOut x nOut complex) += blocks of the Gram blk of two row groups of G
+// rows (groups a and b; see integral_kernels.cu)
+int launchGramBlockAdd(const double* blk, int n2, int G, int a, int b, int nOut, int addAA, int addBB, double* out,
+                       cudaStream_t s);
 // tcgen05 tensor-core Gram; returns kErrUnsupported when the shape has no variant
 int launchGramTc(const GramArgs& a, int precision, int numSMs, cudaStream_t s, double* out, double* scratch,
                  size_t scratchDoubles);
