@@ -973,30 +973,42 @@ __global__ void __launch_bounds__(kThreadsHL, 1) gramTcHiLoKernel(const __grid_c
 	}
 }
 
-// FP64 sum of the CTAs' partials in CTA order; assembles the Hermitian matrix
-// (upper triangle from Re and D, lower mirrored, real diagonal).  sym: the
-// first partial is S with Re = (S + S^T) / 2 (the hi/lo kernel).
-__global__ void gramTcReduceKernel(const float* partials, int grid, int W, int N, int sym, double* out)
+// FP64 sum of the CTAs' partials; assembles the Hermitian matrix (upper
+// triangle from Re and D, lower mirrored, real diagonal).  sym: the first
+// partial is S with Re = (S + S^T) / 2 (the hi/lo kernel).  One warp per
+// element: lane l sums CTAs l, l + 32, ... in order, a fixed butterfly
+// combines the lanes (the same order on every run).
+__global__ void __launch_bounds__(256) gramTcReduceKernel(const float* partials, int grid, int W, int N, int sym,
+                                                          double* out)
 {
+	const int lane = threadIdx.x & 31;
+	const int nWarps = (int)((gridDim.x * blockDim.x) >> 5);
 	const int n = W * W;
-	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+	for (int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); e < n; e += nWarps) {
 		const int i = e / W, j = e - i * W;
 		if (i > j)
 			continue;
 		double re = 0., im = 0.;
-		for (int c = 0; c < grid; ++c) {
+		for (int c = lane; c < grid; c += 32) {
 			const float* Re = partials + (size_t)c * 2 * 128 * N;
 			const float* D = Re + (size_t)128 * N;
 			re += sym ? 0.5 * ((double)Re[(size_t)i * N + j] + (double)Re[(size_t)j * N + i])
 			          : (double)Re[(size_t)i * N + j];
 			im += (double)D[(size_t)i * N + j] - (double)D[(size_t)j * N + i];
 		}
-		if (i == j)
-			im = 0.;
-		out[(size_t)e * 2] = re;
-		out[(size_t)e * 2 + 1] = im;
-		out[((size_t)j * W + i) * 2] = re;
-		out[((size_t)j * W + i) * 2 + 1] = -im;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			re += __shfl_xor_sync(0xffffffffu, re, o);
+			im += __shfl_xor_sync(0xffffffffu, im, o);
+		}
+		if (lane == 0) {
+			if (i == j)
+				im = 0.;
+			out[(size_t)e * 2] = re;
+			out[(size_t)e * 2 + 1] = im;
+			out[((size_t)j * W + i) * 2] = re;
+			out[((size_t)j * W + i) * 2 + 1] = -im;
+		}
 	}
 }
 
@@ -1117,7 +1129,7 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	countLaunches(1);
 	PWA_CHECK_RET(cudaCheck(cudaGetLastError(), "gram TC launch"));
 	const int n = g.W * g.W;
-	const int blocks = std::max(1, std::min(1024, (n + 255) / 256));
+	const int blocks = std::max(1, std::min(4096, (n + 7) / 8));  // eight warps per block, one per element
 	gramTcReduceKernel<<<blocks, 256, 0, s>>>(a.partials, grid, g.W, a.N, hiLo ? 1 : 0, out);
 	countLaunches(1);
 	return cudaCheck(cudaGetLastError(), "gram TC reduce launch");

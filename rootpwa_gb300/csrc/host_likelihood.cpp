@@ -1303,9 +1303,11 @@ int pwa_likelihood_hessian(pwa_likelihood* L, const double* par, double* H)
 	groupsOf(nY1, &gs1, &ng1);
 	groupsOf(nY2, &gs2, &ng2);
 	const uint64_t rows1 = (uint64_t)gs1 * ng1, rows2 = (uint64_t)gs2 * ng2;
-	// event slabs sized so that the [d; conj d; 1] columns stay below ~1 GB;
-	// a multiple of 64 events (the tensor maps want an even row stride)
-	uint64_t slab = (uint64_t)1 << 30;
+	// event slabs sized so that the [d; conj d; 1] columns stay below ~4 GB
+	// (10^6 events of the 349-column set in one slab: fewer, longer Gram
+	// launches); a multiple of 64 events (the tensor maps want an even row
+	// stride)
+	uint64_t slab = (uint64_t)4 << 30;
 	slab /= rows1 * sizeof(float2);
 	slab = std::max<uint64_t>(1024, std::min<uint64_t>(slab, (L->nEvents + 63) / 64 * 64)) / 64 * 64;
 	const uint32_t maxGram = std::max(ng1 > 1 ? 2 * gs1 : gs1, ng2 > 1 ? 2 * gs2 : gs2);
