@@ -2,7 +2,9 @@
 639-859) and the covariance matrix (:929-981) against the FP64 oracle.
 
 Tolerance: max |H - H_ref| / max |H_ref| below 2e-5 (FP32 event products,
-FP64 sums across chunks)."""
+TF32x3 tensor-core Gram sums, FP64 across CTAs).  compass88 at rank 2 has
+2 x 2 x 87 + 1 = 349 Gram columns, which run as Grams of pairs of 48-row
+groups (the last group padded); compass15 at rank 3 (91 columns) as one."""
 import numpy as np
 import pytest
 
