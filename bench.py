@@ -889,7 +889,7 @@ def run_precision(args):
         out["fdf_vs_oracle"][red] = {"ll_rel": abs(f - f0) / abs(f0),
                                      "grad_normwise": float(np.max(np.abs(gg - g0)) / np.max(np.abs(g0))),
                                      "us_per_fdf_host_call": us,
-                                     "cross_tile": {"fp64": "FP32 partials of 32 tiles folded into FP64",
+                                     "cross_tile": {"fp64": "FP32 partials of 64 tiles folded into FP64",
                                                     "kahan_fp32": "every tile into compensated FP32",
                                                     "fp32": "plain FP32 over all tiles"}[red]}
     # effect of the integral arithmetic on LL and gradient (GPU FdF, FP64 reductions)

@@ -98,10 +98,10 @@ __host__ __device__ inline int waveSplit(int W0, int W, int* nNeg, int* wn, int*
 
 // Tiles whose gradient partials are summed in FP32 before the warp
 // reduce-scatter folds them into the FP64 accumulators (a lane's FP32
-// partial then covers 128 events of one wave; the LL and gradient errors
+// partial then covers 256 events of one wave; the LL and gradient errors
 // against FP64 at 1 M events are the same as with 8).  The compensated mode
 // folds every tile; the plain FP32 mode only after the last one.
-constexpr int kFold = 32;
+constexpr int kFold = 64;
 __device__ __forceinline__ int foldTiles(int reduction) { return reduction == 0 ? kFold : reduction == 1 ? 1 : 1 << 30; }
 
 

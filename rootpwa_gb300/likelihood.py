@@ -361,7 +361,7 @@ class pwaLikelihood:
         N.call("pwa_likelihood_set_stream", self._h, C.c_void_p(int(stream_handle)))
 
     def setReduction(self, mode):
-        """cross-tile reduction: 'fp64' (default: FP32 partials of 32 tiles
+        """cross-tile reduction: 'fp64' (default: FP32 partials of 64 tiles
         folded into FP64), 'kahan_fp32' (every tile into compensated FP32) or
         'fp32' (plain FP32 over all tiles)."""
         m = {"fp64": N.REDUCE_FP64, "kahan_fp32": N.REDUCE_KAHAN_FP32,

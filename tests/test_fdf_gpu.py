@@ -187,9 +187,10 @@ def test_reduction_modes(mode):
     """The three cross-tile reduction modes at 50,000 events: each within the
     engine's tolerances of the FP64 oracle and bitwise reproducible.  The
     compensated mode folds every tile, so its sums differ from the FP64
-    mode's; here every block holds fewer than 32 tiles, so the FP64 mode (a
-    fold every 32 tiles) and the plain FP32 mode (one fold after the last
-    tile) fold at the same point and agree bitwise."""
+    mode's; here every block holds fewer than 64 tiles, so the FP64 mode (a
+    fold every 64 tiles of the main kernel, 32 of the narrow one) and the
+    plain FP32 mode (one fold after the last tile) fold at the same point and
+    agree bitwise."""
     w = synth.make_workload("compass88", seed=5, n_data=50000, n_mc=4000)
     O, G = pair(w)
     G.setReduction(mode)
