@@ -17,10 +17,11 @@ struct pwa_mlp {
 	// training set on the device
 	DevBuf trainX, trainT;
 	long step = 0;
-	// split-K partials of the GEMMs with few output tiles
+	// K-slice partials of the tensor-core GEMMs
 	int numSMs = 1;
 	DevBuf work;
 	size_t workFloats = 0;
+	DevBuf dErr;  // device error flag of the GEMM kernel's bounded waits
 
 	~pwa_mlp()
 	{
@@ -53,20 +54,32 @@ int mlpEnsureBatch(pwa_mlp* N, int B)
 	return kOk;
 }
 
-// one product, split over K when its output has few tiles; the workspace
-// grows to the largest split product on first use (a batch size's first step)
+// one product on the tensor cores, split over K so that its blocks cover
+// the GPU; the workspace of the K-slice partials grows to the largest product
+// on first use (a batch size's first step)
 int mlpGemm(pwa_mlp* N, MlpGemm g, cudaStream_t s)
 {
 	g.splitK = mlpGemmSplit(g, N->numSMs);
-	if (g.splitK > 1) {
-		const size_t need = (size_t)g.splitK * g.M * g.N;
-		if (need > N->workFloats) {
-			PWA_TRY(N->work.alloc(need * sizeof(float), "MLP split-K workspace"));
-			N->workFloats = need;
-		}
-		g.work = N->work.as<float>();
+	const size_t need = (size_t)g.splitK * g.M * g.N;
+	if (need > N->workFloats) {
+		PWA_TRY(N->work.alloc(need * sizeof(float), "MLP K-slice workspace"));
+		N->workFloats = need;
 	}
+	g.work = N->work.as<float>();
+	g.devErr = N->dErr.as<unsigned>();
 	return launchMlpGemm(g, s);
+}
+
+// after a synchronisation: a bounded wait of a GEMM kernel expired?
+int mlpCheckDevice(pwa_mlp* N)
+{
+	unsigned e = 0;
+	PWA_TRY(cudaCheck(cudaMemcpy(&e, N->dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "MLP error flag"));
+	if (e) {
+		cudaMemset(N->dErr.p, 0, sizeof(unsigned));
+		return setError(kErrTimeout, "MLP GEMM kernel: a bounded device-side wait expired");
+	}
+	return kOk;
 }
 
 MlpGemm gemmXWt(int M, int N, int K, const uint16_t* X, const uint16_t* W)
@@ -243,6 +256,8 @@ int pwa_mlp_create(pwa_mlp** out, uint32_t nIn, uint32_t nHidden1, uint32_t nHid
 	for (DevBuf* b : {&N->params, &N->grads, &N->adamM, &N->adamV})
 		PWA_TRY(b->alloc(N->nPar * 4, "MLP parameters"));
 	PWA_TRY(N->w16.alloc(N->nPar * 2, "MLP BF16 weights"));
+	PWA_TRY(N->dErr.alloc(sizeof(unsigned), "MLP error flag"));
+	PWA_TRY(cudaCheck(cudaMemset(N->dErr.p, 0, sizeof(unsigned)), "memset"));
 	// He-normal weights (std sqrt(2 / fan_in)), zero biases, from a seeded host RNG
 	std::vector<float> p(N->nPar, 0.f);
 	std::mt19937_64 rng(seed);
@@ -306,7 +321,8 @@ int pwa_mlp_forward(pwa_mlp* N, const float* X, uint32_t B, float* Y)
 	PWA_TRY(mlpForward(N, (int)B));
 	PWA_TRY(cudaCheck(cudaMemcpyAsync(Y, N->y32.p, (size_t)B * N->nOut * 4, cudaMemcpyDeviceToHost, N->stream),
 	                  "download"));
-	return cudaCheck(cudaStreamSynchronize(N->stream), "MLP forward");
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(N->stream), "MLP forward"));
+	return mlpCheckDevice(N);
 }
 
 int pwa_mlp_gradient(pwa_mlp* N, const float* X, const float* T, uint32_t B, double* loss, float* grad)
@@ -322,7 +338,8 @@ int pwa_mlp_gradient(pwa_mlp* N, const float* X, const float* T, uint32_t B, dou
 	if (grad)
 		PWA_TRY(cudaCheck(cudaMemcpyAsync(grad, N->grads.p, N->nPar * 4, cudaMemcpyDeviceToHost, N->stream),
 		                  "download"));
-	return cudaCheck(cudaStreamSynchronize(N->stream), "MLP gradient");
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(N->stream), "MLP gradient"));
+	return mlpCheckDevice(N);
 }
 
 int pwa_mlp_train(pwa_mlp* N, const float* X, const float* T, uint64_t nSamples, uint32_t batch, uint32_t epochs,
@@ -374,6 +391,7 @@ int pwa_mlp_train(pwa_mlp* N, const float* X, const float* T, uint64_t nSamples,
 		}
 		if (lossHistory)
 			lossHistory[ep] = epochLoss / (double)std::max<uint64_t>(1, steps);
+		PWA_TRY(mlpCheckDevice(N));
 	}
 	N->trainX.release();
 	N->trainT.release();

@@ -299,10 +299,11 @@ struct MlpGemm {
 	const uint16_t* mask;  // BF16 [M][N]: zero the output where mask <= 0, or null
 	float* C32;          // FP32 [M][N] or null
 	uint16_t* C16;       // BF16 [M][N] or null
-	int splitK;          // > 1: K in splitK slices, FP32 partials in work, then the epilogue kernel
-	float* work;         // FP32 [splitK][M][N] when splitK > 1
+	int splitK;          // K slices (whole K steps of 64): FP32 partials in work, then the epilogue kernel
+	float* work;         // FP32 [splitK][M][N]
+	unsigned* devErr;    // device error flag (a bounded wait of the tensor-core kernel expired)
 };
-// K slices for an output of few tiles (at least two blocks per SM), 1 otherwise
+// K slices for the tensor-core GEMM (its blocks cover the SMs about twice)
 int mlpGemmSplit(const MlpGemm& g, int numSMs);
 int launchMlpGemm(const MlpGemm& g, cudaStream_t s);
 int launchColSum(const float* X, int M, int N, float* out, cudaStream_t s);

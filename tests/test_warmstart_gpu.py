@@ -19,7 +19,9 @@ import helpers
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("shape,B", [((37, 64, 48, 10), 33), ((5203, 512, 512, 102), 64)])
+# batches of 33 and 300 rows: one and three 128-row tiles of the tensor-core
+# GEMM (and K of 33 / 300 in the weight-gradient products dY^T X)
+@pytest.mark.parametrize("shape,B", [((37, 64, 48, 10), 33), ((37, 64, 48, 10), 300), ((5203, 512, 512, 102), 64)])
 def test_mlp_gradient_matches_oracle(shape, B):
     rng = np.random.default_rng(1)
     net = R.pwaMLP(*shape, seed=3)
