@@ -18,9 +18,11 @@
 //                       G_{s,w} += sum_e c S_{s,e} conj(A_{w,e});
 //                       per-thread FP32 (compensated for -ln L and c) over up
 //                       to 8 tiles, then FP64; FP64 partials per item.
-//                       Groups of 32 starts use two tile stages and one block
-//                       per SM; groups of 8 (little work per tile) one stage
-//                       and three blocks per SM, which take turns;
+//                       Groups of 32 starts: two tile stages, one block per SM;
+//   fdfBatch8Kernel  -- the same for groups of 8 starts (little work per
+//                       tile): register-blocked phases over a quarter of the
+//                       waves or events per thread, combined by shuffles; one
+//                       stage, several blocks per SM taking turns;
 //   batchFinishKernel -- one warp per problem: sums the items' partials in item
 //                       order (deterministic), adds nEvt (Re V^H I^acc V +
 //                       V_flat^2 eta) and the half-Cauchy prior in FP64
@@ -340,6 +342,320 @@ __global__ void __launch_bounds__(kBThreads, MINB) fdfBatchKernel(const BatchArg
 			}
 			out[(size_t)s * NV] = l;
 			out[(size_t)s * NV + 1] = c;
+		}
+		__syncthreads();
+	}
+}
+
+// ---- start groups of 8: register-blocked phases ----
+// With 8 starts a tile holds little work for 256 threads.  Mapped like the
+// 32-start kernel (2 starts x 2 events per thread in phase 1, 2 starts x 1
+// wave in phase 2) every complex product needs 12 bytes of shared-memory
+// loads, and the shared-memory pipe bounds the kernel.  Here a thread forms
+// 4 starts x 4 events over a quarter of the waves in phase 1 (6 bytes per
+// product) and 4 starts x 2 waves over a quarter of the events in phase 2
+// (6 bytes); the four lanes that split the same products combine them with a
+// two-step shuffle reduce-scatter.  Partial sums are compensated FP32 over
+// the item's tiles and FP64 per item, so the FP64 accumulators do not hold
+// registers during the tile loop (three blocks per SM, 80 registers).
+struct Batch8Smem {
+	size_t stage, vs, ts, flat, bar, total;
+};
+
+__host__ __device__ inline Batch8Smem batch8Smem(int W)
+{
+	auto up = [](size_t x) { return (x + 127) & ~size_t(127); };
+	Batch8Smem L{};
+	L.stage = 0;
+	L.vs = up((size_t)W * kBE * 8);
+	L.ts = up(L.vs + (size_t)W * 8 * 16);
+	L.flat = up(L.ts + (size_t)kBE * 8 * 8);
+	L.bar = up(L.flat + 8 * 4);
+	L.total = L.bar + 8 + 128;
+	return L;
+}
+
+// V of start s at wave w: 16-byte slot w * 8 + ((s + 2 (w & 3)) & 7), holding
+// (vx, vx, -vy, vy); c S of start s at event e: 8-byte slot
+// e * 8 + 2 ((s / 2 + ((e >> 1) & 1)) & 3) + (s & 1).  With these skews the
+// phase-1 V loads and the phase-2 c S loads of a quarter-warp hit distinct
+// 16-byte bank groups (the tile's own rotation, storeRot, does the same for
+// the amplitude loads).
+__device__ __forceinline__ int b8VSlot(int w, int s) { return w * 8 + ((s + 2 * (w & 3)) & 7); }
+__device__ __forceinline__ int b8TSlot(int e, int s) { return e * 8 + 2 * ((s / 2 + ((e >> 1) & 1)) & 3) + (s & 1); }
+
+__global__ void __launch_bounds__(kBThreads, 3) fdfBatch8Kernel(const BatchArgs a)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	constexpr int SG = 8;
+	const int W = a.W, P = a.P;
+	const Batch8Smem lay = batch8Smem(W);
+	float4* Vs = reinterpret_cast<float4*>(smem + lay.vs);
+	float2* Ts = reinterpret_cast<float2*>(smem + lay.ts);
+	float* flat2 = reinterpret_cast<float*>(smem + lay.flat);
+	uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.bar);
+	__shared__ double redLL[kBThreads / 32][4], redC[kBThreads / 32][4];
+
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint32_t tileBytes = (uint32_t)W * kBE * 8u;
+	const uint32_t tileAddr = smemAddr(smem + lay.stage), vAddr = smemAddr(Vs), tAddr = smemAddr(Ts);
+	// phase-1 role: waves w = kq (mod 4), events 4 eg .. 4 eg + 3, starts
+	// 4 sq .. 4 sq + 3; after the reduce-scatter the lane holds starts
+	// 4 sq + 2 b1 + {0, 1} of events eb + {0, 1}
+	const int kq = lane & 3, b0 = kq & 1, b1 = kq >> 1;
+	const int eg = (lane >> 2) | ((warp & 3) << 3), sq = warp >> 2;
+	const int eb = 4 * eg + 2 * (b0 ^ (eg & 1));
+	// the lane's rows all have rotation 4 kq; odd event groups load their
+	// upper 16 bytes first, so that a quarter-warp covers all 32 banks
+	const uint32_t col = (uint32_t)((4 * eg + 4 * kq) & (kBE - 1)) * 8u;
+	const uint32_t c0 = col + 16u * (uint32_t)(eg & 1), c1 = col + 16u * (uint32_t)(1 - (eg & 1));
+	const int vBase = 4 * sq + 2 * kq;  // V slot of start 4 sq + i: (vBase + i) & 7
+	// phase-2 role: events 4 i + eq, starts 4 sg .. 4 sg + 3, waves 2 wp and
+	// 2 wp + 1; after the reduce-scatter the lane holds starts
+	// 4 sg + 2 (eq >> 1) + {0, 1} of wave 2 wp + (eq & 1)
+	const int eq = lane & 3, sg = (lane >> 2) & 1, wp = (lane >> 3) | (warp << 2);
+	const bool p2 = 2 * wp < W;
+	const int wa = min(2 * wp, W - 1), wb = min(2 * wp + 1, W - 1);
+	const int ra = (int)storeRot((uint32_t)wa, kBE), rb = (int)storeRot((uint32_t)wb, kBE);
+	const uint32_t tq0 = (uint32_t)(2 * ((2 * sg + (eq >> 1)) & 3)) * 8u;      // starts 4 sg, +1
+	const uint32_t tq1 = (uint32_t)(2 * ((2 * sg + 1 + (eq >> 1)) & 3)) * 8u;  // starts 4 sg + 2, +3
+
+	if (tid == 0) {
+		mbarInit(bar, 1);
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+	uint32_t phase = 0u;
+	bool failed = false;
+
+	for (int item = blockIdx.x; item < a.nItems && !failed; item += gridDim.x) {
+		const BatchItem it = a.items[item];
+		const BinDesc bin = a.bins[it.bin];
+		const int q0 = bin.q0 + it.group * SG;
+		const int ns = min(SG, bin.nStarts - it.group * SG);
+		const int act = (tid < ns) ? a.active[q0 + tid] : 0;
+		if (!__syncthreads_or(act))
+			continue;
+		for (int k = tid; k < W * SG; k += kBThreads) {
+			const int w = k / SG, s = k - w * SG;
+			float vr = 0.f, vi = 0.f;
+			if (s < ns) {
+				const double* x = a.x + (size_t)(q0 + s) * P;
+				const int ir = a.slotRe[w], ii = a.slotIm[w];
+				vr = ir >= 0 ? (float)x[ir] : 0.f;
+				vi = ii >= 0 ? (float)x[ii] : 0.f;
+			}
+			Vs[b8VSlot(w, s)] = make_float4(vr, vr, -vi, vi);
+		}
+		if (tid < SG) {
+			const double f = (tid < ns) ? a.x[(size_t)(q0 + tid) * P + P - 1] : 0.;
+			flat2[tid] = (float)(f * f);
+		}
+		const int nt = (int)(it.t1 - it.t0);
+		if (tid == 0 && nt > 0) {
+			fenceProxyAsync();
+			mbarArriveExpectTx(bar, tileBytes);
+			bulkCopyG2S(smem + lay.stage, bin.amps + (size_t)it.t0 * W * kBE, tileBytes, bar);
+		}
+		__syncthreads();
+
+		float llF[2], llK[2], csF[2], csK[2], gF[4], gK[4];
+#pragma unroll
+		for (int x = 0; x < 2; ++x)
+			llF[x] = llK[x] = csF[x] = csK[x] = 0.f;
+#pragma unroll
+		for (int x = 0; x < 4; ++x)
+			gF[x] = gK[x] = 0.f;
+
+		int k = 0;
+		for (; k < nt; ++k) {
+			const bool ok = mbarWaitBounded(bar, phase);
+			phase ^= 1u;
+			const uint64_t ev0 = (uint64_t)(it.t0 + k) * kBE;
+
+			// ---- phase 1: S = V A over the lane's waves, 4 starts x 4 events ----
+			{
+				float2 S[4][4];  // [start][event of the lane's order]
+#pragma unroll
+				for (int i = 0; i < 4; ++i)
+#pragma unroll
+					for (int j = 0; j < 4; ++j)
+						S[i][j] = make_float2(0.f, 0.f);
+#pragma unroll 1
+				for (int w = kq; w < W; w += 4) {
+					const uint32_t row = tileAddr + (uint32_t)w * (uint32_t)(kBE * 8);
+					const float4 p0 = lds128(row + c0), p1 = lds128(row + c1);
+					const float2 av[4] = {make_float2(p0.x, p0.y), make_float2(p0.z, p0.w), make_float2(p1.x, p1.y),
+					                      make_float2(p1.z, p1.w)};
+					const uint32_t vRow = vAddr + (uint32_t)w * 128u;
+#pragma unroll
+					for (int i = 0; i < 4; ++i) {
+						const float4 v = lds128(vRow + (uint32_t)((vBase + i) & 7) * 16u);
+						const float2 vx = make_float2(v.x, v.y), vy = make_float2(v.z, v.w);
+						// (vx, vx) (ax, ay) + (-vy, vy) (ay, ax) = V A
+#pragma unroll
+						for (int j = 0; j < 4; ++j) {
+							S[i][j] = ffma2(vx, av[j], S[i][j]);
+							S[i][j] = ffma2(vy, make_float2(av[j].y, av[j].x), S[i][j]);
+						}
+					}
+				}
+				// reduce-scatter over the four wave slices: lane bit 2 keeps
+				// starts 2 b1, 2 b1 + 1, lane bit 1 the events 2 b0, 2 b0 + 1
+				float2 R1[2][4];
+#pragma unroll
+				for (int x = 0; x < 2; ++x)
+#pragma unroll
+					for (int j = 0; j < 4; ++j) {
+						const float2 keep = b1 ? S[2 + x][j] : S[x][j];
+						const float2 send = b1 ? S[x][j] : S[2 + x][j];
+						R1[x][j] = make_float2(keep.x + __shfl_xor_sync(0xffffffffu, send.x, 2),
+						                       keep.y + __shfl_xor_sync(0xffffffffu, send.y, 2));
+					}
+				float2 T[2][2];  // [start 4 sq + 2 b1 + x][event eb + y]
+#pragma unroll
+				for (int y = 0; y < 2; ++y) {
+					const bool valid = ev0 + (uint64_t)(eb + y) < bin.nEvents;
+#pragma unroll
+					for (int x = 0; x < 2; ++x) {
+						const float2 keep = b0 ? R1[x][2 + y] : R1[x][y];
+						const float2 send = b0 ? R1[x][y] : R1[x][2 + y];
+						const float sx = keep.x + __shfl_xor_sync(0xffffffffu, send.x, 1);
+						const float sy = keep.y + __shfl_xor_sync(0xffffffffu, send.y, 1);
+						const float L = fmaf(sx, sx, fmaf(sy, sy, flat2[4 * sq + 2 * b1 + x]));
+						const float c = valid ? -2.f / L : 0.f;
+						if (valid)
+							kahanAdd(llF[x], llK[x], -logf(L));
+						kahanAdd(csF[x], csK[x], c);
+						T[x][y] = make_float2(c * sx, c * sy);
+					}
+				}
+				// the two events' stores in an order that alternates with
+				// the event group (halves the bank conflicts of the stores)
+#pragma unroll
+				for (int t = 0; t < 2; ++t) {
+					const int y = (eg & 1) ^ t;
+					*reinterpret_cast<float4*>(&Ts[b8TSlot(eb + y, 4 * sq + 2 * b1)]) =
+					    make_float4(T[0][y].x, T[0][y].y, T[1][y].x, T[1][y].y);
+				}
+			}
+			// c S complete
+			if (__syncthreads_or(!ok)) {
+				failed = true;
+				break;
+			}
+
+			// ---- phase 2: G += sum_e c S conj(A), 4 starts x 2 waves over a quarter of the events ----
+			{
+				float2 Pp[4][2], Qp[4][2];
+#pragma unroll
+				for (int i = 0; i < 4; ++i)
+#pragma unroll
+					for (int j = 0; j < 2; ++j)
+						Pp[i][j] = Qp[i][j] = make_float2(0.f, 0.f);
+				if (p2) {
+					const uint32_t rowA = tileAddr + (uint32_t)wa * (uint32_t)(kBE * 8);
+					const uint32_t rowB = tileAddr + (uint32_t)wb * (uint32_t)(kBE * 8);
+#pragma unroll 1
+					for (int i = 0; i < kBE / 4; ++i) {
+						const int e = 4 * i + eq;
+						const uint32_t tRow = tAddr + (uint32_t)e * 64u;
+						const float4 t01 = lds128(tRow + tq0), t23 = lds128(tRow + tq1);
+						const float2 t[4] = {make_float2(t01.x, t01.y), make_float2(t01.z, t01.w),
+						                     make_float2(t23.x, t23.y), make_float2(t23.z, t23.w)};
+						const float2 xa = lds64(rowA + (uint32_t)((e + ra) & (kBE - 1)) * 8u);
+						const float2 xb = lds64(rowB + (uint32_t)((e + rb) & (kBE - 1)) * 8u);
+						const float2 xaS = make_float2(xa.y, xa.x), xbS = make_float2(xb.y, xb.x);
+#pragma unroll
+						for (int i4 = 0; i4 < 4; ++i4) {
+							Pp[i4][0] = ffma2(t[i4], xa, Pp[i4][0]);  // (tx ax, ty ay)
+							Qp[i4][0] = ffma2(t[i4], xaS, Qp[i4][0]);  // (tx ay, ty ax)
+							Pp[i4][1] = ffma2(t[i4], xb, Pp[i4][1]);
+							Qp[i4][1] = ffma2(t[i4], xbS, Qp[i4][1]);
+						}
+					}
+				}
+				// G = (P.x + P.y, Q.y - Q.x); reduce-scatter over the four
+				// event residues: lane bit 2 keeps starts 2 (eq >> 1) + {0, 1},
+				// lane bit 1 the wave 2 wp + (eq & 1)
+				const int e1 = eq >> 1, e0 = eq & 1;
+				float2 H[2][2];  // [start x][wave j]
+#pragma unroll
+				for (int x = 0; x < 2; ++x)
+#pragma unroll
+					for (int j = 0; j < 2; ++j) {
+						const int ik = e1 ? 2 + x : x, is = e1 ? x : 2 + x;
+						const float2 keep = make_float2(Pp[ik][j].x + Pp[ik][j].y, Qp[ik][j].y - Qp[ik][j].x);
+						const float2 send = make_float2(Pp[is][j].x + Pp[is][j].y, Qp[is][j].y - Qp[is][j].x);
+						H[x][j] = make_float2(keep.x + __shfl_xor_sync(0xffffffffu, send.x, 2),
+						                      keep.y + __shfl_xor_sync(0xffffffffu, send.y, 2));
+					}
+#pragma unroll
+				for (int x = 0; x < 2; ++x) {
+					const float2 keep = e0 ? H[x][1] : H[x][0];
+					const float2 send = e0 ? H[x][0] : H[x][1];
+					kahanAdd(gF[2 * x], gK[2 * x], keep.x + __shfl_xor_sync(0xffffffffu, send.x, 1));
+					kahanAdd(gF[2 * x + 1], gK[2 * x + 1], keep.y + __shfl_xor_sync(0xffffffffu, send.y, 1));
+				}
+			}
+			// the next tile loads once every thread is done with this one
+			__syncthreads();
+			if (tid == 0 && k + 1 < nt) {
+				fenceProxyAsync();
+				mbarArriveExpectTx(bar, tileBytes);
+				bulkCopyG2S(smem + lay.stage, bin.amps + (size_t)(it.t0 + k + 1) * W * kBE, tileBytes, bar);
+			}
+		}
+		if (failed) {
+			// the copy of tile k (the one whose wait expired) lands before
+			// the block exits
+			if (tid == 0) {
+				atomicOr(a.devErr, (unsigned)kDevErrTimeout);
+				mbarWaitBounded(bar, phase ^ 1u);
+			}
+			break;
+		}
+
+		// ---- partials of this item: [SG][2 + 2W] FP64 ----
+		const int NV = 2 + 2 * W;
+		double* out = a.partials + (size_t)item * SG * NV;
+		// -ln L and sum c: the lanes with equal b1 hold the same starts
+#pragma unroll
+		for (int x = 0; x < 2; ++x) {
+			double l = (double)llF[x] - (double)llK[x], c = (double)csF[x] - (double)csK[x];
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				if (o == 2)
+					continue;
+				l += __shfl_xor_sync(0xffffffffu, l, o);
+				c += __shfl_xor_sync(0xffffffffu, c, o);
+			}
+			if ((lane & ~2) == 0) {
+				redLL[warp][2 * b1 + x] = l;
+				redC[warp][2 * b1 + x] = c;
+			}
+		}
+		{
+			const int w = 2 * wp + (eq & 1);
+			if (w < W) {
+#pragma unroll
+				for (int x = 0; x < 2; ++x) {
+					const int s = 4 * sg + 2 * (eq >> 1) + x;
+					out[(size_t)s * NV + 2 + 2 * w] = (double)gF[2 * x] - (double)gK[2 * x];
+					out[(size_t)s * NV + 3 + 2 * w] = (double)gF[2 * x + 1] - (double)gK[2 * x + 1];
+				}
+			}
+		}
+		__syncthreads();
+		if (tid < SG) {
+			// warps 4 (s / 4) .. 4 (s / 4) + 3 hold start s, in a fixed order
+			double l = 0., c = 0.;
+			for (int wv = 4 * (tid >> 2); wv < 4 * (tid >> 2) + 4; ++wv) {
+				l += redLL[wv][tid & 3];
+				c += redC[wv][tid & 3];
+			}
+			out[(size_t)tid * NV] = l;
+			out[(size_t)tid * NV + 1] = c;
 		}
 		__syncthreads();
 	}
@@ -691,12 +1007,26 @@ int launchBatchT(const BatchArgs& a, int numSMs, cudaStream_t s)
 	return cudaCheck(cudaGetLastError(), "batch FdF launch");
 }
 
+// persistent grid: numSMs x the blocks that fit on an SM (at most three)
+int launchBatch8(const BatchArgs& a, int numSMs, cudaStream_t s)
+{
+	const size_t smemBytes = batch8Smem(a.W).total;
+	int perSM = 1;
+	const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fdfBatch8Kernel, kBThreads, smemBytes);
+	if (e != cudaSuccess)
+		return cudaCheck(e, "batch FdF occupancy");
+	perSM = std::max(1, std::min(perSM, 3));
+	fdfBatch8Kernel<<<numSMs * perSM, kBThreads, smemBytes, s>>>(a);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "batch FdF launch");
+}
+
 }  // namespace
 
-size_t batchSmemBytes(int W, int SG) { return batchSmem(W, SG, SG == 8 ? 1 : 2).total; }
+size_t batchSmemBytes(int W, int SG) { return SG == 8 ? batch8Smem(W).total : batchSmem(W, SG, 2).total; }
 
-// start groups of 32: two stages, one block per SM; of 8: one stage, up to
-// three blocks per SM
+// start groups of 32: two stages, one block per SM; of 8: the
+// register-blocked kernel, one stage, up to three blocks per SM
 int configureBatchFdf(int W, int SG, size_t maxSmem)
 {
 	if (W < 1 || W > 64)
@@ -706,7 +1036,9 @@ int configureBatchFdf(int W, int SG, size_t maxSmem)
 	if (SG == 32)
 		return configureBatchT<32, 4, 4, 4, 2, 2, 1>(W);
 	if (SG == 8)
-		return configureBatchT<8, 2, 2, 2, 1, 1, 3>(W);
+		return cudaCheck(cudaFuncSetAttribute(fdfBatch8Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                      (int)batch8Smem(W).total),
+		                 "batch smem attribute");
 	return setError(kErrUnsupported, "batched FdF: start-group size must be 8 or 32");
 }
 
@@ -717,7 +1049,7 @@ int launchBatchFdf(const BatchArgs& a, int numSMs, cudaStream_t s)
 	if (a.SG == 32)
 		return launchBatchT<32, 4, 4, 4, 2, 2, 1>(a, numSMs, s);
 	if (a.SG == 8)
-		return launchBatchT<8, 2, 2, 2, 1, 1, 3>(a, numSMs, s);
+		return launchBatch8(a, numSMs, s);
 	return setError(kErrUnsupported, "batched FdF: start-group size must be 8 or 32");
 }
 

@@ -64,11 +64,13 @@ def test_batched_fdf_against_oracle():
         assert helpers.normwise(g[q], g0) < 1e-5
 
 
-def test_chunking_and_autotune_keep_results():
+@pytest.mark.parametrize("group", [32, 8])
+def test_chunking_and_autotune_keep_results(group):
     """Tiles per work item only re-partition the FP32 tile partials that are
     folded into FP64: values agree to FP32 rounding of those partials."""
     bins = make_bins([900, 20000])
     M = R.pwaMultibin()
+    M.setOptions(startGroup=group)
     for (w, L) in bins:
         M.addBin(L, 6)
     x = np.random.default_rng(7).standard_normal((M.nmbProblems(), M.nmbPars()))
