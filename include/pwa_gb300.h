@@ -169,6 +169,24 @@ int pwa_integral_write_ascii(const pwa_integral* I, const char* path);
 #define PWA_GRAM_NOALLOC_MAX_WAVES 256
 int pwa_gram_device_noalloc(const void* amps, uint64_t nK, uint64_t ldK, uint32_t nWaves, const double* weights,
                             int precision, double* out, void* stream);
+/*
+ * No reference counterpart: the Gram sums of many bins in one call, for the
+ * moment features of the learned warm start (the data-averaged
+ * M_ij = <A_i conj(A_j)> of every kinematic bin).  amps[b]: complex64
+ * [nWaves][nEvents[b]] contiguous on the current device; outGram:
+ * nBins x nWaves x nWaves complex128 raw sums sum_k A_ik conj(A_jk) on the
+ * device; outSums: NULL or nBins x nWaves complex128 raw sums sum_k A_ik
+ * (compensated FP32 per thread, FP64 across threads).
+ * precision: PWA_PRECISION_FP32 (SIMT) or a tensor-core precision
+ * (PWA_PRECISION_TF32, _TF32X3, _BF16X3; bins whose rows are not 16-byte
+ * aligned, i.e. an odd nEvents[b] or base, are first copied into an aligned
+ * buffer; bins under 128 events use the FP32 SIMT kernel).  The kernels
+ * are ordered on `stream`; the call allocates its
+ * partial-sum and alignment buffers and returns after the stream has
+ * completed them.
+ */
+int pwa_gram_device_batch(const void* const* amps, const uint64_t* nEvents, uint32_t nBins, uint32_t nWaves,
+                          int precision, double* outGram, double* outSums, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* pwaLikelihood                                                              */

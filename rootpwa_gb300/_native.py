@@ -83,6 +83,7 @@ SIGNATURES = {
     "pwa_integral_read_ascii": (i, [vp, cc]),
     "pwa_integral_write_ascii": (i, [vp, cc]),
     "pwa_gram_device_noalloc": (i, [vp, u64, u64, u32, vp, i, vp, vp]),
+    "pwa_gram_device_batch": (i, [C.POINTER(vp), C.POINTER(u64), u32, u32, i, vp, vp, vp]),
     "pwa_multibin_create": (i, [pvp]),
     "pwa_multibin_destroy": (i, [vp]),
     "pwa_multibin_add_bin": (i, [vp, vp, u32]),

@@ -936,20 +936,29 @@ int launchGramTc(const GramArgs& g, int precision, int numSMs, cudaStream_t s, d
 	if (cr != CUDA_SUCCESS)
 		return setError(kErrCuda, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
 
-	if (hiLo) {
-		auto* k = a.bf16 ? gramTcHiLoKernel<true> : gramTcHiLoKernel<false>;
+	// the dynamic shared-memory limit of each variant is raised once to the
+	// largest size asked for (a host call that per-bin batches would
+	// otherwise repeat hundreds of times)
+	static std::mutex attrMutex;
+	static size_t configured[4] = {0, 0, 0, 0};
+	auto ensureSmem = [&](const void* k, int variant) -> int {
+		std::lock_guard<std::mutex> lock(attrMutex);
+		if (smemBytes <= configured[variant])
+			return kOk;
 		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes),
 		                        "gram TC smem attribute"));
+		configured[variant] = smemBytes;
+		return kOk;
+	};
+	if (hiLo) {
+		auto* k = a.bf16 ? gramTcHiLoKernel<true> : gramTcHiLoKernel<false>;
+		PWA_CHECK_RET(ensureSmem((const void*)k, a.bf16 ? 1 : 0));
 		k<<<grid, kThreadsHL, smemBytes, s>>>(map, a);
 	} else if (a.N <= kMaxNDB) {
-		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                             (int)smemBytes),
-		                        "gram TC smem attribute"));
+		PWA_CHECK_RET(ensureSmem((const void*)gramTcKernel<true>, 2));
 		gramTcKernel<true><<<grid, kThreadsDB, smemBytes, s>>>(map, a);
 	} else {
-		PWA_CHECK_RET(cudaCheck(cudaFuncSetAttribute(gramTcKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                             (int)smemBytes),
-		                        "gram TC smem attribute"));
+		PWA_CHECK_RET(ensureSmem((const void*)gramTcKernel<false>, 3));
 		gramTcKernel<false><<<grid, kThreadsTc, smemBytes, s>>>(map, a);
 	}
 	countLaunches(1);

@@ -522,4 +522,95 @@ int pwa_integral_write_ascii(const pwa_integral* I, const char* path)
 	return out.good() ? kOk : setError(kErrIo, "problems writing integral to ASCII file");
 }
 
+int pwa_gram_device_batch(const void* const* amps, const uint64_t* nEvents, uint32_t nBins, uint32_t nWaves,
+                          int precision, double* outGram, double* outSums, void* stream)
+{
+	if (!amps || !nEvents || !outGram)
+		return setError(kErrArg, "pwa_gram_device_batch: null argument");
+	if (nWaves == 0 || nWaves > 4096)
+		return setError(kErrArg, "pwa_gram_device_batch: nWaves must be in 1..4096");
+	const bool tc = (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3 ||
+	                 precision == PWA_PRECISION_BF16X3);
+	if (!tc && precision != PWA_PRECISION_FP32)
+		return setError(kErrUnsupported, "pwa_gram_device_batch: precision must be PWA_PRECISION_FP32, "
+		                                 "PWA_PRECISION_TF32, PWA_PRECISION_TF32X3 or PWA_PRECISION_BF16X3");
+	for (uint32_t b = 0; b < nBins; ++b)
+		if (!amps[b] || nEvents[b] == 0)
+			return setError(kErrArg, "pwa_gram_device_batch: bin " + std::to_string(b) + " has no amplitudes");
+	if (nBins == 0)
+		return kOk;
+	int dev, sms;
+	size_t smem;
+	PWA_TRY(deviceInfo(&dev, &sms, &smem));
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	const int W = (int)nWaves;
+	uint64_t nMax = 0;
+	for (uint32_t b = 0; b < nBins; ++b)
+		nMax = std::max(nMax, nEvents[b]);
+	// partials of the largest bin, reused bin after bin in stream order
+	const int tps = (W + 63) / 64;
+	const int nTiles = tps * (tps + 1) / 2;
+	const int simtChunks = (int)std::min<uint64_t>((uint64_t)std::max(1, (4 * sms + nTiles - 1) / nTiles),
+	                                               std::max<uint64_t>(1, nMax / 64));
+	const size_t tcScratch = tc ? gramTcScratchFloats(W, sms) / 2 + 1 : 0;
+	// tensor-core precisions: bins whose rows are not 16-byte aligned (odd
+	// event count or base) are copied into an aligned buffer of even row
+	// length first, reused bin after bin in stream order
+	uint64_t nPad = 0;
+	if (tc)
+		for (uint32_t b = 0; b < nBins; ++b)
+			if (nEvents[b] >= 128 && ((nEvents[b] & 1ull) || (reinterpret_cast<uintptr_t>(amps[b]) & 15u)))
+				nPad = std::max<uint64_t>(nPad, nEvents[b] + (nEvents[b] & 1ull));
+	DevBuf dPart, dErr, dAlign;
+	PWA_TRY(dPart.alloc(std::max(tcScratch, (size_t)simtChunks * W * W * 2) * sizeof(double), "gram batch partials"));
+	if (nPad)
+		PWA_TRY(dAlign.alloc((size_t)W * nPad * sizeof(float2), "gram batch alignment buffer"));
+	PWA_TRY(dErr.alloc(sizeof(unsigned), "flag"));
+	PWA_TRY(cudaCheck(cudaMemsetAsync(dErr.p, 0, sizeof(unsigned), s), "memset"));
+	for (uint32_t b = 0; b < nBins; ++b) {
+		const uint64_t n = nEvents[b];
+		GramArgs g{};
+		g.amps = static_cast<const float2*>(amps[b]);
+		g.K = n;
+		g.ldK = n;
+		g.W = W;
+		g.devErr = dErr.as<unsigned>();
+		double* out = outGram + (size_t)b * W * W * 2;
+		if (outSums)
+			PWA_TRY(launchRowSums(g.amps, n, n, W, outSums + (size_t)b * W * 2, s));
+		// the tensor-core kernel reads rows with TMA: an even row length
+		// (16-byte rows) and a 16-byte aligned base; bins shorter than one
+		// 128-event box take the SIMT kernel
+		int st = kErrUnsupported;
+		if (tc && n >= 128) {
+			if ((n & 1ull) || (reinterpret_cast<uintptr_t>(amps[b]) & 15u)) {
+				const uint64_t ld = n + (n & 1ull);
+				PWA_TRY(cudaCheck(cudaMemcpy2DAsync(dAlign.p, ld * sizeof(float2), amps[b], n * sizeof(float2),
+				                                    n * sizeof(float2), W, cudaMemcpyDeviceToDevice, s),
+				                  "gram batch realignment"));
+				g.amps = dAlign.as<float2>();
+				g.ldK = ld;
+			}
+			st = launchGramTc(g, precision, sms, s, out, dPart.as<double>(), tcScratch);
+			if (st != kOk && st != kErrUnsupported)
+				return st;
+		}
+		// FP32, or a shape the tensor-core kernel does not take: SIMT kernel
+		if (st != kOk) {
+			g.amps = static_cast<const float2*>(amps[b]);
+			g.ldK = n;
+			g.chunks = (int)std::min<uint64_t>((uint64_t)simtChunks, std::max<uint64_t>(1, n / 64));
+			g.partials = dPart.as<double>();
+			PWA_TRY(launchGramSimt(g, 1, s));
+			PWA_TRY(launchGramReduce(g.partials, g.chunks, W, out, 0, s));
+		}
+	}
+	PWA_TRY(cudaCheck(cudaStreamSynchronize(s), "gram batch"));
+	unsigned err = 0;
+	PWA_TRY(cudaCheck(cudaMemcpy(&err, dErr.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "flag"));
+	if (err)
+		return setError(kErrTimeout, "pwa_gram_device_batch: a bounded device-side wait expired");
+	return kOk;
+}
+
 }  // extern "C"

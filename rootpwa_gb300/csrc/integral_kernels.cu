@@ -213,4 +213,52 @@ int launchGramReduce(const double* partials, int chunks, int W, double* out, int
 	return cudaCheck(cudaGetLastError(), "gram reduce launch");
 }
 
+namespace {
+
+// out[w] = sum_k a[w][k] (complex64 rows of stride ld): one block per row,
+// compensated FP32 sums per thread (GB300's FP64 pipe is a small fraction
+// of its FP32 rate, and one FP64 add per element made this kernel slower
+// than the Gram itself), FP64 across the block's threads, a fixed reduction
+// order (thread-strided partial sums, then a shared-memory tree), so the
+// result does not depend on the run.
+__global__ void __launch_bounds__(256) rowSumsKernel(const float2* __restrict__ a, uint64_t n, uint64_t ld,
+                                                     double* out)
+{
+	__shared__ double sre[256], sim[256];
+	const float2* row = a + (uint64_t)blockIdx.x * ld;
+	float re = 0.f, im = 0.f, cre = 0.f, cim = 0.f;
+	for (uint64_t k = threadIdx.x; k < n; k += 256) {
+		const float2 v = row[k];
+		const float yr = v.x - cre, tr = re + yr;
+		cre = (tr - re) - yr;
+		re = tr;
+		const float yi = v.y - cim, ti = im + yi;
+		cim = (ti - im) - yi;
+		im = ti;
+	}
+	sre[threadIdx.x] = (double)re - (double)cre;
+	sim[threadIdx.x] = (double)im - (double)cim;
+	__syncthreads();
+	for (int o = 128; o > 0; o >>= 1) {
+		if ((int)threadIdx.x < o) {
+			sre[threadIdx.x] += sre[threadIdx.x + o];
+			sim[threadIdx.x] += sim[threadIdx.x + o];
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		out[2 * blockIdx.x] = sre[0];
+		out[2 * blockIdx.x + 1] = sim[0];
+	}
+}
+
+}  // namespace
+
+int launchRowSums(const float2* a, uint64_t n, uint64_t ld, int W, double* out, cudaStream_t s)
+{
+	rowSumsKernel<<<W, 256, 0, s>>>(a, n, ld, out);
+	countLaunches(1);
+	return cudaCheck(cudaGetLastError(), "row sums launch");
+}
+
 }  // namespace pwa

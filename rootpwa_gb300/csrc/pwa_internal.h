@@ -164,6 +164,9 @@ struct GramArgs {
 int launchGramSimt(const GramArgs& a, int precision, cudaStream_t s);
 // out = (accumulate ? out : 0) + sum of chunk partials, mirrored to the lower triangle
 int launchGramReduce(const double* partials, int chunks, int W, double* out, int accumulate, cudaStream_t s);
+// out[w] = sum_k a[w][k] for W complex64 rows of n elements (row stride ld),
+// FP64 (complex128 out[W])
+int launchRowSums(const float2* a, uint64_t n, uint64_t ld, int W, double* out, cudaStream_t s);
 // out (nOut x nOut complex) += blocks of the Gram blk of two row groups of G
 // rows (groups a and b; see integral_kernels.cu)
 int launchGramBlockAdd(const double* blk, int n2, int G, int a, int b, int nOut, int addAA, int addBB, double* out,

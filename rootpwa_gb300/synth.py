@@ -148,16 +148,25 @@ def draw_bin_device(model, v_true, flat, n_events, seed, pool_factor=4, device="
     """Data events of one bin, importance-resampled from phase-space draws in
     proportion to the rank-1 intensity |sum_w V_w A_w|^2 + flat^2 (multinomial
     resampling with replacement from a pool of pool_factor * n_events draws).
-    Returns complex64 [wave][event] on the device."""
+    Returns complex64 [wave][event] on the device.
+
+    The same seed gives the same events in every process: the intensities
+    come from elementwise products and fixed-order reductions, the
+    cumulative distribution and the uniform draws from numpy on the host (a
+    library matrix-vector product or a device-side cumulative sum may round
+    differently from run to run, which moves a few resampled events)."""
     import torch
     pool = draw_device(model, pool_factor * n_events, seed=seed, device=device)
-    v = torch.from_numpy(v_true.astype(np.complex64)).to(device)
-    s = v @ pool
-    inten = (s.real * s.real + s.imag * s.imag + flat * flat).float()
-    g = torch.Generator(device=device)
-    g.manual_seed(int(seed) + 7919)
-    idx = torch.multinomial(inten, n_events, replacement=True, generator=g)
-    return pool[:, idx].contiguous()
+    vr = torch.from_numpy(v_true.real.astype(np.float32)).to(device)[:, None]
+    vi = torch.from_numpy(v_true.imag.astype(np.float32)).to(device)[:, None]
+    pr, pi = pool.real, pool.imag
+    sr = (vr * pr - vi * pi).sum(dim=0)
+    si = (vr * pi + vi * pr).sum(dim=0)
+    inten = (sr * sr + si * si + np.float32(flat * flat)).double().cpu().numpy()
+    cdf = np.cumsum(inten)
+    u = np.random.Generator(np.random.PCG64(int(seed) + 7919)).random(n_events) * cdf[-1]
+    idx = np.minimum(np.searchsorted(cdf, u, side="right"), len(cdf) - 1)
+    return pool[:, torch.from_numpy(idx).to(device)].contiguous()
 
 
 # -- three-pion events and waves for the decay-amplitude step ---------------------

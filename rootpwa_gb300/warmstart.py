@@ -113,38 +113,37 @@ def moment_features(names, data, norm_diag, precision="tf32x3"):
     return np.concatenate([M.real.ravel(), M.imag.ravel(), [np.log(n)]]).astype(np.float32)
 
 
-def moment_features_batch(datas, norm_diags):
+def moment_features_batch(datas, norm_diags, precision="tf32x3"):
     """moment_features of many bins at once, from device amplitudes in place:
-    the W x W sums A conj(A)^T of each bin by the allocation-free Gram entry
-    point (pwa_gram_device_noalloc, FP32, all bins ordered on one stream),
-    the sums of A by a device reduction, one download at the end."""
+    the W x W sums A conj(A)^T and the sums of A of every bin by one call of
+    pwa_gram_device_batch (the integral's Gram kernels, by default the same
+    TF32x3 precision as moment_features), one download at the end."""
     import torch
     W = datas[0].shape[0]
     nb = len(datas)
     gram = torch.empty((nb, W, W), dtype=torch.complex128, device=datas[0].device)
     sums = torch.empty((nb, W), dtype=torch.complex128, device=datas[0].device)
-    stream = torch.cuda.current_stream()
-    for b, d in enumerate(datas):
-        assert d.is_contiguous() and d.dtype == torch.complex64
-        n = d.shape[1]
-        N.call("pwa_gram_device_noalloc", C.c_void_p(d.data_ptr()), n, n, W, None, 1,
-               C.c_void_p(gram[b].data_ptr()), C.c_void_p(stream.cuda_stream))
-        sums[b] = d.sum(dim=1).to(torch.complex128)
-    G = gram.cpu().numpy()
-    S = sums.cpu().numpy()
-    F = []
-    for b, d in enumerate(datas):
-        n = d.shape[1]
-        M = np.empty((W + 1, W + 1), dtype=np.complex128)
-        M[:W, :W] = G[b]
-        M[:W, W] = S[b]
-        M[W, :W] = np.conj(S[b])
-        M[W, W] = n
-        M /= n
-        sc = np.concatenate([1.0 / np.sqrt(np.asarray(norm_diags[b], dtype=np.float64)), [1.0]])
-        M = M * sc[:, None] * sc[None, :]
-        F.append(np.concatenate([M.real.ravel(), M.imag.ravel(), [np.log(n)]]))
-    return np.asarray(F, dtype=np.float32)
+    for d in datas:
+        assert d.is_contiguous() and d.dtype == torch.complex64 and d.shape[0] == W
+    ptrs = (C.c_void_p * nb)(*[d.data_ptr() for d in datas])
+    counts = (C.c_uint64 * nb)(*[d.shape[1] for d in datas])
+    N.call("pwa_gram_device_batch", ptrs, counts, nb, W, N.PRECISION[precision], C.c_void_p(gram.data_ptr()),
+           C.c_void_p(sums.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    # assembled on the device (the same FP64 operations as moment_features),
+    # one download of the FP32 features
+    dev = gram.device
+    n = torch.tensor([d.shape[1] for d in datas], dtype=torch.float64, device=dev)
+    sc = torch.ones((nb, W + 1), dtype=torch.float64, device=dev)
+    sc[:, :W] = 1.0 / torch.sqrt(torch.as_tensor(np.asarray(norm_diags, dtype=np.float64).reshape(nb, W), device=dev))
+    M = torch.empty((nb, W + 1, W + 1), dtype=torch.complex128, device=dev)
+    M[:, :W, :W] = gram
+    M[:, :W, W] = sums
+    M[:, W, :W] = sums.conj()
+    M[:, W, W] = n
+    M /= n[:, None, None]
+    M *= sc[:, :, None] * sc[:, None, :]
+    F = torch.cat([M.real.reshape(nb, -1), M.imag.reshape(nb, -1), torch.log(n)[:, None]], dim=1)
+    return F.to(torch.float32).cpu().numpy()
 
 
 def prod_amp_indices(L):
