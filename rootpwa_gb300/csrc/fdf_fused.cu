@@ -285,10 +285,10 @@ __global__ void __launch_bounds__(kThreads, 1) fdfFusedKernel(const FdfArgs a, c
 			for (int e = 0; e < 2; ++e)
 				L = fmaf(S[r][e].x, S[r][e].x, fmaf(S[r][e].y, S[r][e].y, L));
 		const bool valid = (e0 + (uint64_t)(pe0 + mine)) < a.nEvents;
-		const float c = valid ? -2.f / L : 0.f;
+		const float c = valid ? eventWeight(L) : 0.f;
 		if (phLo == 0) {
 			if (valid)
-				llPart += -logf(L);
+				llPart += -eventLog(L);
 			cPart += c;
 		}
 

@@ -202,8 +202,8 @@ __global__ void __launch_bounds__(kThreads, 1) fdfNarrowKernel(const FdfArgs a, 
 #pragma unroll
 				for (int e = 0; e < 2; ++e)
 					L = fmaf(S[r][e].x, S[r][e].x, fmaf(S[r][e].y, S[r][e].y, L));
-			const float c = -2.f / L;
-			llPart += -logf(L);
+			const float c = eventWeight(L);
+			llPart += -eventLog(L);
 			cPart += c;
 			if (a.withGrad) {
 				// G += c S conj(A): (ax tx + ay ty, ax ty - ay tx)
