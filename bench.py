@@ -71,6 +71,9 @@ def parse():
                     help="fdf: the headline FdF benchmark; multibin: whole multibin fit, plain multi-start vs "
                          "learned warm start; precision: error of each arithmetic variant against FP64; "
                          "isobar: decay amplitudes of the 88-wave 3pi set")
+    ap.add_argument("--cross-tile-events", type=int, default=2_500_000,
+                    help="precision: data events of the second cross-tile reduction comparison (several FP64 "
+                         "folds per block; at 1 M events a block holds fewer tiles than one fold period)")
     ap.add_argument("--oracle-mc", type=int, default=200_000,
                     help="precision: MC events of the integrals compared with the CPU FP64 oracle")
     ap.add_argument("--bins", type=int, default=400, help="multibin: kinematic bins (100 mass x 4 t')")
@@ -869,29 +872,45 @@ def run_precision(args):
         assert O.addAmplitude(n, host[k].astype(np.complex128))
     assert O.finishInit()
     f0, g0 = O.FdF(par, threads=cpu_threads())
-    out["fdf_vs_oracle"] = {"events": args.n_data}
-    for red in ["fp64", "kahan_fp32", "fp32"]:
-        L = R.pwaLikelihood()
-        L.init(names, refl, None, RANK, 0.0)
-        L.addNormIntegral(copy(ints["fp64"]))
-        L.addAccIntegral(copy(accs["fp64"]))
+    def cross_tile(key, dev_data, nev, fref, gref):
+        out[key] = {"events": nev, "tiles_per_block": round(nev / 128 / 152, 1)}
+        for red in ["fp64", "kahan_fp32", "fp32"]:
+            L = R.pwaLikelihood()
+            L.init(names, refl, None, RANK, 0.0)
+            L.addNormIntegral(copy(ints["fp64"]))
+            L.addAccIntegral(copy(accs["fp64"]))
+            for k, n in enumerate(names):
+                L.addAmplitude(n, dev_data[k])
+            L.finishInit()
+            L.setReduction(red)
+            f, gg = L.FdF(par)
+            for _ in range(5):
+                L.FdF(par)
+            t0 = time.perf_counter()
+            for _ in range(100):
+                L.FdF(par)
+            us = (time.perf_counter() - t0) / 100 * 1e6
+            out[key][red] = {"ll_rel": abs(f - fref) / abs(fref),
+                             "grad_normwise": float(np.max(np.abs(gg - gref)) / np.max(np.abs(gref))),
+                             "us_per_fdf_host_call": us,
+                             "cross_tile": {"fp64": "FP32 partials of 64 tiles folded into FP64",
+                                            "kahan_fp32": "every tile into compensated FP32",
+                                            "fp32": "plain FP32 over all tiles"}[red]}
+
+    cross_tile("fdf_vs_oracle", data, args.n_data, f0, g0)
+    # a larger set: each block folds its FP32 partials into FP64 more than once
+    if args.cross_tile_events > args.n_data:
+        data2 = synth.draw_device(model, args.cross_tile_events, seed=12)
+        O2 = OracleLikelihood()
+        assert O2.init(names, refl, None, RANK, 0.0)
+        assert O2.addNormIntegral(oracle_copy(ints["fp64"])) and O2.addAccIntegral(oracle_copy(accs["fp64"]))
         for k, n in enumerate(names):
-            L.addAmplitude(n, data[k])
-        L.finishInit()
-        L.setReduction(red)
-        f, gg = L.FdF(par)
-        for _ in range(5):
-            L.FdF(par)
-        t0 = time.perf_counter()
-        for _ in range(100):
-            L.FdF(par)
-        us = (time.perf_counter() - t0) / 100 * 1e6
-        out["fdf_vs_oracle"][red] = {"ll_rel": abs(f - f0) / abs(f0),
-                                     "grad_normwise": float(np.max(np.abs(gg - g0)) / np.max(np.abs(g0))),
-                                     "us_per_fdf_host_call": us,
-                                     "cross_tile": {"fp64": "FP32 partials of 64 tiles folded into FP64",
-                                                    "kahan_fp32": "every tile into compensated FP32",
-                                                    "fp32": "plain FP32 over all tiles"}[red]}
+            assert O2.addAmplitude(n, data2[k].cpu().numpy().astype(np.complex128))
+        assert O2.finishInit()
+        f2, g2 = O2.FdF(par, threads=cpu_threads())
+        del O2
+        cross_tile("fdf_cross_tile_large", data2, args.cross_tile_events, f2, g2)
+        del data2
     # effect of the integral arithmetic on LL and gradient (GPU FdF, FP64 reductions)
     out["fdf_integral_variant"] = {}
     base = None
