@@ -172,7 +172,7 @@ int pwa_gram_device_noalloc(const void* amps, uint64_t nK, uint64_t ldK, uint32_
 /*
  * No reference counterpart: the Gram sums of many bins in one call, for the
  * moment features of the learned warm start (the data-averaged
- * M_ij = <A_i conj(A_j)> of every kinematic bin).  amps[b]: complex64
+ * M_ij = <A_i conj(A_j)> of every kinematic bin); nWaves <= 1024.  amps[b]: complex64
  * [nWaves][nEvents[b]] contiguous on the current device; outGram:
  * nBins x nWaves x nWaves complex128 raw sums sum_k A_ik conj(A_jk) on the
  * device; outSums: NULL or nBins x nWaves complex128 raw sums sum_k A_ik

@@ -527,8 +527,8 @@ int pwa_gram_device_batch(const void* const* amps, const uint64_t* nEvents, uint
 {
 	if (!amps || !nEvents || !outGram)
 		return setError(kErrArg, "pwa_gram_device_batch: null argument");
-	if (nWaves == 0 || nWaves > 4096)
-		return setError(kErrArg, "pwa_gram_device_batch: nWaves must be in 1..4096");
+	if (nWaves == 0 || nWaves > 1024)
+		return setError(kErrArg, "pwa_gram_device_batch: nWaves must be in 1..1024");
 	const bool tc = (precision == PWA_PRECISION_TF32 || precision == PWA_PRECISION_TF32X3 ||
 	                 precision == PWA_PRECISION_BF16X3);
 	if (!tc && precision != PWA_PRECISION_FP32)
@@ -550,8 +550,11 @@ int pwa_gram_device_batch(const void* const* amps, const uint64_t* nEvents, uint
 	// partials of the largest bin, reused bin after bin in stream order
 	const int tps = (W + 63) / 64;
 	const int nTiles = tps * (tps + 1) / 2;
-	const int simtChunks = (int)std::min<uint64_t>((uint64_t)std::max(1, (4 * sms + nTiles - 1) / nTiles),
-	                                               std::max<uint64_t>(1, nMax / 64));
+	// SIMT chunks as integrate() takes them, within 256 MiB of FP64 partials
+	const uint64_t partialBudget = std::max<uint64_t>(1, (256ull << 20) / ((uint64_t)W * W * 2 * sizeof(double)));
+	const int simtChunks = (int)std::min<uint64_t>(
+	    std::min<uint64_t>((uint64_t)std::max(1, (4 * sms + nTiles - 1) / nTiles), std::max<uint64_t>(1, nMax / 64)),
+	    partialBudget);
 	const size_t tcScratch = tc ? gramTcScratchFloats(W, sms) / 2 + 1 : 0;
 	// tensor-core precisions: bins whose rows are not 16-byte aligned (odd
 	// event count or base) are copied into an aligned buffer of even row

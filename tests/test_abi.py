@@ -276,3 +276,23 @@ def test_integral_comparison_and_clear():
     assert not I1.hasIdenticalWaveSet(I4) and I1 != I4
     I1.clear()
     assert I1.nmbWaves() == 0 and I1.nmbEvents() == 0 and not I1.containsWave("a")
+
+
+def test_gram_batch_rejects_bad_arguments_without_device_work():
+    """pwa_gram_device_batch checks its arguments before any device call."""
+    one = (C.c_void_p * 1)(C.c_void_p(16))
+    with pytest.raises(N.PwaError) as e:
+        N.call("pwa_gram_device_batch", None, None, 1, 8, N.PRECISION["fp32"], None, None, None)
+    assert e.value.status == N.ERROR_INVALID_ARGUMENT
+    with pytest.raises(N.PwaError) as e:
+        N.call("pwa_gram_device_batch", one, (C.c_uint64 * 1)(8), 1, 1025, N.PRECISION["fp32"],
+               C.c_void_p(16), None, None)
+    assert e.value.status == N.ERROR_INVALID_ARGUMENT and "1024" in str(e.value)
+    with pytest.raises(N.PwaError) as e:
+        N.call("pwa_gram_device_batch", one, (C.c_uint64 * 1)(0), 1, 8, N.PRECISION["fp32"],
+               C.c_void_p(16), None, None)
+    assert e.value.status == N.ERROR_INVALID_ARGUMENT
+    with pytest.raises(N.PwaError) as e:
+        N.call("pwa_gram_device_batch", one, (C.c_uint64 * 1)(8), 1, 8, N.PRECISION["fp64"],
+               C.c_void_p(16), None, None)
+    assert e.value.status == 7
