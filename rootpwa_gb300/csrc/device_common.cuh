@@ -92,12 +92,14 @@ __device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.as
 __device__ __forceinline__ void gridDependencyWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void gridDependencyTrigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-// Per-event c = -2 / L and ln L of the FdF and batched-FdF kernels with the
-// hardware reciprocal and base-2 logarithm (a few instructions each, where
-// the IEEE division and the full-accuracy logf took about 30 per warp and
-// event; 2.3 % of the 87-wave, 10^6-event FdF).  Relative errors are about
-// 2^-21; the FdF's LL error against the FP64 oracle at 10^6 events went from
-// 2.7e-9 to 3.7e-8, the gradient's from 1.9e-8 to 2.6e-8.
+// Per-event c = -2 / L and ln L of the FdF kernels with the hardware
+// reciprocal and base-2 logarithm (a few instructions each, where the IEEE
+// division and the full-accuracy logf took about 30 per warp and event;
+// 2.3 % of the 87-wave, 10^6-event FdF).  Relative errors are about 2^-21;
+// the FdF's LL error against the FP64 oracle at 10^6 events went from 2.7e-9
+// to 3.7e-8, the gradient's from 1.9e-8 to 2.6e-8.  The batched-fit kernels
+// keep the IEEE forms: their line searches work near the rounding floor of
+// f, where the faster forms changed the plain fit's convergence tail.
 __device__ __forceinline__ float eventWeight(float L) { return __fdividef(-2.f, L); }
 __device__ __forceinline__ float eventLog(float L) { return __logf(L); }
 
