@@ -65,9 +65,9 @@ __host__ __device__ inline BatchSmem batchSmem(int W, int SG, int NST)
 
 // SG starts per group; phase 1: SPT starts x EPT events per thread;
 // phase 2: SPT2 starts x WPT waves per thread (waves < 64).  NST tile stages
-// per block: 2 (the next tile loads while this one is used) or 1 (several
-// blocks per SM, MINB, take turns instead; for small start groups, whose
-// blocks have little work per tile).
+// per block: 2 (the next tile loads while this one is used) or 1 (MINB
+// blocks per SM take turns instead).  Instantiated for groups of 32 starts
+// (two stages, one block per SM); groups of 8 use fdfBatch8Kernel below.
 template <int SG, int SPT, int EPT, int SPT2, int WPT, int NST, int MINB>
 __global__ void __launch_bounds__(kBThreads, MINB) fdfBatchKernel(const BatchArgs a)
 {
